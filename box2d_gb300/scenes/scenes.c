@@ -1,0 +1,637 @@
+/*
+ * Scene builders for the benchmark configurations and parity tests, written only
+ * against the public Box2D C API. The same file is compiled against three libraries:
+ * the GB300 library (box2d_gb300.h), the CPU oracle, and -- in the development
+ * container only -- the reference itself, so one scene definition drives all three.
+ *
+ * Random numbers: XorShift32 with seed 12345 mapped to [0, 32767], the generator of
+ * shared/utils.h:29-65 in the reference; normal variates by Box-Muller on that stream.
+ *
+ * Exported entry points (prefix b2s_) keep a small table of live scenes and read body
+ * state through b2Body_* getters, so they never touch library internals.
+ */
+#ifdef B2S_REFERENCE_HEADERS
+#include "box2d/box2d.h"
+#else
+#include "box2d_gb300.h"
+#endif
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define B2S_EXPORT __attribute__( ( visibility( "default" ) ) )
+
+typedef struct b2sRng
+{
+	uint32_t state;
+} b2sRng;
+
+static int b2sRandomInt( b2sRng* r )
+{
+	uint32_t x = r->state;
+	x ^= x << 13;
+	x ^= x >> 17;
+	x ^= x << 5;
+	r->state = x;
+	return (int)( x % ( 32767 + 1 ) );
+}
+
+static float b2sRandomFloatRange( b2sRng* r, float lo, float hi )
+{
+	float v = (float)( b2sRandomInt( r ) & 32767 );
+	v /= 32767;
+	v = ( hi - lo ) * v + lo;
+	return v;
+}
+
+static int b2sRandomIntRange( b2sRng* r, int lo, int hi )
+{
+	return lo + b2sRandomInt( r ) % ( hi - lo + 1 );
+}
+
+/* Box-Muller on two uniform draws in (0, 1] */
+static float b2sRandomNormal( b2sRng* r, float sigma )
+{
+	float u1 = b2sRandomFloatRange( r, 1.0f / 32768.0f, 1.0f );
+	float u2 = b2sRandomFloatRange( r, 0.0f, 1.0f );
+	double z = sqrt( -2.0 * log( (double)u1 ) ) * cos( 2.0 * 3.14159265358979323846 * (double)u2 );
+	return sigma * (float)z;
+}
+
+typedef struct b2sScene
+{
+	int inUse;
+	b2WorldId worldId;
+	b2BodyId* bodies;
+	int bodyCount, bodyCapacity;
+	int dynamicCount;
+	float targetX, targetY;
+} b2sScene;
+
+#define B2S_MAX_SCENES 4096
+static b2sScene b2s_scenes[B2S_MAX_SCENES];
+
+static void b2sAddBody( b2sScene* s, b2BodyId id, int dynamic )
+{
+	if ( s->bodyCount == s->bodyCapacity )
+	{
+		s->bodyCapacity = s->bodyCapacity ? 2 * s->bodyCapacity : 256;
+		s->bodies = realloc( s->bodies, (size_t)s->bodyCapacity * sizeof( b2BodyId ) );
+	}
+	s->bodies[s->bodyCount++] = id;
+	s->dynamicCount += dynamic;
+}
+
+static b2BodyId b2sBody( b2sScene* s, b2BodyType type, float x, float y )
+{
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = type;
+	bd.position.x = x;
+	bd.position.y = y;
+	b2BodyId id = b2CreateBody( s->worldId, &bd );
+	b2sAddBody( s, id, type == b2_dynamicBody );
+	return id;
+}
+
+/* Large pyramid (benchmark scene large_pyramid, shared/benchmarks.c:89-131).
+   ground 0: b2MakeBox(100, 1) at y = -1 as in the reference scene;
+   ground 1: one 200 m static segment at y = 0. */
+static void b2sLargePyramid( b2sScene* s, int baseCount, int groundKind )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	{
+		b2ShapeDef sd = b2DefaultShapeDef();
+		if ( groundKind == 0 )
+		{
+			b2BodyId g = b2sBody( s, b2_staticBody, 0.0f, -1.0f );
+			b2Polygon box = b2MakeBox( 100.0f, 1.0f );
+			b2CreatePolygonShape( g, &sd, &box );
+		}
+		else
+		{
+			b2BodyId g = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+			b2Segment seg = { { -100.0f, 0.0f }, { 100.0f, 0.0f } };
+			b2CreateSegmentShape( g, &sd, &seg );
+		}
+	}
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	float a = 0.5f;
+	b2Polygon box = b2MakeSquare( a );
+	float shift = 1.0f * a;
+	for ( int i = 0; i < baseCount; ++i )
+	{
+		float y = ( 2.0f * i + 1.0f ) * shift;
+		for ( int j = i; j < baseCount; ++j )
+		{
+			float x = ( i + 1.0f ) * shift + 2.0f * ( j - i ) * shift - a * baseCount;
+			b2BodyId id = b2sBody( s, b2_dynamicBody, x, y );
+			b2CreatePolygonShape( id, &sd, &box );
+		}
+	}
+}
+
+/* Many pyramids with rain: a grid of gridN x gridN pyramids of pyramidRows rows of
+   0.5 m boxes, 12 m apart; each grid row stands on its own span of one static ground
+   body (rows 7 m apart); rainCount circles of radius U(0.1, 0.3) start 30-60 m above the
+   top row. */
+static void b2sManyPyramidsRain( b2sScene* s, int gridN, int pyramidRows, int rainCount, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	float extent = 0.25f;
+	float spacing = 12.0f;
+	float rowDelta = 2.0f * extent * pyramidRows + 2.0f;
+	float width = spacing * gridN;
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	for ( int r = 0; r < gridN; ++r )
+	{
+		float gy = r * rowDelta;
+		b2Segment seg = { { -0.5f * width - 2.0f, gy }, { 0.5f * width + 2.0f, gy } };
+		b2CreateSegmentShape( ground, &sd, &seg );
+	}
+	b2Polygon box = b2MakeSquare( extent );
+	for ( int r = 0; r < gridN; ++r )
+	{
+		float baseY = r * rowDelta;
+		for ( int c = 0; c < gridN; ++c )
+		{
+			float centerX = -0.5f * width + ( c + 0.5f ) * spacing;
+			for ( int i = 0; i < pyramidRows; ++i )
+			{
+				float y = ( 2.0f * i + 1.0f ) * extent + baseY;
+				for ( int j = i; j < pyramidRows; ++j )
+				{
+					float x = ( i + 1.0f ) * extent + 2.0f * ( j - i ) * extent + centerX - extent * pyramidRows;
+					b2BodyId id = b2sBody( s, b2_dynamicBody, x, y );
+					b2CreatePolygonShape( id, &sd, &box );
+				}
+			}
+		}
+	}
+	float topY = ( gridN - 1 ) * rowDelta + 2.0f * extent * pyramidRows;
+	for ( int k = 0; k < rainCount; ++k )
+	{
+		float x = b2sRandomFloatRange( rng, -0.5f * width, 0.5f * width );
+		float y = topY + b2sRandomFloatRange( rng, 30.0f, 60.0f );
+		float radius = b2sRandomFloatRange( rng, 0.1f, 0.3f );
+		b2BodyId id = b2sBody( s, b2_dynamicBody, x, y );
+		b2Circle circle = { { 0.0f, 0.0f }, radius };
+		b2CreateCircleShape( id, &sd, &circle );
+	}
+}
+
+/* Reference many_pyramids (shared/benchmarks.c:157-195): rowCount x columnCount pyramids of
+   10 rows of 1 m boxes, 20 stacked ground segments. */
+static void b2sManyPyramidsReference( b2sScene* s, int rowCount, int columnCount )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	int baseCount = 10;
+	float extent = 0.5f;
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	float groundDeltaY = 2.0f * extent * ( baseCount + 1.0f );
+	float groundWidth = 2.0f * extent * columnCount * ( baseCount + 1.0f );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	float groundY = 0.0f;
+	for ( int i = 0; i < rowCount; ++i )
+	{
+		b2Segment seg = { { -0.5f * groundWidth, groundY }, { 0.5f * groundWidth, groundY } };
+		b2CreateSegmentShape( ground, &sd, &seg );
+		groundY += groundDeltaY;
+	}
+	float baseWidth = 2.0f * extent * baseCount;
+	float baseY = 0.0f;
+	b2Polygon box = b2MakeSquare( extent );
+	for ( int i = 0; i < rowCount; ++i )
+	{
+		for ( int j = 0; j < columnCount; ++j )
+		{
+			float centerX = -0.5f * groundWidth + j * ( baseWidth + 2.0f * extent ) + 2.0f * extent;
+			for ( int r = 0; r < baseCount; ++r )
+			{
+				float y = ( 2.0f * r + 1.0f ) * extent + baseY;
+				for ( int q = r; q < baseCount; ++q )
+				{
+					float x = ( r + 1.0f ) * extent + 2.0f * ( q - r ) * extent + centerX - 0.5f;
+					b2BodyId id = b2sBody( s, b2_dynamicBody, x, y );
+					b2CreatePolygonShape( id, &sd, &box );
+				}
+			}
+		}
+		baseY += groundDeltaY;
+	}
+}
+
+/* Joint grid: n x n circles of radius 0.4 joined to the upper and left neighbours by
+   revolute joints (shared/benchmarks.c:20-87). pinAll != 0 makes the whole top row static
+   (the reference pins 7 bodies of it); grid circles use category 2 / mask ~2 so they do not
+   collide with each other. mixedCount shapes (capsule, convex polygon or segment) with
+   velocities N(0, 2) are dropped on the grid. */
+static void b2sJointGrid( b2sScene* s, int n, int pinAll, int mixedCount, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId* grid = malloc( (size_t)n * n * sizeof( b2BodyId ) );
+	int index = 0;
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.filter.categoryBits = 2;
+	sd.filter.maskBits = ~(uint64_t)2;
+	b2Circle circle = { { 0.0f, 0.0f }, 0.4f };
+	b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+	jd.base.drawScale = 0.4f;
+	for ( int k = 0; k < n; ++k )
+	{
+		for ( int i = 0; i < n; ++i )
+		{
+			int isStatic = pinAll ? ( i == 0 ) : ( k >= n / 2 - 3 && k <= n / 2 + 3 && i == 0 );
+			b2BodyId body = b2sBody( s, isStatic ? b2_staticBody : b2_dynamicBody, (float)k, -(float)i );
+			b2CreateCircleShape( body, &sd, &circle );
+			if ( i > 0 )
+			{
+				jd.base.bodyIdA = grid[index - 1];
+				jd.base.bodyIdB = body;
+				jd.base.localFrameA.p.x = 0.0f;
+				jd.base.localFrameA.p.y = -0.5f;
+				jd.base.localFrameB.p.x = 0.0f;
+				jd.base.localFrameB.p.y = 0.5f;
+				b2CreateRevoluteJoint( s->worldId, &jd );
+			}
+			if ( k > 0 )
+			{
+				jd.base.bodyIdA = grid[index - n];
+				jd.base.bodyIdB = body;
+				jd.base.localFrameA.p.x = 0.5f;
+				jd.base.localFrameA.p.y = 0.0f;
+				jd.base.localFrameB.p.x = -0.5f;
+				jd.base.localFrameB.p.y = 0.0f;
+				b2CreateRevoluteJoint( s->worldId, &jd );
+			}
+			grid[index++] = body;
+		}
+	}
+	free( grid );
+	b2ShapeDef md = b2DefaultShapeDef();
+	for ( int m = 0; m < mixedCount; ++m )
+	{
+		float x = b2sRandomFloatRange( rng, 0.0f, (float)( n - 1 ) );
+		float y = b2sRandomFloatRange( rng, 2.0f, 2.0f + 0.3f * (float)n );
+		b2BodyId body = b2sBody( s, b2_dynamicBody, x, y );
+		int kind = b2sRandomIntRange( rng, 0, 2 );
+		if ( kind == 0 )
+		{
+			float length = b2sRandomFloatRange( rng, 0.5f, 1.5f );
+			float radius = b2sRandomFloatRange( rng, 0.1f, 0.25f );
+			b2Capsule cap = { { -0.5f * length, 0.0f }, { 0.5f * length, 0.0f }, radius };
+			b2CreateCapsuleShape( body, &md, &cap );
+		}
+		else if ( kind == 1 )
+		{
+			int count = b2sRandomIntRange( rng, 3, 8 );
+			float radius = b2sRandomFloatRange( rng, 0.3f, 0.6f );
+			b2Vec2 pts[8];
+			for ( int v = 0; v < count; ++v )
+			{
+				float angle = 2.0f * 3.14159265359f * v / count + b2sRandomFloatRange( rng, -0.2f, 0.2f );
+				b2CosSin cs = b2ComputeCosSin( angle );
+				pts[v].x = radius * cs.cosine;
+				pts[v].y = radius * cs.sine;
+			}
+			float rounding = b2sRandomFloatRange( rng, 0.0f, 0.05f );
+			b2Hull hull = b2ComputeHull( pts, count );
+			b2Polygon poly = hull.count >= 3 ? b2MakePolygon( &hull, rounding ) : b2MakeBox( 0.3f, 0.3f );
+			b2CreatePolygonShape( body, &md, &poly );
+		}
+		else
+		{
+			float length = b2sRandomFloatRange( rng, 0.5f, 1.5f );
+			b2Segment seg = { { -0.5f * length, 0.0f }, { 0.5f * length, 0.0f } };
+			b2CreateSegmentShape( body, &md, &seg );
+		}
+		b2Vec2 v = { b2sRandomNormal( rng, 2.0f ), b2sRandomNormal( rng, 2.0f ) };
+		b2Body_SetLinearVelocity( body, v );
+	}
+}
+
+/* One world of the batched configuration: U{10..400} bodies (boxes of half-extent
+   U(0.2, 0.8), circles of radius U(0.1, 0.5), capsules), dropped from heights U(1, 20)
+   into a static container of three segments, velocities N(0, 1), friction U(0.2, 0.9),
+   restitution U(0, 0.3). bodyCount <= 0 draws the count. */
+static void b2sBatchWorld( b2sScene* s, int bodyCount, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	if ( bodyCount <= 0 ) bodyCount = b2sRandomIntRange( rng, 10, 400 );
+	float halfWidth = 2.0f + 0.1f * (float)bodyCount;
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	b2ShapeDef gd = b2DefaultShapeDef();
+	b2Segment floorSeg = { { -halfWidth, 0.0f }, { halfWidth, 0.0f } };
+	b2Segment leftSeg = { { -halfWidth, 0.0f }, { -halfWidth, 40.0f } };
+	b2Segment rightSeg = { { halfWidth, 0.0f }, { halfWidth, 40.0f } };
+	b2CreateSegmentShape( ground, &gd, &floorSeg );
+	b2CreateSegmentShape( ground, &gd, &leftSeg );
+	b2CreateSegmentShape( ground, &gd, &rightSeg );
+	for ( int k = 0; k < bodyCount; ++k )
+	{
+		float x = b2sRandomFloatRange( rng, -halfWidth + 1.0f, halfWidth - 1.0f );
+		float y = b2sRandomFloatRange( rng, 1.0f, 20.0f );
+		b2BodyId body = b2sBody( s, b2_dynamicBody, x, y );
+		b2ShapeDef sd = b2DefaultShapeDef();
+		sd.material.friction = b2sRandomFloatRange( rng, 0.2f, 0.9f );
+		sd.material.restitution = b2sRandomFloatRange( rng, 0.0f, 0.3f );
+		int kind = b2sRandomIntRange( rng, 0, 2 );
+		if ( kind == 0 )
+		{
+			float h = b2sRandomFloatRange( rng, 0.2f, 0.8f );
+			b2Polygon box = b2MakeBox( h, h );
+			b2CreatePolygonShape( body, &sd, &box );
+		}
+		else if ( kind == 1 )
+		{
+			b2Circle c = { { 0.0f, 0.0f }, b2sRandomFloatRange( rng, 0.1f, 0.5f ) };
+			b2CreateCircleShape( body, &sd, &c );
+		}
+		else
+		{
+			float hl = b2sRandomFloatRange( rng, 0.1f, 0.5f );
+			b2Capsule cap = { { -hl, 0.0f }, { hl, 0.0f }, b2sRandomFloatRange( rng, 0.1f, 0.3f ) };
+			b2CreateCapsuleShape( body, &sd, &cap );
+		}
+		b2Vec2 v = { b2sRandomNormal( rng, 1.0f ), b2sRandomNormal( rng, 1.0f ) };
+		b2Body_SetLinearVelocity( body, v );
+	}
+}
+
+/* One world of the differentiable batch: columns x rows boxes of 0.5 m side stacked on a
+   static ramp inclined U(10, 30) degrees; initial velocities N(0, 0.5), friction
+   U(0.3, 0.8). The target point is drawn from the same stream. */
+static void b2sRampWorld( b2sScene* s, int columns, int rows, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	float angle = b2sRandomFloatRange( rng, 10.0f, 30.0f ) * 3.14159265359f / 180.0f;
+	b2BodyDef gdef = b2DefaultBodyDef();
+	gdef.rotation = b2MakeRot( -angle );
+	b2BodyId ground = b2CreateBody( s->worldId, &gdef );
+	b2sAddBody( s, ground, 0 );
+	b2ShapeDef gd = b2DefaultShapeDef();
+	b2Polygon ramp = b2MakeBox( 30.0f, 0.5f );
+	b2CreatePolygonShape( ground, &gd, &ramp );
+	b2Rot q = b2MakeRot( -angle );
+	float h = 0.25f;
+	for ( int c = 0; c < columns; ++c )
+	{
+		for ( int r = 0; r < rows; ++r )
+		{
+			float lx = -4.0f + 1.0f * c;
+			float ly = 0.5f + h + 2.0f * h * r + 0.01f * r;
+			b2BodyDef bd = b2DefaultBodyDef();
+			bd.type = b2_dynamicBody;
+			bd.position.x = q.c * lx - q.s * ly;
+			bd.position.y = q.s * lx + q.c * ly;
+			bd.rotation = q;
+			bd.linearVelocity.x = b2sRandomNormal( rng, 0.5f );
+			bd.linearVelocity.y = b2sRandomNormal( rng, 0.5f );
+			bd.angularVelocity = b2sRandomNormal( rng, 0.5f );
+			b2BodyId body = b2CreateBody( s->worldId, &bd );
+			b2sAddBody( s, body, 1 );
+			b2ShapeDef sd = b2DefaultShapeDef();
+			sd.material.friction = b2sRandomFloatRange( rng, 0.3f, 0.8f );
+			b2Polygon box = b2MakeBox( h, h );
+			b2CreatePolygonShape( body, &sd, &box );
+		}
+	}
+	s->targetX = b2sRandomFloatRange( rng, -10.0f, 10.0f );
+	s->targetY = b2sRandomFloatRange( rng, -5.0f, 5.0f );
+}
+
+/* A single box dropped on a ground box (test_world.c:19-99, HelloWorld) */
+static void b2sHelloWorld( b2sScene* s )
+{
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, -10.0f );
+	b2Polygon groundBox = b2MakeBox( 50.0f, 10.0f );
+	b2ShapeDef gsd = b2DefaultShapeDef();
+	b2CreatePolygonShape( ground, &gsd, &groundBox );
+	b2BodyId body = b2sBody( s, b2_dynamicBody, 0.0f, 4.0f );
+	b2Polygon box = b2MakeBox( 1.0f, 1.0f );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	sd.density = 1.0f;
+	sd.material.friction = 0.3f;
+	b2CreatePolygonShape( body, &sd, &box );
+}
+
+/* A mixed bag of every shape pair on a box ground: circles, capsules, boxes and rounded
+   polygons falling onto each other and onto segments; used by the manifold parity tests. */
+static void b2sShapeZoo( b2sScene* s, int count, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	b2ShapeDef gd = b2DefaultShapeDef();
+	b2Polygon gbox = b2MakeOffsetBox( 20.0f, 0.5f, ( b2Vec2 ){ 0.0f, -0.5f }, b2MakeRot( 0.0f ) );
+	b2CreatePolygonShape( ground, &gd, &gbox );
+	b2Segment s1 = { { -20.0f, 0.0f }, { -20.0f, 20.0f } };
+	b2Segment s2 = { { 20.0f, 0.0f }, { 20.0f, 20.0f } };
+	b2CreateSegmentShape( ground, &gd, &s1 );
+	b2CreateSegmentShape( ground, &gd, &s2 );
+	for ( int k = 0; k < count; ++k )
+	{
+		float x = b2sRandomFloatRange( rng, -18.0f, 18.0f );
+		float y = b2sRandomFloatRange( rng, 1.0f, 15.0f );
+		b2BodyDef bd = b2DefaultBodyDef();
+		bd.type = b2_dynamicBody;
+		bd.position.x = x;
+		bd.position.y = y;
+		bd.rotation = b2MakeRot( b2sRandomFloatRange( rng, -3.0f, 3.0f ) );
+		b2BodyId body = b2CreateBody( s->worldId, &bd );
+		b2sAddBody( s, body, 1 );
+		b2ShapeDef sd = b2DefaultShapeDef();
+		sd.material.friction = b2sRandomFloatRange( rng, 0.1f, 0.9f );
+		sd.material.restitution = b2sRandomFloatRange( rng, 0.0f, 0.4f );
+		int kind = b2sRandomIntRange( rng, 0, 3 );
+		if ( kind == 0 )
+		{
+			b2Circle c = { { 0.0f, 0.0f }, b2sRandomFloatRange( rng, 0.2f, 0.6f ) };
+			b2CreateCircleShape( body, &sd, &c );
+		}
+		else if ( kind == 1 )
+		{
+			float hl = b2sRandomFloatRange( rng, 0.2f, 0.7f );
+			b2Capsule cap = { { -hl, 0.0f }, { hl, 0.0f }, b2sRandomFloatRange( rng, 0.1f, 0.4f ) };
+			b2CreateCapsuleShape( body, &sd, &cap );
+		}
+		else if ( kind == 2 )
+		{
+			b2Polygon box = b2MakeBox( b2sRandomFloatRange( rng, 0.2f, 0.8f ), b2sRandomFloatRange( rng, 0.2f, 0.8f ) );
+			b2CreatePolygonShape( body, &sd, &box );
+		}
+		else
+		{
+			int count = b2sRandomIntRange( rng, 3, 8 );
+			float radius = b2sRandomFloatRange( rng, 0.3f, 0.7f );
+			b2Vec2 pts[8];
+			for ( int v = 0; v < count; ++v )
+			{
+				float angle = 2.0f * 3.14159265359f * v / count + b2sRandomFloatRange( rng, -0.2f, 0.2f );
+				b2CosSin cs = b2ComputeCosSin( angle );
+				pts[v].x = radius * cs.cosine;
+				pts[v].y = radius * cs.sine;
+			}
+			b2Hull hull = b2ComputeHull( pts, count );
+			b2Polygon poly = hull.count >= 3 ? b2MakePolygon( &hull, b2sRandomFloatRange( rng, 0.0f, 0.1f ) ) : b2MakeBox( 0.4f, 0.4f );
+			b2CreatePolygonShape( body, &sd, &poly );
+		}
+	}
+}
+
+enum
+{
+	B2S_LARGE_PYRAMID = 0,
+	B2S_MANY_PYRAMIDS_RAIN = 1,
+	B2S_JOINT_GRID_MIXED = 2,
+	B2S_BATCH_WORLD = 3,
+	B2S_RAMP_WORLD = 4,
+	B2S_MANY_PYRAMIDS_REF = 5,
+	B2S_JOINT_GRID_REF = 6,
+	B2S_HELLO_WORLD = 7,
+	B2S_SHAPE_ZOO = 8,
+};
+
+/* Create a scene. kind selects the builder; a, b, c are its size parameters; seed feeds
+   the random stream (0 means 12345). flags bit 0 disables continuous collision.
+   Returns a handle >= 0, or -1 when the scene table is full or the world was refused. */
+B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int flags )
+{
+	int h = -1;
+	for ( int i = 0; i < B2S_MAX_SCENES; ++i )
+	{
+		if ( b2s_scenes[i].inUse == 0 )
+		{
+			h = i;
+			break;
+		}
+	}
+	if ( h < 0 ) return -1;
+	b2sScene* s = b2s_scenes + h;
+	memset( s, 0, sizeof( *s ) );
+	b2WorldDef wd = b2DefaultWorldDef();
+	if ( flags & 1 ) wd.enableContinuous = false;
+	s->worldId = b2CreateWorld( &wd );
+	if ( s->worldId.index1 == 0 ) return -1;
+	s->inUse = 1;
+	b2sRng rng = { seed ? seed : 12345u };
+	switch ( kind )
+	{
+		case B2S_LARGE_PYRAMID: b2sLargePyramid( s, a, b ); break;
+		case B2S_MANY_PYRAMIDS_RAIN: b2sManyPyramidsRain( s, a, b, c, &rng ); break;
+		case B2S_JOINT_GRID_MIXED: b2sJointGrid( s, a, 1, b, &rng ); break;
+		case B2S_BATCH_WORLD: b2sBatchWorld( s, a, &rng ); break;
+		case B2S_RAMP_WORLD: b2sRampWorld( s, a, b, &rng ); break;
+		case B2S_MANY_PYRAMIDS_REF: b2sManyPyramidsReference( s, a, b ); break;
+		case B2S_JOINT_GRID_REF: b2sJointGrid( s, a, 0, 0, &rng ); break;
+		case B2S_HELLO_WORLD: b2sHelloWorld( s ); break;
+		case B2S_SHAPE_ZOO: b2sShapeZoo( s, a, &rng ); break;
+		default: break;
+	}
+	return h;
+}
+
+B2S_EXPORT void b2s_destroy( int h )
+{
+	b2sScene* s = b2s_scenes + h;
+	if ( s->inUse == 0 ) return;
+	b2DestroyWorld( s->worldId );
+	free( s->bodies );
+	memset( s, 0, sizeof( *s ) );
+}
+
+B2S_EXPORT void b2s_step( int h, float dt, int subSteps, int count )
+{
+	for ( int i = 0; i < count; ++i ) b2World_Step( b2s_scenes[h].worldId, dt, subSteps );
+}
+
+B2S_EXPORT int b2s_body_count( int h ) { return b2s_scenes[h].bodyCount; }
+
+B2S_EXPORT int b2s_dynamic_count( int h ) { return b2s_scenes[h].dynamicCount; }
+
+B2S_EXPORT uint32_t b2s_world_id( int h )
+{
+	b2WorldId id = b2s_scenes[h].worldId;
+	return ( (uint32_t)id.index1 << 16 ) | id.generation;
+}
+
+/* 7 floats per body in creation order: p.x, p.y, q.c, q.s, v.x, v.y, w */
+B2S_EXPORT void b2s_get_state( int h, float* out )
+{
+	b2sScene* s = b2s_scenes + h;
+	for ( int i = 0; i < s->bodyCount; ++i )
+	{
+		b2Transform xf = b2Body_GetTransform( s->bodies[i] );
+		b2Vec2 v = b2Body_GetLinearVelocity( s->bodies[i] );
+		float w = b2Body_GetAngularVelocity( s->bodies[i] );
+		float* o = out + 7 * i;
+		o[0] = (float)xf.p.x;
+		o[1] = (float)xf.p.y;
+		o[2] = xf.q.c;
+		o[3] = xf.q.s;
+		o[4] = v.x;
+		o[5] = v.y;
+		o[6] = w;
+	}
+}
+
+/* FNV-1a 64 over the bit patterns of b2s_get_state */
+B2S_EXPORT uint64_t b2s_state_hash( int h )
+{
+	b2sScene* s = b2s_scenes + h;
+	uint64_t hash = 14695981039346656037ull;
+	float buf[7];
+	for ( int i = 0; i < s->bodyCount; ++i )
+	{
+		b2Transform xf = b2Body_GetTransform( s->bodies[i] );
+		b2Vec2 v = b2Body_GetLinearVelocity( s->bodies[i] );
+		buf[0] = (float)xf.p.x;
+		buf[1] = (float)xf.p.y;
+		buf[2] = xf.q.c;
+		buf[3] = xf.q.s;
+		buf[4] = v.x;
+		buf[5] = v.y;
+		buf[6] = b2Body_GetAngularVelocity( s->bodies[i] );
+		for ( int k = 0; k < 7; ++k )
+		{
+			uint32_t bits;
+			memcpy( &bits, buf + k, 4 );
+			hash = ( hash ^ bits ) * 1099511628211ull;
+		}
+	}
+	return hash;
+}
+
+/* Apply a per-body linear and angular velocity (3 floats per body, creation order;
+   static bodies are skipped by the library). */
+B2S_EXPORT void b2s_set_velocities( int h, const float* in )
+{
+	b2sScene* s = b2s_scenes + h;
+	for ( int i = 0; i < s->bodyCount; ++i )
+	{
+		b2Vec2 v = { in[3 * i], in[3 * i + 1] };
+		b2Body_SetLinearVelocity( s->bodies[i], v );
+		b2Body_SetAngularVelocity( s->bodies[i], in[3 * i + 2] );
+	}
+}
+
+B2S_EXPORT void b2s_target( int h, float* out )
+{
+	out[0] = b2s_scenes[h].targetX;
+	out[1] = b2s_scenes[h].targetY;
+}
+
+B2S_EXPORT void b2s_counters( int h, int* out )
+{
+	b2Counters c = b2World_GetCounters( b2s_scenes[h].worldId );
+	out[0] = c.bodyCount;
+	out[1] = c.shapeCount;
+	out[2] = c.contactCount;
+	out[3] = c.jointCount;
+	for ( int i = 0; i < 24; ++i ) out[4 + i] = c.colorCounts[i];
+	out[28] = c.awakeContactCount;
+	out[29] = c.recycledContactCount;
+}

@@ -1,0 +1,612 @@
+/*
+ * box2d_gb300.h -- public C ABI of the GB300 step library.
+ *
+ * This header declares the subset of Box2D v3.2's public API (include/box2d/box2d.h,
+ * types.h, collision.h, math_functions.h, id.h, base.h in the reference) that a program
+ * needs to build worlds, step them and read results. Every struct below has the same
+ * field order, types and size as the reference declaration it stands in for, so a
+ * program compiled against the reference headers links against this library unchanged
+ * (the layouts are checked at build time against the reference headers by
+ * oracle/abi_check.c when those headers are present).
+ *
+ * float32 only: b2Pos is b2Vec2 and b2WorldTransform is b2Transform, as in the reference
+ * when BOX2D_DOUBLE_PRECISION is off (math_functions.h:69-70).
+ */
+#ifndef BOX2D_GB300_H
+#define BOX2D_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define B2G_API extern "C" __attribute__( ( visibility( "default" ) ) )
+#define B2G_INLINE static inline
+#define B2G_LITERAL( T ) T
+#else
+#define B2G_API __attribute__( ( visibility( "default" ) ) )
+#define B2G_INLINE static inline
+#define B2G_LITERAL( T ) ( T )
+#endif
+
+#define B2_NULL_INDEX ( -1 )
+#define B2_MAX_POLYGON_VERTICES 8
+#define B2_PI 3.14159265359f
+#define B2_DEFAULT_CATEGORY_BITS 1
+#define B2_DEFAULT_MASK_BITS UINT64_MAX
+#define B2_GRAPH_COLOR_COUNT 24
+
+/* ---- math types (math_functions.h:19-96) ---- */
+typedef struct b2Vec2
+{
+	float x, y;
+} b2Vec2;
+
+typedef struct b2CosSin
+{
+	float cosine;
+	float sine;
+} b2CosSin;
+
+typedef struct b2Rot
+{
+	float c, s;
+} b2Rot;
+
+typedef struct b2Transform
+{
+	b2Vec2 p;
+	b2Rot q;
+} b2Transform;
+
+typedef b2Vec2 b2Pos;
+typedef b2Transform b2WorldTransform;
+
+typedef struct b2Mat22
+{
+	b2Vec2 cx, cy;
+} b2Mat22;
+
+typedef struct b2AABB
+{
+	b2Vec2 lowerBound;
+	b2Vec2 upperBound;
+} b2AABB;
+
+/* ---- ids (id.h:37-81) ---- */
+typedef struct b2WorldId
+{
+	uint16_t index1;
+	uint16_t generation;
+} b2WorldId;
+
+typedef struct b2BodyId
+{
+	int32_t index1;
+	uint16_t world0;
+	uint16_t generation;
+} b2BodyId;
+
+typedef struct b2ShapeId
+{
+	int32_t index1;
+	uint16_t world0;
+	uint16_t generation;
+} b2ShapeId;
+
+typedef struct b2JointId
+{
+	int32_t index1;
+	uint16_t world0;
+	uint16_t generation;
+} b2JointId;
+
+typedef struct b2ContactId
+{
+	int32_t index1;
+	uint16_t world0;
+	int16_t padding;
+	uint32_t generation;
+} b2ContactId;
+
+#define B2_IS_NULL( id ) ( ( id ).index1 == 0 )
+#define B2_IS_NON_NULL( id ) ( ( id ).index1 != 0 )
+
+/* ---- geometry (collision.h) ---- */
+typedef struct b2MassData
+{
+	float mass;
+	b2Vec2 center;
+	float rotationalInertia;
+} b2MassData;
+
+typedef struct b2Circle
+{
+	b2Vec2 center;
+	float radius;
+} b2Circle;
+
+typedef struct b2Capsule
+{
+	b2Vec2 center1;
+	b2Vec2 center2;
+	float radius;
+} b2Capsule;
+
+typedef struct b2Polygon
+{
+	b2Vec2 vertices[B2_MAX_POLYGON_VERTICES];
+	b2Vec2 normals[B2_MAX_POLYGON_VERTICES];
+	b2Vec2 centroid;
+	float radius;
+	int count;
+} b2Polygon;
+
+typedef struct b2Segment
+{
+	b2Vec2 point1;
+	b2Vec2 point2;
+} b2Segment;
+
+typedef struct b2Hull
+{
+	b2Vec2 points[B2_MAX_POLYGON_VERTICES];
+	int count;
+} b2Hull;
+
+typedef struct b2ManifoldPoint
+{
+	b2Vec2 anchorA;
+	b2Vec2 anchorB;
+	float separation;
+	float baseSeparation;
+	float normalImpulse;
+	float tangentImpulse;
+	float totalNormalImpulse;
+	float normalVelocity;
+	uint16_t id;
+	bool persisted;
+} b2ManifoldPoint;
+
+typedef struct b2Manifold
+{
+	b2Vec2 normal;
+	float rollingImpulse;
+	b2ManifoldPoint points[2];
+	int pointCount;
+} b2Manifold;
+
+typedef struct b2LocalManifoldPoint
+{
+	b2Vec2 point;
+	float separation;
+	uint16_t id;
+} b2LocalManifoldPoint;
+
+typedef struct b2LocalManifold
+{
+	b2Vec2 normal;
+	b2LocalManifoldPoint points[2];
+	int pointCount;
+} b2LocalManifold;
+
+/* ---- world / body / shape definitions (types.h) ---- */
+typedef void b2TaskCallback( void* taskContext );
+typedef void* b2EnqueueTaskCallback( b2TaskCallback* task, void* taskContext, void* userContext );
+typedef void b2FinishTaskCallback( void* userTask, void* userContext );
+typedef float b2FrictionCallback( float frictionA, uint64_t userMaterialIdA, float frictionB, uint64_t userMaterialIdB );
+typedef float b2RestitutionCallback( float restitutionA, uint64_t userMaterialIdA, float restitutionB,
+									 uint64_t userMaterialIdB );
+
+typedef struct b2Capacity
+{
+	int staticShapeCount;
+	int dynamicShapeCount;
+	int staticBodyCount;
+	int dynamicBodyCount;
+	int contactCount;
+} b2Capacity;
+
+typedef struct b2WorldDef
+{
+	b2Vec2 gravity;
+	float restitutionThreshold;
+	float hitEventThreshold;
+	float contactHertz;
+	float contactDampingRatio;
+	float contactSpeed;
+	float maximumLinearSpeed;
+	b2FrictionCallback* frictionCallback;
+	b2RestitutionCallback* restitutionCallback;
+	bool enableSleep;
+	bool enableContinuous;
+	bool enableContactSoftening;
+	int workerCount;
+	b2EnqueueTaskCallback* enqueueTask;
+	b2FinishTaskCallback* finishTask;
+	void* userTaskContext;
+	void* userData;
+	b2Capacity capacity;
+	int internalValue;
+} b2WorldDef;
+
+typedef enum b2BodyType
+{
+	b2_staticBody = 0,
+	b2_kinematicBody = 1,
+	b2_dynamicBody = 2,
+	b2_bodyTypeCount,
+} b2BodyType;
+
+typedef struct b2MotionLocks
+{
+	bool linearX;
+	bool linearY;
+	bool angularZ;
+} b2MotionLocks;
+
+typedef struct b2BodyDef
+{
+	b2BodyType type;
+	b2Pos position;
+	b2Rot rotation;
+	b2Vec2 linearVelocity;
+	float angularVelocity;
+	float linearDamping;
+	float angularDamping;
+	float gravityScale;
+	float sleepThreshold;
+	float safetyFactor;
+	const char* name;
+	void* userData;
+	b2MotionLocks motionLocks;
+	bool enableSleep;
+	bool isAwake;
+	bool isBullet;
+	bool isEnabled;
+	bool allowFastRotation;
+	bool enableContactRecycling;
+	int internalValue;
+} b2BodyDef;
+
+typedef struct b2Filter
+{
+	uint64_t categoryBits;
+	uint64_t maskBits;
+	int groupIndex;
+} b2Filter;
+
+typedef enum b2ShapeType
+{
+	b2_circleShape,
+	b2_capsuleShape,
+	b2_segmentShape,
+	b2_polygonShape,
+	b2_chainSegmentShape,
+	b2_shapeTypeCount
+} b2ShapeType;
+
+typedef struct b2SurfaceMaterial
+{
+	float friction;
+	float restitution;
+	float rollingResistance;
+	float tangentSpeed;
+	uint64_t userMaterialId;
+	uint32_t customColor;
+} b2SurfaceMaterial;
+
+typedef struct b2ShapeDef
+{
+	void* userData;
+	b2SurfaceMaterial material;
+	float density;
+	b2Filter filter;
+	bool enableCustomFiltering;
+	bool isSensor;
+	bool enableSensorEvents;
+	bool enableContactEvents;
+	bool enableHitEvents;
+	bool enablePreSolveEvents;
+	bool invokeContactCreation;
+	bool updateBodyMass;
+	int internalValue;
+} b2ShapeDef;
+
+typedef struct b2Profile
+{
+	float step;
+	float pairs;
+	float collide;
+	float solve;
+	float solverSetup;
+	float constraints;
+	float prepareConstraints;
+	float integrateVelocities;
+	float warmStart;
+	float solveImpulses;
+	float integratePositions;
+	float relaxImpulses;
+	float applyRestitution;
+	float storeImpulses;
+	float splitIslands;
+	float transforms;
+	float sensorHits;
+	float jointEvents;
+	float hitEvents;
+	float refit;
+	float bullets;
+	float sleepIslands;
+	float sensors;
+} b2Profile;
+
+typedef struct b2Counters
+{
+	int64_t byteCount;
+	int bodyCount;
+	int shapeCount;
+	int contactCount;
+	int jointCount;
+	int islandCount;
+	int stackUsed;
+	int staticTreeHeight;
+	int treeHeight;
+	int taskCount;
+	int colorCounts[24];
+	int awakeContactCount;
+	int recycledContactCount;
+} b2Counters;
+
+/* ---- joints (types.h b2JointDef family) ---- */
+typedef enum b2JointType
+{
+	b2_distanceJoint,
+	b2_filterJoint,
+	b2_motorJoint,
+	b2_moverJoint,
+	b2_pogoJoint,
+	b2_prismaticJoint,
+	b2_revoluteJoint,
+	b2_weldJoint,
+	b2_wheelJoint,
+} b2JointType;
+
+typedef struct b2JointDef
+{
+	void* userData;
+	b2BodyId bodyIdA;
+	b2BodyId bodyIdB;
+	b2Transform localFrameA;
+	b2Transform localFrameB;
+	float forceThreshold;
+	float torqueThreshold;
+	float constraintHertz;
+	float constraintDampingRatio;
+	float drawScale;
+	bool collideConnected;
+} b2JointDef;
+
+typedef struct b2DistanceJointDef
+{
+	b2JointDef base;
+	float length;
+	bool enableSpring;
+	float lowerSpringForce;
+	float upperSpringForce;
+	float hertz;
+	float dampingRatio;
+	bool enableLimit;
+	float minLength;
+	float maxLength;
+	bool enableMotor;
+	float maxMotorForce;
+	float motorSpeed;
+	int internalValue;
+} b2DistanceJointDef;
+
+typedef struct b2PrismaticJointDef
+{
+	b2JointDef base;
+	bool enableSpring;
+	float hertz;
+	float dampingRatio;
+	float targetTranslation;
+	bool enableLimit;
+	float lowerTranslation;
+	float upperTranslation;
+	bool enableMotor;
+	float maxMotorForce;
+	float motorSpeed;
+	int internalValue;
+} b2PrismaticJointDef;
+
+typedef struct b2RevoluteJointDef
+{
+	b2JointDef base;
+	float targetAngle;
+	bool enableSpring;
+	float hertz;
+	float dampingRatio;
+	bool enableLimit;
+	float lowerAngle;
+	float upperAngle;
+	bool enableMotor;
+	float maxMotorTorque;
+	float motorSpeed;
+	int internalValue;
+} b2RevoluteJointDef;
+
+typedef struct b2WeldJointDef
+{
+	b2JointDef base;
+	float linearHertz;
+	float angularHertz;
+	float linearDampingRatio;
+	float angularDampingRatio;
+	int internalValue;
+} b2WeldJointDef;
+
+typedef struct b2WheelJointDef
+{
+	b2JointDef base;
+	bool enableSpring;
+	float hertz;
+	float dampingRatio;
+	bool enableLimit;
+	float lowerTranslation;
+	float upperTranslation;
+	bool enableMotor;
+	float maxMotorTorque;
+	float motorSpeed;
+	int internalValue;
+} b2WheelJointDef;
+
+/* ---- events (types.h) ---- */
+typedef struct b2ContactBeginTouchEvent
+{
+	b2ShapeId shapeIdA;
+	b2ShapeId shapeIdB;
+	b2ContactId contactId;
+} b2ContactBeginTouchEvent;
+
+typedef struct b2ContactEndTouchEvent
+{
+	b2ShapeId shapeIdA;
+	b2ShapeId shapeIdB;
+	b2ContactId contactId;
+} b2ContactEndTouchEvent;
+
+typedef struct b2ContactHitEvent
+{
+	b2ShapeId shapeIdA;
+	b2ShapeId shapeIdB;
+	b2ContactId contactId;
+	b2Pos point;
+	b2Vec2 normal;
+	float approachSpeed;
+} b2ContactHitEvent;
+
+typedef struct b2ContactEvents
+{
+	b2ContactBeginTouchEvent* beginEvents;
+	b2ContactEndTouchEvent* endEvents;
+	b2ContactHitEvent* hitEvents;
+	int beginCount;
+	int endCount;
+	int hitCount;
+} b2ContactEvents;
+
+typedef struct b2BodyMoveEvent
+{
+	void* userData;
+	b2WorldTransform transform;
+	b2BodyId bodyId;
+	bool fellAsleep;
+} b2BodyMoveEvent;
+
+typedef struct b2BodyEvents
+{
+	b2BodyMoveEvent* moveEvents;
+	int moveCount;
+} b2BodyEvents;
+
+/* ---- inline math used by callers (math_functions.h) ---- */
+B2G_INLINE b2Vec2 b2Add( b2Vec2 a, b2Vec2 b )
+{
+	return B2G_LITERAL( b2Vec2 ){ a.x + b.x, a.y + b.y };
+}
+
+B2G_INLINE b2Vec2 b2Sub( b2Vec2 a, b2Vec2 b )
+{
+	return B2G_LITERAL( b2Vec2 ){ a.x - b.x, a.y - b.y };
+}
+
+/* ---- API: base (base.h:150-164) ---- */
+B2G_API uint64_t b2GetTicks( void );
+B2G_API float b2GetMilliseconds( uint64_t ticks );
+B2G_API uint32_t b2Hash( uint32_t hash, const uint8_t* data, int count );
+
+/* ---- API: math (math_functions.h, math_functions.c) ---- */
+B2G_API float b2Atan2( float y, float x );
+B2G_API b2CosSin b2ComputeCosSin( float radians );
+B2G_API b2Rot b2MakeRot( float radians );
+
+/* ---- API: geometry (collision.h:160-230, geometry.c, hull.c) ---- */
+B2G_API b2Hull b2ComputeHull( const b2Vec2* points, int count );
+B2G_API b2Polygon b2MakePolygon( const b2Hull* hull, float radius );
+B2G_API b2Polygon b2MakeOffsetPolygon( const b2Hull* hull, b2Vec2 position, b2Rot rotation );
+B2G_API b2Polygon b2MakeSquare( float halfWidth );
+B2G_API b2Polygon b2MakeBox( float halfWidth, float halfHeight );
+B2G_API b2Polygon b2MakeRoundedBox( float halfWidth, float halfHeight, float radius );
+B2G_API b2Polygon b2MakeOffsetBox( float halfWidth, float halfHeight, b2Vec2 center, b2Rot rotation );
+B2G_API b2MassData b2ComputeCircleMass( const b2Circle* shape, float density );
+B2G_API b2MassData b2ComputeCapsuleMass( const b2Capsule* shape, float density );
+B2G_API b2MassData b2ComputePolygonMass( const b2Polygon* shape, float density );
+B2G_API b2LocalManifold b2CollidePolygons( const b2Polygon* polygonA, const b2Polygon* polygonB, b2Transform xf );
+
+/* ---- API: world (box2d.h:34-200) ---- */
+B2G_API b2WorldDef b2DefaultWorldDef( void );
+B2G_API b2BodyDef b2DefaultBodyDef( void );
+B2G_API b2Filter b2DefaultFilter( void );
+B2G_API b2ShapeDef b2DefaultShapeDef( void );
+B2G_API b2SurfaceMaterial b2DefaultSurfaceMaterial( void );
+
+B2G_API b2WorldId b2CreateWorld( const b2WorldDef* def );
+B2G_API void b2DestroyWorld( b2WorldId worldId );
+B2G_API bool b2World_IsValid( b2WorldId id );
+B2G_API void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount );
+B2G_API b2BodyEvents b2World_GetBodyEvents( b2WorldId worldId );
+B2G_API b2ContactEvents b2World_GetContactEvents( b2WorldId worldId );
+B2G_API void b2World_EnableSleeping( b2WorldId worldId, bool flag );
+B2G_API bool b2World_IsSleepingEnabled( b2WorldId worldId );
+B2G_API void b2World_EnableContinuous( b2WorldId worldId, bool flag );
+B2G_API bool b2World_IsContinuousEnabled( b2WorldId worldId );
+B2G_API void b2World_EnableWarmStarting( b2WorldId worldId, bool flag );
+B2G_API void b2World_SetGravity( b2WorldId worldId, b2Vec2 gravity );
+B2G_API b2Vec2 b2World_GetGravity( b2WorldId worldId );
+B2G_API int b2World_GetAwakeBodyCount( b2WorldId worldId );
+B2G_API b2Profile b2World_GetProfile( b2WorldId worldId );
+B2G_API b2Counters b2World_GetCounters( b2WorldId worldId );
+
+/* ---- API: bodies (box2d.h:355-550) ---- */
+B2G_API b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def );
+B2G_API bool b2Body_IsValid( b2BodyId id );
+B2G_API b2BodyType b2Body_GetType( b2BodyId bodyId );
+B2G_API b2Pos b2Body_GetPosition( b2BodyId bodyId );
+B2G_API b2Rot b2Body_GetRotation( b2BodyId bodyId );
+B2G_API b2WorldTransform b2Body_GetTransform( b2BodyId bodyId );
+B2G_API b2Vec2 b2Body_GetLocalPoint( b2BodyId bodyId, b2Pos worldPoint );
+B2G_API b2Pos b2Body_GetWorldPoint( b2BodyId bodyId, b2Vec2 localPoint );
+B2G_API b2Vec2 b2Body_GetLinearVelocity( b2BodyId bodyId );
+B2G_API float b2Body_GetAngularVelocity( b2BodyId bodyId );
+B2G_API void b2Body_SetLinearVelocity( b2BodyId bodyId, b2Vec2 linearVelocity );
+B2G_API void b2Body_SetAngularVelocity( b2BodyId bodyId, float angularVelocity );
+B2G_API float b2Body_GetMass( b2BodyId bodyId );
+B2G_API float b2Body_GetRotationalInertia( b2BodyId bodyId );
+B2G_API b2Vec2 b2Body_GetLocalCenterOfMass( b2BodyId bodyId );
+B2G_API b2Pos b2Body_GetWorldCenterOfMass( b2BodyId bodyId );
+B2G_API bool b2Body_IsAwake( b2BodyId bodyId );
+
+/* ---- API: shapes (box2d.h:659-724) ---- */
+B2G_API b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Circle* circle );
+B2G_API b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Segment* segment );
+B2G_API b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Capsule* capsule );
+B2G_API b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon );
+B2G_API void b2Shape_SetFriction( b2ShapeId shapeId, float friction );
+B2G_API float b2Shape_GetFriction( b2ShapeId shapeId );
+
+/* ---- API: joints (box2d.h:760-1100) ---- */
+B2G_API b2DistanceJointDef b2DefaultDistanceJointDef( void );
+B2G_API b2PrismaticJointDef b2DefaultPrismaticJointDef( void );
+B2G_API b2RevoluteJointDef b2DefaultRevoluteJointDef( void );
+B2G_API b2WeldJointDef b2DefaultWeldJointDef( void );
+B2G_API b2WheelJointDef b2DefaultWheelJointDef( void );
+B2G_API b2JointId b2CreateDistanceJoint( b2WorldId worldId, const b2DistanceJointDef* def );
+B2G_API b2JointId b2CreatePrismaticJoint( b2WorldId worldId, const b2PrismaticJointDef* def );
+B2G_API b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def );
+B2G_API b2JointId b2CreateWeldJoint( b2WorldId worldId, const b2WeldJointDef* def );
+B2G_API b2JointId b2CreateWheelJoint( b2WorldId worldId, const b2WheelJointDef* def );
+B2G_API b2JointType b2Joint_GetType( b2JointId jointId );
+B2G_API float b2RevoluteJoint_GetAngle( b2JointId jointId );
+
+#endif /* BOX2D_GB300_H */
