@@ -1,0 +1,127 @@
+"""GB300 (sm_103a) implementation of Box2D v3.2's per-step hot path behind the Box2D C API.
+
+The product is the shared library ``libbox2d_gb300.so`` in this directory: it exports the
+``box2d.h`` subset declared in ``include/box2d_gb300.h`` (b2CreateWorld, b2World_Step,
+bodies, shapes, joints, events) and runs the step on the GPU. This module only locates
+and loads it with ctypes, plus the scene builders compiled into it (``b2s_*``) and the
+parity probes (``b2p_*``). There is no CPU path: if the library or a CUDA device is
+missing, loading or world creation fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent
+LIB_PATH = PKG_DIR / "libbox2d_gb300.so"
+
+# scene kinds of scenes.c
+LARGE_PYRAMID = 0
+MANY_PYRAMIDS_RAIN = 1
+JOINT_GRID_MIXED = 2
+BATCH_WORLD = 3
+RAMP_WORLD = 4
+MANY_PYRAMIDS_REF = 5
+JOINT_GRID_REF = 6
+HELLO_WORLD = 7
+SHAPE_ZOO = 8
+
+NO_CONTINUOUS = 1
+
+
+def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
+    c_int, c_u32, c_u64, c_f, c_p = ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float, ctypes.c_void_p
+    sig = {
+        "b2s_create": (c_int, [c_int, c_int, c_int, c_int, c_u32, c_int]),
+        "b2s_destroy": (None, [c_int]),
+        "b2s_step": (None, [c_int, c_f, c_int, c_int]),
+        "b2s_body_count": (c_int, [c_int]),
+        "b2s_dynamic_count": (c_int, [c_int]),
+        "b2s_world_id": (c_u32, [c_int]),
+        "b2s_get_state": (None, [c_int, c_p]),
+        "b2s_state_hash": (c_u64, [c_int]),
+        "b2s_set_velocities": (None, [c_int, c_p]),
+        "b2s_target": (None, [c_int, c_p]),
+        "b2s_counters": (None, [c_int, c_p]),
+        "b2p_contacts": (c_int, [c_u32, c_p, c_int]),
+        "b2p_contact_floats": (c_int, [c_u32, c_p, c_int]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def load_library(path: str | Path | None = None) -> ctypes.CDLL:
+    """Load a Box2D-API shared library (the GB300 library by default) with its scene and
+    probe entry points bound. Raises if the file is missing."""
+    p = Path(path) if path is not None else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"` "
+            "(the GB300 step library has no CPU fallback)")
+    return _bind(ctypes.CDLL(str(p)))
+
+
+class Scene:
+    """A world built by one of the scene builders, stepped through the public C API."""
+
+    def __init__(self, lib: ctypes.CDLL, kind: int, a: int = 0, b: int = 0, c: int = 0, seed: int = 0, flags: int = 0):
+        self.lib = lib
+        self.handle = lib.b2s_create(kind, a, b, c, seed, flags)
+        if self.handle < 0:
+            raise RuntimeError("scene creation failed (no world slot, or no usable CUDA device for the GB300 library)")
+        self.body_count = lib.b2s_body_count(self.handle)
+        self.dynamic_count = lib.b2s_dynamic_count(self.handle)
+
+    @property
+    def world_id(self) -> int:
+        return self.lib.b2s_world_id(self.handle)
+
+    def step(self, count: int = 1, dt: float = 1.0 / 60.0, substeps: int = 4) -> None:
+        self.lib.b2s_step(self.handle, dt, substeps, count)
+
+    def state(self) -> np.ndarray:
+        out = np.zeros((self.body_count, 7), np.float32)
+        self.lib.b2s_get_state(self.handle, out.ctypes.data)
+        return out
+
+    def state_hash(self) -> int:
+        return int(self.lib.b2s_state_hash(self.handle))
+
+    def contacts(self) -> np.ndarray:
+        cap = 1 << 16
+        while True:
+            buf = np.zeros((cap, 8), np.int32)
+            n = self.lib.b2p_contacts(self.world_id, buf.ctypes.data, cap)
+            if n <= cap:
+                return buf[:n]
+            cap = n
+
+    def contact_floats(self) -> np.ndarray:
+        cap = 1 << 16
+        while True:
+            buf = np.zeros((cap, 12), np.float32)
+            n = self.lib.b2p_contact_floats(self.world_id, buf.ctypes.data, cap)
+            if n <= cap:
+                return buf[:n]
+            cap = n
+
+    def counters(self) -> np.ndarray:
+        out = np.zeros(30, np.int32)
+        self.lib.b2s_counters(self.handle, out.ctypes.data)
+        return out
+
+    def close(self) -> None:
+        if self.handle >= 0:
+            self.lib.b2s_destroy(self.handle)
+            self.handle = -1
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

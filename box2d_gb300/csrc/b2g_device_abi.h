@@ -1,0 +1,240 @@
+/*
+ * Thin C ABI between the C17 host side of the GB300 step library and its CUDA kernels,
+ * plus the plain-old-data records both sides agree on.
+ *
+ * Device memory layout (one world = one b2gDeviceWorld):
+ *   bodies, indexed by body id (static and awake alike): transform, center, inverse mass
+ *     data, extents, awake index, type/flags, shape list range
+ *   awake solver state, indexed by awake index (the reference's awake-set order,
+ *     body.c:200-260): b2BodyState as two float4 (v.x, v.y, w, flags) and
+ *     (dp.x, dp.y, dq.c, dq.s), plus the integration parameters
+ *   shapes, indexed by shape id: geometry, material, AABB, fat AABB, enlarge flag
+ *   contacts, indexed by contact id (stable across color moves): the b2ContactSim fields
+ *   graph colors: per color an array of contact ids and joint ids in the reference's array
+ *     order; contact constraints are laid out color by color, one slot per contact
+ *
+ * Every function returns 0 on success or a CUDA error code.
+ */
+#ifndef B2G_DEVICE_ABI_H
+#define B2G_DEVICE_ABI_H
+
+#include "box2d_gb300.h"
+
+#ifdef __cplusplus
+extern "C"
+{
+#endif
+
+#define B2G_OVERFLOW_INDEX ( B2_GRAPH_COLOR_COUNT - 1 )
+
+/* body flag bits (body.h b2BodyFlags) */
+enum
+{
+	B2G_LOCK_X = 0x1,
+	B2G_LOCK_Y = 0x2,
+	B2G_LOCK_Z = 0x4,
+	B2G_IS_FAST = 0x8,
+	B2G_IS_BULLET = 0x10,
+	B2G_SPEED_CAPPED = 0x20,
+	B2G_HAD_TOI = 0x40,
+	B2G_ALLOW_FAST_ROTATION = 0x80,
+	B2G_ENLARGE_BOUNDS = 0x100,
+	B2G_DYNAMIC_FLAG = 0x200,
+	B2G_DIRTY_MASS = 0x400,
+	B2G_ENABLE_SLEEP = 0x800,
+	B2G_ENABLE_RECYCLING = 0x1000,
+	B2G_TRANSIENT = B2G_IS_FAST | B2G_SPEED_CAPPED | B2G_HAD_TOI,
+};
+
+/* contact sim flag bits (contact.h b2ContactFlags) */
+enum
+{
+	B2G_C_TOUCHING = 0x1,
+	B2G_C_HIT_EVENT = 0x2,
+	B2G_C_ENABLE_EVENTS = 0x4,
+	B2G_C_RECYCLE = 0x8,
+	B2G_S_TOUCHING = 0x10000,
+	B2G_S_DISJOINT = 0x20000,
+	B2G_S_STARTED = 0x40000,
+	B2G_S_STOPPED = 0x80000,
+	B2G_S_HIT_EVENT = 0x100000,
+	B2G_S_PRESOLVE = 0x200000,
+	B2G_S_RELATIVE_VALID = 0x400000,
+	B2G_S_LIVE = 0x40000000, /* slot holds a contact (device bookkeeping only) */
+};
+
+/* shape record (b2Shape geometry + material). Circles keep center in v[0]; capsules and
+   segments keep their two points in v[0], v[1]; polygons use the full b2Polygon. */
+typedef struct b2gShape
+{
+	int type;
+	int bodyId;
+	int enableHitEvents;
+	int count;
+	b2Vec2 v[B2_MAX_POLYGON_VERTICES];
+	b2Vec2 n[B2_MAX_POLYGON_VERTICES];
+	b2Vec2 centroid;
+	float radius;
+	float aabbMargin;
+	float friction, restitution, rollingResistance, tangentSpeed;
+} b2gShape;
+
+/* contact record (contact.h:103-142 b2ContactSim without ids kept on the host) */
+typedef struct b2gContact
+{
+	int shapeIdA, shapeIdB;
+	uint32_t simFlags;
+	int bodySimIndexA, bodySimIndexB;
+	float invMassA, invIA, invMassB, invIB;
+	float friction, restitution, rollingResistance, tangentSpeed;
+	b2Rot cachedRotationA, cachedRotationB;
+	b2Transform cachedRelativePose;
+	b2Manifold manifold;
+} b2gContact;
+
+/* new contact written by the host into the contact slot of its id */
+typedef struct b2gContactInit
+{
+	int contactId;
+	int shapeIdA, shapeIdB;
+	uint32_t simFlags;
+	float friction, restitution;
+} b2gContactInit;
+
+/* one contact constraint slot (contact_solver.c:1070-1100 b2ContactConstraintWide lane) */
+typedef struct b2gContactLane
+{
+	int indexA, indexB; /* awake index + 1, 0 = none */
+	float invMassA, invMassB, invIA, invIB;
+	b2Vec2 normal;
+	float friction, tangentSpeed, rollingResistance, rollingMass, rollingImpulse;
+	float biasRate, massScale, impulseScale;
+	b2Vec2 anchorA1, anchorB1;
+	float normalMass1, tangentMass1, baseSeparation1, normalImpulse1, totalNormalImpulse1, tangentImpulse1;
+	b2Vec2 anchorA2, anchorB2;
+	float baseSeparation2, normalImpulse2, totalNormalImpulse2, tangentImpulse2, normalMass2, tangentMass2;
+	float restitution, relativeVelocity1, relativeVelocity2;
+	int groupFlags; /* bit 0: a lane of its 4-wide group has rolling resistance; bit 1: restitution */
+	int pointCount;
+} b2gContactLane;
+
+/* joint record (joint.h:267-301 b2JointSim, revolute/prismatic/weld/wheel/distance) */
+typedef struct b2gJoint
+{
+	int type;
+	int bodyIdA, bodyIdB;
+	int indexA, indexB; /* awake indices, -1 = static */
+	b2Transform localFrameA, localFrameB;
+	float invMassA, invMassB, invIA, invIB;
+	float constraintHertz, constraintDampingRatio;
+	float softBias, softMass, softImpulse; /* constraint softness */
+	b2Transform frameA, frameB;
+	b2Vec2 deltaCenter;
+	/* per-type parameters */
+	float p[16];
+	/* per-type accumulated impulses and solver constants */
+	float s[16];
+	int enableSpring, enableLimit, enableMotor, jointId;
+} b2gJoint;
+
+/* step constants (b2StepContext, solver.h:155-237) */
+typedef struct b2gStepParams
+{
+	float dt, inv_dt, h, inv_h;
+	int subStepCount;
+	float contactBiasRate, contactMassScale, contactImpulseScale;
+	float staticBiasRate, staticMassScale, staticImpulseScale;
+	float restitutionThreshold, maxLinearVelocity, contactSpeed, contactHertz, contactDampingRatio;
+	float gravityX, gravityY;
+	float jointHertzCap;
+	int enableWarmStarting, enableContinuous, enableSleep, enableContactSoftening;
+	float contactRecycleDistance;
+} b2gStepParams;
+
+/* per-step results the host reads back */
+typedef struct b2gStepCounters
+{
+	int stateChangeCount;
+	int enlargedBodyCount;
+	int recycledContactCount;
+	int pairCount;
+	int pairOverflow;
+	int fastBodyCount;
+	int status; /* nonzero: a device check failed (see B2G_STATUS_*) */
+	int pad;
+} b2gStepCounters;
+
+enum
+{
+	B2G_STATUS_OK = 0,
+	B2G_STATUS_NAN = 1,
+	B2G_STATUS_CAPACITY = 2,
+};
+
+typedef struct b2gDeviceWorld b2gDeviceWorld;
+
+/* lifetime */
+int b2gDev_Create( b2gDeviceWorld** out );
+void b2gDev_Destroy( b2gDeviceWorld* dw );
+const char* b2gDev_ErrorString( int code );
+
+/* uploads of cold data (whole arrays; called when the host marks them dirty) */
+int b2gDev_UploadShapes( b2gDeviceWorld* dw, const b2gShape* shapes, const float* aabbs, const float* fatAABBs, int count );
+int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const float* xf, const float* center, const float* localCenter,
+						 const float* invMass, const float* invI, const float* minExtent, const float* maxExtent,
+						 const float* sleepThreshold, const float* safetyFactor, const int* awakeIndex, const uint32_t* typeFlags,
+						 const int* shapeStart, const int* shapeCount, const int* shapeList, int shapeListCount );
+int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int* awakeBodyId, const float* stateV, const float* stateD,
+						const float* params, const float* center0 );
+int b2gDev_DownloadAwake( b2gDeviceWorld* dw, int awakeCount, float* stateV, float* stateD, float* params, float* center0 );
+int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* center, uint32_t* typeFlags );
+int b2gDev_DownloadShapeBoxes( b2gDeviceWorld* dw, int shapeCount, float* aabbs, float* fatAABBs );
+int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float vx, float vy, float w, int which );
+
+/* contacts */
+int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity );
+int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* inits, int count );
+int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* contactIds, int count );
+int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* colorContactIds, const int* colorContactOffsets,
+						 int totalContacts );
+int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count );
+
+/* joints */
+int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* colorJointOffsets );
+int b2gDev_DownloadJoints( b2gDeviceWorld* dw, b2gJoint* joints, int count );
+
+/* broadphase: tree nodes as (aabb float4, child1, child2 / userData, flags) */
+typedef struct b2gTreeNode
+{
+	b2AABB aabb;
+	int child1; /* leaf: shape id */
+	int child2; /* leaf: -1 */
+	int isLeaf;
+	int categoryNonZero; /* the node's category bits intersect the query mask (all ones) */
+} b2gTreeNode;
+
+int b2gDev_UploadTree( b2gDeviceWorld* dw, int treeType, const b2gTreeNode* nodes, int nodeCount, int root );
+/* query each moved proxy's fat AABB; pairs come back grouped per move in the reference's
+   order (proxy list newest first). outPairs holds (shapeA, shapeB); outCounts per move */
+int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* moveProxyKeys, const float* moveBoxes, const int* moveShapeIds,
+					  int moveCount, int** outPairs, int** outCounts, int* outTotal );
+
+/* narrowphase over every live contact; returns the state-change list (contactId, flags)
+   sorted by contact id */
+int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* params, int contactIdCapacity, const int** outChanges,
+					int* outChangeCount, int* outRecycled );
+
+/* Soft Step solver + body finalization; returns enlarged bodies (awake index, ascending) */
+int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* params, const int* activeColors, int activeColorCount,
+				  const int* colorContactCounts, const int* colorJointCounts, int awakeCount, const int** outEnlarged,
+				  int* outEnlargedCount, const float** outFatBoxes, int* outStatus );
+
+/* bookkeeping for profiles */
+int b2gDev_Synchronize( b2gDeviceWorld* dw );
+void b2gDev_Timings( b2gDeviceWorld* dw, float* pairsMs, float* collideMs, float* solveMs );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,1508 @@
+/*
+ * GB300 (sm_103a) kernels of the Box2D v3.2 step and the thin C ABI the C17 host calls
+ * (b2g_device_abi.h). One CUDA stream per world; all buffers are device-resident and grow
+ * by doubling. Kernels:
+ *   k_markMoved / k_findPairs / k_clearMoved  broadphase pair query (broad_phase.c:172-399)
+ *   k_initContacts / k_killContacts           contact slot lifecycle
+ *   k_collide                                 narrowphase + recycling (physics_world.c:451-609)
+ *   k_prepareContacts / k_prepareJoints       constraint preparation
+ *   k_integrateVelocities / k_integratePositions (solver.c:66-162)
+ *   k_colorStage                              warm start / solve / relax / restitution per color
+ *   k_overflowStage                           ordered scalar pass over the overflow color
+ *   k_storeImpulses                           (contact_solver.c:2238-2331)
+ *   k_finalizeBodies                          transforms, sleep metric, fat AABBs (solver.c:553-743)
+ * Bit-exact mode: compiled with --fmad=false, IEEE division/sqrt, no flush-to-zero.
+ */
+#include "joints.cuh"
+#include "manifold.cuh"
+#include "solver.cuh"
+
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define B2G_THREADS 128
+#define B2G_PAIR_STACK 256
+
+struct b2gDeviceWorld
+{
+	cudaStream_t stream;
+	cudaEvent_t ev[8];
+	float pairsMs, collideMs, solveMs;
+	/* bodies by id */
+	int bodyCap, bodyCount;
+	float4* xf;
+	float2* center;
+	float2* localCenter;
+	float* invMass;
+	float* invI;
+	float* minExtent;
+	float* maxExtent;
+	float* sleepThreshold;
+	float* safetyFactor;
+	int* awakeIndex;
+	int* bodyType;
+	uint32_t* bodyFlags;
+	int* shapeStart;
+	int* shapeCount;
+	int* shapeList;
+	int shapeListCap;
+	/* awake bodies */
+	int awakeCap, awakeCount;
+	int* awakeBodyId;
+	float4* stateV;
+	float4* stateD;
+	float* params; /* 8 per body: force.x, force.y, torque, linDamp, angDamp, gravityScale, invMass, invI */
+	float4* center0; /* center0.x, center0.y, rotation0.c, rotation0.s */
+	int* enlargedBody;
+	/* shapes */
+	int shapeCap, shapeCountTotal;
+	b2gShape* shapes;
+	float4* aabb;
+	float4* fat;
+	int* shapeEnlarged;
+	/* contacts */
+	int contactCap;
+	b2gContact* contacts;
+	int* colorIds;
+	int colorIdsCap;
+	int colorOffsets[B2_GRAPH_COLOR_COUNT + 1];
+	b2gContactLane* lanes;
+	int laneCap;
+	/* joints in color order */
+	b2gJoint* joints;
+	int jointCap, jointCount;
+	int jointOffsets[B2_GRAPH_COLOR_COUNT + 1];
+	/* broadphase */
+	b2gTreeNode* tree[3];
+	int treeCap[3], treeRoot[3];
+	unsigned char* moved[3];
+	int movedCap[3];
+	int* moveKeys;
+	float4* moveBoxes;
+	int* moveShapes;
+	int moveCap;
+	int* pairBuf;
+	int* pairCounts;
+	int pairPerMove;
+	int pairBufCap;
+	/* outputs */
+	int* changes;
+	int changeCap;
+	int* enlargedRecs;
+	float4* enlargedBoxes;
+	int enlargedCap, enlargedBoxesCap;
+	b2gStepCounters* counters;
+	/* pinned host staging */
+	b2gStepCounters* hCounters;
+	int* hChanges;
+	int hChangesCap;
+	int* hRecs;
+	float* hBoxes;
+	int hRecsCap, hBoxesCap;
+	int* hPairs;
+	int* hPairCounts;
+	int hPairsCap, hPairCountsCap;
+	int* hSortTmp;
+	int hSortTmpCap;
+};
+
+#define CK( x )                                                                                                                \
+	do                                                                                                                           \
+	{                                                                                                                            \
+		cudaError_t e_ = ( x );                                                                                                  \
+		if ( e_ != cudaSuccess ) return (int)e_;                                                                                 \
+	} while ( 0 )
+
+static int grow( void** ptr, int* cap, int need, size_t elem )
+{
+	if ( need <= *cap && *ptr != NULL ) return 0;
+	int nc = *cap > 0 ? *cap : 64;
+	while ( nc < need ) nc *= 2;
+	void* p = NULL;
+	CK( cudaMalloc( &p, (size_t)nc * elem ) );
+	CK( cudaMemset( p, 0, (size_t)nc * elem ) );
+	if ( *ptr != NULL )
+	{
+		if ( *cap > 0 ) CK( cudaMemcpy( p, *ptr, (size_t)( *cap ) * elem, cudaMemcpyDeviceToDevice ) );
+		CK( cudaFree( *ptr ) );
+	}
+	*ptr = p;
+	*cap = nc;
+	return 0;
+}
+
+static int growHost( void** ptr, int* cap, int need, size_t elem )
+{
+	if ( need <= *cap && *ptr != NULL ) return 0;
+	int nc = *cap > 0 ? *cap : 64;
+	while ( nc < need ) nc *= 2;
+	void* p = NULL;
+	CK( cudaMallocHost( &p, (size_t)nc * elem ) );
+	if ( *ptr != NULL ) CK( cudaFreeHost( *ptr ) );
+	*ptr = p;
+	*cap = nc;
+	return 0;
+}
+
+static inline int blocks( int n ) { return ( n + B2G_THREADS - 1 ) / B2G_THREADS; }
+
+/* ======================= broadphase pair query ======================= */
+__global__ void k_markMoved( unsigned char* movedDyn, unsigned char* movedKin, unsigned char* movedStat, const int* keys, int n,
+							 unsigned char value )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	int key = keys[i];
+	int type = key & 3, id = key >> 2;
+	unsigned char* m = type == b2_dynamicBody ? movedDyn : ( type == b2_kinematicBody ? movedKin : movedStat );
+	m[id] = value;
+}
+
+static __device__ __forceinline__ bool d_overlaps( b2AABB a, float4 b )
+{
+	return !( b.x > a.upperBound.x || b.y > a.upperBound.y || a.lowerBound.x > b.z || a.lowerBound.y > b.w );
+}
+
+/* one thread per moved proxy; stack DFS with child1 pushed before child2, as
+   b2DynamicTree_Query (dynamic_tree.c:1085-1135); dedupe as b2PairQueryCallback
+   (broad_phase.c:172-219). Hits are written in visit order. */
+__global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat, const b2gTreeNode* __restrict__ tKin, int rootKin,
+							 const b2gTreeNode* __restrict__ tDyn, int rootDyn, const unsigned char* __restrict__ movedDyn,
+							 const int* __restrict__ keys, const float4* __restrict__ boxes, const int* __restrict__ queryShapes,
+							 int n, int* __restrict__ pairs, int* __restrict__ counts, int capPerMove,
+							 b2gStepCounters* counters )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	int queryKey = keys[i];
+	int queryType = queryKey & 3;
+	float4 box = boxes[i];
+	int queryShape = queryShapes[i];
+	int count = 0;
+	int stack[B2G_PAIR_STACK];
+	for ( int pass = 0; pass < 3; ++pass )
+	{
+		int treeType;
+		const b2gTreeNode* nodes;
+		int root;
+		if ( pass == 0 )
+		{
+			if ( queryType != b2_dynamicBody ) continue;
+			treeType = b2_kinematicBody;
+			nodes = tKin;
+			root = rootKin;
+		}
+		else if ( pass == 1 )
+		{
+			if ( queryType != b2_dynamicBody ) continue;
+			treeType = b2_staticBody;
+			nodes = tStat;
+			root = rootStat;
+		}
+		else
+		{
+			treeType = b2_dynamicBody;
+			nodes = tDyn;
+			root = rootDyn;
+		}
+		if ( root < 0 ) continue;
+		int sp = 0;
+		stack[sp++] = root;
+		while ( sp > 0 )
+		{
+			int nodeId = stack[--sp];
+			const b2gTreeNode node = nodes[nodeId];
+			if ( d_overlaps( node.aabb, box ) == false || node.categoryNonZero == 0 ) continue;
+			if ( node.isLeaf )
+			{
+				int proxyKey = ( nodeId << 2 ) | treeType;
+				if ( proxyKey == queryKey ) continue;
+				if ( queryType == b2_dynamicBody )
+				{
+					if ( treeType == b2_dynamicBody && proxyKey < queryKey && movedDyn[nodeId] ) continue;
+				}
+				else
+				{
+					if ( movedDyn[nodeId] ) continue;
+				}
+				int shapeId = node.child1;
+				int a = proxyKey < queryKey ? shapeId : queryShape;
+				int b = proxyKey < queryKey ? queryShape : shapeId;
+				if ( count < capPerMove )
+				{
+					pairs[2 * ( (size_t)i * capPerMove + count )] = a;
+					pairs[2 * ( (size_t)i * capPerMove + count ) + 1] = b;
+				}
+				count += 1;
+			}
+			else
+			{
+				if ( sp + 2 > B2G_PAIR_STACK )
+				{
+					atomicOr( &counters->status, B2G_STATUS_CAPACITY );
+					break;
+				}
+				stack[sp++] = node.child1;
+				stack[sp++] = node.child2;
+			}
+		}
+	}
+	counts[i] = count;
+	if ( count > capPerMove ) atomicMax( &counters->pairOverflow, count );
+}
+
+/* ======================= contacts ======================= */
+__global__ void k_initContacts( b2gContact* contacts, const b2gContactInit* inits, int n )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	b2gContactInit in = inits[i];
+	b2gContact c;
+	memset( &c, 0, sizeof( c ) );
+	c.shapeIdA = in.shapeIdA;
+	c.shapeIdB = in.shapeIdB;
+	c.simFlags = in.simFlags | B2G_S_LIVE;
+	c.bodySimIndexA = -1;
+	c.bodySimIndexB = -1;
+	c.friction = in.friction;
+	c.restitution = in.restitution;
+	contacts[in.contactId] = c;
+}
+
+__global__ void k_killContacts( b2gContact* contacts, const int* ids, int n )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	contacts[ids[i]].simFlags = 0;
+}
+
+struct d_collideArgs
+{
+	b2gContact* contacts;
+	int capacity;
+	const b2gShape* shapes;
+	const float4* fat;
+	const float4* xf;
+	const float2* center;
+	const float2* localCenter;
+	const float* invMass;
+	const float* invI;
+	const float* maxExtent;
+	const int* awakeIndex;
+	const int* bodyType;
+	const uint32_t* bodyFlags;
+	int* changes;
+	b2gStepCounters* counters;
+	float recycleDistance;
+};
+
+/* physics_world.c:451-609 and contact.c:519-698, one thread per contact slot */
+__global__ void k_collide( d_collideArgs a )
+{
+	int contactId = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( contactId >= a.capacity ) return;
+	b2gContact* cs = a.contacts + contactId;
+	uint32_t simFlags = cs->simFlags;
+	if ( ( simFlags & B2G_S_LIVE ) == 0 ) return;
+	float recycleDistance = a.recycleDistance;
+	float recycleNonTouching = d_min( recycleDistance, D_SPECULATIVE_DISTANCE );
+	int shapeIdA = cs->shapeIdA, shapeIdB = cs->shapeIdB;
+	const b2gShape* shapeA = a.shapes + shapeIdA;
+	const b2gShape* shapeB = a.shapes + shapeIdB;
+	float4 fa = a.fat[shapeIdA], fb = a.fat[shapeIdB];
+	bool overlap = !( fb.x > fa.z || fb.y > fa.w || fa.x > fb.z || fa.y > fb.w );
+	if ( overlap == false )
+	{
+		simFlags |= B2G_S_DISJOINT;
+		simFlags &= ~B2G_S_TOUCHING;
+		cs->simFlags = simFlags;
+		int slot = atomicAdd( &a.counters->stateChangeCount, 1 );
+		a.changes[2 * slot] = contactId;
+		a.changes[2 * slot + 1] = (int)simFlags;
+		return;
+	}
+	bool wasTouching = ( simFlags & B2G_S_TOUCHING ) != 0;
+	int bodyIdA = shapeA->bodyId, bodyIdB = shapeB->bodyId;
+	float4 xa = a.xf[bodyIdA], xb = a.xf[bodyIdB];
+	b2Transform xfA = { { xa.x, xa.y }, { xa.z, xa.w } };
+	b2Transform xfB = { { xb.x, xb.y }, { xb.z, xb.w } };
+	cs->bodySimIndexA = a.awakeIndex[bodyIdA];
+	cs->invMassA = a.invMass[bodyIdA];
+	cs->invIA = a.invI[bodyIdA];
+	cs->bodySimIndexB = a.awakeIndex[bodyIdB];
+	cs->invMassB = a.invMass[bodyIdB];
+	cs->invIB = a.invI[bodyIdB];
+	bool isFast = ( a.bodyFlags[bodyIdA] & B2G_IS_FAST ) || ( a.bodyFlags[bodyIdB] & B2G_IS_FAST );
+	if ( isFast == false && recycleDistance > 0.0f && ( simFlags & B2G_S_RELATIVE_VALID ) && ( simFlags & B2G_C_RECYCLE ) )
+	{
+		b2Rot cachedQA = cs->cachedRotationA, cachedQB = cs->cachedRotationB;
+		b2Transform xfc = cs->cachedRelativePose;
+		b2Transform xf = d_invMulTransforms( xfA, xfB );
+		float cosA = d_relativeCos( xfA.q, cachedQA );
+		float cosB = d_relativeCos( xfB.q, cachedQB );
+		float minCos = d_min( cosA, cosB );
+		float maxExtentA = a.bodyType[bodyIdA] == b2_staticBody ? 0.0f : a.maxExtent[bodyIdA];
+		float maxExtentB = a.bodyType[bodyIdB] == b2_staticBody ? 0.0f : a.maxExtent[bodyIdB];
+		float maxExtent = d_max( maxExtentA, maxExtentB );
+		float distance = d_distance( xf.p, xfc.p );
+		b2Rot qr = d_invMulRot( xf.q, xfc.q );
+		float tolerance = wasTouching ? recycleDistance : recycleNonTouching;
+		if ( minCos > D_CONTACT_RECYCLE_COS_ANGLE && distance + maxExtent * d_abs( qr.s ) < tolerance )
+		{
+			b2Rot dqA = d_mulRot( xfA.q, d_invertRot( cachedQA ) );
+			b2Rot dqB = d_mulRot( xfB.q, d_invertRot( cachedQB ) );
+			b2Vec2 normal = cs->manifold.normal;
+			float2 cA = a.center[bodyIdA], cB = a.center[bodyIdB];
+			b2Vec2 dc = { cB.x - cA.x, cB.y - cA.y };
+			for ( int i = 0; i < cs->manifold.pointCount; ++i )
+			{
+				b2ManifoldPoint* mp = cs->manifold.points + i;
+				b2Vec2 rA = d_rotate( dqA, mp->anchorA );
+				b2Vec2 rB = d_rotate( dqB, mp->anchorB );
+				b2Vec2 dp = d_add( dc, d_sub( rB, rA ) );
+				mp->separation = mp->baseSeparation + d_dot( dp, normal );
+				mp->persisted = true;
+			}
+			atomicAdd( &a.counters->recycledContactCount, 1 );
+			return;
+		}
+	}
+	cs->cachedRotationA = xfA.q;
+	cs->cachedRotationB = xfB.q;
+	cs->cachedRelativePose = d_invMulTransforms( xfA, xfB );
+	simFlags |= B2G_S_RELATIVE_VALID;
+	float2 lcA = a.localCenter[bodyIdA], lcB = a.localCenter[bodyIdB];
+	b2Vec2 centerOffsetA = d_rotate( xfA.q, d_v( lcA.x, lcA.y ) );
+	b2Vec2 centerOffsetB = d_rotate( xfB.q, d_v( lcB.x, lcB.y ) );
+
+	/* b2UpdateContact */
+	b2Manifold oldManifold = cs->manifold;
+	b2Transform rel = d_invMulTransforms( xfA, xfB );
+	b2LocalManifold local = d_collideShapes( shapeA, shapeB, rel );
+	b2Manifold m;
+	memset( &m, 0, sizeof( m ) );
+	m.normal = d_rotate( xfA.q, local.normal );
+	m.pointCount = local.pointCount;
+	b2Vec2 originDelta = { xfA.p.x - xfB.p.x, xfA.p.y - xfB.p.y };
+	for ( int i = 0; i < local.pointCount; ++i )
+	{
+		b2ManifoldPoint* mp = m.points + i;
+		mp->anchorA = d_rotate( xfA.q, local.points[i].point );
+		mp->anchorB = d_add( mp->anchorA, originDelta );
+		mp->separation = local.points[i].separation;
+		mp->id = local.points[i].id;
+	}
+	cs->friction = sqrtf( shapeA->friction * shapeB->friction );
+	cs->restitution = d_max( shapeA->restitution, shapeB->restitution );
+	if ( shapeA->rollingResistance > 0.0f || shapeB->rollingResistance > 0.0f )
+	{
+		float rA = shapeA->type == b2_segmentShape ? 0.0f : shapeA->radius;
+		float rB = shapeB->type == b2_segmentShape ? 0.0f : shapeB->radius;
+		float maxRadius = d_max( rA, rB );
+		cs->rollingResistance = d_max( shapeA->rollingResistance, shapeB->rollingResistance ) * maxRadius;
+	}
+	else
+	{
+		cs->rollingResistance = 0.0f;
+	}
+	cs->tangentSpeed = shapeA->tangentSpeed + shapeB->tangentSpeed;
+	int pointCount = m.pointCount;
+	bool touching = pointCount > 0;
+	if ( touching && ( shapeA->enableHitEvents || shapeB->enableHitEvents ) ) simFlags |= B2G_S_HIT_EVENT;
+	else simFlags &= ~B2G_S_HIT_EVENT;
+	if ( pointCount > 0 ) m.rollingImpulse = oldManifold.rollingImpulse;
+	for ( int i = 0; i < pointCount; ++i )
+	{
+		b2ManifoldPoint* mp2 = m.points + i;
+		mp2->anchorA = d_sub( mp2->anchorA, centerOffsetA );
+		mp2->anchorB = d_sub( mp2->anchorB, centerOffsetB );
+		mp2->normalImpulse = 0.0f;
+		mp2->tangentImpulse = 0.0f;
+		mp2->totalNormalImpulse = 0.0f;
+		mp2->normalVelocity = 0.0f;
+		mp2->persisted = false;
+		uint16_t id2 = mp2->id;
+		for ( int j = 0; j < oldManifold.pointCount; ++j )
+		{
+			b2ManifoldPoint* mp1 = oldManifold.points + j;
+			if ( mp1->id == id2 )
+			{
+				mp2->normalImpulse = mp1->normalImpulse;
+				mp2->tangentImpulse = mp1->tangentImpulse;
+				mp2->persisted = true;
+				mp1->normalImpulse = 0.0f;
+				mp1->tangentImpulse = 0.0f;
+				break;
+			}
+		}
+	}
+	if ( touching ) simFlags |= B2G_S_TOUCHING;
+	else simFlags &= ~B2G_S_TOUCHING;
+	for ( int i = 0; i < m.pointCount; ++i ) m.points[i].baseSeparation = m.points[i].separation;
+	cs->manifold = m;
+	bool changed = false;
+	if ( touching && wasTouching == false )
+	{
+		simFlags |= B2G_S_STARTED;
+		changed = true;
+	}
+	else if ( touching == false && wasTouching )
+	{
+		simFlags |= B2G_S_STOPPED;
+		changed = true;
+	}
+	if ( changed )
+	{
+		/* the host's state pass clears the started / stopped bits */
+		int slot = atomicAdd( &a.counters->stateChangeCount, 1 );
+		a.changes[2 * slot] = contactId;
+		a.changes[2 * slot + 1] = (int)simFlags;
+		simFlags &= ~( B2G_S_STARTED | B2G_S_STOPPED );
+	}
+	cs->simFlags = simFlags;
+}
+
+/* ======================= solver ======================= */
+struct d_solveArgs
+{
+	b2gContact* contacts;
+	const int* colorIds;
+	b2gContactLane* lanes;
+	b2gJoint* joints;
+	float4* sv;
+	float4* sd;
+	const float* params;
+	int awakeCount;
+	b2gStepParams p;
+};
+
+/* contact_solver.c:1573-1809 (graph colors) and :20-160 (overflow), one thread per slot */
+__global__ void k_prepareContacts( d_solveArgs a, int begin, int end, int overflowBegin )
+{
+	int slot = begin + blockIdx.x * blockDim.x + threadIdx.x;
+	if ( slot >= end ) return;
+	int contactId = a.colorIds[slot];
+	const b2gContact* cs = a.contacts + contactId;
+	const b2Manifold* m = &cs->manifold;
+	b2gContactLane c;
+	float warmStartScale = a.p.enableWarmStarting ? 1.0f : 0.0f;
+	int indexA = cs->bodySimIndexA, indexB = cs->bodySimIndexB;
+	c.indexA = indexA + 1;
+	c.indexB = indexB + 1;
+	b2Vec2 vA = { 0.0f, 0.0f }, vB = { 0.0f, 0.0f };
+	float wA = 0.0f, wB = 0.0f;
+	float mA = cs->invMassA, iA = cs->invIA, mB = cs->invMassB, iB = cs->invIB;
+	if ( indexA != -1 )
+	{
+		float4 v = a.sv[indexA];
+		vA = d_v( v.x, v.y );
+		wA = v.z;
+	}
+	if ( indexB != -1 )
+	{
+		float4 v = a.sv[indexB];
+		vB = d_v( v.x, v.y );
+		wB = v.z;
+	}
+	c.invMassA = mA;
+	c.invMassB = mB;
+	c.invIA = iA;
+	c.invIB = iB;
+	{
+		float k = iA + iB;
+		c.rollingMass = k > 0.0f ? 1.0f / k : 0.0f;
+	}
+	bool isOverflow = slot >= overflowBegin;
+	float biasRate = a.p.contactBiasRate, massScale = a.p.contactMassScale, impulseScale = a.p.contactImpulseScale;
+	if ( indexA == -1 || indexB == -1 )
+	{
+		biasRate = a.p.staticBiasRate;
+		massScale = a.p.staticMassScale;
+		impulseScale = a.p.staticImpulseScale;
+	}
+	else if ( a.p.enableContactSoftening && isOverflow == false )
+	{
+		float contactHertz = d_min( a.p.contactHertz, 0.125f * a.p.inv_h );
+		float ratio = 1.0f;
+		if ( mA < mB ) ratio = d_max( 0.5f, mA / mB );
+		else if ( mB < mA ) ratio = d_max( 0.5f, mB / mA );
+		d_makeSoftInto( ratio * contactHertz, ratio * a.p.contactDampingRatio, a.p.h, &biasRate, &massScale, &impulseScale );
+	}
+	b2Vec2 normal = m->normal;
+	c.normal = normal;
+	c.friction = cs->friction;
+	c.tangentSpeed = cs->tangentSpeed;
+	c.restitution = cs->restitution;
+	c.rollingResistance = cs->rollingResistance;
+	c.rollingImpulse = warmStartScale * m->rollingImpulse;
+	c.biasRate = biasRate;
+	c.massScale = massScale;
+	c.impulseScale = impulseScale;
+	c.pointCount = m->pointCount;
+	b2Vec2 tangent = d_rightPerp( normal );
+	{
+		const b2ManifoldPoint* mp = m->points + 0;
+		b2Vec2 rA = mp->anchorA, rB = mp->anchorB;
+		c.anchorA1 = rA;
+		c.anchorB1 = rB;
+		c.baseSeparation1 = mp->separation - d_dot( d_sub( rB, rA ), normal );
+		c.normalImpulse1 = warmStartScale * mp->normalImpulse;
+		c.tangentImpulse1 = warmStartScale * mp->tangentImpulse;
+		c.totalNormalImpulse1 = 0.0f;
+		float rnA = d_cross( rA, normal ), rnB = d_cross( rB, normal );
+		float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+		c.normalMass1 = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+		float rtA = d_cross( rA, tangent ), rtB = d_cross( rB, tangent );
+		float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+		c.tangentMass1 = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+		b2Vec2 vrA = d_add( vA, d_crossSV( wA, rA ) );
+		b2Vec2 vrB = d_add( vB, d_crossSV( wB, rB ) );
+		c.relativeVelocity1 = d_dot( normal, d_sub( vrB, vrA ) );
+	}
+	if ( m->pointCount == 2 )
+	{
+		const b2ManifoldPoint* mp = m->points + 1;
+		b2Vec2 rA = mp->anchorA, rB = mp->anchorB;
+		c.anchorA2 = rA;
+		c.anchorB2 = rB;
+		c.baseSeparation2 = mp->separation - d_dot( d_sub( rB, rA ), normal );
+		c.normalImpulse2 = warmStartScale * mp->normalImpulse;
+		c.tangentImpulse2 = warmStartScale * mp->tangentImpulse;
+		c.totalNormalImpulse2 = 0.0f;
+		float rnA = d_cross( rA, normal ), rnB = d_cross( rB, normal );
+		float kNormal = mA + mB + iA * rnA * rnA + iB * rnB * rnB;
+		c.normalMass2 = kNormal > 0.0f ? 1.0f / kNormal : 0.0f;
+		float rtA = d_cross( rA, tangent ), rtB = d_cross( rB, tangent );
+		float kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
+		c.tangentMass2 = kTangent > 0.0f ? 1.0f / kTangent : 0.0f;
+		b2Vec2 vrA = d_add( vA, d_crossSV( wA, rA ) );
+		b2Vec2 vrB = d_add( vB, d_crossSV( wB, rB ) );
+		c.relativeVelocity2 = d_dot( normal, d_sub( vrB, vrA ) );
+	}
+	else
+	{
+		c.baseSeparation2 = 0.0f;
+		c.normalImpulse2 = 0.0f;
+		c.tangentImpulse2 = 0.0f;
+		c.totalNormalImpulse2 = 0.0f;
+		c.anchorA2 = d_v( 0.0f, 0.0f );
+		c.anchorB2 = d_v( 0.0f, 0.0f );
+		c.normalMass2 = 0.0f;
+		c.tangentMass2 = 0.0f;
+		c.relativeVelocity2 = 0.0f;
+	}
+	c.groupFlags = 0;
+	a.lanes[slot] = c;
+}
+
+/* per 4-wide group of a color: does any lane have rolling resistance / restitution */
+__global__ void k_groupFlags( d_solveArgs a, int colorBegin, int colorCount )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= colorCount ) return;
+	int g0 = ( i / 4 ) * 4;
+	int flags = 0;
+	for ( int k = g0; k < g0 + 4 && k < colorCount; ++k )
+	{
+		const b2gContactLane* l = a.lanes + colorBegin + k;
+		flags |= l->rollingResistance != 0.0f ? 1 : 0;
+		flags |= l->restitution != 0.0f ? 2 : 0;
+	}
+	a.lanes[colorBegin + i].groupFlags = flags;
+}
+
+__global__ void k_prepareJoints( d_solveArgs a, d_jointBodies bodies, int count )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= count ) return;
+	d_prepareJoint( a.joints + i, &bodies, a.p.h, a.p.inv_h, a.p.enableWarmStarting != 0 );
+}
+
+/* solver.c:66-112 */
+__global__ void k_integrateVelocities( d_solveArgs a )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= a.awakeCount ) return;
+	float h = a.p.h;
+	const float* pr = a.params + 8 * i;
+	float4 s = a.sv[i];
+	b2Vec2 v = { s.x, s.y };
+	float w = s.z;
+	float linearDamping = 1.0f / ( 1.0f + h * pr[3] );
+	float angularDamping = 1.0f / ( 1.0f + h * pr[4] );
+	float invMass = pr[6];
+	float gravityScale = invMass > 0.0f ? pr[5] : 0.0f;
+	b2Vec2 force = { pr[0], pr[1] };
+	b2Vec2 gravity = { a.p.gravityX, a.p.gravityY };
+	b2Vec2 lvd = d_add( d_mulSV( h * invMass, force ), d_mulSV( h * gravityScale, gravity ) );
+	float avd = h * pr[7] * pr[2];
+	v = d_mulAdd( lvd, linearDamping, v );
+	w = avd + angularDamping * w;
+	a.sv[i] = make_float4( v.x, v.y, w, s.w );
+}
+
+/* solver.c:114-162 */
+__global__ void k_integratePositions( d_solveArgs a )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= a.awakeCount ) return;
+	float h = a.p.h;
+	float maxLinearSpeed = a.p.maxLinearVelocity;
+	float maxAngularSpeed = D_MAX_ROTATION * a.p.inv_dt;
+	float maxLinearSq = maxLinearSpeed * maxLinearSpeed;
+	float maxAngularSq = maxAngularSpeed * maxAngularSpeed;
+	float4 s = a.sv[i];
+	float4 d = a.sd[i];
+	uint32_t flags = __float_as_uint( s.w );
+	b2Vec2 v = { s.x, s.y };
+	float w = s.z;
+	v.x = ( flags & B2G_LOCK_X ) ? 0.0f : v.x;
+	v.y = ( flags & B2G_LOCK_Y ) ? 0.0f : v.y;
+	w = ( flags & B2G_LOCK_Z ) ? 0.0f : w;
+	if ( d_dot( v, v ) > maxLinearSq )
+	{
+		float ratio = maxLinearSpeed / d_length( v );
+		v = d_mulSV( ratio, v );
+		flags |= B2G_SPEED_CAPPED;
+	}
+	if ( w * w > maxAngularSq && ( flags & B2G_ALLOW_FAST_ROTATION ) == 0 )
+	{
+		float ratio = maxAngularSpeed / d_abs( w );
+		w *= ratio;
+		flags |= B2G_SPEED_CAPPED;
+	}
+	b2Vec2 dp = d_mulAdd( d_v( d.x, d.y ), h, v );
+	b2Rot dq = d_integrateRotation( b2Rot{ d.z, d.w }, h * w );
+	a.sv[i] = make_float4( v.x, v.y, w, __uint_as_float( flags ) );
+	a.sd[i] = make_float4( dp.x, dp.y, dq.c, dq.s );
+}
+
+enum
+{
+	STAGE_WARM = 0,
+	STAGE_SOLVE = 1,
+	STAGE_RELAX = 2,
+	STAGE_RESTITUTION = 3,
+};
+
+/* one graph color: threads [0, jointCount) run joints, the rest run contact lanes */
+__global__ void k_colorStage( d_solveArgs a, int jointBegin, int jointCount, int laneBegin, int laneCount, int stage )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i < jointCount )
+	{
+		b2gJoint* j = a.joints + jointBegin + i;
+		if ( stage == STAGE_WARM ) d_warmStartJoint( j, a.sv, a.sd );
+		else if ( stage == STAGE_SOLVE ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, true );
+		else if ( stage == STAGE_RELAX ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, false );
+		return;
+	}
+	i -= jointCount;
+	if ( i >= laneCount ) return;
+	b2gContactLane* c = a.lanes + laneBegin + i;
+	if ( stage == STAGE_WARM ) d_warmStartLane( c, a.sv, a.sd );
+	else if ( stage == STAGE_SOLVE ) d_solveLane( c, a.sv, a.sd, a.p.inv_h, -a.p.contactSpeed, true );
+	else if ( stage == STAGE_RELAX ) d_solveLane( c, a.sv, a.sd, a.p.inv_h, -a.p.contactSpeed, false );
+	else d_restitutionLane( c, a.sv, a.sd, a.p.restitutionThreshold );
+}
+
+/* overflow color: one thread walks joints then contacts in array order (joint.c:1542-1591,
+   contact_solver.c:20-545) */
+__global__ void k_overflowStage( d_solveArgs a, int jointBegin, int jointCount, int laneBegin, int laneCount, int stage )
+{
+	if ( blockIdx.x != 0 || threadIdx.x != 0 ) return;
+	for ( int i = 0; i < jointCount; ++i )
+	{
+		b2gJoint* j = a.joints + jointBegin + i;
+		if ( stage == STAGE_WARM ) d_warmStartJoint( j, a.sv, a.sd );
+		else if ( stage == STAGE_SOLVE ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, true );
+		else if ( stage == STAGE_RELAX ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, false );
+	}
+	for ( int i = 0; i < laneCount; ++i )
+	{
+		b2gContactLane* c = a.lanes + laneBegin + i;
+		if ( stage == STAGE_WARM ) d_warmStartOverflow( c, a.sv, a.sd );
+		else if ( stage == STAGE_SOLVE ) d_solveOverflow( c, a.sv, a.sd, a.p.inv_h, a.p.contactSpeed, true );
+		else if ( stage == STAGE_RELAX ) d_solveOverflow( c, a.sv, a.sd, a.p.inv_h, a.p.contactSpeed, false );
+		else d_restitutionOverflow( c, a.sv, a.sd, a.p.restitutionThreshold );
+	}
+}
+
+/* contact_solver.c:2238-2331 (colors) and :516-545 (overflow) */
+__global__ void k_storeImpulses( d_solveArgs a, int begin, int end, int overflowBegin )
+{
+	int slot = begin + blockIdx.x * blockDim.x + threadIdx.x;
+	if ( slot >= end ) return;
+	const b2gContactLane* c = a.lanes + slot;
+	b2Manifold* m = &a.contacts[a.colorIds[slot]].manifold;
+	if ( slot >= overflowBegin )
+	{
+		for ( int j = 0; j < m->pointCount; ++j )
+		{
+			m->points[j].normalImpulse = j == 0 ? c->normalImpulse1 : c->normalImpulse2;
+			m->points[j].tangentImpulse = j == 0 ? c->tangentImpulse1 : c->tangentImpulse2;
+			m->points[j].totalNormalImpulse = j == 0 ? c->totalNormalImpulse1 : c->totalNormalImpulse2;
+			m->points[j].normalVelocity = j == 0 ? c->relativeVelocity1 : c->relativeVelocity2;
+		}
+		m->rollingImpulse = c->rollingImpulse;
+		return;
+	}
+	m->rollingImpulse = c->rollingImpulse;
+	m->points[0].normalImpulse = c->normalImpulse1;
+	m->points[0].tangentImpulse = c->tangentImpulse1;
+	m->points[0].totalNormalImpulse = c->totalNormalImpulse1;
+	m->points[0].normalVelocity = c->relativeVelocity1;
+	m->points[1].normalImpulse = c->normalImpulse2;
+	m->points[1].tangentImpulse = c->tangentImpulse2;
+	m->points[1].totalNormalImpulse = c->totalNormalImpulse2;
+	m->points[1].normalVelocity = c->relativeVelocity2;
+}
+
+/* geometry.c:400-506 fat AABB (built in double, narrowed once) */
+static __device__ float4 d_fatBox( double lx, double ly, double ux, double uy, double r )
+{
+	return make_float4( (float)__dsub_rn( lx, r ), (float)__dsub_rn( ly, r ), (float)__dadd_rn( ux, r ), (float)__dadd_rn( uy, r ) );
+}
+
+static __device__ float4 d_computeFatShapeAABB( const b2gShape* s, b2Transform xf, float extra )
+{
+	switch ( s->type )
+	{
+		case b2_circleShape:
+		{
+			b2Vec2 c = d_transformWorldPoint( xf, s->v[0] );
+			double r = __dadd_rn( (double)s->radius, (double)extra );
+			return d_fatBox( c.x, c.y, c.x, c.y, r );
+		}
+		case b2_capsuleShape:
+		case b2_segmentShape:
+		{
+			b2Vec2 v1 = d_transformWorldPoint( xf, s->v[0] );
+			b2Vec2 v2 = d_transformWorldPoint( xf, s->v[1] );
+			double r = s->type == b2_capsuleShape ? __dadd_rn( (double)s->radius, (double)extra ) : (double)extra;
+			return d_fatBox( v1.x < v2.x ? v1.x : v2.x, v1.y < v2.y ? v1.y : v2.y, v1.x > v2.x ? v1.x : v2.x,
+							 v1.y > v2.y ? v1.y : v2.y, r );
+		}
+		case b2_polygonShape:
+		{
+			b2Vec2 v = d_transformWorldPoint( xf, s->v[0] );
+			double lx = v.x, ly = v.y, ux = v.x, uy = v.y;
+			for ( int i = 1; i < s->count; ++i )
+			{
+				v = d_transformWorldPoint( xf, s->v[i] );
+				lx = v.x < lx ? v.x : lx;
+				ly = v.y < ly ? v.y : ly;
+				ux = v.x > ux ? v.x : ux;
+				uy = v.y > uy ? v.y : uy;
+			}
+			double r = __dadd_rn( (double)s->radius, (double)extra );
+			return d_fatBox( lx, ly, ux, uy, r );
+		}
+		default:
+			return make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+	}
+}
+
+struct d_finalizeArgs
+{
+	float4* sv;
+	float4* sd;
+	float* params;
+	float4* center0;
+	const int* awakeBodyId;
+	int awakeCount;
+	float4* xf;
+	float2* center;
+	const float2* localCenter;
+	const float* minExtent;
+	const float* maxExtent;
+	const float* sleepThreshold;
+	const float* safetyFactor;
+	const int* bodyType;
+	uint32_t* bodyFlags;
+	const int* shapeStart;
+	const int* shapeCount;
+	const int* shapeList;
+	const b2gShape* shapes;
+	float4* aabb;
+	float4* fat;
+	int* shapeEnlarged;
+	int* enlargedRecs;
+	float4* enlargedBoxes;
+	int enlargedCap;
+	b2gStepCounters* counters;
+	float dt, inv_dt;
+	int enableSleep, enableContinuous;
+};
+
+/* solver.c:553-743, one thread per awake body. A body with an enlarged shape (or a fast
+   bullet) appends one record per shape, as one contiguous group:
+   (awake index, shape id, enlarged, fast bullet) + fat box. */
+__global__ void k_finalizeBodies( d_finalizeArgs a )
+{
+	int simIndex = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( simIndex >= a.awakeCount ) return;
+	int bodyId = a.awakeBodyId[simIndex];
+	float4 s = a.sv[simIndex];
+	float4 d = a.sd[simIndex];
+	b2Vec2 v = { s.x, s.y };
+	float w = s.z;
+	uint32_t stateFlags = __float_as_uint( s.w );
+	if ( isfinite( v.x ) == false || isfinite( v.y ) == false || isfinite( w ) == false )
+		atomicOr( &a.counters->status, B2G_STATUS_NAN );
+	float2 c2 = a.center[bodyId];
+	float4 x4 = a.xf[bodyId];
+	b2Vec2 center = { c2.x + d.x, c2.y + d.y };
+	b2Rot q = d_normalizeRot( d_mulRot( b2Rot{ d.z, d.w }, b2Rot{ x4.z, x4.w } ) );
+	float maxExtent = a.maxExtent[bodyId];
+	float maxVelocity = d_length( v ) + d_abs( w ) * maxExtent;
+	float maxDeltaPosition = d_length( d_v( d.x, d.y ) ) + d_abs( d.w ) * maxExtent;
+	float positionSleepFactor = 0.5f;
+	float sleepVelocity = d_max( maxVelocity, positionSleepFactor * a.inv_dt * maxDeltaPosition );
+	float2 lc = a.localCenter[bodyId];
+	b2Vec2 p = d_add( center, d_neg( d_rotate( q, d_v( lc.x, lc.y ) ) ) );
+	a.xf[bodyId] = make_float4( p.x, p.y, q.c, q.s );
+	a.center[bodyId] = make_float2( center.x, center.y );
+	a.sd[simIndex] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+	float* pr = a.params + 8 * simIndex;
+	pr[0] = 0.0f;
+	pr[1] = 0.0f;
+	pr[2] = 0.0f;
+	uint32_t bodyFlags = a.bodyFlags[bodyId];
+	bodyFlags &= ~B2G_TRANSIENT;
+	bodyFlags |= ( stateFlags & ( B2G_SPEED_CAPPED | B2G_HAD_TOI ) );
+	stateFlags &= ~B2G_TRANSIENT;
+	a.sv[simIndex] = make_float4( v.x, v.y, w, __uint_as_float( stateFlags ) );
+	bool isBullet = ( bodyFlags & B2G_IS_BULLET ) != 0;
+	if ( a.enableSleep == 0 || ( bodyFlags & B2G_ENABLE_SLEEP ) == 0 || sleepVelocity > a.sleepThreshold[bodyId] )
+	{
+		float maxMotion = d_max( maxDeltaPosition, maxVelocity * a.dt );
+		if ( a.bodyType[bodyId] == b2_dynamicBody && a.enableContinuous && maxMotion > a.safetyFactor[bodyId] * a.minExtent[bodyId] )
+		{
+			/* fast body: continuous collision is not part of the device path yet; advance the
+			   sweep like a slow body and report it */
+			bodyFlags |= B2G_IS_FAST;
+			atomicAdd( &a.counters->fastBodyCount, 1 );
+		}
+	}
+	a.center0[simIndex] = make_float4( center.x, center.y, q.c, q.s );
+	a.bodyFlags[bodyId] = bodyFlags;
+	bool isFast = ( bodyFlags & B2G_IS_FAST ) != 0;
+	b2Transform transform = { p, q };
+	int start = a.shapeStart[bodyId], count = a.shapeCount[bodyId];
+	bool anyEnlarged = false;
+	for ( int k = 0; k < count; ++k )
+	{
+		int shapeId = a.shapeList[start + k];
+		int enlarged = 0;
+		if ( isFast == false )
+		{
+			const b2gShape* shape = a.shapes + shapeId;
+			float4 aabb = d_computeFatShapeAABB( shape, transform, D_SPECULATIVE_DISTANCE );
+			a.aabb[shapeId] = aabb;
+			float4 fat = a.fat[shapeId];
+			bool contains = fat.x <= aabb.x && fat.y <= aabb.y && aabb.z <= fat.z && aabb.w <= fat.w;
+			if ( contains == false )
+			{
+				float margin = shape->aabbMargin;
+				a.fat[shapeId] = make_float4( aabb.x - margin, aabb.y - margin, aabb.z + margin, aabb.w + margin );
+				enlarged = 1;
+				anyEnlarged = true;
+			}
+		}
+		a.shapeEnlarged[shapeId] = enlarged;
+	}
+	bool fastBullet = isFast && isBullet;
+	if ( anyEnlarged || fastBullet )
+	{
+		int base = atomicAdd( &a.counters->enlargedBodyCount, count );
+		for ( int k = 0; k < count && base + k < a.enlargedCap; ++k )
+		{
+			int shapeId = a.shapeList[start + k];
+			int* r = a.enlargedRecs + 4 * ( base + k );
+			r[0] = simIndex;
+			r[1] = shapeId;
+			r[2] = a.shapeEnlarged[shapeId];
+			r[3] = fastBullet ? 1 : 0;
+			a.enlargedBoxes[base + k] = a.fat[shapeId];
+		}
+	}
+}
+
+__global__ void k_setVelocity( float4* sv, int index, float vx, float vy, float w, int which )
+{
+	float4 s = sv[index];
+	if ( which == 1 )
+	{
+		s.x = vx;
+		s.y = vy;
+	}
+	else
+	{
+		s.z = w;
+	}
+	sv[index] = s;
+}
+
+/* ======================= ABI ======================= */
+extern "C" const char* b2gDev_ErrorString( int code ) { return cudaGetErrorString( (cudaError_t)code ); }
+
+extern "C" int b2gDev_Create( b2gDeviceWorld** out )
+{
+	int count = 0;
+	cudaError_t e = cudaGetDeviceCount( &count );
+	if ( e != cudaSuccess ) return (int)e;
+	if ( count == 0 ) return (int)cudaErrorNoDevice;
+	b2gDeviceWorld* dw = (b2gDeviceWorld*)calloc( 1, sizeof( b2gDeviceWorld ) );
+	CK( cudaStreamCreateWithFlags( &dw->stream, cudaStreamNonBlocking ) );
+	for ( int i = 0; i < 8; ++i ) CK( cudaEventCreate( dw->ev + i ) );
+	CK( cudaMalloc( &dw->counters, sizeof( b2gStepCounters ) ) );
+	CK( cudaMallocHost( &dw->hCounters, sizeof( b2gStepCounters ) ) );
+	for ( int t = 0; t < 3; ++t ) dw->treeRoot[t] = -1;
+	dw->pairPerMove = 32;
+	*out = dw;
+	return 0;
+}
+
+extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
+{
+	if ( dw == NULL ) return;
+	cudaStreamSynchronize( dw->stream );
+	void* dptrs[] = { dw->xf,		  dw->center,	 dw->localCenter, dw->invMass,		dw->invI,		  dw->minExtent,
+					  dw->maxExtent,  dw->sleepThreshold, dw->safetyFactor, dw->awakeIndex, dw->bodyType,	dw->bodyFlags,
+					  dw->shapeStart, dw->shapeCount, dw->shapeList, dw->awakeBodyId,	dw->stateV,		  dw->stateD,
+					  dw->params,	  dw->center0,	 dw->enlargedBody, dw->shapes,		dw->aabb,		  dw->fat,
+					  dw->shapeEnlarged, dw->contacts, dw->colorIds,	dw->lanes,		dw->joints,		  dw->tree[0],
+					  dw->tree[1],	  dw->tree[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  dw->moveKeys,
+					  dw->moveBoxes,  dw->moveShapes, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
+					  dw->enlargedBoxes, dw->counters };
+	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
+		if ( dptrs[i] ) cudaFree( dptrs[i] );
+	void* hptrs[] = { dw->hCounters, dw->hChanges, dw->hRecs, dw->hBoxes, dw->hPairs, dw->hPairCounts };
+	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
+		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
+	free( dw->hSortTmp );
+	for ( int i = 0; i < 8; ++i ) cudaEventDestroy( dw->ev[i] );
+	cudaStreamDestroy( dw->stream );
+	free( dw );
+}
+
+#define GROW( field, capField, need, T ) CK2( grow( (void**)&dw->field, &dw->capField, ( need ), sizeof( T ) ) )
+#define CK2( x )                                                                                                               \
+	do                                                                                                                           \
+	{                                                                                                                            \
+		int r_ = ( x );                                                                                                          \
+		if ( r_ != 0 ) return r_;                                                                                                \
+	} while ( 0 )
+
+extern "C" int b2gDev_UploadShapes( b2gDeviceWorld* dw, const b2gShape* shapes, const float* aabbs, const float* fatAABBs,
+									 int count )
+{
+	int cap = dw->shapeCap;
+	CK2( grow( (void**)&dw->shapes, &cap, count, sizeof( b2gShape ) ) );
+	cap = dw->shapeCap;
+	CK2( grow( (void**)&dw->aabb, &cap, count, sizeof( float4 ) ) );
+	cap = dw->shapeCap;
+	CK2( grow( (void**)&dw->fat, &cap, count, sizeof( float4 ) ) );
+	cap = dw->shapeCap;
+	CK2( grow( (void**)&dw->shapeEnlarged, &cap, count, sizeof( int ) ) );
+	dw->shapeCap = cap;
+	dw->shapeCountTotal = count;
+	if ( count > 0 )
+	{
+		CK( cudaMemcpy( dw->shapes, shapes, (size_t)count * sizeof( b2gShape ), cudaMemcpyHostToDevice ) );
+		CK( cudaMemcpy( dw->aabb, aabbs, (size_t)count * sizeof( float4 ), cudaMemcpyHostToDevice ) );
+		CK( cudaMemcpy( dw->fat, fatAABBs, (size_t)count * sizeof( float4 ), cudaMemcpyHostToDevice ) );
+	}
+	return 0;
+}
+
+template <typename T> static int upload( T** dptr, int* cap, const T* src, int n, int* capOut )
+{
+	int c = *cap;
+	CK2( grow( (void**)dptr, &c, n, sizeof( T ) ) );
+	*capOut = c;
+	if ( n > 0 ) CK( cudaMemcpy( *dptr, src, (size_t)n * sizeof( T ), cudaMemcpyHostToDevice ) );
+	return 0;
+}
+
+extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const float* xf, const float* center,
+									 const float* localCenter, const float* invMass, const float* invI, const float* minExtent,
+									 const float* maxExtent, const float* sleepThreshold, const float* safetyFactor,
+									 const int* awakeIndex, const uint32_t* typeFlags, const int* shapeStart,
+									 const int* shapeCount, const int* shapeList, int shapeListCount )
+{
+	int cap0 = dw->bodyCap, capOut = 0;
+	CK2( upload( &dw->xf, &cap0, (const float4*)xf, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->center, &cap0, (const float2*)center, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->localCenter, &cap0, (const float2*)localCenter, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->invMass, &cap0, invMass, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->invI, &cap0, invI, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->minExtent, &cap0, minExtent, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->maxExtent, &cap0, maxExtent, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->sleepThreshold, &cap0, sleepThreshold, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->safetyFactor, &cap0, safetyFactor, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->awakeIndex, &cap0, awakeIndex, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->shapeStart, &cap0, shapeStart, bodyCount, &capOut ) );
+	cap0 = dw->bodyCap;
+	CK2( upload( &dw->shapeCount, &cap0, shapeCount, bodyCount, &capOut ) );
+	int* type = (int*)malloc( (size_t)( bodyCount > 0 ? bodyCount : 1 ) * sizeof( int ) );
+	uint32_t* flags = (uint32_t*)malloc( (size_t)( bodyCount > 0 ? bodyCount : 1 ) * sizeof( uint32_t ) );
+	for ( int i = 0; i < bodyCount; ++i )
+	{
+		type[i] = (int)( typeFlags[i] & 3 );
+		flags[i] = typeFlags[i] >> 2;
+	}
+	cap0 = dw->bodyCap;
+	int rc = upload( &dw->bodyType, &cap0, type, bodyCount, &capOut );
+	cap0 = dw->bodyCap;
+	if ( rc == 0 ) rc = upload( &dw->bodyFlags, &cap0, flags, bodyCount, &capOut );
+	free( type );
+	free( flags );
+	if ( rc != 0 ) return rc;
+	dw->bodyCap = capOut;
+	dw->bodyCount = bodyCount;
+	CK2( upload( &dw->shapeList, &dw->shapeListCap, shapeList, shapeListCount, &dw->shapeListCap ) );
+	return 0;
+}
+
+extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int* awakeBodyId, const float* stateV,
+									const float* stateD, const float* params, const float* center0 )
+{
+	int cap0 = dw->awakeCap, capOut = 0;
+	CK2( upload( &dw->awakeBodyId, &cap0, awakeBodyId, awakeCount, &capOut ) );
+	cap0 = dw->awakeCap;
+	CK2( upload( &dw->stateV, &cap0, (const float4*)stateV, awakeCount, &capOut ) );
+	cap0 = dw->awakeCap;
+	CK2( upload( &dw->stateD, &cap0, (const float4*)stateD, awakeCount, &capOut ) );
+	cap0 = dw->awakeCap;
+	CK2( upload( &dw->center0, &cap0, (const float4*)center0, awakeCount, &capOut ) );
+	cap0 = dw->awakeCap;
+	CK2( grow( (void**)&dw->enlargedBody, &cap0, awakeCount, sizeof( int ) ) );
+	int pcap = dw->awakeCap * 8;
+	CK2( grow( (void**)&dw->params, &pcap, 8 * awakeCount, sizeof( float ) ) );
+	if ( awakeCount > 0 ) CK( cudaMemcpy( dw->params, params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyHostToDevice ) );
+	dw->awakeCap = capOut;
+	dw->awakeCount = awakeCount;
+	return 0;
+}
+
+extern "C" int b2gDev_DownloadAwake( b2gDeviceWorld* dw, int awakeCount, float* stateV, float* stateD, float* params,
+									  float* center0 )
+{
+	if ( awakeCount == 0 ) return 0;
+	CK( cudaStreamSynchronize( dw->stream ) );
+	CK( cudaMemcpy( stateV, dw->stateV, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	CK( cudaMemcpy( stateD, dw->stateD, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	CK( cudaMemcpy( params, dw->params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyDeviceToHost ) );
+	CK( cudaMemcpy( center0, dw->center0, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	return 0;
+}
+
+extern "C" int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* center, uint32_t* flags )
+{
+	if ( bodyCount == 0 ) return 0;
+	CK( cudaStreamSynchronize( dw->stream ) );
+	CK( cudaMemcpy( xf, dw->xf, (size_t)bodyCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	CK( cudaMemcpy( center, dw->center, (size_t)bodyCount * sizeof( float2 ), cudaMemcpyDeviceToHost ) );
+	CK( cudaMemcpy( flags, dw->bodyFlags, (size_t)bodyCount * sizeof( uint32_t ), cudaMemcpyDeviceToHost ) );
+	return 0;
+}
+
+extern "C" int b2gDev_DownloadShapeBoxes( b2gDeviceWorld* dw, int shapeCount, float* aabbs, float* fatAABBs )
+{
+	if ( shapeCount == 0 ) return 0;
+	CK( cudaStreamSynchronize( dw->stream ) );
+	CK( cudaMemcpy( aabbs, dw->aabb, (size_t)shapeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	CK( cudaMemcpy( fatAABBs, dw->fat, (size_t)shapeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	return 0;
+}
+
+extern "C" int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float vx, float vy, float w, int which )
+{
+	k_setVelocity<<<1, 1, 0, dw->stream>>>( dw->stateV, awakeIndex, vx, vy, w, which );
+	return (int)cudaGetLastError();
+}
+
+extern "C" int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity )
+{
+	CK2( grow( (void**)&dw->contacts, &dw->contactCap, capacity > 0 ? capacity : 1, sizeof( b2gContact ) ) );
+	int c = dw->changeCap;
+	CK2( grow( (void**)&dw->changes, &c, 2 * ( capacity > 0 ? capacity : 1 ), sizeof( int ) ) );
+	dw->changeCap = c;
+	return 0;
+}
+
+static int stage( b2gDeviceWorld* dw, void** dptr, int* cap, const void* src, size_t bytes )
+{
+	CK2( grow( dptr, cap, (int)bytes, 1 ) );
+	CK( cudaMemcpyAsync( *dptr, src, bytes, cudaMemcpyHostToDevice, dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	return 0;
+}
+
+static void* s_staging = NULL;
+static int s_stagingCap = 0;
+
+extern "C" int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* inits, int count )
+{
+	if ( count == 0 ) return 0;
+	CK2( stage( dw, &s_staging, &s_stagingCap, inits, (size_t)count * sizeof( b2gContactInit ) ) );
+	k_initContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const b2gContactInit*)s_staging, count );
+	CK( cudaGetLastError() );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	return 0;
+}
+
+extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int count )
+{
+	if ( count == 0 ) return 0;
+	CK2( stage( dw, &s_staging, &s_stagingCap, ids, (size_t)count * sizeof( int ) ) );
+	k_killContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const int*)s_staging, count );
+	CK( cudaGetLastError() );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	return 0;
+}
+
+extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const int* offsets, int total )
+{
+	CK2( grow( (void**)&dw->colorIds, &dw->colorIdsCap, total > 0 ? total : 1, sizeof( int ) ) );
+	if ( total > 0 ) CK( cudaMemcpy( dw->colorIds, ids, (size_t)total * sizeof( int ), cudaMemcpyHostToDevice ) );
+	memcpy( dw->colorOffsets, offsets, sizeof( dw->colorOffsets ) );
+	return 0;
+}
+
+extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count )
+{
+	if ( count == 0 ) return 0;
+	CK( cudaStreamSynchronize( dw->stream ) );
+	CK( cudaMemcpy( out, dw->contacts, (size_t)count * sizeof( b2gContact ), cudaMemcpyDeviceToHost ) );
+	return 0;
+}
+
+extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* offsets )
+{
+	CK2( grow( (void**)&dw->joints, &dw->jointCap, count > 0 ? count : 1, sizeof( b2gJoint ) ) );
+	if ( count > 0 ) CK( cudaMemcpy( dw->joints, joints, (size_t)count * sizeof( b2gJoint ), cudaMemcpyHostToDevice ) );
+	memcpy( dw->jointOffsets, offsets, sizeof( dw->jointOffsets ) );
+	dw->jointCount = count;
+	return 0;
+}
+
+extern "C" int b2gDev_DownloadJoints( b2gDeviceWorld* dw, b2gJoint* byId, int idCount )
+{
+	int n = dw->jointCount;
+	if ( n == 0 ) return 0;
+	b2gJoint* tmp = (b2gJoint*)malloc( (size_t)n * sizeof( b2gJoint ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	cudaError_t e = cudaMemcpy( tmp, dw->joints, (size_t)n * sizeof( b2gJoint ), cudaMemcpyDeviceToHost );
+	if ( e == cudaSuccess )
+	{
+		for ( int i = 0; i < n; ++i )
+			if ( tmp[i].jointId >= 0 && tmp[i].jointId < idCount ) byId[tmp[i].jointId] = tmp[i];
+	}
+	free( tmp );
+	return (int)e;
+}
+
+extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gTreeNode* nodes, int nodeCount, int root )
+{
+	CK2( grow( (void**)&dw->tree[type], &dw->treeCap[type], nodeCount > 0 ? nodeCount : 1, sizeof( b2gTreeNode ) ) );
+	if ( nodeCount > 0 )
+		CK( cudaMemcpyAsync( dw->tree[type], nodes, (size_t)nodeCount * sizeof( b2gTreeNode ), cudaMemcpyHostToDevice,
+							 dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	int mc = dw->movedCap[type];
+	CK2( grow( (void**)&dw->moved[type], &mc, nodeCount > 0 ? nodeCount : 1, 1 ) );
+	dw->movedCap[type] = mc;
+	dw->treeRoot[type] = root;
+	return 0;
+}
+
+extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int n,
+								  int** outPairs, int** outCounts, int* outTotal )
+{
+	CK( cudaEventRecord( dw->ev[0], dw->stream ) );
+	int cap = dw->moveCap;
+	CK2( grow( (void**)&dw->moveKeys, &cap, n, sizeof( int ) ) );
+	cap = dw->moveCap;
+	CK2( grow( (void**)&dw->moveBoxes, &cap, n, sizeof( float4 ) ) );
+	cap = dw->moveCap;
+	CK2( grow( (void**)&dw->moveShapes, &cap, n, sizeof( int ) ) );
+	cap = dw->moveCap;
+	CK2( grow( (void**)&dw->pairCounts, &cap, n, sizeof( int ) ) );
+	dw->moveCap = cap;
+	CK( cudaMemcpyAsync( dw->moveKeys, keys, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) );
+	CK( cudaMemcpyAsync( dw->moveBoxes, boxes, (size_t)n * sizeof( float4 ), cudaMemcpyHostToDevice, dw->stream ) );
+	CK( cudaMemcpyAsync( dw->moveShapes, shapes, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) );
+	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
+															   dw->moved[b2_staticBody], dw->moveKeys, n, 1 );
+	CK( cudaGetLastError() );
+	for ( int attempt = 0; attempt < 8; ++attempt )
+	{
+		CK2( grow( (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
+		CK( cudaMemsetAsync( dw->counters, 0, sizeof( b2gStepCounters ), dw->stream ) );
+		k_findPairs<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>(
+			dw->tree[b2_staticBody], dw->treeRoot[b2_staticBody], dw->tree[b2_kinematicBody], dw->treeRoot[b2_kinematicBody],
+			dw->tree[b2_dynamicBody], dw->treeRoot[b2_dynamicBody], dw->moved[b2_dynamicBody], dw->moveKeys, dw->moveBoxes,
+			dw->moveShapes, n, dw->pairBuf, dw->pairCounts, dw->pairPerMove, dw->counters );
+		CK( cudaGetLastError() );
+		CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaStreamSynchronize( dw->stream ) );
+		if ( dw->hCounters->status != 0 ) return (int)cudaErrorIllegalState;
+		if ( dw->hCounters->pairOverflow <= dw->pairPerMove ) break;
+		while ( dw->pairPerMove < dw->hCounters->pairOverflow ) dw->pairPerMove *= 2;
+	}
+	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
+															   dw->moved[b2_staticBody], dw->moveKeys, n, 0 );
+	CK( cudaGetLastError() );
+	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, n, sizeof( int ) ) );
+	CK( cudaMemcpyAsync( dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+	int* raw = NULL;
+	int rawCap = 0;
+	CK2( growHost( (void**)&raw, &rawCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
+	CK( cudaMemcpyAsync( raw, dw->pairBuf, (size_t)2 * n * dw->pairPerMove * sizeof( int ), cudaMemcpyDeviceToHost,
+						 dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	int total = 0;
+	for ( int i = 0; i < n; ++i ) total += dw->hPairCounts[i];
+	CK2( growHost( (void**)&dw->hPairs, &dw->hPairsCap, 2 * ( total > 0 ? total : 1 ), sizeof( int ) ) );
+	int o = 0;
+	for ( int i = 0; i < n; ++i )
+	{
+		int c = dw->hPairCounts[i];
+		memcpy( dw->hPairs + 2 * o, raw + 2 * (size_t)i * dw->pairPerMove, (size_t)c * 2 * sizeof( int ) );
+		o += c;
+	}
+	cudaFreeHost( raw );
+	CK( cudaEventRecord( dw->ev[1], dw->stream ) );
+	*outPairs = dw->hPairs;
+	*outCounts = dw->hPairCounts;
+	*outTotal = total;
+	return 0;
+}
+
+static int cmpChange( const void* a, const void* b )
+{
+	int x = ( (const int*)a )[0], y = ( (const int*)b )[0];
+	return ( x > y ) - ( x < y );
+}
+
+extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int contactIdCapacity, const int** outChanges,
+								int* outChangeCount, int* outRecycled )
+{
+	CK( cudaEventRecord( dw->ev[2], dw->stream ) );
+	CK( cudaMemsetAsync( dw->counters, 0, sizeof( b2gStepCounters ), dw->stream ) );
+	*outChangeCount = 0;
+	*outRecycled = 0;
+	if ( contactIdCapacity > 0 )
+	{
+		d_collideArgs a;
+		a.contacts = dw->contacts;
+		a.capacity = contactIdCapacity;
+		a.shapes = dw->shapes;
+		a.fat = dw->fat;
+		a.xf = dw->xf;
+		a.center = dw->center;
+		a.localCenter = dw->localCenter;
+		a.invMass = dw->invMass;
+		a.invI = dw->invI;
+		a.maxExtent = dw->maxExtent;
+		a.awakeIndex = dw->awakeIndex;
+		a.bodyType = dw->bodyType;
+		a.bodyFlags = dw->bodyFlags;
+		a.changes = dw->changes;
+		a.counters = dw->counters;
+		a.recycleDistance = p->contactRecycleDistance;
+		k_collide<<<blocks( contactIdCapacity ), B2G_THREADS, 0, dw->stream>>>( a );
+		CK( cudaGetLastError() );
+	}
+	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	int n = dw->hCounters->stateChangeCount;
+	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( n > 0 ? n : 1 ), sizeof( int ) ) );
+	if ( n > 0 )
+	{
+		CK( cudaMemcpyAsync( dw->hChanges, dw->changes, (size_t)2 * n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaStreamSynchronize( dw->stream ) );
+		qsort( dw->hChanges, (size_t)n, 2 * sizeof( int ), cmpChange );
+	}
+	CK( cudaEventRecord( dw->ev[3], dw->stream ) );
+	*outChanges = dw->hChanges;
+	*outChangeCount = n;
+	*outRecycled = dw->hCounters->recycledContactCount;
+	return 0;
+}
+
+struct recKey
+{
+	int simIndex, order;
+};
+
+static int cmpRec( const void* a, const void* b )
+{
+	const recKey* x = (const recKey*)a;
+	const recKey* y = (const recKey*)b;
+	if ( x->simIndex != y->simIndex ) return ( x->simIndex > y->simIndex ) - ( x->simIndex < y->simIndex );
+	return ( x->order > y->order ) - ( x->order < y->order );
+}
+
+extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const int* activeColors, int activeColorCount,
+							  const int* colorContactCounts, const int* colorJointCounts, int awakeCount,
+							  const int** outRecs, int* outCount, const float** outBoxes, int* outStatus )
+{
+	(void)colorContactCounts;
+	(void)colorJointCounts;
+	CK( cudaEventRecord( dw->ev[4], dw->stream ) );
+	int total = dw->colorOffsets[B2_GRAPH_COLOR_COUNT];
+	int overflowBegin = dw->colorOffsets[B2G_OVERFLOW_INDEX];
+	CK2( grow( (void**)&dw->lanes, &dw->laneCap, total > 0 ? total : 1, sizeof( b2gContactLane ) ) );
+	CK( cudaMemsetAsync( dw->counters, 0, sizeof( b2gStepCounters ), dw->stream ) );
+	d_solveArgs a;
+	a.contacts = dw->contacts;
+	a.colorIds = dw->colorIds;
+	a.lanes = dw->lanes;
+	a.joints = dw->joints;
+	a.sv = dw->stateV;
+	a.sd = dw->stateD;
+	a.params = dw->params;
+	a.awakeCount = awakeCount;
+	a.p = *p;
+	int jointTotal = dw->jointOffsets[B2_GRAPH_COLOR_COUNT];
+	if ( jointTotal > 0 )
+	{
+		d_jointBodies jb = { dw->xf, dw->center, dw->localCenter, dw->invMass, dw->invI, dw->awakeIndex };
+		k_prepareJoints<<<blocks( jointTotal ), B2G_THREADS, 0, dw->stream>>>( a, jb, jointTotal );
+	}
+	if ( total > 0 ) k_prepareContacts<<<blocks( total ), B2G_THREADS, 0, dw->stream>>>( a, 0, total, overflowBegin );
+	for ( int k = 0; k < activeColorCount; ++k )
+	{
+		int c = activeColors[k];
+		int begin = dw->colorOffsets[c], count = dw->colorOffsets[c + 1] - begin;
+		if ( count > 0 ) k_groupFlags<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( a, begin, count );
+	}
+	CK( cudaGetLastError() );
+	int ovJointBegin = dw->jointOffsets[B2G_OVERFLOW_INDEX];
+	int ovJointCount = dw->jointOffsets[B2_GRAPH_COLOR_COUNT] - ovJointBegin;
+	int ovCount = total - overflowBegin;
+	bool hasOverflow = ovJointCount + ovCount > 0;
+	for ( int sub = 0; sub < p->subStepCount; ++sub )
+	{
+		k_integrateVelocities<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( a );
+		for ( int stage = STAGE_WARM; stage <= STAGE_RELAX; ++stage )
+		{
+			if ( stage == STAGE_RELAX )
+				k_integratePositions<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( a );
+			if ( hasOverflow ) k_overflowStage<<<1, 1, 0, dw->stream>>>( a, ovJointBegin, ovJointCount, overflowBegin, ovCount, stage );
+			for ( int k = 0; k < activeColorCount; ++k )
+			{
+				int c = activeColors[k];
+				int jb = dw->jointOffsets[c], jc = dw->jointOffsets[c + 1] - jb;
+				int lb = dw->colorOffsets[c], lc = dw->colorOffsets[c + 1] - lb;
+				if ( jc + lc > 0 ) k_colorStage<<<blocks( jc + lc ), B2G_THREADS, 0, dw->stream>>>( a, jb, jc, lb, lc, stage );
+			}
+		}
+	}
+	if ( hasOverflow ) k_overflowStage<<<1, 1, 0, dw->stream>>>( a, ovJointBegin, ovJointCount, overflowBegin, ovCount, STAGE_RESTITUTION );
+	for ( int k = 0; k < activeColorCount; ++k )
+	{
+		int c = activeColors[k];
+		int lb = dw->colorOffsets[c], lc = dw->colorOffsets[c + 1] - lb;
+		if ( lc > 0 ) k_colorStage<<<blocks( lc ), B2G_THREADS, 0, dw->stream>>>( a, 0, 0, lb, lc, STAGE_RESTITUTION );
+	}
+	if ( total > 0 ) k_storeImpulses<<<blocks( total ), B2G_THREADS, 0, dw->stream>>>( a, 0, total, overflowBegin );
+	CK( cudaGetLastError() );
+
+	/* finalize */
+	int shapeTotal = dw->shapeCountTotal;
+	CK2( grow( (void**)&dw->enlargedRecs, &dw->enlargedCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( int ) ) );
+	CK2( grow( (void**)&dw->enlargedBoxes, &dw->enlargedBoxesCap, shapeTotal > 0 ? shapeTotal : 1, sizeof( float4 ) ) );
+	d_finalizeArgs f;
+	f.sv = dw->stateV;
+	f.sd = dw->stateD;
+	f.params = dw->params;
+	f.center0 = dw->center0;
+	f.awakeBodyId = dw->awakeBodyId;
+	f.awakeCount = awakeCount;
+	f.xf = dw->xf;
+	f.center = dw->center;
+	f.localCenter = dw->localCenter;
+	f.minExtent = dw->minExtent;
+	f.maxExtent = dw->maxExtent;
+	f.sleepThreshold = dw->sleepThreshold;
+	f.safetyFactor = dw->safetyFactor;
+	f.bodyType = dw->bodyType;
+	f.bodyFlags = dw->bodyFlags;
+	f.shapeStart = dw->shapeStart;
+	f.shapeCount = dw->shapeCount;
+	f.shapeList = dw->shapeList;
+	f.shapes = dw->shapes;
+	f.aabb = dw->aabb;
+	f.fat = dw->fat;
+	f.shapeEnlarged = dw->shapeEnlarged;
+	f.enlargedRecs = dw->enlargedRecs;
+	f.enlargedBoxes = dw->enlargedBoxes;
+	f.enlargedCap = shapeTotal;
+	f.counters = dw->counters;
+	f.dt = p->dt;
+	f.inv_dt = p->inv_dt;
+	f.enableSleep = p->enableSleep;
+	f.enableContinuous = p->enableContinuous;
+	k_finalizeBodies<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( f );
+	CK( cudaGetLastError() );
+	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	int n = dw->hCounters->enlargedBodyCount;
+	if ( n > shapeTotal ) n = shapeTotal;
+	CK2( growHost( (void**)&dw->hRecs, &dw->hRecsCap, 4 * ( n > 0 ? n : 1 ), sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hBoxes, &dw->hBoxesCap, 4 * ( n > 0 ? n : 1 ), sizeof( float ) ) );
+	if ( n > 0 )
+	{
+		int* recs = (int*)malloc( (size_t)n * 4 * sizeof( int ) );
+		float* boxes = (float*)malloc( (size_t)n * 4 * sizeof( float ) );
+		CK( cudaMemcpy( recs, dw->enlargedRecs, (size_t)n * 4 * sizeof( int ), cudaMemcpyDeviceToHost ) );
+		CK( cudaMemcpy( boxes, dw->enlargedBoxes, (size_t)n * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+		recKey* keys = (recKey*)malloc( (size_t)n * sizeof( recKey ) );
+		for ( int i = 0; i < n; ++i )
+		{
+			keys[i].simIndex = recs[4 * i];
+			keys[i].order = i;
+		}
+		qsort( keys, (size_t)n, sizeof( recKey ), cmpRec );
+		for ( int i = 0; i < n; ++i )
+		{
+			memcpy( dw->hRecs + 4 * i, recs + 4 * keys[i].order, 4 * sizeof( int ) );
+			memcpy( dw->hBoxes + 4 * i, boxes + 4 * keys[i].order, 4 * sizeof( float ) );
+		}
+		free( keys );
+		free( recs );
+		free( boxes );
+	}
+	CK( cudaEventRecord( dw->ev[5], dw->stream ) );
+	*outRecs = dw->hRecs;
+	*outBoxes = dw->hBoxes;
+	*outCount = n;
+	*outStatus = dw->hCounters->status;
+	return 0;
+}
+
+extern "C" int b2gDev_Synchronize( b2gDeviceWorld* dw ) { return (int)cudaStreamSynchronize( dw->stream ); }
+
+extern "C" void b2gDev_Timings( b2gDeviceWorld* dw, float* pairsMs, float* collideMs, float* solveMs )
+{
+	cudaEventElapsedTime( pairsMs, dw->ev[0], dw->ev[1] );
+	cudaEventElapsedTime( collideMs, dw->ev[2], dw->ev[3] );
+	cudaEventElapsedTime( solveMs, dw->ev[4], dw->ev[5] );
+}

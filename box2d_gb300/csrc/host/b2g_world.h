@@ -1,0 +1,174 @@
+/*
+ * Host world model of the GB300 step library. The host keeps the serial bookkeeping of
+ * Box2D v3.2's step -- ids, body/shape/contact/joint records, the broadphase trees, the
+ * move buffer, the shape-pair set and the graph colors -- in the exact array orders of
+ * the reference (so contact ids and colors come out identical). All per-step numeric work
+ * (pair query, narrowphase, solver, finalize) runs on the device; the host only reads
+ * back compact change lists.
+ */
+#ifndef B2G_WORLD_H
+#define B2G_WORLD_H
+
+#include "../b2g_device_abi.h"
+#include "b2g_host.h"
+
+#define H_MAX_WORLDS 128
+
+enum
+{
+	H_STATIC_SET = 0,
+	H_DISABLED_SET = 1,
+	H_AWAKE_SET = 2,
+};
+
+typedef struct h_body
+{
+	void* userData;
+	int setIndex, localIndex; /* awake index for the awake set, static index otherwise */
+	int headContactKey, contactCount;
+	int headShapeId, shapeCount;
+	int headJointKey, jointCount;
+	float mass, inertia;
+	float sleepThreshold, sleepTime, safetyFactor;
+	int id;
+	uint32_t flags;
+	b2BodyType type;
+	uint16_t generation;
+	/* cold simulation data (device is authoritative for transform/velocity after a step) */
+	b2Transform transform;
+	b2Vec2 center, localCenter;
+	float invMass, invInertia, minExtent, maxExtent;
+	float linearDamping, angularDamping, gravityScale;
+	uint32_t simFlags;
+	b2Vec2 linearVelocity;
+	float angularVelocity;
+} h_body;
+
+typedef struct h_shape
+{
+	int id, bodyId, prevShapeId, nextShapeId;
+	b2ShapeType type;
+	b2SurfaceMaterial material;
+	float density, aabbMargin;
+	b2AABB aabb, fatAABB;
+	b2Vec2 localCentroid;
+	int proxyKey;
+	b2Filter filter;
+	void* userData;
+	union
+	{
+		b2Capsule capsule;
+		b2Circle circle;
+		b2Polygon polygon;
+		b2Segment segment;
+	};
+	uint16_t generation;
+	int enableContactEvents, enableHitEvents, isSensor;
+} h_shape;
+
+typedef struct h_contactEdge
+{
+	int bodyId, prevKey, nextKey;
+} h_contactEdge;
+
+typedef struct h_contact
+{
+	h_contactEdge edges[2];
+	int setIndex, colorIndex, localIndex;
+	int shapeIdA, shapeIdB, contactId;
+	uint32_t flags, generation;
+} h_contact;
+
+typedef struct h_jointEdge
+{
+	int bodyId, prevKey, nextKey;
+} h_jointEdge;
+
+typedef struct h_joint
+{
+	void* userData;
+	int setIndex, colorIndex, localIndex;
+	h_jointEdge edges[2];
+	int jointId;
+	b2JointType type;
+	uint16_t generation;
+	int collideConnected;
+} h_joint;
+
+typedef struct h_color
+{
+	h_bitSet bodySet;
+	h_intArray contactIds; /* reference array order (add at end, swap-remove) */
+	h_intArray jointIds;
+} h_color;
+
+typedef struct h_world
+{
+	int inUse;
+	uint16_t worldId, generation;
+	h_idPool bodyIdPool, shapeIdPool, contactIdPool, jointIdPool;
+	H_ARRAY( h_body ) bodies;
+	H_ARRAY( h_shape ) shapes;
+	H_ARRAY( h_contact ) contacts;
+	H_ARRAY( h_joint ) joints;
+	H_ARRAY( b2gJoint ) jointRecords; /* by joint id; device copy is authoritative */
+	h_intArray awakeBodyIds;		  /* awake index -> body id */
+	int staticCount;
+	h_intArray awakeContactIds;		  /* non-touching contacts, reference array order */
+	h_color colors[B2_GRAPH_COLOR_COUNT];
+	h_tree trees[3];
+	h_bitSet movedProxies[3];
+	h_intArray moveArray;
+	h_pairSet pairSet;
+	/* settings */
+	b2Vec2 gravity;
+	float hitEventThreshold, restitutionThreshold, maxLinearSpeed, contactSpeed, contactHertz, contactDampingRatio;
+	int enableSleep, enableWarmStarting, enableContactSoftening, enableContinuous, locked;
+	/* events */
+	H_ARRAY( b2BodyMoveEvent ) moveEvents;
+	H_ARRAY( b2ContactBeginTouchEvent ) beginEvents;
+	H_ARRAY( b2ContactEndTouchEvent ) endEvents[2];
+	int endEventArrayIndex;
+	int stepIndex;
+	int recycledContactCount;
+	b2Profile profile;
+	/* device mirror */
+	b2gDeviceWorld* dev;
+	int devReady;			/* device arrays hold the current world */
+	int hostStateValid;		/* host body transforms/velocities match the device */
+	int moveEventsValid;	/* move event array matches the last step */
+	int colorsDirty, jointsDirty, treesDirty;
+	H_ARRAY( b2gContactInit ) pendingInits;
+	h_intArray pendingKills;
+	int lastStatus;
+} h_world;
+
+h_world* h_worldFromId( b2WorldId id );
+h_world* h_worldByIndex( int index );
+
+/* geometry helpers (geometry.c) */
+b2AABB h_computeFatShapeAABB( const h_shape* shape, b2Transform xf, float extra );
+b2Vec2 h_getShapeCentroid( const h_shape* shape );
+float h_computeShapeMargin( const h_shape* shape );
+b2MassData h_computeShapeMass( const h_shape* shape );
+void h_computeShapeExtent( const h_shape* shape, b2Vec2 localCenter, float* minExtent, float* maxExtent );
+
+/* world.c internals used by step.c and joint.c */
+void h_syncFromDevice( h_world* w );
+void h_ensureDevice( h_world* w );
+void h_createContact( h_world* w, h_shape* a, h_shape* b );
+void h_destroyContact( h_world* w, h_contact* c );
+void h_addContactToGraph( h_world* w, h_contact* c );
+void h_removeContactFromGraph( h_world* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex );
+int h_assignJointColor( h_world* w, int bodyIdA, int bodyIdB, b2BodyType typeA, b2BodyType typeB );
+int h_shouldBodiesCollide( h_world* w, h_body* a, h_body* b );
+int h_canCollide( b2ShapeType a, b2ShapeType b );
+int h_isPrimary( b2ShapeType a, b2ShapeType b );
+void h_bufferMove( h_world* w, int proxyKey );
+void h_fail( h_world* w, const char* what, int code );
+
+#define H_PROXY_TYPE( K ) ( (b2BodyType)( ( K ) & 3 ) )
+#define H_PROXY_ID( K ) ( ( K ) >> 2 )
+#define H_PROXY_KEY( ID, T ) ( ( ( ID ) << 2 ) | ( T ) )
+
+#endif

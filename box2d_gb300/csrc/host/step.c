@@ -1,0 +1,363 @@
+/*
+ * b2World_Step for the GB300 step library (physics_world.c:845-1005 in the reference).
+ *
+ * The stage order is the reference's: pair update -> narrowphase -> contact-state pass ->
+ * Soft Step solver -> finalize -> proxy enlargement. The data-parallel parts run on the
+ * device; the host keeps only the serial, order-defining bookkeeping:
+ *   - contact creation in move-array order from the device pair lists,
+ *   - the contact-state pass in ascending contact id (begin/end events, graph colors),
+ *   - proxy enlargement in ascending awake index, which builds the next move array.
+ * Each of these reads one compact list back from the device.
+ */
+#include "b2g_world.h"
+
+#include <stdio.h>
+
+static float h_ms( uint64_t t0 ) { return b2GetMilliseconds( t0 ); }
+
+/* upload one broadphase tree as device query nodes */
+static void h_uploadTree( h_world* w, int type )
+{
+	h_tree* t = w->trees + type;
+	int n = t->nodeCapacity;
+	b2gTreeNode* nodes = malloc( (size_t)( n > 0 ? n : 1 ) * sizeof( b2gTreeNode ) );
+	for ( int i = 0; i < n; ++i )
+	{
+		const h_treeNode* s = t->nodes + i;
+		b2gTreeNode* d = nodes + i;
+		d->aabb = s->aabb;
+		d->isLeaf = ( s->flags & H_NODE_LEAF ) ? 1 : 0;
+		d->categoryNonZero = s->categoryBits != 0;
+		if ( d->isLeaf )
+		{
+			d->child1 = (int)s->userData;
+			d->child2 = -1;
+		}
+		else
+		{
+			d->child1 = s->child1;
+			d->child2 = s->child2;
+		}
+	}
+	int rc = b2gDev_UploadTree( w->dev, type, nodes, n, t->nodeCount == 0 ? -1 : t->root );
+	free( nodes );
+	if ( rc != 0 ) h_fail( w, "tree upload", rc );
+}
+
+static int h_shouldShapesCollide( b2Filter a, b2Filter b )
+{
+	if ( a.groupIndex == b.groupIndex && a.groupIndex != 0 ) return a.groupIndex > 0;
+	return ( a.maskBits & b.categoryBits ) != 0 && ( a.categoryBits & b.maskBits ) != 0;
+}
+
+/* broad_phase.c:412-529. The device returns, per move, every overlapping proxy in the
+   reference's query order (kinematic, static, dynamic trees; DFS child2 first) after the
+   self and moved-pair dedupe; the host applies the remaining filters and creates contacts
+   newest-first per move, as the reference's prepended pair lists do. */
+static void h_updatePairs( h_world* w )
+{
+	int moveCount = w->moveArray.count;
+	if ( moveCount == 0 ) return;
+	if ( w->treesDirty )
+	{
+		for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
+		w->treesDirty = 0;
+	}
+	float* boxes = malloc( (size_t)moveCount * 4 * sizeof( float ) );
+	int* shapeIds = malloc( (size_t)moveCount * sizeof( int ) );
+	for ( int i = 0; i < moveCount; ++i )
+	{
+		int key = w->moveArray.data[i];
+		const h_tree* tree = w->trees + H_PROXY_TYPE( key );
+		const h_treeNode* node = tree->nodes + H_PROXY_ID( key );
+		boxes[4 * i] = node->aabb.lowerBound.x;
+		boxes[4 * i + 1] = node->aabb.lowerBound.y;
+		boxes[4 * i + 2] = node->aabb.upperBound.x;
+		boxes[4 * i + 3] = node->aabb.upperBound.y;
+		shapeIds[i] = (int)node->userData;
+	}
+	int* pairs = NULL;
+	int* counts = NULL;
+	int total = 0;
+	int rc = b2gDev_FindPairs( w->dev, w->moveArray.data, boxes, shapeIds, moveCount, &pairs, &counts, &total );
+	if ( rc != 0 ) h_fail( w, "pair query", rc );
+	int offset = 0;
+	for ( int i = 0; i < moveCount; ++i )
+	{
+		int n = counts[i];
+		for ( int k = n - 1; k >= 0; --k )
+		{
+			int shapeIdA = pairs[2 * ( offset + k )];
+			int shapeIdB = pairs[2 * ( offset + k ) + 1];
+			if ( h_pairSetContains( &w->pairSet, H_SHAPE_PAIR_KEY( shapeIdA, shapeIdB ) ) ) continue;
+			h_shape* sA = w->shapes.data + shapeIdA;
+			h_shape* sB = w->shapes.data + shapeIdB;
+			if ( sA->bodyId == sB->bodyId ) continue;
+			if ( sA->isSensor || sB->isSensor ) continue;
+			if ( h_shouldShapesCollide( sA->filter, sB->filter ) == 0 ) continue;
+			if ( h_canCollide( sA->type, sB->type ) == 0 ) continue;
+			if ( h_shouldBodiesCollide( w, w->bodies.data + sA->bodyId, w->bodies.data + sB->bodyId ) == 0 ) continue;
+			h_createContact( w, sA, sB );
+		}
+		offset += n;
+	}
+	free( boxes );
+	free( shapeIds );
+	/* b2UpdateTreesTask (broad_phase.c:401-410) */
+	h_treeRebuild( w->trees + b2_dynamicBody, 0 );
+	h_treeRebuild( w->trees + b2_kinematicBody, 0 );
+	w->treesDirty = 1;
+	for ( int i = 0; i < w->moveArray.count; ++i )
+	{
+		int key = w->moveArray.data[i];
+		h_bitClear( w->movedProxies + H_PROXY_TYPE( key ), H_PROXY_ID( key ) );
+	}
+	w->moveArray.count = 0;
+}
+
+static void h_flushContacts( h_world* w )
+{
+	int rc = b2gDev_ReserveContacts( w->dev, w->contactIdPool.nextIndex );
+	if ( rc == 0 && w->pendingKills.count > 0 ) rc = b2gDev_KillContacts( w->dev, w->pendingKills.data, w->pendingKills.count );
+	if ( rc == 0 && w->pendingInits.count > 0 ) rc = b2gDev_InitContacts( w->dev, w->pendingInits.data, w->pendingInits.count );
+	if ( rc != 0 ) h_fail( w, "contact upload", rc );
+	w->pendingKills.count = 0;
+	w->pendingInits.count = 0;
+}
+
+static void h_uploadColors( h_world* w )
+{
+	if ( w->colorsDirty == 0 ) return;
+	int offsets[B2_GRAPH_COLOR_COUNT + 1];
+	int total = 0;
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
+	{
+		offsets[i] = total;
+		total += w->colors[i].contactIds.count;
+	}
+	offsets[B2_GRAPH_COLOR_COUNT] = total;
+	int* ids = malloc( (size_t)( total > 0 ? total : 1 ) * sizeof( int ) );
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
+		memcpy( ids + offsets[i], w->colors[i].contactIds.data, (size_t)w->colors[i].contactIds.count * sizeof( int ) );
+	int rc = b2gDev_UploadColors( w->dev, ids, offsets, total );
+	free( ids );
+	if ( rc != 0 ) h_fail( w, "color upload", rc );
+	w->colorsDirty = 0;
+}
+
+static void h_uploadJoints( h_world* w )
+{
+	if ( w->jointsDirty == 0 ) return;
+	int offsets[B2_GRAPH_COLOR_COUNT + 1];
+	int total = 0;
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
+	{
+		offsets[i] = total;
+		total += w->colors[i].jointIds.count;
+	}
+	offsets[B2_GRAPH_COLOR_COUNT] = total;
+	/* joints go to the device in color order; the device keeps the joint id in each record */
+	b2gJoint* ordered = malloc( (size_t)( total > 0 ? total : 1 ) * sizeof( b2gJoint ) );
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
+	{
+		for ( int k = 0; k < w->colors[i].jointIds.count; ++k )
+		{
+			int jointId = w->colors[i].jointIds.data[k];
+			ordered[offsets[i] + k] = w->jointRecords.data[jointId];
+			ordered[offsets[i] + k].jointId = jointId;
+		}
+	}
+	int rc = b2gDev_UploadJoints( w->dev, ordered, total, offsets );
+	free( ordered );
+	if ( rc != 0 ) h_fail( w, "joint upload", rc );
+	w->jointsDirty = 0;
+}
+
+static int h_cmpInt( const void* a, const void* b )
+{
+	int x = *(const int*)a, y = *(const int*)b;
+	return ( x > y ) - ( x < y );
+}
+
+/* physics_world.c:711-836: serial state pass in ascending contact id */
+static void h_contactStatePass( h_world* w, const int* changes, int count )
+{
+	int endEventArrayIndex = w->endEventArrayIndex;
+	for ( int i = 0; i < count; ++i )
+	{
+		int contactId = changes[2 * i];
+		uint32_t simFlags = (uint32_t)changes[2 * i + 1];
+		h_contact* contact = w->contacts.data + contactId;
+		int colorIndex = contact->colorIndex;
+		int localIndex = contact->localIndex;
+		const h_shape* shapeA = w->shapes.data + contact->shapeIdA;
+		const h_shape* shapeB = w->shapes.data + contact->shapeIdB;
+		b2ShapeId shapeIdA = { shapeA->id + 1, w->worldId, shapeA->generation };
+		b2ShapeId shapeIdB = { shapeB->id + 1, w->worldId, shapeB->generation };
+		b2ContactId fullId;
+		fullId.index1 = contactId + 1;
+		fullId.world0 = w->worldId;
+		fullId.padding = 0;
+		fullId.generation = contact->generation;
+		uint32_t flags = contact->flags;
+		if ( simFlags & B2G_S_DISJOINT )
+		{
+			h_destroyContact( w, contact );
+		}
+		else if ( simFlags & B2G_S_STARTED )
+		{
+			if ( flags & B2G_C_ENABLE_EVENTS )
+			{
+				b2ContactBeginTouchEvent ev = { shapeIdA, shapeIdB, fullId };
+				h_push( w->beginEvents, ev );
+			}
+			contact->flags |= B2G_C_TOUCHING;
+			h_addContactToGraph( w, contact );
+			int moved = h_removeSwap( w->awakeContactIds, localIndex );
+			if ( moved != B2_NULL_INDEX ) w->contacts.data[w->awakeContactIds.data[localIndex]].localIndex = localIndex;
+		}
+		else if ( simFlags & B2G_S_STOPPED )
+		{
+			contact->flags &= ~B2G_C_TOUCHING;
+			if ( contact->flags & B2G_C_ENABLE_EVENTS )
+			{
+				b2ContactEndTouchEvent ev = { shapeIdA, shapeIdB, fullId };
+				h_push( w->endEvents[endEventArrayIndex], ev );
+			}
+			int bodyIdA = contact->edges[0].bodyId, bodyIdB = contact->edges[1].bodyId;
+			contact->colorIndex = B2_NULL_INDEX;
+			contact->localIndex = w->awakeContactIds.count;
+			h_push( w->awakeContactIds, contactId );
+			h_removeContactFromGraph( w, bodyIdA, bodyIdB, colorIndex, localIndex );
+		}
+	}
+}
+
+/* solver.c:1837-1909: enlarge proxies in ascending awake index; this builds the next move
+   array. Each record is (awakeIndex, shapeId, enlargedFlag, bodyFast) + fat box. */
+static void h_enlargeProxies( h_world* w, const int* recs, const float* boxes, int count )
+{
+	for ( int i = 0; i < count; ++i )
+	{
+		int shapeId = recs[4 * i + 1];
+		int enlarged = recs[4 * i + 2];
+		int fastBullet = recs[4 * i + 3];
+		h_shape* s = w->shapes.data + shapeId;
+		if ( fastBullet )
+		{
+			h_bufferMove( w, s->proxyKey );
+			continue;
+		}
+		if ( enlarged )
+		{
+			b2AABB fat = { { boxes[4 * i], boxes[4 * i + 1] }, { boxes[4 * i + 2], boxes[4 * i + 3] } };
+			s->fatAABB = fat;
+			h_treeEnlargeProxy( w->trees + H_PROXY_TYPE( s->proxyKey ), H_PROXY_ID( s->proxyKey ), fat );
+			h_bufferMove( w, s->proxyKey );
+			w->treesDirty = 1;
+		}
+	}
+}
+
+void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w == NULL || w->locked ) return;
+	w->moveEvents.count = 0;
+	w->moveEventsValid = 0;
+	w->beginEvents.count = 0;
+	memset( &w->profile, 0, sizeof( w->profile ) );
+	w->locked = 1;
+	uint64_t stepTicks = b2GetTicks();
+
+	h_ensureDevice( w );
+
+	uint64_t t0 = b2GetTicks();
+	h_updatePairs( w );
+	w->profile.pairs = h_ms( t0 );
+
+	b2gStepParams p;
+	memset( &p, 0, sizeof( p ) );
+	p.dt = timeStep;
+	p.subStepCount = h_maxi( 1, subStepCount );
+	if ( timeStep > 0.0f )
+	{
+		p.inv_dt = 1.0f / timeStep;
+		p.h = timeStep / p.subStepCount;
+		p.inv_h = p.subStepCount * p.inv_dt;
+	}
+	float contactHertz = h_min( w->contactHertz, 0.125f * p.inv_h );
+	h_softness cs = h_makeSoft( contactHertz, w->contactDampingRatio, p.h );
+	h_softness ss = h_makeSoft( 2.0f * contactHertz, w->contactDampingRatio, p.h );
+	p.contactBiasRate = cs.biasRate;
+	p.contactMassScale = cs.massScale;
+	p.contactImpulseScale = cs.impulseScale;
+	p.staticBiasRate = ss.biasRate;
+	p.staticMassScale = ss.massScale;
+	p.staticImpulseScale = ss.impulseScale;
+	p.restitutionThreshold = w->restitutionThreshold;
+	p.maxLinearVelocity = w->maxLinearSpeed;
+	p.contactSpeed = w->contactSpeed;
+	p.contactHertz = w->contactHertz;
+	p.contactDampingRatio = w->contactDampingRatio;
+	p.gravityX = w->gravity.x;
+	p.gravityY = w->gravity.y;
+	p.enableWarmStarting = w->enableWarmStarting;
+	p.enableContinuous = w->enableContinuous;
+	p.enableSleep = w->enableSleep;
+	p.enableContactSoftening = w->enableContactSoftening;
+	p.contactRecycleDistance = 10.0f * H_LINEAR_SLOP;
+
+	/* narrowphase + state pass */
+	t0 = b2GetTicks();
+	h_flushContacts( w );
+	h_uploadColors( w );
+	const int* changes = NULL;
+	int changeCount = 0, recycled = 0;
+	int rc = b2gDev_Collide( w->dev, &p, w->contactIdPool.nextIndex, &changes, &changeCount, &recycled );
+	if ( rc != 0 ) h_fail( w, "narrowphase", rc );
+	w->recycledContactCount = recycled;
+	h_contactStatePass( w, changes, changeCount );
+	h_flushContacts( w );
+	w->profile.collide = h_ms( t0 );
+
+	if ( timeStep > 0.0f )
+	{
+		t0 = b2GetTicks();
+		w->stepIndex += 1;
+		h_uploadColors( w );
+		h_uploadJoints( w );
+		int activeColors[B2_GRAPH_COLOR_COUNT];
+		int contactCounts[B2_GRAPH_COLOR_COUNT];
+		int jointCounts[B2_GRAPH_COLOR_COUNT];
+		int activeCount = 0;
+		for ( int i = 0; i < B2_GRAPH_COLOR_COUNT - 1; ++i )
+		{
+			if ( w->colors[i].contactIds.count + w->colors[i].jointIds.count > 0 ) activeColors[activeCount++] = i;
+		}
+		for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
+		{
+			contactCounts[i] = w->colors[i].contactIds.count;
+			jointCounts[i] = w->colors[i].jointIds.count;
+		}
+		const int* recs = NULL;
+		const float* boxes = NULL;
+		int enlargedCount = 0, status = 0;
+		if ( w->awakeBodyIds.count > 0 )
+		{
+			rc = b2gDev_Solve( w->dev, &p, activeColors, activeCount, contactCounts, jointCounts, w->awakeBodyIds.count, &recs,
+							   &enlargedCount, &boxes, &status );
+			if ( rc != 0 ) h_fail( w, "solver", rc );
+			w->lastStatus = status;
+			if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
+			h_enlargeProxies( w, recs, boxes, enlargedCount );
+		}
+		w->profile.solve = h_ms( t0 );
+	}
+	w->hostStateValid = 0;
+	w->profile.step = h_ms( stepTicks );
+	w->endEventArrayIndex = 1 - w->endEventArrayIndex;
+	w->endEvents[w->endEventArrayIndex].count = 0;
+	w->locked = 0;
+	(void)h_cmpInt;
+}

@@ -1,0 +1,1196 @@
+/*
+ * Public API entry points of the GB300 step library (box2d.h subset) and the host's serial
+ * bookkeeping: worlds, bodies, shapes, contact records, graph coloring and the move buffer
+ * (physics_world.c, body.c, shape.c, contact.c, constraint_graph.c, broad_phase.h in the
+ * reference). Numeric body state lives on the device after the first step; getters read
+ * it back lazily (one bulk copy per step), setters write through.
+ */
+#include "b2g_world.h"
+
+#include <stdio.h>
+
+static h_world h_worlds[H_MAX_WORLDS];
+
+h_world* h_worldByIndex( int index ) { return h_worlds + index; }
+
+h_world* h_worldFromId( b2WorldId id )
+{
+	if ( id.index1 < 1 || id.index1 > H_MAX_WORLDS ) return NULL;
+	h_world* w = h_worlds + ( id.index1 - 1 );
+	if ( w->inUse == 0 || w->generation != id.generation ) return NULL;
+	return w;
+}
+
+void h_fail( h_world* w, const char* what, int code )
+{
+	fprintf( stderr, "box2d_gb300: %s failed: %s\n", what, b2gDev_ErrorString( code ) );
+	if ( w ) w->lastStatus = code;
+	abort();
+}
+
+/* ---------------- pair set ---------------- */
+static uint64_t h_hashKey( uint64_t k )
+{
+	k ^= k >> 33;
+	k *= 0xff51afd7ed558ccdull;
+	k ^= k >> 33;
+	return k;
+}
+
+static void h_pairSetGrow( h_pairSet* s )
+{
+	int oldCap = s->capacity;
+	uint64_t* old = s->keys;
+	s->capacity = oldCap == 0 ? 1024 : oldCap * 2;
+	s->keys = malloc( (size_t)s->capacity * 8 );
+	memset( s->keys, 0xff, (size_t)s->capacity * 8 );
+	s->count = 0;
+	for ( int i = 0; i < oldCap; ++i )
+		if ( old[i] != UINT64_MAX ) h_pairSetAdd( s, old[i] );
+	free( old );
+}
+
+void h_pairSetAdd( h_pairSet* s, uint64_t key )
+{
+	if ( 2 * ( s->count + 1 ) > s->capacity ) h_pairSetGrow( s );
+	uint64_t mask = (uint64_t)s->capacity - 1;
+	uint64_t i = h_hashKey( key ) & mask;
+	while ( s->keys[i] != UINT64_MAX )
+	{
+		if ( s->keys[i] == key ) return;
+		i = ( i + 1 ) & mask;
+	}
+	s->keys[i] = key;
+	s->count += 1;
+}
+
+int h_pairSetContains( const h_pairSet* s, uint64_t key )
+{
+	if ( s->capacity == 0 ) return 0;
+	uint64_t mask = (uint64_t)s->capacity - 1;
+	uint64_t i = h_hashKey( key ) & mask;
+	while ( s->keys[i] != UINT64_MAX )
+	{
+		if ( s->keys[i] == key ) return 1;
+		i = ( i + 1 ) & mask;
+	}
+	return 0;
+}
+
+void h_pairSetRemove( h_pairSet* s, uint64_t key )
+{
+	if ( s->capacity == 0 ) return;
+	uint64_t mask = (uint64_t)s->capacity - 1;
+	uint64_t i = h_hashKey( key ) & mask;
+	while ( s->keys[i] != UINT64_MAX )
+	{
+		if ( s->keys[i] == key ) break;
+		i = ( i + 1 ) & mask;
+	}
+	if ( s->keys[i] == UINT64_MAX ) return;
+	/* backward-shift deletion */
+	uint64_t j = i;
+	while ( 1 )
+	{
+		j = ( j + 1 ) & mask;
+		if ( s->keys[j] == UINT64_MAX ) break;
+		uint64_t h = h_hashKey( s->keys[j] ) & mask;
+		int shouldMove = ( i <= j ) ? ( h <= i || h > j ) : ( h <= i && h > j );
+		if ( shouldMove )
+		{
+			s->keys[i] = s->keys[j];
+			i = j;
+		}
+	}
+	s->keys[i] = UINT64_MAX;
+	s->count -= 1;
+}
+
+void h_pairSetFree( h_pairSet* s )
+{
+	free( s->keys );
+	memset( s, 0, sizeof( *s ) );
+}
+
+/* ---------------- defaults (types.c:8-89, joint.c:16-112) ---------------- */
+b2WorldDef b2DefaultWorldDef( void )
+{
+	b2WorldDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.gravity = h_v( 0.0f, -10.0f );
+	def.hitEventThreshold = 1.0f;
+	def.restitutionThreshold = 1.0f;
+	def.contactSpeed = 3.0f;
+	def.contactHertz = 30.0f;
+	def.contactDampingRatio = 10.0f;
+	def.maximumLinearSpeed = 400.0f;
+	def.enableSleep = true;
+	def.enableContinuous = true;
+	def.internalValue = 1152023;
+	return def;
+}
+
+b2BodyDef b2DefaultBodyDef( void )
+{
+	b2BodyDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.type = b2_staticBody;
+	def.rotation.c = 1.0f;
+	def.safetyFactor = 0.5f;
+	def.sleepThreshold = 0.05f;
+	def.gravityScale = 1.0f;
+	def.enableSleep = true;
+	def.enableContactRecycling = true;
+	def.isAwake = true;
+	def.isEnabled = true;
+	def.internalValue = 1152023;
+	return def;
+}
+
+b2Filter b2DefaultFilter( void )
+{
+	b2Filter f = { B2_DEFAULT_CATEGORY_BITS, B2_DEFAULT_MASK_BITS, 0 };
+	return f;
+}
+
+b2SurfaceMaterial b2DefaultSurfaceMaterial( void )
+{
+	b2SurfaceMaterial m;
+	memset( &m, 0, sizeof( m ) );
+	m.friction = 0.6f;
+	return m;
+}
+
+b2ShapeDef b2DefaultShapeDef( void )
+{
+	b2ShapeDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.material.friction = 0.6f;
+	def.density = 1.0f;
+	def.filter = b2DefaultFilter();
+	def.updateBodyMass = true;
+	def.invokeContactCreation = true;
+	def.internalValue = 1152023;
+	return def;
+}
+
+/* ---------------- world (physics_world.c:159-444) ---------------- */
+b2WorldId b2CreateWorld( const b2WorldDef* def )
+{
+	int index = -1;
+	for ( int i = 0; i < H_MAX_WORLDS; ++i )
+	{
+		if ( h_worlds[i].inUse == 0 )
+		{
+			index = i;
+			break;
+		}
+	}
+	b2WorldId nullId = { 0, 0 };
+	if ( index < 0 ) return nullId;
+	h_world* w = h_worlds + index;
+	uint16_t generation = w->generation;
+	memset( w, 0, sizeof( *w ) );
+	w->worldId = (uint16_t)index;
+	w->generation = generation;
+	int rc = b2gDev_Create( &w->dev );
+	if ( rc != 0 )
+	{
+		fprintf( stderr, "box2d_gb300: no usable CUDA device (%s); the GB300 step library has no CPU path\n",
+				 b2gDev_ErrorString( rc ) );
+		return nullId;
+	}
+	w->inUse = 1;
+	for ( int i = 0; i < 3; ++i ) w->trees[i] = h_treeCreate( 16 );
+	w->gravity = def->gravity;
+	w->hitEventThreshold = def->hitEventThreshold;
+	w->restitutionThreshold = def->restitutionThreshold;
+	w->maxLinearSpeed = def->maximumLinearSpeed;
+	w->contactSpeed = def->contactSpeed;
+	w->contactHertz = def->contactHertz;
+	w->contactDampingRatio = def->contactDampingRatio;
+	w->enableSleep = def->enableSleep;
+	w->enableWarmStarting = 1;
+	w->enableContactSoftening = def->enableContactSoftening;
+	w->enableContinuous = def->enableContinuous;
+	w->hostStateValid = 1;
+	w->colorsDirty = 1;
+	w->jointsDirty = 1;
+	w->treesDirty = 1;
+	b2WorldId id = { (uint16_t)( index + 1 ), w->generation };
+	return id;
+}
+
+void b2DestroyWorld( b2WorldId worldId )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w == NULL ) return;
+	b2gDev_Destroy( w->dev );
+	for ( int i = 0; i < 3; ++i )
+	{
+		h_treeDestroy( w->trees + i );
+		free( w->movedProxies[i].bits );
+	}
+	h_free( w->bodyIdPool.freeArray );
+	h_free( w->shapeIdPool.freeArray );
+	h_free( w->contactIdPool.freeArray );
+	h_free( w->jointIdPool.freeArray );
+	h_free( w->bodies );
+	h_free( w->shapes );
+	h_free( w->contacts );
+	h_free( w->joints );
+	h_free( w->jointRecords );
+	h_free( w->awakeBodyIds );
+	h_free( w->awakeContactIds );
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
+	{
+		free( w->colors[i].bodySet.bits );
+		h_free( w->colors[i].contactIds );
+		h_free( w->colors[i].jointIds );
+	}
+	h_free( w->moveArray );
+	h_pairSetFree( &w->pairSet );
+	h_free( w->moveEvents );
+	h_free( w->beginEvents );
+	h_free( w->endEvents[0] );
+	h_free( w->endEvents[1] );
+	h_free( w->pendingInits );
+	h_free( w->pendingKills );
+	uint16_t generation = w->generation;
+	memset( w, 0, sizeof( *w ) );
+	w->generation = generation + 1;
+}
+
+bool b2World_IsValid( b2WorldId id ) { return h_worldFromId( id ) != NULL; }
+
+void b2World_EnableSleeping( b2WorldId worldId, bool flag )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w ) w->enableSleep = flag;
+}
+
+bool b2World_IsSleepingEnabled( b2WorldId worldId ) { return h_worldFromId( worldId )->enableSleep; }
+
+void b2World_EnableContinuous( b2WorldId worldId, bool flag )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w ) w->enableContinuous = flag;
+}
+
+bool b2World_IsContinuousEnabled( b2WorldId worldId ) { return h_worldFromId( worldId )->enableContinuous; }
+
+void b2World_EnableWarmStarting( b2WorldId worldId, bool flag )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w ) w->enableWarmStarting = flag;
+}
+
+void b2World_SetGravity( b2WorldId worldId, b2Vec2 gravity )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w ) w->gravity = gravity;
+}
+
+b2Vec2 b2World_GetGravity( b2WorldId worldId ) { return h_worldFromId( worldId )->gravity; }
+
+int b2World_GetAwakeBodyCount( b2WorldId worldId ) { return h_worldFromId( worldId )->awakeBodyIds.count; }
+
+b2Profile b2World_GetProfile( b2WorldId worldId ) { return h_worldFromId( worldId )->profile; }
+
+b2Counters b2World_GetCounters( b2WorldId worldId )
+{
+	h_world* w = h_worldFromId( worldId );
+	b2Counters c;
+	memset( &c, 0, sizeof( c ) );
+	c.bodyCount = w->bodyIdPool.nextIndex - w->bodyIdPool.freeArray.count;
+	c.shapeCount = w->shapeIdPool.nextIndex - w->shapeIdPool.freeArray.count;
+	c.contactCount = w->contactIdPool.nextIndex - w->contactIdPool.freeArray.count;
+	c.jointCount = w->jointIdPool.nextIndex - w->jointIdPool.freeArray.count;
+	c.staticTreeHeight = h_treeHeight( w->trees + b2_staticBody );
+	c.treeHeight = h_treeHeight( w->trees + b2_dynamicBody );
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
+		c.colorCounts[i] = w->colors[i].contactIds.count + w->colors[i].jointIds.count;
+	c.awakeContactCount = w->awakeContactIds.count;
+	c.recycledContactCount = w->recycledContactCount;
+	return c;
+}
+
+b2BodyEvents b2World_GetBodyEvents( b2WorldId worldId )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w->moveEventsValid == 0 && w->stepIndex > 0 )
+	{
+		/* materialize the move events of the last step from the device state
+		   (solver.c:608-612 fills one per awake body) */
+		h_syncFromDevice( w );
+		int n = w->awakeBodyIds.count;
+		h_reserve( w->moveEvents, n );
+		w->moveEvents.count = n;
+		for ( int i = 0; i < n; ++i )
+		{
+			h_body* b = w->bodies.data + w->awakeBodyIds.data[i];
+			b2BodyMoveEvent* ev = w->moveEvents.data + i;
+			ev->transform = b->transform;
+			ev->bodyId.index1 = b->id + 1;
+			ev->bodyId.world0 = w->worldId;
+			ev->bodyId.generation = b->generation;
+			ev->userData = b->userData;
+			ev->fellAsleep = false;
+		}
+		w->moveEventsValid = 1;
+	}
+	b2BodyEvents e = { w->moveEvents.data, w->moveEvents.count };
+	return e;
+}
+
+b2ContactEvents b2World_GetContactEvents( b2WorldId worldId )
+{
+	h_world* w = h_worldFromId( worldId );
+	int endIndex = w->endEventArrayIndex;
+	b2ContactEvents e;
+	memset( &e, 0, sizeof( e ) );
+	e.beginEvents = w->beginEvents.data;
+	e.beginCount = w->beginEvents.count;
+	e.endEvents = w->endEvents[endIndex].data;
+	e.endCount = w->endEvents[endIndex].count;
+	return e;
+}
+
+/* ---------------- device mirror ---------------- */
+
+/* Pull transforms, centers and velocities (and joint impulses) back from the device. */
+void h_syncFromDevice( h_world* w )
+{
+	if ( w->hostStateValid || w->devReady == 0 ) return;
+	int nb = w->bodies.count;
+	int na = w->awakeBodyIds.count;
+	float* xf = malloc( (size_t)( nb > 0 ? nb : 1 ) * 4 * sizeof( float ) );
+	float* center = malloc( (size_t)( nb > 0 ? nb : 1 ) * 2 * sizeof( float ) );
+	uint32_t* typeFlags = malloc( (size_t)( nb > 0 ? nb : 1 ) * sizeof( uint32_t ) );
+	float* sv = malloc( (size_t)( na > 0 ? na : 1 ) * 4 * sizeof( float ) );
+	float* sd = malloc( (size_t)( na > 0 ? na : 1 ) * 4 * sizeof( float ) );
+	float* params = malloc( (size_t)( na > 0 ? na : 1 ) * 8 * sizeof( float ) );
+	float* c0 = malloc( (size_t)( na > 0 ? na : 1 ) * 4 * sizeof( float ) );
+	int rc = b2gDev_DownloadBodies( w->dev, nb, xf, center, typeFlags );
+	if ( rc == 0 ) rc = b2gDev_DownloadAwake( w->dev, na, sv, sd, params, c0 );
+	if ( rc != 0 ) h_fail( w, "device download", rc );
+	for ( int i = 0; i < nb; ++i )
+	{
+		h_body* b = w->bodies.data + i;
+		if ( b->id != i ) continue;
+		b->transform.p = h_v( xf[4 * i], xf[4 * i + 1] );
+		b->transform.q.c = xf[4 * i + 2];
+		b->transform.q.s = xf[4 * i + 3];
+		b->center = h_v( center[2 * i], center[2 * i + 1] );
+		b->flags = ( b->flags & ~(uint32_t)B2G_TRANSIENT ) | ( typeFlags[i] & B2G_TRANSIENT );
+	}
+	for ( int a = 0; a < na; ++a )
+	{
+		h_body* b = w->bodies.data + w->awakeBodyIds.data[a];
+		b->linearVelocity = h_v( sv[4 * a], sv[4 * a + 1] );
+		b->angularVelocity = sv[4 * a + 2];
+	}
+	free( xf );
+	free( center );
+	free( typeFlags );
+	free( sv );
+	free( sd );
+	free( params );
+	free( c0 );
+	if ( w->joints.count > 0 )
+	{
+		rc = b2gDev_DownloadJoints( w->dev, w->jointRecords.data, w->jointRecords.count );
+		if ( rc != 0 ) h_fail( w, "joint download", rc );
+	}
+	w->hostStateValid = 1;
+}
+
+static void h_markHostChanged( h_world* w )
+{
+	h_syncFromDevice( w );
+	w->devReady = 0;
+}
+
+/* Upload every body, shape, joint and tree (cold data) when the host world changed. */
+void h_ensureDevice( h_world* w )
+{
+	if ( w->devReady ) return;
+	int nb = w->bodies.count;
+	int na = w->awakeBodyIds.count;
+	int ns = w->shapes.count;
+	size_t nbc = (size_t)( nb > 0 ? nb : 1 ), nac = (size_t)( na > 0 ? na : 1 ), nsc = (size_t)( ns > 0 ? ns : 1 );
+	float* xf = calloc( nbc * 4, sizeof( float ) );
+	float* center = calloc( nbc * 2, sizeof( float ) );
+	float* localCenter = calloc( nbc * 2, sizeof( float ) );
+	float* invMass = calloc( nbc, sizeof( float ) );
+	float* invI = calloc( nbc, sizeof( float ) );
+	float* minExtent = calloc( nbc, sizeof( float ) );
+	float* maxExtent = calloc( nbc, sizeof( float ) );
+	float* sleepThreshold = calloc( nbc, sizeof( float ) );
+	float* safetyFactor = calloc( nbc, sizeof( float ) );
+	int* awakeIndex = calloc( nbc, sizeof( int ) );
+	uint32_t* typeFlags = calloc( nbc, sizeof( uint32_t ) );
+	int* shapeStart = calloc( nbc, sizeof( int ) );
+	int* shapeCount = calloc( nbc, sizeof( int ) );
+	int* shapeList = calloc( nsc, sizeof( int ) );
+	int listCount = 0;
+	for ( int i = 0; i < nb; ++i )
+	{
+		h_body* b = w->bodies.data + i;
+		awakeIndex[i] = -1;
+		if ( b->id != i ) continue;
+		xf[4 * i] = b->transform.p.x;
+		xf[4 * i + 1] = b->transform.p.y;
+		xf[4 * i + 2] = b->transform.q.c;
+		xf[4 * i + 3] = b->transform.q.s;
+		center[2 * i] = b->center.x;
+		center[2 * i + 1] = b->center.y;
+		localCenter[2 * i] = b->localCenter.x;
+		localCenter[2 * i + 1] = b->localCenter.y;
+		invMass[i] = b->invMass;
+		invI[i] = b->invInertia;
+		minExtent[i] = b->minExtent;
+		maxExtent[i] = b->maxExtent;
+		sleepThreshold[i] = b->sleepThreshold;
+		safetyFactor[i] = b->safetyFactor;
+		awakeIndex[i] = b->setIndex == H_AWAKE_SET ? b->localIndex : -1;
+		typeFlags[i] = (uint32_t)b->type | ( b->flags << 2 );
+		shapeStart[i] = listCount;
+		int sid = b->headShapeId;
+		while ( sid != B2_NULL_INDEX )
+		{
+			shapeList[listCount++] = sid;
+			sid = w->shapes.data[sid].nextShapeId;
+		}
+		shapeCount[i] = listCount - shapeStart[i];
+	}
+	int* awakeBodyId = w->awakeBodyIds.data;
+	float* sv = calloc( nac * 4, sizeof( float ) );
+	float* sd = calloc( nac * 4, sizeof( float ) );
+	float* params = calloc( nac * 8, sizeof( float ) );
+	float* c0 = calloc( nac * 4, sizeof( float ) );
+	for ( int a = 0; a < na; ++a )
+	{
+		h_body* b = w->bodies.data + awakeBodyId[a];
+		uint32_t fl = b->simFlags;
+		float flBits;
+		memcpy( &flBits, &fl, 4 );
+		sv[4 * a] = b->linearVelocity.x;
+		sv[4 * a + 1] = b->linearVelocity.y;
+		sv[4 * a + 2] = b->angularVelocity;
+		sv[4 * a + 3] = flBits;
+		sd[4 * a + 2] = 1.0f;
+		params[8 * a + 0] = 0.0f; /* force.x */
+		params[8 * a + 1] = 0.0f; /* force.y */
+		params[8 * a + 2] = 0.0f; /* torque */
+		params[8 * a + 3] = b->linearDamping;
+		params[8 * a + 4] = b->angularDamping;
+		params[8 * a + 5] = b->gravityScale;
+		params[8 * a + 6] = b->invMass;
+		params[8 * a + 7] = b->invInertia;
+		c0[4 * a] = b->center.x;
+		c0[4 * a + 1] = b->center.y;
+		c0[4 * a + 2] = b->transform.q.c;
+		c0[4 * a + 3] = b->transform.q.s;
+	}
+	b2gShape* shapes = calloc( nsc, sizeof( b2gShape ) );
+	float* aabbs = calloc( nsc * 4, sizeof( float ) );
+	float* fats = calloc( nsc * 4, sizeof( float ) );
+	for ( int i = 0; i < ns; ++i )
+	{
+		h_shape* s = w->shapes.data + i;
+		b2gShape* d = shapes + i;
+		if ( s->id != i )
+		{
+			d->type = -1;
+			continue;
+		}
+		d->type = s->type;
+		d->bodyId = s->bodyId;
+		d->enableHitEvents = s->enableHitEvents;
+		switch ( s->type )
+		{
+			case b2_circleShape:
+				d->v[0] = s->circle.center;
+				d->radius = s->circle.radius;
+				d->count = 1;
+				break;
+			case b2_capsuleShape:
+				d->v[0] = s->capsule.center1;
+				d->v[1] = s->capsule.center2;
+				d->radius = s->capsule.radius;
+				d->count = 2;
+				break;
+			case b2_segmentShape:
+				d->v[0] = s->segment.point1;
+				d->v[1] = s->segment.point2;
+				d->count = 2;
+				break;
+			case b2_polygonShape:
+				memcpy( d->v, s->polygon.vertices, sizeof( d->v ) );
+				memcpy( d->n, s->polygon.normals, sizeof( d->n ) );
+				d->centroid = s->polygon.centroid;
+				d->radius = s->polygon.radius;
+				d->count = s->polygon.count;
+				break;
+			default:
+				break;
+		}
+		d->aabbMargin = s->aabbMargin;
+		d->friction = s->material.friction;
+		d->restitution = s->material.restitution;
+		d->rollingResistance = s->material.rollingResistance;
+		d->tangentSpeed = s->material.tangentSpeed;
+		aabbs[4 * i] = s->aabb.lowerBound.x;
+		aabbs[4 * i + 1] = s->aabb.lowerBound.y;
+		aabbs[4 * i + 2] = s->aabb.upperBound.x;
+		aabbs[4 * i + 3] = s->aabb.upperBound.y;
+		fats[4 * i] = s->fatAABB.lowerBound.x;
+		fats[4 * i + 1] = s->fatAABB.lowerBound.y;
+		fats[4 * i + 2] = s->fatAABB.upperBound.x;
+		fats[4 * i + 3] = s->fatAABB.upperBound.y;
+	}
+	int rc = b2gDev_UploadBodies( w->dev, nb, xf, center, localCenter, invMass, invI, minExtent, maxExtent, sleepThreshold, safetyFactor,
+								  awakeIndex, typeFlags,
+								  shapeStart, shapeCount, shapeList, listCount );
+	if ( rc == 0 ) rc = b2gDev_UploadAwake( w->dev, na, awakeBodyId, sv, sd, params, c0 );
+	if ( rc == 0 ) rc = b2gDev_UploadShapes( w->dev, shapes, aabbs, fats, ns );
+	if ( rc != 0 ) h_fail( w, "device upload", rc );
+	free( xf );
+	free( center );
+	free( localCenter );
+	free( invMass );
+	free( invI );
+	free( minExtent );
+	free( maxExtent );
+	free( sleepThreshold );
+	free( safetyFactor );
+	free( awakeIndex );
+	free( typeFlags );
+	free( shapeStart );
+	free( shapeCount );
+	free( shapeList );
+	free( sv );
+	free( sd );
+	free( params );
+	free( c0 );
+	free( shapes );
+	free( aabbs );
+	free( fats );
+	w->jointsDirty = 1;
+	w->treesDirty = 1;
+	w->colorsDirty = 1;
+	w->devReady = 1;
+}
+
+/* ---------------- bodies (body.c:174-330, :524-650) ---------------- */
+static h_body* h_getBody( b2BodyId id ) { return h_worlds[id.world0].bodies.data + ( id.index1 - 1 ); }
+
+b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
+{
+	h_world* w = h_worldFromId( worldId );
+	b2BodyId nullId = { 0, 0, 0 };
+	if ( w == NULL || w->locked ) return nullId;
+	h_markHostChanged( w );
+	int bodyId = h_allocId( &w->bodyIdPool );
+	if ( bodyId == w->bodies.count )
+	{
+		h_body z;
+		memset( &z, 0, sizeof( z ) );
+		h_push( w->bodies, z );
+	}
+	h_body* b = w->bodies.data + bodyId;
+	uint16_t generation = b->generation;
+	memset( b, 0, sizeof( *b ) );
+	uint32_t flags = 0;
+	flags |= def->motionLocks.linearX ? B2G_LOCK_X : 0;
+	flags |= def->motionLocks.linearY ? B2G_LOCK_Y : 0;
+	flags |= def->motionLocks.angularZ ? B2G_LOCK_Z : 0;
+	flags |= def->isBullet ? B2G_IS_BULLET : 0;
+	flags |= def->allowFastRotation ? B2G_ALLOW_FAST_ROTATION : 0;
+	flags |= def->type == b2_dynamicBody ? B2G_DYNAMIC_FLAG : 0;
+	flags |= def->enableSleep ? B2G_ENABLE_SLEEP : 0;
+	flags |= def->enableContactRecycling ? B2G_ENABLE_RECYCLING : 0;
+	b->transform.p = def->position;
+	b->transform.q = def->rotation;
+	b->center = def->position;
+	b->minExtent = H_HUGE;
+	b->maxExtent = 0.0f;
+	b->linearDamping = def->linearDamping;
+	b->angularDamping = def->angularDamping;
+	b->gravityScale = def->gravityScale;
+	b->simFlags = flags;
+	b->linearVelocity = def->linearVelocity;
+	b->angularVelocity = def->angularVelocity;
+	b->userData = def->userData;
+	if ( def->type == b2_staticBody )
+	{
+		b->setIndex = H_STATIC_SET;
+		b->localIndex = w->staticCount++;
+	}
+	else
+	{
+		b->setIndex = H_AWAKE_SET;
+		b->localIndex = w->awakeBodyIds.count;
+		h_push( w->awakeBodyIds, bodyId );
+	}
+	b->generation = generation + 1;
+	b->headShapeId = B2_NULL_INDEX;
+	b->headContactKey = B2_NULL_INDEX;
+	b->headJointKey = B2_NULL_INDEX;
+	b->id = bodyId;
+	b->sleepThreshold = def->sleepThreshold;
+	b->safetyFactor = def->safetyFactor;
+	b->type = def->type;
+	b->flags = flags;
+	b2BodyId id = { bodyId + 1, w->worldId, b->generation };
+	return id;
+}
+
+bool b2Body_IsValid( b2BodyId id )
+{
+	if ( id.world0 >= H_MAX_WORLDS ) return false;
+	h_world* w = h_worlds + id.world0;
+	if ( w->inUse == 0 || id.index1 < 1 || id.index1 > w->bodies.count ) return false;
+	h_body* b = w->bodies.data + id.index1 - 1;
+	return b->id == id.index1 - 1 && b->generation == id.generation;
+}
+
+b2BodyType b2Body_GetType( b2BodyId bodyId ) { return h_getBody( bodyId )->type; }
+
+b2WorldTransform b2Body_GetTransform( b2BodyId bodyId )
+{
+	h_syncFromDevice( h_worlds + bodyId.world0 );
+	return h_getBody( bodyId )->transform;
+}
+
+b2Pos b2Body_GetPosition( b2BodyId bodyId ) { return b2Body_GetTransform( bodyId ).p; }
+
+b2Rot b2Body_GetRotation( b2BodyId bodyId ) { return b2Body_GetTransform( bodyId ).q; }
+
+b2Vec2 b2Body_GetLocalPoint( b2BodyId bodyId, b2Pos worldPoint )
+{
+	return h_invTransformPoint( b2Body_GetTransform( bodyId ), worldPoint );
+}
+
+b2Pos b2Body_GetWorldPoint( b2BodyId bodyId, b2Vec2 localPoint )
+{
+	return h_transformWorldPoint( b2Body_GetTransform( bodyId ), localPoint );
+}
+
+b2Vec2 b2Body_GetLinearVelocity( b2BodyId bodyId )
+{
+	h_syncFromDevice( h_worlds + bodyId.world0 );
+	h_body* b = h_getBody( bodyId );
+	return b->setIndex == H_AWAKE_SET ? b->linearVelocity : h_v( 0.0f, 0.0f );
+}
+
+float b2Body_GetAngularVelocity( b2BodyId bodyId )
+{
+	h_syncFromDevice( h_worlds + bodyId.world0 );
+	h_body* b = h_getBody( bodyId );
+	return b->setIndex == H_AWAKE_SET ? b->angularVelocity : 0.0f;
+}
+
+/* body.c:790-840: the new velocity goes to the host record and straight to the device */
+void b2Body_SetLinearVelocity( b2BodyId bodyId, b2Vec2 v )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( b->type == b2_staticBody ) return;
+	b->linearVelocity = v;
+	if ( w->devReady )
+	{
+		int rc = b2gDev_SetBodyVelocity( w->dev, b->localIndex, v.x, v.y, 0.0f, 1 );
+		if ( rc != 0 ) h_fail( w, "set velocity", rc );
+	}
+}
+
+void b2Body_SetAngularVelocity( b2BodyId bodyId, float av )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( b->type == b2_staticBody ) return;
+	b->angularVelocity = av;
+	if ( w->devReady )
+	{
+		int rc = b2gDev_SetBodyVelocity( w->dev, b->localIndex, 0.0f, 0.0f, av, 2 );
+		if ( rc != 0 ) h_fail( w, "set velocity", rc );
+	}
+}
+
+float b2Body_GetMass( b2BodyId bodyId ) { return h_getBody( bodyId )->mass; }
+
+float b2Body_GetRotationalInertia( b2BodyId bodyId ) { return h_getBody( bodyId )->inertia; }
+
+b2Vec2 b2Body_GetLocalCenterOfMass( b2BodyId bodyId ) { return h_getBody( bodyId )->localCenter; }
+
+b2Pos b2Body_GetWorldCenterOfMass( b2BodyId bodyId )
+{
+	h_syncFromDevice( h_worlds + bodyId.world0 );
+	return h_getBody( bodyId )->center;
+}
+
+bool b2Body_IsAwake( b2BodyId bodyId ) { return h_getBody( bodyId )->setIndex == H_AWAKE_SET; }
+
+/* body.c:524-650 */
+static void h_updateBodyMassData( h_world* w, h_body* body )
+{
+	body->flags &= ~B2G_DIRTY_MASS;
+	body->mass = 0.0f;
+	body->inertia = 0.0f;
+	body->invMass = 0.0f;
+	body->invInertia = 0.0f;
+	body->localCenter = h_v( 0.0f, 0.0f );
+	body->minExtent = H_HUGE;
+	body->maxExtent = 0.0f;
+	if ( body->type != b2_dynamicBody )
+	{
+		body->center = body->transform.p;
+		if ( body->type == b2_kinematicBody )
+		{
+			int sid = body->headShapeId;
+			while ( sid != B2_NULL_INDEX )
+			{
+				const h_shape* s = w->shapes.data + sid;
+				float mn, mx;
+				h_computeShapeExtent( s, h_v( 0.0f, 0.0f ), &mn, &mx );
+				body->minExtent = h_min( body->minExtent, mn );
+				body->maxExtent = h_max( body->maxExtent, mx );
+				sid = s->nextShapeId;
+			}
+		}
+		return;
+	}
+	int shapeCount = body->shapeCount;
+	b2MassData* masses = calloc( (size_t)( shapeCount > 0 ? shapeCount : 1 ), sizeof( b2MassData ) );
+	b2Vec2 localCenter = h_v( 0.0f, 0.0f );
+	int sid = body->headShapeId;
+	int si = 0;
+	while ( sid != B2_NULL_INDEX )
+	{
+		const h_shape* s = w->shapes.data + sid;
+		sid = s->nextShapeId;
+		if ( s->density == 0.0f )
+		{
+			si += 1;
+			continue;
+		}
+		b2MassData md = h_computeShapeMass( s );
+		body->mass += md.mass;
+		localCenter = h_mulAdd( localCenter, md.mass, md.center );
+		masses[si++] = md;
+	}
+	if ( body->mass > 0.0f )
+	{
+		body->invMass = 1.0f / body->mass;
+		localCenter = h_mulSV( body->invMass, localCenter );
+	}
+	for ( si = 0; si < shapeCount; ++si )
+	{
+		b2MassData md = masses[si];
+		if ( md.mass == 0.0f ) continue;
+		b2Vec2 offset = h_sub( localCenter, md.center );
+		float inertia = md.rotationalInertia + md.mass * h_dot( offset, offset );
+		body->inertia += inertia;
+	}
+	free( masses );
+	if ( body->inertia > 0.0f && ( body->flags & B2G_LOCK_Z ) == 0 )
+	{
+		body->invInertia = 1.0f / body->inertia;
+	}
+	else
+	{
+		body->inertia = 0.0f;
+		body->invInertia = 0.0f;
+	}
+	b2Vec2 oldCenter = body->center;
+	body->localCenter = localCenter;
+	body->center = h_transformWorldPoint( body->transform, body->localCenter );
+	if ( body->setIndex == H_AWAKE_SET )
+	{
+		b2Vec2 dl = h_crossSV( body->angularVelocity, h_sub( body->center, oldCenter ) );
+		body->linearVelocity = h_add( body->linearVelocity, dl );
+	}
+	sid = body->headShapeId;
+	while ( sid != B2_NULL_INDEX )
+	{
+		const h_shape* s = w->shapes.data + sid;
+		float mn, mx;
+		h_computeShapeExtent( s, localCenter, &mn, &mx );
+		body->minExtent = h_min( body->minExtent, mn );
+		body->maxExtent = h_max( body->maxExtent, mx );
+		sid = s->nextShapeId;
+	}
+}
+
+/* ---------------- move buffer (broad_phase.h:70-80) ---------------- */
+void h_bufferMove( h_world* w, int proxyKey )
+{
+	int type = H_PROXY_TYPE( proxyKey );
+	int id = H_PROXY_ID( proxyKey );
+	if ( h_bitGet( w->movedProxies + type, id ) == 0 )
+	{
+		h_bitSet1( w->movedProxies + type, id );
+		h_push( w->moveArray, proxyKey );
+	}
+}
+
+/* ---------------- shapes (shape.c:85-270, :1034-1044) ---------------- */
+static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const void* geometry, b2ShapeType type )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_markHostChanged( w );
+	h_body* body = h_getBody( bodyId );
+	b2Transform transform = body->transform;
+	int shapeId = h_allocId( &w->shapeIdPool );
+	if ( shapeId == w->shapes.count )
+	{
+		h_shape z;
+		memset( &z, 0, sizeof( z ) );
+		h_push( w->shapes, z );
+	}
+	h_shape* s = w->shapes.data + shapeId;
+	uint16_t generation = s->generation;
+	memset( s, 0, sizeof( *s ) );
+	switch ( type )
+	{
+		case b2_capsuleShape: s->capsule = *(const b2Capsule*)geometry; break;
+		case b2_circleShape: s->circle = *(const b2Circle*)geometry; break;
+		case b2_polygonShape: s->polygon = *(const b2Polygon*)geometry; break;
+		case b2_segmentShape: s->segment = *(const b2Segment*)geometry; break;
+		default: break;
+	}
+	s->id = shapeId;
+	s->bodyId = body->id;
+	s->type = type;
+	s->density = def->density;
+	s->material = def->material;
+	s->filter = def->filter;
+	s->userData = def->userData;
+	s->enableContactEvents = def->enableContactEvents;
+	s->enableHitEvents = def->enableHitEvents;
+	s->isSensor = def->isSensor;
+	s->proxyKey = B2_NULL_INDEX;
+	s->localCentroid = h_getShapeCentroid( s );
+	s->aabbMargin = h_computeShapeMargin( s );
+	s->generation = generation + 1;
+	{
+		b2BodyType proxyType = body->type;
+		b2AABB aabb = h_computeFatShapeAABB( s, transform, H_SPECULATIVE_DISTANCE );
+		s->aabb = aabb;
+		float margin = proxyType == b2_staticBody ? H_SPECULATIVE_DISTANCE : s->aabbMargin;
+		b2AABB fat = { { aabb.lowerBound.x - margin, aabb.lowerBound.y - margin },
+					   { aabb.upperBound.x + margin, aabb.upperBound.y + margin } };
+		s->fatAABB = fat;
+		int proxyId = h_treeCreateProxy( w->trees + proxyType, s->fatAABB, s->filter.categoryBits, (uint64_t)shapeId );
+		s->proxyKey = H_PROXY_KEY( proxyId, proxyType );
+		if ( proxyType != b2_staticBody || def->invokeContactCreation || def->isSensor ) h_bufferMove( w, s->proxyKey );
+		w->treesDirty = 1;
+	}
+	if ( body->headShapeId != B2_NULL_INDEX ) w->shapes.data[body->headShapeId].prevShapeId = shapeId;
+	s->prevShapeId = B2_NULL_INDEX;
+	s->nextShapeId = body->headShapeId;
+	body->headShapeId = shapeId;
+	body->shapeCount += 1;
+	if ( def->updateBodyMass ) h_updateBodyMassData( w, body );
+	else body->flags |= B2G_DIRTY_MASS;
+	b2ShapeId id = { s->id + 1, bodyId.world0, s->generation };
+	return id;
+}
+
+b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Circle* circle )
+{
+	return h_createShape( bodyId, def, circle, b2_circleShape );
+}
+
+b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Capsule* capsule )
+{
+	if ( h_distanceSq( capsule->center1, capsule->center2 ) <= H_LINEAR_SLOP * H_LINEAR_SLOP )
+	{
+		b2ShapeId nullId = { 0, 0, 0 };
+		return nullId;
+	}
+	return h_createShape( bodyId, def, capsule, b2_capsuleShape );
+}
+
+b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon )
+{
+	return h_createShape( bodyId, def, polygon, b2_polygonShape );
+}
+
+b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Segment* segment )
+{
+	if ( h_distanceSq( segment->point1, segment->point2 ) <= H_LINEAR_SLOP * H_LINEAR_SLOP )
+	{
+		b2ShapeId nullId = { 0, 0, 0 };
+		return nullId;
+	}
+	return h_createShape( bodyId, def, segment, b2_segmentShape );
+}
+
+void b2Shape_SetFriction( b2ShapeId shapeId, float friction )
+{
+	h_world* w = h_worlds + shapeId.world0;
+	h_markHostChanged( w );
+	w->shapes.data[shapeId.index1 - 1].material.friction = friction;
+}
+
+float b2Shape_GetFriction( b2ShapeId shapeId )
+{
+	return h_worlds[shapeId.world0].shapes.data[shapeId.index1 - 1].material.friction;
+}
+
+/* ---------------- contact register table (contact.c:188-206) ---------------- */
+/* shape types: circle 0, capsule 1, segment 2, polygon 3 */
+int h_canCollide( b2ShapeType a, b2ShapeType b )
+{
+	if ( (int)a > 3 || (int)b > 3 ) return 0;
+	return !( a == b2_segmentShape && b == b2_segmentShape );
+}
+
+int h_isPrimary( b2ShapeType a, b2ShapeType b )
+{
+	static const int prim[4][4] = {
+		{ 1, 0, 0, 0 },
+		{ 1, 1, 0, 0 },
+		{ 1, 1, 0, 1 },
+		{ 1, 1, 0, 1 },
+	};
+	if ( (int)a > 3 || (int)b > 3 ) return 0;
+	return prim[a][b];
+}
+
+/* ---------------- contacts (contact.c:214-501) ---------------- */
+void h_createContact( h_world* w, h_shape* shapeA, h_shape* shapeB )
+{
+	if ( h_canCollide( shapeA->type, shapeB->type ) == 0 ) return;
+	if ( h_isPrimary( shapeA->type, shapeB->type ) == 0 )
+	{
+		h_createContact( w, shapeB, shapeA );
+		return;
+	}
+	h_body* bodyA = w->bodies.data + shapeA->bodyId;
+	h_body* bodyB = w->bodies.data + shapeB->bodyId;
+	int contactId = h_allocId( &w->contactIdPool );
+	if ( contactId == w->contacts.count )
+	{
+		h_contact z;
+		memset( &z, 0, sizeof( z ) );
+		h_push( w->contacts, z );
+	}
+	h_contact* c = w->contacts.data + contactId;
+	c->contactId = contactId;
+	c->generation += 1;
+	c->setIndex = H_AWAKE_SET;
+	c->colorIndex = B2_NULL_INDEX;
+	c->localIndex = w->awakeContactIds.count;
+	c->shapeIdA = shapeA->id;
+	c->shapeIdB = shapeB->id;
+	c->flags = 0;
+	if ( ( bodyA->flags & B2G_ENABLE_RECYCLING ) && ( bodyB->flags & B2G_ENABLE_RECYCLING ) ) c->flags |= B2G_C_RECYCLE;
+	if ( shapeA->enableContactEvents || shapeB->enableContactEvents ) c->flags |= B2G_C_ENABLE_EVENTS;
+	{
+		c->edges[0].bodyId = shapeA->bodyId;
+		c->edges[0].prevKey = B2_NULL_INDEX;
+		c->edges[0].nextKey = bodyA->headContactKey;
+		int keyA = ( contactId << 1 ) | 0;
+		int head = bodyA->headContactKey;
+		if ( head != B2_NULL_INDEX ) w->contacts.data[head >> 1].edges[head & 1].prevKey = keyA;
+		bodyA->headContactKey = keyA;
+		bodyA->contactCount += 1;
+	}
+	{
+		c->edges[1].bodyId = shapeB->bodyId;
+		c->edges[1].prevKey = B2_NULL_INDEX;
+		c->edges[1].nextKey = bodyB->headContactKey;
+		int keyB = ( contactId << 1 ) | 1;
+		int head = bodyB->headContactKey;
+		if ( head != B2_NULL_INDEX ) w->contacts.data[head >> 1].edges[head & 1].prevKey = keyB;
+		bodyB->headContactKey = keyB;
+		bodyB->contactCount += 1;
+	}
+	h_pairSetAdd( &w->pairSet, H_SHAPE_PAIR_KEY( shapeA->id, shapeB->id ) );
+	h_push( w->awakeContactIds, contactId );
+	b2gContactInit init;
+	init.contactId = contactId;
+	init.shapeIdA = shapeA->id;
+	init.shapeIdB = shapeB->id;
+	init.simFlags = c->flags;
+	init.friction = sqrtf( shapeA->material.friction * shapeB->material.friction );
+	init.restitution = h_max( shapeA->material.restitution, shapeB->material.restitution );
+	h_push( w->pendingInits, init );
+}
+
+static void h_removeNonTouchingContact( h_world* w, int localIndex )
+{
+	int moved = h_removeSwap( w->awakeContactIds, localIndex );
+	if ( moved != B2_NULL_INDEX ) w->contacts.data[w->awakeContactIds.data[localIndex]].localIndex = localIndex;
+}
+
+void h_destroyContact( h_world* w, h_contact* c )
+{
+	h_pairSetRemove( &w->pairSet, H_SHAPE_PAIR_KEY( c->shapeIdA, c->shapeIdB ) );
+	h_contactEdge* eA = c->edges + 0;
+	h_contactEdge* eB = c->edges + 1;
+	int bodyIdA = eA->bodyId, bodyIdB = eB->bodyId;
+	h_body* bodyA = w->bodies.data + bodyIdA;
+	h_body* bodyB = w->bodies.data + bodyIdB;
+	uint32_t flags = c->flags;
+	if ( ( flags & B2G_C_TOUCHING ) && ( flags & B2G_C_ENABLE_EVENTS ) )
+	{
+		const h_shape* sA = w->shapes.data + c->shapeIdA;
+		const h_shape* sB = w->shapes.data + c->shapeIdB;
+		b2ContactEndTouchEvent ev;
+		memset( &ev, 0, sizeof( ev ) );
+		ev.shapeIdA.index1 = sA->id + 1;
+		ev.shapeIdA.world0 = w->worldId;
+		ev.shapeIdA.generation = sA->generation;
+		ev.shapeIdB.index1 = sB->id + 1;
+		ev.shapeIdB.world0 = w->worldId;
+		ev.shapeIdB.generation = sB->generation;
+		ev.contactId.index1 = c->contactId + 1;
+		ev.contactId.world0 = w->worldId;
+		ev.contactId.generation = c->generation;
+		h_push( w->endEvents[w->endEventArrayIndex], ev );
+	}
+	if ( eA->prevKey != B2_NULL_INDEX ) w->contacts.data[eA->prevKey >> 1].edges[eA->prevKey & 1].nextKey = eA->nextKey;
+	if ( eA->nextKey != B2_NULL_INDEX ) w->contacts.data[eA->nextKey >> 1].edges[eA->nextKey & 1].prevKey = eA->prevKey;
+	int contactId = c->contactId;
+	if ( bodyA->headContactKey == ( ( contactId << 1 ) | 0 ) ) bodyA->headContactKey = eA->nextKey;
+	bodyA->contactCount -= 1;
+	if ( eB->prevKey != B2_NULL_INDEX ) w->contacts.data[eB->prevKey >> 1].edges[eB->prevKey & 1].nextKey = eB->nextKey;
+	if ( eB->nextKey != B2_NULL_INDEX ) w->contacts.data[eB->nextKey >> 1].edges[eB->nextKey & 1].prevKey = eB->prevKey;
+	if ( bodyB->headContactKey == ( ( contactId << 1 ) | 1 ) ) bodyB->headContactKey = eB->nextKey;
+	bodyB->contactCount -= 1;
+	if ( c->colorIndex != B2_NULL_INDEX ) h_removeContactFromGraph( w, bodyIdA, bodyIdB, c->colorIndex, c->localIndex );
+	else h_removeNonTouchingContact( w, c->localIndex );
+	c->contactId = B2_NULL_INDEX;
+	c->setIndex = B2_NULL_INDEX;
+	c->colorIndex = B2_NULL_INDEX;
+	c->localIndex = B2_NULL_INDEX;
+	h_freeId( &w->contactIdPool, contactId );
+	h_push( w->pendingKills, contactId );
+}
+
+/* ---------------- graph coloring (constraint_graph.c:66-291) ---------------- */
+void h_addContactToGraph( h_world* w, h_contact* contact )
+{
+	int colorIndex = B2G_OVERFLOW_INDEX;
+	int bodyIdA = contact->edges[0].bodyId, bodyIdB = contact->edges[1].bodyId;
+	b2BodyType typeA = w->bodies.data[bodyIdA].type, typeB = w->bodies.data[bodyIdB].type;
+	if ( typeA == b2_dynamicBody && typeB == b2_dynamicBody )
+	{
+		for ( int i = 0; i < B2_GRAPH_COLOR_COUNT - 4; ++i )
+		{
+			h_color* color = w->colors + i;
+			if ( h_bitGet( &color->bodySet, bodyIdA ) || h_bitGet( &color->bodySet, bodyIdB ) ) continue;
+			h_bitSet1( &color->bodySet, bodyIdA );
+			h_bitSet1( &color->bodySet, bodyIdB );
+			colorIndex = i;
+			break;
+		}
+	}
+	else if ( typeA == b2_dynamicBody )
+	{
+		for ( int i = B2G_OVERFLOW_INDEX - 1; i >= 1; --i )
+		{
+			h_color* color = w->colors + i;
+			if ( h_bitGet( &color->bodySet, bodyIdA ) ) continue;
+			h_bitSet1( &color->bodySet, bodyIdA );
+			colorIndex = i;
+			break;
+		}
+	}
+	else if ( typeB == b2_dynamicBody )
+	{
+		for ( int i = B2G_OVERFLOW_INDEX - 1; i >= 1; --i )
+		{
+			h_color* color = w->colors + i;
+			if ( h_bitGet( &color->bodySet, bodyIdB ) ) continue;
+			h_bitSet1( &color->bodySet, bodyIdB );
+			colorIndex = i;
+			break;
+		}
+	}
+	h_color* color = w->colors + colorIndex;
+	contact->colorIndex = colorIndex;
+	contact->localIndex = color->contactIds.count;
+	h_push( color->contactIds, contact->contactId );
+	w->colorsDirty = 1;
+}
+
+void h_removeContactFromGraph( h_world* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex )
+{
+	h_color* color = w->colors + colorIndex;
+	if ( colorIndex != B2G_OVERFLOW_INDEX )
+	{
+		h_bitClear( &color->bodySet, bodyIdA );
+		h_bitClear( &color->bodySet, bodyIdB );
+	}
+	int moved = h_removeSwap( color->contactIds, localIndex );
+	if ( moved != B2_NULL_INDEX ) w->contacts.data[color->contactIds.data[localIndex]].localIndex = localIndex;
+	w->colorsDirty = 1;
+}
+
+int h_assignJointColor( h_world* w, int bodyIdA, int bodyIdB, b2BodyType typeA, b2BodyType typeB )
+{
+	if ( typeA == b2_dynamicBody && typeB == b2_dynamicBody )
+	{
+		for ( int i = 0; i < B2_GRAPH_COLOR_COUNT - 4; ++i )
+		{
+			h_color* color = w->colors + i;
+			if ( h_bitGet( &color->bodySet, bodyIdA ) || h_bitGet( &color->bodySet, bodyIdB ) ) continue;
+			h_bitSet1( &color->bodySet, bodyIdA );
+			h_bitSet1( &color->bodySet, bodyIdB );
+			return i;
+		}
+	}
+	else if ( typeA == b2_dynamicBody )
+	{
+		for ( int i = B2G_OVERFLOW_INDEX - 1; i >= 1; --i )
+		{
+			h_color* color = w->colors + i;
+			if ( h_bitGet( &color->bodySet, bodyIdA ) ) continue;
+			h_bitSet1( &color->bodySet, bodyIdA );
+			return i;
+		}
+	}
+	else if ( typeB == b2_dynamicBody )
+	{
+		for ( int i = B2G_OVERFLOW_INDEX - 1; i >= 1; --i )
+		{
+			h_color* color = w->colors + i;
+			if ( h_bitGet( &color->bodySet, bodyIdB ) ) continue;
+			h_bitSet1( &color->bodySet, bodyIdB );
+			return i;
+		}
+	}
+	return B2G_OVERFLOW_INDEX;
+}
+
+/* body.c:2076-2110 */
+int h_shouldBodiesCollide( h_world* w, h_body* bodyA, h_body* bodyB )
+{
+	if ( bodyA->type != b2_dynamicBody && bodyB->type != b2_dynamicBody ) return 0;
+	int jointKey, otherBodyId;
+	if ( bodyA->jointCount < bodyB->jointCount )
+	{
+		jointKey = bodyA->headJointKey;
+		otherBodyId = bodyB->id;
+	}
+	else
+	{
+		jointKey = bodyB->headJointKey;
+		otherBodyId = bodyA->id;
+	}
+	while ( jointKey != B2_NULL_INDEX )
+	{
+		int jointId = jointKey >> 1;
+		int edgeIndex = jointKey & 1;
+		h_joint* j = w->joints.data + jointId;
+		if ( j->collideConnected == 0 && j->edges[edgeIndex ^ 1].bodyId == otherBodyId ) return 0;
+		jointKey = j->edges[edgeIndex].nextKey;
+	}
+	return 1;
+}
