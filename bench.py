@@ -1,0 +1,268 @@
+"""Benchmark of the GB300 Box2D step: body-steps/s on one GB300.
+
+Workload (default): many pyramids with rain -- a 20x20 grid of 10-row pyramids of 0.5 m
+boxes (22000 dynamic bodies) plus 2000 falling circles, dt 1/60 s, 4 substeps, float32.
+One timed "step" is one b2World_Step of that world. Inputs (the world) are resident on the
+device when the timed region starts; each timed step is bracketed by CUDA events on the
+library's stream, and L2 is flushed (a 256 MiB write) between timed steps, outside them.
+
+`value` = dynamic bodies x timed steps / summed device-timed step time, all ranks.
+`e2e`   = the same metric with, per step, b2World_Step followed by the body move-event read
+          (every awake body transform copied to host), wall-clocked; the byte counts are the
+          library's own host<->device traffic plus the move events.
+`roofline` is for the solver (constraint preparation through impulse storage), the
+dominant device stage: algorithmic bytes from the reference data layout
+(S*(120 Nb + 708 Nc + 604 Nj) + 364 Nc per step; +260 Nc with restitution) over its
+CUDA-event time, against the measured HBM copy bandwidth.
+`cpu_baseline` times the CPU oracle (a serial restatement of the reference step) on a
+bounded sample of the same workload on this machine's host.
+
+--impl reference runs that CPU step alone with the same line format.
+Multi-GPU: independent replicas per rank (the step of one world does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import box2d_gb300 as B  # noqa: E402
+
+WORKLOADS = {
+    # name: (kind, a, b, c, seed, flags, description)
+    "many_pyramids": (B.MANY_PYRAMIDS_RAIN, 20, 10, 2000, 0, B.NO_CONTINUOUS,
+                      "20x20 grid of 10-row pyramids of 0.5 m boxes + 2000 rain circles"),
+    "large_pyramid": (B.LARGE_PYRAMID, 100, 1, 0, 0, 0, "100-row pyramid of 5050 boxes on a 200 m segment"),
+    "joint_grid": (B.JOINT_GRID_MIXED, 100, 3000, 0, 0, B.NO_CONTINUOUS,
+                   "100x100 revolute circle grid + 3000 mixed shapes"),
+}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.summary = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=5)
+        rows = [r.split(",") for r in out.strip().splitlines() if r.strip()]
+        sm = [float(r[1]) for r in rows if len(r) > 2 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 2 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                    reasons.add(name)
+        self.summary = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                        "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def algorithmic_bytes(counters: np.ndarray, awake: int, substeps: int, restitution: bool) -> float:
+    """Per-step compulsory bytes of the solver stage (solver data of the reference)."""
+    colors = counters[4:28]
+    joints = int(counters[3])
+    nc = int(colors.sum()) - joints
+    b = substeps * (120 * awake + 708 * nc + 604 * joints) + 364 * nc
+    if restitution:
+        b += 260 * nc
+    return float(b)
+
+
+def run_gpu(args, rank: int, world_size: int) -> dict:
+    import torch
+
+    dev = rank % max(1, torch.cuda.device_count())
+    torch.cuda.set_device(dev)
+    kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
+    lib = B.load_library()
+    scene = B.Scene(lib, kind, a, b, c, seed, flags)
+    dyn = scene.dynamic_count
+    stream = torch.cuda.ExternalStream(lib.b2p_stream(scene.world_id))
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        scene.step()
+    torch.cuda.synchronize()
+    scene.timings(reset=True)
+    counters_before = scene.counters()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    solver_ms = 0.0
+    alg_bytes = 0.0
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clocks:
+        for k in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            starts[k].record(stream)
+            scene.step()
+            ends[k].record(stream)
+            alg_bytes += algorithmic_bytes(scene.counters(), dyn, 4, False)
+        torch.cuda.synchronize()
+    if world_size > 1:
+        torch.distributed.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    stage_ms, traffic = scene.timings(reset=True)
+    total_ms = float(sum(step_ms))
+    solver_ms = float(stage_ms[2])
+    launches = int(traffic[2])
+
+    # end to end: step + read every transform back through the public API, wall clock
+    scene.timings(reset=True)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 200))
+    move_bytes = 0
+    for _ in range(e2e_steps):
+        scene.step()
+        st = scene.state()
+        move_bytes += st.nbytes
+    e2e_s = time.perf_counter() - t0
+    _, e2e_traffic = scene.timings(reset=True)
+    counters = scene.counters()
+    scene.close()
+    pk = peaks()
+    achieved = alg_bytes / (solver_ms * 1e-3) / 1e9 if solver_ms > 0 else 0.0
+    return {
+        "total_ms": total_ms, "step_ms": step_ms, "dyn": dyn, "solver_ms": solver_ms, "alg_bytes": alg_bytes,
+        "achieved_gbs": achieved, "peak": pk, "launches": launches, "clocks": clocks.summary,
+        "e2e_value": dyn * e2e_steps / e2e_s, "e2e_h2d": float(e2e_traffic[0]) / e2e_steps,
+        "e2e_d2h": float(e2e_traffic[1] + move_bytes) / e2e_steps, "counters": counters.tolist(),
+        "stage_ms": stage_ms.tolist(), "desc": desc, "counters_before": counters_before.tolist(),
+    }
+
+
+def run_cpu_sample(args, budget_s: float, max_steps: int) -> dict:
+    """The oracle (serial CPU restatement of the reference step) on the same workload."""
+    kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
+    lib = B.load_library(ROOT / "oracle" / "liboracle.so")
+    scene = B.Scene(lib, kind, a, b, c, seed, flags)
+    for _ in range(max(1, args.warmup)):
+        scene.step()
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps and time.perf_counter() - t0 < budget_s:
+        scene.step()
+        n += 1
+    dt = time.perf_counter() - t0
+    dyn = scene.dynamic_count
+    scene.close()
+    return {"value": dyn * n / dt, "steps": n, "seconds": dt, "dyn": dyn}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="many_pyramids", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
+    config = {"workload": args.workload, "description": desc, "dt": 1.0 / 60.0, "substeps": 4,
+              "continuous": not bool(flags & B.NO_CONTINUOUS), "sleep": False,
+              "l2": "flushed between timed steps (256 MiB write, outside the timed region)",
+              "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single world"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cores = 1
+        r = run_cpu_sample(args, budget_s=60.0, max_steps=args.steps)
+        line = {"metric": "body-steps/s", "value": r["value"], "unit": "body-steps/s", "n_gpus": args.gpus,
+                "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / max(1, r["steps"]),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded scene builders)", "config": config, "impl": "reference",
+                "cpu_baseline": {"value": r["value"], "unit": "body-steps/s", "cores": cores, "kind": "port",
+                                 "sample": f"{r['steps']} steps after {args.warmup} warm-up steps, serial C oracle"},
+                "e2e": {"value": r["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world_size > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    r = run_gpu(args, rank, world_size)
+    total_ms = r["total_ms"]
+    if world_size > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    if rank != 0:
+        return
+    value = world_size * r["dyn"] * args.steps / (total_ms * 1e-3)
+    cpu = None
+    if not args.no_cpu_baseline:
+        c = run_cpu_sample(args, budget_s=20.0, max_steps=400)
+        cpu = {"value": c["value"], "unit": "body-steps/s", "cores": 1, "kind": "port",
+               "sample": f"{c['steps']} steps ({c['seconds']:.1f} s) of the same world after warm-up, serial C oracle"}
+    pk = r["peak"]
+    line = {
+        "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene builders)", "config": config,
+        "roofline": {"bound": "hbm", "kernel": "solver (prepare..store)", "achieved": r["achieved_gbs"],
+                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": r["achieved_gbs"] / pk["hbm_gbs"],
+                     "peak_source": pk["source"], "traffic": None,
+                     "alg_bytes_per_step": r["alg_bytes"] / args.steps,
+                     "solver_ms_per_step": r["solver_ms"] / args.steps},
+        "cpu_baseline": cpu,
+        "e2e": {"value": r["e2e_value"] * world_size, "unit": "body-steps/s", "h2d_bytes_per_step": r["e2e_h2d"],
+                "d2h_bytes_per_step": r["e2e_d2h"]},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "stage_ms_per_step": [x / args.steps for x in r["stage_ms"]],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -48,6 +48,16 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2p_contacts": (c_int, [c_u32, c_p, c_int]),
         "b2p_contact_floats": (c_int, [c_u32, c_p, c_int]),
     }
+    optional = {
+        "b2p_timings": (c_int, [c_u32, c_p, c_p, c_int]),
+        "b2p_stream": (c_p, [c_u32]),
+        "b2p_status": (c_int, [c_u32]),
+    }
+    for name, (res, args) in optional.items():
+        if hasattr(lib, name):
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
         fn.restype = res
@@ -109,6 +119,14 @@ class Scene:
             if n <= cap:
                 return buf[:n]
             cap = n
+
+    def timings(self, reset: bool = False) -> tuple[np.ndarray, np.ndarray]:
+        """Accumulated device stage times (ms: pairs, narrowphase, solver, finalize) and
+        host<->device traffic (bytes: to device, to host) and kernels launched."""
+        ms = np.zeros(4, np.float32)
+        traffic = np.zeros(3, np.int64)
+        self.lib.b2p_timings(self.world_id, ms.ctypes.data, traffic.ctypes.data, int(reset))
+        return ms, traffic
 
     def counters(self) -> np.ndarray:
         out = np.zeros(30, np.int32)

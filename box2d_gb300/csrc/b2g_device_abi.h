@@ -231,7 +231,8 @@ int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* params, const int* ac
 
 /* bookkeeping for profiles */
 int b2gDev_Synchronize( b2gDeviceWorld* dw );
-void b2gDev_Timings( b2gDeviceWorld* dw, float* pairsMs, float* collideMs, float* solveMs );
+void b2gDev_Timings( b2gDeviceWorld* dw, float* stageMs, long long* traffic, int reset );
+void* b2gDev_Stream( b2gDeviceWorld* dw );
 
 #ifdef __cplusplus
 }

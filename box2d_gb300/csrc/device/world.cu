@@ -28,8 +28,10 @@
 struct b2gDeviceWorld
 {
 	cudaStream_t stream;
-	cudaEvent_t ev[8];
-	float pairsMs, collideMs, solveMs;
+	cudaEvent_t ev[10];
+	float pairsMs, collideMs, solveMs, finalizeMs; /* accumulated device time per stage */
+	long long h2dBytes, d2hBytes;				   /* accumulated host<->device traffic */
+	long long launches;							   /* kernels launched */
 	/* bodies by id */
 	int bodyCap, bodyCount;
 	float4* xf;
@@ -957,7 +959,7 @@ extern "C" int b2gDev_Create( b2gDeviceWorld** out )
 	if ( count == 0 ) return (int)cudaErrorNoDevice;
 	b2gDeviceWorld* dw = (b2gDeviceWorld*)calloc( 1, sizeof( b2gDeviceWorld ) );
 	CK( cudaStreamCreateWithFlags( &dw->stream, cudaStreamNonBlocking ) );
-	for ( int i = 0; i < 8; ++i ) CK( cudaEventCreate( dw->ev + i ) );
+	for ( int i = 0; i < 10; ++i ) CK( cudaEventCreate( dw->ev + i ) );
 	CK( cudaMalloc( &dw->counters, sizeof( b2gStepCounters ) ) );
 	CK( cudaMallocHost( &dw->hCounters, sizeof( b2gStepCounters ) ) );
 	for ( int t = 0; t < 3; ++t ) dw->treeRoot[t] = -1;
@@ -984,7 +986,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
 		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
 	free( dw->hSortTmp );
-	for ( int i = 0; i < 8; ++i ) cudaEventDestroy( dw->ev[i] );
+	for ( int i = 0; i < 10; ++i ) cudaEventDestroy( dw->ev[i] );
 	cudaStreamDestroy( dw->stream );
 	free( dw );
 }
@@ -1012,19 +1014,19 @@ extern "C" int b2gDev_UploadShapes( b2gDeviceWorld* dw, const b2gShape* shapes, 
 	dw->shapeCountTotal = count;
 	if ( count > 0 )
 	{
-		CK( cudaMemcpy( dw->shapes, shapes, (size_t)count * sizeof( b2gShape ), cudaMemcpyHostToDevice ) );
-		CK( cudaMemcpy( dw->aabb, aabbs, (size_t)count * sizeof( float4 ), cudaMemcpyHostToDevice ) );
-		CK( cudaMemcpy( dw->fat, fatAABBs, (size_t)count * sizeof( float4 ), cudaMemcpyHostToDevice ) );
+		CK( ( dw->h2dBytes += (long long)( (size_t)count * sizeof( b2gShape ) ), cudaMemcpy( dw->shapes, shapes, (size_t)count * sizeof( b2gShape ), cudaMemcpyHostToDevice ) ) );
+		CK( ( dw->h2dBytes += (long long)( (size_t)count * sizeof( float4 ) ), cudaMemcpy( dw->aabb, aabbs, (size_t)count * sizeof( float4 ), cudaMemcpyHostToDevice ) ) );
+		CK( ( dw->h2dBytes += (long long)( (size_t)count * sizeof( float4 ) ), cudaMemcpy( dw->fat, fatAABBs, (size_t)count * sizeof( float4 ), cudaMemcpyHostToDevice ) ) );
 	}
 	return 0;
 }
 
-template <typename T> static int upload( T** dptr, int* cap, const T* src, int n, int* capOut )
+template <typename T> static int upload( b2gDeviceWorld* dw, T** dptr, int* cap, const T* src, int n, int* capOut )
 {
 	int c = *cap;
 	CK2( grow( (void**)dptr, &c, n, sizeof( T ) ) );
 	*capOut = c;
-	if ( n > 0 ) CK( cudaMemcpy( *dptr, src, (size_t)n * sizeof( T ), cudaMemcpyHostToDevice ) );
+	if ( n > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( T ) ), cudaMemcpy( *dptr, src, (size_t)n * sizeof( T ), cudaMemcpyHostToDevice ) ) );
 	return 0;
 }
 
@@ -1035,29 +1037,29 @@ extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const flo
 									 const int* shapeCount, const int* shapeList, int shapeListCount )
 {
 	int cap0 = dw->bodyCap, capOut = 0;
-	CK2( upload( &dw->xf, &cap0, (const float4*)xf, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->xf, &cap0, (const float4*)xf, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->center, &cap0, (const float2*)center, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->center, &cap0, (const float2*)center, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->localCenter, &cap0, (const float2*)localCenter, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->localCenter, &cap0, (const float2*)localCenter, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->invMass, &cap0, invMass, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->invMass, &cap0, invMass, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->invI, &cap0, invI, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->invI, &cap0, invI, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->minExtent, &cap0, minExtent, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->minExtent, &cap0, minExtent, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->maxExtent, &cap0, maxExtent, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->maxExtent, &cap0, maxExtent, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->sleepThreshold, &cap0, sleepThreshold, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->sleepThreshold, &cap0, sleepThreshold, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->safetyFactor, &cap0, safetyFactor, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->safetyFactor, &cap0, safetyFactor, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->awakeIndex, &cap0, awakeIndex, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->awakeIndex, &cap0, awakeIndex, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->shapeStart, &cap0, shapeStart, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->shapeStart, &cap0, shapeStart, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
-	CK2( upload( &dw->shapeCount, &cap0, shapeCount, bodyCount, &capOut ) );
+	CK2( upload( dw, &dw->shapeCount, &cap0, shapeCount, bodyCount, &capOut ) );
 	int* type = (int*)malloc( (size_t)( bodyCount > 0 ? bodyCount : 1 ) * sizeof( int ) );
 	uint32_t* flags = (uint32_t*)malloc( (size_t)( bodyCount > 0 ? bodyCount : 1 ) * sizeof( uint32_t ) );
 	for ( int i = 0; i < bodyCount; ++i )
@@ -1066,15 +1068,15 @@ extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const flo
 		flags[i] = typeFlags[i] >> 2;
 	}
 	cap0 = dw->bodyCap;
-	int rc = upload( &dw->bodyType, &cap0, type, bodyCount, &capOut );
+	int rc = upload( dw, &dw->bodyType, &cap0, type, bodyCount, &capOut );
 	cap0 = dw->bodyCap;
-	if ( rc == 0 ) rc = upload( &dw->bodyFlags, &cap0, flags, bodyCount, &capOut );
+	if ( rc == 0 ) rc = upload( dw, &dw->bodyFlags, &cap0, flags, bodyCount, &capOut );
 	free( type );
 	free( flags );
 	if ( rc != 0 ) return rc;
 	dw->bodyCap = capOut;
 	dw->bodyCount = bodyCount;
-	CK2( upload( &dw->shapeList, &dw->shapeListCap, shapeList, shapeListCount, &dw->shapeListCap ) );
+	CK2( upload( dw, &dw->shapeList, &dw->shapeListCap, shapeList, shapeListCount, &dw->shapeListCap ) );
 	return 0;
 }
 
@@ -1082,18 +1084,18 @@ extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int
 									const float* stateD, const float* params, const float* center0 )
 {
 	int cap0 = dw->awakeCap, capOut = 0;
-	CK2( upload( &dw->awakeBodyId, &cap0, awakeBodyId, awakeCount, &capOut ) );
+	CK2( upload( dw, &dw->awakeBodyId, &cap0, awakeBodyId, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
-	CK2( upload( &dw->stateV, &cap0, (const float4*)stateV, awakeCount, &capOut ) );
+	CK2( upload( dw, &dw->stateV, &cap0, (const float4*)stateV, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
-	CK2( upload( &dw->stateD, &cap0, (const float4*)stateD, awakeCount, &capOut ) );
+	CK2( upload( dw, &dw->stateD, &cap0, (const float4*)stateD, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
-	CK2( upload( &dw->center0, &cap0, (const float4*)center0, awakeCount, &capOut ) );
+	CK2( upload( dw, &dw->center0, &cap0, (const float4*)center0, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
 	CK2( grow( (void**)&dw->enlargedBody, &cap0, awakeCount, sizeof( int ) ) );
 	int pcap = dw->awakeCap * 8;
 	CK2( grow( (void**)&dw->params, &pcap, 8 * awakeCount, sizeof( float ) ) );
-	if ( awakeCount > 0 ) CK( cudaMemcpy( dw->params, params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyHostToDevice ) );
+	if ( awakeCount > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)awakeCount * 8 * sizeof( float ) ), cudaMemcpy( dw->params, params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyHostToDevice ) ) );
 	dw->awakeCap = capOut;
 	dw->awakeCount = awakeCount;
 	return 0;
@@ -1104,10 +1106,10 @@ extern "C" int b2gDev_DownloadAwake( b2gDeviceWorld* dw, int awakeCount, float* 
 {
 	if ( awakeCount == 0 ) return 0;
 	CK( cudaStreamSynchronize( dw->stream ) );
-	CK( cudaMemcpy( stateV, dw->stateV, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
-	CK( cudaMemcpy( stateD, dw->stateD, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
-	CK( cudaMemcpy( params, dw->params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyDeviceToHost ) );
-	CK( cudaMemcpy( center0, dw->center0, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)awakeCount * sizeof( float4 ) ), cudaMemcpy( stateV, dw->stateV, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)awakeCount * sizeof( float4 ) ), cudaMemcpy( stateD, dw->stateD, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)awakeCount * 8 * sizeof( float ) ), cudaMemcpy( params, dw->params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyDeviceToHost ) ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)awakeCount * sizeof( float4 ) ), cudaMemcpy( center0, dw->center0, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
 	return 0;
 }
 
@@ -1115,9 +1117,9 @@ extern "C" int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* 
 {
 	if ( bodyCount == 0 ) return 0;
 	CK( cudaStreamSynchronize( dw->stream ) );
-	CK( cudaMemcpy( xf, dw->xf, (size_t)bodyCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
-	CK( cudaMemcpy( center, dw->center, (size_t)bodyCount * sizeof( float2 ), cudaMemcpyDeviceToHost ) );
-	CK( cudaMemcpy( flags, dw->bodyFlags, (size_t)bodyCount * sizeof( uint32_t ), cudaMemcpyDeviceToHost ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)bodyCount * sizeof( float4 ) ), cudaMemcpy( xf, dw->xf, (size_t)bodyCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)bodyCount * sizeof( float2 ) ), cudaMemcpy( center, dw->center, (size_t)bodyCount * sizeof( float2 ), cudaMemcpyDeviceToHost ) ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)bodyCount * sizeof( uint32_t ) ), cudaMemcpy( flags, dw->bodyFlags, (size_t)bodyCount * sizeof( uint32_t ), cudaMemcpyDeviceToHost ) ) );
 	return 0;
 }
 
@@ -1125,14 +1127,15 @@ extern "C" int b2gDev_DownloadShapeBoxes( b2gDeviceWorld* dw, int shapeCount, fl
 {
 	if ( shapeCount == 0 ) return 0;
 	CK( cudaStreamSynchronize( dw->stream ) );
-	CK( cudaMemcpy( aabbs, dw->aabb, (size_t)shapeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
-	CK( cudaMemcpy( fatAABBs, dw->fat, (size_t)shapeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)shapeCount * sizeof( float4 ) ), cudaMemcpy( aabbs, dw->aabb, (size_t)shapeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)shapeCount * sizeof( float4 ) ), cudaMemcpy( fatAABBs, dw->fat, (size_t)shapeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
 	return 0;
 }
 
 extern "C" int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float vx, float vy, float w, int which )
 {
 	k_setVelocity<<<1, 1, 0, dw->stream>>>( dw->stateV, awakeIndex, vx, vy, w, which );
+	dw->launches += 1;
 	return (int)cudaGetLastError();
 }
 
@@ -1148,7 +1151,7 @@ extern "C" int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity )
 static int stage( b2gDeviceWorld* dw, void** dptr, int* cap, const void* src, size_t bytes )
 {
 	CK2( grow( dptr, cap, (int)bytes, 1 ) );
-	CK( cudaMemcpyAsync( *dptr, src, bytes, cudaMemcpyHostToDevice, dw->stream ) );
+	CK( ( dw->h2dBytes += (long long)( bytes ), cudaMemcpyAsync( *dptr, src, bytes, cudaMemcpyHostToDevice, dw->stream ) ) );
 	CK( cudaStreamSynchronize( dw->stream ) );
 	return 0;
 }
@@ -1161,6 +1164,7 @@ extern "C" int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* in
 	if ( count == 0 ) return 0;
 	CK2( stage( dw, &s_staging, &s_stagingCap, inits, (size_t)count * sizeof( b2gContactInit ) ) );
 	k_initContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const b2gContactInit*)s_staging, count );
+	dw->launches += 1;
 	CK( cudaGetLastError() );
 	CK( cudaStreamSynchronize( dw->stream ) );
 	return 0;
@@ -1171,6 +1175,7 @@ extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int coun
 	if ( count == 0 ) return 0;
 	CK2( stage( dw, &s_staging, &s_stagingCap, ids, (size_t)count * sizeof( int ) ) );
 	k_killContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const int*)s_staging, count );
+	dw->launches += 1;
 	CK( cudaGetLastError() );
 	CK( cudaStreamSynchronize( dw->stream ) );
 	return 0;
@@ -1179,7 +1184,7 @@ extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int coun
 extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const int* offsets, int total )
 {
 	CK2( grow( (void**)&dw->colorIds, &dw->colorIdsCap, total > 0 ? total : 1, sizeof( int ) ) );
-	if ( total > 0 ) CK( cudaMemcpy( dw->colorIds, ids, (size_t)total * sizeof( int ), cudaMemcpyHostToDevice ) );
+	if ( total > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)total * sizeof( int ) ), cudaMemcpy( dw->colorIds, ids, (size_t)total * sizeof( int ), cudaMemcpyHostToDevice ) ) );
 	memcpy( dw->colorOffsets, offsets, sizeof( dw->colorOffsets ) );
 	return 0;
 }
@@ -1188,14 +1193,14 @@ extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int
 {
 	if ( count == 0 ) return 0;
 	CK( cudaStreamSynchronize( dw->stream ) );
-	CK( cudaMemcpy( out, dw->contacts, (size_t)count * sizeof( b2gContact ), cudaMemcpyDeviceToHost ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)count * sizeof( b2gContact ) ), cudaMemcpy( out, dw->contacts, (size_t)count * sizeof( b2gContact ), cudaMemcpyDeviceToHost ) ) );
 	return 0;
 }
 
 extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* offsets )
 {
 	CK2( grow( (void**)&dw->joints, &dw->jointCap, count > 0 ? count : 1, sizeof( b2gJoint ) ) );
-	if ( count > 0 ) CK( cudaMemcpy( dw->joints, joints, (size_t)count * sizeof( b2gJoint ), cudaMemcpyHostToDevice ) );
+	if ( count > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)count * sizeof( b2gJoint ) ), cudaMemcpy( dw->joints, joints, (size_t)count * sizeof( b2gJoint ), cudaMemcpyHostToDevice ) ) );
 	memcpy( dw->jointOffsets, offsets, sizeof( dw->jointOffsets ) );
 	dw->jointCount = count;
 	return 0;
@@ -1207,7 +1212,7 @@ extern "C" int b2gDev_DownloadJoints( b2gDeviceWorld* dw, b2gJoint* byId, int id
 	if ( n == 0 ) return 0;
 	b2gJoint* tmp = (b2gJoint*)malloc( (size_t)n * sizeof( b2gJoint ) );
 	CK( cudaStreamSynchronize( dw->stream ) );
-	cudaError_t e = cudaMemcpy( tmp, dw->joints, (size_t)n * sizeof( b2gJoint ), cudaMemcpyDeviceToHost );
+	cudaError_t e = ( dw->d2hBytes += (long long)( (size_t)n * sizeof( b2gJoint ) ), cudaMemcpy( tmp, dw->joints, (size_t)n * sizeof( b2gJoint ), cudaMemcpyDeviceToHost ) );
 	if ( e == cudaSuccess )
 	{
 		for ( int i = 0; i < n; ++i )
@@ -1221,8 +1226,8 @@ extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gTreeNod
 {
 	CK2( grow( (void**)&dw->tree[type], &dw->treeCap[type], nodeCount > 0 ? nodeCount : 1, sizeof( b2gTreeNode ) ) );
 	if ( nodeCount > 0 )
-		CK( cudaMemcpyAsync( dw->tree[type], nodes, (size_t)nodeCount * sizeof( b2gTreeNode ), cudaMemcpyHostToDevice,
-							 dw->stream ) );
+		CK( ( dw->h2dBytes += (long long)( (size_t)nodeCount * sizeof( b2gTreeNode ) ), cudaMemcpyAsync( dw->tree[type], nodes, (size_t)nodeCount * sizeof( b2gTreeNode ), cudaMemcpyHostToDevice,
+							 dw->stream ) ) );
 	CK( cudaStreamSynchronize( dw->stream ) );
 	int mc = dw->movedCap[type];
 	CK2( grow( (void**)&dw->moved[type], &mc, nodeCount > 0 ? nodeCount : 1, 1 ) );
@@ -1244,11 +1249,12 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 	cap = dw->moveCap;
 	CK2( grow( (void**)&dw->pairCounts, &cap, n, sizeof( int ) ) );
 	dw->moveCap = cap;
-	CK( cudaMemcpyAsync( dw->moveKeys, keys, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) );
-	CK( cudaMemcpyAsync( dw->moveBoxes, boxes, (size_t)n * sizeof( float4 ), cudaMemcpyHostToDevice, dw->stream ) );
-	CK( cudaMemcpyAsync( dw->moveShapes, shapes, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) );
+	CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( int ) ), cudaMemcpyAsync( dw->moveKeys, keys, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) ) );
+	CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( float4 ) ), cudaMemcpyAsync( dw->moveBoxes, boxes, (size_t)n * sizeof( float4 ), cudaMemcpyHostToDevice, dw->stream ) ) );
+	CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( int ) ), cudaMemcpyAsync( dw->moveShapes, shapes, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) ) );
 	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
 															   dw->moved[b2_staticBody], dw->moveKeys, n, 1 );
+	dw->launches += 1;
 	CK( cudaGetLastError() );
 	for ( int attempt = 0; attempt < 8; ++attempt )
 	{
@@ -1258,8 +1264,9 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 			dw->tree[b2_staticBody], dw->treeRoot[b2_staticBody], dw->tree[b2_kinematicBody], dw->treeRoot[b2_kinematicBody],
 			dw->tree[b2_dynamicBody], dw->treeRoot[b2_dynamicBody], dw->moved[b2_dynamicBody], dw->moveKeys, dw->moveBoxes,
 			dw->moveShapes, n, dw->pairBuf, dw->pairCounts, dw->pairPerMove, dw->counters );
+		dw->launches += 1;
 		CK( cudaGetLastError() );
-		CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( ( dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) ), cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) ) );
 		CK( cudaStreamSynchronize( dw->stream ) );
 		if ( dw->hCounters->status != 0 ) return (int)cudaErrorIllegalState;
 		if ( dw->hCounters->pairOverflow <= dw->pairPerMove ) break;
@@ -1267,14 +1274,15 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 	}
 	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
 															   dw->moved[b2_staticBody], dw->moveKeys, n, 0 );
+	dw->launches += 1;
 	CK( cudaGetLastError() );
 	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, n, sizeof( int ) ) );
-	CK( cudaMemcpyAsync( dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)n * sizeof( int ) ), cudaMemcpyAsync( dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) ) );
 	int* raw = NULL;
 	int rawCap = 0;
 	CK2( growHost( (void**)&raw, &rawCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
-	CK( cudaMemcpyAsync( raw, dw->pairBuf, (size_t)2 * n * dw->pairPerMove * sizeof( int ), cudaMemcpyDeviceToHost,
-						 dw->stream ) );
+	CK( ( dw->d2hBytes += (long long)( (size_t)2 * n * dw->pairPerMove * sizeof( int ) ), cudaMemcpyAsync( raw, dw->pairBuf, (size_t)2 * n * dw->pairPerMove * sizeof( int ), cudaMemcpyDeviceToHost,
+						 dw->stream ) ) );
 	CK( cudaStreamSynchronize( dw->stream ) );
 	int total = 0;
 	for ( int i = 0; i < n; ++i ) total += dw->hPairCounts[i];
@@ -1288,6 +1296,12 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 	}
 	cudaFreeHost( raw );
 	CK( cudaEventRecord( dw->ev[1], dw->stream ) );
+	CK( cudaEventSynchronize( dw->ev[1] ) );
+	{
+		float ms = 0.0f;
+		cudaEventElapsedTime( &ms, dw->ev[0], dw->ev[1] );
+		dw->pairsMs += ms;
+	}
 	*outPairs = dw->hPairs;
 	*outCounts = dw->hPairCounts;
 	*outTotal = total;
@@ -1326,20 +1340,28 @@ extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int c
 		a.changes = dw->changes;
 		a.counters = dw->counters;
 		a.recycleDistance = p->contactRecycleDistance;
+		CK( cudaEventRecord( dw->ev[9], dw->stream ) );
 		k_collide<<<blocks( contactIdCapacity ), B2G_THREADS, 0, dw->stream>>>( a );
+		dw->launches += 1;
 		CK( cudaGetLastError() );
+		CK( cudaEventRecord( dw->ev[3], dw->stream ) );
 	}
-	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( ( dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) ), cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) ) );
 	CK( cudaStreamSynchronize( dw->stream ) );
+	if ( contactIdCapacity > 0 )
+	{
+		float ms = 0.0f;
+		cudaEventElapsedTime( &ms, dw->ev[9], dw->ev[3] );
+		dw->collideMs += ms;
+	}
 	int n = dw->hCounters->stateChangeCount;
 	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( n > 0 ? n : 1 ), sizeof( int ) ) );
 	if ( n > 0 )
 	{
-		CK( cudaMemcpyAsync( dw->hChanges, dw->changes, (size_t)2 * n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( ( dw->d2hBytes += (long long)( (size_t)2 * n * sizeof( int ) ), cudaMemcpyAsync( dw->hChanges, dw->changes, (size_t)2 * n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) ) );
 		CK( cudaStreamSynchronize( dw->stream ) );
 		qsort( dw->hChanges, (size_t)n, 2 * sizeof( int ), cmpChange );
 	}
-	CK( cudaEventRecord( dw->ev[3], dw->stream ) );
 	*outChanges = dw->hChanges;
 	*outChangeCount = n;
 	*outRecycled = dw->hCounters->recycledContactCount;
@@ -1381,17 +1403,27 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	a.awakeCount = awakeCount;
 	a.p = *p;
 	int jointTotal = dw->jointOffsets[B2_GRAPH_COLOR_COUNT];
+	CK( cudaEventRecord( dw->ev[6], dw->stream ) );
 	if ( jointTotal > 0 )
 	{
 		d_jointBodies jb = { dw->xf, dw->center, dw->localCenter, dw->invMass, dw->invI, dw->awakeIndex };
 		k_prepareJoints<<<blocks( jointTotal ), B2G_THREADS, 0, dw->stream>>>( a, jb, jointTotal );
+		dw->launches += 1;
 	}
-	if ( total > 0 ) k_prepareContacts<<<blocks( total ), B2G_THREADS, 0, dw->stream>>>( a, 0, total, overflowBegin );
+	if ( total > 0 )
+	{
+		k_prepareContacts<<<blocks( total ), B2G_THREADS, 0, dw->stream>>>( a, 0, total, overflowBegin );
+		dw->launches += 1;
+	}
 	for ( int k = 0; k < activeColorCount; ++k )
 	{
 		int c = activeColors[k];
 		int begin = dw->colorOffsets[c], count = dw->colorOffsets[c + 1] - begin;
-		if ( count > 0 ) k_groupFlags<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( a, begin, count );
+		if ( count > 0 )
+		{
+			k_groupFlags<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( a, begin, count );
+			dw->launches += 1;
+		}
 	}
 	CK( cudaGetLastError() );
 	int ovJointBegin = dw->jointOffsets[B2G_OVERFLOW_INDEX];
@@ -1401,29 +1433,54 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	for ( int sub = 0; sub < p->subStepCount; ++sub )
 	{
 		k_integrateVelocities<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( a );
+		dw->launches += 1;
 		for ( int stage = STAGE_WARM; stage <= STAGE_RELAX; ++stage )
 		{
 			if ( stage == STAGE_RELAX )
+			{
 				k_integratePositions<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( a );
-			if ( hasOverflow ) k_overflowStage<<<1, 1, 0, dw->stream>>>( a, ovJointBegin, ovJointCount, overflowBegin, ovCount, stage );
+				dw->launches += 1;
+			}
+			if ( hasOverflow )
+			{
+				k_overflowStage<<<1, 1, 0, dw->stream>>>( a, ovJointBegin, ovJointCount, overflowBegin, ovCount, stage );
+				dw->launches += 1;
+			}
 			for ( int k = 0; k < activeColorCount; ++k )
 			{
 				int c = activeColors[k];
 				int jb = dw->jointOffsets[c], jc = dw->jointOffsets[c + 1] - jb;
 				int lb = dw->colorOffsets[c], lc = dw->colorOffsets[c + 1] - lb;
-				if ( jc + lc > 0 ) k_colorStage<<<blocks( jc + lc ), B2G_THREADS, 0, dw->stream>>>( a, jb, jc, lb, lc, stage );
+				if ( jc + lc > 0 )
+				{
+					k_colorStage<<<blocks( jc + lc ), B2G_THREADS, 0, dw->stream>>>( a, jb, jc, lb, lc, stage );
+					dw->launches += 1;
+				}
 			}
 		}
 	}
-	if ( hasOverflow ) k_overflowStage<<<1, 1, 0, dw->stream>>>( a, ovJointBegin, ovJointCount, overflowBegin, ovCount, STAGE_RESTITUTION );
+	if ( hasOverflow )
+	{
+		k_overflowStage<<<1, 1, 0, dw->stream>>>( a, ovJointBegin, ovJointCount, overflowBegin, ovCount, STAGE_RESTITUTION );
+		dw->launches += 1;
+	}
 	for ( int k = 0; k < activeColorCount; ++k )
 	{
 		int c = activeColors[k];
 		int lb = dw->colorOffsets[c], lc = dw->colorOffsets[c + 1] - lb;
-		if ( lc > 0 ) k_colorStage<<<blocks( lc ), B2G_THREADS, 0, dw->stream>>>( a, 0, 0, lb, lc, STAGE_RESTITUTION );
+		if ( lc > 0 )
+		{
+			k_colorStage<<<blocks( lc ), B2G_THREADS, 0, dw->stream>>>( a, 0, 0, lb, lc, STAGE_RESTITUTION );
+			dw->launches += 1;
+		}
 	}
-	if ( total > 0 ) k_storeImpulses<<<blocks( total ), B2G_THREADS, 0, dw->stream>>>( a, 0, total, overflowBegin );
+	if ( total > 0 )
+	{
+		k_storeImpulses<<<blocks( total ), B2G_THREADS, 0, dw->stream>>>( a, 0, total, overflowBegin );
+		dw->launches += 1;
+	}
 	CK( cudaGetLastError() );
+	CK( cudaEventRecord( dw->ev[7], dw->stream ) );
 
 	/* finalize */
 	int shapeTotal = dw->shapeCountTotal;
@@ -1461,9 +1518,18 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	f.enableSleep = p->enableSleep;
 	f.enableContinuous = p->enableContinuous;
 	k_finalizeBodies<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( f );
+	dw->launches += 1;
 	CK( cudaGetLastError() );
-	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( cudaEventRecord( dw->ev[8], dw->stream ) );
+	CK( ( dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) ), cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) ) );
 	CK( cudaStreamSynchronize( dw->stream ) );
+	{
+		float ms = 0.0f;
+		cudaEventElapsedTime( &ms, dw->ev[6], dw->ev[7] );
+		dw->solveMs += ms;
+		cudaEventElapsedTime( &ms, dw->ev[7], dw->ev[8] );
+		dw->finalizeMs += ms;
+	}
 	int n = dw->hCounters->enlargedBodyCount;
 	if ( n > shapeTotal ) n = shapeTotal;
 	CK2( growHost( (void**)&dw->hRecs, &dw->hRecsCap, 4 * ( n > 0 ? n : 1 ), sizeof( int ) ) );
@@ -1472,8 +1538,8 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	{
 		int* recs = (int*)malloc( (size_t)n * 4 * sizeof( int ) );
 		float* boxes = (float*)malloc( (size_t)n * 4 * sizeof( float ) );
-		CK( cudaMemcpy( recs, dw->enlargedRecs, (size_t)n * 4 * sizeof( int ), cudaMemcpyDeviceToHost ) );
-		CK( cudaMemcpy( boxes, dw->enlargedBoxes, (size_t)n * sizeof( float4 ), cudaMemcpyDeviceToHost ) );
+		CK( ( dw->d2hBytes += (long long)( (size_t)n * 4 * sizeof( int ) ), cudaMemcpy( recs, dw->enlargedRecs, (size_t)n * 4 * sizeof( int ), cudaMemcpyDeviceToHost ) ) );
+		CK( ( dw->d2hBytes += (long long)( (size_t)n * sizeof( float4 ) ), cudaMemcpy( boxes, dw->enlargedBoxes, (size_t)n * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
 		recKey* keys = (recKey*)malloc( (size_t)n * sizeof( recKey ) );
 		for ( int i = 0; i < n; ++i )
 		{
@@ -1500,9 +1566,23 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 
 extern "C" int b2gDev_Synchronize( b2gDeviceWorld* dw ) { return (int)cudaStreamSynchronize( dw->stream ); }
 
-extern "C" void b2gDev_Timings( b2gDeviceWorld* dw, float* pairsMs, float* collideMs, float* solveMs )
+/* accumulated device milliseconds per stage since the last reset: pairs (query and
+   copies), narrowphase kernel, solver (prepare through store), finalize; and traffic */
+extern "C" void b2gDev_Timings( b2gDeviceWorld* dw, float* out, long long* traffic, int reset )
 {
-	cudaEventElapsedTime( pairsMs, dw->ev[0], dw->ev[1] );
-	cudaEventElapsedTime( collideMs, dw->ev[2], dw->ev[3] );
-	cudaEventElapsedTime( solveMs, dw->ev[4], dw->ev[5] );
+	out[0] = dw->pairsMs;
+	out[1] = dw->collideMs;
+	out[2] = dw->solveMs;
+	out[3] = dw->finalizeMs;
+	traffic[0] = dw->h2dBytes;
+	traffic[1] = dw->d2hBytes;
+	traffic[2] = dw->launches;
+	if ( reset )
+	{
+		dw->pairsMs = dw->collideMs = dw->solveMs = dw->finalizeMs = 0.0f;
+		dw->h2dBytes = dw->d2hBytes = 0;
+		dw->launches = 0;
+	}
 }
+
+extern "C" void* b2gDev_Stream( b2gDeviceWorld* dw ) { return (void*)dw->stream; }

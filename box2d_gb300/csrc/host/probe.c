@@ -88,3 +88,22 @@ B2P_EXPORT int b2p_status( uint32_t packedWorldId )
 	h_world* w = h_worldFromId( id );
 	return w == NULL ? -1 : w->lastStatus;
 }
+
+/* accumulated device stage times (ms: pairs, narrowphase, solver, finalize) and
+   host<->device traffic (bytes: to device, to host) and the number of kernels launched since the last reset */
+B2P_EXPORT int b2p_timings( uint32_t packedWorldId, float* stageMs, long long* traffic, int reset )
+{
+	b2WorldId id = { (uint16_t)( packedWorldId >> 16 ), (uint16_t)( packedWorldId & 0xFFFF ) };
+	h_world* w = h_worldFromId( id );
+	if ( w == NULL ) return -1;
+	b2gDev_Timings( w->dev, stageMs, traffic, reset );
+	return 0;
+}
+
+/* the CUDA stream every kernel of this world is launched on (cudaStream_t) */
+B2P_EXPORT void* b2p_stream( uint32_t packedWorldId )
+{
+	b2WorldId id = { (uint16_t)( packedWorldId >> 16 ), (uint16_t)( packedWorldId & 0xFFFF ) };
+	h_world* w = h_worldFromId( id );
+	return w == NULL ? NULL : b2gDev_Stream( w->dev );
+}

@@ -1,0 +1,59 @@
+/*
+ * b2g_probe.h -- parity probes and scene builders exported by the GB300 step library.
+ * These have no counterpart in the reference's public API: they exist so tests can read
+ * the contact table and drive the benchmark scenes through the same C ABI on every
+ * build (GB300 library, CPU oracle, and the reference build in the development container).
+ */
+#ifndef B2G_PROBE_H
+#define B2G_PROBE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C"
+{
+#endif
+
+/* Live contact table, ascending contact id, 8 ints per row:
+   contactId, shapeIdA, shapeIdB, colorIndex, pointCount, featureId0, featureId1, touching.
+   packedWorldId = (index1 << 16) | generation. Returns the row count (may exceed capacity). */
+int b2p_contacts( uint32_t packedWorldId, int* out, int capacity );
+
+/* 12 floats per live contact: normal (2), then per point: separation, normalImpulse,
+   tangentImpulse, anchorA (2). Returns the row count. */
+int b2p_contact_floats( uint32_t packedWorldId, float* out, int capacity );
+
+/* Device status of the last step: 0 ok, 1 non-finite body velocity, 2 capacity exceeded. */
+int b2p_status( uint32_t packedWorldId );
+
+/* Accumulated device time per stage since the last reset, in ms: pair query, narrowphase
+   kernel, solver (prepare through store), finalize; and host<->device traffic in bytes
+   (to device, to host) and kernels launched, as traffic[0..2]. reset != 0 zeroes them after reading. */
+int b2p_timings( uint32_t packedWorldId, float* stageMs, long long* traffic, int reset );
+
+/* The CUDA stream (cudaStream_t) the world's kernels are launched on. */
+void* b2p_stream( uint32_t packedWorldId );
+
+/* Scene builders (box2d_gb300/scenes/scenes.c). kind: 0 large pyramid, 1 many pyramids
+   with rain, 2 joint grid with mixed shapes, 3 one batched world, 4 one ramp world,
+   5 reference many_pyramids, 6 reference joint_grid, 7 hello world, 8 shape zoo.
+   flags bit 0 disables continuous collision. Returns a handle or -1. */
+int b2s_create( int kind, int a, int b, int c, uint32_t seed, int flags );
+void b2s_destroy( int handle );
+void b2s_step( int handle, float timeStep, int subStepCount, int count );
+int b2s_body_count( int handle );
+int b2s_dynamic_count( int handle );
+uint32_t b2s_world_id( int handle );
+/* 7 floats per body in creation order: p.x, p.y, q.c, q.s, v.x, v.y, w */
+void b2s_get_state( int handle, float* out );
+/* FNV-1a 64 over the bit patterns of b2s_get_state */
+uint64_t b2s_state_hash( int handle );
+void b2s_set_velocities( int handle, const float* in );
+void b2s_target( int handle, float* out );
+void b2s_counters( int handle, int* out );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -6,8 +6,8 @@
  * needs to build worlds, step them and read results. Every struct below has the same
  * field order, types and size as the reference declaration it stands in for, so a
  * program compiled against the reference headers links against this library unchanged
- * (the layouts are checked at build time against the reference headers by
- * oracle/abi_check.c when those headers are present).
+ * (tests/test_abi.py compiles a layout probe against both headers where the reference
+ * headers are present and requires identical sizes and offsets).
  *
  * float32 only: b2Pos is b2Vec2 and b2WorldTransform is b2Transform, as in the reference
  * when BOX2D_DOUBLE_PRECISION is off (math_functions.h:69-70).
@@ -542,7 +542,6 @@ B2G_API b2Polygon b2MakeOffsetBox( float halfWidth, float halfHeight, b2Vec2 cen
 B2G_API b2MassData b2ComputeCircleMass( const b2Circle* shape, float density );
 B2G_API b2MassData b2ComputeCapsuleMass( const b2Capsule* shape, float density );
 B2G_API b2MassData b2ComputePolygonMass( const b2Polygon* shape, float density );
-B2G_API b2LocalManifold b2CollidePolygons( const b2Polygon* polygonA, const b2Polygon* polygonB, b2Transform xf );
 
 /* ---- API: world (box2d.h:34-200) ---- */
 B2G_API b2WorldDef b2DefaultWorldDef( void );

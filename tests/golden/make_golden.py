@@ -1,0 +1,64 @@
+"""Record golden parity fixtures from the reference itself.
+
+Runs only where the reference sources are present: builds the reference from its own
+sources into oracle/_ref (oracle/Makefile, target `ref`), drives it through the scene
+builders of box2d_gb300/scenes/scenes.c, and writes, per scene, the FNV-1a hash of every
+body's (position, rotation, velocity) after each step plus a digest of the live contact
+table (contact id, shape pair, graph color, point count, feature ids, touching) at a few
+steps. The committed JSON files are what tests compare the oracle and the GB300 library
+against on machines without the reference.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import box2d_gb300 as B  # noqa: E402
+
+# (name, kind, a, b, c, seed, flags, steps, contact digest steps)
+SCENES = [
+    ("large_pyramid_20", B.LARGE_PYRAMID, 20, 0, 0, 0, 0, 300, [1, 10, 100, 300]),
+    ("large_pyramid_100_segment", B.LARGE_PYRAMID, 100, 1, 0, 0, 0, 40, [1, 40]),
+    ("shape_zoo_200", B.SHAPE_ZOO, 200, 0, 0, 7, B.NO_CONTINUOUS, 300, [1, 50, 300]),
+    ("many_pyramids_rain_3x3", B.MANY_PYRAMIDS_RAIN, 3, 10, 100, 0, B.NO_CONTINUOUS, 300, [1, 100, 300]),
+    ("joint_grid_20", B.JOINT_GRID_REF, 20, 0, 0, 0, 0, 120, [1, 120]),
+    ("joint_grid_mixed_12", B.JOINT_GRID_MIXED, 12, 40, 0, 3, B.NO_CONTINUOUS, 200, [1, 100, 200]),
+    ("batch_world_60", B.BATCH_WORLD, 60, 0, 0, 11, B.NO_CONTINUOUS, 200, [1, 200]),
+    ("ramp_world_4x4", B.RAMP_WORLD, 4, 4, 0, 5, B.NO_CONTINUOUS, 120, [1, 120]),
+]
+
+
+def contact_digest(table) -> str:
+    return hashlib.sha256(table.astype("<i4").tobytes()).hexdigest()
+
+
+def main() -> None:
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"], check=True)
+    ref = B.load_library(ROOT / "oracle" / "_ref" / "libref.so")
+    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES:
+        with B.Scene(ref, kind, a, b, c, seed, flags) as s:
+            hashes, digests = [], {}
+            for k in range(1, steps + 1):
+                s.step()
+                hashes.append(f"{s.state_hash():016x}")
+                if k in digest_steps:
+                    table = s.contacts()
+                    digests[str(k)] = {"count": int(table.shape[0]), "sha256": contact_digest(table),
+                                       "touching": int(table[:, 7].sum()) if len(table) else 0}
+            data = {"scene": name, "kind": kind, "a": a, "b": b, "c": c, "seed": seed, "flags": flags,
+                    "dt": 1.0 / 60.0, "substeps": 4, "bodies": s.body_count, "state_hashes": hashes,
+                    "contact_digests": digests, "source": "reference built from its own sources (oracle/Makefile ref)"}
+        (Path(__file__).parent / f"{name}.json").write_text(json.dumps(data, indent=1))
+        print(name, steps, "steps", s.body_count, "bodies")
+
+
+if __name__ == "__main__":
+    main()

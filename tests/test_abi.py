@@ -1,0 +1,98 @@
+"""The C ABI: the GB300 library loads on CPU-only machines and exports every function
+declared in include/*.h; the public structs have the reference's layout (checked by
+compiling a layout probe against the reference headers where they are present)."""
+from __future__ import annotations
+
+import ctypes
+import re
+import subprocess
+import tempfile
+from pathlib import Path
+
+import pytest
+
+import box2d_gb300 as B
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions() -> set[str]:
+    """Every exported function prototype of include/*.h (B2G_API lines of the public
+    header, plain prototypes of the probe header)."""
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        for line in h.read_text().splitlines():
+            m = re.match(r"^B2G_API\s+[\w\s\*]+?\b(b2\w+)\s*\(", line) or \
+                re.match(r"^(?:int|void|float|uint32_t|uint64_t)\s+\**(b2\w+)\s*\(", line)
+            if m:
+                names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_function():
+    if not B.LIB_PATH.exists():
+        import box2d_gb300._build as bld
+        bld.build_library()
+    lib = ctypes.CDLL(str(B.LIB_PATH))
+    missing = [n for n in sorted(declared_functions()) if not hasattr(lib, n)]
+    assert not missing, f"declared but not exported: {missing}"
+    assert len(declared_functions()) > 80
+
+
+def test_oracle_exports_the_public_api(oracle):
+    skip = {"b2p_status", "b2p_timings", "b2p_stream"}
+    missing = [n for n in sorted(declared_functions()) if n not in skip and not hasattr(oracle, n)]
+    assert not missing, missing
+
+
+REF_INCLUDE = Path("/root/reference/include")
+
+
+@pytest.mark.skipif(not REF_INCLUDE.is_dir(), reason="reference headers not present on this machine")
+def test_struct_layouts_match_reference():
+    """Compile one program against the reference headers and one against ours; both print
+    sizeof/offsetof of every public struct the API passes by value or pointer."""
+    structs = {
+        "b2WorldDef": ["gravity", "frictionCallback", "enableSleep", "workerCount", "userData", "capacity", "internalValue"],
+        "b2BodyDef": ["type", "position", "rotation", "linearVelocity", "name", "userData", "motionLocks", "enableSleep",
+                      "enableContactRecycling", "internalValue"],
+        "b2ShapeDef": ["userData", "material", "density", "filter", "enableCustomFiltering", "updateBodyMass",
+                       "internalValue"],
+        "b2Polygon": ["vertices", "normals", "centroid", "radius", "count"],
+        "b2Manifold": ["normal", "rollingImpulse", "points", "pointCount"],
+        "b2ManifoldPoint": ["anchorA", "separation", "normalVelocity", "id", "persisted"],
+        "b2RevoluteJointDef": ["base", "targetAngle", "enableSpring", "lowerAngle", "enableMotor", "motorSpeed",
+                               "internalValue"],
+        "b2PrismaticJointDef": ["base", "enableSpring", "targetTranslation", "maxMotorForce", "internalValue"],
+        "b2WeldJointDef": ["base", "linearHertz", "angularDampingRatio", "internalValue"],
+        "b2WheelJointDef": ["base", "enableSpring", "lowerTranslation", "motorSpeed", "internalValue"],
+        "b2DistanceJointDef": ["base", "length", "enableSpring", "maxLength", "motorSpeed", "internalValue"],
+        "b2JointDef": ["userData", "bodyIdA", "localFrameA", "forceThreshold", "drawScale", "collideConnected"],
+        "b2BodyMoveEvent": ["userData", "transform", "bodyId", "fellAsleep"],
+        "b2ContactBeginTouchEvent": ["shapeIdA", "shapeIdB", "contactId"],
+        "b2ContactEvents": ["beginEvents", "endEvents", "hitEvents", "beginCount", "hitCount"],
+        "b2Counters": ["byteCount", "colorCounts", "recycledContactCount"],
+        "b2Profile": ["step", "solve", "sensors"],
+        "b2Capacity": ["contactCount"],
+        "b2SurfaceMaterial": ["friction", "userMaterialId", "customColor"],
+        "b2Filter": ["categoryBits", "maskBits", "groupIndex"],
+        "b2Hull": ["points", "count"],
+        "b2ContactId": ["index1", "world0", "padding", "generation"],
+        "b2BodyId": ["index1", "world0", "generation"],
+    }
+    body = ["#include <stdio.h>", "#include <stddef.h>", "int main(void){"]
+    for s, fields in structs.items():
+        body.append(f'printf("{s} %zu\\n", sizeof({s}));')
+        for f in fields:
+            body.append(f'printf("{s}.{f} %zu\\n", offsetof({s}, {f}));')
+    body.append("return 0;}")
+    src = "\n".join(body)
+    outs = []
+    with tempfile.TemporaryDirectory() as td:
+        for name, inc, hdr in (("ref", REF_INCLUDE, "box2d/box2d.h"), ("ours", ROOT / "include", "box2d_gb300.h")):
+            c = Path(td) / f"{name}.c"
+            c.write_text(f'#include "{hdr}"\n' + src)
+            exe = Path(td) / name
+            subprocess.run(["gcc", "-std=gnu17", "-I", str(inc), str(c), "-o", str(exe)], check=True)
+            outs.append(subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout)
+    assert outs[0] == outs[1]

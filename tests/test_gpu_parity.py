@@ -1,0 +1,99 @@
+"""Parity of the GB300 library with the reference: per-step body-state hashes and
+contact tables must match the golden fixtures recorded from the reference, and the live
+CPU oracle on further seeds and at full benchmark sizes. Tolerance: bit-exact (the
+library is built with --fmad=false, IEEE division and square root)."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+import pytest
+
+import box2d_gb300 as B
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_gpu_matches_reference_fixture(gpu_lib, name):
+    g = load_golden(name)
+    with B.Scene(gpu_lib, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
+        assert s.body_count == g["bodies"]
+        for k, expected in enumerate(g["state_hashes"], start=1):
+            s.step(1, g["dt"], g["substeps"])
+            assert f"{s.state_hash():016x}" == expected, f"{name}: body state differs from the reference at step {k}"
+            d = g["contact_digests"].get(str(k))
+            if d is not None:
+                table = s.contacts()
+                assert table.shape[0] == d["count"], f"{name}: contact count at step {k}"
+                assert hashlib.sha256(table.astype("<i4").tobytes()).hexdigest() == d["sha256"], \
+                    f"{name}: contact table (ids, pairs, colors, feature ids) at step {k}"
+
+
+def _lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps, check_every=1):
+    with B.Scene(gpu_lib, kind, a, b, c, seed, flags) as g, B.Scene(oracle, kind, a, b, c, seed, flags) as o:
+        for k in range(1, steps + 1):
+            g.step()
+            o.step()
+            if k % check_every == 0 or k == steps:
+                if g.state_hash() != o.state_hash():
+                    gs, os_ = g.state(), o.state()
+                    bad = np.nonzero((gs.view(np.uint32) != os_.view(np.uint32)).any(1))[0]
+                    pytest.fail(f"state differs at step {k} in {len(bad)} bodies, first {bad[:5]}")
+        gc, oc = g.contacts(), o.contacts()
+        assert gc.shape == oc.shape and (gc == oc).all(), "contact tables differ"
+        return g.body_count, gc.shape[0]
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 4])
+def test_gpu_vs_oracle_shape_zoo_seeds(gpu_lib, oracle, seed):
+    _lockstep(gpu_lib, oracle, B.SHAPE_ZOO, 150, 0, 0, seed, B.NO_CONTINUOUS, 150)
+
+
+@pytest.mark.parametrize("seed", [21, 22, 23])
+def test_gpu_vs_oracle_batch_worlds(gpu_lib, oracle, seed):
+    _lockstep(gpu_lib, oracle, B.BATCH_WORLD, 0, 0, 0, seed, B.NO_CONTINUOUS, 150)
+
+
+def test_gpu_vs_oracle_joint_grid_mixed(gpu_lib, oracle):
+    _lockstep(gpu_lib, oracle, B.JOINT_GRID_MIXED, 30, 200, 0, 9, B.NO_CONTINUOUS, 120)
+
+
+def test_gpu_vs_oracle_full_large_pyramid(gpu_lib, oracle):
+    """Full-size large pyramid (5050 boxes, segment ground) for 100 steps."""
+    bodies, contacts = _lockstep(gpu_lib, oracle, B.LARGE_PYRAMID, 100, 1, 0, 0, 0, 100, check_every=10)
+    assert bodies == 5051 and contacts > 14000
+
+
+def test_gpu_vs_oracle_full_many_pyramids(gpu_lib, oracle):
+    """Full-size many-pyramids-with-rain scene (22000 boxes + 2000 circles), 40 steps."""
+    bodies, contacts = _lockstep(gpu_lib, oracle, B.MANY_PYRAMIDS_RAIN, 20, 10, 2000, 0, B.NO_CONTINUOUS, 40,
+                                 check_every=10)
+    assert bodies == 24001
+
+
+def test_gpu_edge_cases(gpu_lib, oracle):
+    # a world whose only body is a dropped box (single contact life cycle), zero and
+    # one substep, and a zero time step (collide only, no solve)
+    for substeps in (1, 4):
+        with B.Scene(gpu_lib, B.HELLO_WORLD) as g, B.Scene(oracle, B.HELLO_WORLD) as o:
+            for k in range(40):
+                g.step(1, 1.0 / 60.0, substeps)
+                o.step(1, 1.0 / 60.0, substeps)
+                assert g.state_hash() == o.state_hash(), (substeps, k)
+    with B.Scene(gpu_lib, B.LARGE_PYRAMID, 5, 0) as g, B.Scene(oracle, B.LARGE_PYRAMID, 5, 0) as o:
+        g.step(1, 0.0, 4)
+        o.step(1, 0.0, 4)
+        assert g.state_hash() == o.state_hash()
+        assert (g.contacts() == o.contacts()).all()
+        g.step(5)
+        o.step(5)
+        assert g.state_hash() == o.state_hash()
+
+
+def test_gpu_empty_world(gpu_lib):
+    with B.Scene(gpu_lib, B.LARGE_PYRAMID, 0, 0) as g:
+        g.step(3)
+        assert g.body_count == 1
+        assert g.contacts().shape[0] == 0
