@@ -958,7 +958,9 @@ extern "C" int b2gDev_Create( b2gDeviceWorld** out )
 	if ( e != cudaSuccess ) return (int)e;
 	if ( count == 0 ) return (int)cudaErrorNoDevice;
 	b2gDeviceWorld* dw = (b2gDeviceWorld*)calloc( 1, sizeof( b2gDeviceWorld ) );
-	CK( cudaStreamCreateWithFlags( &dw->stream, cudaStreamNonBlocking ) );
+	/* a blocking stream: buffer growth (cudaMalloc + cudaMemset / cudaMemcpy on the legacy
+	   default stream) is then ordered before every kernel of this world */
+	CK( cudaStreamCreate( &dw->stream ) );
 	for ( int i = 0; i < 10; ++i ) CK( cudaEventCreate( dw->ev + i ) );
 	CK( cudaMalloc( &dw->counters, sizeof( b2gStepCounters ) ) );
 	CK( cudaMallocHost( &dw->hCounters, sizeof( b2gStepCounters ) ) );
