@@ -21,7 +21,9 @@ LIB = PKG / "libbox2d_gb300.so"
 
 HOST_SOURCES = ["csrc/host/world.c", "csrc/host/step.c", "csrc/host/joint.c", "csrc/host/tree.c",
                 "csrc/host/geometry.c", "csrc/host/probe.c", "scenes/scenes.c"]
-DEVICE_SOURCES = ["csrc/device/world.cu"]
+# (source, extra nvcc flags). The persistent solver reads state written by other SMs
+# between grid barriers, so its global loads bypass L1 (-dlcm=cg).
+DEVICE_SOURCES = [("csrc/device/world.cu", []), ("csrc/device/persistent.cu", ["-Xptxas", "-dlcm=cg"])]
 
 NVCC_FLAGS = ["-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC",
@@ -64,12 +66,12 @@ def build_library(force: bool = False) -> Path:
         objects.append(o)
         if force or _needs(o, [s] + headers):
             jobs.append(["gcc", *CFLAGS, *include, "-c", str(s), "-o", str(o)])
-    for src in DEVICE_SOURCES:
+    for src, extra in DEVICE_SOURCES:
         s = PKG / src
         o = BUILD / (src.replace("/", "_") + ".o")
         objects.append(o)
         if force or _needs(o, [s] + headers):
-            jobs.append([nvcc, *NVCC_FLAGS, *include, "-c", str(s), "-o", str(o)])
+            jobs.append([nvcc, *NVCC_FLAGS, *extra, *include, "-c", str(s), "-o", str(o)])
     with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
         list(ex.map(_run, jobs))
     if force or jobs or _needs(LIB, objects):
