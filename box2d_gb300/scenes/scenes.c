@@ -5,7 +5,10 @@
  * container only -- the reference itself, so one scene definition drives all three.
  *
  * Random numbers: XorShift32 with seed 12345 mapped to [0, 32767], the generator of
- * shared/utils.h:29-65 in the reference; normal variates by Box-Muller on that stream.
+ * shared/utils.h:29-65 in the reference; normal variates from sums of that stream's draws.
+ * Every draw is its own statement: C leaves the evaluation order of function arguments
+ * and initializer lists unspecified, and gcc orders them differently on x86-64 and
+ * aarch64, which would build different worlds on the two machines.
  *
  * Exported entry points (prefix b2s_) keep a small table of live scenes and read body
  * state through b2Body_* getters, so they never touch library internals.
@@ -51,13 +54,15 @@ static int b2sRandomIntRange( b2sRng* r, int lo, int hi )
 	return lo + b2sRandomInt( r ) % ( hi - lo + 1 );
 }
 
-/* Box-Muller on two uniform draws in (0, 1] */
+/* approximately normal variate: Irwin-Hall sum of four uniform draws, centred and scaled
+   to unit variance. Plain float arithmetic only, so no libm routine (whose last-bit
+   rounding may differ between platforms) can change a scene. */
 static float b2sRandomNormal( b2sRng* r, float sigma )
 {
-	float u1 = b2sRandomFloatRange( r, 1.0f / 32768.0f, 1.0f );
-	float u2 = b2sRandomFloatRange( r, 0.0f, 1.0f );
-	double z = sqrt( -2.0 * log( (double)u1 ) ) * cos( 2.0 * 3.14159265358979323846 * (double)u2 );
-	return sigma * (float)z;
+	float sum = 0.0f;
+	for ( int k = 0; k < 4; ++k )
+		sum += b2sRandomFloatRange( r, 0.0f, 1.0f );
+	return sigma * ( ( sum - 2.0f ) * 1.7320508f );
 }
 
 typedef struct b2sScene
@@ -309,7 +314,10 @@ static void b2sJointGrid( b2sScene* s, int n, int pinAll, int mixedCount, b2sRng
 			b2Segment seg = { { -0.5f * length, 0.0f }, { 0.5f * length, 0.0f } };
 			b2CreateSegmentShape( body, &md, &seg );
 		}
-		b2Vec2 v = { b2sRandomNormal( rng, 2.0f ), b2sRandomNormal( rng, 2.0f ) };
+		/* one draw per statement: argument and initializer evaluation order is unspecified */
+		b2Vec2 v;
+		v.x = b2sRandomNormal( rng, 2.0f );
+		v.y = b2sRandomNormal( rng, 2.0f );
 		b2Body_SetLinearVelocity( body, v );
 	}
 }
@@ -357,7 +365,9 @@ static void b2sBatchWorld( b2sScene* s, int bodyCount, b2sRng* rng )
 			b2Capsule cap = { { -hl, 0.0f }, { hl, 0.0f }, b2sRandomFloatRange( rng, 0.1f, 0.3f ) };
 			b2CreateCapsuleShape( body, &sd, &cap );
 		}
-		b2Vec2 v = { b2sRandomNormal( rng, 1.0f ), b2sRandomNormal( rng, 1.0f ) };
+		b2Vec2 v;
+		v.x = b2sRandomNormal( rng, 1.0f );
+		v.y = b2sRandomNormal( rng, 1.0f );
 		b2Body_SetLinearVelocity( body, v );
 	}
 }
@@ -460,7 +470,9 @@ static void b2sShapeZoo( b2sScene* s, int count, b2sRng* rng )
 		}
 		else if ( kind == 2 )
 		{
-			b2Polygon box = b2MakeBox( b2sRandomFloatRange( rng, 0.2f, 0.8f ), b2sRandomFloatRange( rng, 0.2f, 0.8f ) );
+			float hx = b2sRandomFloatRange( rng, 0.2f, 0.8f );
+			float hy = b2sRandomFloatRange( rng, 0.2f, 0.8f );
+			b2Polygon box = b2MakeBox( hx, hy );
 			b2CreatePolygonShape( body, &sd, &box );
 		}
 		else
