@@ -23,7 +23,8 @@ HOST_SOURCES = ["csrc/host/world.c", "csrc/host/step.c", "csrc/host/joint.c", "c
                 "csrc/host/geometry.c", "csrc/host/probe.c", "scenes/scenes.c"]
 # (source, extra nvcc flags). The persistent solver reads state written by other SMs
 # between grid barriers, so its global loads bypass L1 (-dlcm=cg).
-DEVICE_SOURCES = [("csrc/device/world.cu", []), ("csrc/device/persistent.cu", ["-Xptxas", "-dlcm=cg"])]
+DEVICE_SOURCES = [("csrc/device/world.cu", []), ("csrc/device/components.cu", []),
+                  ("csrc/device/persistent.cu", ["-Xptxas", "-dlcm=cg"])]
 
 NVCC_FLAGS = ["-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC",

@@ -1,0 +1,81 @@
+/*
+ * Component solver interface between world.cu and components.cu.
+ *
+ * The awake constraint graph splits into connected components over non-static bodies
+ * (two bodies are connected when a colored contact or joint links them). Components share
+ * no body that the solver writes, so each can run the whole Soft Step -- prepare, every
+ * substep's integrate / warm start / solve / relax per color, restitution, store -- on its
+ * own, in the reference's color order restricted to its constraints. Because the
+ * constraints of one color touch disjoint bodies, the results are bit-identical to the
+ * global color sweep of solver.c:1010-1198.
+ *
+ * Small components are packed into bins; one CTA solves a bin out of shared memory with
+ * __syncthreads between colors. Components too large for a bin keep the global per-color
+ * path, driven by per-color lists of their constraints.
+ */
+#pragma once
+
+#include "stages.cuh"
+
+#include <cuda_runtime.h>
+
+/* shared-memory bytes a body, a contact and a joint occupy in a bin */
+#define B2G_BIN_BODY_BYTES 32
+#define B2G_BIN_CONTACT_BYTES ( (int)sizeof( b2gContactLane ) + 4 )
+#define B2G_BIN_JOINT_BYTES ( (int)sizeof( b2gJoint ) + 4 )
+/* a component heavier than this is solved on the global path; a bin holds less than twice it */
+#define B2G_BIN_CAP_BYTES ( 40 * 1024 )
+/* field widths of the packed (bodies, contacts, joints) allocation cursor */
+#define B2G_CURSOR_BODY_BITS 21
+#define B2G_CURSOR_CONTACT_BITS 22
+#define B2G_CURSOR_JOINT_BITS 21
+
+/* device-written summary of one component analysis, read by the host */
+struct b2gCompSummary
+{
+	unsigned long long cursor; /* packed totals of the small components */
+	int bigBodies;			   /* bodies in big components */
+	int bigBodyCount;		   /* fill counters of the big lists (written after the analysis) */
+	int smallComponents, bigComponents;
+	int bigContactCount[B2_GRAPH_COLOR_COUNT];
+	int bigJointCount[B2_GRAPH_COLOR_COUNT];
+};
+
+/* scratch buffers, grown on demand; sized by awake bodies, contact slots, joints, bins */
+struct b2gCompBuffers
+{
+	int awakeCap, slotCap, jointCap, binCap;
+	int* parent;	 /* union-find forest, then the root of each awake body */
+	int* compData;	 /* per root: counts (3), offsets (3), fill (3), bin */
+	int* bodyList;	 /* small components' bodies, component-contiguous */
+	int* localIndex; /* awake index -> index within its bin */
+	int* slotList;	 /* small components' contact slots */
+	int* jointList;	 /* small components' joint indices */
+	int* binRange;	 /* per bin: begin bodies/contacts/joints (min), end (max) */
+	int* bigBodyList;
+	int* bigSlotList;  /* per color, at the color's slot offset */
+	int* bigJointList; /* per color, at the color's joint offset */
+	b2gCompSummary* summary;
+	b2gCompSummary* hSummary; /* pinned */
+	/* sizes of the last analysis */
+	int n, total, jointTotal;
+	const int* awakeIndex;
+};
+
+extern "C" int b2gDev_CompReserve( b2gCompBuffers* b, int awake, int slots, int joints );
+extern "C" void b2gDev_CompFree( b2gCompBuffers* b );
+
+/* find components and pack the small ones into bins; waits for the summary. forceBig puts
+   every component on the global path (an overflow color exists). */
+extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const int* awakeIndex,
+								   int total, int jointTotal, int forceBig, cudaStream_t stream, long long* launches );
+
+/* solve every bin (small components) */
+extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets,
+									 const d_jointBodies* jb, b2gStepCounters* counters, cudaStream_t stream,
+									 long long* launches );
+
+/* global per-color path over the big components' constraints */
+extern "C" int b2gDev_CompSolveBig( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
+									const int* activeColors, int activeColorCount, int total, int jointTotal,
+									cudaStream_t stream, long long* launches );

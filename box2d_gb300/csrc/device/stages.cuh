@@ -23,8 +23,9 @@ struct d_solveArgs
 	b2gStepParams p;
 };
 
-/* contact_solver.c:1573-1809 (graph colors) and :20-160 (overflow), one thread per slot */
-static __device__ void d_prepareContactSlot( const d_solveArgs& a, int slot, int overflowBegin )
+/* contact_solver.c:1573-1809 (graph colors) and :20-160 (overflow), one thread per slot;
+   the constraint is written to `out` */
+static __device__ void d_prepareContactLane( const d_solveArgs& a, int slot, int overflowBegin, b2gContactLane* out )
 {
 	int contactId = a.colorIds[slot];
 	const b2gContact* cs = a.contacts + contactId;
@@ -152,7 +153,12 @@ static __device__ void d_prepareContactSlot( const d_solveArgs& a, int slot, int
 			c.groupFlags |= other->restitution != 0.0f ? 2 : 0;
 		}
 	}
-	a.lanes[slot] = c;
+	*out = c;
+}
+
+static __device__ __forceinline__ void d_prepareContactSlot( const d_solveArgs& a, int slot, int overflowBegin )
+{
+	d_prepareContactLane( a, slot, overflowBegin, a.lanes + slot );
 }
 
 static __device__ void d_prepareJointItem( const d_solveArgs& a, const d_jointBodies& bodies, int i )
@@ -160,12 +166,12 @@ static __device__ void d_prepareJointItem( const d_solveArgs& a, const d_jointBo
 	d_prepareJoint( a.joints + i, &bodies, a.p.h, a.p.inv_h, a.p.enableWarmStarting != 0 );
 }
 
-/* solver.c:66-112 */
-static __device__ void d_integrateVelocitiesItem( const d_solveArgs& a, int i )
+/* solver.c:66-112; pr = the body's 8 integration parameters (force, torque, damping,
+   gravity scale, inverse mass, inverse inertia) */
+static __device__ __forceinline__ void d_integrateVelocitiesState( const b2gStepParams& P, float4* sv, int i, const float* pr )
 {
-	float h = a.p.h;
-	const float* pr = a.params + 8 * i;
-	float4 s = a.sv[i];
+	float h = P.h;
+	float4 s = sv[i];
 	b2Vec2 v = { s.x, s.y };
 	float w = s.z;
 	float linearDamping = 1.0f / ( 1.0f + h * pr[3] );
@@ -173,24 +179,29 @@ static __device__ void d_integrateVelocitiesItem( const d_solveArgs& a, int i )
 	float invMass = pr[6];
 	float gravityScale = invMass > 0.0f ? pr[5] : 0.0f;
 	b2Vec2 force = { pr[0], pr[1] };
-	b2Vec2 gravity = { a.p.gravityX, a.p.gravityY };
+	b2Vec2 gravity = { P.gravityX, P.gravityY };
 	b2Vec2 lvd = d_add( d_mulSV( h * invMass, force ), d_mulSV( h * gravityScale, gravity ) );
 	float avd = h * pr[7] * pr[2];
 	v = d_mulAdd( lvd, linearDamping, v );
 	w = avd + angularDamping * w;
-	a.sv[i] = make_float4( v.x, v.y, w, s.w );
+	sv[i] = make_float4( v.x, v.y, w, s.w );
+}
+
+static __device__ __forceinline__ void d_integrateVelocitiesItem( const d_solveArgs& a, int i )
+{
+	d_integrateVelocitiesState( a.p, a.sv, i, a.params + 8 * i );
 }
 
 /* solver.c:114-162 */
-static __device__ void d_integratePositionsItem( const d_solveArgs& a, int i )
+static __device__ __forceinline__ void d_integratePositionsState( const b2gStepParams& P, float4* sv, float4* sd, int i )
 {
-	float h = a.p.h;
-	float maxLinearSpeed = a.p.maxLinearVelocity;
-	float maxAngularSpeed = D_MAX_ROTATION * a.p.inv_dt;
+	float h = P.h;
+	float maxLinearSpeed = P.maxLinearVelocity;
+	float maxAngularSpeed = D_MAX_ROTATION * P.inv_dt;
 	float maxLinearSq = maxLinearSpeed * maxLinearSpeed;
 	float maxAngularSq = maxAngularSpeed * maxAngularSpeed;
-	float4 s = a.sv[i];
-	float4 d = a.sd[i];
+	float4 s = sv[i];
+	float4 d = sd[i];
 	uint32_t flags = __float_as_uint( s.w );
 	b2Vec2 v = { s.x, s.y };
 	float w = s.z;
@@ -211,8 +222,13 @@ static __device__ void d_integratePositionsItem( const d_solveArgs& a, int i )
 	}
 	b2Vec2 dp = d_mulAdd( d_v( d.x, d.y ), h, v );
 	b2Rot dq = d_integrateRotation( b2Rot{ d.z, d.w }, h * w );
-	a.sv[i] = make_float4( v.x, v.y, w, __uint_as_float( flags ) );
-	a.sd[i] = make_float4( dp.x, dp.y, dq.c, dq.s );
+	sv[i] = make_float4( v.x, v.y, w, __uint_as_float( flags ) );
+	sd[i] = make_float4( dp.x, dp.y, dq.c, dq.s );
+}
+
+static __device__ __forceinline__ void d_integratePositionsItem( const d_solveArgs& a, int i )
+{
+	d_integratePositionsState( a.p, a.sv, a.sd, i );
 }
 
 enum
@@ -222,6 +238,22 @@ enum
 	STAGE_RELAX = 2,
 	STAGE_RESTITUTION = 3,
 };
+
+/* one joint or one contact lane of a graph color at a stage, body state in sv/sd */
+static __device__ __forceinline__ void d_jointStage( const b2gStepParams& P, b2gJoint* j, float4* sv, float4* sd, int stage )
+{
+	if ( stage == STAGE_WARM ) d_warmStartJoint( j, sv, sd );
+	else if ( stage == STAGE_SOLVE ) d_solveJoint( j, sv, sd, P.h, P.inv_h, true );
+	else if ( stage == STAGE_RELAX ) d_solveJoint( j, sv, sd, P.h, P.inv_h, false );
+}
+
+static __device__ __forceinline__ void d_laneStage( const b2gStepParams& P, b2gContactLane* c, float4* sv, float4* sd, int stage )
+{
+	if ( stage == STAGE_WARM ) d_warmStartLane( c, sv, sd );
+	else if ( stage == STAGE_SOLVE ) d_solveLane( c, sv, sd, P.inv_h, -P.contactSpeed, true );
+	else if ( stage == STAGE_RELAX ) d_solveLane( c, sv, sd, P.inv_h, -P.contactSpeed, false );
+	else d_restitutionLane( c, sv, sd, P.restitutionThreshold );
+}
 
 /* one graph color: threads [0, jointCount) run joints, the rest run contact lanes */
 static __device__ void d_colorStageItem( const d_solveArgs& a, int jointBegin, int jointCount, int laneBegin, int laneCount,
@@ -267,11 +299,9 @@ static __device__ void d_overflowStageAll( const d_solveArgs& a, int jointBegin,
 }
 
 /* contact_solver.c:2238-2331 (colors) and :516-545 (overflow) */
-static __device__ void d_storeSlot( const d_solveArgs& a, int slot, int overflowBegin )
+static __device__ void d_storeLane( const b2gContactLane* c, b2Manifold* m, bool isOverflow )
 {
-	const b2gContactLane* c = a.lanes + slot;
-	b2Manifold* m = &a.contacts[a.colorIds[slot]].manifold;
-	if ( slot >= overflowBegin )
+	if ( isOverflow )
 	{
 		for ( int j = 0; j < m->pointCount; ++j )
 		{
@@ -292,6 +322,11 @@ static __device__ void d_storeSlot( const d_solveArgs& a, int slot, int overflow
 	m->points[1].tangentImpulse = c->tangentImpulse2;
 	m->points[1].totalNormalImpulse = c->totalNormalImpulse2;
 	m->points[1].normalVelocity = c->relativeVelocity2;
+}
+
+static __device__ __forceinline__ void d_storeSlot( const d_solveArgs& a, int slot, int overflowBegin )
+{
+	d_storeLane( a.lanes + slot, &a.contacts[a.colorIds[slot]].manifold, slot >= overflowBegin );
 }
 
 /* geometry.c:400-506 fat AABB (built in double, narrowed once) */

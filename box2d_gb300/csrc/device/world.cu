@@ -13,9 +13,8 @@
  *   k_finalizeBodies                          transforms, sleep metric, fat AABBs (solver.c:553-743)
  * Bit-exact mode: compiled with --fmad=false, IEEE division/sqrt, no flush-to-zero.
  */
-#include "joints.cuh"
+#include "components.cuh"
 #include "manifold.cuh"
-#include "solver.cuh"
 
 #include <cuda_runtime.h>
 #include <stdio.h>
@@ -25,6 +24,18 @@
 #define B2G_THREADS 128
 #define B2G_PAIR_STACK 256
 
+/* solver strategies, chosen per world from the B2G_SOLVER environment variable at creation:
+   "components" (default) solves small connected components one CTA each out of shared
+   memory and the rest with one launch per color stage; "launches" uses the per-stage
+   launches for everything; "persistent" runs all stages in one cooperative launch. All
+   three produce identical results. */
+enum
+{
+	B2G_SOLVER_COMPONENTS = 0,
+	B2G_SOLVER_LAUNCHES = 1,
+	B2G_SOLVER_PERSISTENT = 2,
+};
+
 struct b2gDeviceWorld
 {
 	cudaStream_t stream;
@@ -32,7 +43,9 @@ struct b2gDeviceWorld
 	float pairsMs, collideMs, solveMs, finalizeMs; /* accumulated device time per stage */
 	long long h2dBytes, d2hBytes;				   /* accumulated host<->device traffic */
 	long long launches;							   /* kernels launched */
-	int persistent;								   /* solver as one cooperative launch (default) */
+	int solverMode;								   /* B2G_SOLVER_* */
+	int compSkip;								   /* steps left before the next component analysis */
+	b2gCompBuffers comp;						   /* component solver scratch */
 	void* persistentScratch;					   /* barrier counter, generation, error, restitution flag */
 	/* bodies by id */
 	int bodyCap, bodyCount;
@@ -558,7 +571,9 @@ extern "C" int b2gDev_Create( b2gDeviceWorld** out )
 	dw->pairPerMove = 32;
 	{
 		const char* mode = getenv( "B2G_SOLVER" );
-		dw->persistent = !( mode != NULL && strcmp( mode, "launches" ) == 0 );
+		dw->solverMode = B2G_SOLVER_COMPONENTS;
+		if ( mode != NULL && strcmp( mode, "launches" ) == 0 ) dw->solverMode = B2G_SOLVER_LAUNCHES;
+		if ( mode != NULL && strcmp( mode, "persistent" ) == 0 ) dw->solverMode = B2G_SOLVER_PERSISTENT;
 	}
 	*out = dw;
 	return 0;
@@ -576,6 +591,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->tree[1],	  dw->tree[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  dw->moveKeys,
 					  dw->moveBoxes,  dw->moveShapes, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
 					  dw->enlargedBoxes, dw->counters, dw->persistentScratch };
+	b2gDev_CompFree( &dw->comp );
 	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
 		if ( dptrs[i] ) cudaFree( dptrs[i] );
 	void* hptrs[] = { dw->hCounters, dw->hChanges, dw->hRecs, dw->hBoxes, dw->hPairs, dw->hPairCounts };
@@ -1040,7 +1056,35 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	int ovCount0 = total - overflowBegin;
 	d_jointBodies jb0 = { dw->xf, dw->center, dw->localCenter, dw->invMass, dw->invI, dw->awakeIndex };
 	CK( cudaEventRecord( dw->ev[6], dw->stream ) );
-	if ( dw->persistent )
+	bool solved = false;
+	if ( dw->solverMode == B2G_SOLVER_COMPONENTS && dw->compSkip > 0 ) dw->compSkip -= 1;
+	else if ( dw->solverMode == B2G_SOLVER_COMPONENTS && awakeCount < ( 1 << B2G_CURSOR_BODY_BITS ) &&
+			  total < ( 1 << B2G_CURSOR_CONTACT_BITS ) && jointTotal < ( 1 << B2G_CURSOR_JOINT_BITS ) )
+	{
+		int forceBig = ovJointCount0 + ovCount0 > 0;
+		CK2( b2gDev_CompAnalyze( &dw->comp, &a, dw->jointOffsets, dw->awakeIndex, total, jointTotal, forceBig, dw->stream,
+								 &dw->launches ) );
+		const b2gCompSummary* hs = dw->comp.hSummary;
+		if ( hs->smallComponents > 0 )
+		{
+			CK2( b2gDev_CompSolveBins( &dw->comp, &a, dw->jointOffsets, &jb0, dw->counters, dw->stream, &dw->launches ) );
+			if ( hs->bigComponents > 0 )
+				CK2( b2gDev_CompSolveBig( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, total, jointTotal,
+										  dw->stream, &dw->launches ) );
+			solved = true;
+		}
+		/* mostly one big component: skip the analysis for a while */
+		if ( 10ll * hs->bigBodies > 9ll * awakeCount || hs->smallComponents == 0 ) dw->compSkip = 15;
+	}
+	if ( solved )
+	{
+		CK( cudaEventRecord( dw->ev[7], dw->stream ) );
+		k_finalizeBodies<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( f );
+		dw->launches += 1;
+		CK( cudaGetLastError() );
+		CK( cudaEventRecord( dw->ev[8], dw->stream ) );
+	}
+	else if ( dw->solverMode == B2G_SOLVER_PERSISTENT )
 	{
 		/* one cooperative launch: solver stages and finalize */
 		int ranges[4 * B2_GRAPH_COLOR_COUNT];
@@ -1153,7 +1197,7 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 		cudaEventElapsedTime( &ms, dw->ev[7], dw->ev[8] );
 		dw->finalizeMs += ms;
 	}
-	if ( dw->persistent )
+	if ( solved == false && dw->solverMode == B2G_SOLVER_PERSISTENT )
 	{
 		int err = 0;
 		CK( cudaMemcpy( &err, (int*)dw->persistentScratch + 2, sizeof( int ), cudaMemcpyDeviceToHost ) );

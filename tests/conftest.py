@@ -6,6 +6,7 @@ import json
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -43,3 +44,20 @@ def oracle():
 def gpu_lib():
     """The GB300 library; fails (does not skip) when it is missing on a GPU run."""
     return B.load_library()
+
+
+def lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps, check_every=1):
+    """Step the same scene on the GB300 library and the oracle; every `check_every` steps the
+    body states must be bit-identical, and at the end the contact tables too."""
+    with B.Scene(gpu_lib, kind, a, b, c, seed, flags) as g, B.Scene(oracle, kind, a, b, c, seed, flags) as o:
+        for k in range(1, steps + 1):
+            g.step()
+            o.step()
+            if k % check_every == 0 or k == steps:
+                if g.state_hash() != o.state_hash():
+                    gs, os_ = g.state(), o.state()
+                    bad = np.nonzero((gs.view(np.uint32) != os_.view(np.uint32)).any(1))[0]
+                    pytest.fail(f"state differs at step {k} in {len(bad)} bodies, first {bad[:5]}")
+        gc, oc = g.contacts(), o.contacts()
+        assert gc.shape == oc.shape and (gc == oc).all(), "contact tables differ"
+        return g.body_count, gc.shape[0]

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import box2d_gb300 as B
-from conftest import golden_cases, load_golden
+from conftest import golden_cases, load_golden, lockstep
 
 pytestmark = pytest.mark.gpu
 
@@ -31,19 +31,8 @@ def test_gpu_matches_reference_fixture(gpu_lib, name):
                     f"{name}: contact table (ids, pairs, colors, feature ids) at step {k}"
 
 
-def _lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps, check_every=1):
-    with B.Scene(gpu_lib, kind, a, b, c, seed, flags) as g, B.Scene(oracle, kind, a, b, c, seed, flags) as o:
-        for k in range(1, steps + 1):
-            g.step()
-            o.step()
-            if k % check_every == 0 or k == steps:
-                if g.state_hash() != o.state_hash():
-                    gs, os_ = g.state(), o.state()
-                    bad = np.nonzero((gs.view(np.uint32) != os_.view(np.uint32)).any(1))[0]
-                    pytest.fail(f"state differs at step {k} in {len(bad)} bodies, first {bad[:5]}")
-        gc, oc = g.contacts(), o.contacts()
-        assert gc.shape == oc.shape and (gc == oc).all(), "contact tables differ"
-        return g.body_count, gc.shape[0]
+def _lockstep(*args, **kw):
+    return lockstep(*args, **kw)
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3, 4])

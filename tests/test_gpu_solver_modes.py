@@ -1,0 +1,33 @@
+"""The three solver strategies of the GB300 library -- connected components in shared
+memory (default), one launch per color stage, one cooperative launch -- must each match
+the oracle bit for bit. The scenes cover worlds whose components are all small, worlds
+that mix one big component with small ones, joints inside shared-memory bins, and
+restitution."""
+from __future__ import annotations
+
+import pytest
+
+import box2d_gb300 as B
+from conftest import lockstep
+
+pytestmark = pytest.mark.gpu
+
+MODES = ["components", "launches", "persistent"]
+
+# (id, kind, a, b, c, seed, flags, steps)
+CASES = [
+    ("pyramids_all_small", B.MANY_PYRAMIDS_RAIN, 4, 10, 200, 0, B.NO_CONTINUOUS, 60),
+    ("pyramids_big_and_small", B.MANY_PYRAMIDS_RAIN, 2, 30, 600, 0, B.NO_CONTINUOUS, 40),
+    ("joint_grid_in_bins", B.JOINT_GRID_MIXED, 6, 20, 0, 5, B.NO_CONTINUOUS, 80),
+    ("joint_grid_big", B.JOINT_GRID_MIXED, 20, 60, 0, 5, B.NO_CONTINUOUS, 60),
+    ("shape_zoo_restitution", B.SHAPE_ZOO, 150, 0, 0, 2, B.NO_CONTINUOUS, 100),
+    ("batch_world", B.BATCH_WORLD, 0, 0, 0, 22, B.NO_CONTINUOUS, 100),
+]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_solver_mode_matches_oracle(gpu_lib, oracle, monkeypatch, mode, case):
+    monkeypatch.setenv("B2G_SOLVER", mode)
+    _, kind, a, b, c, seed, flags, steps = case
+    lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps)
