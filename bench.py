@@ -107,6 +107,10 @@ def algorithmic_bytes(counters: np.ndarray, awake: int, substeps: int, restituti
     return float(b)
 
 
+HOST_PHASES = ["tree_upload", "pair_query", "contact_create", "tree_rebuild", "narrowphase", "state_pass", "uploads",
+               "solver", "enlarge"]
+
+
 def run_gpu(args, rank: int, world_size: int) -> dict:
     import torch
 
@@ -122,6 +126,7 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
         scene.step()
     torch.cuda.synchronize()
     scene.timings(reset=True)
+    scene.host_profile(reset=True)
     counters_before = scene.counters()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -143,6 +148,7 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
         torch.distributed.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     stage_ms, traffic = scene.timings(reset=True)
+    host_ms = scene.host_profile(reset=True)
     total_ms = float(sum(step_ms))
     solver_ms = float(stage_ms[2])
     launches = int(traffic[2])
@@ -168,6 +174,7 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
         "e2e_value": dyn * e2e_steps / e2e_s, "e2e_h2d": float(e2e_traffic[0]) / e2e_steps,
         "e2e_d2h": float(e2e_traffic[1] + move_bytes) / e2e_steps, "counters": counters.tolist(),
         "stage_ms": stage_ms.tolist(), "desc": desc, "counters_before": counters_before.tolist(),
+        "host_ms": host_ms.tolist(),
     }
 
 
@@ -260,6 +267,7 @@ def main() -> None:
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "stage_ms_per_step": [x / args.steps for x in r["stage_ms"]],
+        "host_ms_per_step": {k: v / args.steps for k, v in zip(HOST_PHASES, r["host_ms"])},
     }
     print(json.dumps(line))
 

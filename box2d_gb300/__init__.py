@@ -52,6 +52,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2p_timings": (c_int, [c_u32, c_p, c_p, c_int]),
         "b2p_stream": (c_p, [c_u32]),
         "b2p_status": (c_int, [c_u32]),
+        "b2p_host_profile": (c_int, [c_u32, c_p, c_int]),
     }
     for name, (res, args) in optional.items():
         if hasattr(lib, name):
@@ -127,6 +128,14 @@ class Scene:
         traffic = np.zeros(3, np.int64)
         self.lib.b2p_timings(self.world_id, ms.ctypes.data, traffic.ctypes.data, int(reset))
         return ms, traffic
+
+    def host_profile(self, reset: bool = False) -> np.ndarray:
+        """Accumulated host time per step phase (ms): tree upload, pair query, contact
+        creation, tree rebuild, narrowphase, contact-state pass, uploads, solver, proxy
+        enlargement, unused."""
+        out = np.zeros(10, np.float32)
+        self.lib.b2p_host_profile(self.world_id, out.ctypes.data, int(reset))
+        return out
 
     def counters(self) -> np.ndarray:
         out = np.zeros(30, np.int32)

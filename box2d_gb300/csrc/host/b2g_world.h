@@ -132,6 +132,8 @@ typedef struct h_world
 	int stepIndex;
 	int recycledContactCount;
 	b2Profile profile;
+	/* accumulated host-side time per step phase (ms), see H_PHASE_* */
+	float hostMs[10];
 	/* device mirror */
 	b2gDeviceWorld* dev;
 	int devReady;			/* device arrays hold the current world */
@@ -170,5 +172,20 @@ void h_fail( h_world* w, const char* what, int code );
 #define H_PROXY_TYPE( K ) ( (b2BodyType)( ( K ) & 3 ) )
 #define H_PROXY_ID( K ) ( ( K ) >> 2 )
 #define H_PROXY_KEY( ID, T ) ( ( ( ID ) << 2 ) | ( T ) )
+
+/* host phases timed per step */
+enum
+{
+	H_PHASE_TREE_UPLOAD = 0,
+	H_PHASE_PAIR_QUERY = 1,	  /* device pair query call, includes its wait */
+	H_PHASE_CONTACT_CREATE = 2,
+	H_PHASE_TREE_REBUILD = 3,
+	H_PHASE_COLLIDE = 4, /* device narrowphase call, includes its wait */
+	H_PHASE_STATE_PASS = 5,
+	H_PHASE_UPLOADS = 6, /* contact / color / joint uploads */
+	H_PHASE_SOLVE = 7,	 /* device solver + finalize call, includes its wait */
+	H_PHASE_ENLARGE = 8,
+	H_PHASE_COUNT = 10,
+};
 
 #endif

@@ -107,3 +107,16 @@ B2P_EXPORT void* b2p_stream( uint32_t packedWorldId )
 	h_world* w = h_worldFromId( id );
 	return w == NULL ? NULL : b2gDev_Stream( w->dev );
 }
+
+/* accumulated host time per step phase since the last reset, in ms: tree upload, pair
+   query, contact creation, tree rebuild, narrowphase, contact-state pass, contact / color /
+   joint uploads, solver, proxy enlargement, (unused) */
+B2P_EXPORT int b2p_host_profile( uint32_t packedWorldId, float* out, int reset )
+{
+	b2WorldId id = { (uint16_t)( packedWorldId >> 16 ), (uint16_t)( packedWorldId & 0xFFFF ) };
+	h_world* w = h_worldFromId( id );
+	if ( w == NULL ) return -1;
+	memcpy( out, w->hostMs, sizeof( w->hostMs ) );
+	if ( reset ) memset( w->hostMs, 0, sizeof( w->hostMs ) );
+	return 0;
+}

@@ -15,6 +15,14 @@
 
 static float h_ms( uint64_t t0 ) { return b2GetMilliseconds( t0 ); }
 
+/* add the time since *t to phase `phase` and restart *t */
+static void h_lap( h_world* w, int phase, uint64_t* t )
+{
+	uint64_t now = b2GetTicks();
+	w->hostMs[phase] += b2GetMilliseconds( *t );
+	*t = now;
+}
+
 /* upload one broadphase tree as device query nodes */
 static void h_uploadTree( h_world* w, int type )
 {
@@ -58,11 +66,13 @@ static void h_updatePairs( h_world* w )
 {
 	int moveCount = w->moveArray.count;
 	if ( moveCount == 0 ) return;
+	uint64_t lap = b2GetTicks();
 	if ( w->treesDirty )
 	{
 		for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
 		w->treesDirty = 0;
 	}
+	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
 	float* boxes = malloc( (size_t)moveCount * 4 * sizeof( float ) );
 	int* shapeIds = malloc( (size_t)moveCount * sizeof( int ) );
 	for ( int i = 0; i < moveCount; ++i )
@@ -81,6 +91,7 @@ static void h_updatePairs( h_world* w )
 	int total = 0;
 	int rc = b2gDev_FindPairs( w->dev, w->moveArray.data, boxes, shapeIds, moveCount, &pairs, &counts, &total );
 	if ( rc != 0 ) h_fail( w, "pair query", rc );
+	h_lap( w, H_PHASE_PAIR_QUERY, &lap );
 	int offset = 0;
 	for ( int i = 0; i < moveCount; ++i )
 	{
@@ -103,10 +114,12 @@ static void h_updatePairs( h_world* w )
 	}
 	free( boxes );
 	free( shapeIds );
+	h_lap( w, H_PHASE_CONTACT_CREATE, &lap );
 	/* b2UpdateTreesTask (broad_phase.c:401-410) */
 	h_treeRebuild( w->trees + b2_dynamicBody, 0 );
 	h_treeRebuild( w->trees + b2_kinematicBody, 0 );
 	w->treesDirty = 1;
+	h_lap( w, H_PHASE_TREE_REBUILD, &lap );
 	for ( int i = 0; i < w->moveArray.count; ++i )
 	{
 		int key = w->moveArray.data[i];
@@ -310,20 +323,26 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 
 	/* narrowphase + state pass */
 	t0 = b2GetTicks();
+	uint64_t lap = t0;
 	h_flushContacts( w );
 	h_uploadColors( w );
+	h_lap( w, H_PHASE_UPLOADS, &lap );
 	const int* changes = NULL;
 	int changeCount = 0, recycled = 0;
 	int rc = b2gDev_Collide( w->dev, &p, w->contactIdPool.nextIndex, &changes, &changeCount, &recycled );
 	if ( rc != 0 ) h_fail( w, "narrowphase", rc );
+	h_lap( w, H_PHASE_COLLIDE, &lap );
 	w->recycledContactCount = recycled;
 	h_contactStatePass( w, changes, changeCount );
+	h_lap( w, H_PHASE_STATE_PASS, &lap );
 	h_flushContacts( w );
+	h_lap( w, H_PHASE_UPLOADS, &lap );
 	w->profile.collide = h_ms( t0 );
 
 	if ( timeStep > 0.0f )
 	{
 		t0 = b2GetTicks();
+		lap = t0;
 		w->stepIndex += 1;
 		h_uploadColors( w );
 		h_uploadJoints( w );
@@ -345,12 +364,15 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 		int enlargedCount = 0, status = 0;
 		if ( w->awakeBodyIds.count > 0 )
 		{
+			h_lap( w, H_PHASE_UPLOADS, &lap );
 			rc = b2gDev_Solve( w->dev, &p, activeColors, activeCount, contactCounts, jointCounts, w->awakeBodyIds.count, &recs,
 							   &enlargedCount, &boxes, &status );
 			if ( rc != 0 ) h_fail( w, "solver", rc );
+			h_lap( w, H_PHASE_SOLVE, &lap );
 			w->lastStatus = status;
 			if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
 			h_enlargeProxies( w, recs, boxes, enlargedCount );
+			h_lap( w, H_PHASE_ENLARGE, &lap );
 		}
 		w->profile.solve = h_ms( t0 );
 	}

@@ -31,6 +31,12 @@ int b2p_status( uint32_t packedWorldId );
    (to device, to host) and kernels launched, as traffic[0..2]. reset != 0 zeroes them after reading. */
 int b2p_timings( uint32_t packedWorldId, float* stageMs, long long* traffic, int reset );
 
+/* Accumulated host time per step phase since the last reset, in ms, 10 floats: tree
+   upload, pair query, contact creation, tree rebuild, narrowphase, contact-state pass,
+   contact/color/joint uploads, solver, proxy enlargement, unused. Device waits are
+   included in the phase that waits. reset != 0 zeroes them after reading. */
+int b2p_host_profile( uint32_t packedWorldId, float* out, int reset );
+
 /* The CUDA stream (cudaStream_t) the world's kernels are launched on. */
 void* b2p_stream( uint32_t packedWorldId );
 
