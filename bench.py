@@ -38,6 +38,10 @@ sys.path.insert(0, str(ROOT))
 
 import box2d_gb300 as B  # noqa: E402
 
+# untimed steps before the warm-up: the many-pyramids rain reaches the pyramids after about
+# 150 steps, so the timed window starts where the scene's contact churn does
+START_STEPS = {"many_pyramids": 200, "large_pyramid": 0, "joint_grid": 0}
+
 WORKLOADS = {
     # name: (kind, a, b, c, seed, flags, description)
     "many_pyramids": (B.MANY_PYRAMIDS_RAIN, 20, 10, 2000, 0, B.NO_CONTINUOUS,
@@ -122,6 +126,7 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
     dyn = scene.dynamic_count
     stream = torch.cuda.ExternalStream(lib.b2p_stream(scene.world_id))
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    scene.step(args.start_step)
     for _ in range(args.warmup):
         scene.step()
     torch.cuda.synchronize()
@@ -153,15 +158,20 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
     solver_ms = float(stage_ms[2])
     launches = int(traffic[2])
 
-    # end to end: step + read every transform back through the public API, wall clock
+    # end to end: step + the step's body move events (b2World_GetBodyEvents, every awake
+    # body's transform) read back through the public API, wall clock
     scene.timings(reset=True)
+    events = np.zeros((scene.body_count, 4), np.float32)
     t0 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 200))
     move_bytes = 0
+    step_s = 0.0
     for _ in range(e2e_steps):
+        t1 = time.perf_counter()
         scene.step()
-        st = scene.state()
-        move_bytes += st.nbytes
+        step_s += time.perf_counter() - t1
+        ev = scene.move_events(events)
+        move_bytes += ev.nbytes
     e2e_s = time.perf_counter() - t0
     _, e2e_traffic = scene.timings(reset=True)
     counters = scene.counters()
@@ -172,9 +182,10 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
         "total_ms": total_ms, "step_ms": step_ms, "dyn": dyn, "solver_ms": solver_ms, "alg_bytes": alg_bytes,
         "achieved_gbs": achieved, "peak": pk, "launches": launches, "clocks": clocks.summary,
         "e2e_value": dyn * e2e_steps / e2e_s, "e2e_h2d": float(e2e_traffic[0]) / e2e_steps,
-        "e2e_d2h": float(e2e_traffic[1] + move_bytes) / e2e_steps, "counters": counters.tolist(),
+        "e2e_d2h": float(e2e_traffic[1]) / e2e_steps, "counters": counters.tolist(),
         "stage_ms": stage_ms.tolist(), "desc": desc, "counters_before": counters_before.tolist(),
-        "host_ms": host_ms.tolist(),
+        "host_ms": host_ms.tolist(), "e2e_step_ms": 1e3 * step_s / e2e_steps,
+        "e2e_read_ms": 1e3 * (e2e_s - step_s) / e2e_steps,
     }
 
 
@@ -183,6 +194,7 @@ def run_cpu_sample(args, budget_s: float, max_steps: int) -> dict:
     kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
     lib = B.load_library(ROOT / "oracle" / "liboracle.so")
     scene = B.Scene(lib, kind, a, b, c, seed, flags)
+    scene.step(args.start_step)
     for _ in range(max(1, args.warmup)):
         scene.step()
     t0 = time.perf_counter()
@@ -204,13 +216,18 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="many_pyramids", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--start-step", type=int, default=-1,
+                    help="untimed steps before the warm-up (default: per workload)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.start_step < 0:
+        args.start_step = START_STEPS[args.workload]
 
     rank = int(os.environ.get("RANK", "0"))
     world_size = int(os.environ.get("WORLD_SIZE", "1"))
     kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
     config = {"workload": args.workload, "description": desc, "dt": 1.0 / 60.0, "substeps": 4,
+              "timed_window": f"steps {args.start_step + args.warmup + 1}..{args.start_step + args.warmup + args.steps}",
               "continuous": not bool(flags & B.NO_CONTINUOUS), "sleep": False,
               "l2": "flushed between timed steps (256 MiB write, outside the timed region)",
               "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single world"}
@@ -225,7 +242,7 @@ def main() -> None:
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded scene builders)", "config": config, "impl": "reference",
                 "cpu_baseline": {"value": r["value"], "unit": "body-steps/s", "cores": cores, "kind": "port",
-                                 "sample": f"{r['steps']} steps after {args.warmup} warm-up steps, serial C oracle"},
+                                 "sample": f"{r['steps']} steps after {args.start_step + args.warmup} untimed steps, serial C oracle"},
                 "e2e": {"value": r["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -250,7 +267,8 @@ def main() -> None:
     if not args.no_cpu_baseline:
         c = run_cpu_sample(args, budget_s=20.0, max_steps=400)
         cpu = {"value": c["value"], "unit": "body-steps/s", "cores": 1, "kind": "port",
-               "sample": f"{c['steps']} steps ({c['seconds']:.1f} s) of the same world after warm-up, serial C oracle"}
+               "sample": f"{c['steps']} steps ({c['seconds']:.1f} s) of the same world after "
+                         f"{args.start_step + args.warmup} untimed steps, serial C oracle"}
     pk = r["peak"]
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
@@ -263,7 +281,8 @@ def main() -> None:
                      "solver_ms_per_step": r["solver_ms"] / args.steps},
         "cpu_baseline": cpu,
         "e2e": {"value": r["e2e_value"] * world_size, "unit": "body-steps/s", "h2d_bytes_per_step": r["e2e_h2d"],
-                "d2h_bytes_per_step": r["e2e_d2h"]},
+                "d2h_bytes_per_step": r["e2e_d2h"], "step_ms": r["e2e_step_ms"], "read_ms": r["e2e_read_ms"],
+                "read": "b2World_GetBodyEvents after every step (transforms of all awake bodies)"},
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
         "stage_ms_per_step": [x / args.steps for x in r["stage_ms"]],

@@ -41,6 +41,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2s_dynamic_count": (c_int, [c_int]),
         "b2s_world_id": (c_u32, [c_int]),
         "b2s_get_state": (None, [c_int, c_p]),
+        "b2s_move_events": (c_int, [c_int, c_p, c_int]),
         "b2s_state_hash": (c_u64, [c_int]),
         "b2s_set_velocities": (None, [c_int, c_p]),
         "b2s_target": (None, [c_int, c_p]),
@@ -99,6 +100,13 @@ class Scene:
         out = np.zeros((self.body_count, 7), np.float32)
         self.lib.b2s_get_state(self.handle, out.ctypes.data)
         return out
+
+    def move_events(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Transforms (p.x, p.y, q.c, q.s) of the last step's body move events."""
+        if out is None or out.shape[0] < self.body_count:
+            out = np.zeros((self.body_count, 4), np.float32)
+        n = self.lib.b2s_move_events(self.handle, out.ctypes.data, out.shape[0])
+        return out[:n]
 
     def state_hash(self) -> int:
         return int(self.lib.b2s_state_hash(self.handle))

@@ -21,9 +21,10 @@ LIB = PKG / "libbox2d_gb300.so"
 
 HOST_SOURCES = ["csrc/host/world.c", "csrc/host/step.c", "csrc/host/joint.c", "csrc/host/tree.c",
                 "csrc/host/geometry.c", "csrc/host/probe.c", "scenes/scenes.c"]
-# (source, extra nvcc flags). The persistent solver reads state written by other SMs
-# between grid barriers, so its global loads bypass L1 (-dlcm=cg).
+# (source, extra nvcc flags). The cluster and persistent solvers read state written by
+# other SMs between barriers, so their global loads bypass L1 (-dlcm=cg).
 DEVICE_SOURCES = [("csrc/device/world.cu", []), ("csrc/device/components.cu", []),
+                  ("csrc/device/cluster.cu", ["-Xptxas", "-dlcm=cg"]),
                   ("csrc/device/persistent.cu", ["-Xptxas", "-dlcm=cg"])]
 
 NVCC_FLAGS = ["-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
@@ -77,7 +78,7 @@ def build_library(force: bool = False) -> Path:
         list(ex.map(_run, jobs))
     if force or jobs or _needs(LIB, objects):
         _run([nvcc, "-shared", "-cudart", "static", "-gencode", "arch=compute_103a,code=sm_103a", "-o", str(LIB),
-              *[str(o) for o in objects], "-Xlinker", "-Bsymbolic", "-lm"])
+              *[str(o) for o in objects], "-Xlinker", "-Bsymbolic", "-lm", "-lpthread"])
     return LIB
 
 

@@ -188,6 +188,10 @@ int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int* awakeBody
 						const float* params, const float* center0 );
 int b2gDev_DownloadAwake( b2gDeviceWorld* dw, int awakeCount, float* stateV, float* stateD, float* params, float* center0 );
 int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* center, uint32_t* typeFlags );
+/* body transforms (4 floats), centers (2), flags and awake velocities (4) in one wait;
+   the pointers refer to page-locked staging valid until the next call */
+int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awakeCount, const float** xf, const float** center,
+						  const uint32_t** flags, const float** stateV );
 int b2gDev_DownloadShapeBoxes( b2gDeviceWorld* dw, int shapeCount, float* aabbs, float* fatAABBs );
 int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float vx, float vy, float w, int which );
 
@@ -213,7 +217,25 @@ typedef struct b2gTreeNode
 	int categoryNonZero; /* the node's category bits intersect the query mask (all ones) */
 } b2gTreeNode;
 
-int b2gDev_UploadTree( b2gDeviceWorld* dw, int treeType, const b2gTreeNode* nodes, int nodeCount, int root );
+/* host tree node (dynamic_tree.c b2TreeNode fields), uploaded as is */
+typedef struct b2gHostTreeNode
+{
+	b2AABB aabb;
+	uint64_t categoryBits;
+	int child1, child2; /* internal nodes */
+	uint64_t userData;	/* leaves: shape id */
+	int parent;
+	uint16_t height;
+	uint16_t flags; /* 0x4: leaf */
+} b2gHostTreeNode;
+
+/* copy nodeCount host nodes to the device and convert them to query nodes on the
+   device. The host array must stay unchanged until the next pair query returns. */
+int b2gDev_UploadTree( b2gDeviceWorld* dw, int treeType, const b2gHostTreeNode* nodes, int nodeCount, int root );
+
+/* page-locked host memory (NULL on failure) for arrays uploaded every step */
+void* b2gDev_HostAlloc( size_t bytes );
+void b2gDev_HostFree( void* p );
 /* query each moved proxy's fat AABB; pairs come back grouped per move in the reference's
    order (proxy list newest first). outPairs holds (shapeA, shapeB); outCounts per move */
 int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* moveProxyKeys, const float* moveBoxes, const int* moveShapeIds,

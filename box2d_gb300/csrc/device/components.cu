@@ -568,6 +568,11 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 	k_compAssign<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->compData, b->binRange, b->binCap, b->summary, n, forceBig );
 	*launches += 1;
 	CKC( cudaGetLastError() );
+	/* the lists now, so the summary read below carries the big components' per-color counts */
+	d_compArgs c = compArgs( b, jointOffsets, awakeIndex );
+	k_compScatter<<<compBlocks( n + cons ), B2G_COMP_THREADS, 0, stream>>>( *a, c, n, total, jointTotal );
+	*launches += 1;
+	CKC( cudaGetLastError() );
 	CKC( cudaMemcpyAsync( b->hSummary, b->summary, sizeof( b2gCompSummary ), cudaMemcpyDeviceToHost, stream ) );
 	CKC( cudaStreamSynchronize( stream ) );
 	return 0;
@@ -585,9 +590,6 @@ extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, co
 		s_configured = 1;
 	}
 	d_compArgs c = compArgs( b, jointOffsets, b->awakeIndex );
-	int items = b->n + b->total + b->jointTotal;
-	k_compScatter<<<compBlocks( items ), B2G_COMP_THREADS, 0, stream>>>( *a, c, b->n, b->total, b->jointTotal );
-	*launches += 1;
 	unsigned long long cur = b->hSummary->cursor;
 	long long bo = (long long)( cur >> ( B2G_CURSOR_CONTACT_BITS + B2G_CURSOR_JOINT_BITS ) );
 	long long co = (long long)( ( cur >> B2G_CURSOR_JOINT_BITS ) & ( ( 1ull << B2G_CURSOR_CONTACT_BITS ) - 1 ) );

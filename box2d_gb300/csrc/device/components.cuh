@@ -65,8 +65,9 @@ struct b2gCompBuffers
 extern "C" int b2gDev_CompReserve( b2gCompBuffers* b, int awake, int slots, int joints );
 extern "C" void b2gDev_CompFree( b2gCompBuffers* b );
 
-/* find components and pack the small ones into bins; waits for the summary. forceBig puts
-   every component on the global path (an overflow color exists). */
+/* find components, pack the small ones into bins and build the component-contiguous and
+   big-component lists; waits for the summary. forceBig puts every component on the
+   global path (an overflow color exists). */
 extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const int* awakeIndex,
 								   int total, int jointTotal, int forceBig, cudaStream_t stream, long long* launches );
 
@@ -78,4 +79,10 @@ extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, co
 /* global per-color path over the big components' constraints */
 extern "C" int b2gDev_CompSolveBig( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
 									const int* activeColors, int activeColorCount, int total, int jointTotal,
+									cudaStream_t stream, long long* launches );
+
+/* cluster solver (cluster.cu) over every constraint (useLists = 0) or the big-component
+   lists; 0 = launched, -1 = does not fit a cluster, else a CUDA error */
+extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
+									const int* activeColors, int activeColorCount, int useLists, int bodyCount,
 									cudaStream_t stream, long long* launches );

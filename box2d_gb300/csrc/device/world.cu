@@ -26,7 +26,8 @@
 
 /* solver strategies, chosen per world from the B2G_SOLVER environment variable at creation:
    "components" (default) solves small connected components one CTA each out of shared
-   memory and the rest with one launch per color stage; "launches" uses the per-stage
+   memory and the rest in one thread-block cluster (or, when they do not fit one, with one
+   launch per color stage); "launches" uses the per-stage
    launches for everything; "persistent" runs all stages in one cooperative launch. All
    three produce identical results. */
 enum
@@ -45,6 +46,8 @@ struct b2gDeviceWorld
 	long long launches;							   /* kernels launched */
 	int solverMode;								   /* B2G_SOLVER_* */
 	int compSkip;								   /* steps left before the next component analysis */
+	int compValid;								   /* the component lists match the current constraint graph */
+	int topologyDirty;							   /* colors, joints or the awake set changed since the analysis */
 	b2gCompBuffers comp;						   /* component solver scratch */
 	void* persistentScratch;					   /* barrier counter, generation, error, restitution flag */
 	/* bodies by id */
@@ -94,12 +97,33 @@ struct b2gDeviceWorld
 	/* broadphase */
 	b2gTreeNode* tree[3];
 	int treeCap[3], treeRoot[3];
+	b2gHostTreeNode* treeRaw[3]; /* host node arrays as uploaded */
+	int treeRawCap[3];
 	unsigned char* moved[3];
 	int movedCap[3];
 	int* moveKeys;
 	float4* moveBoxes;
 	int* moveShapes;
 	int moveCap;
+	void* moveStage; /* device: boxes, keys, shapes of the moved proxies */
+	int moveStageCap;
+	void* hMoveStage; /* pinned host staging of the same */
+	int hMoveStageCap;
+	int* pairPacked; /* pairs packed per move at atomically claimed offsets */
+	int* pairOffsets;
+	int pairPackedCap, pairOffsetsCap;
+	int* hPairOffsets;
+	int* hPairPacked;
+	int hPairOffsetsCap, hPairPackedCap;
+	int pairWindow;	  /* pairs copied back with the counters */
+	int changeWindow; /* state changes copied back with the counters */
+	int recWindow;	  /* enlarged-proxy records copied back with the counters */
+	int pairsTimingPending;
+	/* upload arena (page-locked host + device) */
+	void* upHost;
+	void* upDev;
+	int upCap;
+	size_t upUsed;
 	int* pairBuf;
 	int* pairCounts;
 	int pairPerMove;
@@ -123,6 +147,16 @@ struct b2gDeviceWorld
 	int hPairsCap, hPairCountsCap;
 	int* hSortTmp;
 	int hSortTmpCap;
+	int* hRecsRaw;
+	float* hBoxesRaw;
+	int hRecsRawCap, hBoxesRawCap;
+	void* hSortKeys;
+	int hSortKeysCap;
+	float4* hXf;
+	float2* hCenter;
+	uint32_t* hFlags;
+	float4* hStateV;
+	int hXfCap, hCenterCap, hFlagsCap, hStateVCap;
 };
 
 #define CK( x )                                                                                                                \
@@ -157,7 +191,11 @@ static int growHost( void** ptr, int* cap, int need, size_t elem )
 	while ( nc < need ) nc *= 2;
 	void* p = NULL;
 	CK( cudaMallocHost( &p, (size_t)nc * elem ) );
-	if ( *ptr != NULL ) CK( cudaFreeHost( *ptr ) );
+	if ( *ptr != NULL )
+	{
+		if ( *cap > 0 ) memcpy( p, *ptr, (size_t)( *cap ) * elem );
+		CK( cudaFreeHost( *ptr ) );
+	}
 	*ptr = p;
 	*cap = nc;
 	return 0;
@@ -184,7 +222,10 @@ static __device__ __forceinline__ bool d_overlaps( b2AABB a, float4 b )
 
 /* one thread per moved proxy; stack DFS with child1 pushed before child2, as
    b2DynamicTree_Query (dynamic_tree.c:1085-1135); dedupe as b2PairQueryCallback
-   (broad_phase.c:172-219). Hits are written in visit order. */
+   (broad_phase.c:172-219). Hits are written in visit order. Both children of a popped
+   node are loaded and tested together and only overlapping ones are pushed: the visit
+   order of the overlapping nodes is the reference's, with half the dependent loads. A
+   stack entry is (child1, child2) of an overlapping internal node, or (~leaf node, shape). */
 __global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat, const b2gTreeNode* __restrict__ tKin, int rootKin,
 							 const b2gTreeNode* __restrict__ tDyn, int rootDyn, const unsigned char* __restrict__ movedDyn,
 							 const int* __restrict__ keys, const float4* __restrict__ boxes, const int* __restrict__ queryShapes,
@@ -198,7 +239,7 @@ __global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat
 	float4 box = boxes[i];
 	int queryShape = queryShapes[i];
 	int count = 0;
-	int stack[B2G_PAIR_STACK];
+	int2 stack[B2G_PAIR_STACK];
 	for ( int pass = 0; pass < 3; ++pass )
 	{
 		int treeType;
@@ -226,14 +267,18 @@ __global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat
 		}
 		if ( root < 0 ) continue;
 		int sp = 0;
-		stack[sp++] = root;
+		{
+			const b2gTreeNode r = nodes[root];
+			if ( d_overlaps( r.aabb, box ) == false || r.categoryNonZero == 0 ) continue;
+			stack[sp++] = r.isLeaf ? make_int2( ~root, r.child1 ) : make_int2( r.child1, r.child2 );
+		}
+		bool full = false;
 		while ( sp > 0 )
 		{
-			int nodeId = stack[--sp];
-			const b2gTreeNode node = nodes[nodeId];
-			if ( d_overlaps( node.aabb, box ) == false || node.categoryNonZero == 0 ) continue;
-			if ( node.isLeaf )
+			int2 e = stack[--sp];
+			if ( e.x < 0 )
 			{
+				int nodeId = ~e.x;
 				int proxyKey = ( nodeId << 2 ) | treeType;
 				if ( proxyKey == queryKey ) continue;
 				if ( queryType == b2_dynamicBody )
@@ -244,7 +289,7 @@ __global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat
 				{
 					if ( movedDyn[nodeId] ) continue;
 				}
-				int shapeId = node.child1;
+				int shapeId = e.y;
 				int a = proxyKey < queryKey ? shapeId : queryShape;
 				int b = proxyKey < queryKey ? queryShape : shapeId;
 				if ( count < capPerMove )
@@ -253,17 +298,24 @@ __global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat
 					pairs[2 * ( (size_t)i * capPerMove + count ) + 1] = b;
 				}
 				count += 1;
+				continue;
 			}
-			else
+			const b2gTreeNode c1 = nodes[e.x];
+			const b2gTreeNode c2 = nodes[e.y];
+			bool hit1 = d_overlaps( c1.aabb, box ) && c1.categoryNonZero != 0;
+			bool hit2 = d_overlaps( c2.aabb, box ) && c2.categoryNonZero != 0;
+			if ( sp + 2 > B2G_PAIR_STACK )
 			{
-				if ( sp + 2 > B2G_PAIR_STACK )
-				{
-					atomicOr( &counters->status, B2G_STATUS_CAPACITY );
-					break;
-				}
-				stack[sp++] = node.child1;
-				stack[sp++] = node.child2;
+				full = true;
+				break;
 			}
+			if ( hit1 ) stack[sp++] = c1.isLeaf ? make_int2( ~e.x, c1.child1 ) : make_int2( c1.child1, c1.child2 );
+			if ( hit2 ) stack[sp++] = c2.isLeaf ? make_int2( ~e.y, c2.child1 ) : make_int2( c2.child1, c2.child2 );
+		}
+		if ( full )
+		{
+			atomicOr( &counters->status, B2G_STATUS_CAPACITY );
+			break;
 		}
 	}
 	counts[i] = count;
@@ -588,13 +640,17 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->shapeStart, dw->shapeCount, dw->shapeList, dw->awakeBodyId,	dw->stateV,		  dw->stateD,
 					  dw->params,	  dw->center0,	 dw->enlargedBody, dw->shapes,		dw->aabb,		  dw->fat,
 					  dw->shapeEnlarged, dw->contacts, dw->colorIds,	dw->lanes,		dw->joints,		  dw->tree[0],
-					  dw->tree[1],	  dw->tree[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  dw->moveKeys,
-					  dw->moveBoxes,  dw->moveShapes, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
+					  dw->tree[1],	  dw->tree[2], dw->treeRaw[0], dw->treeRaw[1], dw->treeRaw[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  
+					  dw->moveStage, dw->pairPacked, dw->pairOffsets, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
 					  dw->enlargedBoxes, dw->counters, dw->persistentScratch };
 	b2gDev_CompFree( &dw->comp );
 	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
 		if ( dptrs[i] ) cudaFree( dptrs[i] );
-	void* hptrs[] = { dw->hCounters, dw->hChanges, dw->hRecs, dw->hBoxes, dw->hPairs, dw->hPairCounts };
+	if ( dw->upDev ) cudaFree( dw->upDev );
+	if ( dw->upHost ) cudaFreeHost( dw->upHost );
+	void* hptrs[] = { dw->hCounters, dw->hChanges,	   dw->hRecs,	   dw->hBoxes,	   dw->hPairs,	  dw->hPairCounts,
+					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw, dw->hSortKeys,
+					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV };
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
 		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
 	free( dw->hSortTmp );
@@ -648,6 +704,7 @@ extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const flo
 									 const int* awakeIndex, const uint32_t* typeFlags, const int* shapeStart,
 									 const int* shapeCount, const int* shapeList, int shapeListCount )
 {
+	dw->topologyDirty = 1;
 	int cap0 = dw->bodyCap, capOut = 0;
 	CK2( upload( dw, &dw->xf, &cap0, (const float4*)xf, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
@@ -695,6 +752,7 @@ extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const flo
 extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int* awakeBodyId, const float* stateV,
 									const float* stateD, const float* params, const float* center0 )
 {
+	dw->topologyDirty = 1;
 	int cap0 = dw->awakeCap, capOut = 0;
 	CK2( upload( dw, &dw->awakeBodyId, &cap0, awakeBodyId, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
@@ -722,6 +780,35 @@ extern "C" int b2gDev_DownloadAwake( b2gDeviceWorld* dw, int awakeCount, float* 
 	CK( ( dw->d2hBytes += (long long)( (size_t)awakeCount * sizeof( float4 ) ), cudaMemcpy( stateD, dw->stateD, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
 	CK( ( dw->d2hBytes += (long long)( (size_t)awakeCount * 8 * sizeof( float ) ), cudaMemcpy( params, dw->params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyDeviceToHost ) ) );
 	CK( ( dw->d2hBytes += (long long)( (size_t)awakeCount * sizeof( float4 ) ), cudaMemcpy( center0, dw->center0, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
+	return 0;
+}
+
+static int drain( b2gDeviceWorld* dw );
+
+/* transforms, centers and flags of every body and velocities of the awake bodies, in one
+   wait, into page-locked staging that stays valid until the next call */
+extern "C" int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awakeCount, const float** xf, const float** center,
+									 const uint32_t** flags, const float** stateV )
+{
+	int nb = bodyCount > 0 ? bodyCount : 1, na = awakeCount > 0 ? awakeCount : 1;
+	CK2( growHost( (void**)&dw->hXf, &dw->hXfCap, nb, sizeof( float4 ) ) );
+	CK2( growHost( (void**)&dw->hCenter, &dw->hCenterCap, nb, sizeof( float2 ) ) );
+	CK2( growHost( (void**)&dw->hFlags, &dw->hFlagsCap, nb, sizeof( uint32_t ) ) );
+	CK2( growHost( (void**)&dw->hStateV, &dw->hStateVCap, na, sizeof( float4 ) ) );
+	if ( bodyCount > 0 )
+	{
+		CK( cudaMemcpyAsync( dw->hXf, dw->xf, (size_t)bodyCount * sizeof( float4 ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hCenter, dw->center, (size_t)bodyCount * sizeof( float2 ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hFlags, dw->bodyFlags, (size_t)bodyCount * sizeof( uint32_t ), cudaMemcpyDeviceToHost, dw->stream ) );
+	}
+	if ( awakeCount > 0 )
+		CK( cudaMemcpyAsync( dw->hStateV, dw->stateV, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost, dw->stream ) );
+	dw->d2hBytes += (long long)bodyCount * 28 + (long long)awakeCount * 16;
+	CK2( drain( dw ) );
+	*xf = (const float*)dw->hXf;
+	*center = (const float*)dw->hCenter;
+	*flags = dw->hFlags;
+	*stateV = (const float*)dw->hStateV;
 	return 0;
 }
 
@@ -760,43 +847,92 @@ extern "C" int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity )
 	return 0;
 }
 
-static int stage( b2gDeviceWorld* dw, void** dptr, int* cap, const void* src, size_t bytes )
+/* Upload arena: small per-step uploads are copied into page-locked host memory and sent
+   with cudaMemcpyAsync on the world stream, so they need no wait. Arena space is reused
+   only after the stream has been drained (every step drains it at its readbacks). */
+static int arenaAlloc( b2gDeviceWorld* dw, size_t bytes, size_t* offset )
 {
-	CK2( grow( dptr, cap, (int)bytes, 1 ) );
-	CK( ( dw->h2dBytes += (long long)( bytes ), cudaMemcpyAsync( *dptr, src, bytes, cudaMemcpyHostToDevice, dw->stream ) ) );
-	CK( cudaStreamSynchronize( dw->stream ) );
+	size_t need = ( bytes + 15 ) & ~(size_t)15;
+	if ( dw->upUsed + need > (size_t)dw->upCap )
+	{
+		/* drain the stream: earlier uploads may still read the arena */
+		CK( cudaStreamSynchronize( dw->stream ) );
+		dw->upUsed = 0;
+		if ( need > (size_t)dw->upCap )
+		{
+			int nc = dw->upCap > 0 ? dw->upCap : 1 << 16;
+			while ( (size_t)nc < need ) nc *= 2;
+			if ( dw->upHost ) CK( cudaFreeHost( dw->upHost ) );
+			if ( dw->upDev ) CK( cudaFree( dw->upDev ) );
+			dw->upHost = NULL;
+			dw->upDev = NULL;
+			CK( cudaMallocHost( &dw->upHost, (size_t)nc ) );
+			CK( cudaMalloc( &dw->upDev, (size_t)nc ) );
+			dw->upCap = nc;
+		}
+	}
+	*offset = dw->upUsed;
+	dw->upUsed += need;
 	return 0;
 }
 
-static void* s_staging = NULL;
-static int s_stagingCap = 0;
+/* send `bytes` from host memory `src` to device address `dst` without waiting */
+static int uploadTo( b2gDeviceWorld* dw, void* dst, const void* src, size_t bytes )
+{
+	if ( bytes == 0 ) return 0;
+	size_t off = 0;
+	CK2( arenaAlloc( dw, bytes, &off ) );
+	memcpy( (char*)dw->upHost + off, src, bytes );
+	dw->h2dBytes += (long long)bytes;
+	CK( cudaMemcpyAsync( dst, (char*)dw->upHost + off, bytes, cudaMemcpyHostToDevice, dw->stream ) );
+	return 0;
+}
+
+/* send `bytes` into the device side of the arena; returns the device address */
+static int uploadStaged( b2gDeviceWorld* dw, const void* src, size_t bytes, void** devPtr )
+{
+	size_t off = 0;
+	CK2( arenaAlloc( dw, bytes, &off ) );
+	memcpy( (char*)dw->upHost + off, src, bytes );
+	dw->h2dBytes += (long long)bytes;
+	CK( cudaMemcpyAsync( (char*)dw->upDev + off, (char*)dw->upHost + off, bytes, cudaMemcpyHostToDevice, dw->stream ) );
+	*devPtr = (char*)dw->upDev + off;
+	return 0;
+}
+
+/* wait for the stream; afterwards the upload arena is free again */
+static int drain( b2gDeviceWorld* dw )
+{
+	CK( cudaStreamSynchronize( dw->stream ) );
+	dw->upUsed = 0;
+	return 0;
+}
 
 extern "C" int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* inits, int count )
 {
 	if ( count == 0 ) return 0;
-	CK2( stage( dw, &s_staging, &s_stagingCap, inits, (size_t)count * sizeof( b2gContactInit ) ) );
-	k_initContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const b2gContactInit*)s_staging, count );
+	void* d = NULL;
+	CK2( uploadStaged( dw, inits, (size_t)count * sizeof( b2gContactInit ), &d ) );
+	k_initContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const b2gContactInit*)d, count );
 	dw->launches += 1;
-	CK( cudaGetLastError() );
-	CK( cudaStreamSynchronize( dw->stream ) );
-	return 0;
+	return (int)cudaGetLastError();
 }
 
 extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int count )
 {
 	if ( count == 0 ) return 0;
-	CK2( stage( dw, &s_staging, &s_stagingCap, ids, (size_t)count * sizeof( int ) ) );
-	k_killContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const int*)s_staging, count );
+	void* d = NULL;
+	CK2( uploadStaged( dw, ids, (size_t)count * sizeof( int ), &d ) );
+	k_killContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const int*)d, count );
 	dw->launches += 1;
-	CK( cudaGetLastError() );
-	CK( cudaStreamSynchronize( dw->stream ) );
-	return 0;
+	return (int)cudaGetLastError();
 }
 
 extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const int* offsets, int total )
 {
+	dw->topologyDirty = 1;
 	CK2( grow( (void**)&dw->colorIds, &dw->colorIdsCap, total > 0 ? total : 1, sizeof( int ) ) );
-	if ( total > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)total * sizeof( int ) ), cudaMemcpy( dw->colorIds, ids, (size_t)total * sizeof( int ), cudaMemcpyHostToDevice ) ) );
+	CK2( uploadTo( dw, dw->colorIds, ids, (size_t)total * sizeof( int ) ) );
 	memcpy( dw->colorOffsets, offsets, sizeof( dw->colorOffsets ) );
 	return 0;
 }
@@ -811,8 +947,9 @@ extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int
 
 extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* offsets )
 {
+	dw->topologyDirty = 1;
 	CK2( grow( (void**)&dw->joints, &dw->jointCap, count > 0 ? count : 1, sizeof( b2gJoint ) ) );
-	if ( count > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)count * sizeof( b2gJoint ) ), cudaMemcpy( dw->joints, joints, (size_t)count * sizeof( b2gJoint ), cudaMemcpyHostToDevice ) ) );
+	CK2( uploadTo( dw, dw->joints, joints, (size_t)count * sizeof( b2gJoint ) ) );
 	memcpy( dw->jointOffsets, offsets, sizeof( dw->jointOffsets ) );
 	dw->jointCount = count;
 	return 0;
@@ -834,36 +971,94 @@ extern "C" int b2gDev_DownloadJoints( b2gDeviceWorld* dw, b2gJoint* byId, int id
 	return (int)e;
 }
 
-extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gTreeNode* nodes, int nodeCount, int root )
+__global__ void k_convertTree( const b2gHostTreeNode* __restrict__ raw, b2gTreeNode* __restrict__ out, int n )
 {
-	CK2( grow( (void**)&dw->tree[type], &dw->treeCap[type], nodeCount > 0 ? nodeCount : 1, sizeof( b2gTreeNode ) ) );
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	b2gHostTreeNode h = raw[i];
+	b2gTreeNode d;
+	d.aabb = h.aabb;
+	d.isLeaf = ( h.flags & 0x4 ) ? 1 : 0;
+	d.categoryNonZero = h.categoryBits != 0;
+	d.child1 = d.isLeaf ? (int)h.userData : h.child1;
+	d.child2 = d.isLeaf ? -1 : h.child2;
+	out[i] = d;
+}
+
+extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gHostTreeNode* nodes, int nodeCount, int root )
+{
+	int need = nodeCount > 0 ? nodeCount : 1;
+	CK2( grow( (void**)&dw->tree[type], &dw->treeCap[type], need, sizeof( b2gTreeNode ) ) );
+	CK2( grow( (void**)&dw->treeRaw[type], &dw->treeRawCap[type], need, sizeof( b2gHostTreeNode ) ) );
 	if ( nodeCount > 0 )
-		CK( ( dw->h2dBytes += (long long)( (size_t)nodeCount * sizeof( b2gTreeNode ) ), cudaMemcpyAsync( dw->tree[type], nodes, (size_t)nodeCount * sizeof( b2gTreeNode ), cudaMemcpyHostToDevice,
-							 dw->stream ) ) );
-	CK( cudaStreamSynchronize( dw->stream ) );
+	{
+		dw->h2dBytes += (long long)( (size_t)nodeCount * sizeof( b2gHostTreeNode ) );
+		CK( cudaMemcpyAsync( dw->treeRaw[type], nodes, (size_t)nodeCount * sizeof( b2gHostTreeNode ), cudaMemcpyHostToDevice,
+							 dw->stream ) );
+		k_convertTree<<<blocks( nodeCount ), B2G_THREADS, 0, dw->stream>>>( dw->treeRaw[type], dw->tree[type], nodeCount );
+		dw->launches += 1;
+		CK( cudaGetLastError() );
+	}
 	int mc = dw->movedCap[type];
-	CK2( grow( (void**)&dw->moved[type], &mc, nodeCount > 0 ? nodeCount : 1, 1 ) );
+	CK2( grow( (void**)&dw->moved[type], &mc, need, 1 ) );
 	dw->movedCap[type] = mc;
 	dw->treeRoot[type] = root;
 	return 0;
+}
+
+extern "C" void* b2gDev_HostAlloc( size_t bytes )
+{
+	void* p = NULL;
+	if ( cudaMallocHost( &p, bytes ) != cudaSuccess ) return NULL;
+	return p;
+}
+
+extern "C" void b2gDev_HostFree( void* p )
+{
+	if ( p != NULL ) cudaFreeHost( p );
+}
+
+/* per move: claim a contiguous run of the packed pair buffer */
+__global__ void k_packPairs( const int* __restrict__ pairs, const int* __restrict__ counts, int n, int capPerMove,
+							 int* __restrict__ packed, int* __restrict__ offsets, b2gStepCounters* counters )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	int c = counts[i];
+	if ( c > capPerMove ) c = capPerMove;
+	int o = atomicAdd( &counters->pairCount, c );
+	offsets[i] = o;
+	for ( int k = 0; k < c; ++k )
+	{
+		packed[2 * ( o + k )] = pairs[2 * ( (size_t)i * capPerMove + k )];
+		packed[2 * ( o + k ) + 1] = pairs[2 * ( (size_t)i * capPerMove + k ) + 1];
+	}
 }
 
 extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int n,
 								  int** outPairs, int** outCounts, int* outTotal )
 {
 	CK( cudaEventRecord( dw->ev[0], dw->stream ) );
-	int cap = dw->moveCap;
-	CK2( grow( (void**)&dw->moveKeys, &cap, n, sizeof( int ) ) );
-	cap = dw->moveCap;
-	CK2( grow( (void**)&dw->moveBoxes, &cap, n, sizeof( float4 ) ) );
-	cap = dw->moveCap;
-	CK2( grow( (void**)&dw->moveShapes, &cap, n, sizeof( int ) ) );
-	cap = dw->moveCap;
-	CK2( grow( (void**)&dw->pairCounts, &cap, n, sizeof( int ) ) );
-	dw->moveCap = cap;
-	CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( int ) ), cudaMemcpyAsync( dw->moveKeys, keys, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) ) );
-	CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( float4 ) ), cudaMemcpyAsync( dw->moveBoxes, boxes, (size_t)n * sizeof( float4 ), cudaMemcpyHostToDevice, dw->stream ) ) );
-	CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( int ) ), cudaMemcpyAsync( dw->moveShapes, shapes, (size_t)n * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) ) );
+	/* one staged copy of the moved proxies (pinned host memory) */
+	int stageBytes = n * 24;
+	CK2( growHost( &dw->hMoveStage, &dw->hMoveStageCap, stageBytes, 1 ) );
+	CK2( grow( &dw->moveStage, &dw->moveStageCap, stageBytes, 1 ) );
+	{
+		float* sb = (float*)dw->hMoveStage;
+		memcpy( sb, boxes, (size_t)n * 16 );
+		memcpy( sb + 4 * (size_t)n, keys, (size_t)n * 4 );
+		memcpy( sb + 5 * (size_t)n, shapes, (size_t)n * 4 );
+	}
+	dw->h2dBytes += stageBytes;
+	CK( cudaMemcpyAsync( dw->moveStage, dw->hMoveStage, (size_t)stageBytes, cudaMemcpyHostToDevice, dw->stream ) );
+	dw->moveBoxes = (float4*)dw->moveStage;
+	dw->moveKeys = (int*)( dw->moveBoxes + n );
+	dw->moveShapes = dw->moveKeys + n;
+	CK2( grow( (void**)&dw->pairCounts, &dw->moveCap, n, sizeof( int ) ) );
+	CK2( grow( (void**)&dw->pairOffsets, &dw->pairOffsetsCap, n, sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, n, sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hPairOffsets, &dw->hPairOffsetsCap, n, sizeof( int ) ) );
+	if ( dw->pairWindow < 4096 ) dw->pairWindow = 4096;
 	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
 															   dw->moved[b2_staticBody], dw->moveKeys, n, 1 );
 	dw->launches += 1;
@@ -871,15 +1066,26 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 	for ( int attempt = 0; attempt < 8; ++attempt )
 	{
 		CK2( grow( (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
+		CK2( grow( (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
+		int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
+		CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * window, sizeof( int ) ) );
 		CK( cudaMemsetAsync( dw->counters, 0, sizeof( b2gStepCounters ), dw->stream ) );
 		k_findPairs<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>(
 			dw->tree[b2_staticBody], dw->treeRoot[b2_staticBody], dw->tree[b2_kinematicBody], dw->treeRoot[b2_kinematicBody],
 			dw->tree[b2_dynamicBody], dw->treeRoot[b2_dynamicBody], dw->moved[b2_dynamicBody], dw->moveKeys, dw->moveBoxes,
 			dw->moveShapes, n, dw->pairBuf, dw->pairCounts, dw->pairPerMove, dw->counters );
-		dw->launches += 1;
+		k_packPairs<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->pairBuf, dw->pairCounts, n, dw->pairPerMove,
+																  dw->pairPacked, dw->pairOffsets, dw->counters );
+		dw->launches += 2;
 		CK( cudaGetLastError() );
-		CK( ( dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) ), cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) ) );
-		CK( cudaStreamSynchronize( dw->stream ) );
+		/* counters, per-move counts and offsets, and the first `window` pairs in one wait */
+		dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) + (size_t)n * 8 + (size_t)window * 8 );
+		CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hPairOffsets, dw->pairOffsets, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hPairPacked, dw->pairPacked, (size_t)window * 2 * sizeof( int ), cudaMemcpyDeviceToHost,
+							 dw->stream ) );
+		CK2( drain( dw ) );
 		if ( dw->hCounters->status != 0 ) return (int)cudaErrorIllegalState;
 		if ( dw->hCounters->pairOverflow <= dw->pairPerMove ) break;
 		while ( dw->pairPerMove < dw->hCounters->pairOverflow ) dw->pairPerMove *= 2;
@@ -888,32 +1094,28 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 															   dw->moved[b2_staticBody], dw->moveKeys, n, 0 );
 	dw->launches += 1;
 	CK( cudaGetLastError() );
-	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, n, sizeof( int ) ) );
-	CK( ( dw->d2hBytes += (long long)( (size_t)n * sizeof( int ) ), cudaMemcpyAsync( dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) ) );
-	int* raw = NULL;
-	int rawCap = 0;
-	CK2( growHost( (void**)&raw, &rawCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
-	CK( ( dw->d2hBytes += (long long)( (size_t)2 * n * dw->pairPerMove * sizeof( int ) ), cudaMemcpyAsync( raw, dw->pairBuf, (size_t)2 * n * dw->pairPerMove * sizeof( int ), cudaMemcpyDeviceToHost,
-						 dw->stream ) ) );
-	CK( cudaStreamSynchronize( dw->stream ) );
-	int total = 0;
-	for ( int i = 0; i < n; ++i ) total += dw->hPairCounts[i];
+	int total = dw->hCounters->pairCount;
+	int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
+	if ( total > window )
+	{
+		CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * total, sizeof( int ) ) );
+		dw->d2hBytes += (long long)( total - window ) * 8;
+		CK( cudaMemcpyAsync( dw->hPairPacked + 2 * window, dw->pairPacked + 2 * window, (size_t)( total - window ) * 2 * sizeof( int ),
+							 cudaMemcpyDeviceToHost, dw->stream ) );
+		CK2( drain( dw ) );
+	}
+	if ( 2 * total > dw->pairWindow ) dw->pairWindow = 2 * total;
+	/* pairs in move order for the host */
 	CK2( growHost( (void**)&dw->hPairs, &dw->hPairsCap, 2 * ( total > 0 ? total : 1 ), sizeof( int ) ) );
 	int o = 0;
 	for ( int i = 0; i < n; ++i )
 	{
 		int c = dw->hPairCounts[i];
-		memcpy( dw->hPairs + 2 * o, raw + 2 * (size_t)i * dw->pairPerMove, (size_t)c * 2 * sizeof( int ) );
+		memcpy( dw->hPairs + 2 * o, dw->hPairPacked + 2 * (size_t)dw->hPairOffsets[i], (size_t)c * 2 * sizeof( int ) );
 		o += c;
 	}
-	cudaFreeHost( raw );
 	CK( cudaEventRecord( dw->ev[1], dw->stream ) );
-	CK( cudaEventSynchronize( dw->ev[1] ) );
-	{
-		float ms = 0.0f;
-		cudaEventElapsedTime( &ms, dw->ev[0], dw->ev[1] );
-		dw->pairsMs += ms;
-	}
+	dw->pairsTimingPending = 1;
 	*outPairs = dw->hPairs;
 	*outCounts = dw->hPairCounts;
 	*outTotal = total;
@@ -958,22 +1160,39 @@ extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int c
 		CK( cudaGetLastError() );
 		CK( cudaEventRecord( dw->ev[3], dw->stream ) );
 	}
-	CK( ( dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) ), cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) ) );
-	CK( cudaStreamSynchronize( dw->stream ) );
+	/* the counters and the first `window` state changes come back in one wait */
+	if ( dw->changeWindow < 1024 ) dw->changeWindow = 1024;
+	int window = dw->changeWindow < contactIdCapacity ? dw->changeWindow : contactIdCapacity;
+	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( window > 0 ? window : 1 ), sizeof( int ) ) );
+	dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) + (size_t)window * 8 );
+	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+	if ( window > 0 )
+		CK( cudaMemcpyAsync( dw->hChanges, dw->changes, (size_t)window * 2 * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK2( drain( dw ) );
 	if ( contactIdCapacity > 0 )
 	{
 		float ms = 0.0f;
 		cudaEventElapsedTime( &ms, dw->ev[9], dw->ev[3] );
 		dw->collideMs += ms;
 	}
-	int n = dw->hCounters->stateChangeCount;
-	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( n > 0 ? n : 1 ), sizeof( int ) ) );
-	if ( n > 0 )
+	if ( dw->pairsTimingPending )
 	{
-		CK( ( dw->d2hBytes += (long long)( (size_t)2 * n * sizeof( int ) ), cudaMemcpyAsync( dw->hChanges, dw->changes, (size_t)2 * n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) ) );
-		CK( cudaStreamSynchronize( dw->stream ) );
-		qsort( dw->hChanges, (size_t)n, 2 * sizeof( int ), cmpChange );
+		float ms = 0.0f;
+		cudaEventElapsedTime( &ms, dw->ev[0], dw->ev[1] );
+		dw->pairsMs += ms;
+		dw->pairsTimingPending = 0;
 	}
+	int n = dw->hCounters->stateChangeCount;
+	if ( n > window )
+	{
+		CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * n, sizeof( int ) ) );
+		dw->d2hBytes += (long long)( n - window ) * 8;
+		CK( cudaMemcpyAsync( dw->hChanges + 2 * window, dw->changes + 2 * window, (size_t)( n - window ) * 2 * sizeof( int ),
+							 cudaMemcpyDeviceToHost, dw->stream ) );
+		CK2( drain( dw ) );
+	}
+	if ( 2 * n > dw->changeWindow ) dw->changeWindow = 2 * n;
+	if ( n > 1 ) qsort( dw->hChanges, (size_t)n, 2 * sizeof( int ), cmpChange );
 	*outChanges = dw->hChanges;
 	*outChangeCount = n;
 	*outRecycled = dw->hCounters->recycledContactCount;
@@ -1057,24 +1276,52 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	d_jointBodies jb0 = { dw->xf, dw->center, dw->localCenter, dw->invMass, dw->invI, dw->awakeIndex };
 	CK( cudaEventRecord( dw->ev[6], dw->stream ) );
 	bool solved = false;
-	if ( dw->solverMode == B2G_SOLVER_COMPONENTS && dw->compSkip > 0 ) dw->compSkip -= 1;
+	if ( dw->solverMode == B2G_SOLVER_COMPONENTS && dw->compSkip > 0 )
+	{
+		dw->compSkip -= 1;
+		dw->compValid = 0;
+	}
 	else if ( dw->solverMode == B2G_SOLVER_COMPONENTS && awakeCount < ( 1 << B2G_CURSOR_BODY_BITS ) &&
 			  total < ( 1 << B2G_CURSOR_CONTACT_BITS ) && jointTotal < ( 1 << B2G_CURSOR_JOINT_BITS ) )
 	{
-		int forceBig = ovJointCount0 + ovCount0 > 0;
-		CK2( b2gDev_CompAnalyze( &dw->comp, &a, dw->jointOffsets, dw->awakeIndex, total, jointTotal, forceBig, dw->stream,
-								 &dw->launches ) );
+		/* the components only change with the constraint graph: reuse the last analysis while
+		   no color, joint or awake-set upload happened */
+		bool reuse = dw->compValid && dw->topologyDirty == 0 && dw->comp.n == awakeCount && dw->comp.total == total &&
+					 dw->comp.jointTotal == jointTotal;
+		if ( reuse == false )
+		{
+			int forceBig = ovJointCount0 + ovCount0 > 0;
+			CK2( b2gDev_CompAnalyze( &dw->comp, &a, dw->jointOffsets, dw->awakeIndex, total, jointTotal, forceBig, dw->stream,
+									 &dw->launches ) );
+			dw->topologyDirty = 0;
+			dw->compValid = 0;
+		}
 		const b2gCompSummary* hs = dw->comp.hSummary;
 		if ( hs->smallComponents > 0 )
 		{
+			dw->compValid = 1;
 			CK2( b2gDev_CompSolveBins( &dw->comp, &a, dw->jointOffsets, &jb0, dw->counters, dw->stream, &dw->launches ) );
 			if ( hs->bigComponents > 0 )
-				CK2( b2gDev_CompSolveBig( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, total, jointTotal,
-										  dw->stream, &dw->launches ) );
+			{
+				int rc = b2gDev_ClusterSolve( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, 1,
+											  hs->bigBodies, dw->stream, &dw->launches );
+				if ( rc > 0 ) return rc;
+				if ( rc < 0 )
+					CK2( b2gDev_CompSolveBig( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, total,
+											  jointTotal, dw->stream, &dw->launches ) );
+			}
 			solved = true;
 		}
 		/* mostly one big component: skip the analysis for a while */
 		if ( 10ll * hs->bigBodies > 9ll * awakeCount || hs->smallComponents == 0 ) dw->compSkip = 15;
+	}
+	/* one big constraint graph: the cluster solver when it fits */
+	if ( solved == false && dw->solverMode == B2G_SOLVER_COMPONENTS && ovJointCount0 + ovCount0 == 0 )
+	{
+		int rc = b2gDev_ClusterSolve( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, 0, awakeCount,
+									  dw->stream, &dw->launches );
+		if ( rc > 0 ) return rc;
+		solved = rc == 0;
 	}
 	if ( solved )
 	{
@@ -1188,8 +1435,21 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 		CK( cudaGetLastError() );
 		CK( cudaEventRecord( dw->ev[8], dw->stream ) );
 	}
-	CK( ( dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) ), cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) ) );
-	CK( cudaStreamSynchronize( dw->stream ) );
+	/* the counters and the first `window` enlarged-proxy records come back in one wait */
+	if ( dw->recWindow < 1024 ) dw->recWindow = 1024;
+	int recWindow = dw->recWindow < shapeTotal ? dw->recWindow : shapeTotal;
+	CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( float ) ) );
+	dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) + (size_t)recWindow * 32 );
+	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+	if ( recWindow > 0 )
+	{
+		CK( cudaMemcpyAsync( dw->hRecsRaw, dw->enlargedRecs, (size_t)recWindow * 4 * sizeof( int ), cudaMemcpyDeviceToHost,
+							 dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hBoxesRaw, dw->enlargedBoxes, (size_t)recWindow * sizeof( float4 ), cudaMemcpyDeviceToHost,
+							 dw->stream ) );
+	}
+	CK2( drain( dw ) );
 	{
 		float ms = 0.0f;
 		cudaEventElapsedTime( &ms, dw->ev[6], dw->ev[7] );
@@ -1212,13 +1472,24 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	if ( n > shapeTotal ) n = shapeTotal;
 	CK2( growHost( (void**)&dw->hRecs, &dw->hRecsCap, 4 * ( n > 0 ? n : 1 ), sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hBoxes, &dw->hBoxesCap, 4 * ( n > 0 ? n : 1 ), sizeof( float ) ) );
+	if ( n > recWindow )
+	{
+		CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * n, sizeof( int ) ) );
+		CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * n, sizeof( float ) ) );
+		dw->d2hBytes += (long long)( n - recWindow ) * 32;
+		CK( cudaMemcpyAsync( dw->hRecsRaw + 4 * recWindow, dw->enlargedRecs + 4 * recWindow, (size_t)( n - recWindow ) * 4 * sizeof( int ),
+							 cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hBoxesRaw + 4 * recWindow, dw->enlargedBoxes + recWindow, (size_t)( n - recWindow ) * sizeof( float4 ),
+							 cudaMemcpyDeviceToHost, dw->stream ) );
+		CK2( drain( dw ) );
+	}
+	if ( 2 * n > dw->recWindow ) dw->recWindow = 2 * n;
 	if ( n > 0 )
 	{
-		int* recs = (int*)malloc( (size_t)n * 4 * sizeof( int ) );
-		float* boxes = (float*)malloc( (size_t)n * 4 * sizeof( float ) );
-		CK( ( dw->d2hBytes += (long long)( (size_t)n * 4 * sizeof( int ) ), cudaMemcpy( recs, dw->enlargedRecs, (size_t)n * 4 * sizeof( int ), cudaMemcpyDeviceToHost ) ) );
-		CK( ( dw->d2hBytes += (long long)( (size_t)n * sizeof( float4 ) ), cudaMemcpy( boxes, dw->enlargedBoxes, (size_t)n * sizeof( float4 ), cudaMemcpyDeviceToHost ) ) );
-		recKey* keys = (recKey*)malloc( (size_t)n * sizeof( recKey ) );
+		const int* recs = dw->hRecsRaw;
+		const float* boxes = dw->hBoxesRaw;
+		CK2( growHost( (void**)&dw->hSortKeys, &dw->hSortKeysCap, n, sizeof( recKey ) ) );
+		recKey* keys = (recKey*)dw->hSortKeys;
 		for ( int i = 0; i < n; ++i )
 		{
 			keys[i].simIndex = recs[4 * i];
@@ -1230,9 +1501,6 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 			memcpy( dw->hRecs + 4 * i, recs + 4 * keys[i].order, 4 * sizeof( int ) );
 			memcpy( dw->hBoxes + 4 * i, boxes + 4 * keys[i].order, 4 * sizeof( float ) );
 		}
-		free( keys );
-		free( recs );
-		free( boxes );
 	}
 	CK( cudaEventRecord( dw->ev[5], dw->stream ) );
 	*outRecs = dw->hRecs;

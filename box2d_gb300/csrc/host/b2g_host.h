@@ -318,10 +318,16 @@ typedef struct h_tree
 {
 	h_treeNode* nodes;
 	int root, nodeCount, nodeCapacity, freeList, proxyCount;
+	int version; /* bumped by every change of the node array */
+	int pinned;	 /* nodes live in page-locked memory */
 	int* leafIndices;
 	b2Vec2* leafCenters;
 	int rebuildCapacity;
 } h_tree;
+
+/* node array storage, provided by the library (page-locked above a size threshold) */
+void* h_nodeAlloc( size_t bytes, int* pinned );
+void h_nodeFree( void* p, int pinned );
 
 h_tree h_treeCreate( int proxyCapacity );
 void h_treeDestroy( h_tree* t );

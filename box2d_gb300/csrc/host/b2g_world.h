@@ -138,11 +138,15 @@ typedef struct h_world
 	b2gDeviceWorld* dev;
 	int devReady;			/* device arrays hold the current world */
 	int hostStateValid;		/* host body transforms/velocities match the device */
+	int jointsHostValid;	/* host joint records (impulses) match the device */
 	int moveEventsValid;	/* move event array matches the last step */
-	int colorsDirty, jointsDirty, treesDirty;
+	int colorsDirty, jointsDirty;
+	int uploadedTreeVersion[3];		 /* tree version last sent to the device */
+	const void* uploadedTreeNodes[3]; /* node array it was sent from */
 	H_ARRAY( b2gContactInit ) pendingInits;
 	h_intArray pendingKills;
 	int lastStatus;
+	void* rebuildWorker; /* host thread for the tree rebuild (step.c) */
 } h_world;
 
 h_world* h_worldFromId( b2WorldId id );
@@ -157,6 +161,7 @@ void h_computeShapeExtent( const h_shape* shape, b2Vec2 localCenter, float* minE
 
 /* world.c internals used by step.c and joint.c */
 void h_syncFromDevice( h_world* w );
+void h_syncJointsFromDevice( h_world* w );
 void h_ensureDevice( h_world* w );
 void h_createContact( h_world* w, h_shape* a, h_shape* b );
 void h_destroyContact( h_world* w, h_contact* c );
@@ -168,6 +173,8 @@ int h_canCollide( b2ShapeType a, b2ShapeType b );
 int h_isPrimary( b2ShapeType a, b2ShapeType b );
 void h_bufferMove( h_world* w, int proxyKey );
 void h_fail( h_world* w, const char* what, int code );
+void h_joinRebuild( h_world* w );
+void h_stopRebuildWorker( h_world* w );
 
 #define H_PROXY_TYPE( K ) ( (b2BodyType)( ( K ) & 3 ) )
 #define H_PROXY_ID( K ) ( ( K ) >> 2 )

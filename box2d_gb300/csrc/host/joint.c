@@ -120,6 +120,7 @@ static void h_destroyContactsBetweenBodies( h_world* w, h_body* bodyA, h_body* b
 static b2gJoint* h_createJoint( h_world* w, const b2JointDef* def, b2JointType type, b2JointId* outId )
 {
 	h_syncFromDevice( w );
+	h_syncJointsFromDevice( w );
 	h_body* bodyA = w->bodies.data + def->bodyIdA.index1 - 1;
 	h_body* bodyB = w->bodies.data + def->bodyIdB.index1 - 1;
 	if ( def->collideConnected == false ) h_destroyContactsBetweenBodies( w, bodyA, bodyB );

@@ -11,6 +11,8 @@
  */
 #include "b2g_world.h"
 
+#include <pthread.h>
+#include <stddef.h>
 #include <stdio.h>
 
 static float h_ms( uint64_t t0 ) { return b2GetMilliseconds( t0 ); }
@@ -23,33 +25,119 @@ static void h_lap( h_world* w, int phase, uint64_t* t )
 	*t = now;
 }
 
-/* upload one broadphase tree as device query nodes */
+/* The partial tree rebuild after the pair query (b2UpdateTreesTask, broad_phase.c:401-410)
+   touches only the trees, which nothing else uses until the proxies are enlarged at the
+   end of the solve. The reference runs it as a task beside the narrowphase; here a
+   per-world host thread runs it while the device does the narrowphase and the solver. */
+typedef struct h_rebuildWorker
+{
+	pthread_t thread;
+	pthread_mutex_t mu;
+	pthread_cond_t cv;
+	int pending, busy, quit;
+	h_world* w;
+} h_rebuildWorker;
+
+static void h_rebuildTrees( h_world* w )
+{
+	h_treeRebuild( w->trees + b2_dynamicBody, 0 );
+	h_treeRebuild( w->trees + b2_kinematicBody, 0 );
+}
+
+static void* h_rebuildMain( void* arg )
+{
+	h_rebuildWorker* k = arg;
+	pthread_mutex_lock( &k->mu );
+	for ( ;; )
+	{
+		while ( k->pending == 0 && k->quit == 0 ) pthread_cond_wait( &k->cv, &k->mu );
+		if ( k->quit ) break;
+		k->pending = 0;
+		pthread_mutex_unlock( &k->mu );
+		h_rebuildTrees( k->w );
+		pthread_mutex_lock( &k->mu );
+		k->busy = 0;
+		pthread_cond_broadcast( &k->cv );
+	}
+	pthread_mutex_unlock( &k->mu );
+	return NULL;
+}
+
+/* run the rebuild on the world's worker thread (started on first use); small trees are
+   rebuilt inline */
+static void h_postRebuild( h_world* w )
+{
+	if ( w->trees[b2_dynamicBody].proxyCount < 2048 )
+	{
+		h_rebuildTrees( w );
+		return;
+	}
+	h_rebuildWorker* k = w->rebuildWorker;
+	if ( k == NULL )
+	{
+		k = calloc( 1, sizeof( h_rebuildWorker ) );
+		k->w = w;
+		pthread_mutex_init( &k->mu, NULL );
+		pthread_cond_init( &k->cv, NULL );
+		if ( pthread_create( &k->thread, NULL, h_rebuildMain, k ) != 0 )
+		{
+			pthread_mutex_destroy( &k->mu );
+			pthread_cond_destroy( &k->cv );
+			free( k );
+			h_rebuildTrees( w );
+			return;
+		}
+		w->rebuildWorker = k;
+	}
+	pthread_mutex_lock( &k->mu );
+	k->pending = 1;
+	k->busy = 1;
+	pthread_cond_broadcast( &k->cv );
+	pthread_mutex_unlock( &k->mu );
+}
+
+/* wait for a posted rebuild; the trees are the main thread's again afterwards */
+void h_joinRebuild( h_world* w )
+{
+	h_rebuildWorker* k = w->rebuildWorker;
+	if ( k == NULL ) return;
+	pthread_mutex_lock( &k->mu );
+	while ( k->busy ) pthread_cond_wait( &k->cv, &k->mu );
+	pthread_mutex_unlock( &k->mu );
+}
+
+void h_stopRebuildWorker( h_world* w )
+{
+	h_rebuildWorker* k = w->rebuildWorker;
+	if ( k == NULL ) return;
+	pthread_mutex_lock( &k->mu );
+	while ( k->busy ) pthread_cond_wait( &k->cv, &k->mu );
+	k->quit = 1;
+	pthread_cond_broadcast( &k->cv );
+	pthread_mutex_unlock( &k->mu );
+	pthread_join( k->thread, NULL );
+	pthread_mutex_destroy( &k->mu );
+	pthread_cond_destroy( &k->cv );
+	free( k );
+	w->rebuildWorker = NULL;
+}
+
+/* upload one broadphase tree when it changed since its last upload; the node array is
+   sent as is (page-locked for large trees) and converted to query nodes on the device */
+_Static_assert( sizeof( h_treeNode ) == sizeof( b2gHostTreeNode ), "host tree node layout" );
+_Static_assert( offsetof( h_treeNode, userData ) == offsetof( b2gHostTreeNode, userData ), "host tree node layout" );
+_Static_assert( offsetof( h_treeNode, flags ) == offsetof( b2gHostTreeNode, flags ), "host tree node layout" );
+_Static_assert( H_NODE_LEAF == 0x4, "leaf flag" );
+
 static void h_uploadTree( h_world* w, int type )
 {
 	h_tree* t = w->trees + type;
-	int n = t->nodeCapacity;
-	b2gTreeNode* nodes = malloc( (size_t)( n > 0 ? n : 1 ) * sizeof( b2gTreeNode ) );
-	for ( int i = 0; i < n; ++i )
-	{
-		const h_treeNode* s = t->nodes + i;
-		b2gTreeNode* d = nodes + i;
-		d->aabb = s->aabb;
-		d->isLeaf = ( s->flags & H_NODE_LEAF ) ? 1 : 0;
-		d->categoryNonZero = s->categoryBits != 0;
-		if ( d->isLeaf )
-		{
-			d->child1 = (int)s->userData;
-			d->child2 = -1;
-		}
-		else
-		{
-			d->child1 = s->child1;
-			d->child2 = s->child2;
-		}
-	}
-	int rc = b2gDev_UploadTree( w->dev, type, nodes, n, t->nodeCount == 0 ? -1 : t->root );
-	free( nodes );
+	if ( w->uploadedTreeVersion[type] == t->version && w->uploadedTreeNodes[type] == t->nodes ) return;
+	int rc = b2gDev_UploadTree( w->dev, type, (const b2gHostTreeNode*)t->nodes, t->nodeCapacity,
+								t->nodeCount == 0 ? -1 : t->root );
 	if ( rc != 0 ) h_fail( w, "tree upload", rc );
+	w->uploadedTreeVersion[type] = t->version;
+	w->uploadedTreeNodes[type] = t->nodes;
 }
 
 static int h_shouldShapesCollide( b2Filter a, b2Filter b )
@@ -67,11 +155,7 @@ static void h_updatePairs( h_world* w )
 	int moveCount = w->moveArray.count;
 	if ( moveCount == 0 ) return;
 	uint64_t lap = b2GetTicks();
-	if ( w->treesDirty )
-	{
-		for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
-		w->treesDirty = 0;
-	}
+	for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
 	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
 	float* boxes = malloc( (size_t)moveCount * 4 * sizeof( float ) );
 	int* shapeIds = malloc( (size_t)moveCount * sizeof( int ) );
@@ -115,10 +199,8 @@ static void h_updatePairs( h_world* w )
 	free( boxes );
 	free( shapeIds );
 	h_lap( w, H_PHASE_CONTACT_CREATE, &lap );
-	/* b2UpdateTreesTask (broad_phase.c:401-410) */
-	h_treeRebuild( w->trees + b2_dynamicBody, 0 );
-	h_treeRebuild( w->trees + b2_kinematicBody, 0 );
-	w->treesDirty = 1;
+	/* b2UpdateTreesTask (broad_phase.c:401-410), overlapped with the narrowphase and solver */
+	h_postRebuild( w );
 	h_lap( w, H_PHASE_TREE_REBUILD, &lap );
 	for ( int i = 0; i < w->moveArray.count; ++i )
 	{
@@ -161,6 +243,8 @@ static void h_uploadColors( h_world* w )
 static void h_uploadJoints( h_world* w )
 {
 	if ( w->jointsDirty == 0 ) return;
+	/* the host records must carry the device's accumulated impulses before the re-upload */
+	h_syncJointsFromDevice( w );
 	int offsets[B2_GRAPH_COLOR_COUNT + 1];
 	int total = 0;
 	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
@@ -267,7 +351,6 @@ static void h_enlargeProxies( h_world* w, const int* recs, const float* boxes, i
 			s->fatAABB = fat;
 			h_treeEnlargeProxy( w->trees + H_PROXY_TYPE( s->proxyKey ), H_PROXY_ID( s->proxyKey ), fat );
 			h_bufferMove( w, s->proxyKey );
-			w->treesDirty = 1;
 		}
 	}
 }
@@ -369,6 +452,8 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 							   &enlargedCount, &boxes, &status );
 			if ( rc != 0 ) h_fail( w, "solver", rc );
 			h_lap( w, H_PHASE_SOLVE, &lap );
+			h_joinRebuild( w );
+			h_lap( w, H_PHASE_TREE_REBUILD, &lap );
 			w->lastStatus = status;
 			if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
 			h_enlargeProxies( w, recs, boxes, enlargedCount );
@@ -376,7 +461,9 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 		}
 		w->profile.solve = h_ms( t0 );
 	}
+	h_joinRebuild( w );
 	w->hostStateValid = 0;
+	w->jointsHostValid = 0;
 	w->profile.step = h_ms( stepTicks );
 	w->endEventArrayIndex = 1 - w->endEventArrayIndex;
 	w->endEvents[w->endEventArrayIndex].count = 0;

@@ -14,7 +14,8 @@ h_tree h_treeCreate( int proxyCapacity )
 	memset( &t, 0, sizeof( t ) );
 	t.root = B2_NULL_INDEX;
 	t.nodeCapacity = 2 * capacity - 1;
-	t.nodes = calloc( (size_t)t.nodeCapacity, sizeof( h_treeNode ) );
+	t.nodes = h_nodeAlloc( (size_t)t.nodeCapacity * sizeof( h_treeNode ), &t.pinned );
+	memset( t.nodes, 0, (size_t)t.nodeCapacity * sizeof( h_treeNode ) );
 	for ( int i = 0; i < t.nodeCapacity - 1; ++i ) t.nodes[i].parent = i + 1;
 	t.nodes[t.nodeCapacity - 1].parent = B2_NULL_INDEX;
 	t.freeList = 0;
@@ -23,7 +24,7 @@ h_tree h_treeCreate( int proxyCapacity )
 
 void h_treeDestroy( h_tree* t )
 {
-	free( t->nodes );
+	h_nodeFree( t->nodes, t->pinned );
 	free( t->leafIndices );
 	free( t->leafCenters );
 	memset( t, 0, sizeof( *t ) );
@@ -35,7 +36,12 @@ static int h_allocNode( h_tree* t )
 	{
 		int oldCapacity = t->nodeCapacity;
 		t->nodeCapacity += oldCapacity >> 1;
-		t->nodes = realloc( t->nodes, (size_t)t->nodeCapacity * sizeof( h_treeNode ) );
+		int pinned = 0;
+		h_treeNode* grown = h_nodeAlloc( (size_t)t->nodeCapacity * sizeof( h_treeNode ), &pinned );
+		memcpy( grown, t->nodes, (size_t)oldCapacity * sizeof( h_treeNode ) );
+		h_nodeFree( t->nodes, t->pinned );
+		t->nodes = grown;
+		t->pinned = pinned;
 		memset( t->nodes + t->nodeCount, 0, (size_t)( t->nodeCapacity - t->nodeCount ) * sizeof( h_treeNode ) );
 		for ( int i = t->nodeCount; i < t->nodeCapacity - 1; ++i ) t->nodes[i].parent = i + 1;
 		t->nodes[t->nodeCapacity - 1].parent = B2_NULL_INDEX;
@@ -43,6 +49,7 @@ static int h_allocNode( h_tree* t )
 	}
 	int idx = t->freeList;
 	h_treeNode* n = t->nodes + idx;
+	t->version += 1;
 	t->freeList = n->parent;
 	memset( n, 0, sizeof( *n ) );
 	n->categoryBits = B2_DEFAULT_CATEGORY_BITS;
@@ -56,6 +63,7 @@ static int h_allocNode( h_tree* t )
 
 static void h_freeNode( h_tree* t, int id )
 {
+	t->version += 1;
 	t->nodes[id].parent = t->freeList;
 	t->nodes[id].flags = 0;
 	t->freeList = id;
@@ -444,6 +452,7 @@ void h_treeMoveProxy( h_tree* t, int proxyId, b2AABB aabb )
 void h_treeEnlargeProxy( h_tree* t, int proxyId, b2AABB aabb )
 {
 	h_treeNode* nodes = t->nodes;
+	t->version += 1;
 	nodes[proxyId].aabb = aabb;
 	int parentIndex = nodes[proxyId].parent;
 	while ( parentIndex != B2_NULL_INDEX )
@@ -617,6 +626,7 @@ int h_treeRebuild( h_tree* t, int fullBuild )
 {
 	int proxyCount = t->proxyCount;
 	if ( proxyCount == 0 ) return 0;
+	t->version += 1;
 	if ( proxyCount > t->rebuildCapacity )
 	{
 		int nc = proxyCount + proxyCount / 2;

@@ -214,9 +214,10 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 	w->enableContactSoftening = def->enableContactSoftening;
 	w->enableContinuous = def->enableContinuous;
 	w->hostStateValid = 1;
+	w->jointsHostValid = 1;
 	w->colorsDirty = 1;
 	w->jointsDirty = 1;
-	w->treesDirty = 1;
+	for ( int t = 0; t < 3; ++t ) w->uploadedTreeVersion[t] = -1;
 	b2WorldId id = { (uint16_t)( index + 1 ), w->generation };
 	return id;
 }
@@ -225,6 +226,7 @@ void b2DestroyWorld( b2WorldId worldId )
 {
 	h_world* w = h_worldFromId( worldId );
 	if ( w == NULL ) return;
+	h_stopRebuildWorker( w );
 	b2gDev_Destroy( w->dev );
 	for ( int i = 0; i < 3; ++i )
 	{
@@ -359,20 +361,16 @@ b2ContactEvents b2World_GetContactEvents( b2WorldId worldId )
 /* ---------------- device mirror ---------------- */
 
 /* Pull transforms, centers and velocities (and joint impulses) back from the device. */
+/* bring body transforms and velocities back from the device (what the getters and the
+   move events read); joint impulses come back only before host-side changes */
 void h_syncFromDevice( h_world* w )
 {
 	if ( w->hostStateValid || w->devReady == 0 ) return;
 	int nb = w->bodies.count;
 	int na = w->awakeBodyIds.count;
-	float* xf = malloc( (size_t)( nb > 0 ? nb : 1 ) * 4 * sizeof( float ) );
-	float* center = malloc( (size_t)( nb > 0 ? nb : 1 ) * 2 * sizeof( float ) );
-	uint32_t* typeFlags = malloc( (size_t)( nb > 0 ? nb : 1 ) * sizeof( uint32_t ) );
-	float* sv = malloc( (size_t)( na > 0 ? na : 1 ) * 4 * sizeof( float ) );
-	float* sd = malloc( (size_t)( na > 0 ? na : 1 ) * 4 * sizeof( float ) );
-	float* params = malloc( (size_t)( na > 0 ? na : 1 ) * 8 * sizeof( float ) );
-	float* c0 = malloc( (size_t)( na > 0 ? na : 1 ) * 4 * sizeof( float ) );
-	int rc = b2gDev_DownloadBodies( w->dev, nb, xf, center, typeFlags );
-	if ( rc == 0 ) rc = b2gDev_DownloadAwake( w->dev, na, sv, sd, params, c0 );
+	const float *xf = NULL, *center = NULL, *sv = NULL;
+	const uint32_t* typeFlags = NULL;
+	int rc = b2gDev_DownloadState( w->dev, nb, na, &xf, &center, &typeFlags, &sv );
 	if ( rc != 0 ) h_fail( w, "device download", rc );
 	for ( int i = 0; i < nb; ++i )
 	{
@@ -390,24 +388,24 @@ void h_syncFromDevice( h_world* w )
 		b->linearVelocity = h_v( sv[4 * a], sv[4 * a + 1] );
 		b->angularVelocity = sv[4 * a + 2];
 	}
-	free( xf );
-	free( center );
-	free( typeFlags );
-	free( sv );
-	free( sd );
-	free( params );
-	free( c0 );
+	w->hostStateValid = 1;
+}
+
+void h_syncJointsFromDevice( h_world* w )
+{
+	if ( w->jointsHostValid || w->devReady == 0 ) return;
 	if ( w->joints.count > 0 )
 	{
-		rc = b2gDev_DownloadJoints( w->dev, w->jointRecords.data, w->jointRecords.count );
+		int rc = b2gDev_DownloadJoints( w->dev, w->jointRecords.data, w->jointRecords.count );
 		if ( rc != 0 ) h_fail( w, "joint download", rc );
 	}
-	w->hostStateValid = 1;
+	w->jointsHostValid = 1;
 }
 
 static void h_markHostChanged( h_world* w )
 {
 	h_syncFromDevice( w );
+	h_syncJointsFromDevice( w );
 	w->devReady = 0;
 }
 
@@ -578,7 +576,7 @@ void h_ensureDevice( h_world* w )
 	free( aabbs );
 	free( fats );
 	w->jointsDirty = 1;
-	w->treesDirty = 1;
+
 	w->colorsDirty = 1;
 	w->devReady = 1;
 }
@@ -886,7 +884,7 @@ static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const vo
 		int proxyId = h_treeCreateProxy( w->trees + proxyType, s->fatAABB, s->filter.categoryBits, (uint64_t)shapeId );
 		s->proxyKey = H_PROXY_KEY( proxyId, proxyType );
 		if ( proxyType != b2_staticBody || def->invokeContactCreation || def->isSensor ) h_bufferMove( w, s->proxyKey );
-		w->treesDirty = 1;
+	
 	}
 	if ( body->headShapeId != B2_NULL_INDEX ) w->shapes.data[body->headShapeId].prevShapeId = shapeId;
 	s->prevShapeId = B2_NULL_INDEX;
@@ -1193,4 +1191,33 @@ int h_shouldBodiesCollide( h_world* w, h_body* bodyA, h_body* bodyB )
 		jointKey = j->edges[edgeIndex].nextKey;
 	}
 	return 1;
+}
+
+/* tree node storage: page-locked above 4096 nodes so the per-step upload is a plain DMA */
+void* h_nodeAlloc( size_t bytes, int* pinned )
+{
+	*pinned = 0;
+	if ( bytes >= 4096 * sizeof( h_treeNode ) )
+	{
+		void* p = b2gDev_HostAlloc( bytes );
+		if ( p != NULL )
+		{
+			*pinned = 1;
+			return p;
+		}
+	}
+	void* p = malloc( bytes );
+	if ( p == NULL )
+	{
+		fprintf( stderr, "box2d_gb300: out of host memory (%zu bytes)\n", bytes );
+		abort();
+	}
+	return p;
+}
+
+void h_nodeFree( void* p, int pinned )
+{
+	if ( p == NULL ) return;
+	if ( pinned ) b2gDev_HostFree( p );
+	else free( p );
 }

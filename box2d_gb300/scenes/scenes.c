@@ -571,6 +571,23 @@ B2S_EXPORT uint32_t b2s_world_id( int h )
 }
 
 /* 7 floats per body in creation order: p.x, p.y, q.c, q.s, v.x, v.y, w */
+/* the last step's body move events (b2World_GetBodyEvents): 4 floats per event
+   (p.x, p.y, q.c, q.s) up to capacity; returns the event count */
+B2S_EXPORT int b2s_move_events( int handle, float* out, int capacity )
+{
+	b2BodyEvents ev = b2World_GetBodyEvents( b2s_scenes[handle].worldId );
+	int n = ev.moveCount < capacity ? ev.moveCount : capacity;
+	for ( int i = 0; i < n; ++i )
+	{
+		b2Transform xf = ev.moveEvents[i].transform;
+		out[4 * i] = xf.p.x;
+		out[4 * i + 1] = xf.p.y;
+		out[4 * i + 2] = xf.q.c;
+		out[4 * i + 3] = xf.q.s;
+	}
+	return ev.moveCount;
+}
+
 B2S_EXPORT void b2s_get_state( int h, float* out )
 {
 	b2sScene* s = b2s_scenes + h;

@@ -52,6 +52,9 @@ int b2s_dynamic_count( int handle );
 uint32_t b2s_world_id( int handle );
 /* 7 floats per body in creation order: p.x, p.y, q.c, q.s, v.x, v.y, w */
 void b2s_get_state( int handle, float* out );
+/* the last step's body move events (b2World_GetBodyEvents), 4 floats per event:
+   p.x, p.y, q.c, q.s, up to capacity; returns the event count */
+int b2s_move_events( int handle, float* out, int capacity );
 /* FNV-1a 64 over the bit patterns of b2s_get_state */
 uint64_t b2s_state_hash( int handle );
 void b2s_set_velocities( int handle, const float* in );
