@@ -27,6 +27,7 @@ MANY_PYRAMIDS_REF = 5
 JOINT_GRID_REF = 6
 HELLO_WORLD = 7
 SHAPE_ZOO = 8
+JOINT_ZOO = 9
 
 NO_CONTINUOUS = 1
 

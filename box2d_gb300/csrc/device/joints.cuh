@@ -1,7 +1,8 @@
 /*
  * Device joint solvers: prepare / warm start / solve per joint, one thread per joint of a
- * graph color. Revolute follows revolute_joint.c:217-500 of the reference with the same
- * operation order. The parameter slots of b2gJoint are documented in host/joint.c.
+ * graph color, with the reference's operation order: revolute_joint.c:217-500,
+ * prismatic_joint.c:295-667, weld_joint.c:148-454 (non-block solver), wheel_joint.c:197-525,
+ * distance_joint.c:250-543. The parameter slots of b2gJoint are documented in host/joint.c.
  */
 #pragma once
 
@@ -75,19 +76,20 @@ typedef struct d_jointBodies
 	const int* awakeIndex;
 } d_jointBodies;
 
-/* revolute_joint.c:217-281 */
-static __device__ void d_prepareRevolute( b2gJoint* j, const d_jointBodies* bodies, float h, bool warmStart )
+/* the part of every b2Prepare*Joint shared by all types: masses, awake indices, joint frames
+   relative to the centers of mass, and the center delta (revolute_joint.c:217-262 and the
+   same lines of the other joint files) */
+static __device__ void d_prepareJointFrames( b2gJoint* j, const d_jointBodies* bodies )
 {
 	int idA = j->bodyIdA, idB = j->bodyIdB;
 	float4 xfA = bodies->xf[idA], xfB = bodies->xf[idB];
 	b2Rot qA = { xfA.z, xfA.w }, qB = { xfB.z, xfB.w };
 	float2 lcA = bodies->localCenter[idA], lcB = bodies->localCenter[idB];
 	float2 cA = bodies->center[idA], cB = bodies->center[idB];
-	float mA = bodies->invMass[idA], iA = bodies->invI[idA], mB = bodies->invMass[idB], iB = bodies->invI[idB];
-	j->invMassA = mA;
-	j->invMassB = mB;
-	j->invIA = iA;
-	j->invIB = iB;
+	j->invMassA = bodies->invMass[idA];
+	j->invMassB = bodies->invMass[idB];
+	j->invIA = bodies->invI[idA];
+	j->invIB = bodies->invI[idB];
 	j->indexA = bodies->awakeIndex[idA];
 	j->indexB = bodies->awakeIndex[idB];
 	j->frameA.q = d_mulRot( qA, j->localFrameA.q );
@@ -95,17 +97,18 @@ static __device__ void d_prepareRevolute( b2gJoint* j, const d_jointBodies* bodi
 	j->frameB.q = d_mulRot( qB, j->localFrameB.q );
 	j->frameB.p = d_rotate( qB, d_sub( j->localFrameB.p, d_v( lcB.x, lcB.y ) ) );
 	j->deltaCenter = d_v( cB.x - cA.x, cB.y - cA.y );
-	float k = iA + iB;
+}
+
+/* revolute_joint.c:217-281 */
+static __device__ void d_prepareRevolute( b2gJoint* j, const d_jointBodies* bodies, float h, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	float k = j->invIA + j->invIB;
 	j->s[6] = k > 0.0f ? 1.0f / k : 0.0f;
 	d_makeSoftInto( j->p[1], j->p[2], h, j->s + 7, j->s + 8, j->s + 9 );
 	if ( warmStart == false )
 	{
-		j->s[0] = 0.0f;
-		j->s[1] = 0.0f;
-		j->s[2] = 0.0f;
-		j->s[3] = 0.0f;
-		j->s[4] = 0.0f;
-		j->s[5] = 0.0f;
+		for ( int i = 0; i < 6; ++i ) j->s[i] = 0.0f;
 	}
 }
 
@@ -267,6 +270,642 @@ static __device__ void d_solveRevolute( b2gJoint* j, float4* sv, const float4* s
 	if ( B.dynamic ) sv[j->indexB] = make_float4( vB.x, vB.y, wB, B.v.w );
 }
 
+/* velocity update of one axial row: P = impulse * axis with lever arms a1, a2 */
+static __device__ __forceinline__ void d_applyAxial( b2Vec2* vA, float* wA, b2Vec2* vB, float* wB, float mA, float iA, float mB,
+													 float iB, b2Vec2 axis, float a1, float a2, float impulse )
+{
+	b2Vec2 P = d_mulSV( impulse, axis );
+	float LA = impulse * a1;
+	float LB = impulse * a2;
+	*vA = d_mulSub( *vA, mA, P );
+	*wA -= iA * LA;
+	*vB = d_mulAdd( *vB, mB, P );
+	*wB += iB * LB;
+}
+
+static __device__ __forceinline__ void d_storeVelocities( float4* sv, const b2gJoint* j, const d_stateRef& A, const d_stateRef& B,
+														  b2Vec2 vA, float wA, b2Vec2 vB, float wB )
+{
+	if ( A.dynamic ) sv[j->indexA] = make_float4( vA.x, vA.y, wA, A.v.w );
+	if ( B.dynamic ) sv[j->indexB] = make_float4( vB.x, vB.y, wB, B.v.w );
+}
+
+/* ---- prismatic (prismatic_joint.c:295-667)
+   p: hertz, dampingRatio, targetTranslation, lowerTranslation, upperTranslation,
+      maxMotorForce, motorSpeed
+   s: impulse.x, impulse.y, springImpulse, motorImpulse, lowerImpulse, upperImpulse,
+      spring softness (3) ---- */
+static __device__ void d_preparePrismatic( b2gJoint* j, const d_jointBodies* bodies, float h, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	d_makeSoftInto( j->p[0], j->p[1], h, j->s + 6, j->s + 7, j->s + 8 );
+	if ( warmStart == false )
+	{
+		for ( int i = 0; i < 6; ++i ) j->s[i] = 0.0f;
+	}
+}
+
+static __device__ void d_warmStartPrismatic( b2gJoint* j, float4* sv, const float4* sd )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 d = d_add( d_add( d_sub( d_v( B.d.x, B.d.y ), d_v( A.d.x, A.d.y ) ), j->deltaCenter ), d_sub( rB, rA ) );
+	b2Vec2 axisA = d_rotate( j->frameA.q, d_v( 1.0f, 0.0f ) );
+	axisA = d_rotate( dqA, axisA );
+	float a1 = d_cross( d_add( rA, d ), axisA );
+	float a2 = d_cross( rB, axisA );
+	float axialImpulse = j->s[2] + j->s[3] + j->s[4] - j->s[5];
+	b2Vec2 perpA = d_leftPerp( axisA );
+	float s1 = d_cross( d_add( rA, d ), perpA );
+	float s2 = d_cross( rB, perpA );
+	float perpImpulse = j->s[0];
+	float angleImpulse = j->s[1];
+	b2Vec2 P = d_add( d_mulSV( axialImpulse, axisA ), d_mulSV( perpImpulse, perpA ) );
+	float LA = axialImpulse * a1 + perpImpulse * s1 + angleImpulse;
+	float LB = axialImpulse * a2 + perpImpulse * s2 + angleImpulse;
+	if ( A.dynamic )
+	{
+		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, P );
+		sv[j->indexA] = make_float4( v.x, v.y, A.v.z - iA * LA, A.v.w );
+	}
+	if ( B.dynamic )
+	{
+		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, P );
+		sv[j->indexB] = make_float4( v.x, v.y, B.v.z + iB * LB, B.v.w );
+	}
+}
+
+static __device__ void d_solvePrismatic( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
+	float wA = A.v.z, wB = B.v.z;
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Rot qA = d_mulRot( dqA, j->frameA.q );
+	b2Rot qB = d_mulRot( dqB, j->frameB.q );
+	b2Rot relQ = d_invMulRot( qA, qB );
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 d = d_add( d_add( d_sub( d_v( B.d.x, B.d.y ), d_v( A.d.x, A.d.y ) ), j->deltaCenter ), d_sub( rB, rA ) );
+	b2Vec2 axisA = d_rotate( j->frameA.q, d_v( 1.0f, 0.0f ) );
+	axisA = d_rotate( dqA, axisA );
+	float translation = d_dot( axisA, d );
+	float a1 = d_cross( d_add( rA, d ), axisA );
+	float a2 = d_cross( rB, axisA );
+	float k = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+	float axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+	if ( j->enableSpring )
+	{
+		float C = translation - j->p[2];
+		float bias = j->s[6] * C;
+		float massScale = j->s[7];
+		float impulseScale = j->s[8];
+		float Cdot = d_dot( axisA, d_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+		float deltaImpulse = -massScale * axialMass * ( Cdot + bias ) - impulseScale * j->s[2];
+		j->s[2] += deltaImpulse;
+		d_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, deltaImpulse );
+	}
+	if ( j->enableMotor )
+	{
+		float Cdot = d_dot( axisA, d_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+		float impulse = axialMass * ( j->p[6] - Cdot );
+		float oldImpulse = j->s[3];
+		float maxImpulse = h * j->p[5];
+		j->s[3] = d_clamp( j->s[3] + impulse, -maxImpulse, maxImpulse );
+		impulse = j->s[3] - oldImpulse;
+		d_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, impulse );
+	}
+	if ( j->enableLimit )
+	{
+		float speculativeDistance = 0.25f * ( j->p[4] - j->p[3] );
+		{
+			float C = translation - j->p[3];
+			if ( C < speculativeDistance )
+			{
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( C > 0.0f ) bias = d_min( C, 1.0f ) * inv_h;
+				else if ( useBias )
+				{
+					bias = j->softBias * C;
+					massScale = j->softMass;
+					impulseScale = j->softImpulse;
+				}
+				float oldImpulse = j->s[4];
+				float Cdot = d_dot( axisA, d_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+				float deltaImpulse = -axialMass * massScale * ( Cdot + bias ) - impulseScale * oldImpulse;
+				j->s[4] = d_max( oldImpulse + deltaImpulse, 0.0f );
+				deltaImpulse = j->s[4] - oldImpulse;
+				d_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, deltaImpulse );
+			}
+			else
+			{
+				j->s[4] = 0.0f;
+			}
+		}
+		{
+			float C = j->p[4] - translation;
+			if ( C < speculativeDistance )
+			{
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( C > 0.0f ) bias = d_min( C, 1.0f ) * inv_h;
+				else if ( useBias )
+				{
+					bias = j->softBias * C;
+					massScale = j->softMass;
+					impulseScale = j->softImpulse;
+				}
+				float oldImpulse = j->s[5];
+				float Cdot = d_dot( axisA, d_sub( vA, vB ) ) + a1 * wA - a2 * wB;
+				float deltaImpulse = -axialMass * massScale * ( Cdot + bias ) - impulseScale * oldImpulse;
+				j->s[5] = d_max( oldImpulse + deltaImpulse, 0.0f );
+				deltaImpulse = j->s[5] - oldImpulse;
+				b2Vec2 P = d_mulSV( deltaImpulse, axisA );
+				float LA = deltaImpulse * a1;
+				float LB = deltaImpulse * a2;
+				vA = d_mulAdd( vA, mA, P );
+				wA += iA * LA;
+				vB = d_mulSub( vB, mB, P );
+				wB -= iB * LB;
+			}
+			else
+			{
+				j->s[5] = 0.0f;
+			}
+		}
+	}
+	{
+		b2Vec2 perpA = d_leftPerp( axisA );
+		float s1 = d_cross( d_add( d, rA ), perpA );
+		float s2 = d_cross( rB, perpA );
+		b2Vec2 Cdot;
+		Cdot.x = d_dot( perpA, d_sub( vB, vA ) ) + s2 * wB - s1 * wA;
+		Cdot.y = wB - wA;
+		b2Vec2 bias = { 0.0f, 0.0f };
+		float massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias )
+		{
+			b2Vec2 C;
+			C.x = d_dot( perpA, d );
+			C.y = d_atan2( relQ.s, relQ.c );
+			bias = d_mulSV( j->softBias, C );
+			massScale = j->softMass;
+			impulseScale = j->softImpulse;
+		}
+		float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+		float k12 = iA * s1 + iB * s2;
+		float k22 = iA + iB;
+		if ( k22 == 0.0f ) k22 = 1.0f;
+		b2Vec2 b = d_solve22( k11, k12, k12, k22, d_add( Cdot, bias ) );
+		b2Vec2 deltaImpulse;
+		deltaImpulse.x = -massScale * b.x - impulseScale * j->s[0];
+		deltaImpulse.y = -massScale * b.y - impulseScale * j->s[1];
+		j->s[0] += deltaImpulse.x;
+		j->s[1] += deltaImpulse.y;
+		b2Vec2 P = d_mulSV( deltaImpulse.x, perpA );
+		float LA = deltaImpulse.x * s1 + deltaImpulse.y;
+		float LB = deltaImpulse.x * s2 + deltaImpulse.y;
+		vA = d_mulSub( vA, mA, P );
+		wA -= iA * LA;
+		vB = d_mulAdd( vB, mB, P );
+		wB += iB * LB;
+	}
+	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+}
+
+/* ---- weld (weld_joint.c:148-454, the non-block solver)
+   p: linearHertz, linearDampingRatio, angularHertz, angularDampingRatio
+   s: linearImpulse.x, linearImpulse.y, angularImpulse, axialMass, linear softness (3),
+      angular softness (3) ---- */
+static __device__ void d_prepareWeld( b2gJoint* j, const d_jointBodies* bodies, float h, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	float ka = j->invIA + j->invIB;
+	j->s[3] = ka > 0.0f ? 1.0f / ka : 0.0f;
+	if ( j->p[0] == 0.0f )
+	{
+		j->s[4] = j->softBias;
+		j->s[5] = j->softMass;
+		j->s[6] = j->softImpulse;
+	}
+	else
+	{
+		d_makeSoftInto( j->p[0], j->p[1], h, j->s + 4, j->s + 5, j->s + 6 );
+	}
+	if ( j->p[2] == 0.0f )
+	{
+		j->s[7] = j->softBias;
+		j->s[8] = j->softMass;
+		j->s[9] = j->softImpulse;
+	}
+	else
+	{
+		d_makeSoftInto( j->p[2], j->p[3], h, j->s + 7, j->s + 8, j->s + 9 );
+	}
+	if ( warmStart == false )
+	{
+		j->s[0] = 0.0f;
+		j->s[1] = 0.0f;
+		j->s[2] = 0.0f;
+	}
+}
+
+static __device__ void d_warmStartWeld( b2gJoint* j, float4* sv, const float4* sd )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 linearImpulse = { j->s[0], j->s[1] };
+	float angularImpulse = j->s[2];
+	if ( A.dynamic )
+	{
+		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, linearImpulse );
+		float w = A.v.z - iA * ( d_cross( rA, linearImpulse ) + angularImpulse );
+		sv[j->indexA] = make_float4( v.x, v.y, w, A.v.w );
+	}
+	if ( B.dynamic )
+	{
+		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, linearImpulse );
+		float w = B.v.z + iB * ( d_cross( rB, linearImpulse ) + angularImpulse );
+		sv[j->indexB] = make_float4( v.x, v.y, w, B.v.w );
+	}
+}
+
+static __device__ void d_solveWeld( b2gJoint* j, float4* sv, const float4* sd, bool useBias )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
+	float wA = A.v.z, wB = B.v.z;
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	{
+		b2Rot qA = d_mulRot( dqA, j->frameA.q );
+		b2Rot qB = d_mulRot( dqB, j->frameB.q );
+		b2Rot relQ = d_invMulRot( qA, qB );
+		float jointAngle = d_atan2( relQ.s, relQ.c );
+		float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias || j->p[2] > 0.0f )
+		{
+			float C = jointAngle;
+			bias = j->s[7] * C;
+			massScale = j->s[8];
+			impulseScale = j->s[9];
+		}
+		float Cdot = wB - wA;
+		float impulse = -massScale * j->s[3] * ( Cdot + bias ) - impulseScale * j->s[2];
+		j->s[2] += impulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	{
+		b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+		b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+		b2Vec2 bias = { 0.0f, 0.0f };
+		float massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias || j->p[0] > 0.0f )
+		{
+			b2Vec2 dcA = { A.d.x, A.d.y }, dcB = { B.d.x, B.d.y };
+			b2Vec2 C = d_add( d_add( d_sub( dcB, dcA ), d_sub( rB, rA ) ), j->deltaCenter );
+			bias = d_mulSV( j->s[4], C );
+			massScale = j->s[5];
+			impulseScale = j->s[6];
+		}
+		b2Vec2 Cdot = d_sub( d_add( vB, d_crossSV( wB, rB ) ), d_add( vA, d_crossSV( wA, rA ) ) );
+		float k11 = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+		float k12 = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+		float k22 = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+		b2Vec2 b = d_solve22( k11, k12, k12, k22, d_add( Cdot, bias ) );
+		b2Vec2 impulse = { -massScale * b.x - impulseScale * j->s[0], -massScale * b.y - impulseScale * j->s[1] };
+		j->s[0] += impulse.x;
+		j->s[1] += impulse.y;
+		vA = d_mulSub( vA, mA, impulse );
+		wA -= iA * d_cross( rA, impulse );
+		vB = d_mulAdd( vB, mB, impulse );
+		wB += iB * d_cross( rB, impulse );
+	}
+	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+}
+
+/* ---- wheel (wheel_joint.c:197-525)
+   p: lowerTranslation, upperTranslation, maxMotorTorque, motorSpeed, hertz, dampingRatio
+   s: perpImpulse, motorImpulse, springImpulse, lowerImpulse, upperImpulse, perpMass,
+      motorMass, axialMass, spring softness (3) ---- */
+static __device__ void d_prepareWheel( b2gJoint* j, const d_jointBodies* bodies, float h, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	b2Vec2 rA = j->frameA.p, rB = j->frameB.p;
+	b2Vec2 d = d_add( j->deltaCenter, d_sub( rB, rA ) );
+	b2Vec2 axisA = d_rotate( j->frameA.q, d_v( 1.0f, 0.0f ) );
+	b2Vec2 perpA = d_leftPerp( axisA );
+	float s1 = d_cross( d_add( d, rA ), perpA );
+	float s2 = d_cross( rB, perpA );
+	float kp = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+	j->s[5] = kp > 0.0f ? 1.0f / kp : 0.0f;
+	float a1 = d_cross( d_add( d, rA ), axisA );
+	float a2 = d_cross( rB, axisA );
+	float ka = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+	j->s[7] = ka > 0.0f ? 1.0f / ka : 0.0f;
+	d_makeSoftInto( j->p[4], j->p[5], h, j->s + 8, j->s + 9, j->s + 10 );
+	float km = iA + iB;
+	j->s[6] = km > 0.0f ? 1.0f / km : 0.0f;
+	if ( warmStart == false )
+	{
+		for ( int i = 0; i < 5; ++i ) j->s[i] = 0.0f;
+	}
+}
+
+static __device__ void d_warmStartWheel( b2gJoint* j, float4* sv, const float4* sd )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 d = d_add( d_add( d_sub( d_v( B.d.x, B.d.y ), d_v( A.d.x, A.d.y ) ), j->deltaCenter ), d_sub( rB, rA ) );
+	b2Vec2 axisA = d_rotate( j->frameA.q, d_v( 1.0f, 0.0f ) );
+	axisA = d_rotate( dqA, axisA );
+	b2Vec2 perpA = d_leftPerp( axisA );
+	float a1 = d_cross( d_add( d, rA ), axisA );
+	float a2 = d_cross( rB, axisA );
+	float s1 = d_cross( d_add( d, rA ), perpA );
+	float s2 = d_cross( rB, perpA );
+	float axialImpulse = j->s[2] + j->s[3] - j->s[4];
+	b2Vec2 P = d_add( d_mulSV( axialImpulse, axisA ), d_mulSV( j->s[0], perpA ) );
+	float LA = axialImpulse * a1 + j->s[0] * s1 + j->s[1];
+	float LB = axialImpulse * a2 + j->s[0] * s2 + j->s[1];
+	if ( A.dynamic )
+	{
+		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, P );
+		sv[j->indexA] = make_float4( v.x, v.y, A.v.z - iA * LA, A.v.w );
+	}
+	if ( B.dynamic )
+	{
+		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, P );
+		sv[j->indexB] = make_float4( v.x, v.y, B.v.z + iB * LB, B.v.w );
+	}
+}
+
+static __device__ void d_solveWheel( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
+	float wA = A.v.z, wB = B.v.z;
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	bool fixedRotation = ( iA + iB == 0.0f );
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 d = d_add( d_add( d_sub( d_v( B.d.x, B.d.y ), d_v( A.d.x, A.d.y ) ), j->deltaCenter ), d_sub( rB, rA ) );
+	b2Vec2 axisA = d_rotate( j->frameA.q, d_v( 1.0f, 0.0f ) );
+	axisA = d_rotate( dqA, axisA );
+	float translation = d_dot( axisA, d );
+	float a1 = d_cross( d_add( d, rA ), axisA );
+	float a2 = d_cross( rB, axisA );
+	if ( j->enableMotor && fixedRotation == false )
+	{
+		float Cdot = wB - wA - j->p[3];
+		float impulse = -j->s[6] * Cdot;
+		float oldImpulse = j->s[1];
+		float maxImpulse = h * j->p[2];
+		j->s[1] = d_clamp( j->s[1] + impulse, -maxImpulse, maxImpulse );
+		impulse = j->s[1] - oldImpulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	if ( j->enableSpring )
+	{
+		float C = translation;
+		float bias = j->s[8] * C;
+		float massScale = j->s[9];
+		float impulseScale = j->s[10];
+		float Cdot = d_dot( axisA, d_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+		float impulse = -massScale * j->s[7] * ( Cdot + bias ) - impulseScale * j->s[2];
+		j->s[2] += impulse;
+		d_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, impulse );
+	}
+	if ( j->enableLimit )
+	{
+		{
+			float C = translation - j->p[0];
+			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+			if ( C > 0.0f ) bias = C * inv_h;
+			else if ( useBias )
+			{
+				bias = j->softBias * C;
+				massScale = j->softMass;
+				impulseScale = j->softImpulse;
+			}
+			float Cdot = d_dot( axisA, d_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+			float impulse = -massScale * j->s[7] * ( Cdot + bias ) - impulseScale * j->s[3];
+			float oldImpulse = j->s[3];
+			j->s[3] = d_max( oldImpulse + impulse, 0.0f );
+			impulse = j->s[3] - oldImpulse;
+			d_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, impulse );
+		}
+		{
+			float C = j->p[1] - translation;
+			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+			if ( C > 0.0f ) bias = C * inv_h;
+			else if ( useBias )
+			{
+				bias = j->softBias * C;
+				massScale = j->softMass;
+				impulseScale = j->softImpulse;
+			}
+			float Cdot = d_dot( axisA, d_sub( vA, vB ) ) + a1 * wA - a2 * wB;
+			float impulse = -massScale * j->s[7] * ( Cdot + bias ) - impulseScale * j->s[4];
+			float oldImpulse = j->s[4];
+			j->s[4] = d_max( oldImpulse + impulse, 0.0f );
+			impulse = j->s[4] - oldImpulse;
+			b2Vec2 P = d_mulSV( impulse, axisA );
+			float LA = impulse * a1;
+			float LB = impulse * a2;
+			vA = d_mulAdd( vA, mA, P );
+			wA += iA * LA;
+			vB = d_mulSub( vB, mB, P );
+			wB -= iB * LB;
+		}
+	}
+	{
+		b2Vec2 perpA = d_leftPerp( axisA );
+		float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias )
+		{
+			float C = d_dot( perpA, d );
+			bias = j->softBias * C;
+			massScale = j->softMass;
+			impulseScale = j->softImpulse;
+		}
+		float s1 = d_cross( d_add( d, rA ), perpA );
+		float s2 = d_cross( rB, perpA );
+		float Cdot = d_dot( perpA, d_sub( vB, vA ) ) + s2 * wB - s1 * wA;
+		float impulse = -massScale * j->s[5] * ( Cdot + bias ) - impulseScale * j->s[0];
+		j->s[0] += impulse;
+		d_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, perpA, s1, s2, impulse );
+	}
+	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+}
+
+/* ---- distance (distance_joint.c:250-543); the anchors are the frames' origins
+   p: length, hertz, dampingRatio, lowerSpringForce, upperSpringForce, minLength,
+      maxLength, maxMotorForce, motorSpeed
+   s: impulse, lowerImpulse, upperImpulse, motorImpulse, axialMass, distance softness (3) ---- */
+static __device__ void d_prepareDistance( b2gJoint* j, const d_jointBodies* bodies, float h, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	b2Vec2 rA = j->frameA.p, rB = j->frameB.p;
+	b2Vec2 separation = d_add( d_sub( rB, rA ), j->deltaCenter );
+	b2Vec2 axis = d_normalize( separation );
+	float crA = d_cross( rA, axis );
+	float crB = d_cross( rB, axis );
+	float k = mA + mB + iA * crA * crA + iB * crB * crB;
+	j->s[4] = k > 0.0f ? 1.0f / k : 0.0f;
+	d_makeSoftInto( j->p[1], j->p[2], h, j->s + 5, j->s + 6, j->s + 7 );
+	if ( warmStart == false )
+	{
+		for ( int i = 0; i < 4; ++i ) j->s[i] = 0.0f;
+	}
+}
+
+static __device__ void d_warmStartDistance( b2gJoint* j, float4* sv, const float4* sd )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 ds = d_add( d_sub( d_v( B.d.x, B.d.y ), d_v( A.d.x, A.d.y ) ), d_sub( rB, rA ) );
+	b2Vec2 separation = d_add( j->deltaCenter, ds );
+	b2Vec2 axis = d_normalize( separation );
+	float axialImpulse = j->s[0] + j->s[1] - j->s[2] + j->s[3];
+	b2Vec2 P = d_mulSV( axialImpulse, axis );
+	if ( A.dynamic )
+	{
+		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, P );
+		sv[j->indexA] = make_float4( v.x, v.y, A.v.z - iA * d_cross( rA, P ), A.v.w );
+	}
+	if ( B.dynamic )
+	{
+		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, P );
+		sv[j->indexB] = make_float4( v.x, v.y, B.v.z + iB * d_cross( rB, P ), B.v.w );
+	}
+}
+
+static __device__ __forceinline__ void d_applyLinear( b2Vec2* vA, float* wA, b2Vec2* vB, float* wB, float mA, float iA, float mB,
+													  float iB, b2Vec2 rA, b2Vec2 rB, b2Vec2 P )
+{
+	*vA = d_mulSub( *vA, mA, P );
+	*wA -= iA * d_cross( rA, P );
+	*vB = d_mulAdd( *vB, mB, P );
+	*wB += iB * d_cross( rB, P );
+}
+
+static __device__ void d_solveDistance( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
+	float wA = A.v.z, wB = B.v.z;
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 ds = d_add( d_sub( d_v( B.d.x, B.d.y ), d_v( A.d.x, A.d.y ) ), d_sub( rB, rA ) );
+	b2Vec2 separation = d_add( j->deltaCenter, ds );
+	float length = d_length( separation );
+	b2Vec2 axis = d_normalize( separation );
+	float axialMass = j->s[4];
+	if ( j->enableSpring && ( j->p[5] < j->p[6] || j->enableLimit == 0 ) )
+	{
+		if ( j->p[1] > 0.0f )
+		{
+			b2Vec2 vr = d_add( d_sub( vB, vA ), d_sub( d_crossSV( wB, rB ), d_crossSV( wA, rA ) ) );
+			float cdot = d_dot( axis, vr );
+			float c = length - j->p[0];
+			float bias = j->s[5] * c;
+			float m = j->s[6] * axialMass;
+			float oldImpulse = j->s[0];
+			float impulse = -m * ( cdot + bias ) - j->s[7] * oldImpulse;
+			j->s[0] = d_clamp( j->s[0] + impulse, j->p[3] * h, j->p[4] * h );
+			impulse = j->s[0] - oldImpulse;
+			d_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, d_mulSV( impulse, axis ) );
+		}
+		if ( j->enableMotor )
+		{
+			b2Vec2 vr = d_add( d_sub( vB, vA ), d_sub( d_crossSV( wB, rB ), d_crossSV( wA, rA ) ) );
+			float Cdot = d_dot( axis, vr );
+			float impulse = axialMass * ( j->p[8] - Cdot );
+			float oldImpulse = j->s[3];
+			float maxImpulse = h * j->p[7];
+			j->s[3] = d_clamp( j->s[3] + impulse, -maxImpulse, maxImpulse );
+			impulse = j->s[3] - oldImpulse;
+			d_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, d_mulSV( impulse, axis ) );
+		}
+		if ( j->enableLimit )
+		{
+			{
+				b2Vec2 vr = d_add( d_sub( vB, vA ), d_sub( d_crossSV( wB, rB ), d_crossSV( wA, rA ) ) );
+				float cdot = d_dot( axis, vr );
+				float c = length - j->p[5];
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( c > 0.0f ) bias = c * inv_h;
+				else if ( useBias )
+				{
+					bias = j->softBias * c;
+					massScale = j->softMass;
+					impulseScale = j->softImpulse;
+				}
+				float impulse = -massScale * axialMass * ( cdot + bias ) - impulseScale * j->s[1];
+				float newImpulse = d_max( 0.0f, j->s[1] + impulse );
+				impulse = newImpulse - j->s[1];
+				j->s[1] = newImpulse;
+				d_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, d_mulSV( impulse, axis ) );
+			}
+			{
+				b2Vec2 vr = d_add( d_sub( vA, vB ), d_sub( d_crossSV( wA, rA ), d_crossSV( wB, rB ) ) );
+				float Cdot = d_dot( axis, vr );
+				float C = j->p[6] - length;
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( C > 0.0f ) bias = C * inv_h;
+				else if ( useBias )
+				{
+					bias = j->softBias * C;
+					massScale = j->softMass;
+					impulseScale = j->softImpulse;
+				}
+				float impulse = -massScale * axialMass * ( Cdot + bias ) - impulseScale * j->s[2];
+				float newImpulse = d_max( 0.0f, j->s[2] + impulse );
+				impulse = newImpulse - j->s[2];
+				j->s[2] = newImpulse;
+				d_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, d_mulSV( -impulse, axis ) );
+			}
+		}
+	}
+	else
+	{
+		b2Vec2 vr = d_add( d_sub( vB, vA ), d_sub( d_crossSV( wB, rB ), d_crossSV( wA, rA ) ) );
+		float Cdot = d_dot( axis, vr );
+		float C = length - j->p[0];
+		float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias )
+		{
+			bias = j->softBias * C;
+			massScale = j->softMass;
+			impulseScale = j->softImpulse;
+		}
+		float impulse = -massScale * axialMass * ( Cdot + bias ) - impulseScale * j->s[0];
+		j->s[0] += impulse;
+		d_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, d_mulSV( impulse, axis ) );
+	}
+	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+}
+
 /* joint.c:1406-1540 dispatch */
 static __device__ void d_prepareJoint( b2gJoint* j, const d_jointBodies* bodies, float h, float inv_h, bool warmStart )
 {
@@ -274,7 +913,11 @@ static __device__ void d_prepareJoint( b2gJoint* j, const d_jointBodies* bodies,
 	d_makeSoftInto( hertz, j->constraintDampingRatio, h, &j->softBias, &j->softMass, &j->softImpulse );
 	switch ( j->type )
 	{
+		case b2_distanceJoint: d_prepareDistance( j, bodies, h, warmStart ); break;
+		case b2_prismaticJoint: d_preparePrismatic( j, bodies, h, warmStart ); break;
 		case b2_revoluteJoint: d_prepareRevolute( j, bodies, h, warmStart ); break;
+		case b2_weldJoint: d_prepareWeld( j, bodies, h, warmStart ); break;
+		case b2_wheelJoint: d_prepareWheel( j, bodies, h, warmStart ); break;
 		default: break;
 	}
 }
@@ -283,7 +926,11 @@ static __device__ void d_warmStartJoint( b2gJoint* j, float4* sv, const float4* 
 {
 	switch ( j->type )
 	{
+		case b2_distanceJoint: d_warmStartDistance( j, sv, sd ); break;
+		case b2_prismaticJoint: d_warmStartPrismatic( j, sv, sd ); break;
 		case b2_revoluteJoint: d_warmStartRevolute( j, sv, sd ); break;
+		case b2_weldJoint: d_warmStartWeld( j, sv, sd ); break;
+		case b2_wheelJoint: d_warmStartWheel( j, sv, sd ); break;
 		default: break;
 	}
 }
@@ -292,7 +939,11 @@ static __device__ void d_solveJoint( b2gJoint* j, float4* sv, const float4* sd, 
 {
 	switch ( j->type )
 	{
+		case b2_distanceJoint: d_solveDistance( j, sv, sd, h, inv_h, useBias ); break;
+		case b2_prismaticJoint: d_solvePrismatic( j, sv, sd, h, inv_h, useBias ); break;
 		case b2_revoluteJoint: d_solveRevolute( j, sv, sd, h, inv_h, useBias ); break;
+		case b2_weldJoint: d_solveWeld( j, sv, sd, useBias ); break;
+		case b2_wheelJoint: d_solveWheel( j, sv, sd, h, inv_h, useBias ); break;
 		default: break;
 	}
 }

@@ -22,7 +22,7 @@
  *   distance : p = length, hertz, dampingRatio, lowerSpringForce, upperSpringForce,
  *                  minLength, maxLength, maxMotorForce, motorSpeed
  *              s = impulse, lowerImpulse, upperImpulse, motorImpulse, axialMass,
- *                  distance softness (3), anchorA (2), anchorB (2)
+ *                  distance softness (3); the anchors are frameA.p and frameB.p
  */
 #include "b2g_world.h"
 

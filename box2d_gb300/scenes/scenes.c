@@ -19,6 +19,7 @@
 #include "box2d_gb300.h"
 #endif
 
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -494,6 +495,199 @@ static void b2sShapeZoo( b2sScene* s, int count, b2sRng* rng )
 	}
 }
 
+/* Joint zoo: `count` copies, 14 m apart, of five mechanisms on one static ground segment --
+   a prismatic slider (limits, and a motor or a spring), a welded chain (rigid or soft), a
+   two-wheeled cart on wheel joints (spring, limits, motor), a chain of circles on distance
+   joints (rigid, spring with limits, motor) and a revolute pendulum (limits, motor, spring)
+   -- plus a few boxes dropped onto them. */
+static b2JointDef b2sJointBase( b2BodyId a, b2BodyId b, float ax, float ay, float bx, float by )
+{
+	b2JointDef j;
+	memset( &j, 0, sizeof( j ) );
+	j.bodyIdA = a;
+	j.bodyIdB = b;
+	j.localFrameA.p.x = ax;
+	j.localFrameA.p.y = ay;
+	j.localFrameA.q.c = 1.0f;
+	j.localFrameB.p.x = bx;
+	j.localFrameB.p.y = by;
+	j.localFrameB.q.c = 1.0f;
+	j.forceThreshold = FLT_MAX;
+	j.torqueThreshold = FLT_MAX;
+	j.drawScale = 1.0f;
+	return j;
+}
+
+static void b2sJointZoo( b2sScene* s, int count, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	{
+		b2ShapeDef sd = b2DefaultShapeDef();
+		b2Segment seg = { { -10.0f, 0.0f }, { 14.0f * count + 10.0f, 0.0f } };
+		b2CreateSegmentShape( ground, &sd, &seg );
+	}
+	b2ShapeDef sd = b2DefaultShapeDef();
+	for ( int k = 0; k < count; ++k )
+	{
+		float x0 = 14.0f * k;
+		int variant = k % 2;
+		/* prismatic slider on a tilted axis */
+		{
+			b2BodyId box = b2sBody( s, b2_dynamicBody, x0, 4.0f );
+			b2Polygon p = b2MakeBox( 0.5f, 0.25f );
+			b2CreatePolygonShape( box, &sd, &p );
+			b2PrismaticJointDef jd = b2DefaultPrismaticJointDef();
+			b2JointDef base = b2sJointBase( ground, box, x0, 4.0f, 0.0f, 0.0f );
+			float angle = b2sRandomFloatRange( rng, -0.8f, 0.8f );
+			base.localFrameA.q = b2MakeRot( angle );
+			base.localFrameB.q = b2MakeRot( angle );
+			jd.base = base;
+			jd.base.constraintHertz = 60.0f;
+			jd.base.constraintDampingRatio = 2.0f;
+			jd.enableLimit = true;
+			jd.lowerTranslation = -2.0f;
+			jd.upperTranslation = 2.0f;
+			if ( variant == 0 )
+			{
+				jd.enableMotor = true;
+				jd.maxMotorForce = 50.0f;
+				jd.motorSpeed = b2sRandomFloatRange( rng, -2.0f, 2.0f );
+			}
+			else
+			{
+				jd.enableSpring = true;
+				jd.hertz = 2.0f;
+				jd.dampingRatio = 0.5f;
+				jd.targetTranslation = 0.5f;
+			}
+			b2CreatePrismaticJoint( s->worldId, &jd );
+		}
+		/* welded chain hanging from a static anchor */
+		{
+			b2BodyId prev = ground;
+			float px = x0 + 3.0f, py = 6.0f;
+			for ( int i = 0; i < 4; ++i )
+			{
+				b2BodyId link = b2sBody( s, b2_dynamicBody, px + 0.8f * i + 0.4f, py );
+				b2Polygon p = b2MakeBox( 0.4f, 0.1f );
+				b2CreatePolygonShape( link, &sd, &p );
+				b2WeldJointDef jd = b2DefaultWeldJointDef();
+				float ax = i == 0 ? px : 0.4f;
+				jd.base = b2sJointBase( prev, link, ax, i == 0 ? py : 0.0f, -0.4f, 0.0f );
+				jd.base.constraintHertz = 60.0f;
+				jd.base.constraintDampingRatio = 2.0f;
+				if ( variant == 1 )
+				{
+					jd.linearHertz = 5.0f;
+					jd.angularHertz = 3.0f;
+					jd.linearDampingRatio = 0.7f;
+					jd.angularDampingRatio = 0.5f;
+				}
+				b2CreateWeldJoint( s->worldId, &jd );
+				prev = link;
+			}
+		}
+		/* cart on two wheel joints */
+		{
+			float cx = x0 + 8.0f, cy = 1.2f;
+			b2BodyId chassis = b2sBody( s, b2_dynamicBody, cx, cy );
+			b2Polygon p = b2MakeBox( 1.0f, 0.25f );
+			b2CreatePolygonShape( chassis, &sd, &p );
+			for ( int wi = 0; wi < 2; ++wi )
+			{
+				float wx = wi == 0 ? -0.7f : 0.7f;
+				b2BodyId wheel = b2sBody( s, b2_dynamicBody, cx + wx, cy - 0.55f );
+				b2Circle c = { { 0.0f, 0.0f }, 0.3f };
+				b2CreateCircleShape( wheel, &sd, &c );
+				b2WheelJointDef jd = b2DefaultWheelJointDef();
+				jd.base = b2sJointBase( chassis, wheel, wx, -0.55f, 0.0f, 0.0f );
+				jd.base.localFrameA.q = b2MakeRot( 0.5f * B2_PI );
+				jd.base.constraintHertz = 60.0f;
+				jd.base.constraintDampingRatio = 2.0f;
+				jd.enableSpring = true;
+				jd.hertz = 4.0f;
+				jd.dampingRatio = 0.7f;
+				jd.enableLimit = true;
+				jd.lowerTranslation = -0.25f;
+				jd.upperTranslation = 0.25f;
+				jd.enableMotor = wi == 0;
+				jd.maxMotorTorque = 10.0f;
+				jd.motorSpeed = variant == 0 ? -5.0f : 3.0f;
+				b2CreateWheelJoint( s->worldId, &jd );
+			}
+		}
+		/* chain of circles on distance joints */
+		{
+			b2BodyId prev = ground;
+			float px = x0 + 11.0f, py = 8.0f;
+			for ( int i = 0; i < 5; ++i )
+			{
+				b2BodyId bead = b2sBody( s, b2_dynamicBody, px + 0.5f * ( i + 1 ), py );
+				b2Circle c = { { 0.0f, 0.0f }, 0.15f };
+				b2CreateCircleShape( bead, &sd, &c );
+				b2DistanceJointDef jd = b2DefaultDistanceJointDef();
+				jd.base = b2sJointBase( prev, bead, i == 0 ? px : 0.0f, i == 0 ? py : 0.0f, 0.0f, 0.0f );
+				jd.base.constraintHertz = 60.0f;
+				jd.base.constraintDampingRatio = 2.0f;
+				jd.length = 0.5f;
+				int mode = ( i + k ) % 3;
+				if ( mode == 1 )
+				{
+					jd.enableSpring = true;
+					jd.hertz = 3.0f;
+					jd.dampingRatio = 0.3f;
+					jd.enableLimit = true;
+					jd.minLength = 0.3f;
+					jd.maxLength = 0.8f;
+				}
+				else if ( mode == 2 )
+				{
+					jd.enableSpring = true;
+					jd.hertz = 0.0f;
+					jd.enableMotor = true;
+					jd.maxMotorForce = 5.0f;
+					jd.motorSpeed = 0.5f;
+					jd.enableLimit = true;
+					jd.minLength = 0.2f;
+					jd.maxLength = 1.0f;
+				}
+				b2CreateDistanceJoint( s->worldId, &jd );
+				prev = bead;
+			}
+		}
+		/* revolute pendulum */
+		{
+			b2BodyId arm = b2sBody( s, b2_dynamicBody, x0 + 1.0f, 10.0f );
+			b2Polygon p = b2MakeBox( 1.0f, 0.1f );
+			b2CreatePolygonShape( arm, &sd, &p );
+			b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+			jd.base = b2sJointBase( ground, arm, x0, 10.0f, -1.0f, 0.0f );
+			jd.base.constraintHertz = 60.0f;
+			jd.base.constraintDampingRatio = 2.0f;
+			jd.enableLimit = true;
+			jd.lowerAngle = -0.5f * B2_PI;
+			jd.upperAngle = 0.25f * B2_PI;
+			jd.enableMotor = variant == 0;
+			jd.maxMotorTorque = 20.0f;
+			jd.motorSpeed = 1.0f;
+			jd.enableSpring = variant == 1;
+			jd.hertz = 1.0f;
+			jd.dampingRatio = 0.2f;
+			b2CreateRevoluteJoint( s->worldId, &jd );
+		}
+		/* boxes dropped onto the mechanisms */
+		for ( int i = 0; i < 3; ++i )
+		{
+			float bx = x0 + b2sRandomFloatRange( rng, 0.0f, 12.0f );
+			float by = b2sRandomFloatRange( rng, 12.0f, 16.0f );
+			b2BodyId box = b2sBody( s, b2_dynamicBody, bx, by );
+			b2Polygon p = b2MakeSquare( 0.3f );
+			b2CreatePolygonShape( box, &sd, &p );
+		}
+	}
+}
+
 enum
 {
 	B2S_LARGE_PYRAMID = 0,
@@ -505,6 +699,7 @@ enum
 	B2S_JOINT_GRID_REF = 6,
 	B2S_HELLO_WORLD = 7,
 	B2S_SHAPE_ZOO = 8,
+	B2S_JOINT_ZOO = 9,
 };
 
 /* Create a scene. kind selects the builder; a, b, c are its size parameters; seed feeds
@@ -541,6 +736,7 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 		case B2S_JOINT_GRID_REF: b2sJointGrid( s, a, 0, 0, &rng ); break;
 		case B2S_HELLO_WORLD: b2sHelloWorld( s ); break;
 		case B2S_SHAPE_ZOO: b2sShapeZoo( s, a, &rng ); break;
+		case B2S_JOINT_ZOO: b2sJointZoo( s, a, &rng ); break;
 		default: break;
 	}
 	return h;

@@ -42,7 +42,8 @@ void* b2p_stream( uint32_t packedWorldId );
 
 /* Scene builders (box2d_gb300/scenes/scenes.c). kind: 0 large pyramid, 1 many pyramids
    with rain, 2 joint grid with mixed shapes, 3 one batched world, 4 one ramp world,
-   5 reference many_pyramids, 6 reference joint_grid, 7 hello world, 8 shape zoo.
+   5 reference many_pyramids, 6 reference joint_grid, 7 hello world, 8 shape zoo,
+   9 joint zoo (prismatic, weld, wheel, distance and revolute mechanisms).
    flags bit 0 disables continuous collision. Returns a handle or -1. */
 int b2s_create( int kind, int a, int b, int c, uint32_t seed, int flags );
 void b2s_destroy( int handle );

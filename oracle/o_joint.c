@@ -1,7 +1,8 @@
 /*
  * Oracle (test checker only): joint creation (joint.c:16-720), the per-type dispatch
- * (joint.c:1406-1540) and the joint solvers. Revolute follows revolute_joint.c:217-500;
- * prismatic, weld, wheel and distance follow their *_joint.c files.
+ * (joint.c:1406-1540) and the joint solvers: revolute_joint.c:217-500,
+ * prismatic_joint.c:295-667, weld_joint.c:148-454 (the non-block solver the reference
+ * compiles, B2_WELD_BLOCK_SOLVE 0), wheel_joint.c:197-525, distance_joint.c:250-543.
  */
 #include "o_core.h"
 
@@ -481,6 +482,719 @@ static void o_solveRevolute( o_world* w, o_stepContext* ctx, o_jointSim* base, i
 	}
 }
 
+/* ---------------- prismatic (prismatic_joint.c:295-667) ---------------- */
+static void o_preparePrismatic( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	int ia, ib;
+	o_bodySim* simA = o_jointBodySim( w, base->bodyIdA, &ia );
+	o_bodySim* simB = o_jointBodySim( w, base->bodyIdB, &ib );
+	base->invMassA = simA->invMass;
+	base->invMassB = simB->invMass;
+	base->invIA = simA->invInertia;
+	base->invIB = simB->invInertia;
+	o_prismaticJoint* j = &base->prismaticJoint;
+	j->indexA = ia;
+	j->indexB = ib;
+	j->frameA.q = o_mulRot( simA->transform.q, base->localFrameA.q );
+	j->frameA.p = o_rotate( simA->transform.q, o_sub( base->localFrameA.p, simA->localCenter ) );
+	j->frameB.q = o_mulRot( simB->transform.q, base->localFrameB.q );
+	j->frameB.p = o_rotate( simB->transform.q, o_sub( base->localFrameB.p, simB->localCenter ) );
+	j->deltaCenter = o_v( simB->center.x - simA->center.x, simB->center.y - simA->center.y );
+	j->springSoftness = o_makeSoft( j->hertz, j->dampingRatio, ctx->h );
+	if ( ctx->enableWarmStarting == 0 )
+	{
+		j->impulse = o_v( 0.0f, 0.0f );
+		j->springImpulse = 0.0f;
+		j->motorImpulse = 0.0f;
+		j->lowerImpulse = 0.0f;
+		j->upperImpulse = 0.0f;
+	}
+}
+
+static void o_warmStartPrismatic( o_world* w, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_prismaticJoint* j = &base->prismaticJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	b2Vec2 d = o_add( o_add( o_sub( sB->deltaPosition, sA->deltaPosition ), j->deltaCenter ), o_sub( rB, rA ) );
+	b2Vec2 axisA = o_rotate( j->frameA.q, o_v( 1.0f, 0.0f ) );
+	axisA = o_rotate( sA->deltaRotation, axisA );
+	float a1 = o_cross( o_add( rA, d ), axisA );
+	float a2 = o_cross( rB, axisA );
+	float axialImpulse = j->springImpulse + j->motorImpulse + j->lowerImpulse - j->upperImpulse;
+	b2Vec2 perpA = o_leftPerp( axisA );
+	float s1 = o_cross( o_add( rA, d ), perpA );
+	float s2 = o_cross( rB, perpA );
+	float perpImpulse = j->impulse.x;
+	float angleImpulse = j->impulse.y;
+	b2Vec2 P = o_add( o_mulSV( axialImpulse, axisA ), o_mulSV( perpImpulse, perpA ) );
+	float LA = axialImpulse * a1 + perpImpulse * s1 + angleImpulse;
+	float LB = axialImpulse * a2 + perpImpulse * s2 + angleImpulse;
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = o_mulSub( sA->linearVelocity, mA, P );
+		sA->angularVelocity -= iA * LA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = o_mulAdd( sB->linearVelocity, mB, P );
+		sB->angularVelocity += iB * LB;
+	}
+}
+
+/* one axial row (spring, motor or limit) applied along axisA with lever arms a1, a2 */
+static void o_applyAxial( b2Vec2* vA, float* wA, b2Vec2* vB, float* wB, float mA, float iA, float mB, float iB, b2Vec2 axisA,
+						  float a1, float a2, float impulse )
+{
+	b2Vec2 P = o_mulSV( impulse, axisA );
+	float LA = impulse * a1;
+	float LB = impulse * a2;
+	*vA = o_mulSub( *vA, mA, P );
+	*wA -= iA * LA;
+	*vB = o_mulAdd( *vB, mB, P );
+	*wB += iB * LB;
+}
+
+static void o_solvePrismatic( o_world* w, o_stepContext* ctx, o_jointSim* base, int useBias )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_prismaticJoint* j = &base->prismaticJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 vA = sA->linearVelocity, vB = sB->linearVelocity;
+	float wA = sA->angularVelocity, wB = sB->angularVelocity;
+	b2Rot qA = o_mulRot( sA->deltaRotation, j->frameA.q );
+	b2Rot qB = o_mulRot( sB->deltaRotation, j->frameB.q );
+	b2Rot relQ = o_invMulRot( qA, qB );
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	b2Vec2 d = o_add( o_add( o_sub( sB->deltaPosition, sA->deltaPosition ), j->deltaCenter ), o_sub( rB, rA ) );
+	b2Vec2 axisA = o_rotate( j->frameA.q, o_v( 1.0f, 0.0f ) );
+	axisA = o_rotate( sA->deltaRotation, axisA );
+	float translation = o_dot( axisA, d );
+	float a1 = o_cross( o_add( rA, d ), axisA );
+	float a2 = o_cross( rB, axisA );
+	float k = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+	float axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+	o_softness softness = base->constraintSoftness;
+	if ( j->enableSpring )
+	{
+		float C = translation - j->targetTranslation;
+		float bias = j->springSoftness.biasRate * C;
+		float massScale = j->springSoftness.massScale;
+		float impulseScale = j->springSoftness.impulseScale;
+		float Cdot = o_dot( axisA, o_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+		float deltaImpulse = -massScale * axialMass * ( Cdot + bias ) - impulseScale * j->springImpulse;
+		j->springImpulse += deltaImpulse;
+		o_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, deltaImpulse );
+	}
+	if ( j->enableMotor )
+	{
+		float Cdot = o_dot( axisA, o_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+		float impulse = axialMass * ( j->motorSpeed - Cdot );
+		float oldImpulse = j->motorImpulse;
+		float maxImpulse = ctx->h * j->maxMotorForce;
+		j->motorImpulse = o_clamp( j->motorImpulse + impulse, -maxImpulse, maxImpulse );
+		impulse = j->motorImpulse - oldImpulse;
+		o_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, impulse );
+	}
+	if ( j->enableLimit )
+	{
+		float speculativeDistance = 0.25f * ( j->upperTranslation - j->lowerTranslation );
+		{
+			float C = translation - j->lowerTranslation;
+			if ( C < speculativeDistance )
+			{
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( C > 0.0f ) bias = o_min( C, 1.0f ) * ctx->inv_h;
+				else if ( useBias )
+				{
+					bias = softness.biasRate * C;
+					massScale = softness.massScale;
+					impulseScale = softness.impulseScale;
+				}
+				float oldImpulse = j->lowerImpulse;
+				float Cdot = o_dot( axisA, o_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+				float deltaImpulse = -axialMass * massScale * ( Cdot + bias ) - impulseScale * oldImpulse;
+				j->lowerImpulse = o_max( oldImpulse + deltaImpulse, 0.0f );
+				deltaImpulse = j->lowerImpulse - oldImpulse;
+				o_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, deltaImpulse );
+			}
+			else
+			{
+				j->lowerImpulse = 0.0f;
+			}
+		}
+		{
+			float C = j->upperTranslation - translation;
+			if ( C < speculativeDistance )
+			{
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( C > 0.0f ) bias = o_min( C, 1.0f ) * ctx->inv_h;
+				else if ( useBias )
+				{
+					bias = softness.biasRate * C;
+					massScale = softness.massScale;
+					impulseScale = softness.impulseScale;
+				}
+				float oldImpulse = j->upperImpulse;
+				float Cdot = o_dot( axisA, o_sub( vA, vB ) ) + a1 * wA - a2 * wB;
+				float deltaImpulse = -axialMass * massScale * ( Cdot + bias ) - impulseScale * oldImpulse;
+				j->upperImpulse = o_max( oldImpulse + deltaImpulse, 0.0f );
+				deltaImpulse = j->upperImpulse - oldImpulse;
+				b2Vec2 P = o_mulSV( deltaImpulse, axisA );
+				float LA = deltaImpulse * a1;
+				float LB = deltaImpulse * a2;
+				vA = o_mulAdd( vA, mA, P );
+				wA += iA * LA;
+				vB = o_mulSub( vB, mB, P );
+				wB -= iB * LB;
+			}
+			else
+			{
+				j->upperImpulse = 0.0f;
+			}
+		}
+	}
+	{
+		b2Vec2 perpA = o_leftPerp( axisA );
+		float s1 = o_cross( o_add( d, rA ), perpA );
+		float s2 = o_cross( rB, perpA );
+		b2Vec2 Cdot;
+		Cdot.x = o_dot( perpA, o_sub( vB, vA ) ) + s2 * wB - s1 * wA;
+		Cdot.y = wB - wA;
+		b2Vec2 bias = { 0.0f, 0.0f };
+		float massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias )
+		{
+			b2Vec2 C;
+			C.x = o_dot( perpA, d );
+			C.y = b2Atan2( relQ.s, relQ.c );
+			bias = o_mulSV( softness.biasRate, C );
+			massScale = softness.massScale;
+			impulseScale = softness.impulseScale;
+		}
+		float k11 = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+		float k12 = iA * s1 + iB * s2;
+		float k22 = iA + iB;
+		if ( k22 == 0.0f ) k22 = 1.0f;
+		b2Vec2 b = o_solve22( k11, k12, k12, k22, o_add( Cdot, bias ) );
+		b2Vec2 deltaImpulse;
+		deltaImpulse.x = -massScale * b.x - impulseScale * j->impulse.x;
+		deltaImpulse.y = -massScale * b.y - impulseScale * j->impulse.y;
+		j->impulse.x += deltaImpulse.x;
+		j->impulse.y += deltaImpulse.y;
+		b2Vec2 P = o_mulSV( deltaImpulse.x, perpA );
+		float LA = deltaImpulse.x * s1 + deltaImpulse.y;
+		float LB = deltaImpulse.x * s2 + deltaImpulse.y;
+		vA = o_mulSub( vA, mA, P );
+		wA -= iA * LA;
+		vB = o_mulAdd( vB, mB, P );
+		wB += iB * LB;
+	}
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = vA;
+		sA->angularVelocity = wA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = vB;
+		sB->angularVelocity = wB;
+	}
+}
+
+/* ---------------- weld (weld_joint.c:148-454, the non-block solver) ---------------- */
+static void o_prepareWeld( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	int ia, ib;
+	o_bodySim* simA = o_jointBodySim( w, base->bodyIdA, &ia );
+	o_bodySim* simB = o_jointBodySim( w, base->bodyIdB, &ib );
+	float iA = simA->invInertia, iB = simB->invInertia;
+	base->invMassA = simA->invMass;
+	base->invMassB = simB->invMass;
+	base->invIA = iA;
+	base->invIB = iB;
+	o_weldJoint* j = &base->weldJoint;
+	j->indexA = ia;
+	j->indexB = ib;
+	j->frameA.q = o_mulRot( simA->transform.q, base->localFrameA.q );
+	j->frameA.p = o_rotate( simA->transform.q, o_sub( base->localFrameA.p, simA->localCenter ) );
+	j->frameB.q = o_mulRot( simB->transform.q, base->localFrameB.q );
+	j->frameB.p = o_rotate( simB->transform.q, o_sub( base->localFrameB.p, simB->localCenter ) );
+	j->deltaCenter = o_v( simB->center.x - simA->center.x, simB->center.y - simA->center.y );
+	float ka = iA + iB;
+	j->axialMass = ka > 0.0f ? 1.0f / ka : 0.0f;
+	j->linearSpring = j->linearHertz == 0.0f ? base->constraintSoftness : o_makeSoft( j->linearHertz, j->linearDampingRatio, ctx->h );
+	j->angularSpring =
+		j->angularHertz == 0.0f ? base->constraintSoftness : o_makeSoft( j->angularHertz, j->angularDampingRatio, ctx->h );
+	if ( ctx->enableWarmStarting == 0 )
+	{
+		j->linearImpulse = o_v( 0.0f, 0.0f );
+		j->angularImpulse = 0.0f;
+	}
+}
+
+static void o_warmStartWeld( o_world* w, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_weldJoint* j = &base->weldJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = o_mulSub( sA->linearVelocity, mA, j->linearImpulse );
+		sA->angularVelocity -= iA * ( o_cross( rA, j->linearImpulse ) + j->angularImpulse );
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = o_mulAdd( sB->linearVelocity, mB, j->linearImpulse );
+		sB->angularVelocity += iB * ( o_cross( rB, j->linearImpulse ) + j->angularImpulse );
+	}
+}
+
+static void o_solveWeld( o_world* w, o_jointSim* base, int useBias )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_weldJoint* j = &base->weldJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 vA = sA->linearVelocity, vB = sB->linearVelocity;
+	float wA = sA->angularVelocity, wB = sB->angularVelocity;
+	{
+		b2Rot qA = o_mulRot( sA->deltaRotation, j->frameA.q );
+		b2Rot qB = o_mulRot( sB->deltaRotation, j->frameB.q );
+		b2Rot relQ = o_invMulRot( qA, qB );
+		float jointAngle = b2Atan2( relQ.s, relQ.c );
+		float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias || j->angularHertz > 0.0f )
+		{
+			float C = jointAngle;
+			bias = j->angularSpring.biasRate * C;
+			massScale = j->angularSpring.massScale;
+			impulseScale = j->angularSpring.impulseScale;
+		}
+		float Cdot = wB - wA;
+		float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->angularImpulse;
+		j->angularImpulse += impulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	{
+		b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+		b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+		b2Vec2 bias = { 0.0f, 0.0f };
+		float massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias || j->linearHertz > 0.0f )
+		{
+			b2Vec2 dcA = sA->deltaPosition, dcB = sB->deltaPosition;
+			b2Vec2 C = o_add( o_add( o_sub( dcB, dcA ), o_sub( rB, rA ) ), j->deltaCenter );
+			bias = o_mulSV( j->linearSpring.biasRate, C );
+			massScale = j->linearSpring.massScale;
+			impulseScale = j->linearSpring.impulseScale;
+		}
+		b2Vec2 Cdot = o_sub( o_add( vB, o_crossSV( wB, rB ) ), o_add( vA, o_crossSV( wA, rA ) ) );
+		float k11 = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+		float k12 = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+		float k22 = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+		b2Vec2 b = o_solve22( k11, k12, k12, k22, o_add( Cdot, bias ) );
+		b2Vec2 impulse = { -massScale * b.x - impulseScale * j->linearImpulse.x, -massScale * b.y - impulseScale * j->linearImpulse.y };
+		j->linearImpulse = o_add( j->linearImpulse, impulse );
+		vA = o_mulSub( vA, mA, impulse );
+		wA -= iA * o_cross( rA, impulse );
+		vB = o_mulAdd( vB, mB, impulse );
+		wB += iB * o_cross( rB, impulse );
+	}
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = vA;
+		sA->angularVelocity = wA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = vB;
+		sB->angularVelocity = wB;
+	}
+}
+
+/* ---------------- wheel (wheel_joint.c:197-525) ---------------- */
+static void o_prepareWheel( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	int ia, ib;
+	o_bodySim* simA = o_jointBodySim( w, base->bodyIdA, &ia );
+	o_bodySim* simB = o_jointBodySim( w, base->bodyIdB, &ib );
+	float mA = simA->invMass, iA = simA->invInertia, mB = simB->invMass, iB = simB->invInertia;
+	base->invMassA = mA;
+	base->invMassB = mB;
+	base->invIA = iA;
+	base->invIB = iB;
+	o_wheelJoint* j = &base->wheelJoint;
+	j->indexA = ia;
+	j->indexB = ib;
+	j->frameA.q = o_mulRot( simA->transform.q, base->localFrameA.q );
+	j->frameA.p = o_rotate( simA->transform.q, o_sub( base->localFrameA.p, simA->localCenter ) );
+	j->frameB.q = o_mulRot( simB->transform.q, base->localFrameB.q );
+	j->frameB.p = o_rotate( simB->transform.q, o_sub( base->localFrameB.p, simB->localCenter ) );
+	j->deltaCenter = o_v( simB->center.x - simA->center.x, simB->center.y - simA->center.y );
+	b2Vec2 rA = j->frameA.p, rB = j->frameB.p;
+	b2Vec2 d = o_add( j->deltaCenter, o_sub( rB, rA ) );
+	b2Vec2 axisA = o_rotate( j->frameA.q, o_v( 1.0f, 0.0f ) );
+	b2Vec2 perpA = o_leftPerp( axisA );
+	float s1 = o_cross( o_add( d, rA ), perpA );
+	float s2 = o_cross( rB, perpA );
+	float kp = mA + mB + iA * s1 * s1 + iB * s2 * s2;
+	j->perpMass = kp > 0.0f ? 1.0f / kp : 0.0f;
+	float a1 = o_cross( o_add( d, rA ), axisA );
+	float a2 = o_cross( rB, axisA );
+	float ka = mA + mB + iA * a1 * a1 + iB * a2 * a2;
+	j->axialMass = ka > 0.0f ? 1.0f / ka : 0.0f;
+	j->springSoftness = o_makeSoft( j->hertz, j->dampingRatio, ctx->h );
+	float km = iA + iB;
+	j->motorMass = km > 0.0f ? 1.0f / km : 0.0f;
+	if ( ctx->enableWarmStarting == 0 )
+	{
+		j->perpImpulse = 0.0f;
+		j->springImpulse = 0.0f;
+		j->motorImpulse = 0.0f;
+		j->lowerImpulse = 0.0f;
+		j->upperImpulse = 0.0f;
+	}
+}
+
+static void o_warmStartWheel( o_world* w, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_wheelJoint* j = &base->wheelJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	b2Vec2 d = o_add( o_add( o_sub( sB->deltaPosition, sA->deltaPosition ), j->deltaCenter ), o_sub( rB, rA ) );
+	b2Vec2 axisA = o_rotate( j->frameA.q, o_v( 1.0f, 0.0f ) );
+	axisA = o_rotate( sA->deltaRotation, axisA );
+	b2Vec2 perpA = o_leftPerp( axisA );
+	float a1 = o_cross( o_add( d, rA ), axisA );
+	float a2 = o_cross( rB, axisA );
+	float s1 = o_cross( o_add( d, rA ), perpA );
+	float s2 = o_cross( rB, perpA );
+	float axialImpulse = j->springImpulse + j->lowerImpulse - j->upperImpulse;
+	b2Vec2 P = o_add( o_mulSV( axialImpulse, axisA ), o_mulSV( j->perpImpulse, perpA ) );
+	float LA = axialImpulse * a1 + j->perpImpulse * s1 + j->motorImpulse;
+	float LB = axialImpulse * a2 + j->perpImpulse * s2 + j->motorImpulse;
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = o_mulSub( sA->linearVelocity, mA, P );
+		sA->angularVelocity -= iA * LA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = o_mulAdd( sB->linearVelocity, mB, P );
+		sB->angularVelocity += iB * LB;
+	}
+}
+
+static void o_solveWheel( o_world* w, o_stepContext* ctx, o_jointSim* base, int useBias )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_wheelJoint* j = &base->wheelJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 vA = sA->linearVelocity, vB = sB->linearVelocity;
+	float wA = sA->angularVelocity, wB = sB->angularVelocity;
+	int fixedRotation = ( iA + iB == 0.0f );
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	b2Vec2 d = o_add( o_add( o_sub( sB->deltaPosition, sA->deltaPosition ), j->deltaCenter ), o_sub( rB, rA ) );
+	b2Vec2 axisA = o_rotate( j->frameA.q, o_v( 1.0f, 0.0f ) );
+	axisA = o_rotate( sA->deltaRotation, axisA );
+	float translation = o_dot( axisA, d );
+	float a1 = o_cross( o_add( d, rA ), axisA );
+	float a2 = o_cross( rB, axisA );
+	if ( j->enableMotor && fixedRotation == 0 )
+	{
+		float Cdot = wB - wA - j->motorSpeed;
+		float impulse = -j->motorMass * Cdot;
+		float oldImpulse = j->motorImpulse;
+		float maxImpulse = ctx->h * j->maxMotorTorque;
+		j->motorImpulse = o_clamp( j->motorImpulse + impulse, -maxImpulse, maxImpulse );
+		impulse = j->motorImpulse - oldImpulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	if ( j->enableSpring )
+	{
+		float C = translation;
+		float bias = j->springSoftness.biasRate * C;
+		float massScale = j->springSoftness.massScale;
+		float impulseScale = j->springSoftness.impulseScale;
+		float Cdot = o_dot( axisA, o_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+		float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->springImpulse;
+		j->springImpulse += impulse;
+		o_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, impulse );
+	}
+	if ( j->enableLimit )
+	{
+		{
+			float C = translation - j->lowerTranslation;
+			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+			if ( C > 0.0f ) bias = C * ctx->inv_h;
+			else if ( useBias )
+			{
+				bias = base->constraintSoftness.biasRate * C;
+				massScale = base->constraintSoftness.massScale;
+				impulseScale = base->constraintSoftness.impulseScale;
+			}
+			float Cdot = o_dot( axisA, o_sub( vB, vA ) ) + a2 * wB - a1 * wA;
+			float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->lowerImpulse;
+			float oldImpulse = j->lowerImpulse;
+			j->lowerImpulse = o_max( oldImpulse + impulse, 0.0f );
+			impulse = j->lowerImpulse - oldImpulse;
+			o_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, axisA, a1, a2, impulse );
+		}
+		{
+			float C = j->upperTranslation - translation;
+			float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+			if ( C > 0.0f ) bias = C * ctx->inv_h;
+			else if ( useBias )
+			{
+				bias = base->constraintSoftness.biasRate * C;
+				massScale = base->constraintSoftness.massScale;
+				impulseScale = base->constraintSoftness.impulseScale;
+			}
+			float Cdot = o_dot( axisA, o_sub( vA, vB ) ) + a1 * wA - a2 * wB;
+			float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->upperImpulse;
+			float oldImpulse = j->upperImpulse;
+			j->upperImpulse = o_max( oldImpulse + impulse, 0.0f );
+			impulse = j->upperImpulse - oldImpulse;
+			b2Vec2 P = o_mulSV( impulse, axisA );
+			float LA = impulse * a1;
+			float LB = impulse * a2;
+			vA = o_mulAdd( vA, mA, P );
+			wA += iA * LA;
+			vB = o_mulSub( vB, mB, P );
+			wB -= iB * LB;
+		}
+	}
+	{
+		b2Vec2 perpA = o_leftPerp( axisA );
+		float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias )
+		{
+			float C = o_dot( perpA, d );
+			bias = base->constraintSoftness.biasRate * C;
+			massScale = base->constraintSoftness.massScale;
+			impulseScale = base->constraintSoftness.impulseScale;
+		}
+		float s1 = o_cross( o_add( d, rA ), perpA );
+		float s2 = o_cross( rB, perpA );
+		float Cdot = o_dot( perpA, o_sub( vB, vA ) ) + s2 * wB - s1 * wA;
+		float impulse = -massScale * j->perpMass * ( Cdot + bias ) - impulseScale * j->perpImpulse;
+		j->perpImpulse += impulse;
+		o_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, perpA, s1, s2, impulse );
+	}
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = vA;
+		sA->angularVelocity = wA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = vB;
+		sB->angularVelocity = wB;
+	}
+}
+
+/* ---------------- distance (distance_joint.c:250-543) ---------------- */
+static void o_prepareDistance( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	int ia, ib;
+	o_bodySim* simA = o_jointBodySim( w, base->bodyIdA, &ia );
+	o_bodySim* simB = o_jointBodySim( w, base->bodyIdB, &ib );
+	float mA = simA->invMass, iA = simA->invInertia, mB = simB->invMass, iB = simB->invInertia;
+	base->invMassA = mA;
+	base->invMassB = mB;
+	base->invIA = iA;
+	base->invIB = iB;
+	o_distanceJoint* j = &base->distanceJoint;
+	j->indexA = ia;
+	j->indexB = ib;
+	j->anchorA = o_rotate( simA->transform.q, o_sub( base->localFrameA.p, simA->localCenter ) );
+	j->anchorB = o_rotate( simB->transform.q, o_sub( base->localFrameB.p, simB->localCenter ) );
+	j->deltaCenter = o_v( simB->center.x - simA->center.x, simB->center.y - simA->center.y );
+	b2Vec2 rA = j->anchorA, rB = j->anchorB;
+	b2Vec2 separation = o_add( o_sub( rB, rA ), j->deltaCenter );
+	b2Vec2 axis = o_normalize( separation );
+	float crA = o_cross( rA, axis );
+	float crB = o_cross( rB, axis );
+	float k = mA + mB + iA * crA * crA + iB * crB * crB;
+	j->axialMass = k > 0.0f ? 1.0f / k : 0.0f;
+	j->distanceSoftness = o_makeSoft( j->hertz, j->dampingRatio, ctx->h );
+	if ( ctx->enableWarmStarting == 0 )
+	{
+		j->impulse = 0.0f;
+		j->lowerImpulse = 0.0f;
+		j->upperImpulse = 0.0f;
+		j->motorImpulse = 0.0f;
+	}
+}
+
+static void o_warmStartDistance( o_world* w, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_distanceJoint* j = &base->distanceJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->anchorA );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->anchorB );
+	b2Vec2 ds = o_add( o_sub( sB->deltaPosition, sA->deltaPosition ), o_sub( rB, rA ) );
+	b2Vec2 separation = o_add( j->deltaCenter, ds );
+	b2Vec2 axis = o_normalize( separation );
+	float axialImpulse = j->impulse + j->lowerImpulse - j->upperImpulse + j->motorImpulse;
+	b2Vec2 P = o_mulSV( axialImpulse, axis );
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = o_mulSub( sA->linearVelocity, mA, P );
+		sA->angularVelocity -= iA * o_cross( rA, P );
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = o_mulAdd( sB->linearVelocity, mB, P );
+		sB->angularVelocity += iB * o_cross( rB, P );
+	}
+}
+
+/* apply P = impulse * axis at anchors rA, rB */
+static void o_applyLinear( b2Vec2* vA, float* wA, b2Vec2* vB, float* wB, float mA, float iA, float mB, float iB, b2Vec2 rA,
+						   b2Vec2 rB, b2Vec2 P )
+{
+	*vA = o_mulSub( *vA, mA, P );
+	*wA -= iA * o_cross( rA, P );
+	*vB = o_mulAdd( *vB, mB, P );
+	*wB += iB * o_cross( rB, P );
+}
+
+static void o_solveDistance( o_world* w, o_stepContext* ctx, o_jointSim* base, int useBias )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_distanceJoint* j = &base->distanceJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 vA = sA->linearVelocity, vB = sB->linearVelocity;
+	float wA = sA->angularVelocity, wB = sB->angularVelocity;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->anchorA );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->anchorB );
+	b2Vec2 ds = o_add( o_sub( sB->deltaPosition, sA->deltaPosition ), o_sub( rB, rA ) );
+	b2Vec2 separation = o_add( j->deltaCenter, ds );
+	float length = o_length( separation );
+	b2Vec2 axis = o_normalize( separation );
+	if ( j->enableSpring && ( j->minLength < j->maxLength || j->enableLimit == 0 ) )
+	{
+		if ( j->hertz > 0.0f )
+		{
+			b2Vec2 vr = o_add( o_sub( vB, vA ), o_sub( o_crossSV( wB, rB ), o_crossSV( wA, rA ) ) );
+			float cdot = o_dot( axis, vr );
+			float c = length - j->length;
+			float bias = j->distanceSoftness.biasRate * c;
+			float m = j->distanceSoftness.massScale * j->axialMass;
+			float oldImpulse = j->impulse;
+			float impulse = -m * ( cdot + bias ) - j->distanceSoftness.impulseScale * oldImpulse;
+			float h = ctx->h;
+			j->impulse = o_clamp( j->impulse + impulse, j->lowerSpringForce * h, j->upperSpringForce * h );
+			impulse = j->impulse - oldImpulse;
+			o_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, o_mulSV( impulse, axis ) );
+		}
+		if ( j->enableMotor )
+		{
+			b2Vec2 vr = o_add( o_sub( vB, vA ), o_sub( o_crossSV( wB, rB ), o_crossSV( wA, rA ) ) );
+			float Cdot = o_dot( axis, vr );
+			float impulse = j->axialMass * ( j->motorSpeed - Cdot );
+			float oldImpulse = j->motorImpulse;
+			float maxImpulse = ctx->h * j->maxMotorForce;
+			j->motorImpulse = o_clamp( j->motorImpulse + impulse, -maxImpulse, maxImpulse );
+			impulse = j->motorImpulse - oldImpulse;
+			o_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, o_mulSV( impulse, axis ) );
+		}
+		if ( j->enableLimit )
+		{
+			{
+				b2Vec2 vr = o_add( o_sub( vB, vA ), o_sub( o_crossSV( wB, rB ), o_crossSV( wA, rA ) ) );
+				float cdot = o_dot( axis, vr );
+				float c = length - j->minLength;
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( c > 0.0f ) bias = c * ctx->inv_h;
+				else if ( useBias )
+				{
+					bias = base->constraintSoftness.biasRate * c;
+					massScale = base->constraintSoftness.massScale;
+					impulseScale = base->constraintSoftness.impulseScale;
+				}
+				float impulse = -massScale * j->axialMass * ( cdot + bias ) - impulseScale * j->lowerImpulse;
+				float newImpulse = o_max( 0.0f, j->lowerImpulse + impulse );
+				impulse = newImpulse - j->lowerImpulse;
+				j->lowerImpulse = newImpulse;
+				o_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, o_mulSV( impulse, axis ) );
+			}
+			{
+				b2Vec2 vr = o_add( o_sub( vA, vB ), o_sub( o_crossSV( wA, rA ), o_crossSV( wB, rB ) ) );
+				float Cdot = o_dot( axis, vr );
+				float C = j->maxLength - length;
+				float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+				if ( C > 0.0f ) bias = C * ctx->inv_h;
+				else if ( useBias )
+				{
+					bias = base->constraintSoftness.biasRate * C;
+					massScale = base->constraintSoftness.massScale;
+					impulseScale = base->constraintSoftness.impulseScale;
+				}
+				float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->upperImpulse;
+				float newImpulse = o_max( 0.0f, j->upperImpulse + impulse );
+				impulse = newImpulse - j->upperImpulse;
+				j->upperImpulse = newImpulse;
+				o_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, o_mulSV( -impulse, axis ) );
+			}
+		}
+	}
+	else
+	{
+		b2Vec2 vr = o_add( o_sub( vB, vA ), o_sub( o_crossSV( wB, rB ), o_crossSV( wA, rA ) ) );
+		float Cdot = o_dot( axis, vr );
+		float C = length - j->length;
+		float bias = 0.0f, massScale = 1.0f, impulseScale = 0.0f;
+		if ( useBias )
+		{
+			bias = base->constraintSoftness.biasRate * C;
+			massScale = base->constraintSoftness.massScale;
+			impulseScale = base->constraintSoftness.impulseScale;
+		}
+		float impulse = -massScale * j->axialMass * ( Cdot + bias ) - impulseScale * j->impulse;
+		j->impulse += impulse;
+		o_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, o_mulSV( impulse, axis ) );
+	}
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = vA;
+		sA->angularVelocity = wA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = vB;
+		sB->angularVelocity = wB;
+	}
+}
+
 /* ---------------- dispatch (joint.c:1406-1540) ---------------- */
 int o_unsupportedJoints = 0;
 
@@ -490,7 +1204,11 @@ void o_prepareJoint( o_world* w, o_stepContext* ctx, o_jointSim* j )
 	j->constraintSoftness = o_makeSoft( hertz, j->constraintDampingRatio, ctx->h );
 	switch ( j->type )
 	{
+		case b2_distanceJoint: o_prepareDistance( w, ctx, j ); break;
+		case b2_prismaticJoint: o_preparePrismatic( w, ctx, j ); break;
 		case b2_revoluteJoint: o_prepareRevolute( w, ctx, j ); break;
+		case b2_weldJoint: o_prepareWeld( w, ctx, j ); break;
+		case b2_wheelJoint: o_prepareWheel( w, ctx, j ); break;
 		default: o_unsupportedJoints += 1; break;
 	}
 }
@@ -500,7 +1218,11 @@ void o_warmStartJoint( o_world* w, o_stepContext* ctx, o_jointSim* j )
 	(void)ctx;
 	switch ( j->type )
 	{
+		case b2_distanceJoint: o_warmStartDistance( w, j ); break;
+		case b2_prismaticJoint: o_warmStartPrismatic( w, j ); break;
 		case b2_revoluteJoint: o_warmStartRevolute( w, j ); break;
+		case b2_weldJoint: o_warmStartWeld( w, j ); break;
+		case b2_wheelJoint: o_warmStartWheel( w, j ); break;
 		default: break;
 	}
 }
@@ -509,7 +1231,11 @@ void o_solveJoint( o_world* w, o_stepContext* ctx, o_jointSim* j, int useBias )
 {
 	switch ( j->type )
 	{
+		case b2_distanceJoint: o_solveDistance( w, ctx, j, useBias ); break;
+		case b2_prismaticJoint: o_solvePrismatic( w, ctx, j, useBias ); break;
 		case b2_revoluteJoint: o_solveRevolute( w, ctx, j, useBias ); break;
+		case b2_weldJoint: o_solveWeld( w, j, useBias ); break;
+		case b2_wheelJoint: o_solveWheel( w, ctx, j, useBias ); break;
 		default: break;
 	}
 }

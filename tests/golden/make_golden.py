@@ -33,6 +33,7 @@ SCENES = [
     ("joint_grid_mixed_12", B.JOINT_GRID_MIXED, 12, 40, 0, 3, B.NO_CONTINUOUS, 200, [1, 100, 200]),
     ("batch_world_60", B.BATCH_WORLD, 60, 0, 0, 11, B.NO_CONTINUOUS, 200, [1, 200]),
     ("ramp_world_4x4", B.RAMP_WORLD, 4, 4, 0, 5, B.NO_CONTINUOUS, 120, [1, 120]),
+    ("joint_zoo_4", B.JOINT_ZOO, 4, 0, 0, 3, B.NO_CONTINUOUS, 300, [1, 150, 300]),
 ]
 
 

@@ -45,6 +45,12 @@ def test_gpu_vs_oracle_batch_worlds(gpu_lib, oracle, seed):
     _lockstep(gpu_lib, oracle, B.BATCH_WORLD, 0, 0, 0, seed, B.NO_CONTINUOUS, 150)
 
 
+@pytest.mark.parametrize("seed", [5, 6, 7])
+def test_gpu_vs_oracle_joint_zoo(gpu_lib, oracle, seed):
+    """Prismatic, weld, wheel, distance and revolute joints with limits, motors and springs."""
+    _lockstep(gpu_lib, oracle, B.JOINT_ZOO, 8, 0, 0, seed, B.NO_CONTINUOUS, 200)
+
+
 def test_gpu_vs_oracle_joint_grid_mixed(gpu_lib, oracle):
     _lockstep(gpu_lib, oracle, B.JOINT_GRID_MIXED, 30, 200, 0, 9, B.NO_CONTINUOUS, 120)
 

@@ -22,6 +22,7 @@ CASES = [
     ("joint_grid_big", B.JOINT_GRID_MIXED, 20, 60, 0, 5, B.NO_CONTINUOUS, 60),
     ("shape_zoo_restitution", B.SHAPE_ZOO, 150, 0, 0, 2, B.NO_CONTINUOUS, 100),
     ("batch_world", B.BATCH_WORLD, 0, 0, 0, 22, B.NO_CONTINUOUS, 100),
+    ("joint_zoo", B.JOINT_ZOO, 6, 0, 0, 4, B.NO_CONTINUOUS, 150),
 ]
 
 
