@@ -55,6 +55,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2p_stream": (c_p, [c_u32]),
         "b2p_status": (c_int, [c_u32]),
         "b2p_host_profile": (c_int, [c_u32, c_p, c_int]),
+        "b2p_contacts_noalloc": (c_int, [c_u32, c_p, c_int]),
     }
     for name, (res, args) in optional.items():
         if hasattr(lib, name):

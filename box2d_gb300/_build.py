@@ -24,7 +24,7 @@ HOST_SOURCES = ["csrc/host/world.c", "csrc/host/step.c", "csrc/host/joint.c", "c
 # (source, extra nvcc flags). The cluster and persistent solvers read state written by
 # other SMs between barriers, so their global loads bypass L1 (-dlcm=cg).
 DEVICE_SOURCES = [("csrc/device/world.cu", []), ("csrc/device/components.cu", []),
-                  ("csrc/device/cluster.cu", ["-Xptxas", "-dlcm=cg"]),
+                  ("csrc/device/cluster.cu", ["-Xptxas", "-dlcm=cg"]), ("csrc/device/noalloc.cu", []),
                   ("csrc/device/persistent.cu", ["-Xptxas", "-dlcm=cg"])]
 
 NVCC_FLAGS = ["-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",

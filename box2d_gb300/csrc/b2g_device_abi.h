@@ -202,6 +202,12 @@ int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* contactIds, int count );
 int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* colorContactIds, const int* colorContactOffsets,
 						 int totalContacts );
 int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count );
+/* device addresses of the contact records and the color lists, the color offsets and the
+   world's stream (cudaStream_t), for kernels outside world.cu */
+void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const int** colorIds, int* colorOffsets,
+						 void** stream );
+/* the contact table of b2p_contacts built without allocating (noalloc.cu) */
+int b2gDev_ContactTableNoAlloc( b2gDeviceWorld* dw, int capacity, int* out, int outCapacity );
 
 /* joints */
 int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* colorJointOffsets );

@@ -937,6 +937,15 @@ extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const in
 	return 0;
 }
 
+extern "C" void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const int** colorIds, int* colorOffsets,
+									void** stream )
+{
+	*contacts = dw->contacts;
+	*colorIds = dw->colorIds;
+	memcpy( colorOffsets, dw->colorOffsets, sizeof( dw->colorOffsets ) );
+	*stream = (void*)dw->stream;
+}
+
 extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count )
 {
 	if ( count == 0 ) return 0;

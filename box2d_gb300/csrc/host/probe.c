@@ -6,6 +6,8 @@
  */
 #include "b2g_world.h"
 
+#include <stdio.h>
+
 #define B2P_EXPORT __attribute__( ( visibility( "default" ) ) )
 
 static b2gContact* h_downloadContacts( h_world* w )
@@ -119,4 +121,23 @@ B2P_EXPORT int b2p_host_profile( uint32_t packedWorldId, float* out, int reset )
 	memcpy( out, w->hostMs, sizeof( w->hostMs ) );
 	if ( reset ) memset( w->hostMs, 0, sizeof( w->hostMs ) );
 	return 0;
+}
+
+/* b2p_contacts without any allocation: the table is built on the device in a fixed scratch
+   array (see noalloc.cu for its limit and rules). Needs a world that has been stepped with
+   a positive time step since its last change; returns the row count (may exceed
+   capacity), -1 for an unknown or never-stepped world, -2 when the world has more contact
+   ids than the scratch holds, or -(1000 + CUDA error code). */
+B2P_EXPORT int b2p_contacts_noalloc( uint32_t packedWorldId, int* out, int capacity )
+{
+	b2WorldId id = { (uint16_t)( packedWorldId >> 16 ), (uint16_t)( packedWorldId & 0xFFFF ) };
+	h_world* w = h_worldFromId( id );
+	if ( w == NULL || w->devReady == 0 ) return -1;
+	int rc = b2gDev_ContactTableNoAlloc( w->dev, w->contactIdPool.nextIndex, out, capacity );
+	if ( rc == -2 )
+		fprintf( stderr, "b2p_contacts_noalloc: the world has %d contact ids, more than the fixed scratch holds; use b2p_contacts\n",
+				 w->contactIdPool.nextIndex );
+	else if ( rc <= -1000 )
+		fprintf( stderr, "b2p_contacts_noalloc: %s\n", b2gDev_ErrorString( -1000 - rc ) );
+	return rc;
 }

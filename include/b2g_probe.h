@@ -19,6 +19,16 @@ extern "C"
    packedWorldId = (index1 << 16) | generation. Returns the row count (may exceed capacity). */
 int b2p_contacts( uint32_t packedWorldId, int* out, int capacity );
 
+/* The table of b2p_contacts built without allocating anything (no counterpart in the
+   reference). For callers that may not allocate while they run -- a real-time loop or a
+   capture of a CUDA stream, where cudaMalloc/cudaFree and host malloc would stall or be
+   illegal. Limit: 32768 contact ids per world (-2 and a message above it). The scratch is
+   one fixed device array per process: calls whose GPU work overlaps race on it, and the
+   first call on a device (which resolves that array) must precede any stream capture.
+   Returns the row count (may exceed capacity), -1 for an unknown or never-stepped world,
+   or -(1000 + CUDA error code). */
+int b2p_contacts_noalloc( uint32_t packedWorldId, int* out, int capacity );
+
 /* 12 floats per live contact: normal (2), then per point: separation, normalImpulse,
    tangentImpulse, anchorA (2). Returns the row count. */
 int b2p_contact_floats( uint32_t packedWorldId, float* out, int capacity );
