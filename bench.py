@@ -40,7 +40,7 @@ import box2d_gb300 as B  # noqa: E402
 
 # untimed steps before the warm-up: the many-pyramids rain reaches the pyramids after about
 # 150 steps, so the timed window starts where the scene's contact churn does
-START_STEPS = {"many_pyramids": 200, "large_pyramid": 0, "joint_grid": 0}
+START_STEPS = {"many_pyramids": 200, "large_pyramid": 0, "joint_grid": 0, "batch_worlds": 0}
 
 WORKLOADS = {
     # name: (kind, a, b, c, seed, flags, description)
@@ -49,6 +49,8 @@ WORKLOADS = {
     "large_pyramid": (B.LARGE_PYRAMID, 100, 1, 0, 0, 0, "100-row pyramid of 5050 boxes on a 200 m segment"),
     "joint_grid": (B.JOINT_GRID_MIXED, 100, 3000, 0, 0, B.NO_CONTINUOUS,
                    "100x100 revolute circle grid + 3000 mixed shapes"),
+    "batch_worlds": (B.BATCH_WORLD, 0, 0, 0, 12345, B.NO_CONTINUOUS,
+                     "independent worlds of 10-400 boxes, circles and capsules in a 3-segment container"),
 }
 
 
@@ -189,6 +191,57 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
     }
 
 
+def run_batch(args) -> dict:
+    """Batched worlds: `args.worlds` independent worlds (body count drawn from 10-400 per
+    world, seed 12345 + index) stepped together with b2World_StepBatch on all host cores,
+    and, for comparison, the same worlds stepped one after the other (the plain per-world
+    loop). Wall clock: every world's step returns only after its device work is done."""
+    import ctypes
+
+    import torch
+
+    torch.cuda.set_device(0)
+    lib = B.load_library()
+    n = args.worlds
+    scenes = [B.Scene(lib, B.BATCH_WORLD, 0, 0, 0, 12345 + i, B.NO_CONTINUOUS) for i in range(n)]
+    handles = (ctypes.c_int * n)(*[s.handle for s in scenes])
+    dyn = sum(s.dynamic_count for s in scenes)
+    threads = args.threads if args.threads > 0 else 4 * max(1, os.cpu_count() or 1)
+    dt = 1.0 / 60.0
+    lib.b2s_step_batch(handles, n, dt, 4, args.warmup, threads)
+    plain_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    lib.b2s_step_batch(handles, n, dt, 4, plain_steps, 1)
+    plain_s = time.perf_counter() - t0
+    for s in scenes:
+        s.timings(reset=True)
+    with ClockSampler(0) as clocks:
+        t0 = time.perf_counter()
+        lib.b2s_step_batch(handles, n, dt, 4, args.steps, threads)
+        batch_s = time.perf_counter() - t0
+    launches = 0
+    h2d = d2h = 0
+    for s in scenes:
+        _, traffic = s.timings(reset=True)
+        h2d += int(traffic[0])
+        d2h += int(traffic[1])
+        launches += int(traffic[2])
+    # end to end: the batched step plus every world's move events
+    events = __import__("numpy").zeros((max(s.body_count for s in scenes), 4), "float32")
+    e2e_steps = max(1, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        lib.b2s_step_batch(handles, n, dt, 4, 1, threads)
+        for s in scenes:
+            s.move_events(events)
+    e2e_s = time.perf_counter() - t0
+    for s in scenes:
+        s.close()
+    return {"dyn": dyn, "batch_s": batch_s, "plain_s": plain_s, "plain_steps": plain_steps, "threads": threads,
+            "launches": launches, "h2d": h2d / args.steps, "d2h": d2h / args.steps, "clocks": clocks.summary,
+            "e2e_value": dyn * e2e_steps / e2e_s}
+
+
 def run_cpu_sample(args, budget_s: float, max_steps: int) -> dict:
     """The oracle (serial CPU restatement of the reference step) on the same workload."""
     kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
@@ -216,6 +269,8 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="many_pyramids", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--worlds", type=int, default=4096, help="world count of the batch_worlds workload")
+    ap.add_argument("--threads", type=int, default=0, help="host threads of the batch_worlds workload (0: 4 per core)")
     ap.add_argument("--start-step", type=int, default=-1,
                     help="untimed steps before the warm-up (default: per workload)")
     args = ap.parse_args()
@@ -244,6 +299,28 @@ def main() -> None:
                 "cpu_baseline": {"value": r["value"], "unit": "body-steps/s", "cores": cores, "kind": "port",
                                  "sample": f"{r['steps']} steps after {args.start_step + args.warmup} untimed steps, serial C oracle"},
                 "e2e": {"value": r["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if args.workload == "batch_worlds" and args.impl == "gb300":
+        if rank != 0:
+            return
+        r = run_batch(args)
+        value = r["dyn"] * args.steps / r["batch_s"]
+        plain = r["dyn"] * r["plain_steps"] / r["plain_s"]
+        config.update({"worlds": args.worlds, "host_threads": r["threads"],
+                       "l2": "inputs larger than L2 (all worlds' state and constraints), no flush",
+                       "timing": "wall clock; each world's step returns after its device work completes"})
+        line = {
+            "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * r["batch_s"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene builders)",
+            "config": config, "plain_loop": {"value": plain, "steps": r["plain_steps"], "speedup": value / plain},
+            "roofline": None, "cpu_baseline": None,
+            "e2e": {"value": r["e2e_value"], "unit": "body-steps/s", "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"], "read": "every world's move events after every batched step"},
+            "gpu_launches": r["launches"], "clocks": r["clocks"],
+        }
         print(json.dumps(line))
         return
 

@@ -38,6 +38,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2s_create": (c_int, [c_int, c_int, c_int, c_int, c_u32, c_int]),
         "b2s_destroy": (None, [c_int]),
         "b2s_step": (None, [c_int, c_f, c_int, c_int]),
+        "b2s_step_batch": (None, [c_p, c_int, c_f, c_int, c_int, c_int]),
         "b2s_body_count": (c_int, [c_int]),
         "b2s_dynamic_count": (c_int, [c_int]),
         "b2s_world_id": (c_u32, [c_int]),

@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libbox2d_gb300.so"
 
 HOST_SOURCES = ["csrc/host/world.c", "csrc/host/step.c", "csrc/host/joint.c", "csrc/host/tree.c",
-                "csrc/host/geometry.c", "csrc/host/probe.c", "scenes/scenes.c"]
+                "csrc/host/geometry.c", "csrc/host/probe.c", "csrc/host/batch.c", "scenes/scenes.c"]
 # (source, extra nvcc flags). The cluster and persistent solvers read state written by
 # other SMs between barriers, so their global loads bypass L1 (-dlcm=cg).
 DEVICE_SOURCES = [("csrc/device/world.cu", []), ("csrc/device/components.cu", []),
@@ -67,7 +67,7 @@ def build_library(force: bool = False) -> Path:
         o = BUILD / (src.replace("/", "_") + ".o")
         objects.append(o)
         if force or _needs(o, [s] + headers):
-            jobs.append(["gcc", *CFLAGS, *include, "-c", str(s), "-o", str(o)])
+            jobs.append(["gcc", *CFLAGS, "-DB2S_BATCH_API", *include, "-c", str(s), "-o", str(o)])
     for src, extra in DEVICE_SOURCES:
         s = PKG / src
         o = BUILD / (src.replace("/", "_") + ".o")

@@ -237,7 +237,10 @@ typedef struct b2gHostTreeNode
 
 /* copy nodeCount host nodes to the device and convert them to query nodes on the
    device. The host array must stay unchanged until the next pair query returns. */
-int b2gDev_UploadTree( b2gDeviceWorld* dw, int treeType, const b2gHostTreeNode* nodes, int nodeCount, int root );
+int b2gDev_UploadTree( b2gDeviceWorld* dw, int treeType, const b2gHostTreeNode* nodes, int nodeCount, int root,
+					   int hostPinned );
+/* waits of this world block the calling thread (sleep) instead of spinning */
+void b2gDev_SetBlockingSync( b2gDeviceWorld* dw, int on );
 
 /* page-locked host memory (NULL on failure) for arrays uploaded every step */
 void* b2gDev_HostAlloc( size_t bytes );

@@ -18,6 +18,7 @@
 #include "components.cuh"
 
 #include <cooperative_groups.h>
+#include <pthread.h>
 #include <string.h>
 
 namespace cg = cooperative_groups;
@@ -169,7 +170,9 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 									const int* activeColors, int activeColorCount, int useLists, int bodyCount,
 									cudaStream_t stream, long long* launches )
 {
+	static pthread_mutex_t s_lock = PTHREAD_MUTEX_INITIALIZER;
 	static int s_ranks = -1;
+	pthread_mutex_lock( &s_lock );
 	if ( s_ranks < 0 )
 	{
 		s_ranks = 0;
@@ -178,6 +181,7 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 				 cudaSuccess )
 		{
 			cudaGetLastError();
+			pthread_mutex_unlock( &s_lock );
 			return -1;
 		}
 		for ( int ranks = 16; ranks >= 8 && s_ranks == 0; ranks /= 2 )
@@ -199,12 +203,14 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 			cudaGetLastError();
 		}
 	}
-	if ( s_ranks == 0 ) return -1;
+	int ranks = s_ranks;
+	pthread_mutex_unlock( &s_lock );
+	if ( ranks == 0 ) return -1;
 	int counts[B2_GRAPH_COLOR_COUNT];
 	for ( int k = 0; k < activeColorCount; ++k )
 		counts[k] = useLists ? b->hSummary->bigContactCount[activeColors[k]]
 							 : a->colorOffsets[activeColors[k] + 1] - a->colorOffsets[activeColors[k]];
-	size_t smem = clusterSmem( counts, activeColorCount, s_ranks );
+	size_t smem = clusterSmem( counts, activeColorCount, ranks );
 	if ( smem > B2G_CLUSTER_SMEM_MAX ) return -1;
 	d_clusterPlan plan;
 	memset( &plan, 0, sizeof( plan ) );
@@ -222,10 +228,10 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	memset( &cfg, 0, sizeof( cfg ) );
 	cudaLaunchAttribute attr;
 	attr.id = cudaLaunchAttributeClusterDimension;
-	attr.val.clusterDim.x = s_ranks;
+	attr.val.clusterDim.x = ranks;
 	attr.val.clusterDim.y = 1;
 	attr.val.clusterDim.z = 1;
-	cfg.gridDim = dim3( s_ranks );
+	cfg.gridDim = dim3( ranks );
 	cfg.blockDim = dim3( B2G_CLUSTER_THREADS );
 	cfg.dynamicSmemBytes = smem > 0 ? smem : 16;
 	cfg.stream = stream;

@@ -13,6 +13,7 @@
  */
 #include "components.cuh"
 
+#include <pthread.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -194,6 +195,7 @@ struct d_compArgs
 	b2gCompSummary* summary;
 	const int* awakeIndex;
 	d_offsets jointOffsets;
+	int identity; /* one bin holding the whole world: lists and local indices are the identity */
 };
 
 __global__ void k_compScatter( d_solveArgs a, d_compArgs c, int n, int total, int jointTotal )
@@ -249,6 +251,11 @@ __global__ void k_compScatter( d_solveArgs a, d_compArgs c, int n, int total, in
 /* One bin per CTA: bodies, contact constraints and joints of the bin's components live in
    shared memory for the whole step; colors run in ascending index order with a CTA barrier
    between them, exactly the stage sequence of solver.c:1010-1198 without an overflow color. */
+#define D_BODY( x ) ( c.identity ? ( x ) : c.bodyList[x] )
+#define D_SLOT( x ) ( c.identity ? ( x ) : c.slotList[x] )
+#define D_JOINT( x ) ( c.identity ? ( x ) : c.jointList[x] )
+#define D_LOCAL( x ) ( c.identity ? ( x ) : c.localIndex[x] )
+
 __global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a, d_compArgs c, d_jointBodies jb,
 																   b2gStepCounters* counters, int smemBytes )
 {
@@ -256,13 +263,27 @@ __global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a,
 	__shared__ int s_count[B2_GRAPH_COLOR_COUNT], s_start[B2_GRAPH_COLOR_COUNT + 1], s_fill[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_restitution;
 	const int bin = blockIdx.x;
-	const int binCap = c.binCap;
-	const int bb = c.binRange[bin];
-	if ( bb == B2G_BIN_EMPTY ) return;
-	const int cb = c.binRange[binCap + bin], jbeg = c.binRange[2 * binCap + bin];
-	const int nb = c.binRange[3 * binCap + bin] - bb;
-	const int nc = c.binRange[4 * binCap + bin] - cb;
-	const int nj = c.binRange[5 * binCap + bin] - jbeg;
+	int bb, cb, jbeg, nb, nc, nj;
+	if ( c.identity )
+	{
+		bb = 0;
+		cb = 0;
+		jbeg = 0;
+		nb = a.awakeCount;
+		nc = a.colorOffsets[B2_GRAPH_COLOR_COUNT];
+		nj = c.jointOffsets.v[B2_GRAPH_COLOR_COUNT];
+	}
+	else
+	{
+		const int binCap = c.binCap;
+		bb = c.binRange[bin];
+		if ( bb == B2G_BIN_EMPTY ) return;
+		cb = c.binRange[binCap + bin];
+		jbeg = c.binRange[2 * binCap + bin];
+		nb = c.binRange[3 * binCap + bin] - bb;
+		nc = c.binRange[4 * binCap + bin] - cb;
+		nj = c.binRange[5 * binCap + bin] - jbeg;
+	}
 	long long bytes = (long long)B2G_BIN_BODY_BYTES * nb + (long long)B2G_BIN_CONTACT_BYTES * nc + (long long)B2G_BIN_JOINT_BYTES * nj;
 	if ( bytes > smemBytes )
 	{
@@ -282,7 +303,7 @@ __global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a,
 	if ( tid == 0 ) s_restitution = 0;
 	for ( int i = tid; i < nb; i += nt )
 	{
-		int ai = c.bodyList[bb + i];
+		int ai = D_BODY( bb + i );
 		sv[i] = a.sv[ai];
 		sd[i] = a.sd[ai];
 	}
@@ -291,22 +312,22 @@ __global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a,
 	/* prepare (contact_solver.c:1573-1809, joint.c:1593-1629) with bin-local body indices */
 	for ( int k = tid; k < nc; k += nt )
 	{
-		int slot = c.slotList[cb + k];
+		int slot = D_SLOT( cb + k );
 		b2gContactLane* L = lanes + k;
 		d_prepareContactLane( a, slot, overflowBegin, L );
-		L->indexA = L->indexA != 0 ? c.localIndex[L->indexA - 1] + 1 : 0;
-		L->indexB = L->indexB != 0 ? c.localIndex[L->indexB - 1] + 1 : 0;
+		L->indexA = L->indexA != 0 ? D_LOCAL( L->indexA - 1 ) + 1 : 0;
+		L->indexB = L->indexB != 0 ? D_LOCAL( L->indexB - 1 ) + 1 : 0;
 		if ( L->groupFlags & 2 ) s_restitution = 1;
 		atomicAdd( s_count + d_colorOf( a.colorOffsets, slot ), 1 );
 	}
 	for ( int k = tid; k < nj; k += nt )
 	{
-		int g = c.jointList[jbeg + k];
+		int g = D_JOINT( jbeg + k );
 		b2gJoint* J = joints + k;
 		*J = a.joints[g];
 		d_prepareJoint( J, &jb, P.h, P.inv_h, P.enableWarmStarting != 0 );
-		J->indexA = J->indexA >= 0 ? c.localIndex[J->indexA] : -1;
-		J->indexB = J->indexB >= 0 ? c.localIndex[J->indexB] : -1;
+		J->indexA = J->indexA >= 0 ? D_LOCAL( J->indexA ) : -1;
+		J->indexB = J->indexB >= 0 ? D_LOCAL( J->indexB ) : -1;
 		atomicAdd( s_count + d_colorOf( c.jointOffsets.v, g ), 1 );
 	}
 	__syncthreads();
@@ -323,13 +344,13 @@ __global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a,
 	}
 	__syncthreads();
 	/* color buckets: contact k as k, joint k as -(k + 1); order inside a color is free */
-	for ( int k = tid; k < nc; k += nt ) order[atomicAdd( s_fill + d_colorOf( a.colorOffsets, c.slotList[cb + k] ), 1 )] = k;
-	for ( int k = tid; k < nj; k += nt ) order[atomicAdd( s_fill + d_colorOf( c.jointOffsets.v, c.jointList[jbeg + k] ), 1 )] = -( k + 1 );
+	for ( int k = tid; k < nc; k += nt ) order[atomicAdd( s_fill + d_colorOf( a.colorOffsets, D_SLOT( cb + k ) ), 1 )] = k;
+	for ( int k = tid; k < nj; k += nt ) order[atomicAdd( s_fill + d_colorOf( c.jointOffsets.v, D_JOINT( jbeg + k ) ), 1 )] = -( k + 1 );
 	__syncthreads();
 
 	for ( int sub = 0; sub < P.subStepCount; ++sub )
 	{
-		for ( int i = tid; i < nb; i += nt ) d_integrateVelocitiesState( P, sv, i, a.params + 8 * c.bodyList[bb + i] );
+		for ( int i = tid; i < nb; i += nt ) d_integrateVelocitiesState( P, sv, i, a.params + 8 * D_BODY( bb + i ) );
 		__syncthreads();
 		for ( int stage = STAGE_WARM; stage <= STAGE_RELAX; ++stage )
 		{
@@ -371,17 +392,17 @@ __global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a,
 
 	/* store impulses (contact_solver.c:2238-2331), joint impulses and body state */
 	for ( int k = tid; k < nc; k += nt )
-		d_storeLane( lanes + k, &a.contacts[a.colorIds[c.slotList[cb + k]]].manifold, false );
+		d_storeLane( lanes + k, &a.contacts[a.colorIds[D_SLOT( cb + k )]].manifold, false );
 	for ( int k = tid; k < nj; k += nt )
 	{
 		b2gJoint* J = joints + k;
-		J->indexA = J->indexA >= 0 ? c.bodyList[bb + J->indexA] : -1;
-		J->indexB = J->indexB >= 0 ? c.bodyList[bb + J->indexB] : -1;
-		a.joints[c.jointList[jbeg + k]] = *J;
+		J->indexA = J->indexA >= 0 ? D_BODY( bb + J->indexA ) : -1;
+		J->indexB = J->indexB >= 0 ? D_BODY( bb + J->indexB ) : -1;
+		a.joints[D_JOINT( jbeg + k )] = *J;
 	}
 	for ( int i = tid; i < nb; i += nt )
 	{
-		int ai = c.bodyList[bb + i];
+		int ai = D_BODY( bb + i );
 		a.sv[ai] = sv[i];
 		a.sd[ai] = sd[i];
 	}
@@ -526,6 +547,7 @@ static d_compArgs compArgs( b2gCompBuffers* b, const int* jointOffsets, const in
 	c.summary = b->summary;
 	c.awakeIndex = awakeIndex;
 	memcpy( c.jointOffsets.v, jointOffsets, sizeof( c.jointOffsets.v ) );
+	c.identity = 0;
 	return c;
 }
 
@@ -578,17 +600,22 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 	return 0;
 }
 
+static cudaError_t s_binsConfigured = cudaSuccess;
+
+/* once per process: allow the bins kernel its dynamic shared memory */
+static void configureBins( void )
+{
+	s_binsConfigured = cudaFuncSetAttribute( k_solveBins, cudaFuncAttributeMaxDynamicSharedMemorySize, B2G_WORLD_BIN_MAX_BYTES );
+}
+
 extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets,
 									 const d_jointBodies* jb, b2gStepCounters* counters, cudaStream_t stream,
 									 long long* launches )
 {
-	static int s_configured = 0;
+	static pthread_once_t s_once = PTHREAD_ONCE_INIT;
 	const int smemBytes = 2 * B2G_BIN_CAP_BYTES;
-	if ( s_configured == 0 )
-	{
-		CKC( cudaFuncSetAttribute( k_solveBins, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes ) );
-		s_configured = 1;
-	}
+	pthread_once( &s_once, configureBins );
+	CKC( s_binsConfigured );
 	d_compArgs c = compArgs( b, jointOffsets, b->awakeIndex );
 	unsigned long long cur = b->hSummary->cursor;
 	long long bo = (long long)( cur >> ( B2G_CURSOR_CONTACT_BITS + B2G_CURSOR_JOINT_BITS ) );
@@ -658,5 +685,22 @@ extern "C" int b2gDev_CompSolveBig( b2gCompBuffers* b, const d_solveArgs* a, con
 		k_bigStore<<<compBlocks( total ), B2G_COMP_THREADS, 0, stream>>>( *a, b->summary, b->bigSlotList, total );
 		*launches += 1;
 	}
+	return (int)cudaGetLastError();
+}
+
+/* a whole world that fits one CTA's shared memory: one bin, no component analysis */
+extern "C" int b2gDev_SolveWorldBin( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
+									 const int* awakeIndex, int bytes, b2gStepCounters* counters, cudaStream_t stream,
+									 long long* launches )
+{
+	static pthread_once_t s_once = PTHREAD_ONCE_INIT;
+	pthread_once( &s_once, configureBins );
+	CKC( s_binsConfigured );
+	if ( bytes > B2G_WORLD_BIN_MAX_BYTES ) return (int)cudaErrorInvalidValue;
+	d_compArgs c = compArgs( b, jointOffsets, awakeIndex );
+	c.identity = 1;
+	int smem = bytes > 16 ? bytes : 16;
+	k_solveBins<<<1, B2G_BIN_THREADS, smem, stream>>>( *a, c, *jb, counters, smem );
+	*launches += 1;
 	return (int)cudaGetLastError();
 }

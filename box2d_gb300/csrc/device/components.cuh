@@ -25,6 +25,8 @@
 #define B2G_BIN_JOINT_BYTES ( (int)sizeof( b2gJoint ) + 4 )
 /* a component heavier than this is solved on the global path; a bin holds less than twice it */
 #define B2G_BIN_CAP_BYTES ( 40 * 1024 )
+/* a whole world up to this weight is solved by one CTA without component analysis */
+#define B2G_WORLD_BIN_MAX_BYTES ( 200 * 1024 )
 /* field widths of the packed (bodies, contacts, joints) allocation cursor */
 #define B2G_CURSOR_BODY_BITS 21
 #define B2G_CURSOR_CONTACT_BITS 22
@@ -86,3 +88,9 @@ extern "C" int b2gDev_CompSolveBig( b2gCompBuffers* b, const d_solveArgs* a, con
 extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
 									const int* activeColors, int activeColorCount, int useLists, int bodyCount,
 									cudaStream_t stream, long long* launches );
+
+/* one CTA solves the whole world (bytes = its shared-memory weight, at most
+   B2G_WORLD_BIN_MAX_BYTES); no analysis, no lists */
+extern "C" int b2gDev_SolveWorldBin( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
+									 const int* awakeIndex, int bytes, b2gStepCounters* counters, cudaStream_t stream,
+									 long long* launches );

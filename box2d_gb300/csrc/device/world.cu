@@ -119,6 +119,8 @@ struct b2gDeviceWorld
 	int changeWindow; /* state changes copied back with the counters */
 	int recWindow;	  /* enlarged-proxy records copied back with the counters */
 	int pairsTimingPending;
+	cudaEvent_t syncEvent; /* blocking-sync event for waits of batched steps */
+	int blockingSync;
 	/* upload arena (page-locked host + device) */
 	void* upHost;
 	void* upDev;
@@ -617,6 +619,7 @@ extern "C" int b2gDev_Create( b2gDeviceWorld** out )
 	   default stream) is then ordered before every kernel of this world */
 	CK( cudaStreamCreate( &dw->stream ) );
 	for ( int i = 0; i < 10; ++i ) CK( cudaEventCreate( dw->ev + i ) );
+	CK( cudaEventCreateWithFlags( &dw->syncEvent, cudaEventBlockingSync | cudaEventDisableTiming ) );
 	CK( cudaMalloc( &dw->counters, sizeof( b2gStepCounters ) ) );
 	CK( cudaMallocHost( &dw->hCounters, sizeof( b2gStepCounters ) ) );
 	for ( int t = 0; t < 3; ++t ) dw->treeRoot[t] = -1;
@@ -635,6 +638,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 {
 	if ( dw == NULL ) return;
 	cudaStreamSynchronize( dw->stream );
+	cudaEventDestroy( dw->syncEvent );
 	void* dptrs[] = { dw->xf,		  dw->center,	 dw->localCenter, dw->invMass,		dw->invI,		  dw->minExtent,
 					  dw->maxExtent,  dw->sleepThreshold, dw->safetyFactor, dw->awakeIndex, dw->bodyType,	dw->bodyFlags,
 					  dw->shapeStart, dw->shapeCount, dw->shapeList, dw->awakeBodyId,	dw->stateV,		  dw->stateD,
@@ -903,10 +907,22 @@ static int uploadStaged( b2gDeviceWorld* dw, const void* src, size_t bytes, void
 /* wait for the stream; afterwards the upload arena is free again */
 static int drain( b2gDeviceWorld* dw )
 {
-	CK( cudaStreamSynchronize( dw->stream ) );
+	if ( dw->blockingSync )
+	{
+		/* the waiting thread sleeps instead of spinning, so many stepping threads can share
+		   the host cores */
+		CK( cudaEventRecord( dw->syncEvent, dw->stream ) );
+		CK( cudaEventSynchronize( dw->syncEvent ) );
+	}
+	else
+	{
+		CK( cudaStreamSynchronize( dw->stream ) );
+	}
 	dw->upUsed = 0;
 	return 0;
 }
+
+extern "C" void b2gDev_SetBlockingSync( b2gDeviceWorld* dw, int on ) { dw->blockingSync = on; }
 
 extern "C" int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* inits, int count )
 {
@@ -994,16 +1010,25 @@ __global__ void k_convertTree( const b2gHostTreeNode* __restrict__ raw, b2gTreeN
 	out[i] = d;
 }
 
-extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gHostTreeNode* nodes, int nodeCount, int root )
+extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gHostTreeNode* nodes, int nodeCount, int root,
+								   int hostPinned )
 {
 	int need = nodeCount > 0 ? nodeCount : 1;
 	CK2( grow( (void**)&dw->tree[type], &dw->treeCap[type], need, sizeof( b2gTreeNode ) ) );
 	CK2( grow( (void**)&dw->treeRaw[type], &dw->treeRawCap[type], need, sizeof( b2gHostTreeNode ) ) );
 	if ( nodeCount > 0 )
 	{
-		dw->h2dBytes += (long long)( (size_t)nodeCount * sizeof( b2gHostTreeNode ) );
-		CK( cudaMemcpyAsync( dw->treeRaw[type], nodes, (size_t)nodeCount * sizeof( b2gHostTreeNode ), cudaMemcpyHostToDevice,
-							 dw->stream ) );
+		if ( hostPinned )
+		{
+			dw->h2dBytes += (long long)( (size_t)nodeCount * sizeof( b2gHostTreeNode ) );
+			CK( cudaMemcpyAsync( dw->treeRaw[type], nodes, (size_t)nodeCount * sizeof( b2gHostTreeNode ), cudaMemcpyHostToDevice,
+								 dw->stream ) );
+		}
+		else
+		{
+			/* small trees live in pageable memory: stage them through the upload arena */
+			CK2( uploadTo( dw, dw->treeRaw[type], nodes, (size_t)nodeCount * sizeof( b2gHostTreeNode ) ) );
+		}
 		k_convertTree<<<blocks( nodeCount ), B2G_THREADS, 0, dw->stream>>>( dw->treeRaw[type], dw->tree[type], nodeCount );
 		dw->launches += 1;
 		CK( cudaGetLastError() );
@@ -1067,7 +1092,7 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 	CK2( grow( (void**)&dw->pairOffsets, &dw->pairOffsetsCap, n, sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, n, sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hPairOffsets, &dw->hPairOffsetsCap, n, sizeof( int ) ) );
-	if ( dw->pairWindow < 4096 ) dw->pairWindow = 4096;
+	if ( dw->pairWindow < 64 ) dw->pairWindow = 64;
 	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
 															   dw->moved[b2_staticBody], dw->moveKeys, n, 1 );
 	dw->launches += 1;
@@ -1113,7 +1138,8 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 							 cudaMemcpyDeviceToHost, dw->stream ) );
 		CK2( drain( dw ) );
 	}
-	if ( 2 * total > dw->pairWindow ) dw->pairWindow = 2 * total;
+	/* next step's window follows this step's count, both ways */
+	dw->pairWindow = 2 * total > 64 ? 2 * total : 64;
 	/* pairs in move order for the host */
 	CK2( growHost( (void**)&dw->hPairs, &dw->hPairsCap, 2 * ( total > 0 ? total : 1 ), sizeof( int ) ) );
 	int o = 0;
@@ -1170,7 +1196,7 @@ extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int c
 		CK( cudaEventRecord( dw->ev[3], dw->stream ) );
 	}
 	/* the counters and the first `window` state changes come back in one wait */
-	if ( dw->changeWindow < 1024 ) dw->changeWindow = 1024;
+	if ( dw->changeWindow < 64 ) dw->changeWindow = 64;
 	int window = dw->changeWindow < contactIdCapacity ? dw->changeWindow : contactIdCapacity;
 	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( window > 0 ? window : 1 ), sizeof( int ) ) );
 	dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) + (size_t)window * 8 );
@@ -1200,7 +1226,7 @@ extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int c
 							 cudaMemcpyDeviceToHost, dw->stream ) );
 		CK2( drain( dw ) );
 	}
-	if ( 2 * n > dw->changeWindow ) dw->changeWindow = 2 * n;
+	dw->changeWindow = 2 * n > 64 ? 2 * n : 64;
 	if ( n > 1 ) qsort( dw->hChanges, (size_t)n, 2 * sizeof( int ), cmpChange );
 	*outChanges = dw->hChanges;
 	*outChangeCount = n;
@@ -1285,7 +1311,17 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	d_jointBodies jb0 = { dw->xf, dw->center, dw->localCenter, dw->invMass, dw->invI, dw->awakeIndex };
 	CK( cudaEventRecord( dw->ev[6], dw->stream ) );
 	bool solved = false;
-	if ( dw->solverMode == B2G_SOLVER_COMPONENTS && dw->compSkip > 0 )
+	long long worldBytes = (long long)B2G_BIN_BODY_BYTES * awakeCount + (long long)B2G_BIN_CONTACT_BYTES * total +
+						   (long long)B2G_BIN_JOINT_BYTES * jointTotal;
+	if ( dw->solverMode == B2G_SOLVER_COMPONENTS && ovJointCount0 + ovCount0 == 0 && worldBytes <= B2G_WORLD_BIN_MAX_BYTES )
+	{
+		/* small world: one CTA solves all of it from shared memory */
+		CK2( b2gDev_SolveWorldBin( &dw->comp, &a, dw->jointOffsets, &jb0, dw->awakeIndex, (int)worldBytes, dw->counters,
+								   dw->stream, &dw->launches ) );
+		dw->compValid = 0;
+		solved = true;
+	}
+	else if ( dw->solverMode == B2G_SOLVER_COMPONENTS && dw->compSkip > 0 )
 	{
 		dw->compSkip -= 1;
 		dw->compValid = 0;
@@ -1445,7 +1481,7 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 		CK( cudaEventRecord( dw->ev[8], dw->stream ) );
 	}
 	/* the counters and the first `window` enlarged-proxy records come back in one wait */
-	if ( dw->recWindow < 1024 ) dw->recWindow = 1024;
+	if ( dw->recWindow < 64 ) dw->recWindow = 64;
 	int recWindow = dw->recWindow < shapeTotal ? dw->recWindow : shapeTotal;
 	CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( float ) ) );
@@ -1492,7 +1528,7 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 							 cudaMemcpyDeviceToHost, dw->stream ) );
 		CK2( drain( dw ) );
 	}
-	if ( 2 * n > dw->recWindow ) dw->recWindow = 2 * n;
+	dw->recWindow = 2 * n > 64 ? 2 * n : 64;
 	if ( n > 0 )
 	{
 		const int* recs = dw->hRecsRaw;

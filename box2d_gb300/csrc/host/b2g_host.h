@@ -25,7 +25,7 @@
 #define H_TIME_TH_SLEEP 0.5f
 #define H_OVERFLOW_INDEX ( B2_GRAPH_COLOR_COUNT - 1 )
 #define H_DYNAMIC_COLOR_COUNT ( B2_GRAPH_COLOR_COUNT - 4 )
-#define H_MAX_WORLDS 128
+#define H_MAX_WORLDS 4096
 #define H_SIMD_WIDTH 4
 
 /* ---------------- scalar math, same operation order as math_functions.h ---------------- */

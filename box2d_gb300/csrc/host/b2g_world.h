@@ -12,7 +12,7 @@
 #include "../b2g_device_abi.h"
 #include "b2g_host.h"
 
-#define H_MAX_WORLDS 128
+#define H_MAX_WORLDS 4096
 
 enum
 {

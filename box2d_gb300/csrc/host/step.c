@@ -134,7 +134,7 @@ static void h_uploadTree( h_world* w, int type )
 	h_tree* t = w->trees + type;
 	if ( w->uploadedTreeVersion[type] == t->version && w->uploadedTreeNodes[type] == t->nodes ) return;
 	int rc = b2gDev_UploadTree( w->dev, type, (const b2gHostTreeNode*)t->nodes, t->nodeCapacity,
-								t->nodeCount == 0 ? -1 : t->root );
+								t->nodeCount == 0 ? -1 : t->root, t->pinned );
 	if ( rc != 0 ) h_fail( w, "tree upload", rc );
 	w->uploadedTreeVersion[type] = t->version;
 	w->uploadedTreeNodes[type] = t->nodes;

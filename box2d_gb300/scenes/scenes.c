@@ -742,6 +742,24 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 	return h;
 }
 
+/* step `count` scenes `steps` times each with one batched call per step where the library
+   has one (b2World_StepBatch), else one world after the other */
+B2S_EXPORT void b2s_step_batch( const int* handles, int count, float timeStep, int subStepCount, int steps, int threads )
+{
+	b2WorldId* ids = malloc( (size_t)( count > 0 ? count : 1 ) * sizeof( b2WorldId ) );
+	for ( int i = 0; i < count; ++i ) ids[i] = b2s_scenes[handles[i]].worldId;
+	for ( int k = 0; k < steps; ++k )
+	{
+#ifdef B2S_BATCH_API
+		b2World_StepBatch( ids, count, timeStep, subStepCount, threads );
+#else
+		(void)threads;
+		for ( int i = 0; i < count; ++i ) b2World_Step( ids[i], timeStep, subStepCount );
+#endif
+	}
+	free( ids );
+}
+
 B2S_EXPORT void b2s_destroy( int h )
 {
 	b2sScene* s = b2s_scenes + h;

@@ -58,6 +58,9 @@ void* b2p_stream( uint32_t packedWorldId );
 int b2s_create( int kind, int a, int b, int c, uint32_t seed, int flags );
 void b2s_destroy( int handle );
 void b2s_step( int handle, float timeStep, int subStepCount, int count );
+/* step `count` scenes `steps` times, one b2World_StepBatch call (up to `threads` host
+   threads) per step on the GB300 library, one world after the other elsewhere */
+void b2s_step_batch( const int* handles, int count, float timeStep, int subStepCount, int steps, int threads );
 int b2s_body_count( int handle );
 int b2s_dynamic_count( int handle );
 uint32_t b2s_world_id( int handle );

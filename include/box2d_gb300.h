@@ -554,6 +554,11 @@ B2G_API b2WorldId b2CreateWorld( const b2WorldDef* def );
 B2G_API void b2DestroyWorld( b2WorldId worldId );
 B2G_API bool b2World_IsValid( b2WorldId id );
 B2G_API void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount );
+/* Step many independent worlds with the same time step and substeps, using up to
+   threadCount host threads (no counterpart in the reference API). Each world ends exactly
+   as a b2World_Step call on it would leave it. The worlds must be distinct; no other call
+   may use them while the batch runs. */
+B2G_API void b2World_StepBatch( const b2WorldId* worldIds, int worldCount, float timeStep, int subStepCount, int threadCount );
 B2G_API b2BodyEvents b2World_GetBodyEvents( b2WorldId worldId );
 B2G_API b2ContactEvents b2World_GetContactEvents( b2WorldId worldId );
 B2G_API void b2World_EnableSleeping( b2WorldId worldId, bool flag );
