@@ -13,5 +13,5 @@ void o_solveContinuous( o_world* w, int simIndex )
 	o_bodySim* sim = w->awakeSims.data + simIndex;
 	sim->center0 = sim->center;
 	sim->rotation0 = sim->transform.q;
-	o_continuousSkipped += 1;
+	__atomic_fetch_add( &o_continuousSkipped, 1, __ATOMIC_RELAXED );
 }

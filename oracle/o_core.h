@@ -274,6 +274,11 @@ static inline void o_bitGrow( o_bitSet* s, int bit )
 	}
 }
 static inline void o_bitSet1( o_bitSet* s, int bit ) { o_bitGrow( s, bit ); s->bits[bit / 64] |= ( 1ull << ( bit % 64 ) ); }
+/* for parallel loops: the set must already hold `bit` */
+static inline void o_bitSet1Atomic( o_bitSet* s, int bit )
+{
+	__atomic_fetch_or( s->bits + bit / 64, 1ull << ( bit % 64 ), __ATOMIC_RELAXED );
+}
 static inline void o_bitClear( o_bitSet* s, int bit )
 {
 	if ( bit / 64 < s->blockCount ) s->bits[bit / 64] &= ~( 1ull << ( bit % 64 ) );
@@ -686,6 +691,12 @@ void o_solve( o_world* w, o_stepContext* ctx );
 void o_updateBroadPhasePairs( o_world* w );
 void o_collide( o_world* w, o_stepContext* ctx );
 void o_bufferMove( o_world* w, int proxyKey );
+
+/* fork-join loops (o_parallel.c): fcn( ctx, begin, end ) over [0, count), inline when the
+   pool has one thread or count < minParallel */
+typedef void o_rangeFcn( void* ctx, int begin, int end );
+void o_parallelFor( int count, int minParallel, o_rangeFcn* fcn, void* ctx );
+void o_setThreads( int n );
 
 /* joints */
 void o_prepareJoints( o_world* w, o_stepContext* ctx, o_jointSim* joints, int count );

@@ -74,3 +74,6 @@ extern int o_continuousSkipped;
 
 /* number of fast-body continuous steps the oracle could not restate (0 when exact) */
 B2P_EXPORT int b2p_oracle_unsupported( void ) { return o_continuousSkipped; }
+
+/* threads of the oracle's data-parallel loops (1 = serial, the default) */
+B2P_EXPORT void b2o_set_threads( int n ) { o_setThreads( n ); }

@@ -642,11 +642,27 @@ static void o_storeOverflow( o_world* w, o_overflowConstraint* cons )
 }
 
 /* ---------------- body integration (solver.c:66-162) ---------------- */
-static void o_integrateVelocities( o_world* w, o_stepContext* ctx )
+typedef struct o_loopCtx
 {
+	o_world* w;
+	o_stepContext* ctx;
+	o_graphColor* color;
+	o_contactLane* lanes;
+	int* groupRestitution;
+	int jointCount;
+	int stage; /* 0 warm start, 1 solve, 2 relax */
+	const int* prefix;
+} o_loopCtx;
+
+#define O_MIN_PARALLEL 256
+
+static void o_integrateVelocitiesRange( void* p, int begin, int end )
+{
+	o_world* w = ( (o_loopCtx*)p )->w;
+	o_stepContext* ctx = ( (o_loopCtx*)p )->ctx;
 	b2Vec2 gravity = w->gravity;
 	float h = ctx->h;
-	for ( int i = 0; i < w->awakeSims.count; ++i )
+	for ( int i = begin; i < end; ++i )
 	{
 		o_bodySim* sim = w->awakeSims.data + i;
 		o_bodyState* st = w->awakeStates.data + i;
@@ -664,14 +680,22 @@ static void o_integrateVelocities( o_world* w, o_stepContext* ctx )
 	}
 }
 
-static void o_integratePositions( o_world* w, o_stepContext* ctx )
+static void o_integrateVelocities( o_world* w, o_stepContext* ctx )
 {
+	o_loopCtx c = { w, ctx, NULL, NULL, NULL, 0, 0, NULL };
+	o_parallelFor( w->awakeSims.count, O_MIN_PARALLEL, o_integrateVelocitiesRange, &c );
+}
+
+static void o_integratePositionsRange( void* p, int begin, int end )
+{
+	o_world* w = ( (o_loopCtx*)p )->w;
+	o_stepContext* ctx = ( (o_loopCtx*)p )->ctx;
 	float h = ctx->h;
 	float maxLinearSpeed = ctx->maxLinearVelocity;
 	float maxAngularSpeed = O_MAX_ROTATION * ctx->inv_dt;
 	float maxLinearSq = maxLinearSpeed * maxLinearSpeed;
 	float maxAngularSq = maxAngularSpeed * maxAngularSpeed;
-	for ( int i = 0; i < w->awakeStates.count; ++i )
+	for ( int i = begin; i < end; ++i )
 	{
 		o_bodyState* st = w->awakeStates.data + i;
 		b2Vec2 v = st->linearVelocity;
@@ -698,15 +722,21 @@ static void o_integratePositions( o_world* w, o_stepContext* ctx )
 	}
 }
 
+static void o_integratePositions( o_world* w, o_stepContext* ctx )
+{
+	o_loopCtx c = { w, ctx, NULL, NULL, NULL, 0, 0, NULL };
+	o_parallelFor( w->awakeStates.count, O_MIN_PARALLEL, o_integratePositionsRange, &c );
+}
+
 /* ---------------- finalize bodies (solver.c:553-743) ---------------- */
 void o_solveContinuous( o_world* w, int simIndex );
 
-static void o_finalizeBodies( o_world* w, o_stepContext* ctx )
+static void o_finalizeRange( void* p, int begin, int end )
 {
+	o_world* w = ( (o_loopCtx*)p )->w;
+	o_stepContext* ctx = ( (o_loopCtx*)p )->ctx;
 	float timeStep = ctx->dt, invTimeStep = ctx->inv_dt;
-	int n = w->awakeSims.count;
-	o_bitReset( &w->enlargedSimBits, n );
-	for ( int simIndex = 0; simIndex < n; ++simIndex )
+	for ( int simIndex = begin; simIndex < end; ++simIndex )
 	{
 		o_bodyState* st = w->awakeStates.data + simIndex;
 		o_bodySim* sim = w->awakeSims.data + simIndex;
@@ -775,7 +805,7 @@ static void o_finalizeBodies( o_world* w, o_stepContext* ctx )
 			o_shape* shape = w->shapes.data + shapeId;
 			if ( isFast )
 			{
-				o_bitSet1( &w->enlargedSimBits, simIndex );
+				o_bitSet1Atomic( &w->enlargedSimBits, simIndex );
 			}
 			else
 			{
@@ -788,12 +818,65 @@ static void o_finalizeBodies( o_world* w, o_stepContext* ctx )
 								   { aabb.upperBound.x + margin, aabb.upperBound.y + margin } };
 					shape->fatAABB = fat;
 					shape->enlargedAABB = 1;
-					o_bitSet1( &w->enlargedSimBits, simIndex );
+					o_bitSet1Atomic( &w->enlargedSimBits, simIndex );
 				}
 			}
 			shapeId = shape->nextShapeId;
 		}
 	}
+}
+
+static void o_finalizeBodies( o_world* w, o_stepContext* ctx )
+{
+	int n = w->awakeSims.count;
+	o_bitReset( &w->enlargedSimBits, n );
+	o_loopCtx c = { w, ctx, NULL, NULL, NULL, 0, 0, NULL };
+	o_parallelFor( n, O_MIN_PARALLEL, o_finalizeRange, &c );
+}
+
+/* per-color loops of the solver stages (one item = one joint or one contact lane) */
+static void o_prepareJointRange( void* p, int begin, int end )
+{
+	o_loopCtx* c = p;
+	for ( int j = begin; j < end; ++j ) o_prepareJoint( c->w, c->ctx, c->color->jointSims.data + j );
+}
+
+static void o_prepareLaneRange( void* p, int begin, int end )
+{
+	o_loopCtx* c = p;
+	for ( int k = begin; k < end; ++k ) o_prepareLane( c->w, c->ctx, c->color->contactSims.data + k, c->lanes + k );
+}
+
+static void o_colorStageRange( void* p, int begin, int end )
+{
+	o_loopCtx* c = p;
+	for ( int i = begin; i < end; ++i )
+	{
+		if ( i < c->jointCount )
+		{
+			o_jointSim* j = c->color->jointSims.data + i;
+			if ( c->stage == 0 ) o_warmStartJoint( c->w, c->ctx, j );
+			else o_solveJoint( c->w, c->ctx, j, c->stage == 1 );
+		}
+		else
+		{
+			o_contactLane* lane = c->lanes + ( i - c->jointCount );
+			if ( c->stage == 0 ) o_warmStartLane( c->w, lane );
+			else o_solveLane( c->w, c->ctx, lane, c->stage == 1 );
+		}
+	}
+}
+
+static void o_restitutionRange( void* p, int begin, int end )
+{
+	o_loopCtx* c = p;
+	for ( int k = begin; k < end; ++k ) o_restitutionLane( c->w, c->lanes + k, c->groupRestitution[k / O_SIMD_WIDTH] );
+}
+
+static void o_storeRange( void* p, int begin, int end )
+{
+	o_loopCtx* c = p;
+	for ( int k = begin; k < end; ++k ) o_storeLane( c->color->contactSims.data + k, c->lanes + k );
 }
 
 /* ---------------- b2Solve (solver.c:1275-2081) ---------------- */
@@ -833,13 +916,15 @@ void o_solve( o_world* w, o_stepContext* ctx )
 	for ( int a = 0; a < activeColorCount; ++a )
 	{
 		o_graphColor* color = w->colors + activeColors[a];
-		for ( int j = 0; j < color->jointSims.count; ++j ) o_prepareJoint( w, ctx, color->jointSims.data + j );
+		o_loopCtx c = { w, ctx, color, lanes[a], groupRestitution[a], 0, 0, NULL };
+		o_parallelFor( color->jointSims.count, O_MIN_PARALLEL, o_prepareJointRange, &c );
 	}
 	for ( int a = 0; a < activeColorCount; ++a )
 	{
 		o_graphColor* color = w->colors + activeColors[a];
 		int n = laneCounts[a];
-		for ( int k = 0; k < n; ++k ) o_prepareLane( w, ctx, color->contactSims.data + k, lanes[a] + k );
+		o_loopCtx c = { w, ctx, color, lanes[a], groupRestitution[a], 0, 0, NULL };
+		o_parallelFor( n, O_MIN_PARALLEL, o_prepareLaneRange, &c );
 		for ( int g = 0; g * O_SIMD_WIDTH < n; ++g )
 		{
 			int anyRolling = 0, anyRestitution = 0;
@@ -866,16 +951,16 @@ void o_solve( o_world* w, o_stepContext* ctx )
 		for ( int a = 0; a < activeColorCount; ++a )
 		{
 			o_graphColor* color = w->colors + activeColors[a];
-			for ( int j = 0; j < color->jointSims.count; ++j ) o_warmStartJoint( w, ctx, color->jointSims.data + j );
-			for ( int k = 0; k < laneCounts[a]; ++k ) o_warmStartLane( w, lanes[a] + k );
+			o_loopCtx c = { w, ctx, color, lanes[a], groupRestitution[a], color->jointSims.count, 0, NULL };
+			o_parallelFor( color->jointSims.count + laneCounts[a], O_MIN_PARALLEL, o_colorStageRange, &c );
 		}
 		for ( int j = 0; j < overflow->jointSims.count; ++j ) o_solveJoint( w, ctx, overflow->jointSims.data + j, 1 );
 		o_solveOverflow( w, ctx, ocons, overflowCount, 1 );
 		for ( int a = 0; a < activeColorCount; ++a )
 		{
 			o_graphColor* color = w->colors + activeColors[a];
-			for ( int j = 0; j < color->jointSims.count; ++j ) o_solveJoint( w, ctx, color->jointSims.data + j, 1 );
-			for ( int k = 0; k < laneCounts[a]; ++k ) o_solveLane( w, ctx, lanes[a] + k, 1 );
+			o_loopCtx c = { w, ctx, color, lanes[a], groupRestitution[a], color->jointSims.count, 1, NULL };
+			o_parallelFor( color->jointSims.count + laneCounts[a], O_MIN_PARALLEL, o_colorStageRange, &c );
 		}
 		o_integratePositions( w, ctx );
 		for ( int j = 0; j < overflow->jointSims.count; ++j ) o_solveJoint( w, ctx, overflow->jointSims.data + j, 0 );
@@ -883,21 +968,23 @@ void o_solve( o_world* w, o_stepContext* ctx )
 		for ( int a = 0; a < activeColorCount; ++a )
 		{
 			o_graphColor* color = w->colors + activeColors[a];
-			for ( int j = 0; j < color->jointSims.count; ++j ) o_solveJoint( w, ctx, color->jointSims.data + j, 0 );
-			for ( int k = 0; k < laneCounts[a]; ++k ) o_solveLane( w, ctx, lanes[a] + k, 0 );
+			o_loopCtx c = { w, ctx, color, lanes[a], groupRestitution[a], color->jointSims.count, 2, NULL };
+			o_parallelFor( color->jointSims.count + laneCounts[a], O_MIN_PARALLEL, o_colorStageRange, &c );
 		}
 	}
 
 	o_restitutionOverflow( w, ocons, overflowCount );
 	for ( int a = 0; a < activeColorCount; ++a )
 	{
-		for ( int k = 0; k < laneCounts[a]; ++k ) o_restitutionLane( w, lanes[a] + k, groupRestitution[a][k / O_SIMD_WIDTH] );
+		o_loopCtx c = { w, ctx, w->colors + activeColors[a], lanes[a], groupRestitution[a], 0, 0, NULL };
+		o_parallelFor( laneCounts[a], O_MIN_PARALLEL, o_restitutionRange, &c );
 	}
 	o_storeOverflow( w, ocons );
 	for ( int a = 0; a < activeColorCount; ++a )
 	{
 		o_graphColor* color = w->colors + activeColors[a];
-		for ( int k = 0; k < laneCounts[a]; ++k ) o_storeLane( color->contactSims.data + k, lanes[a] + k );
+		o_loopCtx c = { w, ctx, color, lanes[a], groupRestitution[a], 0, 0, NULL };
+		o_parallelFor( laneCounts[a], O_MIN_PARALLEL, o_storeRange, &c );
 		free( lanes[a] );
 		free( groupRestitution[a] );
 	}
@@ -1026,7 +1113,7 @@ static void o_collideContact( o_world* w, o_contactSim* cs )
 	{
 		cs->simFlags |= O_S_DISJOINT;
 		cs->simFlags &= ~O_S_TOUCHING;
-		o_bitSet1( &w->contactStateBits, contactId );
+		o_bitSet1Atomic( &w->contactStateBits, contactId );
 		return;
 	}
 	int wasTouching = ( cs->simFlags & O_S_TOUCHING ) != 0;
@@ -1071,7 +1158,7 @@ static void o_collideContact( o_world* w, o_contactSim* cs )
 				mp->separation = mp->baseSeparation + o_dot( dp, normal );
 				mp->persisted = true;
 			}
-			w->recycledContactCount += 1;
+			__atomic_fetch_add( &w->recycledContactCount, 1, __ATOMIC_RELAXED );
 			return;
 		}
 	}
@@ -1085,14 +1172,28 @@ static void o_collideContact( o_world* w, o_contactSim* cs )
 	if ( touching && wasTouching == 0 )
 	{
 		cs->simFlags |= O_S_STARTED;
-		o_bitSet1( &w->contactStateBits, contactId );
+		o_bitSet1Atomic( &w->contactStateBits, contactId );
 	}
 	else if ( touching == 0 && wasTouching )
 	{
 		cs->simFlags |= O_S_STOPPED;
-		o_bitSet1( &w->contactStateBits, contactId );
+		o_bitSet1Atomic( &w->contactStateBits, contactId );
 	}
 	for ( int i = 0; i < cs->manifold.pointCount; ++i ) cs->manifold.points[i].baseSeparation = cs->manifold.points[i].separation;
+}
+
+static void o_collideRange( void* p, int begin, int end )
+{
+	o_loopCtx* c = p;
+	o_world* w = c->w;
+	int array = 0;
+	for ( int i = begin; i < end; ++i )
+	{
+		while ( c->prefix[array + 1] <= i ) array += 1;
+		int j = i - c->prefix[array];
+		o_contactSim* cs = array < B2_GRAPH_COLOR_COUNT ? w->colors[array].contactSims.data + j : w->awakeContactSims.data + j;
+		o_collideContact( w, cs );
+	}
 }
 
 void o_collide( o_world* w, o_stepContext* ctx )
@@ -1104,12 +1205,13 @@ void o_collide( o_world* w, o_stepContext* ctx )
 	if ( contactCount == 0 ) return;
 	o_bitReset( &w->contactStateBits, w->contactIdPool.nextIndex );
 	w->recycledContactCount = 0;
-	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
-	{
-		o_graphColor* color = w->colors + i;
-		for ( int j = 0; j < color->contactSims.count; ++j ) o_collideContact( w, color->contactSims.data + j );
-	}
-	for ( int j = 0; j < w->awakeContactSims.count; ++j ) o_collideContact( w, w->awakeContactSims.data + j );
+	/* every color's contacts, then the non-touching ones, as one index space */
+	int prefix[B2_GRAPH_COLOR_COUNT + 2];
+	prefix[0] = 0;
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i ) prefix[i + 1] = prefix[i] + w->colors[i].contactSims.count;
+	prefix[B2_GRAPH_COLOR_COUNT + 1] = prefix[B2_GRAPH_COLOR_COUNT] + w->awakeContactSims.count;
+	o_loopCtx c = { w, ctx, NULL, NULL, NULL, 0, 0, prefix };
+	o_parallelFor( prefix[B2_GRAPH_COLOR_COUNT + 1], O_MIN_PARALLEL, o_collideRange, &c );
 
 	int endEventArrayIndex = w->endEventArrayIndex;
 	for ( int k = 0; k < w->contactStateBits.blockCount; ++k )

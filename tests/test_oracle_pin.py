@@ -24,3 +24,20 @@ def test_oracle_matches_reference_fixture(oracle, name):
                 assert table.shape[0] == d["count"], f"{name}: contact count at step {k}"
                 assert hashlib.sha256(table.astype("<i4").tobytes()).hexdigest() == d["sha256"], \
                     f"{name}: contact table (ids, pairs, colors, feature ids) at step {k}"
+
+
+@pytest.mark.parametrize("name", ["large_pyramid_20", "joint_zoo_4", "many_pyramids_rain_3x3"])
+def test_oracle_threads_do_not_change_results(oracle, name):
+    """The oracle's parallel loops compute every item exactly as the serial loop does."""
+    import ctypes
+
+    g = load_golden(name)
+    oracle.b2o_set_threads.argtypes = [ctypes.c_int]
+    oracle.b2o_set_threads(4)
+    try:
+        with B.Scene(oracle, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
+            for k, expected in enumerate(g["state_hashes"][:120], start=1):
+                s.step(1, g["dt"], g["substeps"])
+                assert f"{s.state_hash():016x}" == expected, f"{name}: step {k}"
+    finally:
+        oracle.b2o_set_threads(1)
