@@ -4,12 +4,14 @@
  * substep's integrate velocities / warm start / solve / integrate positions / relax per
  * color, restitution, store -- in one launch. Each color's constraints are split evenly
  * over the CTAs; a CTA keeps its contact constraints in its own shared memory for the whole
- * step; body state stays in global memory (L2). Colors are separated by the hardware
- * cluster barrier, whose release/acquire semantics order the global body-state writes of
- * one color before the reads of the next.
+ * step. The body state lives in the cluster's distributed shared memory: body position p
+ * (its index in the solved body list) sits in CTA p % ranks, slot p / ranks, and every
+ * constraint reads and writes it there through the cluster's shared-memory window. Colors
+ * are separated by the hardware cluster barrier, whose release/acquire semantics order the
+ * body-state writes of one color before the reads of the next. Joints stay in global
+ * memory; each joint is always processed by the same thread.
  *
- * This file is compiled with -Xptxas -dlcm=cg: global loads bypass L1, so body state
- * written by one SM is read from L2 by the others after a barrier.
+ * This file is compiled with -Xptxas -dlcm=cg: global loads bypass L1.
  *
  * Used when the component path leaves constraints in components too big for a bin, no
  * overflow color exists and the constraints fit the cluster's shared memory; the results
@@ -35,8 +37,27 @@ struct d_clusterPlan
 	const int* slotList;
 	const int* jointList;
 	const int* bodyList; /* NULL: all awake bodies */
+	const int* positionOf; /* awake index -> position in bodyList (lists only) */
 	const b2gCompSummary* summary;
 	int bodyCount;
+	int rankShift; /* ranks = 1 << rankShift */
+	int slotsPerRank;
+};
+
+/* body state in distributed shared memory: position p -> CTA p & mask, slot p >> shift */
+struct d_clusterBodies
+{
+	float4* sv;
+	float4* sd;
+	int shift, mask;
+	__device__ __forceinline__ float4& v( int i ) const
+	{
+		return *cg::this_cluster().map_shared_rank( sv + ( i >> shift ), (unsigned)( i & mask ) );
+	}
+	__device__ __forceinline__ float4& d( int i ) const
+	{
+		return *cg::this_cluster().map_shared_rank( sd + ( i >> shift ), (unsigned)( i & mask ) );
+	}
 };
 
 static __device__ __forceinline__ int d_planContactCount( const d_solveArgs& a, const d_clusterPlan& plan, int color )
@@ -53,15 +74,21 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 {
 	cg::cluster_group cluster = cg::this_cluster();
 	const int rank = (int)cluster.block_rank();
-	const int ranks = (int)cluster.num_blocks();
+	const int ranks = 1 << plan.rankShift;
+	const int mask = ranks - 1;
 	extern __shared__ float4 s_mem[];
-	b2gContactLane* lanes = (b2gContactLane*)s_mem;
+	float4* sv = s_mem;
+	float4* sd = sv + plan.slotsPerRank;
+	b2gContactLane* lanes = (b2gContactLane*)( sd + plan.slotsPerRank );
 	__shared__ int s_cBegin[B2_GRAPH_COLOR_COUNT], s_cCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_jBegin[B2_GRAPH_COLOR_COUNT], s_jCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_laneOffset[B2_GRAPH_COLOR_COUNT];
 	const int tid = threadIdx.x, nt = blockDim.x;
 	const b2gStepParams& P = a.p;
 	const int overflowBegin = a.colorOffsets[B2G_OVERFLOW_INDEX];
+	d_clusterBodies bodies = { sv, sd, plan.rankShift, mask };
+	/* this CTA's bodies: positions rank, rank + ranks, ... */
+	const int localCount = plan.bodyCount > rank ? ( plan.bodyCount - rank + ranks - 1 ) >> plan.rankShift : 0;
 
 	/* this CTA's share of every color */
 	if ( tid == 0 )
@@ -81,37 +108,59 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 			offset += ce - cb;
 		}
 	}
+	for ( int s = tid; s < localCount; s += nt )
+	{
+		int p = ( s << plan.rankShift ) + rank;
+		int ai = plan.bodyList ? plan.bodyList[p] : p;
+		sv[s] = a.sv[ai];
+		sd[s] = a.sd[ai];
+	}
 	__syncthreads();
 
-	/* prepare: joints in place (global), contacts into this CTA's shared memory */
+	/* prepare: joints in place (global), contacts into this CTA's shared memory; body
+	   references become positions */
 	for ( int k = 0; k < plan.colorCount; ++k )
 	{
 		int color = plan.colors[k];
 		for ( int t = tid; t < s_jCount[k]; t += nt )
 		{
 			int idx = plan.jointOffsets[color] + s_jBegin[k] + t;
-			d_prepareJointItem( a, jb, plan.useLists ? plan.jointList[idx] : idx );
+			b2gJoint* J = a.joints + ( plan.useLists ? plan.jointList[idx] : idx );
+			d_prepareJoint( J, &jb, P.h, P.inv_h, P.enableWarmStarting != 0 );
+			if ( plan.positionOf )
+			{
+				J->indexA = J->indexA >= 0 ? plan.positionOf[J->indexA] : -1;
+				J->indexB = J->indexB >= 0 ? plan.positionOf[J->indexB] : -1;
+			}
 		}
 		for ( int t = tid; t < s_cCount[k]; t += nt )
 		{
 			int idx = a.colorOffsets[color] + s_cBegin[k] + t;
-			d_prepareContactLane( a, plan.useLists ? plan.slotList[idx] : idx, overflowBegin, lanes + s_laneOffset[k] + t );
+			b2gContactLane* L = lanes + s_laneOffset[k] + t;
+			d_prepareContactLane( a, plan.useLists ? plan.slotList[idx] : idx, overflowBegin, L );
+			if ( plan.positionOf )
+			{
+				L->indexA = L->indexA != 0 ? plan.positionOf[L->indexA - 1] + 1 : 0;
+				L->indexB = L->indexB != 0 ? plan.positionOf[L->indexB - 1] + 1 : 0;
+			}
 		}
 	}
 	cluster.sync();
 
-	const int gtid = rank * nt + tid, gstride = ranks * nt;
 	for ( int sub = 0; sub < P.subStepCount; ++sub )
 	{
-		for ( int i = gtid; i < plan.bodyCount; i += gstride )
-			d_integrateVelocitiesItem( a, plan.bodyList ? plan.bodyList[i] : i );
+		for ( int s = tid; s < localCount; s += nt )
+		{
+			int p = ( s << plan.rankShift ) + rank;
+			int ai = plan.bodyList ? plan.bodyList[p] : p;
+			d_integrateVelocitiesState( P, sv, s, a.params + 8 * ai );
+		}
 		cluster.sync();
 		for ( int stage = STAGE_WARM; stage <= STAGE_RELAX; ++stage )
 		{
 			if ( stage == STAGE_RELAX )
 			{
-				for ( int i = gtid; i < plan.bodyCount; i += gstride )
-					d_integratePositionsItem( a, plan.bodyList ? plan.bodyList[i] : i );
+				for ( int s = tid; s < localCount; s += nt ) d_integratePositionsState( P, sv, sd, s );
 				cluster.sync();
 			}
 			for ( int k = 0; k < plan.colorCount; ++k )
@@ -123,11 +172,11 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 					if ( t < nj )
 					{
 						int idx = plan.jointOffsets[color] + s_jBegin[k] + t;
-						d_jointStage( P, a.joints + ( plan.useLists ? plan.jointList[idx] : idx ), a.sv, a.sd, stage );
+						d_jointStageT( P, a.joints + ( plan.useLists ? plan.jointList[idx] : idx ), bodies, stage );
 					}
 					else
 					{
-						d_laneStage( P, lanes + s_laneOffset[k] + ( t - nj ), a.sv, a.sd, stage );
+						d_laneStageT( P, lanes + s_laneOffset[k] + ( t - nj ), bodies, stage );
 					}
 				}
 				cluster.sync();
@@ -137,11 +186,12 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 	for ( int k = 0; k < plan.colorCount; ++k )
 	{
 		for ( int t = tid; t < s_cCount[k]; t += nt )
-			d_laneStage( P, lanes + s_laneOffset[k] + t, a.sv, a.sd, STAGE_RESTITUTION );
+			d_laneStageT( P, lanes + s_laneOffset[k] + t, bodies, STAGE_RESTITUTION );
 		cluster.sync();
 	}
 
-	/* store impulses (contact_solver.c:2238-2331) */
+	/* store impulses (contact_solver.c:2238-2331), restore joint body indices, write the
+	   bodies back; no CTA touches another's shared memory after the last barrier */
 	for ( int k = 0; k < plan.colorCount; ++k )
 	{
 		int color = plan.colors[k];
@@ -151,6 +201,23 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 			int slot = plan.useLists ? plan.slotList[idx] : idx;
 			d_storeLane( lanes + s_laneOffset[k] + t, &a.contacts[a.colorIds[slot]].manifold, false );
 		}
+		if ( plan.positionOf )
+		{
+			for ( int t = tid; t < s_jCount[k]; t += nt )
+			{
+				int idx = plan.jointOffsets[color] + s_jBegin[k] + t;
+				b2gJoint* J = a.joints + plan.jointList[idx];
+				J->indexA = J->indexA >= 0 ? plan.bodyList[J->indexA] : -1;
+				J->indexB = J->indexB >= 0 ? plan.bodyList[J->indexB] : -1;
+			}
+		}
+	}
+	for ( int s = tid; s < localCount; s += nt )
+	{
+		int p = ( s << plan.rankShift ) + rank;
+		int ai = plan.bodyList ? plan.bodyList[p] : p;
+		a.sv[ai] = sv[s];
+		a.sd[ai] = sd[s];
 	}
 }
 
@@ -210,7 +277,9 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	for ( int k = 0; k < activeColorCount; ++k )
 		counts[k] = useLists ? b->hSummary->bigContactCount[activeColors[k]]
 							 : a->colorOffsets[activeColors[k] + 1] - a->colorOffsets[activeColors[k]];
-	size_t smem = clusterSmem( counts, activeColorCount, ranks );
+	int rankShift = ranks == 16 ? 4 : 3;
+	int slotsPerRank = ( bodyCount + ranks - 1 ) / ranks;
+	size_t smem = clusterSmem( counts, activeColorCount, ranks ) + (size_t)slotsPerRank * 2 * sizeof( float4 );
 	if ( smem > B2G_CLUSTER_SMEM_MAX ) return -1;
 	d_clusterPlan plan;
 	memset( &plan, 0, sizeof( plan ) );
@@ -221,8 +290,25 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	plan.slotList = useLists ? b->bigSlotList : NULL;
 	plan.jointList = useLists ? b->bigJointList : NULL;
 	plan.bodyList = useLists ? b->bigBodyList : NULL;
+	plan.positionOf = useLists ? b->localIndex : NULL;
 	plan.summary = b->summary;
 	plan.bodyCount = bodyCount;
+	plan.rankShift = rankShift;
+	plan.slotsPerRank = slotsPerRank;
+
+	/* threads per CTA: the largest per-CTA share of one color (joints + contacts), rounded to
+	   warps, so a color phase is one pass and no more warps than needed meet at each barrier */
+	int share = 1;
+	for ( int k = 0; k < activeColorCount; ++k )
+	{
+		int color = activeColors[k];
+		int joints = useLists ? b->hSummary->bigJointCount[color] : jointOffsets[color + 1] - jointOffsets[color];
+		int items = ( joints + ranks - 1 ) / ranks + ( counts[k] + ranks - 1 ) / ranks;
+		if ( items > share ) share = items;
+	}
+	int threads = ( ( share + 31 ) / 32 ) * 32;
+	if ( threads < 128 ) threads = 128;
+	if ( threads > B2G_CLUSTER_THREADS ) threads = B2G_CLUSTER_THREADS;
 
 	cudaLaunchConfig_t cfg;
 	memset( &cfg, 0, sizeof( cfg ) );
@@ -232,7 +318,7 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	attr.val.clusterDim.y = 1;
 	attr.val.clusterDim.z = 1;
 	cfg.gridDim = dim3( ranks );
-	cfg.blockDim = dim3( B2G_CLUSTER_THREADS );
+	cfg.blockDim = dim3( threads );
 	cfg.dynamicSmemBytes = smem > 0 ? smem : 16;
 	cfg.stream = stream;
 	cfg.attrs = &attr;

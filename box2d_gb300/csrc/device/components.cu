@@ -215,7 +215,9 @@ __global__ void k_compScatter( d_solveArgs a, d_compArgs c, int n, int total, in
 		}
 		else
 		{
-			c.bigBodyList[atomicAdd( &c.summary->bigBodyCount, 1 )] = i;
+			int pos = atomicAdd( &c.summary->bigBodyCount, 1 );
+			c.bigBodyList[pos] = i;
+			c.localIndex[i] = pos; /* position in the big-body list */
 		}
 		return;
 	}

@@ -119,7 +119,7 @@ struct d_stateRef
 	bool dynamic;
 };
 
-static __device__ __forceinline__ d_stateRef d_loadState( const float4* sv, const float4* sd, int index )
+template <class TBodies> static __device__ __forceinline__ d_stateRef d_loadState( const TBodies& bodies, int index )
 {
 	d_stateRef r;
 	if ( index < 0 )
@@ -129,17 +129,17 @@ static __device__ __forceinline__ d_stateRef d_loadState( const float4* sv, cons
 		r.dynamic = false;
 		return r;
 	}
-	r.v = sv[index];
-	r.d = sd[index];
+	r.v = bodies.v( index );
+	r.d = bodies.d( index );
 	r.dynamic = ( __float_as_uint( r.v.w ) & B2G_DYNAMIC_FLAG ) != 0;
 	return r;
 }
 
 /* revolute_joint.c:283-315 */
-static __device__ void d_warmStartRevolute( b2gJoint* j, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartRevolute( b2gJoint* j, TBodies& bodies )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
 	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
 	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
@@ -150,22 +150,22 @@ static __device__ void d_warmStartRevolute( b2gJoint* j, float4* sv, const float
 		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, linearImpulse );
 		float w = A.v.z;
 		w -= iA * ( d_cross( rA, linearImpulse ) + axialImpulse );
-		sv[j->indexA] = make_float4( v.x, v.y, w, A.v.w );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, w, A.v.w );
 	}
 	if ( B.dynamic )
 	{
 		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, linearImpulse );
 		float w = B.v.z;
 		w += iB * ( d_cross( rB, linearImpulse ) + axialImpulse );
-		sv[j->indexB] = make_float4( v.x, v.y, w, B.v.w );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, w, B.v.w );
 	}
 }
 
 /* revolute_joint.c:317-500 */
-static __device__ void d_solveRevolute( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+template <class TBodies> static __device__ void d_solveRevolute( b2gJoint* j, TBodies& bodies, float h, float inv_h, bool useBias )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
 	float wA = A.v.z, wB = B.v.z;
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
@@ -266,8 +266,8 @@ static __device__ void d_solveRevolute( b2gJoint* j, float4* sv, const float4* s
 		vB = d_mulAdd( vB, mB, impulse );
 		wB += iB * d_cross( rB, impulse );
 	}
-	if ( A.dynamic ) sv[j->indexA] = make_float4( vA.x, vA.y, wA, A.v.w );
-	if ( B.dynamic ) sv[j->indexB] = make_float4( vB.x, vB.y, wB, B.v.w );
+	if ( A.dynamic ) bodies.v( j->indexA ) = make_float4( vA.x, vA.y, wA, A.v.w );
+	if ( B.dynamic ) bodies.v( j->indexB ) = make_float4( vB.x, vB.y, wB, B.v.w );
 }
 
 /* velocity update of one axial row: P = impulse * axis with lever arms a1, a2 */
@@ -283,11 +283,11 @@ static __device__ __forceinline__ void d_applyAxial( b2Vec2* vA, float* wA, b2Ve
 	*wB += iB * LB;
 }
 
-static __device__ __forceinline__ void d_storeVelocities( float4* sv, const b2gJoint* j, const d_stateRef& A, const d_stateRef& B,
+template <class TBodies> static __device__ __forceinline__ void d_storeVelocities( TBodies& bodies, const b2gJoint* j, const d_stateRef& A, const d_stateRef& B,
 														  b2Vec2 vA, float wA, b2Vec2 vB, float wB )
 {
-	if ( A.dynamic ) sv[j->indexA] = make_float4( vA.x, vA.y, wA, A.v.w );
-	if ( B.dynamic ) sv[j->indexB] = make_float4( vB.x, vB.y, wB, B.v.w );
+	if ( A.dynamic ) bodies.v( j->indexA ) = make_float4( vA.x, vA.y, wA, A.v.w );
+	if ( B.dynamic ) bodies.v( j->indexB ) = make_float4( vB.x, vB.y, wB, B.v.w );
 }
 
 /* ---- prismatic (prismatic_joint.c:295-667)
@@ -305,10 +305,10 @@ static __device__ void d_preparePrismatic( b2gJoint* j, const d_jointBodies* bod
 	}
 }
 
-static __device__ void d_warmStartPrismatic( b2gJoint* j, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartPrismatic( b2gJoint* j, TBodies& bodies )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
 	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
 	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
@@ -329,19 +329,19 @@ static __device__ void d_warmStartPrismatic( b2gJoint* j, float4* sv, const floa
 	if ( A.dynamic )
 	{
 		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, P );
-		sv[j->indexA] = make_float4( v.x, v.y, A.v.z - iA * LA, A.v.w );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, A.v.z - iA * LA, A.v.w );
 	}
 	if ( B.dynamic )
 	{
 		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, P );
-		sv[j->indexB] = make_float4( v.x, v.y, B.v.z + iB * LB, B.v.w );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, B.v.z + iB * LB, B.v.w );
 	}
 }
 
-static __device__ void d_solvePrismatic( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+template <class TBodies> static __device__ void d_solvePrismatic( b2gJoint* j, TBodies& bodies, float h, float inv_h, bool useBias )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
 	float wA = A.v.z, wB = B.v.z;
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
@@ -473,7 +473,7 @@ static __device__ void d_solvePrismatic( b2gJoint* j, float4* sv, const float4* 
 		vB = d_mulAdd( vB, mB, P );
 		wB += iB * LB;
 	}
-	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
 }
 
 /* ---- weld (weld_joint.c:148-454, the non-block solver)
@@ -513,10 +513,10 @@ static __device__ void d_prepareWeld( b2gJoint* j, const d_jointBodies* bodies, 
 	}
 }
 
-static __device__ void d_warmStartWeld( b2gJoint* j, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartWeld( b2gJoint* j, TBodies& bodies )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
 	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
 	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
@@ -526,20 +526,20 @@ static __device__ void d_warmStartWeld( b2gJoint* j, float4* sv, const float4* s
 	{
 		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, linearImpulse );
 		float w = A.v.z - iA * ( d_cross( rA, linearImpulse ) + angularImpulse );
-		sv[j->indexA] = make_float4( v.x, v.y, w, A.v.w );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, w, A.v.w );
 	}
 	if ( B.dynamic )
 	{
 		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, linearImpulse );
 		float w = B.v.z + iB * ( d_cross( rB, linearImpulse ) + angularImpulse );
-		sv[j->indexB] = make_float4( v.x, v.y, w, B.v.w );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, w, B.v.w );
 	}
 }
 
-static __device__ void d_solveWeld( b2gJoint* j, float4* sv, const float4* sd, bool useBias )
+template <class TBodies> static __device__ void d_solveWeld( b2gJoint* j, TBodies& bodies, bool useBias )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
 	float wA = A.v.z, wB = B.v.z;
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
@@ -588,7 +588,7 @@ static __device__ void d_solveWeld( b2gJoint* j, float4* sv, const float4* sd, b
 		vB = d_mulAdd( vB, mB, impulse );
 		wB += iB * d_cross( rB, impulse );
 	}
-	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
 }
 
 /* ---- wheel (wheel_joint.c:197-525)
@@ -620,10 +620,10 @@ static __device__ void d_prepareWheel( b2gJoint* j, const d_jointBodies* bodies,
 	}
 }
 
-static __device__ void d_warmStartWheel( b2gJoint* j, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartWheel( b2gJoint* j, TBodies& bodies )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
 	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
 	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
@@ -642,19 +642,19 @@ static __device__ void d_warmStartWheel( b2gJoint* j, float4* sv, const float4* 
 	if ( A.dynamic )
 	{
 		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, P );
-		sv[j->indexA] = make_float4( v.x, v.y, A.v.z - iA * LA, A.v.w );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, A.v.z - iA * LA, A.v.w );
 	}
 	if ( B.dynamic )
 	{
 		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, P );
-		sv[j->indexB] = make_float4( v.x, v.y, B.v.z + iB * LB, B.v.w );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, B.v.z + iB * LB, B.v.w );
 	}
 }
 
-static __device__ void d_solveWheel( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+template <class TBodies> static __device__ void d_solveWheel( b2gJoint* j, TBodies& bodies, float h, float inv_h, bool useBias )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
 	float wA = A.v.z, wB = B.v.z;
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
@@ -749,7 +749,7 @@ static __device__ void d_solveWheel( b2gJoint* j, float4* sv, const float4* sd, 
 		j->s[0] += impulse;
 		d_applyAxial( &vA, &wA, &vB, &wB, mA, iA, mB, iB, perpA, s1, s2, impulse );
 	}
-	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
 }
 
 /* ---- distance (distance_joint.c:250-543); the anchors are the frames' origins
@@ -774,10 +774,10 @@ static __device__ void d_prepareDistance( b2gJoint* j, const d_jointBodies* bodi
 	}
 }
 
-static __device__ void d_warmStartDistance( b2gJoint* j, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartDistance( b2gJoint* j, TBodies& bodies )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
 	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
 	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
@@ -789,12 +789,12 @@ static __device__ void d_warmStartDistance( b2gJoint* j, float4* sv, const float
 	if ( A.dynamic )
 	{
 		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, P );
-		sv[j->indexA] = make_float4( v.x, v.y, A.v.z - iA * d_cross( rA, P ), A.v.w );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, A.v.z - iA * d_cross( rA, P ), A.v.w );
 	}
 	if ( B.dynamic )
 	{
 		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, P );
-		sv[j->indexB] = make_float4( v.x, v.y, B.v.z + iB * d_cross( rB, P ), B.v.w );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, B.v.z + iB * d_cross( rB, P ), B.v.w );
 	}
 }
 
@@ -807,10 +807,10 @@ static __device__ __forceinline__ void d_applyLinear( b2Vec2* vA, float* wA, b2V
 	*wB += iB * d_cross( rB, P );
 }
 
-static __device__ void d_solveDistance( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+template <class TBodies> static __device__ void d_solveDistance( b2gJoint* j, TBodies& bodies, float h, float inv_h, bool useBias )
 {
 	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
-	d_stateRef A = d_loadState( sv, sd, j->indexA ), B = d_loadState( sv, sd, j->indexB );
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
 	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
 	float wA = A.v.z, wB = B.v.z;
 	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
@@ -903,7 +903,7 @@ static __device__ void d_solveDistance( b2gJoint* j, float4* sv, const float4* s
 		j->s[0] += impulse;
 		d_applyLinear( &vA, &wA, &vB, &wB, mA, iA, mB, iB, rA, rB, d_mulSV( impulse, axis ) );
 	}
-	d_storeVelocities( sv, j, A, B, vA, wA, vB, wB );
+	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
 }
 
 /* joint.c:1406-1540 dispatch */
@@ -922,28 +922,28 @@ static __device__ void d_prepareJoint( b2gJoint* j, const d_jointBodies* bodies,
 	}
 }
 
-static __device__ void d_warmStartJoint( b2gJoint* j, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartJoint( b2gJoint* j, TBodies& bodies )
 {
 	switch ( j->type )
 	{
-		case b2_distanceJoint: d_warmStartDistance( j, sv, sd ); break;
-		case b2_prismaticJoint: d_warmStartPrismatic( j, sv, sd ); break;
-		case b2_revoluteJoint: d_warmStartRevolute( j, sv, sd ); break;
-		case b2_weldJoint: d_warmStartWeld( j, sv, sd ); break;
-		case b2_wheelJoint: d_warmStartWheel( j, sv, sd ); break;
+		case b2_distanceJoint: d_warmStartDistance( j, bodies ); break;
+		case b2_prismaticJoint: d_warmStartPrismatic( j, bodies ); break;
+		case b2_revoluteJoint: d_warmStartRevolute( j, bodies ); break;
+		case b2_weldJoint: d_warmStartWeld( j, bodies ); break;
+		case b2_wheelJoint: d_warmStartWheel( j, bodies ); break;
 		default: break;
 	}
 }
 
-static __device__ void d_solveJoint( b2gJoint* j, float4* sv, const float4* sd, float h, float inv_h, bool useBias )
+template <class TBodies> static __device__ void d_solveJoint( b2gJoint* j, TBodies& bodies, float h, float inv_h, bool useBias )
 {
 	switch ( j->type )
 	{
-		case b2_distanceJoint: d_solveDistance( j, sv, sd, h, inv_h, useBias ); break;
-		case b2_prismaticJoint: d_solvePrismatic( j, sv, sd, h, inv_h, useBias ); break;
-		case b2_revoluteJoint: d_solveRevolute( j, sv, sd, h, inv_h, useBias ); break;
-		case b2_weldJoint: d_solveWeld( j, sv, sd, useBias ); break;
-		case b2_wheelJoint: d_solveWheel( j, sv, sd, h, inv_h, useBias ); break;
+		case b2_distanceJoint: d_solveDistance( j, bodies, h, inv_h, useBias ); break;
+		case b2_prismaticJoint: d_solvePrismatic( j, bodies, h, inv_h, useBias ); break;
+		case b2_revoluteJoint: d_solveRevolute( j, bodies, h, inv_h, useBias ); break;
+		case b2_weldJoint: d_solveWeld( j, bodies, useBias ); break;
+		case b2_wheelJoint: d_solveWheel( j, bodies, h, inv_h, useBias ); break;
 		default: break;
 	}
 }

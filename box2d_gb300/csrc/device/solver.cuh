@@ -18,6 +18,16 @@ typedef struct d_body
 	float dpx, dpy, dqc, dqs;
 } d_body;
 
+/* body-state access of the solver functions: awake state in two float4 arrays, indexed by
+   awake index (global memory, or a shared-memory copy with bin-local indices) */
+struct d_arrayBodies
+{
+	float4* sv;
+	float4* sd;
+	__device__ __forceinline__ float4& v( int i ) const { return sv[i]; }
+	__device__ __forceinline__ float4& d( int i ) const { return sd[i]; }
+};
+
 static __device__ __forceinline__ float w_min( float a, float b ) { return a < b ? a : b; }
 static __device__ __forceinline__ float w_max( float a, float b ) { return a > b ? a : b; }
 static __device__ __forceinline__ float w_symClamp( float a, float b )
@@ -26,7 +36,7 @@ static __device__ __forceinline__ float w_symClamp( float a, float b )
 	return w_max( nb, w_min( a, b ) );
 }
 
-static __device__ __forceinline__ d_body d_gather( const float4* __restrict__ sv, const float4* __restrict__ sd, int index1 )
+template <class TBodies> static __device__ __forceinline__ d_body d_gather( TBodies& bodies, int index1 )
 {
 	d_body b;
 	if ( index1 == 0 )
@@ -41,8 +51,8 @@ static __device__ __forceinline__ d_body d_gather( const float4* __restrict__ sv
 		b.dqs = 0.0f;
 		return b;
 	}
-	float4 v = sv[index1 - 1];
-	float4 d = sd[index1 - 1];
+	float4 v = bodies.v( index1 - 1 );
+	float4 d = bodies.d( index1 - 1 );
 	b.vx = v.x;
 	b.vy = v.y;
 	b.w = v.z;
@@ -55,7 +65,7 @@ static __device__ __forceinline__ d_body d_gather( const float4* __restrict__ sv
 }
 
 /* writes only velocities, only for dynamic bodies (contact_solver.c:1526-1562) */
-static __device__ __forceinline__ void d_scatter( float4* __restrict__ sv, int index1, const d_body* b )
+template <class TBodies> static __device__ __forceinline__ void d_scatter( TBodies& bodies, int index1, const d_body* b )
 {
 	if ( index1 == 0 ) return;
 	if ( ( b->flags & B2G_DYNAMIC_FLAG ) == 0 ) return;
@@ -64,13 +74,13 @@ static __device__ __forceinline__ void d_scatter( float4* __restrict__ sv, int i
 	v.y = b->vy;
 	v.z = b->w;
 	v.w = __uint_as_float( b->flags );
-	sv[index1 - 1] = v;
+	bodies.v( index1 - 1 ) = v;
 }
 
 /* contact_solver.c:1811-1871 */
-static __device__ void d_warmStartLane( b2gContactLane* c, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartLane( b2gContactLane* c, TBodies& bodies )
 {
-	d_body bA = d_gather( sv, sd, c->indexA ), bB = d_gather( sv, sd, c->indexB );
+	d_body bA = d_gather( bodies, c->indexA ), bB = d_gather( bodies, c->indexB );
 	float tangentX = c->normal.y;
 	float tangentY = 0.0f - c->normal.x;
 	{
@@ -99,8 +109,8 @@ static __device__ void d_warmStartLane( b2gContactLane* c, float4* sv, const flo
 	}
 	bA.w = bA.w - c->invIA * c->rollingImpulse;
 	bB.w = bB.w + c->invIB * c->rollingImpulse;
-	d_scatter( sv, c->indexA, &bA );
-	d_scatter( sv, c->indexB, &bB );
+	d_scatter( bodies, c->indexA, &bA );
+	d_scatter( bodies, c->indexB, &bB );
 }
 
 static __device__ __forceinline__ void d_normalPoint( const b2gContactLane* c, d_body* bA, d_body* bB, float dpx, float dpy,
@@ -167,10 +177,10 @@ static __device__ __forceinline__ void d_frictionPoint( const b2gContactLane* c,
 }
 
 /* contact_solver.c:1873-2116 */
-static __device__ void d_solveLane( b2gContactLane* c, float4* sv, const float4* sd, float inv_h, float contactSpeedNeg,
+template <class TBodies> static __device__ void d_solveLane( b2gContactLane* c, TBodies& bodies, float inv_h, float contactSpeedNeg,
 									bool useBias )
 {
-	d_body bA = d_gather( sv, sd, c->indexA ), bB = d_gather( sv, sd, c->indexB );
+	d_body bA = d_gather( bodies, c->indexA ), bB = d_gather( bodies, c->indexB );
 	float biasRate, massScale, impulseScale;
 	if ( useBias )
 	{
@@ -205,8 +215,8 @@ static __device__ void d_solveLane( b2gContactLane* c, float4* sv, const float4*
 		d_frictionPoint( c, &bA, &bB, c->anchorA1, c->anchorB1, c->tangentMass1, c->normalImpulse1, &c->tangentImpulse1 );
 		d_frictionPoint( c, &bA, &bB, c->anchorA2, c->anchorB2, c->tangentMass2, c->normalImpulse2, &c->tangentImpulse2 );
 	}
-	d_scatter( sv, c->indexA, &bA );
-	d_scatter( sv, c->indexB, &bB );
+	d_scatter( bodies, c->indexA, &bA );
+	d_scatter( bodies, c->indexB, &bB );
 }
 
 static __device__ __forceinline__ void d_restitutionPoint( const b2gContactLane* c, d_body* bA, d_body* bB, b2Vec2 rA, b2Vec2 rB,
@@ -234,22 +244,22 @@ static __device__ __forceinline__ void d_restitutionPoint( const b2gContactLane*
 }
 
 /* contact_solver.c:2118-2228 */
-static __device__ void d_restitutionLane( b2gContactLane* c, float4* sv, const float4* sd, float threshold )
+template <class TBodies> static __device__ void d_restitutionLane( b2gContactLane* c, TBodies& bodies, float threshold )
 {
 	if ( ( c->groupFlags & 2 ) == 0 ) return;
-	d_body bA = d_gather( sv, sd, c->indexA ), bB = d_gather( sv, sd, c->indexB );
+	d_body bA = d_gather( bodies, c->indexA ), bB = d_gather( bodies, c->indexB );
 	d_restitutionPoint( c, &bA, &bB, c->anchorA1, c->anchorB1, c->relativeVelocity1, c->totalNormalImpulse1, c->normalMass1,
 						threshold, &c->normalImpulse1, &c->totalNormalImpulse1 );
 	d_restitutionPoint( c, &bA, &bB, c->anchorA2, c->anchorB2, c->relativeVelocity2, c->totalNormalImpulse2, c->normalMass2,
 						threshold, &c->normalImpulse2, &c->totalNormalImpulse2 );
-	d_scatter( sv, c->indexA, &bA );
-	d_scatter( sv, c->indexB, &bB );
+	d_scatter( bodies, c->indexA, &bA );
+	d_scatter( bodies, c->indexB, &bB );
 }
 
 /* ---------------- overflow contacts: scalar path (contact_solver.c:20-545) ---------------- */
-static __device__ void d_warmStartOverflow( b2gContactLane* c, float4* sv, const float4* sd )
+template <class TBodies> static __device__ void d_warmStartOverflow( b2gContactLane* c, TBodies& bodies )
 {
-	d_body bA = d_gather( sv, sd, c->indexA ), bB = d_gather( sv, sd, c->indexB );
+	d_body bA = d_gather( bodies, c->indexA ), bB = d_gather( bodies, c->indexB );
 	b2Vec2 vA = { bA.vx, bA.vy }, vB = { bB.vx, bB.vy };
 	float wA = bA.w, wB = bB.w;
 	float mA = c->invMassA, iA = c->invIA, mB = c->invMassB, iB = c->invIB;
@@ -276,14 +286,14 @@ static __device__ void d_warmStartOverflow( b2gContactLane* c, float4* sv, const
 	bB.vx = vB.x;
 	bB.vy = vB.y;
 	bB.w = wB;
-	d_scatter( sv, c->indexA, &bA );
-	d_scatter( sv, c->indexB, &bB );
+	d_scatter( bodies, c->indexA, &bA );
+	d_scatter( bodies, c->indexB, &bB );
 }
 
-static __device__ void d_solveOverflow( b2gContactLane* c, float4* sv, const float4* sd, float inv_h, float contactSpeed,
+template <class TBodies> static __device__ void d_solveOverflow( b2gContactLane* c, TBodies& bodies, float inv_h, float contactSpeed,
 										bool useBias )
 {
-	d_body bA = d_gather( sv, sd, c->indexA ), bB = d_gather( sv, sd, c->indexB );
+	d_body bA = d_gather( bodies, c->indexA ), bB = d_gather( bodies, c->indexB );
 	float mA = c->invMassA, iA = c->invIA, mB = c->invMassB, iB = c->invIB;
 	b2Vec2 vA = { bA.vx, bA.vy }, vB = { bB.vx, bB.vy };
 	float wA = bA.w, wB = bB.w;
@@ -365,15 +375,15 @@ static __device__ void d_solveOverflow( b2gContactLane* c, float4* sv, const flo
 	bB.vx = vB.x;
 	bB.vy = vB.y;
 	bB.w = wB;
-	d_scatter( sv, c->indexA, &bA );
-	d_scatter( sv, c->indexB, &bB );
+	d_scatter( bodies, c->indexA, &bA );
+	d_scatter( bodies, c->indexB, &bB );
 }
 
-static __device__ void d_restitutionOverflow( b2gContactLane* c, float4* sv, const float4* sd, float threshold )
+template <class TBodies> static __device__ void d_restitutionOverflow( b2gContactLane* c, TBodies& bodies, float threshold )
 {
 	float restitution = c->restitution;
 	if ( restitution == 0.0f ) return;
-	d_body bA = d_gather( sv, sd, c->indexA ), bB = d_gather( sv, sd, c->indexB );
+	d_body bA = d_gather( bodies, c->indexA ), bB = d_gather( bodies, c->indexB );
 	float mA = c->invMassA, iA = c->invIA, mB = c->invMassB, iB = c->invIB;
 	b2Vec2 vA = { bA.vx, bA.vy }, vB = { bB.vx, bB.vy };
 	float wA = bA.w, wB = bB.w;
@@ -407,6 +417,6 @@ static __device__ void d_restitutionOverflow( b2gContactLane* c, float4* sv, con
 	bB.vx = vB.x;
 	bB.vy = vB.y;
 	bB.w = wB;
-	d_scatter( sv, c->indexA, &bA );
-	d_scatter( sv, c->indexB, &bB );
+	d_scatter( bodies, c->indexA, &bA );
+	d_scatter( bodies, c->indexB, &bB );
 }

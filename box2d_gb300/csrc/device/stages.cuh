@@ -239,20 +239,35 @@ enum
 	STAGE_RESTITUTION = 3,
 };
 
-/* one joint or one contact lane of a graph color at a stage, body state in sv/sd */
+/* one joint or one contact lane of a graph color at a stage, through a body accessor */
+template <class TBodies>
+static __device__ __forceinline__ void d_jointStageT( const b2gStepParams& P, b2gJoint* j, TBodies& bodies, int stage )
+{
+	if ( stage == STAGE_WARM ) d_warmStartJoint( j, bodies );
+	else if ( stage == STAGE_SOLVE ) d_solveJoint( j, bodies, P.h, P.inv_h, true );
+	else if ( stage == STAGE_RELAX ) d_solveJoint( j, bodies, P.h, P.inv_h, false );
+}
+
+template <class TBodies>
+static __device__ __forceinline__ void d_laneStageT( const b2gStepParams& P, b2gContactLane* c, TBodies& bodies, int stage )
+{
+	if ( stage == STAGE_WARM ) d_warmStartLane( c, bodies );
+	else if ( stage == STAGE_SOLVE ) d_solveLane( c, bodies, P.inv_h, -P.contactSpeed, true );
+	else if ( stage == STAGE_RELAX ) d_solveLane( c, bodies, P.inv_h, -P.contactSpeed, false );
+	else d_restitutionLane( c, bodies, P.restitutionThreshold );
+}
+
+/* the same with body state in two float4 arrays */
 static __device__ __forceinline__ void d_jointStage( const b2gStepParams& P, b2gJoint* j, float4* sv, float4* sd, int stage )
 {
-	if ( stage == STAGE_WARM ) d_warmStartJoint( j, sv, sd );
-	else if ( stage == STAGE_SOLVE ) d_solveJoint( j, sv, sd, P.h, P.inv_h, true );
-	else if ( stage == STAGE_RELAX ) d_solveJoint( j, sv, sd, P.h, P.inv_h, false );
+	d_arrayBodies bodies = { sv, sd };
+	d_jointStageT( P, j, bodies, stage );
 }
 
 static __device__ __forceinline__ void d_laneStage( const b2gStepParams& P, b2gContactLane* c, float4* sv, float4* sd, int stage )
 {
-	if ( stage == STAGE_WARM ) d_warmStartLane( c, sv, sd );
-	else if ( stage == STAGE_SOLVE ) d_solveLane( c, sv, sd, P.inv_h, -P.contactSpeed, true );
-	else if ( stage == STAGE_RELAX ) d_solveLane( c, sv, sd, P.inv_h, -P.contactSpeed, false );
-	else d_restitutionLane( c, sv, sd, P.restitutionThreshold );
+	d_arrayBodies bodies = { sv, sd };
+	d_laneStageT( P, c, bodies, stage );
 }
 
 /* one graph color: threads [0, jointCount) run joints, the rest run contact lanes */
@@ -261,19 +276,12 @@ static __device__ void d_colorStageItem( const d_solveArgs& a, int jointBegin, i
 {
 	if ( i < jointCount )
 	{
-		b2gJoint* j = a.joints + jointBegin + i;
-		if ( stage == STAGE_WARM ) d_warmStartJoint( j, a.sv, a.sd );
-		else if ( stage == STAGE_SOLVE ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, true );
-		else if ( stage == STAGE_RELAX ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, false );
+		d_jointStage( a.p, a.joints + jointBegin + i, a.sv, a.sd, stage );
 		return;
 	}
 	i -= jointCount;
 	if ( i >= laneCount ) return;
-	b2gContactLane* c = a.lanes + laneBegin + i;
-	if ( stage == STAGE_WARM ) d_warmStartLane( c, a.sv, a.sd );
-	else if ( stage == STAGE_SOLVE ) d_solveLane( c, a.sv, a.sd, a.p.inv_h, -a.p.contactSpeed, true );
-	else if ( stage == STAGE_RELAX ) d_solveLane( c, a.sv, a.sd, a.p.inv_h, -a.p.contactSpeed, false );
-	else d_restitutionLane( c, a.sv, a.sd, a.p.restitutionThreshold );
+	d_laneStage( a.p, a.lanes + laneBegin + i, a.sv, a.sd, stage );
 }
 
 /* overflow color: one thread walks joints then contacts in array order (joint.c:1542-1591,
@@ -281,20 +289,15 @@ static __device__ void d_colorStageItem( const d_solveArgs& a, int jointBegin, i
 static __device__ void d_overflowStageAll( const d_solveArgs& a, int jointBegin, int jointCount, int laneBegin, int laneCount,
 											int stage )
 {
-	for ( int i = 0; i < jointCount; ++i )
-	{
-		b2gJoint* j = a.joints + jointBegin + i;
-		if ( stage == STAGE_WARM ) d_warmStartJoint( j, a.sv, a.sd );
-		else if ( stage == STAGE_SOLVE ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, true );
-		else if ( stage == STAGE_RELAX ) d_solveJoint( j, a.sv, a.sd, a.p.h, a.p.inv_h, false );
-	}
+	d_arrayBodies bodies = { a.sv, a.sd };
+	for ( int i = 0; i < jointCount; ++i ) d_jointStage( a.p, a.joints + jointBegin + i, a.sv, a.sd, stage );
 	for ( int i = 0; i < laneCount; ++i )
 	{
 		b2gContactLane* c = a.lanes + laneBegin + i;
-		if ( stage == STAGE_WARM ) d_warmStartOverflow( c, a.sv, a.sd );
-		else if ( stage == STAGE_SOLVE ) d_solveOverflow( c, a.sv, a.sd, a.p.inv_h, a.p.contactSpeed, true );
-		else if ( stage == STAGE_RELAX ) d_solveOverflow( c, a.sv, a.sd, a.p.inv_h, a.p.contactSpeed, false );
-		else d_restitutionOverflow( c, a.sv, a.sd, a.p.restitutionThreshold );
+		if ( stage == STAGE_WARM ) d_warmStartOverflow( c, bodies );
+		else if ( stage == STAGE_SOLVE ) d_solveOverflow( c, bodies, a.p.inv_h, a.p.contactSpeed, true );
+		else if ( stage == STAGE_RELAX ) d_solveOverflow( c, bodies, a.p.inv_h, a.p.contactSpeed, false );
+		else d_restitutionOverflow( c, bodies, a.p.restitutionThreshold );
 	}
 }
 
