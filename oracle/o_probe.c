@@ -71,6 +71,15 @@ B2P_EXPORT int b2p_contact_floats( uint32_t packedWorldId, float* out, int capac
 }
 
 extern int o_continuousSkipped;
+extern int o_continuousCalls;
+extern int o_continuousHits;
+
+/* continuous collision since the library was loaded: fast bodies swept, sweeps that hit */
+B2P_EXPORT void b2p_oracle_ccd_counts( int* out )
+{
+	out[0] = o_continuousCalls;
+	out[1] = o_continuousHits;
+}
 
 /* number of fast-body continuous steps the oracle could not restate (0 when exact) */
 B2P_EXPORT int b2p_oracle_unsupported( void ) { return o_continuousSkipped; }

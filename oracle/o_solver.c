@@ -730,6 +730,7 @@ static void o_integratePositions( o_world* w, o_stepContext* ctx )
 
 /* ---------------- finalize bodies (solver.c:553-743) ---------------- */
 void o_solveContinuous( o_world* w, int simIndex );
+extern int o_continuousSkipped;
 
 static void o_finalizeRange( void* p, int begin, int end )
 {
@@ -779,6 +780,7 @@ static void o_finalizeRange( void* p, int begin, int end )
 					/* bullets are continuous against every body; not part of the GPU path */
 					sim->center0 = sim->center;
 					sim->rotation0 = sim->transform.q;
+					__atomic_fetch_add( &o_continuousSkipped, 1, __ATOMIC_RELAXED );
 				}
 				else
 				{

@@ -34,6 +34,10 @@ SCENES = [
     ("batch_world_60", B.BATCH_WORLD, 60, 0, 0, 11, B.NO_CONTINUOUS, 200, [1, 200]),
     ("ramp_world_4x4", B.RAMP_WORLD, 4, 4, 0, 5, B.NO_CONTINUOUS, 120, [1, 120]),
     ("joint_zoo_4", B.JOINT_ZOO, 4, 0, 0, 3, B.NO_CONTINUOUS, 300, [1, 150, 300]),
+    # continuous collision on: fast bodies are swept against static shapes
+    ("shape_zoo_200_continuous", B.SHAPE_ZOO, 200, 0, 0, 7, 0, 300, [1, 150, 300]),
+    ("many_pyramids_rain_3x3_continuous", B.MANY_PYRAMIDS_RAIN, 3, 10, 100, 0, 0, 300, [1, 150, 300]),
+    ("batch_world_continuous", B.BATCH_WORLD, 0, 0, 0, 21, 0, 300, [1, 300]),
 ]
 
 
