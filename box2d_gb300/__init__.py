@@ -57,6 +57,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2p_status": (c_int, [c_u32]),
         "b2p_host_profile": (c_int, [c_u32, c_p, c_int]),
         "b2p_contacts_noalloc": (c_int, [c_u32, c_p, c_int]),
+        "b2p_continuous_counts": (None, [c_u32, c_p]),
     }
     for name, (res, args) in optional.items():
         if hasattr(lib, name):
@@ -147,6 +148,13 @@ class Scene:
         out = np.zeros(10, np.float32)
         self.lib.b2p_host_profile(self.world_id, out.ctypes.data, int(reset))
         return out
+
+    def continuous_counts(self) -> tuple[int, int]:
+        """Fast non-bullet bodies swept against static shapes, and sweeps that ended at a
+        time of impact, since the world was created."""
+        out = np.zeros(2, np.int32)
+        self.lib.b2p_continuous_counts(self.world_id, out.ctypes.data)
+        return int(out[0]), int(out[1])
 
     def counters(self) -> np.ndarray:
         out = np.zeros(30, np.int32)

@@ -77,6 +77,13 @@ typedef struct b2gShape
 	float radius;
 	float aabbMargin;
 	float friction, restitution, rollingResistance, tangentSpeed;
+	/* continuous collision (solver.c:183-376): filter, sensor flag, and the core circle
+	   (centroid, 0.25 x minimum extent about it) used when the full shape starts overlapped */
+	uint64_t categoryBits, maskBits;
+	int groupIndex;
+	int isSensor;
+	b2Vec2 ccdCentroid;
+	float ccdCoreRadius;
 } b2gShape;
 
 /* contact record (contact.h:103-142 b2ContactSim without ids kept on the host) */
@@ -160,7 +167,9 @@ typedef struct b2gStepCounters
 	int pairCount;
 	int pairOverflow;
 	int fastBodyCount;
-	int status; /* nonzero: a device check failed (see B2G_STATUS_*) */
+	int status;			/* nonzero: a device check failed (see B2G_STATUS_*) */
+	int continuousSweeps; /* fast non-bullet bodies swept against static shapes */
+	int continuousHits;	  /* sweeps that moved the body back to its time of impact */
 	int pad;
 } b2gStepCounters;
 
@@ -211,6 +220,12 @@ int b2gDev_ContactTableNoAlloc( b2gDeviceWorld* dw, int capacity, int* out, int 
 
 /* joints */
 int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* colorJointOffsets );
+/* per body id, the bodies that a joint with collideConnected == false links it to (CSR:
+   offsets has bodyCount + 1 entries); listCount 0 clears it. Read by continuous collision,
+   as b2ShouldBodiesCollide (body.c:2076-2112). */
+/* the counters of the last solve, as read back by it */
+int b2gDev_LastCounters( b2gDeviceWorld* dw, b2gStepCounters* out );
+int b2gDev_UploadJointPartners( b2gDeviceWorld* dw, const int* offsets, int bodyCount, const int* list, int listCount );
 int b2gDev_DownloadJoints( b2gDeviceWorld* dw, b2gJoint* joints, int count );
 
 /* broadphase: tree nodes as (aabb float4, child1, child2 / userData, flags) */

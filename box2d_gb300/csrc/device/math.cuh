@@ -182,5 +182,12 @@ static __device__ __forceinline__ int d_enlargeAABB( b2AABB* a, b2AABB b )
 	if ( a->upperBound.y < b.upperBound.y ) { a->upperBound.y = b.upperBound.y; changed = 1; }
 	return changed;
 }
+
+/* a tree node box against a query box packed as (lower x, lower y, upper x, upper y) */
+static __device__ __forceinline__ bool d_overlaps( b2AABB a, float4 b )
+{
+	return !( b.x > a.upperBound.x || b.y > a.upperBound.y || a.lowerBound.x > b.z || a.lowerBound.y > b.w );
+}
+
 static __device__ __forceinline__ int d_isValidFloat( float a ) { return !isnan( a ) && !isinf( a ); }
 

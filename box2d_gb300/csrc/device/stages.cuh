@@ -5,6 +5,7 @@
  */
 #pragma once
 
+#include "ccd.cuh"
 #include "joints.cuh"
 #include "solver.cuh"
 
@@ -407,7 +408,99 @@ struct d_finalizeArgs
 	b2gStepCounters* counters;
 	float dt, inv_dt;
 	int enableSleep, enableContinuous;
+	d_ccdWorld ccd; /* static tree and filters for the continuous sweep */
 };
+
+/* solver.c:384-550 b2SolveContinuous for a fast non-bullet body: sweep every non-sensor
+   shape from the step's start pose (center0, rotation0) to the solved pose against the
+   static tree, move the body back to the earliest time of impact, and refresh the shape
+   boxes. Kept out of line: fast bodies are rare and the sweep needs a deep stack.
+   Returns whether a shape's fat box was enlarged. */
+static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, int simIndex, int bodyId, b2Vec2 center, b2Rot q )
+{
+	float4 c0 = a.center0[simIndex];
+	b2Vec2 base = { c0.x, c0.y };
+	float2 lc2 = a.localCenter[bodyId];
+	b2Vec2 localCenter = { lc2.x, lc2.y };
+	d_sweep sweep = d_relativeSweep( base, b2Rot{ c0.z, c0.w }, center, q, localCenter, base );
+	b2Transform xf2;
+	xf2.q = sweep.q2;
+	xf2.p = d_sub( sweep.c2, d_rotate( sweep.q2, sweep.localCenter ) );
+	float fraction = 1.0f;
+	bool hit = false, overflow = false;
+	int start = a.shapeStart[bodyId], count = a.shapeCount[bodyId];
+	for ( int k = 0; k < count; ++k )
+	{
+		int shapeId = a.shapeList[start + k];
+		const b2gShape* fastShape = a.shapes + shapeId;
+		float4 box1 = a.aabb[shapeId];
+		float4 box2 = d_offsetAABB( d_computeFatShapeAABB( fastShape, xf2, 0.0f ), base );
+		a.aabb[shapeId] = box2;
+		if ( fastShape->isSensor ) continue;
+		float4 swept = make_float4( d_min( box1.x, box2.x ), d_min( box1.y, box2.y ), d_max( box1.z, box2.z ),
+									d_max( box1.w, box2.w ) );
+		fraction = d_continuousQuery( a.ccd, swept, shapeId, fastShape, sweep, base, fraction, &hit, &overflow );
+	}
+	atomicAdd( &a.counters->continuousSweeps, 1 );
+	if ( overflow ) atomicOr( &a.counters->status, B2G_STATUS_CAPACITY );
+	bool anyEnlarged = false;
+	if ( fraction < 1.0f )
+	{
+		atomicAdd( &a.counters->continuousHits, 1 );
+		b2Rot qt = d_nlerp( sweep.q1, sweep.q2, fraction );
+		b2Vec2 ct = d_lerp( sweep.c1, sweep.c2, fraction );
+		b2Vec2 origin = d_sub( ct, d_rotate( qt, sweep.localCenter ) );
+		b2Transform transform = { d_add( base, origin ), qt };
+		b2Vec2 centerT = d_add( base, ct );
+		a.xf[bodyId] = make_float4( transform.p.x, transform.p.y, qt.c, qt.s );
+		a.center[bodyId] = make_float2( centerT.x, centerT.y );
+		a.center0[simIndex] = make_float4( centerT.x, centerT.y, qt.c, qt.s );
+		for ( int k = 0; k < count; ++k )
+		{
+			int shapeId = a.shapeList[start + k];
+			const b2gShape* shape = a.shapes + shapeId;
+			float4 aabb = d_computeFatShapeAABB( shape, transform, D_SPECULATIVE_DISTANCE );
+			a.aabb[shapeId] = aabb;
+			float4 fat = a.fat[shapeId];
+			int enlarged = 0;
+			if ( ( fat.x <= aabb.x && fat.y <= aabb.y && aabb.z <= fat.z && aabb.w <= fat.w ) == false )
+			{
+				float margin = shape->aabbMargin;
+				a.fat[shapeId] = make_float4( aabb.x - margin, aabb.y - margin, aabb.z + margin, aabb.w + margin );
+				enlarged = 1;
+				anyEnlarged = true;
+			}
+			a.shapeEnlarged[shapeId] = enlarged;
+		}
+	}
+	else
+	{
+		a.center0[simIndex] = make_float4( center.x, center.y, q.c, q.s );
+		for ( int k = 0; k < count; ++k )
+		{
+			int shapeId = a.shapeList[start + k];
+			float4 aabb = a.aabb[shapeId];
+			float4 fat = a.fat[shapeId];
+			int enlarged = 0;
+			if ( ( fat.x <= aabb.x && fat.y <= aabb.y && aabb.z <= fat.z && aabb.w <= fat.w ) == false )
+			{
+				float margin = a.shapes[shapeId].aabbMargin;
+				a.fat[shapeId] = make_float4( aabb.x - margin, aabb.y - margin, aabb.z + margin, aabb.w + margin );
+				enlarged = 1;
+				anyEnlarged = true;
+			}
+			a.shapeEnlarged[shapeId] = enlarged;
+		}
+	}
+	if ( hit )
+	{
+		/* b2_hadTimeOfImpact lands in the body's sim flags, reported by the next finalize */
+		float4 s = a.sv[simIndex];
+		s.w = __uint_as_float( __float_as_uint( s.w ) | B2G_HAD_TOI );
+		a.sv[simIndex] = s;
+	}
+	return anyEnlarged;
+}
 
 /* solver.c:553-743, one thread per awake body. A body with an enlarged shape (or a fast
    bullet) appends one record per shape, as one contiguous group:
@@ -446,24 +539,27 @@ static __device__ void d_finalizeBody( const d_finalizeArgs& a, int simIndex )
 	stateFlags &= ~B2G_TRANSIENT;
 	a.sv[simIndex] = make_float4( v.x, v.y, w, __uint_as_float( stateFlags ) );
 	bool isBullet = ( bodyFlags & B2G_IS_BULLET ) != 0;
+	bool sweep = false;
 	if ( a.enableSleep == 0 || ( bodyFlags & B2G_ENABLE_SLEEP ) == 0 || sleepVelocity > a.sleepThreshold[bodyId] )
 	{
 		float maxMotion = d_max( maxDeltaPosition, maxVelocity * a.dt );
 		if ( a.bodyType[bodyId] == b2_dynamicBody && a.enableContinuous && maxMotion > a.safetyFactor[bodyId] * a.minExtent[bodyId] )
 		{
-			/* fast body: continuous collision is not part of the device path yet; advance the
-			   sweep like a slow body and report it */
+			/* fast body: non-bullets sweep against static shapes here; bullets advance like
+			   a slow body and are re-inserted into the broadphase by the host */
 			bodyFlags |= B2G_IS_FAST;
 			atomicAdd( &a.counters->fastBodyCount, 1 );
+			sweep = isBullet == false;
 		}
 	}
-	a.center0[simIndex] = make_float4( center.x, center.y, q.c, q.s );
 	a.bodyFlags[bodyId] = bodyFlags;
-	bool isFast = ( bodyFlags & B2G_IS_FAST ) != 0;
-	b2Transform transform = { p, q };
 	int start = a.shapeStart[bodyId], count = a.shapeCount[bodyId];
 	bool anyEnlarged = false;
-	for ( int k = 0; k < count; ++k )
+	if ( sweep ) anyEnlarged = d_solveContinuous( a, simIndex, bodyId, center, q );
+	else a.center0[simIndex] = make_float4( center.x, center.y, q.c, q.s );
+	bool isFast = ( bodyFlags & B2G_IS_FAST ) != 0;
+	b2Transform transform = { p, q };
+	for ( int k = 0; k < count && sweep == false; ++k )
 	{
 		int shapeId = a.shapeList[start + k];
 		int enlarged = 0;

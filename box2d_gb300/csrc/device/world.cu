@@ -94,6 +94,11 @@ struct b2gDeviceWorld
 	b2gJoint* joints;
 	int jointCap, jointCount;
 	int jointOffsets[B2_GRAPH_COLOR_COUNT + 1];
+	/* per body: the bodies a non-colliding joint connects it to (continuous collision filter) */
+	int* partnerOffsets;
+	int* partnerList;
+	int partnerOffsetsCap, partnerListCap;
+	int partnerCount; /* 0: no such joint */
 	/* broadphase */
 	b2gTreeNode* tree[3];
 	int treeCap[3], treeRoot[3];
@@ -215,11 +220,6 @@ __global__ void k_markMoved( unsigned char* movedDyn, unsigned char* movedKin, u
 	int type = key & 3, id = key >> 2;
 	unsigned char* m = type == b2_dynamicBody ? movedDyn : ( type == b2_kinematicBody ? movedKin : movedStat );
 	m[id] = value;
-}
-
-static __device__ __forceinline__ bool d_overlaps( b2AABB a, float4 b )
-{
-	return !( b.x > a.upperBound.x || b.y > a.upperBound.y || a.lowerBound.x > b.z || a.lowerBound.y > b.w );
 }
 
 /* one thread per moved proxy; stack DFS with child1 pushed before child2, as
@@ -584,7 +584,9 @@ __global__ void k_storeImpulses( d_solveArgs a, int total, int overflowBegin )
 	if ( slot < total ) d_storeSlot( a, slot, overflowBegin );
 }
 
-__global__ void k_finalizeBodies( d_finalizeArgs f )
+/* the register cap keeps the common path at full occupancy; the rare continuous sweep of
+   a fast body spills instead */
+__global__ void __launch_bounds__( B2G_THREADS, 8 ) k_finalizeBodies( d_finalizeArgs f )
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if ( i < f.awakeCount ) d_finalizeBody( f, i );
@@ -646,7 +648,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->shapeEnlarged, dw->contacts, dw->colorIds,	dw->lanes,		dw->joints,		  dw->tree[0],
 					  dw->tree[1],	  dw->tree[2], dw->treeRaw[0], dw->treeRaw[1], dw->treeRaw[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  
 					  dw->moveStage, dw->pairPacked, dw->pairOffsets, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
-					  dw->enlargedBoxes, dw->counters, dw->persistentScratch };
+					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList };
 	b2gDev_CompFree( &dw->comp );
 	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
 		if ( dptrs[i] ) cudaFree( dptrs[i] );
@@ -980,6 +982,23 @@ extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, 
 	return 0;
 }
 
+extern "C" int b2gDev_LastCounters( b2gDeviceWorld* dw, b2gStepCounters* out )
+{
+	*out = *dw->hCounters;
+	return 0;
+}
+
+extern "C" int b2gDev_UploadJointPartners( b2gDeviceWorld* dw, const int* offsets, int bodyCount, const int* list, int listCount )
+{
+	dw->partnerCount = listCount;
+	if ( listCount == 0 ) return 0;
+	CK2( grow( (void**)&dw->partnerOffsets, &dw->partnerOffsetsCap, bodyCount + 1, sizeof( int ) ) );
+	CK2( grow( (void**)&dw->partnerList, &dw->partnerListCap, listCount, sizeof( int ) ) );
+	CK2( uploadTo( dw, dw->partnerOffsets, offsets, (size_t)( bodyCount + 1 ) * sizeof( int ) ) );
+	CK2( uploadTo( dw, dw->partnerList, list, (size_t)listCount * sizeof( int ) ) );
+	return 0;
+}
+
 extern "C" int b2gDev_DownloadJoints( b2gDeviceWorld* dw, b2gJoint* byId, int idCount )
 {
 	int n = dw->jointCount;
@@ -1305,6 +1324,15 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	f.inv_dt = p->inv_dt;
 	f.enableSleep = p->enableSleep;
 	f.enableContinuous = p->enableContinuous;
+	f.ccd.staticTree = dw->tree[b2_staticBody];
+	f.ccd.staticRoot = dw->tree[b2_staticBody] != NULL ? dw->treeRoot[b2_staticBody] : -1;
+	f.ccd.shapes = dw->shapes;
+	f.ccd.xf = dw->xf;
+	f.ccd.center = dw->center;
+	f.ccd.localCenter = dw->localCenter;
+	f.ccd.bodyFlags = dw->bodyFlags;
+	f.ccd.partnerOffsets = dw->partnerCount > 0 ? dw->partnerOffsets : NULL;
+	f.ccd.partnerList = dw->partnerCount > 0 ? dw->partnerList : NULL;
 	int ovJointBegin0 = dw->jointOffsets[B2G_OVERFLOW_INDEX];
 	int ovJointCount0 = dw->jointOffsets[B2_GRAPH_COLOR_COUNT] - ovJointBegin0;
 	int ovCount0 = total - overflowBegin;

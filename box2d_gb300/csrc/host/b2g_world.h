@@ -146,6 +146,7 @@ typedef struct h_world
 	H_ARRAY( b2gContactInit ) pendingInits;
 	h_intArray pendingKills;
 	int lastStatus;
+	int continuousSweeps, continuousHits; /* accumulated device continuous-collision counters */
 	void* rebuildWorker; /* host thread for the tree rebuild (step.c) */
 } h_world;
 

@@ -91,6 +91,15 @@ B2P_EXPORT int b2p_status( uint32_t packedWorldId )
 	return w == NULL ? -1 : w->lastStatus;
 }
 
+/* continuous collision of one world since its creation: fast bodies swept, sweeps that hit */
+B2P_EXPORT void b2p_continuous_counts( uint32_t packedWorldId, int* out )
+{
+	b2WorldId id = { (uint16_t)( packedWorldId >> 16 ), (uint16_t)( packedWorldId & 0xFFFF ) };
+	h_world* w = h_worldFromId( id );
+	out[0] = w == NULL ? 0 : w->continuousSweeps;
+	out[1] = w == NULL ? 0 : w->continuousHits;
+}
+
 /* accumulated device stage times (ms: pairs, narrowphase, solver, finalize) and
    host<->device traffic (bytes: to device, to host) and the number of kernels launched since the last reset */
 B2P_EXPORT int b2p_timings( uint32_t packedWorldId, float* stageMs, long long* traffic, int reset )

@@ -240,9 +240,44 @@ static void h_uploadColors( h_world* w )
 	w->colorsDirty = 0;
 }
 
+/* per body, the bodies joined to it by a joint that does not collide its bodies: the
+   continuous sweep skips those pairs as b2ShouldBodiesCollide (body.c:2076-2112) does */
+static void h_uploadJointPartners( h_world* w )
+{
+	int bodyCount = w->bodies.count;
+	int* offsets = malloc( (size_t)( bodyCount + 1 ) * sizeof( int ) );
+	int total = 0;
+	for ( int i = 0; i < bodyCount; ++i )
+	{
+		offsets[i] = total;
+		for ( int key = w->bodies.data[i].headJointKey; key != B2_NULL_INDEX; )
+		{
+			const h_joint* j = w->joints.data + ( key >> 1 );
+			if ( j->collideConnected == 0 ) total += 1;
+			key = j->edges[key & 1].nextKey;
+		}
+	}
+	offsets[bodyCount] = total;
+	int* list = malloc( (size_t)( total > 0 ? total : 1 ) * sizeof( int ) );
+	for ( int i = 0, n = 0; i < bodyCount; ++i )
+	{
+		for ( int key = w->bodies.data[i].headJointKey; key != B2_NULL_INDEX; )
+		{
+			const h_joint* j = w->joints.data + ( key >> 1 );
+			if ( j->collideConnected == 0 ) list[n++] = j->edges[( key & 1 ) ^ 1].bodyId;
+			key = j->edges[key & 1].nextKey;
+		}
+	}
+	int rc = b2gDev_UploadJointPartners( w->dev, offsets, bodyCount, list, total );
+	free( offsets );
+	free( list );
+	if ( rc != 0 ) h_fail( w, "joint partner upload", rc );
+}
+
 static void h_uploadJoints( h_world* w )
 {
 	if ( w->jointsDirty == 0 ) return;
+	h_uploadJointPartners( w );
 	/* the host records must carry the device's accumulated impulses before the re-upload */
 	h_syncJointsFromDevice( w );
 	int offsets[B2_GRAPH_COLOR_COUNT + 1];
@@ -429,6 +464,8 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 		w->stepIndex += 1;
 		h_uploadColors( w );
 		h_uploadJoints( w );
+		/* fast bodies sweep against the static tree in the finalize stage */
+		if ( w->enableContinuous ) h_uploadTree( w, b2_staticBody );
 		int activeColors[B2_GRAPH_COLOR_COUNT];
 		int contactCounts[B2_GRAPH_COLOR_COUNT];
 		int jointCounts[B2_GRAPH_COLOR_COUNT];
@@ -455,6 +492,12 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 			h_joinRebuild( w );
 			h_lap( w, H_PHASE_TREE_REBUILD, &lap );
 			w->lastStatus = status;
+			{
+				b2gStepCounters sc;
+				b2gDev_LastCounters( w->dev, &sc );
+				w->continuousSweeps += sc.continuousSweeps;
+				w->continuousHits += sc.continuousHits;
+			}
 			if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
 			h_enlargeProxies( w, recs, boxes, enlargedCount );
 			h_lap( w, H_PHASE_ENLARGE, &lap );

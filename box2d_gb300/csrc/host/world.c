@@ -539,6 +539,17 @@ void h_ensureDevice( h_world* w )
 		d->restitution = s->material.restitution;
 		d->rollingResistance = s->material.rollingResistance;
 		d->tangentSpeed = s->material.tangentSpeed;
+		d->categoryBits = s->filter.categoryBits;
+		d->maskBits = s->filter.maskBits;
+		d->groupIndex = s->filter.groupIndex;
+		d->isSensor = s->isSensor;
+		{
+			b2Vec2 centroid = h_getShapeCentroid( s );
+			float minExtent, maxExtent;
+			h_computeShapeExtent( s, centroid, &minExtent, &maxExtent );
+			d->ccdCentroid = centroid;
+			d->ccdCoreRadius = 0.25f * minExtent;
+		}
 		aabbs[4 * i] = s->aabb.lowerBound.x;
 		aabbs[4 * i + 1] = s->aabb.lowerBound.y;
 		aabbs[4 * i + 2] = s->aabb.upperBound.x;

@@ -50,6 +50,11 @@ int b2p_host_profile( uint32_t packedWorldId, float* out, int reset );
 /* The CUDA stream (cudaStream_t) the world's kernels are launched on. */
 void* b2p_stream( uint32_t packedWorldId );
 
+/* Continuous collision of one world since its creation: out[0] = fast non-bullet bodies
+   swept against static shapes, out[1] = sweeps that moved the body back to a time of
+   impact (solver.c:384-550). */
+void b2p_continuous_counts( uint32_t packedWorldId, int* out );
+
 /* Scene builders (box2d_gb300/scenes/scenes.c). kind: 0 large pyramid, 1 many pyramids
    with rain, 2 joint grid with mixed shapes, 3 one batched world, 4 one ramp world,
    5 reference many_pyramids, 6 reference joint_grid, 7 hello world, 8 shape zoo,

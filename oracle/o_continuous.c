@@ -11,8 +11,6 @@
 #include <float.h>
 
 int o_continuousSkipped = 0;
-int o_continuousCalls = 0; /* fast bodies swept */
-int o_continuousHits = 0;  /* sweeps that ended early at a time of impact */
 
 typedef struct o_proxy
 {
@@ -691,7 +689,7 @@ void o_solveContinuous( o_world* w, int simIndex )
 		__atomic_fetch_add( &o_continuousSkipped, 1, __ATOMIC_RELAXED );
 		return;
 	}
-	__atomic_fetch_add( &o_continuousCalls, 1, __ATOMIC_RELAXED );
+	__atomic_fetch_add( &w->continuousSweeps, 1, __ATOMIC_RELAXED );
 	b2Vec2 base = fastSim->center0;
 	o_continuousContext c;
 	memset( &c, 0, sizeof( c ) );
@@ -719,7 +717,7 @@ void o_solveContinuous( o_world* w, int simIndex )
 	}
 	if ( c.fraction < 1.0f )
 	{
-		__atomic_fetch_add( &o_continuousHits, 1, __ATOMIC_RELAXED );
+		__atomic_fetch_add( &w->continuousHits, 1, __ATOMIC_RELAXED );
 		b2Rot q = o_nlerp( c.sweep.q1, c.sweep.q2, c.fraction );
 		b2Vec2 cc = o_lerp( c.sweep.c1, c.sweep.c2, c.fraction );
 		b2Vec2 origin = o_sub( cc, o_rotate( q, c.sweep.localCenter ) );

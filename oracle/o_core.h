@@ -650,6 +650,7 @@ typedef struct o_world
 	int recycledContactCount;
 	b2Profile profile;
 	o_bitSet contactStateBits, enlargedSimBits;
+	int continuousSweeps, continuousHits; /* fast bodies swept; sweeps that ended at a time of impact */
 } o_world;
 
 o_world* o_getWorld( int index );

@@ -71,14 +71,14 @@ B2P_EXPORT int b2p_contact_floats( uint32_t packedWorldId, float* out, int capac
 }
 
 extern int o_continuousSkipped;
-extern int o_continuousCalls;
-extern int o_continuousHits;
 
-/* continuous collision since the library was loaded: fast bodies swept, sweeps that hit */
-B2P_EXPORT void b2p_oracle_ccd_counts( int* out )
+/* continuous collision of one world since its creation: fast bodies swept, sweeps that hit */
+B2P_EXPORT void b2p_continuous_counts( uint32_t packedWorldId, int* out )
 {
-	out[0] = o_continuousCalls;
-	out[1] = o_continuousHits;
+	b2WorldId id = { (uint16_t)( packedWorldId >> 16 ), (uint16_t)( packedWorldId & 0xFFFF ) };
+	o_world* w = o_worldFromId( id );
+	out[0] = w->continuousSweeps;
+	out[1] = w->continuousHits;
 }
 
 /* number of fast-body continuous steps the oracle could not restate (0 when exact) */

@@ -41,3 +41,15 @@ def test_oracle_threads_do_not_change_results(oracle, name):
                 assert f"{s.state_hash():016x}" == expected, f"{name}: step {k}"
     finally:
         oracle.b2o_set_threads(1)
+
+
+@pytest.mark.parametrize("name", ["shape_zoo_200_continuous", "batch_world_continuous"])
+def test_continuous_fixtures_exercise_time_of_impact(oracle, name):
+    """The continuous-collision fixtures are not vacuous: fast bodies are swept and some
+    sweeps end at a time of impact before the fixture's last step."""
+    g = load_golden(name)
+    assert g["flags"] & B.NO_CONTINUOUS == 0
+    with B.Scene(oracle, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
+        s.step(len(g["state_hashes"]), g["dt"], g["substeps"])
+        sweeps, hits = s.continuous_counts()
+    assert sweeps > 0 and hits > 0, (sweeps, hits)
