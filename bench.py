@@ -44,12 +44,12 @@ START_STEPS = {"many_pyramids": 200, "large_pyramid": 0, "joint_grid": 0, "batch
 
 WORKLOADS = {
     # name: (kind, a, b, c, seed, flags, description)
-    "many_pyramids": (B.MANY_PYRAMIDS_RAIN, 20, 10, 2000, 0, B.NO_CONTINUOUS,
+    "many_pyramids": (B.MANY_PYRAMIDS_RAIN, 20, 10, 2000, 0, 0,
                       "20x20 grid of 10-row pyramids of 0.5 m boxes + 2000 rain circles"),
     "large_pyramid": (B.LARGE_PYRAMID, 100, 1, 0, 0, 0, "100-row pyramid of 5050 boxes on a 200 m segment"),
-    "joint_grid": (B.JOINT_GRID_MIXED, 100, 3000, 0, 0, B.NO_CONTINUOUS,
+    "joint_grid": (B.JOINT_GRID_MIXED, 100, 3000, 0, 0, 0,
                    "100x100 revolute circle grid + 3000 mixed shapes"),
-    "batch_worlds": (B.BATCH_WORLD, 0, 0, 0, 12345, B.NO_CONTINUOUS,
+    "batch_worlds": (B.BATCH_WORLD, 0, 0, 0, 12345, 0,
                      "independent worlds of 10-400 boxes, circles and capsules in a 3-segment container"),
 }
 
@@ -203,7 +203,7 @@ def run_batch(args) -> dict:
     torch.cuda.set_device(0)
     lib = B.load_library()
     n = args.worlds
-    scenes = [B.Scene(lib, B.BATCH_WORLD, 0, 0, 0, 12345 + i, B.NO_CONTINUOUS) for i in range(n)]
+    scenes = [B.Scene(lib, B.BATCH_WORLD, 0, 0, 0, 12345 + i, 0) for i in range(n)]
     handles = (ctypes.c_int * n)(*[s.handle for s in scenes])
     dyn = sum(s.dynamic_count for s in scenes)
     threads = args.threads if args.threads > 0 else 4 * max(1, os.cpu_count() or 1)

@@ -30,6 +30,8 @@ SHAPE_ZOO = 8
 JOINT_ZOO = 9
 
 NO_CONTINUOUS = 1
+NO_WARM_STARTING = 2
+NO_RECYCLING = 4
 
 
 def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
@@ -58,6 +60,19 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2p_host_profile": (c_int, [c_u32, c_p, c_int]),
         "b2p_contacts_noalloc": (c_int, [c_u32, c_p, c_int]),
         "b2p_continuous_counts": (None, [c_u32, c_p]),
+        "b2s_set_friction": (None, [c_int, c_p, c_int]),
+        "b2s_get_friction": (None, [c_int, c_p, c_int]),
+        "b2s_get_centers": (None, [c_int, c_p]),
+        "b2s_body_ids": (None, [c_int, c_p]),
+        "b2Diff_CreateTape": (c_p, [c_p, c_int]),
+        "b2Diff_DestroyTape": (None, [c_p]),
+        "b2Diff_Record": (None, [c_p, ctypes.c_bool]),
+        "b2Diff_StepCount": (c_int, [c_p]),
+        "b2Diff_Backward": (c_int, [c_p, c_p, c_p, c_p, c_p, c_p, c_p]),
+        "b2Diff_Sizes": (None, [c_p, c_p, c_p]),
+        "b2Diff_LastBackwardMs": (c_f, [c_p, c_p]),
+        "b2Diff_LastFailure": (None, [c_p, c_p]),
+        "b2Diff_DownloadTape": (ctypes.c_longlong, [c_p, c_int, c_p, ctypes.c_longlong]),
     }
     for name, (res, args) in optional.items():
         if hasattr(lib, name):

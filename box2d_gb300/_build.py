@@ -20,12 +20,13 @@ BUILD = PKG / "_build"
 LIB = PKG / "libbox2d_gb300.so"
 
 HOST_SOURCES = ["csrc/host/world.c", "csrc/host/step.c", "csrc/host/joint.c", "csrc/host/tree.c",
-                "csrc/host/geometry.c", "csrc/host/probe.c", "csrc/host/batch.c", "scenes/scenes.c"]
+                "csrc/host/geometry.c", "csrc/host/probe.c", "csrc/host/batch.c", "csrc/host/diff.c", "scenes/scenes.c"]
 # (source, extra nvcc flags). The cluster and persistent solvers read state written by
 # other SMs between barriers, so their global loads bypass L1 (-dlcm=cg).
 DEVICE_SOURCES = [("csrc/device/world.cu", []), ("csrc/device/components.cu", []),
                   ("csrc/device/cluster.cu", ["-Xptxas", "-dlcm=cg"]), ("csrc/device/noalloc.cu", []),
-                  ("csrc/device/persistent.cu", ["-Xptxas", "-dlcm=cg"])]
+                  ("csrc/device/persistent.cu", ["-Xptxas", "-dlcm=cg"]),
+                  ("csrc/device/adjoint.cu", [])]
 
 NVCC_FLAGS = ["-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "--fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false", "-Xcompiler", "-fPIC",
@@ -59,7 +60,7 @@ def build_library(force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     nvcc = _nvcc()
     include = ["-I", str(ROOT / "include")]
-    headers = list((PKG / "csrc").rglob("*.h")) + list((PKG / "csrc").rglob("*.cuh")) + [ROOT / "include" / "box2d_gb300.h"]
+    headers = list((PKG / "csrc").rglob("*.h")) + list((PKG / "csrc").rglob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     jobs = []
     objects = []
     for src in HOST_SOURCES:
@@ -84,7 +85,7 @@ def build_library(force: bool = False) -> Path:
 
 def build_oracle(with_reference: bool = True) -> None:
     """Build the CPU oracle and, where the reference sources exist, the reference itself."""
-    _run(["make", "-s", "-C", str(ROOT / "oracle"), "liboracle.so"])
+    _run(["make", "-s", "-C", str(ROOT / "oracle"), "liboracle.so", "libtangent.so"])
     ref = Path(os.environ.get("B2G_REFERENCE_DIR", "/root/reference"))
     if with_reference and (ref / "src").is_dir():
         _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={ref}"])

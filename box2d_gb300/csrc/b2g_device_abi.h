@@ -180,6 +180,77 @@ enum
 	B2G_STATUS_CAPACITY = 2,
 };
 
+/* ---- tape of differentiable stepping (box2d_gb300_diff.h) ----
+   One world's recording, as b2Diff_DownloadTape returns it: a b2gTapeHeader, the world's
+   shapes (b2gShape[shapeCount]), then stepCount step records. A step record is a
+   b2gTapeStep followed by b2gTapeBody[bodyCount] (by body id), float[8 * awakeCount]
+   (integration parameters by awake index, as the solver's), float[awakeCount] (time-of-
+   impact fraction of the step's continuous sweep, 1 = none), int[slotCount] (contact id of
+   each colored slot) and b2gContact[slotCount] (each contact after the narrowphase, in slot
+   order); every part starts on a 16-byte boundary. */
+typedef struct b2gTapeHeader
+{
+	int stepCount, shapeCount, bodyCount, contactCapacity;
+	long long stepOffsets[1]; /* stepCount entries: byte offset of each step from the header */
+} b2gTapeHeader;
+
+typedef struct b2gTapeBody
+{
+	b2Transform xf; /* pose at the start of the step */
+	b2Vec2 center;
+	b2Vec2 localCenter;
+	float vx, vy, w; /* velocity at the start of the step (awake bodies) */
+	uint32_t flags;	 /* state flags (awake bodies) */
+	int awakeIndex;	 /* -1: not awake */
+	int type;
+} b2gTapeBody;
+
+typedef struct b2gTapeStep
+{
+	b2gStepParams params;
+	int bodyCount, awakeCount, slotCount, jointCount;
+	int colorOffsets[B2_GRAPH_COLOR_COUNT + 1];
+	int bytes; /* the whole record */
+	int pad[2];
+} b2gTapeStep;
+
+/* contact sim flag of a contact whose manifold was recycled this step (physics_world.c:508-560) */
+#define B2G_S_RECYCLED 0x800000
+
+#ifdef __CUDACC__
+#define B2G_TAPE_FN static inline __host__ __device__
+#else
+#define B2G_TAPE_FN static inline
+#endif
+
+B2G_TAPE_FN long long b2gTapeAlign( long long x ) { return ( x + 15 ) & ~15LL; }
+
+/* byte offsets of a step record's parts */
+B2G_TAPE_FN long long b2gTapeBodiesOffset( void ) { return b2gTapeAlign( (long long)sizeof( b2gTapeStep ) ); }
+B2G_TAPE_FN long long b2gTapeParamsOffset( int bodyCount )
+{
+	return b2gTapeBodiesOffset() + b2gTapeAlign( (long long)bodyCount * (long long)sizeof( b2gTapeBody ) );
+}
+/* time-of-impact fraction of each awake body's continuous sweep (1: the body advanced to
+   its solved pose), written by the step's finalize */
+B2G_TAPE_FN long long b2gTapeToiOffset( int bodyCount, int awakeCount )
+{
+	return b2gTapeParamsOffset( bodyCount ) + b2gTapeAlign( 32LL * awakeCount );
+}
+B2G_TAPE_FN long long b2gTapeIdsOffset( int bodyCount, int awakeCount )
+{
+	return b2gTapeToiOffset( bodyCount, awakeCount ) + b2gTapeAlign( 4LL * awakeCount );
+}
+B2G_TAPE_FN long long b2gTapeContactsOffset( int bodyCount, int awakeCount, int slotCount )
+{
+	return b2gTapeIdsOffset( bodyCount, awakeCount ) + b2gTapeAlign( 4LL * slotCount );
+}
+B2G_TAPE_FN long long b2gTapeStepBytes( int bodyCount, int awakeCount, int slotCount )
+{
+	return b2gTapeContactsOffset( bodyCount, awakeCount, slotCount ) +
+		   b2gTapeAlign( (long long)slotCount * (long long)sizeof( b2gContact ) );
+}
+
 typedef struct b2gDeviceWorld b2gDeviceWorld;
 
 /* lifetime */
@@ -279,6 +350,33 @@ int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* params, const int* ac
 int b2gDev_Synchronize( b2gDeviceWorld* dw );
 void b2gDev_Timings( b2gDeviceWorld* dw, float* stageMs, long long* traffic, int reset );
 void* b2gDev_Stream( b2gDeviceWorld* dw );
+
+/* ---- differentiable stepping (adjoint.cu) ---- */
+/* append one step record (the state after the narrowphase, before the solver) to a device
+   arena that grows stream-ordered; *offset receives the record's offset in the arena */
+int b2gDev_CaptureTape( b2gDeviceWorld* dw, const b2gStepParams* params, int bodyCount, int awakeCount, int jointCount,
+						void** arena, long long* capacity, long long* used, long long* offset );
+void b2gDev_FreeTapeArena( void* arena );
+const b2gShape* b2gDev_ShapeArray( b2gDeviceWorld* dw, int* count );
+int b2gDev_ContactCapacity( b2gDeviceWorld* dw );
+
+typedef struct b2gAdjointWorld
+{
+	const void* arena;			   /* device tape arena of the world */
+	const long long* stepOffsets; /* host: offset of each step record in the arena */
+	const b2gShape* shapes;		   /* device shapes */
+	int shapeCount, bodyCount, contactCapacity;
+	int maxAwake, maxSlots, maxSubsteps; /* largest awake, slot and substep counts over the steps */
+} b2gAdjointWorld;
+
+/* reverse pass over stepCount recorded steps of every world (see box2d_gb300_diff.h for
+   the host arrays); returns 0, a negative B2_DIFF_* code or a CUDA error. failure (5 ints,
+   may be NULL) receives the first failing world's code, world, step, check and item. */
+int b2gDev_AdjointRun( const b2gAdjointWorld* worlds, int worldCount, int stepCount, const int* bodyOffsets,
+					   const int* shapeOffsets, const float* adjCenter, const float* adjRotation, const float* adjVelocity,
+					   float* gradVelocity, float* gradCenter, float* gradFriction, float* ms, int* launches,
+					   int* failure );
+int b2gDev_DownloadArena( const void* arena, long long bytes, void* out );
 
 #ifdef __cplusplus
 }

@@ -409,6 +409,7 @@ struct d_finalizeArgs
 	float dt, inv_dt;
 	int enableSleep, enableContinuous;
 	d_ccdWorld ccd; /* static tree and filters for the continuous sweep */
+	float* toi;		/* when recording: time-of-impact fraction per awake body (1 = none) */
 };
 
 /* solver.c:384-550 b2SolveContinuous for a fast non-bullet body: sweep every non-sensor
@@ -447,6 +448,7 @@ static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, 
 	if ( fraction < 1.0f )
 	{
 		atomicAdd( &a.counters->continuousHits, 1 );
+		if ( a.toi != nullptr ) a.toi[simIndex] = fraction;
 		b2Rot qt = d_nlerp( sweep.q1, sweep.q2, fraction );
 		b2Vec2 ct = d_lerp( sweep.c1, sweep.c2, fraction );
 		b2Vec2 origin = d_sub( ct, d_rotate( qt, sweep.localCenter ) );
@@ -553,6 +555,7 @@ static __device__ void d_finalizeBody( const d_finalizeArgs& a, int simIndex )
 		}
 	}
 	a.bodyFlags[bodyId] = bodyFlags;
+	if ( a.toi != nullptr ) a.toi[simIndex] = 1.0f;
 	int start = a.shapeStart[bodyId], count = a.shapeCount[bodyId];
 	bool anyEnlarged = false;
 	if ( sweep ) anyEnlarged = d_solveContinuous( a, simIndex, bodyId, center, q );

@@ -99,6 +99,7 @@ struct b2gDeviceWorld
 	int* partnerList;
 	int partnerOffsetsCap, partnerListCap;
 	int partnerCount; /* 0: no such joint */
+	float* tapeToi;	  /* time-of-impact slot of the step being recorded, consumed by the next solve */
 	/* broadphase */
 	b2gTreeNode* tree[3];
 	int treeCap[3], treeRoot[3];
@@ -377,6 +378,7 @@ __global__ void k_collide( d_collideArgs a )
 	b2gContact* cs = a.contacts + contactId;
 	uint32_t simFlags = cs->simFlags;
 	if ( ( simFlags & B2G_S_LIVE ) == 0 ) return;
+	simFlags &= ~(uint32_t)B2G_S_RECYCLED;
 	float recycleDistance = a.recycleDistance;
 	float recycleNonTouching = d_min( recycleDistance, D_SPECULATIVE_DISTANCE );
 	int shapeIdA = cs->shapeIdA, shapeIdB = cs->shapeIdB;
@@ -436,6 +438,8 @@ __global__ void k_collide( d_collideArgs a )
 				mp->separation = mp->baseSeparation + d_dot( dp, normal );
 				mp->persisted = true;
 			}
+			/* marks the manifold as carried over for the differentiable tape */
+			cs->simFlags = simFlags | B2G_S_RECYCLED;
 			atomicAdd( &a.counters->recycledContactCount, 1 );
 			return;
 		}
@@ -982,6 +986,124 @@ extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, 
 	return 0;
 }
 
+/* ======================= tape capture (differentiable stepping) ======================= */
+struct d_colorOffsets
+{
+	int v[B2_GRAPH_COLOR_COUNT + 1];
+};
+
+/* one step record: header, every body's pose and velocity, integration parameters, and the
+   colored contacts in slot order as the narrowphase left them */
+__global__ void k_captureTape( unsigned char* rec, b2gStepParams params, d_colorOffsets offsets, int bodyCount, int awakeCount,
+							   int slotCount, int jointCount, const float4* __restrict__ xf, const float2* __restrict__ center,
+							   const float2* __restrict__ localCenter, const int* __restrict__ awakeIndex,
+							   const int* __restrict__ bodyType, const float4* __restrict__ sv, const float* __restrict__ bodyParams,
+							   const int* __restrict__ colorIds, const b2gContact* __restrict__ contacts )
+{
+	int t = blockIdx.x * blockDim.x + threadIdx.x;
+	int nt = gridDim.x * blockDim.x;
+	if ( t == 0 )
+	{
+		b2gTapeStep h;
+		memset( &h, 0, sizeof( h ) );
+		h.params = params;
+		h.bodyCount = bodyCount;
+		h.awakeCount = awakeCount;
+		h.slotCount = slotCount;
+		h.jointCount = jointCount;
+		for ( int i = 0; i <= B2_GRAPH_COLOR_COUNT; ++i ) h.colorOffsets[i] = offsets.v[i];
+		h.bytes = (int)b2gTapeStepBytes( bodyCount, awakeCount, slotCount );
+		*(b2gTapeStep*)rec = h;
+	}
+	b2gTapeBody* bodies = (b2gTapeBody*)( rec + b2gTapeBodiesOffset() );
+	for ( int i = t; i < bodyCount; i += nt )
+	{
+		b2gTapeBody b;
+		float4 x = xf[i];
+		float2 c = center[i], lc = localCenter[i];
+		b.xf.p = d_v( x.x, x.y );
+		b.xf.q = b2Rot{ x.z, x.w };
+		b.center = d_v( c.x, c.y );
+		b.localCenter = d_v( lc.x, lc.y );
+		int ai = awakeIndex[i];
+		b.awakeIndex = ai;
+		b.type = bodyType[i];
+		if ( ai >= 0 )
+		{
+			float4 v = sv[ai];
+			b.vx = v.x;
+			b.vy = v.y;
+			b.w = v.z;
+			b.flags = __float_as_uint( v.w );
+		}
+		else
+		{
+			b.vx = 0.0f;
+			b.vy = 0.0f;
+			b.w = 0.0f;
+			b.flags = 0;
+		}
+		bodies[i] = b;
+	}
+	float* pr = (float*)( rec + b2gTapeParamsOffset( bodyCount ) );
+	for ( int i = t; i < 8 * awakeCount; i += nt ) pr[i] = bodyParams[i];
+	float* toi = (float*)( rec + b2gTapeToiOffset( bodyCount, awakeCount ) );
+	for ( int i = t; i < awakeCount; i += nt ) toi[i] = 1.0f;
+	int* ids = (int*)( rec + b2gTapeIdsOffset( bodyCount, awakeCount ) );
+	b2gContact* cs = (b2gContact*)( rec + b2gTapeContactsOffset( bodyCount, awakeCount, slotCount ) );
+	for ( int s = t; s < slotCount; s += nt )
+	{
+		int id = colorIds[s];
+		ids[s] = id;
+		cs[s] = contacts[id];
+	}
+}
+
+extern "C" int b2gDev_CaptureTape( b2gDeviceWorld* dw, const b2gStepParams* p, int bodyCount, int awakeCount, int jointCount,
+								   void** arena, long long* capacity, long long* used, long long* offset )
+{
+	int slotCount = dw->colorOffsets[B2_GRAPH_COLOR_COUNT];
+	long long bytes = b2gTapeStepBytes( bodyCount, awakeCount, slotCount );
+	if ( *used + bytes > *capacity )
+	{
+		long long cap = *capacity > 0 ? *capacity : ( 1LL << 20 );
+		while ( cap < *used + bytes ) cap *= 2;
+		void* grown = NULL;
+		CK( cudaMallocAsync( &grown, (size_t)cap, dw->stream ) );
+		if ( *used > 0 ) CK( cudaMemcpyAsync( grown, *arena, (size_t)*used, cudaMemcpyDeviceToDevice, dw->stream ) );
+		if ( *arena != NULL ) CK( cudaFreeAsync( *arena, dw->stream ) );
+		*arena = grown;
+		*capacity = cap;
+	}
+	d_colorOffsets offsets;
+	memcpy( offsets.v, dw->colorOffsets, sizeof( offsets.v ) );
+	int n = bodyCount > slotCount ? bodyCount : slotCount;
+	n = n > 8 * awakeCount ? n : 8 * awakeCount;
+	int grid = blocks( n > 0 ? n : 1 );
+	k_captureTape<<<grid, B2G_THREADS, 0, dw->stream>>>( (unsigned char*)*arena + *used, *p, offsets, bodyCount, awakeCount, slotCount,
+														jointCount, dw->xf, dw->center, dw->localCenter, dw->awakeIndex,
+														dw->bodyType, dw->stateV, dw->params, dw->colorIds, dw->contacts );
+	dw->launches += 1;
+	CK( cudaGetLastError() );
+	*offset = *used;
+	dw->tapeToi = (float*)( (unsigned char*)*arena + *used + b2gTapeToiOffset( bodyCount, awakeCount ) );
+	*used += bytes;
+	return 0;
+}
+
+extern "C" void b2gDev_FreeTapeArena( void* arena )
+{
+	if ( arena != NULL ) cudaFree( arena );
+}
+
+extern "C" const b2gShape* b2gDev_ShapeArray( b2gDeviceWorld* dw, int* count )
+{
+	*count = dw->shapeCountTotal;
+	return dw->shapes;
+}
+
+extern "C" int b2gDev_ContactCapacity( b2gDeviceWorld* dw ) { return dw->contactCap; }
+
 extern "C" int b2gDev_LastCounters( b2gDeviceWorld* dw, b2gStepCounters* out )
 {
 	*out = *dw->hCounters;
@@ -1333,6 +1455,8 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	f.ccd.bodyFlags = dw->bodyFlags;
 	f.ccd.partnerOffsets = dw->partnerCount > 0 ? dw->partnerOffsets : NULL;
 	f.ccd.partnerList = dw->partnerCount > 0 ? dw->partnerList : NULL;
+	f.toi = dw->tapeToi;
+	dw->tapeToi = NULL;
 	int ovJointBegin0 = dw->jointOffsets[B2G_OVERFLOW_INDEX];
 	int ovJointCount0 = dw->jointOffsets[B2_GRAPH_COLOR_COUNT] - ovJointBegin0;
 	int ovCount0 = total - overflowBegin;

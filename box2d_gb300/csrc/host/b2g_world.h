@@ -147,10 +147,14 @@ typedef struct h_world
 	h_intArray pendingKills;
 	int lastStatus;
 	int continuousSweeps, continuousHits; /* accumulated device continuous-collision counters */
+	struct h_tapeWorld* tape;			  /* differentiable-stepping recorder (diff.c), or NULL */
 	void* rebuildWorker; /* host thread for the tree rebuild (step.c) */
 } h_world;
 
 h_world* h_worldFromId( b2WorldId id );
+/* appends the step about to be solved to the world's tape when recording (diff.c) */
+void h_tapeCapture( h_world* w, const b2gStepParams* params );
+void h_tapeDetach( h_world* w );
 h_world* h_worldByIndex( int index );
 
 /* geometry helpers (geometry.c) */

@@ -484,6 +484,7 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 		int enlargedCount = 0, status = 0;
 		if ( w->awakeBodyIds.count > 0 )
 		{
+			if ( w->tape != NULL ) h_tapeCapture( w, &p );
 			h_lap( w, H_PHASE_UPLOADS, &lap );
 			rc = b2gDev_Solve( w->dev, &p, activeColors, activeCount, contactCounts, jointCounts, w->awakeBodyIds.count, &recs,
 							   &enlargedCount, &boxes, &status );

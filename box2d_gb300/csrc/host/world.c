@@ -227,6 +227,7 @@ void b2DestroyWorld( b2WorldId worldId )
 	h_world* w = h_worldFromId( worldId );
 	if ( w == NULL ) return;
 	h_stopRebuildWorker( w );
+	h_tapeDetach( w );
 	b2gDev_Destroy( w->dev );
 	for ( int i = 0; i < 3; ++i )
 	{
@@ -732,15 +733,30 @@ float b2Body_GetMass( b2BodyId bodyId ) { return h_getBody( bodyId )->mass; }
 
 float b2Body_GetRotationalInertia( b2BodyId bodyId ) { return h_getBody( bodyId )->inertia; }
 
-b2Vec2 b2Body_GetLocalCenterOfMass( b2BodyId bodyId ) { return h_getBody( bodyId )->localCenter; }
+b2Vec2 b2Body_GetLocalCenter( b2BodyId bodyId ) { return h_getBody( bodyId )->localCenter; }
 
-b2Pos b2Body_GetWorldCenterOfMass( b2BodyId bodyId )
+b2Pos b2Body_GetWorldCenter( b2BodyId bodyId )
 {
 	h_syncFromDevice( h_worlds + bodyId.world0 );
 	return h_getBody( bodyId )->center;
 }
 
 bool b2Body_IsAwake( b2BodyId bodyId ) { return h_getBody( bodyId )->setIndex == H_AWAKE_SET; }
+
+/* body.c b2Body_GetShapeCount / b2Body_GetShapes: the body's shape list, head first */
+int b2Body_GetShapeCount( b2BodyId bodyId ) { return h_getBody( bodyId )->shapeCount; }
+
+int b2Body_GetShapes( b2BodyId bodyId, b2ShapeId* shapeArray, int capacity )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	int n = 0;
+	for ( int id = h_getBody( bodyId )->headShapeId; id != B2_NULL_INDEX && n < capacity; id = w->shapes.data[id].nextShapeId )
+	{
+		b2ShapeId sid = { id + 1, bodyId.world0, w->shapes.data[id].generation };
+		shapeArray[n++] = sid;
+	}
+	return n;
+}
 
 /* body.c:524-650 */
 static void h_updateBodyMassData( h_world* w, h_body* body )

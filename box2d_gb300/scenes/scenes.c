@@ -74,6 +74,7 @@ typedef struct b2sScene
 	int bodyCount, bodyCapacity;
 	int dynamicCount;
 	float targetX, targetY;
+	int flags; /* creation flags: 1 no continuous, 2 no warm starting, 4 no contact recycling (ramp) */
 } b2sScene;
 
 #define B2S_MAX_SCENES 4096
@@ -403,6 +404,7 @@ static void b2sRampWorld( b2sScene* s, int columns, int rows, b2sRng* rng )
 			bd.linearVelocity.x = b2sRandomNormal( rng, 0.5f );
 			bd.linearVelocity.y = b2sRandomNormal( rng, 0.5f );
 			bd.angularVelocity = b2sRandomNormal( rng, 0.5f );
+			bd.enableContactRecycling = ( s->flags & 4 ) == 0;
 			b2BodyId body = b2CreateBody( s->worldId, &bd );
 			b2sAddBody( s, body, 1 );
 			b2ShapeDef sd = b2DefaultShapeDef();
@@ -724,6 +726,8 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 	s->worldId = b2CreateWorld( &wd );
 	if ( s->worldId.index1 == 0 ) return -1;
 	s->inUse = 1;
+	s->flags = flags;
+	if ( flags & 2 ) b2World_EnableWarmStarting( s->worldId, false );
 	b2sRng rng = { seed ? seed : 12345u };
 	switch ( kind )
 	{
@@ -859,6 +863,50 @@ B2S_EXPORT void b2s_set_velocities( int h, const float* in )
 		b2Body_SetLinearVelocity( s->bodies[i], v );
 		b2Body_SetAngularVelocity( s->bodies[i], in[3 * i + 2] );
 	}
+}
+
+/* friction of every shape on the scene's bodies, indexed by shape id (count entries) */
+B2S_EXPORT void b2s_set_friction( int h, const float* byShape, int count )
+{
+	b2sScene* s = b2s_scenes + h;
+	b2ShapeId ids[16];
+	for ( int i = 0; i < s->bodyCount; ++i )
+	{
+		int n = b2Body_GetShapes( s->bodies[i], ids, 16 );
+		for ( int k = 0; k < n; ++k )
+			if ( ids[k].index1 - 1 < count ) b2Shape_SetFriction( ids[k], byShape[ids[k].index1 - 1] );
+	}
+}
+
+B2S_EXPORT void b2s_get_friction( int h, float* byShape, int count )
+{
+	b2sScene* s = b2s_scenes + h;
+	b2ShapeId ids[16];
+	for ( int i = 0; i < s->bodyCount; ++i )
+	{
+		int n = b2Body_GetShapes( s->bodies[i], ids, 16 );
+		for ( int k = 0; k < n; ++k )
+			if ( ids[k].index1 - 1 < count ) byShape[ids[k].index1 - 1] = b2Shape_GetFriction( ids[k] );
+	}
+}
+
+/* world center of mass of each scene body (2 floats), in the order of b2s_get_state */
+B2S_EXPORT void b2s_get_centers( int h, float* out )
+{
+	b2sScene* s = b2s_scenes + h;
+	for ( int i = 0; i < s->bodyCount; ++i )
+	{
+		b2Pos c = b2Body_GetWorldCenter( s->bodies[i] );
+		out[2 * i] = (float)c.x;
+		out[2 * i + 1] = (float)c.y;
+	}
+}
+
+/* body id of each scene body, in the order of b2s_get_state */
+B2S_EXPORT void b2s_body_ids( int h, int* out )
+{
+	b2sScene* s = b2s_scenes + h;
+	for ( int i = 0; i < s->bodyCount; ++i ) out[i] = s->bodies[i].index1 - 1;
 }
 
 B2S_EXPORT void b2s_target( int h, float* out )

@@ -59,7 +59,8 @@ void b2p_continuous_counts( uint32_t packedWorldId, int* out );
    with rain, 2 joint grid with mixed shapes, 3 one batched world, 4 one ramp world,
    5 reference many_pyramids, 6 reference joint_grid, 7 hello world, 8 shape zoo,
    9 joint zoo (prismatic, weld, wheel, distance and revolute mechanisms).
-   flags bit 0 disables continuous collision. Returns a handle or -1. */
+   flags bit 0 disables continuous collision, bit 1 warm starting, bit 2 contact recycling
+   (ramp scene). Returns a handle or -1. */
 int b2s_create( int kind, int a, int b, int c, uint32_t seed, int flags );
 void b2s_destroy( int handle );
 void b2s_step( int handle, float timeStep, int subStepCount, int count );
@@ -79,6 +80,13 @@ uint64_t b2s_state_hash( int handle );
 void b2s_set_velocities( int handle, const float* in );
 void b2s_target( int handle, float* out );
 void b2s_counters( int handle, int* out );
+/* friction of every shape on the scene's bodies, indexed by shape id (count entries) */
+void b2s_set_friction( int handle, const float* byShape, int count );
+void b2s_get_friction( int handle, float* byShape, int count );
+/* world center of mass of each scene body (2 floats), in the order of b2s_get_state */
+void b2s_get_centers( int handle, float* out );
+/* body id of each scene body, in the order of b2s_get_state */
+void b2s_body_ids( int handle, int* out );
 
 #ifdef __cplusplus
 }

@@ -587,8 +587,8 @@ B2G_API void b2Body_SetLinearVelocity( b2BodyId bodyId, b2Vec2 linearVelocity );
 B2G_API void b2Body_SetAngularVelocity( b2BodyId bodyId, float angularVelocity );
 B2G_API float b2Body_GetMass( b2BodyId bodyId );
 B2G_API float b2Body_GetRotationalInertia( b2BodyId bodyId );
-B2G_API b2Vec2 b2Body_GetLocalCenterOfMass( b2BodyId bodyId );
-B2G_API b2Pos b2Body_GetWorldCenterOfMass( b2BodyId bodyId );
+B2G_API b2Vec2 b2Body_GetLocalCenter( b2BodyId bodyId );
+B2G_API b2Pos b2Body_GetWorldCenter( b2BodyId bodyId );
 B2G_API bool b2Body_IsAwake( b2BodyId bodyId );
 
 /* ---- API: shapes (box2d.h:659-724) ---- */
@@ -598,6 +598,8 @@ B2G_API b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, 
 B2G_API b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon );
 B2G_API void b2Shape_SetFriction( b2ShapeId shapeId, float friction );
 B2G_API float b2Shape_GetFriction( b2ShapeId shapeId );
+B2G_API int b2Body_GetShapeCount( b2BodyId bodyId );
+B2G_API int b2Body_GetShapes( b2BodyId bodyId, b2ShapeId* shapeArray, int capacity );
 
 /* ---- API: joints (box2d.h:760-1100) ---- */
 B2G_API b2DistanceJointDef b2DefaultDistanceJointDef( void );

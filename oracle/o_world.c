@@ -486,13 +486,13 @@ float b2Body_GetMass( b2BodyId bodyId ) { return o_getBody( bodyId )->mass; }
 
 float b2Body_GetRotationalInertia( b2BodyId bodyId ) { return o_getBody( bodyId )->inertia; }
 
-b2Vec2 b2Body_GetLocalCenterOfMass( b2BodyId bodyId )
+b2Vec2 b2Body_GetLocalCenter( b2BodyId bodyId )
 {
 	o_world* w = o_worldByIndex( bodyId.world0 );
 	return o_getBodySim( w, o_getBody( bodyId ) )->localCenter;
 }
 
-b2Pos b2Body_GetWorldCenterOfMass( b2BodyId bodyId )
+b2Pos b2Body_GetWorldCenter( b2BodyId bodyId )
 {
 	o_world* w = o_worldByIndex( bodyId.world0 );
 	return o_getBodySim( w, o_getBody( bodyId ) )->center;
@@ -710,6 +710,21 @@ float b2Shape_GetFriction( b2ShapeId shapeId )
 {
 	o_world* w = o_worldByIndex( shapeId.world0 );
 	return w->shapes.data[shapeId.index1 - 1].material.friction;
+}
+
+/* body.c b2Body_GetShapeCount / b2Body_GetShapes: the body's shape list, head first */
+int b2Body_GetShapeCount( b2BodyId bodyId ) { return o_getBody( bodyId )->shapeCount; }
+
+int b2Body_GetShapes( b2BodyId bodyId, b2ShapeId* shapeArray, int capacity )
+{
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	int n = 0;
+	for ( int id = o_getBody( bodyId )->headShapeId; id != B2_NULL_INDEX && n < capacity; id = w->shapes.data[id].nextShapeId )
+	{
+		b2ShapeId sid = { id + 1, bodyId.world0, w->shapes.data[id].generation };
+		shapeArray[n++] = sid;
+	}
+	return n;
 }
 
 /* ---------------- contacts (contact.c:214-501) ---------------- */

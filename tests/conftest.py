@@ -40,6 +40,24 @@ def oracle():
     return B.load_library(ORACLE_LIB)
 
 
+TANGENT_LIB = ROOT / "oracle" / "libtangent.so"
+
+
+@pytest.fixture(scope="session")
+def tangent():
+    """The FP64 tangent-linear checker of the adjoint (test checker only), built on demand."""
+    import ctypes
+
+    if not TANGENT_LIB.exists():
+        import box2d_gb300._build as bld
+        bld.build_oracle(with_reference=False)
+    lib = ctypes.CDLL(str(TANGENT_LIB))
+    c_p = ctypes.c_void_p
+    lib.b2t_tangent.restype = ctypes.c_int
+    lib.b2t_tangent.argtypes = [c_p, ctypes.c_longlong, c_p, c_p, c_p, c_p]
+    return lib
+
+
 @pytest.fixture(scope="session")
 def gpu_lib():
     """The GB300 library; fails (does not skip) when it is missing on a GPU run."""

@@ -62,3 +62,8 @@ def test_gpu_continuous_rain(gpu_lib, oracle):
 def test_gpu_continuous_full_many_pyramids(gpu_lib, oracle):
     """Full-size many-pyramids-with-rain scene with continuous collision, 40 steps."""
     _lockstep_continuous(gpu_lib, oracle, B.MANY_PYRAMIDS_RAIN, 20, 10, 2000, 0, 40, check_every=10)
+
+
+def test_gpu_continuous_joint_grid_mixed(gpu_lib, oracle):
+    """Revolute circle grid with mixed shapes dropped on it, continuous collision on."""
+    _lockstep_continuous(gpu_lib, oracle, B.JOINT_GRID_MIXED, 30, 200, 0, 9, 120, check_every=5)
