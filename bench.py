@@ -40,7 +40,7 @@ import box2d_gb300 as B  # noqa: E402
 
 # untimed steps before the warm-up: the many-pyramids rain reaches the pyramids after about
 # 150 steps, so the timed window starts where the scene's contact churn does
-START_STEPS = {"many_pyramids": 200, "large_pyramid": 0, "joint_grid": 0, "batch_worlds": 0}
+START_STEPS = {"many_pyramids": 200, "large_pyramid": 0, "joint_grid": 0, "batch_worlds": 0, "diff_batch": 0}
 
 WORKLOADS = {
     # name: (kind, a, b, c, seed, flags, description)
@@ -51,6 +51,9 @@ WORKLOADS = {
                    "100x100 revolute circle grid + 3000 mixed shapes"),
     "batch_worlds": (B.BATCH_WORLD, 0, 0, 0, 12345, 0,
                      "independent worlds of 10-400 boxes, circles and capsules in a 3-segment container"),
+    "diff_batch": (B.RAMP_WORLD, 8, 8, 0, 12345, 0,
+                   "differentiable batch: worlds of 8 x 8 boxes on a 10-30 degree ramp, forward + adjoint "
+                   "(gradient of |final center of mass - target|^2 w.r.t. initial velocities and frictions)"),
 }
 
 
@@ -242,6 +245,70 @@ def run_batch(args) -> dict:
             "e2e_value": dyn * e2e_steps / e2e_s}
 
 
+def run_diff(args) -> dict:
+    """Differentiable batch: `args.worlds` ramp worlds (seed 12345 + index) stepped forward
+    `args.steps` steps with the tape recording (b2World_StepBatch on all host cores), then
+    the adjoint of every recorded step of every world (one launch per step). Wall clock of
+    both halves through the public API, plus the adjoint kernels' device time."""
+    import numpy as np
+
+    import torch
+
+    from box2d_gb300.diff import DiffBatch
+
+    torch.cuda.set_device(0)
+    lib = B.load_library()
+    n = args.worlds
+    threads = args.threads if args.threads > 0 else 4 * max(1, os.cpu_count() or 1)
+    batch = DiffBatch(lib, B.RAMP_WORLD, 8, 8, 0, [12345 + i for i in range(n)])
+    dyn = sum(s.dynamic_count for s in batch.scenes)
+    masks = [np.arange(s.body_count) > 0 for s in batch.scenes]
+    targets = []
+    for s in batch.scenes:
+        t = np.zeros(2, np.float32)
+        lib.b2s_target(s.handle, t.ctypes.data)
+        targets.append(t)
+    v0, f0 = batch.velocities(), batch.friction()
+
+    def forward(steps, record=True):
+        batch.reset()
+        batch.set_velocities(v0)
+        batch.set_friction(f0)
+        t0 = time.perf_counter()
+        batch.step(steps, threads=threads, record=record)
+        return time.perf_counter() - t0
+
+    def backward():
+        cs = batch.centers()
+        grads = []
+        for w, c in enumerate(cs):
+            d = c[masks[w]].astype(np.float64).mean(0) - targets[w]
+            g = np.zeros_like(c)
+            g[masks[w]] = (2.0 * d / masks[w].sum()).astype(np.float32)
+            grads.append(g)
+        t0 = time.perf_counter()
+        gv, _, gf = batch.backward(grads)
+        return time.perf_counter() - t0, gv, gf
+
+    warm_steps = max(1, min(args.steps, 10))
+    for _ in range(args.warmup):
+        forward(warm_steps)
+        backward()
+    plain_s = forward(args.steps, record=False)
+    with ClockSampler(0) as clocks:
+        fwd_s = forward(args.steps)
+        bwd_s, gv, gf = backward()
+    adj_ms, launches = batch.backward_ms()
+    tape_bytes = 0
+    for w in range(min(n, 8)):
+        tape_bytes += len(batch.download_tape(w))
+    tape_bytes = tape_bytes * n / min(n, 8)
+    finite = all(np.isfinite(g).all() for g in gv) and all(np.isfinite(g).all() for g in gf)
+    batch.close()
+    return {"dyn": dyn, "fwd_s": fwd_s, "bwd_s": bwd_s, "plain_s": plain_s, "adj_ms": adj_ms, "launches": launches,
+            "threads": threads, "clocks": clocks.summary, "tape_bytes": tape_bytes, "finite": finite}
+
+
 def run_cpu_sample(args, budget_s: float, max_steps: int) -> dict:
     """The oracle (CPU restatement of the reference step) on the same workload, with its
     data-parallel loops (narrowphase, solver stages, integration, finalize) on every host
@@ -277,12 +344,17 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="many_pyramids", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--worlds", type=int, default=4096, help="world count of the batch_worlds workload")
+    ap.add_argument("--worlds", type=int, default=0,
+                    help="world count of the batch_worlds (default 4096) and diff_batch (default 1024) workloads")
     ap.add_argument("--threads", type=int, default=0, help="host threads of the batch_worlds workload (0: 4 per core)")
     ap.add_argument("--start-step", type=int, default=-1,
                     help="untimed steps before the warm-up (default: per workload)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.worlds <= 0:
+        args.worlds = 1024 if args.workload == "diff_batch" else 4096
+    if args.workload == "diff_batch" and "--steps" not in sys.argv:
+        args.steps = 120
     if args.start_step < 0:
         args.start_step = START_STEPS[args.workload]
 
@@ -307,6 +379,43 @@ def main() -> None:
                 "cpu_baseline": {"value": r["value"], "unit": "body-steps/s", "cores": cores, "kind": "port",
                                  "sample": f"{r['steps']} steps after {args.start_step + args.warmup} untimed steps, C oracle on {cores} threads"},
                 "e2e": {"value": r["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if args.workload == "diff_batch" and args.impl == "gb300":
+        if rank != 0:
+            return
+        r = run_diff(args)
+        total_s = r["fwd_s"] + r["bwd_s"]
+        value = r["dyn"] * args.steps / total_s
+        pk = peaks()
+        achieved = r["tape_bytes"] / (r["adj_ms"] * 1e-3) / 1e9 if r["adj_ms"] > 0 else 0.0
+        cpu = None
+        if not args.no_cpu_baseline:
+            c = run_cpu_sample(args, budget_s=20.0, max_steps=args.steps)
+            cpu = {"value": c["value"], "unit": "body-steps/s (forward only: the reference has no adjoint)",
+                   "cores": c["threads"], "kind": "port",
+                   "sample": f"{c['steps']} forward steps of one ramp world, C oracle on {c['threads']} threads"}
+        config.update({"worlds": args.worlds, "host_threads": r["threads"], "steps_per_pass": args.steps,
+                       "l2": "inputs larger than L2 (every world's tape), no flush",
+                       "timing": "wall clock of the forward pass (recording) and of the adjoint through the public API"})
+        line = {
+            "metric": "body-steps/s", "value": value, "unit": "body-steps/s (forward + adjoint)", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scene builders)", "config": config,
+            "forward": {"seconds": r["fwd_s"], "value": r["dyn"] * args.steps / r["fwd_s"],
+                        "without_recording_seconds": r["plain_s"]},
+            "adjoint": {"seconds": r["bwd_s"], "device_ms": r["adj_ms"], "over_forward": r["bwd_s"] / r["fwd_s"],
+                        "gradients_finite": r["finite"]},
+            "roofline": {"bound": "hbm", "kernel": "k_adjointStep", "achieved": achieved, "peak": pk["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "peak_source": pk["source"], "traffic": None,
+                         "alg_bytes": r["tape_bytes"], "note": "tape bytes read once by the adjoint / its device time"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "read": "final centers of mass and the gradients, through the public API"},
+            "gpu_launches": r["launches"], "clocks": r["clocks"],
+        }
         print(json.dumps(line))
         return
 
