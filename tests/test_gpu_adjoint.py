@@ -147,3 +147,24 @@ def test_adjoint_matches_finite_differences(gpu_lib):
         lm = functional()
         fd = (lp - lm) / (2 * h)
         assert abs(adjoint - fd) <= 2e-2 * max(abs(fd), 1e-3), (adjoint, fd)
+
+
+def test_torch_autograd_function(gpu_lib):
+    """The torch.autograd.Function over the C ABI gives the adjoint's gradients."""
+    torch = pytest.importorskip("torch")
+    from box2d_gb300.diff import make_step_function
+
+    batch, targets = _make(gpu_lib, [31, 32], 4, 4)
+    with batch:
+        v0 = torch.tensor(np.stack(batch.velocities()), requires_grad=True)
+        f0 = torch.tensor(np.stack(batch.friction()), requires_grad=True)
+        StepBatch = make_step_function()
+        centers = StepBatch.apply(v0, f0, batch, 10, 1.0 / 60.0, 4)
+        com = centers[:, 1:].double().mean(1)
+        loss = ((com - torch.tensor(targets)) ** 2).sum()
+        loss.backward()
+        _, gc = _loss_and_grad_centers(batch, targets)
+        gv, _, gf = batch.backward(gc)
+        assert np.allclose(v0.grad.numpy(), np.stack(gv), rtol=1e-5, atol=1e-8)
+        assert np.allclose(f0.grad.numpy(), np.stack(gf), rtol=1e-5, atol=1e-8)
+        assert float(loss) > 0.0
