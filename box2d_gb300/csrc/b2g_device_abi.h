@@ -346,6 +346,29 @@ int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* params, const int* ac
 				  const int* colorContactCounts, const int* colorJointCounts, int awakeCount, const int** outEnlarged,
 				  int* outEnlargedCount, const float** outFatBoxes, int* outStatus );
 
+/* the three waits of a step split in two: issue the work (or record it, see below), then
+   collect the results after the world's wait (b2gDev_Synchronize) or a batch flush */
+int b2gDev_FindPairsIssue( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int count );
+int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int** outCounts, int* outTotal );
+int b2gDev_CollideIssue( b2gDeviceWorld* dw, const b2gStepParams* params, int contactIdCapacity );
+int b2gDev_CollideCollect( b2gDeviceWorld* dw, const int** outChanges, int* outChangeCount, int* outRecycled );
+int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* params, const int* activeColors, int activeColorCount,
+					   int awakeCount );
+int b2gDev_SolveCollect( b2gDeviceWorld* dw, const int** outEnlarged, int* outEnlargedCount, const float** outFatBoxes,
+						 int* outStatus );
+/* whether the world's solve runs as one CTA (the only solve a batch records) */
+int b2gDev_SolveFitsOneBlock( b2gDeviceWorld* dw, int awakeCount );
+
+/* batched stepping: while a world records, its uploads, downloads and kernels are kept;
+   b2gDev_BatchFlush replays the records of many worlds with one launch per kernel kind and
+   position, one upload, one download and one wait */
+typedef struct b2gDevBatch b2gDevBatch;
+int b2gDev_BatchCreate( b2gDevBatch** out );
+void b2gDev_BatchDestroy( b2gDevBatch* batch );
+int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on );
+int b2gDev_BatchFlush( b2gDevBatch* batch, b2gDeviceWorld* const* worlds, int count );
+long long b2gDev_BatchLaunches( b2gDevBatch* batch );
+
 /* bookkeeping for profiles */
 int b2gDev_Synchronize( b2gDeviceWorld* dw );
 void b2gDev_Timings( b2gDeviceWorld* dw, float* stageMs, long long* traffic, int reset );

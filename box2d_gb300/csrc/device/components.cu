@@ -258,13 +258,12 @@ __global__ void k_compScatter( d_solveArgs a, d_compArgs c, int n, int total, in
 #define D_JOINT( x ) ( c.identity ? ( x ) : c.jointList[x] )
 #define D_LOCAL( x ) ( c.identity ? ( x ) : c.localIndex[x] )
 
-__global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a, d_compArgs c, d_jointBodies jb,
-																   b2gStepCounters* counters, int smemBytes )
+static __device__ __forceinline__ void d_solveBin( const d_solveArgs& a, const d_compArgs& c, const d_jointBodies& jb,
+													b2gStepCounters* counters, int smemBytes, const int bin )
 {
 	extern __shared__ float4 s_mem[];
 	__shared__ int s_count[B2_GRAPH_COLOR_COUNT], s_start[B2_GRAPH_COLOR_COUNT + 1], s_fill[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_restitution;
-	const int bin = blockIdx.x;
 	int bb, cb, jbeg, nb, nc, nj;
 	if ( c.identity )
 	{
@@ -408,6 +407,29 @@ __global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a,
 		a.sv[ai] = sv[i];
 		a.sd[ai] = sd[i];
 	}
+}
+
+__global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveBins( d_solveArgs a, d_compArgs c, d_jointBodies jb,
+																   b2gStepCounters* counters, int smemBytes )
+{
+	d_solveBin( a, c, jb, counters, smemBytes, blockIdx.x );
+}
+
+/* one whole world per CTA, for many worlds at once (batched stepping): record r's
+   arguments are at args + offsets[r] */
+struct d_solveBinArgs
+{
+	d_solveArgs a;
+	d_compArgs c;
+	d_jointBodies jb;
+	b2gStepCounters* counters;
+	int smemBytes;
+};
+
+__global__ void __launch_bounds__( B2G_BIN_THREADS ) k_solveWorldBins( const long long* offsets, const unsigned char* args )
+{
+	const d_solveBinArgs& w = *(const d_solveBinArgs*)( args + offsets[blockIdx.x] );
+	d_solveBin( w.a, w.c, w.jb, w.counters, w.smemBytes, 0 );
 }
 
 /* ---------------- global path restricted to big components ---------------- */
@@ -608,6 +630,9 @@ static cudaError_t s_binsConfigured = cudaSuccess;
 static void configureBins( void )
 {
 	s_binsConfigured = cudaFuncSetAttribute( k_solveBins, cudaFuncAttributeMaxDynamicSharedMemorySize, B2G_WORLD_BIN_MAX_BYTES );
+	if ( s_binsConfigured == cudaSuccess )
+		s_binsConfigured =
+			cudaFuncSetAttribute( k_solveWorldBins, cudaFuncAttributeMaxDynamicSharedMemorySize, B2G_WORLD_BIN_MAX_BYTES );
 }
 
 extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets,
@@ -691,6 +716,33 @@ extern "C" int b2gDev_CompSolveBig( b2gCompBuffers* b, const d_solveArgs* a, con
 }
 
 /* a whole world that fits one CTA's shared memory: one bin, no component analysis */
+extern "C" int b2gDev_SolveWorldBinArgs( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
+										 const int* awakeIndex, int bytes, b2gStepCounters* counters, void* out, int* outBytes )
+{
+	if ( bytes > B2G_WORLD_BIN_MAX_BYTES ) return (int)cudaErrorInvalidValue;
+	d_solveBinArgs w;
+	w.a = *a;
+	w.c = compArgs( b, jointOffsets, awakeIndex );
+	w.c.identity = 1;
+	w.jb = *jb;
+	w.counters = counters;
+	w.smemBytes = bytes > 16 ? bytes : 16;
+	if ( out != NULL ) memcpy( out, &w, sizeof( w ) );
+	*outBytes = (int)sizeof( w );
+	return 0;
+}
+
+extern "C" int b2gDev_SolveWorldBinBatch( const long long* offsets, const unsigned char* args, int count, int smemBytes,
+										  cudaStream_t stream )
+{
+	static pthread_once_t s_once = PTHREAD_ONCE_INIT;
+	pthread_once( &s_once, configureBins );
+	CKC( s_binsConfigured );
+	if ( count <= 0 ) return 0;
+	k_solveWorldBins<<<count, B2G_BIN_THREADS, smemBytes > 16 ? smemBytes : 16, stream>>>( offsets, args );
+	return (int)cudaGetLastError();
+}
+
 extern "C" int b2gDev_SolveWorldBin( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
 									 const int* awakeIndex, int bytes, b2gStepCounters* counters, cudaStream_t stream,
 									 long long* launches )

@@ -89,6 +89,14 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 									const int* activeColors, int activeColorCount, int useLists, int bodyCount,
 									cudaStream_t stream, long long* launches );
 
+/* the arguments of the one-CTA world solve, for a batched launch (out may be NULL to get
+   the size), and the batched launch itself: CTA r solves the world whose arguments are at
+   args + offsets[r] */
+extern "C" int b2gDev_SolveWorldBinArgs( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
+										 const int* awakeIndex, int bytes, b2gStepCounters* counters, void* out, int* outBytes );
+extern "C" int b2gDev_SolveWorldBinBatch( const long long* offsets, const unsigned char* args, int count, int smemBytes,
+										  cudaStream_t stream );
+
 /* one CTA solves the whole world (bytes = its shared-memory weight, at most
    B2G_WORLD_BIN_MAX_BYTES); no analysis, no lists */
 extern "C" int b2gDev_SolveWorldBin( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,

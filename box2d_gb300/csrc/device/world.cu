@@ -21,6 +21,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <vector>
+
 #define B2G_THREADS 128
 #define B2G_PAIR_STACK 256
 
@@ -37,9 +39,56 @@ enum
 	B2G_SOLVER_PERSISTENT = 2,
 };
 
+/* device work of one world recorded instead of issued (batched stepping): uploads carry
+   their bytes, kernels their argument blocks; b2gDev_BatchFlush replays the records of
+   many worlds with one launch per kernel kind and level */
+enum
+{
+	D_OP_H2D = 0,
+	D_OP_D2H = 1,
+	D_OP_MEMSET = 2,
+	D_OP_KERNEL = 3,
+	D_OP_D2D = 4, /* device copy: dev <- host (a device address here) */
+};
+
+enum
+{
+	DK_MARK_MOVED = 0,
+	DK_FIND_PAIRS,
+	DK_PACK_PAIRS,
+	DK_CONVERT_TREE,
+	DK_INIT_CONTACTS,
+	DK_KILL_CONTACTS,
+	DK_COLLIDE,
+	DK_FINALIZE,
+	DK_CAPTURE,
+	DK_SOLVE_BIN,
+	DK_COUNT
+};
+
+struct d_deferredOp
+{
+	int kind, kernel;
+	void* dev;		 /* upload/memset destination, download source */
+	void* host;		 /* download destination */
+	long long bytes; /* copy/memset size; kernel argument size */
+	long long at;	 /* offset of the upload bytes / kernel arguments in the world's records */
+	int value;		 /* memset byte */
+	int grid, smem;
+};
+
+struct d_deferred
+{
+	std::vector<d_deferredOp> ops;
+	std::vector<unsigned char> up;	 /* upload bytes */
+	std::vector<unsigned char> args; /* kernel argument blocks */
+};
+
 struct b2gDeviceWorld
 {
 	cudaStream_t stream;
+	d_deferred* defer;			 /* non-NULL: record device work for a batched flush */
+	std::vector<void*> retired; /* device buffers recorded work may name, freed after the flush */
 	cudaEvent_t ev[10];
 	float pairsMs, collideMs, solveMs, finalizeMs; /* accumulated device time per stage */
 	long long h2dBytes, d2hBytes;				   /* accumulated host<->device traffic */
@@ -100,6 +149,9 @@ struct b2gDeviceWorld
 	int partnerOffsetsCap, partnerListCap;
 	int partnerCount; /* 0: no such joint */
 	float* tapeToi;	  /* time-of-impact slot of the step being recorded, consumed by the next solve */
+	int pendingMoves;	  /* moves of the pair query awaiting its results */
+	int pendingCapacity; /* contact id capacity of the narrowphase awaiting its results */
+	int pendingRecWindow, pendingShapeTotal, pendingSolved; /* the solve awaiting its results */
 	/* broadphase */
 	b2gTreeNode* tree[3];
 	int treeCap[3], treeRoot[3];
@@ -174,7 +226,7 @@ struct b2gDeviceWorld
 		if ( e_ != cudaSuccess ) return (int)e_;                                                                                 \
 	} while ( 0 )
 
-static int grow( void** ptr, int* cap, int need, size_t elem )
+static int grow( b2gDeviceWorld* dw, void** ptr, int* cap, int need, size_t elem )
 {
 	if ( need <= *cap && *ptr != NULL ) return 0;
 	int nc = *cap > 0 ? *cap : 64;
@@ -184,8 +236,27 @@ static int grow( void** ptr, int* cap, int need, size_t elem )
 	CK( cudaMemset( p, 0, (size_t)nc * elem ) );
 	if ( *ptr != NULL )
 	{
-		if ( *cap > 0 ) CK( cudaMemcpy( p, *ptr, (size_t)( *cap ) * elem, cudaMemcpyDeviceToDevice ) );
-		CK( cudaFree( *ptr ) );
+		if ( dw->defer )
+		{
+			/* recorded work may still write the old buffer: its contents move in order at the
+			   flush, and the buffer is freed after it */
+			if ( *cap > 0 )
+			{
+				d_deferredOp op;
+				memset( &op, 0, sizeof( op ) );
+				op.kind = D_OP_D2D;
+				op.dev = p;
+				op.host = *ptr;
+				op.bytes = (long long)( *cap ) * (long long)elem;
+				dw->defer->ops.push_back( op );
+			}
+			dw->retired.push_back( *ptr );
+		}
+		else
+		{
+			if ( *cap > 0 ) CK( cudaMemcpy( p, *ptr, (size_t)( *cap ) * elem, cudaMemcpyDeviceToDevice ) );
+			CK( cudaFree( *ptr ) );
+		}
 	}
 	*ptr = p;
 	*cap = nc;
@@ -211,16 +282,143 @@ static int growHost( void** ptr, int* cap, int need, size_t elem )
 
 static inline int blocks( int n ) { return ( n + B2G_THREADS - 1 ) / B2G_THREADS; }
 
-/* ======================= broadphase pair query ======================= */
-__global__ void k_markMoved( unsigned char* movedDyn, unsigned char* movedKin, unsigned char* movedStat, const int* keys, int n,
-							 unsigned char value )
+/* ---- device work, issued or recorded ---- */
+
+/* a kernel written as a body over (arguments, block, grid): one launch for one world, or one
+   launch for the records of many worlds, whose blocks are laid end to end */
+struct d_batchRec
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if ( i >= n ) return;
-	int key = keys[i];
+	long long args;
+	int blockBase, blocks;
+};
+
+template <class Args, void ( *Body )( const Args&, int, int ), int MinBlocks>
+__global__ void __launch_bounds__( B2G_THREADS, MinBlocks ) k_single( Args a )
+{
+	Body( a, blockIdx.x, gridDim.x );
+}
+
+template <class Args, void ( *Body )( const Args&, int, int ), int MinBlocks>
+__global__ void __launch_bounds__( B2G_THREADS, MinBlocks ) k_batched( const d_batchRec* __restrict__ recs, int count,
+																	   const unsigned char* __restrict__ args )
+{
+	int lo = 0, hi = count - 1;
+	while ( lo < hi )
+	{
+		int mid = ( lo + hi + 1 ) >> 1;
+		if ( recs[mid].blockBase <= (int)blockIdx.x ) lo = mid;
+		else hi = mid - 1;
+	}
+	const d_batchRec r = recs[lo];
+	Body( *(const Args*)( args + r.args ), (int)blockIdx.x - r.blockBase, r.blocks );
+}
+
+static long long d_alignArgs( long long x ) { return ( x + 15 ) & ~15LL; }
+
+/* upload: `src` is copied at once (recorded) or sent from pinned memory (issued) */
+static int dev_h2d( b2gDeviceWorld* dw, void* dst, const void* src, size_t bytes )
+{
+	if ( bytes == 0 ) return 0;
+	dw->h2dBytes += (long long)bytes;
+	if ( dw->defer )
+	{
+		d_deferred* d = dw->defer;
+		d_deferredOp op;
+		memset( &op, 0, sizeof( op ) );
+		op.kind = D_OP_H2D;
+		op.dev = dst;
+		op.bytes = (long long)bytes;
+		op.at = (long long)d->up.size();
+		d->up.resize( (size_t)d_alignArgs( op.at + op.bytes ) );
+		memcpy( d->up.data() + op.at, src, bytes );
+		d->ops.push_back( op );
+		return 0;
+	}
+	return (int)cudaMemcpyAsync( dst, src, bytes, cudaMemcpyHostToDevice, dw->stream );
+}
+
+/* download into host memory (pinned when issued); valid after the world's next wait */
+static int dev_d2h( b2gDeviceWorld* dw, void* dst, const void* src, size_t bytes )
+{
+	if ( bytes == 0 ) return 0;
+	dw->d2hBytes += (long long)bytes;
+	if ( dw->defer )
+	{
+		d_deferredOp op;
+		memset( &op, 0, sizeof( op ) );
+		op.kind = D_OP_D2H;
+		op.dev = (void*)src;
+		op.host = dst;
+		op.bytes = (long long)bytes;
+		dw->defer->ops.push_back( op );
+		return 0;
+	}
+	return (int)cudaMemcpyAsync( dst, src, bytes, cudaMemcpyDeviceToHost, dw->stream );
+}
+
+static int dev_memset( b2gDeviceWorld* dw, void* dst, int value, size_t bytes )
+{
+	if ( dw->defer )
+	{
+		d_deferredOp op;
+		memset( &op, 0, sizeof( op ) );
+		op.kind = D_OP_MEMSET;
+		op.dev = dst;
+		op.bytes = (long long)bytes;
+		op.value = value;
+		dw->defer->ops.push_back( op );
+		return 0;
+	}
+	return (int)cudaMemsetAsync( dst, value, bytes, dw->stream );
+}
+
+template <class Args, void ( *Body )( const Args&, int, int ), int MinBlocks = 1>
+static int dev_launch( b2gDeviceWorld* dw, int kernel, int grid, const Args& a )
+{
+	if ( grid <= 0 ) return 0;
+	dw->launches += 1;
+	if ( dw->defer )
+	{
+		d_deferred* d = dw->defer;
+		d_deferredOp op;
+		memset( &op, 0, sizeof( op ) );
+		op.kind = D_OP_KERNEL;
+		op.kernel = kernel;
+		op.grid = grid;
+		op.bytes = (long long)sizeof( Args );
+		op.at = (long long)d->args.size();
+		d->args.resize( (size_t)d_alignArgs( op.at + op.bytes ) );
+		memcpy( d->args.data() + op.at, &a, sizeof( Args ) );
+		d->ops.push_back( op );
+		return 0;
+	}
+	k_single<Args, Body, MinBlocks><<<grid, B2G_THREADS, 0, dw->stream>>>( a );
+	return (int)cudaGetLastError();
+}
+
+/* events only time issued work */
+static void dev_event( b2gDeviceWorld* dw, cudaEvent_t ev )
+{
+	if ( dw->defer == NULL ) cudaEventRecord( ev, dw->stream );
+}
+
+/* ======================= broadphase pair query ======================= */
+struct d_markMovedArgs
+{
+	unsigned char *movedDyn, *movedKin, *movedStat;
+	const int* keys;
+	int n;
+	unsigned char value;
+};
+
+static __device__ void b_markMoved( const d_markMovedArgs& a, int block, int grid )
+{
+	int i = block * blockDim.x + threadIdx.x;
+	if ( i >= a.n ) return;
+	int key = a.keys[i];
 	int type = key & 3, id = key >> 2;
-	unsigned char* m = type == b2_dynamicBody ? movedDyn : ( type == b2_kinematicBody ? movedKin : movedStat );
-	m[id] = value;
+	unsigned char* m = type == b2_dynamicBody ? a.movedDyn : ( type == b2_kinematicBody ? a.movedKin : a.movedStat );
+	m[id] = a.value;
 }
 
 /* one thread per moved proxy; stack DFS with child1 pushed before child2, as
@@ -229,13 +427,36 @@ __global__ void k_markMoved( unsigned char* movedDyn, unsigned char* movedKin, u
    node are loaded and tested together and only overlapping ones are pushed: the visit
    order of the overlapping nodes is the reference's, with half the dependent loads. A
    stack entry is (child1, child2) of an overlapping internal node, or (~leaf node, shape). */
-__global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat, const b2gTreeNode* __restrict__ tKin, int rootKin,
-							 const b2gTreeNode* __restrict__ tDyn, int rootDyn, const unsigned char* __restrict__ movedDyn,
-							 const int* __restrict__ keys, const float4* __restrict__ boxes, const int* __restrict__ queryShapes,
-							 int n, int* __restrict__ pairs, int* __restrict__ counts, int capPerMove,
-							 b2gStepCounters* counters )
+struct d_findPairsArgs
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const b2gTreeNode *tStat, *tKin, *tDyn;
+	int rootStat, rootKin, rootDyn;
+	const unsigned char* movedDyn;
+	const int* keys;
+	const float4* boxes;
+	const int* queryShapes;
+	int n;
+	int* pairs;
+	int* counts;
+	int capPerMove;
+	b2gStepCounters* counters;
+};
+
+static __device__ void b_findPairs( const d_findPairsArgs& fa, int block, int grid )
+{
+	const b2gTreeNode* __restrict__ tStat = fa.tStat;
+	const b2gTreeNode* __restrict__ tKin = fa.tKin;
+	const b2gTreeNode* __restrict__ tDyn = fa.tDyn;
+	const int rootStat = fa.rootStat, rootKin = fa.rootKin, rootDyn = fa.rootDyn;
+	const unsigned char* __restrict__ movedDyn = fa.movedDyn;
+	const int* __restrict__ keys = fa.keys;
+	const float4* __restrict__ boxes = fa.boxes;
+	const int* __restrict__ queryShapes = fa.queryShapes;
+	const int n = fa.n, capPerMove = fa.capPerMove;
+	int* __restrict__ pairs = fa.pairs;
+	int* __restrict__ counts = fa.counts;
+	b2gStepCounters* counters = fa.counters;
+	int i = block * blockDim.x + threadIdx.x;
 	if ( i >= n ) return;
 	int queryKey = keys[i];
 	int queryType = queryKey & 3;
@@ -326,11 +547,19 @@ __global__ void k_findPairs( const b2gTreeNode* __restrict__ tStat, int rootStat
 }
 
 /* ======================= contacts ======================= */
-__global__ void k_initContacts( b2gContact* contacts, const b2gContactInit* inits, int n )
+struct d_contactListArgs
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if ( i >= n ) return;
-	b2gContactInit in = inits[i];
+	b2gContact* contacts;
+	const void* list; /* b2gContactInit (init) or contact ids (kill) */
+	int n;
+};
+
+static __device__ void b_initContacts( const d_contactListArgs& a, int block, int grid )
+{
+	int i = block * blockDim.x + threadIdx.x;
+	if ( i >= a.n ) return;
+	b2gContact* contacts = a.contacts;
+	b2gContactInit in = ( (const b2gContactInit*)a.list )[i];
 	b2gContact c;
 	memset( &c, 0, sizeof( c ) );
 	c.shapeIdA = in.shapeIdA;
@@ -343,11 +572,11 @@ __global__ void k_initContacts( b2gContact* contacts, const b2gContactInit* init
 	contacts[in.contactId] = c;
 }
 
-__global__ void k_killContacts( b2gContact* contacts, const int* ids, int n )
+static __device__ void b_killContacts( const d_contactListArgs& a, int block, int grid )
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if ( i >= n ) return;
-	contacts[ids[i]].simFlags = 0;
+	int i = block * blockDim.x + threadIdx.x;
+	if ( i >= a.n ) return;
+	a.contacts[( (const int*)a.list )[i]].simFlags = 0;
 }
 
 struct d_collideArgs
@@ -371,9 +600,9 @@ struct d_collideArgs
 };
 
 /* physics_world.c:451-609 and contact.c:519-698, one thread per contact slot */
-__global__ void k_collide( d_collideArgs a )
+static __device__ void b_collide( const d_collideArgs& a, int block, int grid )
 {
-	int contactId = blockIdx.x * blockDim.x + threadIdx.x;
+	int contactId = block * blockDim.x + threadIdx.x;
 	if ( contactId >= a.capacity ) return;
 	b2gContact* cs = a.contacts + contactId;
 	uint32_t simFlags = cs->simFlags;
@@ -590,9 +819,9 @@ __global__ void k_storeImpulses( d_solveArgs a, int total, int overflowBegin )
 
 /* the register cap keeps the common path at full occupancy; the rare continuous sweep of
    a fast body spills instead */
-__global__ void __launch_bounds__( B2G_THREADS, 8 ) k_finalizeBodies( d_finalizeArgs f )
+static __device__ void b_finalize( const d_finalizeArgs& f, int block, int grid )
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	int i = block * blockDim.x + threadIdx.x;
 	if ( i < f.awakeCount ) d_finalizeBody( f, i );
 }
 
@@ -620,7 +849,7 @@ extern "C" int b2gDev_Create( b2gDeviceWorld** out )
 	cudaError_t e = cudaGetDeviceCount( &count );
 	if ( e != cudaSuccess ) return (int)e;
 	if ( count == 0 ) return (int)cudaErrorNoDevice;
-	b2gDeviceWorld* dw = (b2gDeviceWorld*)calloc( 1, sizeof( b2gDeviceWorld ) );
+	b2gDeviceWorld* dw = new b2gDeviceWorld(); /* value-initialized: every field zero */
 	/* a blocking stream: buffer growth (cudaMalloc + cudaMemset / cudaMemcpy on the legacy
 	   default stream) is then ordered before every kernel of this world */
 	CK( cudaStreamCreate( &dw->stream ) );
@@ -666,10 +895,12 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	free( dw->hSortTmp );
 	for ( int i = 0; i < 10; ++i ) cudaEventDestroy( dw->ev[i] );
 	cudaStreamDestroy( dw->stream );
-	free( dw );
+	for ( void* r : dw->retired ) cudaFree( r );
+	delete dw->defer;
+	delete dw;
 }
 
-#define GROW( field, capField, need, T ) CK2( grow( (void**)&dw->field, &dw->capField, ( need ), sizeof( T ) ) )
+#define GROW( field, capField, need, T ) CK2( grow( dw, (void**)&dw->field, &dw->capField, ( need ), sizeof( T ) ) )
 #define CK2( x )                                                                                                               \
 	do                                                                                                                           \
 	{                                                                                                                            \
@@ -681,13 +912,13 @@ extern "C" int b2gDev_UploadShapes( b2gDeviceWorld* dw, const b2gShape* shapes, 
 									 int count )
 {
 	int cap = dw->shapeCap;
-	CK2( grow( (void**)&dw->shapes, &cap, count, sizeof( b2gShape ) ) );
+	CK2( grow( dw, (void**)&dw->shapes, &cap, count, sizeof( b2gShape ) ) );
 	cap = dw->shapeCap;
-	CK2( grow( (void**)&dw->aabb, &cap, count, sizeof( float4 ) ) );
+	CK2( grow( dw, (void**)&dw->aabb, &cap, count, sizeof( float4 ) ) );
 	cap = dw->shapeCap;
-	CK2( grow( (void**)&dw->fat, &cap, count, sizeof( float4 ) ) );
+	CK2( grow( dw, (void**)&dw->fat, &cap, count, sizeof( float4 ) ) );
 	cap = dw->shapeCap;
-	CK2( grow( (void**)&dw->shapeEnlarged, &cap, count, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->shapeEnlarged, &cap, count, sizeof( int ) ) );
 	dw->shapeCap = cap;
 	dw->shapeCountTotal = count;
 	if ( count > 0 )
@@ -702,7 +933,7 @@ extern "C" int b2gDev_UploadShapes( b2gDeviceWorld* dw, const b2gShape* shapes, 
 template <typename T> static int upload( b2gDeviceWorld* dw, T** dptr, int* cap, const T* src, int n, int* capOut )
 {
 	int c = *cap;
-	CK2( grow( (void**)dptr, &c, n, sizeof( T ) ) );
+	CK2( grow( dw, (void**)dptr, &c, n, sizeof( T ) ) );
 	*capOut = c;
 	if ( n > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)n * sizeof( T ) ), cudaMemcpy( *dptr, src, (size_t)n * sizeof( T ), cudaMemcpyHostToDevice ) ) );
 	return 0;
@@ -772,9 +1003,9 @@ extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int
 	cap0 = dw->awakeCap;
 	CK2( upload( dw, &dw->center0, &cap0, (const float4*)center0, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
-	CK2( grow( (void**)&dw->enlargedBody, &cap0, awakeCount, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->enlargedBody, &cap0, awakeCount, sizeof( int ) ) );
 	int pcap = dw->awakeCap * 8;
-	CK2( grow( (void**)&dw->params, &pcap, 8 * awakeCount, sizeof( float ) ) );
+	CK2( grow( dw, (void**)&dw->params, &pcap, 8 * awakeCount, sizeof( float ) ) );
 	if ( awakeCount > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)awakeCount * 8 * sizeof( float ) ), cudaMemcpy( dw->params, params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyHostToDevice ) ) );
 	dw->awakeCap = capOut;
 	dw->awakeCount = awakeCount;
@@ -850,9 +1081,9 @@ extern "C" int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float
 
 extern "C" int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity )
 {
-	CK2( grow( (void**)&dw->contacts, &dw->contactCap, capacity > 0 ? capacity : 1, sizeof( b2gContact ) ) );
+	CK2( grow( dw, (void**)&dw->contacts, &dw->contactCap, capacity > 0 ? capacity : 1, sizeof( b2gContact ) ) );
 	int c = dw->changeCap;
-	CK2( grow( (void**)&dw->changes, &c, 2 * ( capacity > 0 ? capacity : 1 ), sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->changes, &c, 2 * ( capacity > 0 ? capacity : 1 ), sizeof( int ) ) );
 	dw->changeCap = c;
 	return 0;
 }
@@ -865,20 +1096,37 @@ static int arenaAlloc( b2gDeviceWorld* dw, size_t bytes, size_t* offset )
 	size_t need = ( bytes + 15 ) & ~(size_t)15;
 	if ( dw->upUsed + need > (size_t)dw->upCap )
 	{
-		/* drain the stream: earlier uploads may still read the arena */
-		CK( cudaStreamSynchronize( dw->stream ) );
-		dw->upUsed = 0;
-		if ( need > (size_t)dw->upCap )
+		if ( dw->defer )
 		{
+			/* recorded work may still name the old device arena: keep it until the flush */
 			int nc = dw->upCap > 0 ? dw->upCap : 1 << 16;
-			while ( (size_t)nc < need ) nc *= 2;
+			while ( (size_t)nc < dw->upUsed + need ) nc *= 2;
+			void* grown = NULL;
+			CK( cudaMalloc( &grown, (size_t)nc ) );
+			if ( dw->upDev ) dw->retired.push_back( dw->upDev );
 			if ( dw->upHost ) CK( cudaFreeHost( dw->upHost ) );
-			if ( dw->upDev ) CK( cudaFree( dw->upDev ) );
-			dw->upHost = NULL;
-			dw->upDev = NULL;
 			CK( cudaMallocHost( &dw->upHost, (size_t)nc ) );
-			CK( cudaMalloc( &dw->upDev, (size_t)nc ) );
+			dw->upDev = grown;
 			dw->upCap = nc;
+			dw->upUsed = 0;
+		}
+		else
+		{
+			/* drain the stream: earlier uploads may still read the arena */
+			CK( cudaStreamSynchronize( dw->stream ) );
+			dw->upUsed = 0;
+			if ( need > (size_t)dw->upCap )
+			{
+				int nc = dw->upCap > 0 ? dw->upCap : 1 << 16;
+				while ( (size_t)nc < need ) nc *= 2;
+				if ( dw->upHost ) CK( cudaFreeHost( dw->upHost ) );
+				if ( dw->upDev ) CK( cudaFree( dw->upDev ) );
+				dw->upHost = NULL;
+				dw->upDev = NULL;
+				CK( cudaMallocHost( &dw->upHost, (size_t)nc ) );
+				CK( cudaMalloc( &dw->upDev, (size_t)nc ) );
+				dw->upCap = nc;
+			}
 		}
 	}
 	*offset = dw->upUsed;
@@ -890,12 +1138,11 @@ static int arenaAlloc( b2gDeviceWorld* dw, size_t bytes, size_t* offset )
 static int uploadTo( b2gDeviceWorld* dw, void* dst, const void* src, size_t bytes )
 {
 	if ( bytes == 0 ) return 0;
+	if ( dw->defer ) return dev_h2d( dw, dst, src, bytes );
 	size_t off = 0;
 	CK2( arenaAlloc( dw, bytes, &off ) );
 	memcpy( (char*)dw->upHost + off, src, bytes );
-	dw->h2dBytes += (long long)bytes;
-	CK( cudaMemcpyAsync( dst, (char*)dw->upHost + off, bytes, cudaMemcpyHostToDevice, dw->stream ) );
-	return 0;
+	return dev_h2d( dw, dst, (char*)dw->upHost + off, bytes );
 }
 
 /* send `bytes` into the device side of the arena; returns the device address */
@@ -903,11 +1150,10 @@ static int uploadStaged( b2gDeviceWorld* dw, const void* src, size_t bytes, void
 {
 	size_t off = 0;
 	CK2( arenaAlloc( dw, bytes, &off ) );
-	memcpy( (char*)dw->upHost + off, src, bytes );
-	dw->h2dBytes += (long long)bytes;
-	CK( cudaMemcpyAsync( (char*)dw->upDev + off, (char*)dw->upHost + off, bytes, cudaMemcpyHostToDevice, dw->stream ) );
 	*devPtr = (char*)dw->upDev + off;
-	return 0;
+	if ( dw->defer ) return dev_h2d( dw, *devPtr, src, bytes );
+	memcpy( (char*)dw->upHost + off, src, bytes );
+	return dev_h2d( dw, *devPtr, (char*)dw->upHost + off, bytes );
 }
 
 /* wait for the stream; afterwards the upload arena is free again */
@@ -935,9 +1181,8 @@ extern "C" int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* in
 	if ( count == 0 ) return 0;
 	void* d = NULL;
 	CK2( uploadStaged( dw, inits, (size_t)count * sizeof( b2gContactInit ), &d ) );
-	k_initContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const b2gContactInit*)d, count );
-	dw->launches += 1;
-	return (int)cudaGetLastError();
+	d_contactListArgs a = { dw->contacts, d, count };
+	return dev_launch<d_contactListArgs, b_initContacts>( dw, DK_INIT_CONTACTS, blocks( count ), a );
 }
 
 extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int count )
@@ -945,15 +1190,14 @@ extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int coun
 	if ( count == 0 ) return 0;
 	void* d = NULL;
 	CK2( uploadStaged( dw, ids, (size_t)count * sizeof( int ), &d ) );
-	k_killContacts<<<blocks( count ), B2G_THREADS, 0, dw->stream>>>( dw->contacts, (const int*)d, count );
-	dw->launches += 1;
-	return (int)cudaGetLastError();
+	d_contactListArgs a = { dw->contacts, d, count };
+	return dev_launch<d_contactListArgs, b_killContacts>( dw, DK_KILL_CONTACTS, blocks( count ), a );
 }
 
 extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const int* offsets, int total )
 {
 	dw->topologyDirty = 1;
-	CK2( grow( (void**)&dw->colorIds, &dw->colorIdsCap, total > 0 ? total : 1, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->colorIds, &dw->colorIdsCap, total > 0 ? total : 1, sizeof( int ) ) );
 	CK2( uploadTo( dw, dw->colorIds, ids, (size_t)total * sizeof( int ) ) );
 	memcpy( dw->colorOffsets, offsets, sizeof( dw->colorOffsets ) );
 	return 0;
@@ -979,7 +1223,7 @@ extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int
 extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* offsets )
 {
 	dw->topologyDirty = 1;
-	CK2( grow( (void**)&dw->joints, &dw->jointCap, count > 0 ? count : 1, sizeof( b2gJoint ) ) );
+	CK2( grow( dw, (void**)&dw->joints, &dw->jointCap, count > 0 ? count : 1, sizeof( b2gJoint ) ) );
 	CK2( uploadTo( dw, dw->joints, joints, (size_t)count * sizeof( b2gJoint ) ) );
 	memcpy( dw->jointOffsets, offsets, sizeof( dw->jointOffsets ) );
 	dw->jointCount = count;
@@ -994,14 +1238,40 @@ struct d_colorOffsets
 
 /* one step record: header, every body's pose and velocity, integration parameters, and the
    colored contacts in slot order as the narrowphase left them */
-__global__ void k_captureTape( unsigned char* rec, b2gStepParams params, d_colorOffsets offsets, int bodyCount, int awakeCount,
-							   int slotCount, int jointCount, const float4* __restrict__ xf, const float2* __restrict__ center,
-							   const float2* __restrict__ localCenter, const int* __restrict__ awakeIndex,
-							   const int* __restrict__ bodyType, const float4* __restrict__ sv, const float* __restrict__ bodyParams,
-							   const int* __restrict__ colorIds, const b2gContact* __restrict__ contacts )
+struct d_captureArgs
 {
-	int t = blockIdx.x * blockDim.x + threadIdx.x;
-	int nt = gridDim.x * blockDim.x;
+	unsigned char* rec;
+	b2gStepParams params;
+	d_colorOffsets offsets;
+	int bodyCount, awakeCount, slotCount, jointCount;
+	const float4* xf;
+	const float2* center;
+	const float2* localCenter;
+	const int* awakeIndex;
+	const int* bodyType;
+	const float4* sv;
+	const float* bodyParams;
+	const int* colorIds;
+	const b2gContact* contacts;
+};
+
+static __device__ void b_capture( const d_captureArgs& ca, int block, int grid )
+{
+	unsigned char* rec = ca.rec;
+	const b2gStepParams& params = ca.params;
+	const d_colorOffsets& offsets = ca.offsets;
+	const int bodyCount = ca.bodyCount, awakeCount = ca.awakeCount, slotCount = ca.slotCount, jointCount = ca.jointCount;
+	const float4* __restrict__ xf = ca.xf;
+	const float2* __restrict__ center = ca.center;
+	const float2* __restrict__ localCenter = ca.localCenter;
+	const int* __restrict__ awakeIndex = ca.awakeIndex;
+	const int* __restrict__ bodyType = ca.bodyType;
+	const float4* __restrict__ sv = ca.sv;
+	const float* __restrict__ bodyParams = ca.bodyParams;
+	const int* __restrict__ colorIds = ca.colorIds;
+	const b2gContact* __restrict__ contacts = ca.contacts;
+	int t = block * blockDim.x + threadIdx.x;
+	int nt = grid * blockDim.x;
 	if ( t == 0 )
 	{
 		b2gTapeStep h;
@@ -1072,6 +1342,8 @@ extern "C" int b2gDev_CaptureTape( b2gDeviceWorld* dw, const b2gStepParams* p, i
 		CK( cudaMallocAsync( &grown, (size_t)cap, dw->stream ) );
 		if ( *used > 0 ) CK( cudaMemcpyAsync( grown, *arena, (size_t)*used, cudaMemcpyDeviceToDevice, dw->stream ) );
 		if ( *arena != NULL ) CK( cudaFreeAsync( *arena, dw->stream ) );
+		/* recorded work runs on another stream: the new arena must exist before the flush */
+		if ( dw->defer ) CK( cudaStreamSynchronize( dw->stream ) );
 		*arena = grown;
 		*capacity = cap;
 	}
@@ -1080,11 +1352,24 @@ extern "C" int b2gDev_CaptureTape( b2gDeviceWorld* dw, const b2gStepParams* p, i
 	int n = bodyCount > slotCount ? bodyCount : slotCount;
 	n = n > 8 * awakeCount ? n : 8 * awakeCount;
 	int grid = blocks( n > 0 ? n : 1 );
-	k_captureTape<<<grid, B2G_THREADS, 0, dw->stream>>>( (unsigned char*)*arena + *used, *p, offsets, bodyCount, awakeCount, slotCount,
-														jointCount, dw->xf, dw->center, dw->localCenter, dw->awakeIndex,
-														dw->bodyType, dw->stateV, dw->params, dw->colorIds, dw->contacts );
-	dw->launches += 1;
-	CK( cudaGetLastError() );
+	d_captureArgs ca;
+	ca.rec = (unsigned char*)*arena + *used;
+	ca.params = *p;
+	ca.offsets = offsets;
+	ca.bodyCount = bodyCount;
+	ca.awakeCount = awakeCount;
+	ca.slotCount = slotCount;
+	ca.jointCount = jointCount;
+	ca.xf = dw->xf;
+	ca.center = dw->center;
+	ca.localCenter = dw->localCenter;
+	ca.awakeIndex = dw->awakeIndex;
+	ca.bodyType = dw->bodyType;
+	ca.sv = dw->stateV;
+	ca.bodyParams = dw->params;
+	ca.colorIds = dw->colorIds;
+	ca.contacts = dw->contacts;
+	CK2( ( dev_launch<d_captureArgs, b_capture>( dw, DK_CAPTURE, grid, ca ) ) );
 	*offset = *used;
 	dw->tapeToi = (float*)( (unsigned char*)*arena + *used + b2gTapeToiOffset( bodyCount, awakeCount ) );
 	*used += bytes;
@@ -1114,8 +1399,8 @@ extern "C" int b2gDev_UploadJointPartners( b2gDeviceWorld* dw, const int* offset
 {
 	dw->partnerCount = listCount;
 	if ( listCount == 0 ) return 0;
-	CK2( grow( (void**)&dw->partnerOffsets, &dw->partnerOffsetsCap, bodyCount + 1, sizeof( int ) ) );
-	CK2( grow( (void**)&dw->partnerList, &dw->partnerListCap, listCount, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->partnerOffsets, &dw->partnerOffsetsCap, bodyCount + 1, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->partnerList, &dw->partnerListCap, listCount, sizeof( int ) ) );
 	CK2( uploadTo( dw, dw->partnerOffsets, offsets, (size_t)( bodyCount + 1 ) * sizeof( int ) ) );
 	CK2( uploadTo( dw, dw->partnerList, list, (size_t)listCount * sizeof( int ) ) );
 	return 0;
@@ -1137,11 +1422,19 @@ extern "C" int b2gDev_DownloadJoints( b2gDeviceWorld* dw, b2gJoint* byId, int id
 	return (int)e;
 }
 
-__global__ void k_convertTree( const b2gHostTreeNode* __restrict__ raw, b2gTreeNode* __restrict__ out, int n )
+struct d_convertTreeArgs
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if ( i >= n ) return;
-	b2gHostTreeNode h = raw[i];
+	const b2gHostTreeNode* raw;
+	b2gTreeNode* out;
+	int n;
+};
+
+static __device__ void b_convertTree( const d_convertTreeArgs& a, int block, int grid )
+{
+	int i = block * blockDim.x + threadIdx.x;
+	if ( i >= a.n ) return;
+	b2gTreeNode* __restrict__ out = a.out;
+	b2gHostTreeNode h = a.raw[i];
 	b2gTreeNode d;
 	d.aabb = h.aabb;
 	d.isLeaf = ( h.flags & 0x4 ) ? 1 : 0;
@@ -1155,27 +1448,24 @@ extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gHostTre
 								   int hostPinned )
 {
 	int need = nodeCount > 0 ? nodeCount : 1;
-	CK2( grow( (void**)&dw->tree[type], &dw->treeCap[type], need, sizeof( b2gTreeNode ) ) );
-	CK2( grow( (void**)&dw->treeRaw[type], &dw->treeRawCap[type], need, sizeof( b2gHostTreeNode ) ) );
+	CK2( grow( dw, (void**)&dw->tree[type], &dw->treeCap[type], need, sizeof( b2gTreeNode ) ) );
+	CK2( grow( dw, (void**)&dw->treeRaw[type], &dw->treeRawCap[type], need, sizeof( b2gHostTreeNode ) ) );
 	if ( nodeCount > 0 )
 	{
-		if ( hostPinned )
+		if ( hostPinned || dw->defer )
 		{
-			dw->h2dBytes += (long long)( (size_t)nodeCount * sizeof( b2gHostTreeNode ) );
-			CK( cudaMemcpyAsync( dw->treeRaw[type], nodes, (size_t)nodeCount * sizeof( b2gHostTreeNode ), cudaMemcpyHostToDevice,
-								 dw->stream ) );
+			CK2( dev_h2d( dw, dw->treeRaw[type], nodes, (size_t)nodeCount * sizeof( b2gHostTreeNode ) ) );
 		}
 		else
 		{
 			/* small trees live in pageable memory: stage them through the upload arena */
 			CK2( uploadTo( dw, dw->treeRaw[type], nodes, (size_t)nodeCount * sizeof( b2gHostTreeNode ) ) );
 		}
-		k_convertTree<<<blocks( nodeCount ), B2G_THREADS, 0, dw->stream>>>( dw->treeRaw[type], dw->tree[type], nodeCount );
-		dw->launches += 1;
-		CK( cudaGetLastError() );
+		d_convertTreeArgs ca = { dw->treeRaw[type], dw->tree[type], nodeCount };
+		CK2( ( dev_launch<d_convertTreeArgs, b_convertTree>( dw, DK_CONVERT_TREE, blocks( nodeCount ), ca ) ) );
 	}
 	int mc = dw->movedCap[type];
-	CK2( grow( (void**)&dw->moved[type], &mc, need, 1 ) );
+	CK2( grow( dw, (void**)&dw->moved[type], &mc, need, 1 ) );
 	dw->movedCap[type] = mc;
 	dw->treeRoot[type] = root;
 	return 0;
@@ -1194,91 +1484,125 @@ extern "C" void b2gDev_HostFree( void* p )
 }
 
 /* per move: claim a contiguous run of the packed pair buffer */
-__global__ void k_packPairs( const int* __restrict__ pairs, const int* __restrict__ counts, int n, int capPerMove,
-							 int* __restrict__ packed, int* __restrict__ offsets, b2gStepCounters* counters )
+struct d_packPairsArgs
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if ( i >= n ) return;
-	int c = counts[i];
-	if ( c > capPerMove ) c = capPerMove;
-	int o = atomicAdd( &counters->pairCount, c );
-	offsets[i] = o;
+	const int* pairs;
+	const int* counts;
+	int n, capPerMove;
+	int* packed;
+	int* offsets;
+	b2gStepCounters* counters;
+};
+
+static __device__ void b_packPairs( const d_packPairsArgs& a, int block, int grid )
+{
+	int i = block * blockDim.x + threadIdx.x;
+	if ( i >= a.n ) return;
+	int c = a.counts[i];
+	if ( c > a.capPerMove ) c = a.capPerMove;
+	int o = atomicAdd( &a.counters->pairCount, c );
+	a.offsets[i] = o;
 	for ( int k = 0; k < c; ++k )
 	{
-		packed[2 * ( o + k )] = pairs[2 * ( (size_t)i * capPerMove + k )];
-		packed[2 * ( o + k ) + 1] = pairs[2 * ( (size_t)i * capPerMove + k ) + 1];
+		a.packed[2 * ( o + k )] = a.pairs[2 * ( (size_t)i * a.capPerMove + k )];
+		a.packed[2 * ( o + k ) + 1] = a.pairs[2 * ( (size_t)i * a.capPerMove + k ) + 1];
 	}
 }
 
-extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int n,
-								  int** outPairs, int** outCounts, int* outTotal )
+/* the pair query of one step, issued (or recorded); its results arrive with the world's
+   next wait: counters, per-move counts and offsets, and the first `window` packed pairs */
+static int findPairsIssue( b2gDeviceWorld* dw, int n )
 {
-	CK( cudaEventRecord( dw->ev[0], dw->stream ) );
-	/* one staged copy of the moved proxies (pinned host memory) */
+	CK2( grow( dw, (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
+	int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
+	CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * window, sizeof( int ) ) );
+	CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
+	d_findPairsArgs fa;
+	fa.tStat = dw->tree[b2_staticBody];
+	fa.tKin = dw->tree[b2_kinematicBody];
+	fa.tDyn = dw->tree[b2_dynamicBody];
+	fa.rootStat = dw->treeRoot[b2_staticBody];
+	fa.rootKin = dw->treeRoot[b2_kinematicBody];
+	fa.rootDyn = dw->treeRoot[b2_dynamicBody];
+	fa.movedDyn = dw->moved[b2_dynamicBody];
+	fa.keys = dw->moveKeys;
+	fa.boxes = dw->moveBoxes;
+	fa.queryShapes = dw->moveShapes;
+	fa.n = n;
+	fa.pairs = dw->pairBuf;
+	fa.counts = dw->pairCounts;
+	fa.capPerMove = dw->pairPerMove;
+	fa.counters = dw->counters;
+	CK2( ( dev_launch<d_findPairsArgs, b_findPairs>( dw, DK_FIND_PAIRS, blocks( n ), fa ) ) );
+	d_packPairsArgs pa = { dw->pairBuf, dw->pairCounts, n, dw->pairPerMove, dw->pairPacked, dw->pairOffsets, dw->counters };
+	CK2( ( dev_launch<d_packPairsArgs, b_packPairs>( dw, DK_PACK_PAIRS, blocks( n ), pa ) ) );
+	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
+	CK2( dev_d2h( dw, dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ) ) );
+	CK2( dev_d2h( dw, dw->hPairOffsets, dw->pairOffsets, (size_t)n * sizeof( int ) ) );
+	CK2( dev_d2h( dw, dw->hPairPacked, dw->pairPacked, (size_t)window * 2 * sizeof( int ) ) );
+	dw->pendingMoves = n;
+	return 0;
+}
+
+extern "C" int b2gDev_FindPairsIssue( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int n )
+{
+	dev_event( dw, dw->ev[0] );
+	/* one staged copy of the moved proxies */
 	int stageBytes = n * 24;
 	CK2( growHost( &dw->hMoveStage, &dw->hMoveStageCap, stageBytes, 1 ) );
-	CK2( grow( &dw->moveStage, &dw->moveStageCap, stageBytes, 1 ) );
+	CK2( grow( dw, &dw->moveStage, &dw->moveStageCap, stageBytes, 1 ) );
 	{
 		float* sb = (float*)dw->hMoveStage;
 		memcpy( sb, boxes, (size_t)n * 16 );
 		memcpy( sb + 4 * (size_t)n, keys, (size_t)n * 4 );
 		memcpy( sb + 5 * (size_t)n, shapes, (size_t)n * 4 );
 	}
-	dw->h2dBytes += stageBytes;
-	CK( cudaMemcpyAsync( dw->moveStage, dw->hMoveStage, (size_t)stageBytes, cudaMemcpyHostToDevice, dw->stream ) );
+	CK2( dev_h2d( dw, dw->moveStage, dw->hMoveStage, (size_t)stageBytes ) );
 	dw->moveBoxes = (float4*)dw->moveStage;
 	dw->moveKeys = (int*)( dw->moveBoxes + n );
 	dw->moveShapes = dw->moveKeys + n;
-	CK2( grow( (void**)&dw->pairCounts, &dw->moveCap, n, sizeof( int ) ) );
-	CK2( grow( (void**)&dw->pairOffsets, &dw->pairOffsetsCap, n, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->pairCounts, &dw->moveCap, n, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->pairOffsets, &dw->pairOffsetsCap, n, sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, n, sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hPairOffsets, &dw->hPairOffsetsCap, n, sizeof( int ) ) );
 	if ( dw->pairWindow < 64 ) dw->pairWindow = 64;
-	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
-															   dw->moved[b2_staticBody], dw->moveKeys, n, 1 );
-	dw->launches += 1;
-	CK( cudaGetLastError() );
+	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 1 };
+	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
+	return findPairsIssue( dw, n );
+}
+
+/* after the wait: the pairs of every move in move order. A per-move overflow or a window
+   too small is redone at once, outside any batch. */
+extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int** outCounts, int* outTotal )
+{
+	int n = dw->pendingMoves;
+	d_deferred* deferred = dw->defer;
+	dw->defer = NULL;
 	for ( int attempt = 0; attempt < 8; ++attempt )
 	{
-		CK2( grow( (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
-		CK2( grow( (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
-		int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
-		CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * window, sizeof( int ) ) );
-		CK( cudaMemsetAsync( dw->counters, 0, sizeof( b2gStepCounters ), dw->stream ) );
-		k_findPairs<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>(
-			dw->tree[b2_staticBody], dw->treeRoot[b2_staticBody], dw->tree[b2_kinematicBody], dw->treeRoot[b2_kinematicBody],
-			dw->tree[b2_dynamicBody], dw->treeRoot[b2_dynamicBody], dw->moved[b2_dynamicBody], dw->moveKeys, dw->moveBoxes,
-			dw->moveShapes, n, dw->pairBuf, dw->pairCounts, dw->pairPerMove, dw->counters );
-		k_packPairs<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->pairBuf, dw->pairCounts, n, dw->pairPerMove,
-																  dw->pairPacked, dw->pairOffsets, dw->counters );
-		dw->launches += 2;
-		CK( cudaGetLastError() );
-		/* counters, per-move counts and offsets, and the first `window` pairs in one wait */
-		dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) + (size_t)n * 8 + (size_t)window * 8 );
-		CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
-		CK( cudaMemcpyAsync( dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
-		CK( cudaMemcpyAsync( dw->hPairOffsets, dw->pairOffsets, (size_t)n * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
-		CK( cudaMemcpyAsync( dw->hPairPacked, dw->pairPacked, (size_t)window * 2 * sizeof( int ), cudaMemcpyDeviceToHost,
-							 dw->stream ) );
-		CK2( drain( dw ) );
-		if ( dw->hCounters->status != 0 ) return (int)cudaErrorIllegalState;
+		if ( dw->hCounters->status != 0 )
+		{
+			dw->defer = deferred;
+			return (int)cudaErrorIllegalState;
+		}
 		if ( dw->hCounters->pairOverflow <= dw->pairPerMove ) break;
 		while ( dw->pairPerMove < dw->hCounters->pairOverflow ) dw->pairPerMove *= 2;
+		CK2( findPairsIssue( dw, n ) );
+		CK2( drain( dw ) );
 	}
-	k_markMoved<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody],
-															   dw->moved[b2_staticBody], dw->moveKeys, n, 0 );
-	dw->launches += 1;
-	CK( cudaGetLastError() );
 	int total = dw->hCounters->pairCount;
 	int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
 	if ( total > window )
 	{
 		CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * total, sizeof( int ) ) );
-		dw->d2hBytes += (long long)( total - window ) * 8;
-		CK( cudaMemcpyAsync( dw->hPairPacked + 2 * window, dw->pairPacked + 2 * window, (size_t)( total - window ) * 2 * sizeof( int ),
-							 cudaMemcpyDeviceToHost, dw->stream ) );
+		CK2( dev_d2h( dw, dw->hPairPacked + 2 * window, dw->pairPacked + 2 * window, (size_t)( total - window ) * 2 * sizeof( int ) ) );
 		CK2( drain( dw ) );
 	}
+	dw->defer = deferred;
+	/* clear the moved flags (recorded with the next batch when batching) */
+	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 0 };
+	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
 	/* next step's window follows this step's count, both ways */
 	dw->pairWindow = 2 * total > 64 ? 2 * total : 64;
 	/* pairs in move order for the host */
@@ -1290,12 +1614,20 @@ extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const floa
 		memcpy( dw->hPairs + 2 * o, dw->hPairPacked + 2 * (size_t)dw->hPairOffsets[i], (size_t)c * 2 * sizeof( int ) );
 		o += c;
 	}
-	CK( cudaEventRecord( dw->ev[1], dw->stream ) );
-	dw->pairsTimingPending = 1;
+	dev_event( dw, dw->ev[1] );
+	dw->pairsTimingPending = dw->defer == NULL;
 	*outPairs = dw->hPairs;
 	*outCounts = dw->hPairCounts;
 	*outTotal = total;
 	return 0;
+}
+
+extern "C" int b2gDev_FindPairs( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int n,
+								  int** outPairs, int** outCounts, int* outTotal )
+{
+	CK2( b2gDev_FindPairsIssue( dw, keys, boxes, shapes, n ) );
+	CK2( drain( dw ) );
+	return b2gDev_FindPairsCollect( dw, outPairs, outCounts, outTotal );
 }
 
 static int cmpChange( const void* a, const void* b )
@@ -1304,13 +1636,12 @@ static int cmpChange( const void* a, const void* b )
 	return ( x > y ) - ( x < y );
 }
 
-extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int contactIdCapacity, const int** outChanges,
-								int* outChangeCount, int* outRecycled )
+/* the narrowphase over every live contact slot, issued (or recorded); the counters and the
+   first `window` state changes arrive with the world's next wait */
+extern "C" int b2gDev_CollideIssue( b2gDeviceWorld* dw, const b2gStepParams* p, int contactIdCapacity )
 {
-	CK( cudaEventRecord( dw->ev[2], dw->stream ) );
-	CK( cudaMemsetAsync( dw->counters, 0, sizeof( b2gStepCounters ), dw->stream ) );
-	*outChangeCount = 0;
-	*outRecycled = 0;
+	dev_event( dw, dw->ev[2] );
+	CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
 	if ( contactIdCapacity > 0 )
 	{
 		d_collideArgs a;
@@ -1330,42 +1661,49 @@ extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int c
 		a.changes = dw->changes;
 		a.counters = dw->counters;
 		a.recycleDistance = p->contactRecycleDistance;
-		CK( cudaEventRecord( dw->ev[9], dw->stream ) );
-		k_collide<<<blocks( contactIdCapacity ), B2G_THREADS, 0, dw->stream>>>( a );
-		dw->launches += 1;
-		CK( cudaGetLastError() );
-		CK( cudaEventRecord( dw->ev[3], dw->stream ) );
+		dev_event( dw, dw->ev[9] );
+		CK2( ( dev_launch<d_collideArgs, b_collide>( dw, DK_COLLIDE, blocks( contactIdCapacity ), a ) ) );
+		dev_event( dw, dw->ev[3] );
 	}
-	/* the counters and the first `window` state changes come back in one wait */
 	if ( dw->changeWindow < 64 ) dw->changeWindow = 64;
 	int window = dw->changeWindow < contactIdCapacity ? dw->changeWindow : contactIdCapacity;
 	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( window > 0 ? window : 1 ), sizeof( int ) ) );
-	dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) + (size_t)window * 8 );
-	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
-	if ( window > 0 )
-		CK( cudaMemcpyAsync( dw->hChanges, dw->changes, (size_t)window * 2 * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
-	CK2( drain( dw ) );
-	if ( contactIdCapacity > 0 )
+	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
+	if ( window > 0 ) CK2( dev_d2h( dw, dw->hChanges, dw->changes, (size_t)window * 2 * sizeof( int ) ) );
+	dw->pendingCapacity = contactIdCapacity;
+	return 0;
+}
+
+/* after the wait: the state changes sorted by contact id */
+extern "C" int b2gDev_CollideCollect( b2gDeviceWorld* dw, const int** outChanges, int* outChangeCount, int* outRecycled )
+{
+	int contactIdCapacity = dw->pendingCapacity;
+	int window = dw->changeWindow < contactIdCapacity ? dw->changeWindow : contactIdCapacity;
+	if ( dw->defer == NULL )
 	{
-		float ms = 0.0f;
-		cudaEventElapsedTime( &ms, dw->ev[9], dw->ev[3] );
-		dw->collideMs += ms;
-	}
-	if ( dw->pairsTimingPending )
-	{
-		float ms = 0.0f;
-		cudaEventElapsedTime( &ms, dw->ev[0], dw->ev[1] );
-		dw->pairsMs += ms;
-		dw->pairsTimingPending = 0;
+		if ( contactIdCapacity > 0 )
+		{
+			float ms = 0.0f;
+			cudaEventElapsedTime( &ms, dw->ev[9], dw->ev[3] );
+			dw->collideMs += ms;
+		}
+		if ( dw->pairsTimingPending )
+		{
+			float ms = 0.0f;
+			cudaEventElapsedTime( &ms, dw->ev[0], dw->ev[1] );
+			dw->pairsMs += ms;
+			dw->pairsTimingPending = 0;
+		}
 	}
 	int n = dw->hCounters->stateChangeCount;
 	if ( n > window )
 	{
+		d_deferred* deferred = dw->defer;
+		dw->defer = NULL;
 		CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * n, sizeof( int ) ) );
-		dw->d2hBytes += (long long)( n - window ) * 8;
-		CK( cudaMemcpyAsync( dw->hChanges + 2 * window, dw->changes + 2 * window, (size_t)( n - window ) * 2 * sizeof( int ),
-							 cudaMemcpyDeviceToHost, dw->stream ) );
+		CK2( dev_d2h( dw, dw->hChanges + 2 * window, dw->changes + 2 * window, (size_t)( n - window ) * 2 * sizeof( int ) ) );
 		CK2( drain( dw ) );
+		dw->defer = deferred;
 	}
 	dw->changeWindow = 2 * n > 64 ? 2 * n : 64;
 	if ( n > 1 ) qsort( dw->hChanges, (size_t)n, 2 * sizeof( int ), cmpChange );
@@ -1373,6 +1711,14 @@ extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int c
 	*outChangeCount = n;
 	*outRecycled = dw->hCounters->recycledContactCount;
 	return 0;
+}
+
+extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int contactIdCapacity, const int** outChanges,
+								int* outChangeCount, int* outRecycled )
+{
+	CK2( b2gDev_CollideIssue( dw, p, contactIdCapacity ) );
+	CK2( drain( dw ) );
+	return b2gDev_CollideCollect( dw, outChanges, outChangeCount, outRecycled );
 }
 
 struct recKey
@@ -1388,17 +1734,16 @@ static int cmpRec( const void* a, const void* b )
 	return ( x->order > y->order ) - ( x->order < y->order );
 }
 
-extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const int* activeColors, int activeColorCount,
-							  const int* colorContactCounts, const int* colorJointCounts, int awakeCount,
-							  const int** outRecs, int* outCount, const float** outBoxes, int* outStatus )
+/* the solver and finalize of one step, issued (or recorded: one-CTA worlds only); the
+   counters and the first `window` enlarged-proxy records arrive with the world's next wait */
+extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, const int* activeColors, int activeColorCount,
+								   int awakeCount )
 {
-	(void)colorContactCounts;
-	(void)colorJointCounts;
-	CK( cudaEventRecord( dw->ev[4], dw->stream ) );
+	dev_event( dw, dw->ev[4] );
 	int total = dw->colorOffsets[B2_GRAPH_COLOR_COUNT];
 	int overflowBegin = dw->colorOffsets[B2G_OVERFLOW_INDEX];
-	CK2( grow( (void**)&dw->lanes, &dw->laneCap, total > 0 ? total : 1, sizeof( b2gContactLane ) ) );
-	CK( cudaMemsetAsync( dw->counters, 0, sizeof( b2gStepCounters ), dw->stream ) );
+	CK2( grow( dw, (void**)&dw->lanes, &dw->laneCap, total > 0 ? total : 1, sizeof( b2gContactLane ) ) );
+	CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
 	d_solveArgs a;
 	a.contacts = dw->contacts;
 	a.colorIds = dw->colorIds;
@@ -1413,8 +1758,8 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	int jointTotal = dw->jointOffsets[B2_GRAPH_COLOR_COUNT];
 	/* finalize */
 	int shapeTotal = dw->shapeCountTotal;
-	CK2( grow( (void**)&dw->enlargedRecs, &dw->enlargedCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( int ) ) );
-	CK2( grow( (void**)&dw->enlargedBoxes, &dw->enlargedBoxesCap, shapeTotal > 0 ? shapeTotal : 1, sizeof( float4 ) ) );
+	CK2( grow( dw, (void**)&dw->enlargedRecs, &dw->enlargedCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->enlargedBoxes, &dw->enlargedBoxesCap, shapeTotal > 0 ? shapeTotal : 1, sizeof( float4 ) ) );
 	d_finalizeArgs f;
 	f.sv = dw->stateV;
 	f.sd = dw->stateD;
@@ -1461,17 +1806,45 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	int ovJointCount0 = dw->jointOffsets[B2_GRAPH_COLOR_COUNT] - ovJointBegin0;
 	int ovCount0 = total - overflowBegin;
 	d_jointBodies jb0 = { dw->xf, dw->center, dw->localCenter, dw->invMass, dw->invI, dw->awakeIndex };
-	CK( cudaEventRecord( dw->ev[6], dw->stream ) );
+	dev_event( dw, dw->ev[6] );
 	bool solved = false;
 	long long worldBytes = (long long)B2G_BIN_BODY_BYTES * awakeCount + (long long)B2G_BIN_CONTACT_BYTES * total +
 						   (long long)B2G_BIN_JOINT_BYTES * jointTotal;
 	if ( dw->solverMode == B2G_SOLVER_COMPONENTS && ovJointCount0 + ovCount0 == 0 && worldBytes <= B2G_WORLD_BIN_MAX_BYTES )
 	{
 		/* small world: one CTA solves all of it from shared memory */
-		CK2( b2gDev_SolveWorldBin( &dw->comp, &a, dw->jointOffsets, &jb0, dw->awakeIndex, (int)worldBytes, dw->counters,
-								   dw->stream, &dw->launches ) );
+		if ( dw->defer )
+		{
+			d_deferred* d = dw->defer;
+			int argBytes = 0;
+			CK2( b2gDev_SolveWorldBinArgs( &dw->comp, &a, dw->jointOffsets, &jb0, dw->awakeIndex, (int)worldBytes, dw->counters, NULL,
+										   &argBytes ) );
+			d_deferredOp op;
+			memset( &op, 0, sizeof( op ) );
+			op.kind = D_OP_KERNEL;
+			op.kernel = DK_SOLVE_BIN;
+			op.grid = 1;
+			op.smem = (int)worldBytes;
+			op.bytes = argBytes;
+			op.at = (long long)d->args.size();
+			d->args.resize( (size_t)d_alignArgs( op.at + op.bytes ) );
+			CK2( b2gDev_SolveWorldBinArgs( &dw->comp, &a, dw->jointOffsets, &jb0, dw->awakeIndex, (int)worldBytes, dw->counters,
+										   d->args.data() + op.at, &argBytes ) );
+			d->ops.push_back( op );
+			dw->launches += 1;
+		}
+		else
+		{
+			CK2( b2gDev_SolveWorldBin( &dw->comp, &a, dw->jointOffsets, &jb0, dw->awakeIndex, (int)worldBytes, dw->counters,
+									   dw->stream, &dw->launches ) );
+		}
 		dw->compValid = 0;
 		solved = true;
+	}
+	else if ( dw->defer )
+	{
+		/* batched stepping records one-CTA worlds only */
+		return (int)cudaErrorNotSupported;
 	}
 	else if ( dw->solverMode == B2G_SOLVER_COMPONENTS && dw->compSkip > 0 )
 	{
@@ -1522,11 +1895,9 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	}
 	if ( solved )
 	{
-		CK( cudaEventRecord( dw->ev[7], dw->stream ) );
-		k_finalizeBodies<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( f );
-		dw->launches += 1;
-		CK( cudaGetLastError() );
-		CK( cudaEventRecord( dw->ev[8], dw->stream ) );
+		dev_event( dw, dw->ev[7] );
+		CK2( ( dev_launch<d_finalizeArgs, b_finalize, 8>( dw, DK_FINALIZE, blocks( awakeCount ), f ) ) );
+		dev_event( dw, dw->ev[8] );
 	}
 	else if ( dw->solverMode == B2G_SOLVER_PERSISTENT )
 	{
@@ -1626,27 +1997,36 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 		CK( cudaGetLastError() );
 
 
-		CK( cudaEventRecord( dw->ev[7], dw->stream ) );
-		k_finalizeBodies<<<blocks( awakeCount ), B2G_THREADS, 0, dw->stream>>>( f );
-		dw->launches += 1;
-		CK( cudaGetLastError() );
-		CK( cudaEventRecord( dw->ev[8], dw->stream ) );
+		dev_event( dw, dw->ev[7] );
+		CK2( ( dev_launch<d_finalizeArgs, b_finalize, 8>( dw, DK_FINALIZE, blocks( awakeCount ), f ) ) );
+		dev_event( dw, dw->ev[8] );
 	}
 	/* the counters and the first `window` enlarged-proxy records come back in one wait */
 	if ( dw->recWindow < 64 ) dw->recWindow = 64;
 	int recWindow = dw->recWindow < shapeTotal ? dw->recWindow : shapeTotal;
 	CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( float ) ) );
-	dw->d2hBytes += (long long)( sizeof( b2gStepCounters ) + (size_t)recWindow * 32 );
-	CK( cudaMemcpyAsync( dw->hCounters, dw->counters, sizeof( b2gStepCounters ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
 	if ( recWindow > 0 )
 	{
-		CK( cudaMemcpyAsync( dw->hRecsRaw, dw->enlargedRecs, (size_t)recWindow * 4 * sizeof( int ), cudaMemcpyDeviceToHost,
-							 dw->stream ) );
-		CK( cudaMemcpyAsync( dw->hBoxesRaw, dw->enlargedBoxes, (size_t)recWindow * sizeof( float4 ), cudaMemcpyDeviceToHost,
-							 dw->stream ) );
+		CK2( dev_d2h( dw, dw->hRecsRaw, dw->enlargedRecs, (size_t)recWindow * 4 * sizeof( int ) ) );
+		CK2( dev_d2h( dw, dw->hBoxesRaw, dw->enlargedBoxes, (size_t)recWindow * sizeof( float4 ) ) );
 	}
-	CK2( drain( dw ) );
+	dw->pendingRecWindow = recWindow;
+	dw->pendingShapeTotal = shapeTotal;
+	dw->pendingSolved = solved ? 1 : 0;
+	return 0;
+}
+
+/* after the wait: status and the enlarged-proxy records in ascending awake index */
+extern "C" int b2gDev_SolveCollect( b2gDeviceWorld* dw, const int** outRecs, int* outCount, const float** outBoxes,
+									 int* outStatus )
+{
+	int recWindow = dw->pendingRecWindow, shapeTotal = dw->pendingShapeTotal;
+	bool solved = dw->pendingSolved != 0;
+	d_deferred* deferred = dw->defer;
+	dw->defer = NULL;
+	if ( deferred == NULL )
 	{
 		float ms = 0.0f;
 		cudaEventElapsedTime( &ms, dw->ev[6], dw->ev[7] );
@@ -1673,11 +2053,8 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 	{
 		CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * n, sizeof( int ) ) );
 		CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * n, sizeof( float ) ) );
-		dw->d2hBytes += (long long)( n - recWindow ) * 32;
-		CK( cudaMemcpyAsync( dw->hRecsRaw + 4 * recWindow, dw->enlargedRecs + 4 * recWindow, (size_t)( n - recWindow ) * 4 * sizeof( int ),
-							 cudaMemcpyDeviceToHost, dw->stream ) );
-		CK( cudaMemcpyAsync( dw->hBoxesRaw + 4 * recWindow, dw->enlargedBoxes + recWindow, (size_t)( n - recWindow ) * sizeof( float4 ),
-							 cudaMemcpyDeviceToHost, dw->stream ) );
+		CK2( dev_d2h( dw, dw->hRecsRaw + 4 * recWindow, dw->enlargedRecs + 4 * recWindow, (size_t)( n - recWindow ) * 4 * sizeof( int ) ) );
+		CK2( dev_d2h( dw, dw->hBoxesRaw + 4 * recWindow, dw->enlargedBoxes + recWindow, (size_t)( n - recWindow ) * sizeof( float4 ) ) );
 		CK2( drain( dw ) );
 	}
 	dw->recWindow = 2 * n > 64 ? 2 * n : 64;
@@ -1699,12 +2076,37 @@ extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const i
 			memcpy( dw->hBoxes + 4 * i, boxes + 4 * keys[i].order, 4 * sizeof( float ) );
 		}
 	}
-	CK( cudaEventRecord( dw->ev[5], dw->stream ) );
+	dw->defer = deferred;
+	dev_event( dw, dw->ev[5] );
 	*outRecs = dw->hRecs;
 	*outBoxes = dw->hBoxes;
 	*outCount = n;
 	*outStatus = dw->hCounters->status;
 	return 0;
+}
+
+extern "C" int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* p, const int* activeColors, int activeColorCount,
+							  const int* colorContactCounts, const int* colorJointCounts, int awakeCount, const int** outRecs,
+							  int* outCount, const float** outBoxes, int* outStatus )
+{
+	(void)colorContactCounts;
+	(void)colorJointCounts;
+	CK2( b2gDev_SolveIssue( dw, p, activeColors, activeColorCount, awakeCount ) );
+	CK2( drain( dw ) );
+	return b2gDev_SolveCollect( dw, outRecs, outCount, outBoxes, outStatus );
+}
+
+/* whether a world's solve runs as one CTA (and can be batched): the same test as the
+   solver's dispatch */
+extern "C" int b2gDev_SolveFitsOneBlock( b2gDeviceWorld* dw, int awakeCount )
+{
+	int total = dw->colorOffsets[B2_GRAPH_COLOR_COUNT];
+	int overflow = total - dw->colorOffsets[B2G_OVERFLOW_INDEX];
+	int jointTotal = dw->jointOffsets[B2_GRAPH_COLOR_COUNT];
+	int jointOverflow = jointTotal - dw->jointOffsets[B2G_OVERFLOW_INDEX];
+	long long bytes = (long long)B2G_BIN_BODY_BYTES * awakeCount + (long long)B2G_BIN_CONTACT_BYTES * total +
+					  (long long)B2G_BIN_JOINT_BYTES * jointTotal;
+	return dw->solverMode == B2G_SOLVER_COMPONENTS && overflow + jointOverflow == 0 && bytes <= B2G_WORLD_BIN_MAX_BYTES;
 }
 
 extern "C" int b2gDev_Synchronize( b2gDeviceWorld* dw ) { return (int)cudaStreamSynchronize( dw->stream ); }
@@ -1729,3 +2131,317 @@ extern "C" void b2gDev_Timings( b2gDeviceWorld* dw, float* out, long long* traff
 }
 
 extern "C" void* b2gDev_Stream( b2gDeviceWorld* dw ) { return (void*)dw->stream; }
+
+/* ======================= batched flush of recorded device work ======================= */
+
+/* one copy of a flush: device to device (uploads from the flush's staging, grown buffers,
+   downloads into the flush's download area) */
+struct d_copyOp
+{
+	unsigned char* dst;
+	const unsigned char* src; /* an offset into the flush's staging when fromStaging */
+	long long bytes;
+	int value; /* >= 0: fill with this byte instead of copying */
+	int fromStaging;
+};
+
+__global__ void k_batchCopy( const d_copyOp* __restrict__ ops, int count, const unsigned char* __restrict__ staging )
+{
+	d_copyOp op = ops[blockIdx.x];
+	if ( op.fromStaging ) op.src = staging + (uintptr_t)op.src;
+	long long n = op.bytes;
+	bool vec = ( ( (uintptr_t)op.dst | (uintptr_t)op.src | (uintptr_t)n ) & 15 ) == 0;
+	if ( op.value >= 0 )
+	{
+		unsigned char v = (unsigned char)op.value;
+		for ( long long i = threadIdx.x; i < n; i += blockDim.x ) op.dst[i] = v;
+	}
+	else if ( vec )
+	{
+		const uint4* s4 = (const uint4*)op.src;
+		uint4* d4 = (uint4*)op.dst;
+		for ( long long i = threadIdx.x; i < n / 16; i += blockDim.x ) d4[i] = s4[i];
+	}
+	else
+	{
+		for ( long long i = threadIdx.x; i < n; i += blockDim.x ) op.dst[i] = op.src[i];
+	}
+}
+
+struct b2gDevBatch
+{
+	cudaStream_t stream;
+	unsigned char *hBlob, *dBlob, *hDown, *dDown;
+	long long blobCap, downCap;
+	std::vector<unsigned char> blob;
+	long long launches;
+};
+
+extern "C" int b2gDev_BatchCreate( b2gDevBatch** out )
+{
+	b2gDevBatch* b = new b2gDevBatch();
+	/* a blocking stream, ordered after buffer growth on the legacy default stream */
+	CK( cudaStreamCreate( &b->stream ) );
+	*out = b;
+	return 0;
+}
+
+extern "C" void b2gDev_BatchDestroy( b2gDevBatch* b )
+{
+	if ( b == NULL ) return;
+	cudaStreamSynchronize( b->stream );
+	if ( b->hBlob ) cudaFreeHost( b->hBlob );
+	if ( b->dBlob ) cudaFree( b->dBlob );
+	if ( b->hDown ) cudaFreeHost( b->hDown );
+	if ( b->dDown ) cudaFree( b->dDown );
+	cudaStreamDestroy( b->stream );
+	delete b;
+}
+
+/* switch a world between issuing its device work and recording it for a flush */
+extern "C" int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on )
+{
+	if ( on )
+	{
+		/* work issued before must be done before recorded work replays on the flush stream */
+		CK( cudaStreamSynchronize( dw->stream ) );
+		if ( dw->defer == NULL ) dw->defer = new d_deferred();
+		dw->upUsed = 0;
+	}
+	else
+	{
+		delete dw->defer;
+		dw->defer = NULL;
+	}
+	return 0;
+}
+
+static int d_reserve( unsigned char** h, unsigned char** d, long long* cap, long long need )
+{
+	if ( need <= *cap ) return 0;
+	long long nc = *cap > 0 ? *cap : ( 1LL << 20 );
+	while ( nc < need ) nc *= 2;
+	if ( *h ) CK( cudaFreeHost( *h ) );
+	if ( *d ) CK( cudaFree( *d ) );
+	*h = NULL;
+	*d = NULL;
+	CK( cudaMallocHost( (void**)h, (size_t)nc ) );
+	CK( cudaMalloc( (void**)d, (size_t)nc ) );
+	*cap = nc;
+	return 0;
+}
+
+/* a level of the replay: at most one unit of every world, run together */
+struct d_levelPlan
+{
+	long long copies, copyCount;						  /* blob offsets of the level's copy table */
+	long long recs[DK_COUNT], recCount[DK_COUNT];		  /* record tables per kernel kind */
+	int blocks[DK_COUNT];								  /* total blocks per kernel kind */
+	int smem;											  /* largest one-CTA world solve */
+};
+
+template <class T> static long long d_blobPush( std::vector<unsigned char>& blob, const T* items, long long count )
+{
+	long long at = d_alignArgs( (long long)blob.size() );
+	blob.resize( (size_t)( at + count * (long long)sizeof( T ) ) );
+	if ( count > 0 ) memcpy( blob.data() + at, items, (size_t)count * sizeof( T ) );
+	return at;
+}
+
+template <class Args, void ( *Body )( const Args&, int, int ), int MinBlocks>
+static int d_launchBatched( b2gDevBatch* b, const d_levelPlan& L, int kind )
+{
+	if ( L.recCount[kind] == 0 ) return 0;
+	k_batched<Args, Body, MinBlocks><<<L.blocks[kind], B2G_THREADS, 0, b->stream>>>(
+		(const d_batchRec*)( b->dBlob + L.recs[kind] ), (int)L.recCount[kind], b->dBlob );
+	b->launches += 1;
+	return (int)cudaGetLastError();
+}
+
+/* replay the recorded work of `n` worlds: every world's records run in order; records of
+   different worlds at the same position run in one launch per kind. One upload, one
+   download and one wait in all. */
+extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds, int n )
+{
+	/* units: a run of consecutive uploads, a run of consecutive downloads, or one other record */
+	std::vector<std::vector<std::pair<int, int>>> units( (size_t)n );
+	size_t levels = 0;
+	for ( int w = 0; w < n; ++w )
+	{
+		const d_deferred* d = worlds[w]->defer;
+		if ( d == NULL ) continue;
+		int count = (int)d->ops.size();
+		for ( int i = 0; i < count; )
+		{
+			int k = d->ops[i].kind;
+			int j = i + 1;
+			if ( k == D_OP_H2D || k == D_OP_D2H )
+				while ( j < count && d->ops[j].kind == k ) ++j;
+			units[w].push_back( std::make_pair( i, j ) );
+			i = j;
+		}
+		levels = units[w].size() > levels ? units[w].size() : levels;
+	}
+	if ( levels == 0 ) return 0;
+	/* the blob: every world's upload bytes and kernel arguments, then the level tables */
+	std::vector<unsigned char>& blob = b->blob;
+	blob.clear();
+	std::vector<long long> upBase( (size_t)n ), argBase( (size_t)n );
+	for ( int w = 0; w < n; ++w )
+	{
+		const d_deferred* d = worlds[w]->defer;
+		if ( d == NULL ) continue;
+		upBase[w] = d_blobPush( blob, d->up.data(), (long long)d->up.size() );
+		argBase[w] = d_blobPush( blob, d->args.data(), (long long)d->args.size() );
+	}
+	/* download layout */
+	long long down = 0;
+	std::vector<std::vector<long long>> downAt( (size_t)n );
+	for ( int w = 0; w < n; ++w )
+	{
+		const d_deferred* d = worlds[w]->defer;
+		if ( d == NULL ) continue;
+		downAt[w].assign( d->ops.size(), -1 );
+		for ( size_t i = 0; i < d->ops.size(); ++i )
+		{
+			if ( d->ops[i].kind != D_OP_D2H ) continue;
+			downAt[w][i] = down;
+			down = d_alignArgs( down + d->ops[i].bytes );
+		}
+	}
+	/* the download area's device address goes into the tables: reserve it first */
+	CK2( d_reserve( &b->hDown, &b->dDown, &b->downCap, down > 0 ? down : 16 ) );
+	std::vector<d_levelPlan> plans( levels );
+	std::vector<d_copyOp> copies;
+	std::vector<d_batchRec> recs[DK_COUNT];
+	std::vector<long long> binOffsets;
+	for ( size_t l = 0; l < levels; ++l )
+	{
+		d_levelPlan& L = plans[l];
+		memset( &L, 0, sizeof( L ) );
+		copies.clear();
+		for ( int k = 0; k < DK_COUNT; ++k ) recs[k].clear();
+		binOffsets.clear();
+		for ( int w = 0; w < n; ++w )
+		{
+			const d_deferred* d = worlds[w]->defer;
+			if ( d == NULL || l >= units[w].size() ) continue;
+			for ( int i = units[w][l].first; i < units[w][l].second; ++i )
+			{
+				const d_deferredOp& op = d->ops[(size_t)i];
+				d_copyOp c;
+				c.value = -1;
+				c.fromStaging = 0;
+				c.bytes = op.bytes;
+				switch ( op.kind )
+				{
+					case D_OP_H2D:
+						c.dst = (unsigned char*)op.dev;
+						c.src = (const unsigned char*)(uintptr_t)( upBase[w] + op.at );
+						c.fromStaging = 1;
+						copies.push_back( c );
+						break;
+					case D_OP_D2D:
+						c.dst = (unsigned char*)op.dev;
+						c.src = (const unsigned char*)op.host;
+						copies.push_back( c );
+						break;
+					case D_OP_D2H:
+						c.dst = b->dDown + downAt[w][(size_t)i];
+						c.src = (const unsigned char*)op.dev;
+						copies.push_back( c );
+						break;
+					case D_OP_MEMSET:
+						c.dst = (unsigned char*)op.dev;
+						c.src = NULL;
+						c.value = op.value & 0xff;
+						copies.push_back( c );
+						break;
+					default:
+					{
+						int k = op.kernel;
+						if ( k == DK_SOLVE_BIN )
+						{
+							binOffsets.push_back( argBase[w] + op.at );
+							L.smem = op.smem > L.smem ? op.smem : L.smem;
+						}
+						else
+						{
+							d_batchRec r;
+							r.args = argBase[w] + op.at;
+							r.blockBase = L.blocks[k];
+							r.blocks = op.grid;
+							recs[k].push_back( r );
+							L.blocks[k] += op.grid;
+						}
+						break;
+					}
+				}
+			}
+		}
+		L.copyCount = (long long)copies.size();
+		L.copies = d_blobPush( blob, copies.data(), L.copyCount );
+		for ( int k = 0; k < DK_COUNT; ++k )
+		{
+			if ( k == DK_SOLVE_BIN )
+			{
+				L.recCount[k] = (long long)binOffsets.size();
+				L.recs[k] = d_blobPush( blob, binOffsets.data(), L.recCount[k] );
+			}
+			else
+			{
+				L.recCount[k] = (long long)recs[k].size();
+				L.recs[k] = d_blobPush( blob, recs[k].data(), L.recCount[k] );
+			}
+		}
+	}
+	CK2( d_reserve( &b->hBlob, &b->dBlob, &b->blobCap, (long long)blob.size() ) );
+	memcpy( b->hBlob, blob.data(), blob.size() );
+	CK( cudaMemcpyAsync( b->dBlob, b->hBlob, blob.size(), cudaMemcpyHostToDevice, b->stream ) );
+	for ( size_t l = 0; l < levels; ++l )
+	{
+		const d_levelPlan& L = plans[l];
+		if ( L.copyCount > 0 )
+		{
+			k_batchCopy<<<(int)L.copyCount, 256, 0, b->stream>>>( (const d_copyOp*)( b->dBlob + L.copies ), (int)L.copyCount,
+																  b->dBlob );
+			b->launches += 1;
+			CK( cudaGetLastError() );
+		}
+		CK2( ( d_launchBatched<d_markMovedArgs, b_markMoved, 1>( b, L, DK_MARK_MOVED ) ) );
+		CK2( ( d_launchBatched<d_findPairsArgs, b_findPairs, 1>( b, L, DK_FIND_PAIRS ) ) );
+		CK2( ( d_launchBatched<d_packPairsArgs, b_packPairs, 1>( b, L, DK_PACK_PAIRS ) ) );
+		CK2( ( d_launchBatched<d_convertTreeArgs, b_convertTree, 1>( b, L, DK_CONVERT_TREE ) ) );
+		CK2( ( d_launchBatched<d_contactListArgs, b_initContacts, 1>( b, L, DK_INIT_CONTACTS ) ) );
+		CK2( ( d_launchBatched<d_contactListArgs, b_killContacts, 1>( b, L, DK_KILL_CONTACTS ) ) );
+		CK2( ( d_launchBatched<d_collideArgs, b_collide, 1>( b, L, DK_COLLIDE ) ) );
+		CK2( ( d_launchBatched<d_finalizeArgs, b_finalize, 8>( b, L, DK_FINALIZE ) ) );
+		CK2( ( d_launchBatched<d_captureArgs, b_capture, 1>( b, L, DK_CAPTURE ) ) );
+		if ( L.recCount[DK_SOLVE_BIN] > 0 )
+		{
+			CK2( b2gDev_SolveWorldBinBatch( (const long long*)( b->dBlob + L.recs[DK_SOLVE_BIN] ), b->dBlob, (int)L.recCount[DK_SOLVE_BIN],
+											L.smem, b->stream ) );
+			b->launches += 1;
+		}
+	}
+	if ( down > 0 ) CK( cudaMemcpyAsync( b->hDown, b->dDown, (size_t)down, cudaMemcpyDeviceToHost, b->stream ) );
+	CK( cudaStreamSynchronize( b->stream ) );
+	/* downloads land where their records asked; the worlds' records are spent */
+	for ( int w = 0; w < n; ++w )
+	{
+		b2gDeviceWorld* dw = worlds[w];
+		d_deferred* d = dw->defer;
+		if ( d == NULL ) continue;
+		for ( size_t i = 0; i < d->ops.size(); ++i )
+			if ( d->ops[i].kind == D_OP_D2H ) memcpy( d->ops[i].host, b->hDown + downAt[w][i], (size_t)d->ops[i].bytes );
+		d->ops.clear();
+		d->up.clear();
+		d->args.clear();
+		for ( void* r : dw->retired ) cudaFree( r );
+		dw->retired.clear();
+		dw->upUsed = 0;
+	}
+	return 0;
+}
+
+extern "C" long long b2gDev_BatchLaunches( b2gDevBatch* b ) { return b->launches; }

@@ -167,4 +167,4 @@ def test_torch_autograd_function(gpu_lib):
         gv, _, gf = batch.backward(gc)
         assert np.allclose(v0.grad.numpy(), np.stack(gv), rtol=1e-5, atol=1e-8)
         assert np.allclose(f0.grad.numpy(), np.stack(gf), rtol=1e-5, atol=1e-8)
-        assert float(loss) > 0.0
+        assert float(loss.detach()) > 0.0
