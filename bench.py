@@ -212,23 +212,30 @@ def run_batch(args) -> dict:
     threads = args.threads if args.threads > 0 else 4 * max(1, os.cpu_count() or 1)
     dt = 1.0 / 60.0
     lib.b2s_step_batch(handles, n, dt, 4, args.warmup, threads)
+    # the plain per-world loop: b2World_Step on each world in turn
     plain_steps = max(1, min(args.steps, 5))
     t0 = time.perf_counter()
-    lib.b2s_step_batch(handles, n, dt, 4, plain_steps, 1)
+    for s in scenes:
+        s.step(plain_steps)
     plain_s = time.perf_counter() - t0
     for s in scenes:
         s.timings(reset=True)
+    prof = np.zeros(12, np.float32)
+    lib.b2p_batch_profile(prof.ctypes.data, 1)
+    launches0 = float(prof[5])
     with ClockSampler(0) as clocks:
         t0 = time.perf_counter()
         lib.b2s_step_batch(handles, n, dt, 4, args.steps, threads)
         batch_s = time.perf_counter() - t0
-    launches = 0
+    lib.b2p_batch_profile(prof.ctypes.data, 1)
     h2d = d2h = 0
     for s in scenes:
         _, traffic = s.timings(reset=True)
         h2d += int(traffic[0])
         d2h += int(traffic[1])
-        launches += int(traffic[2])
+    launches = int(prof[5] - launches0)
+    profile = {k: float(v) / args.steps for k, v in
+               zip(["begin", "pairs", "collide", "finish", "flush", "_", "flush_assembly", "flush_wait"], prof) if k != "_"}
     # end to end: the batched step plus every world's move events
     events = __import__("numpy").zeros((max(s.body_count for s in scenes), 4), "float32")
     e2e_steps = max(1, min(args.steps, 20))
@@ -242,7 +249,7 @@ def run_batch(args) -> dict:
         s.close()
     return {"dyn": dyn, "batch_s": batch_s, "plain_s": plain_s, "plain_steps": plain_steps, "threads": threads,
             "launches": launches, "h2d": h2d / args.steps, "d2h": d2h / args.steps, "clocks": clocks.summary,
-            "e2e_value": dyn * e2e_steps / e2e_s}
+            "e2e_value": dyn * e2e_steps / e2e_s, "profile": profile}
 
 
 def run_diff(args) -> dict:
@@ -295,9 +302,16 @@ def run_diff(args) -> dict:
         forward(warm_steps)
         backward()
     plain_s = forward(args.steps, record=False)
+    prof = np.zeros(12, np.float32)
+    lib.b2p_batch_profile(prof.ctypes.data, 1)
+    launches0 = float(prof[5])
     with ClockSampler(0) as clocks:
         fwd_s = forward(args.steps)
+        lib.b2p_batch_profile(prof.ctypes.data, 1)
         bwd_s, gv, gf = backward()
+    fwd_launches = int(prof[5] - launches0)
+    profile = {k: float(v) / args.steps for k, v in
+               zip(["begin", "pairs", "collide", "finish", "flush", "_", "flush_assembly", "flush_wait"], prof) if k != "_"}
     adj_ms, launches = batch.backward_ms()
     tape_bytes = 0
     for w in range(min(n, 8)):
@@ -305,8 +319,9 @@ def run_diff(args) -> dict:
     tape_bytes = tape_bytes * n / min(n, 8)
     finite = all(np.isfinite(g).all() for g in gv) and all(np.isfinite(g).all() for g in gf)
     batch.close()
-    return {"dyn": dyn, "fwd_s": fwd_s, "bwd_s": bwd_s, "plain_s": plain_s, "adj_ms": adj_ms, "launches": launches,
-            "threads": threads, "clocks": clocks.summary, "tape_bytes": tape_bytes, "finite": finite}
+    return {"dyn": dyn, "fwd_s": fwd_s, "bwd_s": bwd_s, "plain_s": plain_s, "adj_ms": adj_ms,
+            "launches": launches + fwd_launches, "threads": threads, "clocks": clocks.summary, "tape_bytes": tape_bytes,
+            "finite": finite, "profile": profile}
 
 
 def run_cpu_sample(args, budget_s: float, max_steps: int) -> dict:
@@ -405,7 +420,7 @@ def main() -> None:
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded scene builders)", "config": config,
             "forward": {"seconds": r["fwd_s"], "value": r["dyn"] * args.steps / r["fwd_s"],
-                        "without_recording_seconds": r["plain_s"]},
+                        "without_recording_seconds": r["plain_s"], "batch_ms_per_step": r["profile"]},
             "adjoint": {"seconds": r["bwd_s"], "device_ms": r["adj_ms"], "over_forward": r["bwd_s"] / r["fwd_s"],
                         "gradients_finite": r["finite"]},
             "roofline": {"bound": "hbm", "kernel": "k_adjointStep", "achieved": achieved, "peak": pk["hbm_gbs"],
@@ -437,6 +452,7 @@ def main() -> None:
             "e2e": {"value": r["e2e_value"], "unit": "body-steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "read": "every world's move events after every batched step"},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
+            "batch_ms_per_step": r["profile"],
         }
         print(json.dumps(line))
         return

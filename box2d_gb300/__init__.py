@@ -64,6 +64,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2s_get_friction": (None, [c_int, c_p, c_int]),
         "b2s_get_centers": (None, [c_int, c_p]),
         "b2s_body_ids": (None, [c_int, c_p]),
+        "b2p_batch_profile": (None, [c_p, c_int]),
         "b2Diff_CreateTape": (c_p, [c_p, c_int]),
         "b2Diff_DestroyTape": (None, [c_p]),
         "b2Diff_Record": (None, [c_p, ctypes.c_bool]),

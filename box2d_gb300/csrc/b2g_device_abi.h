@@ -366,11 +366,15 @@ typedef struct b2gDevBatch b2gDevBatch;
 int b2gDev_BatchCreate( b2gDevBatch** out );
 void b2gDev_BatchDestroy( b2gDevBatch* batch );
 int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on );
-int b2gDev_BatchFlush( b2gDevBatch* batch, b2gDeviceWorld* const* worlds, int count );
+/* runs fn(ctx, i) for i in [0, count) on the caller's threads */
+typedef void ( *b2gParallelFor )( void* pool, int count, void ( *fn )( void* ctx, int index ), void* ctx );
+int b2gDev_BatchFlush( b2gDevBatch* batch, b2gDeviceWorld* const* worlds, int count, b2gParallelFor parallelFor, void* pool );
 long long b2gDev_BatchLaunches( b2gDevBatch* batch );
+void b2gDev_BatchTimes( b2gDevBatch* batch, double* assembleMs, double* waitMs, int reset );
 
 /* bookkeeping for profiles */
 int b2gDev_Synchronize( b2gDeviceWorld* dw );
+int b2gDev_DeviceSynchronize( void );
 void b2gDev_Timings( b2gDeviceWorld* dw, float* stageMs, long long* traffic, int reset );
 void* b2gDev_Stream( b2gDeviceWorld* dw );
 

@@ -20,6 +20,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include <vector>
 
@@ -1336,14 +1337,35 @@ extern "C" int b2gDev_CaptureTape( b2gDeviceWorld* dw, const b2gStepParams* p, i
 	long long bytes = b2gTapeStepBytes( bodyCount, awakeCount, slotCount );
 	if ( *used + bytes > *capacity )
 	{
-		long long cap = *capacity > 0 ? *capacity : ( 1LL << 20 );
-		while ( cap < *used + bytes ) cap *= 2;
+		/* room for 128 records of this size at first, then four times as much: growing is
+		   an allocation and a copy, which many worlds recording together should rarely pay */
+		long long cap = *capacity > 0 ? 4 * *capacity : 128 * bytes;
+		if ( cap < ( 1LL << 20 ) ) cap = 1LL << 20;
+		while ( cap < *used + bytes ) cap *= 4;
 		void* grown = NULL;
-		CK( cudaMallocAsync( &grown, (size_t)cap, dw->stream ) );
-		if ( *used > 0 ) CK( cudaMemcpyAsync( grown, *arena, (size_t)*used, cudaMemcpyDeviceToDevice, dw->stream ) );
-		if ( *arena != NULL ) CK( cudaFreeAsync( *arena, dw->stream ) );
-		/* recorded work runs on another stream: the new arena must exist before the flush */
-		if ( dw->defer ) CK( cudaStreamSynchronize( dw->stream ) );
+		CK( cudaMalloc( &grown, (size_t)cap ) );
+		if ( *arena != NULL )
+		{
+			if ( dw->defer )
+			{
+				/* recorded captures of earlier steps have run (every flush waits), but this
+				   step's records may not: copy in order at the flush */
+				d_deferredOp op;
+				memset( &op, 0, sizeof( op ) );
+				op.kind = D_OP_D2D;
+				op.dev = grown;
+				op.host = *arena;
+				op.bytes = *used;
+				if ( *used > 0 ) dw->defer->ops.push_back( op );
+				dw->retired.push_back( *arena );
+			}
+			else
+			{
+				if ( *used > 0 ) CK( cudaMemcpyAsync( grown, *arena, (size_t)*used, cudaMemcpyDeviceToDevice, dw->stream ) );
+				CK( cudaStreamSynchronize( dw->stream ) );
+				CK( cudaFree( *arena ) );
+			}
+		}
 		*arena = grown;
 		*capacity = cap;
 	}
@@ -1515,6 +1537,8 @@ static int findPairsIssue( b2gDeviceWorld* dw, int n )
 {
 	CK2( grow( dw, (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
 	CK2( grow( dw, (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
+	/* recorded work reads everything back: a second wait would cost a flush */
+	if ( dw->defer ) dw->pairWindow = n * dw->pairPerMove;
 	int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
 	CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * window, sizeof( int ) ) );
 	CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
@@ -1666,6 +1690,7 @@ extern "C" int b2gDev_CollideIssue( b2gDeviceWorld* dw, const b2gStepParams* p, 
 		dev_event( dw, dw->ev[3] );
 	}
 	if ( dw->changeWindow < 64 ) dw->changeWindow = 64;
+	if ( dw->defer ) dw->changeWindow = contactIdCapacity > 64 ? contactIdCapacity : 64;
 	int window = dw->changeWindow < contactIdCapacity ? dw->changeWindow : contactIdCapacity;
 	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( window > 0 ? window : 1 ), sizeof( int ) ) );
 	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
@@ -2003,6 +2028,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	}
 	/* the counters and the first `window` enlarged-proxy records come back in one wait */
 	if ( dw->recWindow < 64 ) dw->recWindow = 64;
+	if ( dw->defer ) dw->recWindow = shapeTotal > 64 ? shapeTotal : 64;
 	int recWindow = dw->recWindow < shapeTotal ? dw->recWindow : shapeTotal;
 	CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( int ) ) );
 	CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( float ) ) );
@@ -2109,7 +2135,11 @@ extern "C" int b2gDev_SolveFitsOneBlock( b2gDeviceWorld* dw, int awakeCount )
 	return dw->solverMode == B2G_SOLVER_COMPONENTS && overflow + jointOverflow == 0 && bytes <= B2G_WORLD_BIN_MAX_BYTES;
 }
 
-extern "C" int b2gDev_Synchronize( b2gDeviceWorld* dw ) { return (int)cudaStreamSynchronize( dw->stream ); }
+/* the world's wait: its issued work is done and its upload arena free again */
+extern "C" int b2gDev_Synchronize( b2gDeviceWorld* dw ) { return drain( dw ); }
+
+/* every stream of the device is idle (before a batch starts recording) */
+extern "C" int b2gDev_DeviceSynchronize( void ) { return (int)cudaDeviceSynchronize(); }
 
 /* accumulated device milliseconds per stage since the last reset: pairs (query and
    copies), narrowphase kernel, solver (prepare through store), finalize; and traffic */
@@ -2175,7 +2205,26 @@ struct b2gDevBatch
 	long long blobCap, downCap;
 	std::vector<unsigned char> blob;
 	long long launches;
+	double assembleMs, waitMs;
 };
+
+static double d_nowMs( void )
+{
+	struct timespec ts;
+	clock_gettime( CLOCK_MONOTONIC, &ts );
+	return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+extern "C" void b2gDev_BatchTimes( b2gDevBatch* b, double* assembleMs, double* waitMs, int reset )
+{
+	*assembleMs = b->assembleMs;
+	*waitMs = b->waitMs;
+	if ( reset )
+	{
+		b->assembleMs = 0.0;
+		b->waitMs = 0.0;
+	}
+}
 
 extern "C" int b2gDev_BatchCreate( b2gDevBatch** out )
 {
@@ -2203,8 +2252,7 @@ extern "C" int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on )
 {
 	if ( on )
 	{
-		/* work issued before must be done before recorded work replays on the flush stream */
-		CK( cudaStreamSynchronize( dw->stream ) );
+		/* the caller has made the world's stream idle (b2gDev_DeviceSynchronize) */
 		if ( dw->defer == NULL ) dw->defer = new d_deferred();
 		dw->upUsed = 0;
 	}
@@ -2261,8 +2309,54 @@ static int d_launchBatched( b2gDevBatch* b, const d_levelPlan& L, int kind )
 /* replay the recorded work of `n` worlds: every world's records run in order; records of
    different worlds at the same position run in one launch per kind. One upload, one
    download and one wait in all. */
-extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds, int n )
+struct d_flushCopy
 {
+	b2gDevBatch* b;
+	b2gDeviceWorld* const* worlds;
+	const long long* upBase;
+	const long long* argBase;
+	const std::vector<long long>* downAt;
+};
+
+/* world w's upload bytes and kernel arguments into the pinned staging */
+static void d_stageWorld( void* ctx, int w )
+{
+	const d_flushCopy* c = (const d_flushCopy*)ctx;
+	const d_deferred* d = c->worlds[w]->defer;
+	if ( d == NULL ) return;
+	if ( d->up.size() > 0 ) memcpy( c->b->hBlob + c->upBase[w], d->up.data(), d->up.size() );
+	if ( d->args.size() > 0 ) memcpy( c->b->hBlob + c->argBase[w], d->args.data(), d->args.size() );
+}
+
+/* world w's downloads to where its records asked, then its records are spent */
+static void d_deliverWorld( void* ctx, int w )
+{
+	const d_flushCopy* c = (const d_flushCopy*)ctx;
+	b2gDeviceWorld* dw = c->worlds[w];
+	d_deferred* d = dw->defer;
+	if ( d == NULL ) return;
+	for ( size_t i = 0; i < d->ops.size(); ++i )
+		if ( d->ops[i].kind == D_OP_D2H ) memcpy( d->ops[i].host, c->b->hDown + c->downAt[w][i], (size_t)d->ops[i].bytes );
+	d->ops.clear();
+	d->up.clear();
+	d->args.clear();
+	dw->upUsed = 0;
+}
+
+static void d_serialFor( void* pool, int count, void ( *fn )( void*, int ), void* ctx )
+{
+	(void)pool;
+	for ( int i = 0; i < count; ++i ) fn( ctx, i );
+}
+
+/* replay the recorded work of `n` worlds: every world's records run in order; records of
+   different worlds at the same position run in one launch per kind. One upload, one
+   download and one wait in all. `pf` runs the per-world staging and delivery copies on the
+   caller's threads (NULL: serially). */
+extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds, int n, b2gParallelFor pf, void* pool )
+{
+	if ( pf == NULL ) pf = d_serialFor;
+	double t0 = d_nowMs();
 	/* units: a run of consecutive uploads, a run of consecutive downloads, or one other record */
 	std::vector<std::vector<std::pair<int, int>>> units( (size_t)n );
 	size_t levels = 0;
@@ -2283,17 +2377,19 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 		levels = units[w].size() > levels ? units[w].size() : levels;
 	}
 	if ( levels == 0 ) return 0;
-	/* the blob: every world's upload bytes and kernel arguments, then the level tables */
-	std::vector<unsigned char>& blob = b->blob;
-	blob.clear();
-	std::vector<long long> upBase( (size_t)n ), argBase( (size_t)n );
+	/* staging layout: every world's upload bytes and kernel arguments, then the tables */
+	std::vector<long long> upBase( (size_t)n, 0 ), argBase( (size_t)n, 0 );
+	long long at = 0;
 	for ( int w = 0; w < n; ++w )
 	{
 		const d_deferred* d = worlds[w]->defer;
 		if ( d == NULL ) continue;
-		upBase[w] = d_blobPush( blob, d->up.data(), (long long)d->up.size() );
-		argBase[w] = d_blobPush( blob, d->args.data(), (long long)d->args.size() );
+		upBase[w] = at;
+		at = d_alignArgs( at + (long long)d->up.size() );
+		argBase[w] = at;
+		at = d_alignArgs( at + (long long)d->args.size() );
 	}
+	const long long tableBase = at;
 	/* download layout */
 	long long down = 0;
 	std::vector<std::vector<long long>> downAt( (size_t)n );
@@ -2309,8 +2405,10 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 			down = d_alignArgs( down + d->ops[i].bytes );
 		}
 	}
-	/* the download area's device address goes into the tables: reserve it first */
 	CK2( d_reserve( &b->hDown, &b->dDown, &b->downCap, down > 0 ? down : 16 ) );
+	/* the level tables (offsets relative to the staging base) */
+	std::vector<unsigned char>& blob = b->blob;
+	blob.clear();
 	std::vector<d_levelPlan> plans( levels );
 	std::vector<d_copyOp> copies;
 	std::vector<d_batchRec> recs[DK_COUNT];
@@ -2380,24 +2478,29 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 			}
 		}
 		L.copyCount = (long long)copies.size();
-		L.copies = d_blobPush( blob, copies.data(), L.copyCount );
+		L.copies = tableBase + d_blobPush( blob, copies.data(), L.copyCount );
 		for ( int k = 0; k < DK_COUNT; ++k )
 		{
 			if ( k == DK_SOLVE_BIN )
 			{
 				L.recCount[k] = (long long)binOffsets.size();
-				L.recs[k] = d_blobPush( blob, binOffsets.data(), L.recCount[k] );
+				L.recs[k] = tableBase + d_blobPush( blob, binOffsets.data(), L.recCount[k] );
 			}
 			else
 			{
 				L.recCount[k] = (long long)recs[k].size();
-				L.recs[k] = d_blobPush( blob, recs[k].data(), L.recCount[k] );
+				L.recs[k] = tableBase + d_blobPush( blob, recs[k].data(), L.recCount[k] );
 			}
 		}
 	}
-	CK2( d_reserve( &b->hBlob, &b->dBlob, &b->blobCap, (long long)blob.size() ) );
-	memcpy( b->hBlob, blob.data(), blob.size() );
-	CK( cudaMemcpyAsync( b->dBlob, b->hBlob, blob.size(), cudaMemcpyHostToDevice, b->stream ) );
+	long long total = tableBase + (long long)blob.size();
+	CK2( d_reserve( &b->hBlob, &b->dBlob, &b->blobCap, total ) );
+	d_flushCopy fc = { b, worlds, upBase.data(), argBase.data(), downAt.data() };
+	pf( pool, n, d_stageWorld, &fc );
+	memcpy( b->hBlob + tableBase, blob.data(), blob.size() );
+	double t1 = d_nowMs();
+	b->assembleMs += t1 - t0;
+	CK( cudaMemcpyAsync( b->dBlob, b->hBlob, (size_t)total, cudaMemcpyHostToDevice, b->stream ) );
 	for ( size_t l = 0; l < levels; ++l )
 	{
 		const d_levelPlan& L = plans[l];
@@ -2426,20 +2529,13 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 	}
 	if ( down > 0 ) CK( cudaMemcpyAsync( b->hDown, b->dDown, (size_t)down, cudaMemcpyDeviceToHost, b->stream ) );
 	CK( cudaStreamSynchronize( b->stream ) );
-	/* downloads land where their records asked; the worlds' records are spent */
+	b->waitMs += d_nowMs() - t1;
+	pf( pool, n, d_deliverWorld, &fc );
 	for ( int w = 0; w < n; ++w )
 	{
 		b2gDeviceWorld* dw = worlds[w];
-		d_deferred* d = dw->defer;
-		if ( d == NULL ) continue;
-		for ( size_t i = 0; i < d->ops.size(); ++i )
-			if ( d->ops[i].kind == D_OP_D2H ) memcpy( d->ops[i].host, b->hDown + downAt[w][i], (size_t)d->ops[i].bytes );
-		d->ops.clear();
-		d->up.clear();
-		d->args.clear();
 		for ( void* r : dw->retired ) cudaFree( r );
 		dw->retired.clear();
-		dw->upUsed = 0;
 	}
 	return 0;
 }

@@ -148,12 +148,24 @@ typedef struct h_world
 	int lastStatus;
 	int continuousSweeps, continuousHits; /* accumulated device continuous-collision counters */
 	struct h_tapeWorld* tape;			  /* differentiable-stepping recorder (diff.c), or NULL */
+	/* the step in progress, between its phases (step.c) */
+	b2gStepParams stepParams;
+	float stepTimeStep;
+	uint64_t stepTicks, stepT0;
+	int stepPairsIssued, stepSolveIssued, stepSolveLate;
 	void* rebuildWorker; /* host thread for the tree rebuild (step.c) */
 } h_world;
 
 h_world* h_worldFromId( b2WorldId id );
 /* appends the step about to be solved to the world's tape when recording (diff.c) */
 void h_tapeCapture( h_world* w, const b2gStepParams* params );
+/* the step's phases (step.c): begin (issues the pair query), pairs (issues the narrowphase),
+   collide (issues the solver), solve issue (a solve held back from a batch), finish */
+int h_stepBegin( h_world* w, float timeStep, int subStepCount );
+void h_stepPairs( h_world* w );
+int h_stepCollide( h_world* w, int oneBlockOnly );
+int h_stepSolveIssue( h_world* w );
+void h_stepFinish( h_world* w );
 void h_tapeDetach( h_world* w );
 h_world* h_worldByIndex( int index );
 
@@ -197,6 +209,7 @@ enum
 	H_PHASE_UPLOADS = 6, /* contact / color / joint uploads */
 	H_PHASE_SOLVE = 7,	 /* device solver + finalize call, includes its wait */
 	H_PHASE_ENLARGE = 8,
+	H_PHASE_TAPE = 9, /* tape capture of differentiable stepping */
 	H_PHASE_COUNT = 10,
 };
 

@@ -150,10 +150,11 @@ static int h_shouldShapesCollide( b2Filter a, b2Filter b )
    reference's query order (kinematic, static, dynamic trees; DFS child2 first) after the
    self and moved-pair dedupe; the host applies the remaining filters and creates contacts
    newest-first per move, as the reference's prepended pair lists do. */
-static void h_updatePairs( h_world* w )
+/* issue the pair query of the moved proxies; returns whether one was issued */
+static int h_pairsIssue( h_world* w )
 {
 	int moveCount = w->moveArray.count;
-	if ( moveCount == 0 ) return;
+	if ( moveCount == 0 ) return 0;
 	uint64_t lap = b2GetTicks();
 	for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
 	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
@@ -170,10 +171,22 @@ static void h_updatePairs( h_world* w )
 		boxes[4 * i + 3] = node->aabb.upperBound.y;
 		shapeIds[i] = (int)node->userData;
 	}
+	int rc = b2gDev_FindPairsIssue( w->dev, w->moveArray.data, boxes, shapeIds, moveCount );
+	free( boxes );
+	free( shapeIds );
+	if ( rc != 0 ) h_fail( w, "pair query", rc );
+	return 1;
+}
+
+/* after the wait: filter the pairs and create contacts newest-first per move */
+static void h_pairsFinish( h_world* w )
+{
+	int moveCount = w->moveArray.count;
+	uint64_t lap = b2GetTicks();
 	int* pairs = NULL;
 	int* counts = NULL;
 	int total = 0;
-	int rc = b2gDev_FindPairs( w->dev, w->moveArray.data, boxes, shapeIds, moveCount, &pairs, &counts, &total );
+	int rc = b2gDev_FindPairsCollect( w->dev, &pairs, &counts, &total );
 	if ( rc != 0 ) h_fail( w, "pair query", rc );
 	h_lap( w, H_PHASE_PAIR_QUERY, &lap );
 	int offset = 0;
@@ -196,8 +209,6 @@ static void h_updatePairs( h_world* w )
 		}
 		offset += n;
 	}
-	free( boxes );
-	free( shapeIds );
 	h_lap( w, H_PHASE_CONTACT_CREATE, &lap );
 	/* b2UpdateTreesTask (broad_phase.c:401-410), overlapped with the narrowphase and solver */
 	h_postRebuild( w );
@@ -390,64 +401,83 @@ static void h_enlargeProxies( h_world* w, const int* recs, const float* boxes, i
 	}
 }
 
-void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
+/* ---- the step in four phases, split at its three waits (pair query, narrowphase,
+   solver); b2World_Step runs them back to back, b2World_StepBatch runs each phase over
+   many worlds and replaces the waits by one batched flush ---- */
+
+/* phase 1: bookkeeping, device state, the pair query; returns whether work was issued */
+int h_stepBegin( h_world* w, float timeStep, int subStepCount )
 {
-	h_world* w = h_worldFromId( worldId );
-	if ( w == NULL || w->locked ) return;
 	w->moveEvents.count = 0;
 	w->moveEventsValid = 0;
 	w->beginEvents.count = 0;
 	memset( &w->profile, 0, sizeof( w->profile ) );
 	w->locked = 1;
-	uint64_t stepTicks = b2GetTicks();
+	w->stepTicks = b2GetTicks();
+	w->stepTimeStep = timeStep;
 
 	h_ensureDevice( w );
 
-	uint64_t t0 = b2GetTicks();
-	h_updatePairs( w );
-	w->profile.pairs = h_ms( t0 );
-
-	b2gStepParams p;
-	memset( &p, 0, sizeof( p ) );
-	p.dt = timeStep;
-	p.subStepCount = h_maxi( 1, subStepCount );
+	b2gStepParams* p = &w->stepParams;
+	memset( p, 0, sizeof( *p ) );
+	p->dt = timeStep;
+	p->subStepCount = h_maxi( 1, subStepCount );
 	if ( timeStep > 0.0f )
 	{
-		p.inv_dt = 1.0f / timeStep;
-		p.h = timeStep / p.subStepCount;
-		p.inv_h = p.subStepCount * p.inv_dt;
+		p->inv_dt = 1.0f / timeStep;
+		p->h = timeStep / p->subStepCount;
+		p->inv_h = p->subStepCount * p->inv_dt;
 	}
-	float contactHertz = h_min( w->contactHertz, 0.125f * p.inv_h );
-	h_softness cs = h_makeSoft( contactHertz, w->contactDampingRatio, p.h );
-	h_softness ss = h_makeSoft( 2.0f * contactHertz, w->contactDampingRatio, p.h );
-	p.contactBiasRate = cs.biasRate;
-	p.contactMassScale = cs.massScale;
-	p.contactImpulseScale = cs.impulseScale;
-	p.staticBiasRate = ss.biasRate;
-	p.staticMassScale = ss.massScale;
-	p.staticImpulseScale = ss.impulseScale;
-	p.restitutionThreshold = w->restitutionThreshold;
-	p.maxLinearVelocity = w->maxLinearSpeed;
-	p.contactSpeed = w->contactSpeed;
-	p.contactHertz = w->contactHertz;
-	p.contactDampingRatio = w->contactDampingRatio;
-	p.gravityX = w->gravity.x;
-	p.gravityY = w->gravity.y;
-	p.enableWarmStarting = w->enableWarmStarting;
-	p.enableContinuous = w->enableContinuous;
-	p.enableSleep = w->enableSleep;
-	p.enableContactSoftening = w->enableContactSoftening;
-	p.contactRecycleDistance = 10.0f * H_LINEAR_SLOP;
+	float contactHertz = h_min( w->contactHertz, 0.125f * p->inv_h );
+	h_softness cs = h_makeSoft( contactHertz, w->contactDampingRatio, p->h );
+	h_softness ss = h_makeSoft( 2.0f * contactHertz, w->contactDampingRatio, p->h );
+	p->contactBiasRate = cs.biasRate;
+	p->contactMassScale = cs.massScale;
+	p->contactImpulseScale = cs.impulseScale;
+	p->staticBiasRate = ss.biasRate;
+	p->staticMassScale = ss.massScale;
+	p->staticImpulseScale = ss.impulseScale;
+	p->restitutionThreshold = w->restitutionThreshold;
+	p->maxLinearVelocity = w->maxLinearSpeed;
+	p->contactSpeed = w->contactSpeed;
+	p->contactHertz = w->contactHertz;
+	p->contactDampingRatio = w->contactDampingRatio;
+	p->gravityX = w->gravity.x;
+	p->gravityY = w->gravity.y;
+	p->enableWarmStarting = w->enableWarmStarting;
+	p->enableContinuous = w->enableContinuous;
+	p->enableSleep = w->enableSleep;
+	p->enableContactSoftening = w->enableContactSoftening;
+	p->contactRecycleDistance = 10.0f * H_LINEAR_SLOP;
 
-	/* narrowphase + state pass */
-	t0 = b2GetTicks();
-	uint64_t lap = t0;
+	w->stepT0 = b2GetTicks();
+	w->stepPairsIssued = h_pairsIssue( w );
+	return w->stepPairsIssued;
+}
+
+/* phase 2: contacts from the pairs, then the narrowphase is issued */
+void h_stepPairs( h_world* w )
+{
+	if ( w->stepPairsIssued ) h_pairsFinish( w );
+	w->profile.pairs = h_ms( w->stepT0 );
+	w->stepT0 = b2GetTicks();
+	uint64_t lap = w->stepT0;
 	h_flushContacts( w );
 	h_uploadColors( w );
 	h_lap( w, H_PHASE_UPLOADS, &lap );
+	int rc = b2gDev_CollideIssue( w->dev, &w->stepParams, w->contactIdPool.nextIndex );
+	if ( rc != 0 ) h_fail( w, "narrowphase", rc );
+}
+
+/* phase 3: the contact-state pass and graph coloring, then the solver is issued unless
+   `oneBlockOnly` is set and the world's solve is not a one-CTA solve (it is then issued in
+   phase 4); returns whether the solver was issued */
+int h_stepCollide( h_world* w, int oneBlockOnly )
+{
+	uint64_t lap = b2GetTicks();
 	const int* changes = NULL;
 	int changeCount = 0, recycled = 0;
-	int rc = b2gDev_Collide( w->dev, &p, w->contactIdPool.nextIndex, &changes, &changeCount, &recycled );
+	int rc = b2gDev_CollideCollect( w->dev, &changes, &changeCount, &recycled );
 	if ( rc != 0 ) h_fail( w, "narrowphase", rc );
 	h_lap( w, H_PHASE_COLLIDE, &lap );
 	w->recycledContactCount = recycled;
@@ -455,62 +485,87 @@ void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 	h_lap( w, H_PHASE_STATE_PASS, &lap );
 	h_flushContacts( w );
 	h_lap( w, H_PHASE_UPLOADS, &lap );
-	w->profile.collide = h_ms( t0 );
-
-	if ( timeStep > 0.0f )
+	w->profile.collide = h_ms( w->stepT0 );
+	w->stepSolveIssued = 0;
+	w->stepSolveLate = 0;
+	if ( w->stepTimeStep <= 0.0f ) return 0;
+	w->stepT0 = b2GetTicks();
+	lap = w->stepT0;
+	w->stepIndex += 1;
+	h_uploadColors( w );
+	h_uploadJoints( w );
+	h_lap( w, H_PHASE_UPLOADS, &lap );
+	/* fast bodies sweep against the static tree in the finalize stage */
+	if ( w->enableContinuous ) h_uploadTree( w, b2_staticBody );
+	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
+	if ( w->awakeBodyIds.count == 0 ) return 0;
+	if ( oneBlockOnly && b2gDev_SolveFitsOneBlock( w->dev, w->awakeBodyIds.count ) == 0 )
 	{
-		t0 = b2GetTicks();
-		lap = t0;
-		w->stepIndex += 1;
-		h_uploadColors( w );
-		h_uploadJoints( w );
-		/* fast bodies sweep against the static tree in the finalize stage */
-		if ( w->enableContinuous ) h_uploadTree( w, b2_staticBody );
-		int activeColors[B2_GRAPH_COLOR_COUNT];
-		int contactCounts[B2_GRAPH_COLOR_COUNT];
-		int jointCounts[B2_GRAPH_COLOR_COUNT];
-		int activeCount = 0;
-		for ( int i = 0; i < B2_GRAPH_COLOR_COUNT - 1; ++i )
-		{
-			if ( w->colors[i].contactIds.count + w->colors[i].jointIds.count > 0 ) activeColors[activeCount++] = i;
-		}
-		for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
-		{
-			contactCounts[i] = w->colors[i].contactIds.count;
-			jointCounts[i] = w->colors[i].jointIds.count;
-		}
+		w->stepSolveLate = 1;
+		return 0;
+	}
+	return h_stepSolveIssue( w );
+}
+
+int h_stepSolveIssue( h_world* w )
+{
+	int activeColors[B2_GRAPH_COLOR_COUNT];
+	int activeCount = 0;
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT - 1; ++i )
+		if ( w->colors[i].contactIds.count + w->colors[i].jointIds.count > 0 ) activeColors[activeCount++] = i;
+	uint64_t lap = b2GetTicks();
+	if ( w->tape != NULL ) h_tapeCapture( w, &w->stepParams );
+	h_lap( w, H_PHASE_TAPE, &lap );
+	int rc = b2gDev_SolveIssue( w->dev, &w->stepParams, activeColors, activeCount, w->awakeBodyIds.count );
+	if ( rc != 0 ) h_fail( w, "solver", rc );
+	h_lap( w, H_PHASE_SOLVE, &lap );
+	w->stepSolveIssued = 1;
+	return 1;
+}
+
+/* phase 4: enlarged proxies into the broadphase, events, and the step's end */
+void h_stepFinish( h_world* w )
+{
+	uint64_t lap = b2GetTicks();
+	if ( w->stepSolveIssued )
+	{
 		const int* recs = NULL;
 		const float* boxes = NULL;
 		int enlargedCount = 0, status = 0;
-		if ( w->awakeBodyIds.count > 0 )
+		int rc = b2gDev_SolveCollect( w->dev, &recs, &enlargedCount, &boxes, &status );
+		if ( rc != 0 ) h_fail( w, "solver", rc );
+		h_lap( w, H_PHASE_SOLVE, &lap );
+		h_joinRebuild( w );
+		h_lap( w, H_PHASE_TREE_REBUILD, &lap );
+		w->lastStatus = status;
 		{
-			if ( w->tape != NULL ) h_tapeCapture( w, &p );
-			h_lap( w, H_PHASE_UPLOADS, &lap );
-			rc = b2gDev_Solve( w->dev, &p, activeColors, activeCount, contactCounts, jointCounts, w->awakeBodyIds.count, &recs,
-							   &enlargedCount, &boxes, &status );
-			if ( rc != 0 ) h_fail( w, "solver", rc );
-			h_lap( w, H_PHASE_SOLVE, &lap );
-			h_joinRebuild( w );
-			h_lap( w, H_PHASE_TREE_REBUILD, &lap );
-			w->lastStatus = status;
-			{
-				b2gStepCounters sc;
-				b2gDev_LastCounters( w->dev, &sc );
-				w->continuousSweeps += sc.continuousSweeps;
-				w->continuousHits += sc.continuousHits;
-			}
-			if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
-			h_enlargeProxies( w, recs, boxes, enlargedCount );
-			h_lap( w, H_PHASE_ENLARGE, &lap );
+			b2gStepCounters sc;
+			b2gDev_LastCounters( w->dev, &sc );
+			w->continuousSweeps += sc.continuousSweeps;
+			w->continuousHits += sc.continuousHits;
 		}
-		w->profile.solve = h_ms( t0 );
+		if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
+		h_enlargeProxies( w, recs, boxes, enlargedCount );
+		h_lap( w, H_PHASE_ENLARGE, &lap );
 	}
+	if ( w->stepTimeStep > 0.0f ) w->profile.solve = h_ms( w->stepT0 );
 	h_joinRebuild( w );
 	w->hostStateValid = 0;
 	w->jointsHostValid = 0;
-	w->profile.step = h_ms( stepTicks );
+	w->profile.step = h_ms( w->stepTicks );
 	w->endEventArrayIndex = 1 - w->endEventArrayIndex;
 	w->endEvents[w->endEventArrayIndex].count = 0;
 	w->locked = 0;
 	(void)h_cmpInt;
+}
+
+void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w == NULL || w->locked ) return;
+	if ( h_stepBegin( w, timeStep, subStepCount ) ) b2gDev_Synchronize( w->dev );
+	h_stepPairs( w );
+	b2gDev_Synchronize( w->dev );
+	if ( h_stepCollide( w, 0 ) ) b2gDev_Synchronize( w->dev );
+	h_stepFinish( w );
 }

@@ -50,6 +50,13 @@ int b2p_host_profile( uint32_t packedWorldId, float* out, int reset );
 /* The CUDA stream (cudaStream_t) the world's kernels are launched on. */
 void* b2p_stream( uint32_t packedWorldId );
 
+/* Batched stepping (b2World_StepBatch) since the last reset, in milliseconds: out[0..3]
+   the begin, pairs, collide and finish phases on the host threads, out[4] the flushes;
+   out[5] the kernels the flushes launched since the library loaded; out[6], out[7] the
+   flushes' host assembly and their wait for the device; out[8..11] the four phases' thread
+   time summed over worlds (12 floats). */
+void b2p_batch_profile( float* out, int reset );
+
 /* Continuous collision of one world since its creation: out[0] = fast non-bullet bodies
    swept against static shapes, out[1] = sweeps that moved the body back to a time of
    impact (solver.c:384-550). */

@@ -40,7 +40,8 @@ def test_library_exports_every_declared_function():
 
 
 def test_oracle_exports_the_public_api(oracle):
-    skip = {"b2p_status", "b2p_timings", "b2p_stream", "b2p_host_profile", "b2p_contacts_noalloc", "b2World_StepBatch"}
+    skip = {"b2p_status", "b2p_timings", "b2p_stream", "b2p_host_profile", "b2p_contacts_noalloc", "b2World_StepBatch",
+            "b2p_batch_profile"}
     # differentiable stepping (box2d_gb300_diff.h) is an extension of the GB300 library; its
     # checker is the host tangent-linear code, not the oracle's public API
     missing = [n for n in sorted(declared_functions())
