@@ -324,6 +324,31 @@ def run_diff(args) -> dict:
             "finite": finite, "profile": profile}
 
 
+def run_cpu_batch(args, budget_s: float, max_steps: int) -> dict:
+    """The oracle on a sample of the batched workload's worlds (the first `sample` seeds),
+    every host core stepping whole worlds in parallel, as a batch of independent reference
+    worlds would run on a CPU. ctypes releases the interpreter lock during each call."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
+    lib = B.load_library(ROOT / "oracle" / "liboracle.so")
+    threads = max(1, os.cpu_count() or 1)
+    sample = min(args.worlds, 16 * threads)
+    scenes = [B.Scene(lib, kind, a, b, c, seed + i, flags) for i in range(sample)]
+    dyn = sum(s.dynamic_count for s in scenes)
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(lambda s: s.step(max(1, args.warmup)), scenes))
+        t0 = time.perf_counter()
+        n = 0
+        while n < max_steps and time.perf_counter() - t0 < budget_s:
+            list(ex.map(lambda s: s.step(), scenes))
+            n += 1
+        dt = time.perf_counter() - t0
+    for s in scenes:
+        s.close()
+    return {"value": dyn * n / dt, "steps": n, "seconds": dt, "dyn": dyn, "threads": threads, "worlds": sample}
+
+
 def run_cpu_sample(args, budget_s: float, max_steps: int) -> dict:
     """The oracle (CPU restatement of the reference step) on the same workload, with its
     data-parallel loops (narrowphase, solver stages, integration, finalize) on every host
@@ -366,8 +391,6 @@ def main() -> None:
                     help="untimed steps before the warm-up (default: per workload)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-    if args.worlds <= 0:
-        args.worlds = 1024 if args.workload == "diff_batch" else 4096
     if args.workload == "diff_batch" and "--steps" not in sys.argv:
         args.steps = 120
     if args.start_step < 0:
@@ -382,17 +405,23 @@ def main() -> None:
               "l2": "flushed between timed steps (256 MiB write, outside the timed region)",
               "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single world"}
 
+    if args.worlds <= 0:
+        args.worlds = 1024 if args.workload == "diff_batch" else 4096
     if args.impl == "reference":
         if rank != 0:
             return
-        r = run_cpu_sample(args, budget_s=60.0, max_steps=args.steps)
+        batched = args.workload in ("batch_worlds", "diff_batch")
+        r = run_cpu_batch(args, 60.0, args.steps) if batched else run_cpu_sample(args, budget_s=60.0, max_steps=args.steps)
         cores = r["threads"]
+        sample = (f"{r['steps']} steps of {r['worlds']} worlds, one world per task on {cores} threads, C oracle"
+                  if batched else
+                  f"{r['steps']} steps after {args.start_step + args.warmup} untimed steps, C oracle on {cores} threads")
         line = {"metric": "body-steps/s", "value": r["value"], "unit": "body-steps/s", "n_gpus": args.gpus,
                 "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / max(1, r["steps"]),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded scene builders)", "config": config, "impl": "reference",
                 "cpu_baseline": {"value": r["value"], "unit": "body-steps/s", "cores": cores, "kind": "port",
-                                 "sample": f"{r['steps']} steps after {args.start_step + args.warmup} untimed steps, C oracle on {cores} threads"},
+                                 "sample": sample},
                 "e2e": {"value": r["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -407,10 +436,11 @@ def main() -> None:
         achieved = r["tape_bytes"] / (r["adj_ms"] * 1e-3) / 1e9 if r["adj_ms"] > 0 else 0.0
         cpu = None
         if not args.no_cpu_baseline:
-            c = run_cpu_sample(args, budget_s=20.0, max_steps=args.steps)
+            c = run_cpu_batch(args, 20.0, args.steps)
             cpu = {"value": c["value"], "unit": "body-steps/s (forward only: the reference has no adjoint)",
                    "cores": c["threads"], "kind": "port",
-                   "sample": f"{c['steps']} forward steps of one ramp world, C oracle on {c['threads']} threads"}
+                   "sample": f"{c['steps']} forward steps of {c['worlds']} ramp worlds, one world per task on "
+                             f"{c['threads']} threads, C oracle"}
         config.update({"worlds": args.worlds, "host_threads": r["threads"], "steps_per_pass": args.steps,
                        "l2": "inputs larger than L2 (every world's tape), no flush",
                        "timing": "wall clock of the forward pass (recording) and of the adjoint through the public API"})
@@ -438,6 +468,12 @@ def main() -> None:
         if rank != 0:
             return
         r = run_batch(args)
+        r["cpu"] = None
+        if not args.no_cpu_baseline:
+            c = run_cpu_batch(args, 20.0, args.steps)
+            r["cpu"] = {"value": c["value"], "unit": "body-steps/s", "cores": c["threads"], "kind": "port",
+                        "sample": f"{c['steps']} steps of {c['worlds']} worlds, one world per task on "
+                                  f"{c['threads']} threads, C oracle"}
         value = r["dyn"] * args.steps / r["batch_s"]
         plain = r["dyn"] * r["plain_steps"] / r["plain_s"]
         config.update({"worlds": args.worlds, "host_threads": r["threads"],
@@ -448,7 +484,7 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": 1e3 * r["batch_s"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene builders)",
             "config": config, "plain_loop": {"value": plain, "steps": r["plain_steps"], "speedup": value / plain},
-            "roofline": None, "cpu_baseline": None,
+            "roofline": None, "cpu_baseline": r["cpu"],
             "e2e": {"value": r["e2e_value"], "unit": "body-steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "read": "every world's move events after every batched step"},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
