@@ -28,6 +28,8 @@ JOINT_GRID_REF = 6
 HELLO_WORLD = 7
 SHAPE_ZOO = 8
 JOINT_ZOO = 9
+FALLING_HINGES = 10
+SLEEP_PYRAMIDS = 11
 
 NO_CONTINUOUS = 1
 NO_WARM_STARTING = 2
@@ -50,10 +52,15 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2s_set_velocities": (None, [c_int, c_p]),
         "b2s_target": (None, [c_int, c_p]),
         "b2s_counters": (None, [c_int, c_p]),
+        "b2s_run_until_asleep": (c_int, [c_int, c_int, c_p]),
+        "b2s_awake": (c_int, [c_int, c_p]),
         "b2p_contacts": (c_int, [c_u32, c_p, c_int]),
         "b2p_contact_floats": (c_int, [c_u32, c_p, c_int]),
     }
     optional = {
+        "b2s_set_body_velocity": (None, [c_int, c_int, c_f, c_f, c_f]),
+        "b2s_set_awake": (None, [c_int, c_int, c_int]),
+        "b2s_enable_sleep": (None, [c_int, c_int]),
         "b2p_timings": (c_int, [c_u32, c_p, c_p, c_int]),
         "b2p_stream": (c_p, [c_u32]),
         "b2p_status": (c_int, [c_u32]),
@@ -171,6 +178,33 @@ class Scene:
         out = np.zeros(2, np.int32)
         self.lib.b2p_continuous_counts(self.world_id, out.ctypes.data)
         return int(out[0]), int(out[1])
+
+    def run_until_asleep(self, step_limit: int = 500) -> tuple[int, int]:
+        """Step until no body moves (every island asleep); returns (step count, b2Hash of
+        the dynamic bodies' transforms), or (-1, 0) within the limit."""
+        out = np.zeros(1, np.uint32)
+        n = self.lib.b2s_run_until_asleep(self.handle, step_limit, out.ctypes.data)
+        return int(n), int(out[0])
+
+    def apply(self, action: list) -> None:
+        """One scripted change between steps: ["velocity", body, vx, vy, w], ["awake", body,
+        flag] or ["sleeping", flag]."""
+        kind = action[0]
+        if kind == "velocity":
+            self.lib.b2s_set_body_velocity(self.handle, int(action[1]), float(action[2]), float(action[3]),
+                                           float(action[4]))
+        elif kind == "awake":
+            self.lib.b2s_set_awake(self.handle, int(action[1]), int(action[2]))
+        elif kind == "sleeping":
+            self.lib.b2s_enable_sleep(self.handle, int(action[1]))
+        else:
+            raise ValueError(f"unknown scene action {kind!r}")
+
+    def awake(self) -> tuple[int, np.ndarray]:
+        """Awake body count of the world and the awake flag of each scene body."""
+        flags = np.zeros(self.body_count, np.int32)
+        n = self.lib.b2s_awake(self.handle, flags.ctypes.data)
+        return int(n), flags
 
     def counters(self) -> np.ndarray:
         out = np.zeros(30, np.int32)

@@ -171,6 +171,9 @@ typedef struct b2gStepCounters
 	int continuousSweeps; /* fast non-bullet bodies swept against static shapes */
 	int continuousHits;	  /* sweeps that moved the body back to its time of impact */
 	int pad;
+	/* island to split before the next finalize: the largest (sleep time bits << 32 | island
+	   id) over bodies that want to sleep in an island with removed constraints; 0 if none */
+	unsigned long long splitKey;
 } b2gStepCounters;
 
 enum
@@ -216,6 +219,9 @@ typedef struct b2gTapeStep
 
 /* contact sim flag of a contact whose manifold was recycled this step (physics_world.c:508-560) */
 #define B2G_S_RECYCLED 0x800000
+/* the contact is in a sleeping or the disabled solver set: the narrowphase skips it
+   (device bookkeeping only) */
+#define B2G_S_ASLEEP 0x1000000
 
 #ifdef __CUDACC__
 #define B2G_TAPE_FN static inline __host__ __device__
@@ -265,13 +271,34 @@ int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const float* xf, con
 						 const float* sleepThreshold, const float* safetyFactor, const int* awakeIndex, const uint32_t* typeFlags,
 						 const int* shapeStart, const int* shapeCount, const int* shapeList, int shapeListCount );
 int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int* awakeBodyId, const float* stateV, const float* stateD,
-						const float* params, const float* center0 );
+						const float* params, const float* center0, const float* sleepTime );
 int b2gDev_DownloadAwake( b2gDeviceWorld* dw, int awakeCount, float* stateV, float* stateD, float* params, float* center0 );
 int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* center, uint32_t* typeFlags );
 /* body transforms (4 floats), centers (2), flags and awake velocities (4) in one wait;
    the pointers refer to page-locked staging valid until the next call */
 int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awakeCount, const float** xf, const float** center,
-						  const uint32_t** flags, const float** stateV );
+						  const uint32_t** flags, const float** stateV, const float** sleepTime );
+
+/* islands and sleeping. Bodies woken inside a step are appended to the awake set: one
+   record of 10 ints each (body id, awake index, the 8 body parameters as float bits); their
+   velocity starts at zero and their flags are the body's (solver_set.c:35-76). Bodies put
+   to sleep leave it: `slept` body ids, then `pairs` (destination, source) of the awake
+   slots the swap-removals moved (sources at or past the new count). */
+int b2gDev_WakeBodies( b2gDeviceWorld* dw, int newAwakeCount, const int* records, int count );
+int b2gDev_SleepBodies( b2gDeviceWorld* dw, int newAwakeCount, const int* slept, int sleptCount, const int* pairs,
+						int pairCount );
+/* contacts that leave (asleep = 1) or rejoin (0) the set the narrowphase collides */
+int b2gDev_SetContactsAsleep( b2gDeviceWorld* dw, const int* contactIds, int count, int asleep );
+/* the colored contacts' awake body indices from the awake set (after bodies woke) */
+int b2gDev_RefreshContactBodies( b2gDeviceWorld* dw );
+/* the island table of the finalize: per awake index the island's index in the awake set,
+   per awake island (island id, 1 if it has removed constraints); islandCount < 0 turns the
+   island bookkeeping of the finalize off (sleeping disabled) */
+int b2gDev_UploadIslands( b2gDeviceWorld* dw, const int* islandLocal, int awakeCount, const int* islandInfo, int islandCount );
+/* after the solve's wait: the awake-island bits the finalize set and the split key (valid
+   until the next solve) */
+int b2gDev_IslandResults( b2gDeviceWorld* dw, const uint32_t** awakeIslandBits, int* islandCount,
+						  unsigned long long* splitKey );
 int b2gDev_DownloadShapeBoxes( b2gDeviceWorld* dw, int shapeCount, float* aabbs, float* fatAABBs );
 int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float vx, float vy, float w, int which );
 

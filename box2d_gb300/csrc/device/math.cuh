@@ -17,6 +17,7 @@
 #define D_HUGE 100000.0f
 #define D_MAX_ROTATION ( 0.25f * B2_PI )
 #define D_CONTACT_RECYCLE_COS_ANGLE 0.98f
+#define D_TIME_TO_SLEEP 0.5f /* constants.h B2_TIME_TO_SLEEP */
 
 /* ---------------- scalar math, same operation order as math_functions.h ---------------- */
 static __device__ __forceinline__ float d_min( float a, float b ) { return a < b ? a : b; }

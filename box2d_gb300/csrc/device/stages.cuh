@@ -410,6 +410,13 @@ struct d_finalizeArgs
 	int enableSleep, enableContinuous;
 	d_ccdWorld ccd; /* static tree and filters for the continuous sweep */
 	float* toi;		/* when recording: time-of-impact fraction per awake body (1 = none) */
+	/* per awake index the sleep timer; islands (null when sleeping is disabled): per awake
+	   index the island's index in the awake set, per awake island (island id, has removed
+	   constraints); out: one bit per island that stays awake */
+	float* sleepTime;
+	const int* islandLocal;
+	const int2* islandInfo;
+	unsigned int* awakeIslandBits;
 };
 
 /* solver.c:384-550 b2SolveContinuous for a fast non-bullet body: sweep every non-sensor
@@ -542,7 +549,30 @@ static __device__ void d_finalizeBody( const d_finalizeArgs& a, int simIndex )
 	a.sv[simIndex] = make_float4( v.x, v.y, w, __uint_as_float( stateFlags ) );
 	bool isBullet = ( bodyFlags & B2G_IS_BULLET ) != 0;
 	bool sweep = false;
-	if ( a.enableSleep == 0 || ( bodyFlags & B2G_ENABLE_SLEEP ) == 0 || sleepVelocity > a.sleepThreshold[bodyId] )
+	bool sleepy = !( a.enableSleep == 0 || ( bodyFlags & B2G_ENABLE_SLEEP ) == 0 || sleepVelocity > a.sleepThreshold[bodyId] );
+	/* solver.c:637-695: the body's sleep timer, then its island stays awake or, when the
+	   island must be split before it can sleep, becomes the split candidate (largest sleep
+	   time, then largest island id) */
+	float sleepTime = sleepy ? a.sleepTime[simIndex] + a.dt : 0.0f;
+	a.sleepTime[simIndex] = sleepTime;
+	if ( a.islandLocal != nullptr )
+	{
+		int islandIndex = a.islandLocal[simIndex];
+		if ( sleepTime < D_TIME_TO_SLEEP )
+		{
+			atomicOr( a.awakeIslandBits + ( islandIndex >> 5 ), 1u << ( islandIndex & 31 ) );
+		}
+		else
+		{
+			int2 info = a.islandInfo[islandIndex];
+			if ( info.y != 0 )
+			{
+				unsigned long long key = ( (unsigned long long)__float_as_uint( sleepTime ) << 32 ) | (unsigned int)info.x;
+				atomicMax( &a.counters->splitKey, key );
+			}
+		}
+	}
+	if ( sleepy == false )
 	{
 		float maxMotion = d_max( maxDeltaPosition, maxVelocity * a.dt );
 		if ( a.bodyType[bodyId] == b2_dynamicBody && a.enableContinuous && maxMotion > a.safetyFactor[bodyId] * a.minExtent[bodyId] )

@@ -64,6 +64,7 @@ enum
 	DK_FINALIZE,
 	DK_CAPTURE,
 	DK_SOLVE_BIN,
+	DK_ISLAND_OP,
 	DK_COUNT
 };
 
@@ -126,6 +127,18 @@ struct b2gDeviceWorld
 	float* params; /* 8 per body: force.x, force.y, torque, linDamp, angDamp, gravityScale, invMass, invI */
 	float4* center0; /* center0.x, center0.y, rotation0.c, rotation0.s */
 	int* enlargedBody;
+	float* sleepTime; /* seconds each awake body has been still (body.h b2Body.sleepTime) */
+	/* islands of the finalize (sleeping enabled) */
+	int islandsOn, islandCount;
+	int* islandLocal;
+	int islandLocalCap;
+	int2* islandInfo;
+	int islandInfoCap;
+	unsigned int* islandBits;
+	int islandBitsCap;
+	unsigned int* hIslandBits;
+	int hIslandBitsCap;
+	int pendingIslandWords; /* island bits the solve awaiting its results reads back */
 	/* shapes */
 	int shapeCap, shapeCountTotal;
 	b2gShape* shapes;
@@ -218,6 +231,8 @@ struct b2gDeviceWorld
 	uint32_t* hFlags;
 	float4* hStateV;
 	int hXfCap, hCenterCap, hFlagsCap, hStateVCap;
+	float* hSleepTime;
+	int hSleepTimeCap;
 };
 
 #define CK( x )                                                                                                                \
@@ -580,6 +595,97 @@ static __device__ void b_killContacts( const d_contactListArgs& a, int block, in
 	a.contacts[( (const int*)a.list )[i]].simFlags = 0;
 }
 
+/* ======================= islands and sleeping ======================= */
+enum
+{
+	D_ISLAND_WAKE = 0,	   /* append woken bodies to the awake set */
+	D_ISLAND_SLEEP = 1,	   /* bodies that left the awake set */
+	D_ISLAND_GATHER = 2,   /* awake slots moved by the swap-removals */
+	D_ISLAND_CONTACTS = 3, /* contacts leaving or rejoining the narrowphase */
+	D_ISLAND_REFRESH = 4,  /* colored contacts' awake body indices */
+};
+
+struct d_islandOpArgs
+{
+	int mode, n, value;
+	const int* list;
+	int* awakeBodyId;
+	int* awakeIndex;
+	float4* sv;
+	float4* sd;
+	float* params;
+	float4* center0;
+	float* sleepTime;
+	const uint32_t* bodyFlags;
+	const float2* center;
+	const float4* xf;
+	b2gContact* contacts;
+	const int* colorIds;
+	const b2gShape* shapes;
+};
+
+/* solver_set.c:35-76 (a woken body gets the identity state with the body's flags, its sim
+   as it fell asleep: center0 = center, rotation0 = q) and :200-250 (b2RemoveBodySim's
+   swap-removal); the moved slots' sources all lie at or past the new count, so the gather
+   reads nothing it writes */
+static __device__ void b_islandOp( const d_islandOpArgs& a, int block, int grid )
+{
+	int i = block * blockDim.x + threadIdx.x;
+	if ( i >= a.n ) return;
+	switch ( a.mode )
+	{
+		case D_ISLAND_WAKE:
+		{
+			const int* r = a.list + 10 * i;
+			int bodyId = r[0], idx = r[1];
+			a.awakeBodyId[idx] = bodyId;
+			a.awakeIndex[bodyId] = idx;
+			a.sv[idx] = make_float4( 0.0f, 0.0f, 0.0f, __uint_as_float( a.bodyFlags[bodyId] ) );
+			a.sd[idx] = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+			for ( int k = 0; k < 8; ++k ) a.params[8 * idx + k] = __int_as_float( r[2 + k] );
+			float2 c = a.center[bodyId];
+			float4 x = a.xf[bodyId];
+			a.center0[idx] = make_float4( c.x, c.y, x.z, x.w );
+			a.sleepTime[idx] = 0.0f;
+			break;
+		}
+		case D_ISLAND_SLEEP:
+			a.awakeIndex[a.list[i]] = -1;
+			break;
+		case D_ISLAND_GATHER:
+		{
+			int dst = a.list[2 * i], src = a.list[2 * i + 1];
+			int bodyId = a.awakeBodyId[src];
+			a.awakeBodyId[dst] = bodyId;
+			a.awakeIndex[bodyId] = dst;
+			a.sv[dst] = a.sv[src];
+			a.sd[dst] = a.sd[src];
+			for ( int k = 0; k < 8; ++k ) a.params[8 * dst + k] = a.params[8 * src + k];
+			a.center0[dst] = a.center0[src];
+			a.sleepTime[dst] = a.sleepTime[src];
+			break;
+		}
+		case D_ISLAND_CONTACTS:
+		{
+			b2gContact* c = a.contacts + a.list[i];
+			if ( a.value ) c->simFlags |= B2G_S_ASLEEP;
+			else c->simFlags &= ~(uint32_t)B2G_S_ASLEEP;
+			break;
+		}
+		case D_ISLAND_REFRESH:
+		{
+			/* constraint_graph.c:143-178: a contact entering the graph takes its bodies'
+			   current awake indices */
+			b2gContact* c = a.contacts + a.colorIds[i];
+			c->bodySimIndexA = a.awakeIndex[a.shapes[c->shapeIdA].bodyId];
+			c->bodySimIndexB = a.awakeIndex[a.shapes[c->shapeIdB].bodyId];
+			break;
+		}
+		default:
+			break;
+	}
+}
+
 struct d_collideArgs
 {
 	b2gContact* contacts;
@@ -607,7 +713,7 @@ static __device__ void b_collide( const d_collideArgs& a, int block, int grid )
 	if ( contactId >= a.capacity ) return;
 	b2gContact* cs = a.contacts + contactId;
 	uint32_t simFlags = cs->simFlags;
-	if ( ( simFlags & B2G_S_LIVE ) == 0 ) return;
+	if ( ( simFlags & B2G_S_LIVE ) == 0 || ( simFlags & B2G_S_ASLEEP ) != 0 ) return;
 	simFlags &= ~(uint32_t)B2G_S_RECYCLED;
 	float recycleDistance = a.recycleDistance;
 	float recycleNonTouching = d_min( recycleDistance, D_SPECULATIVE_DISTANCE );
@@ -882,7 +988,8 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->shapeEnlarged, dw->contacts, dw->colorIds,	dw->lanes,		dw->joints,		  dw->tree[0],
 					  dw->tree[1],	  dw->tree[2], dw->treeRaw[0], dw->treeRaw[1], dw->treeRaw[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  
 					  dw->moveStage, dw->pairPacked, dw->pairOffsets, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
-					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList };
+					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList,
+					  dw->sleepTime, dw->islandLocal, dw->islandInfo, dw->islandBits };
 	b2gDev_CompFree( &dw->comp );
 	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
 		if ( dptrs[i] ) cudaFree( dptrs[i] );
@@ -890,7 +997,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	if ( dw->upHost ) cudaFreeHost( dw->upHost );
 	void* hptrs[] = { dw->hCounters, dw->hChanges,	   dw->hRecs,	   dw->hBoxes,	   dw->hPairs,	  dw->hPairCounts,
 					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw, dw->hSortKeys,
-					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV };
+					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV, dw->hSleepTime, dw->hIslandBits };
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
 		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
 	free( dw->hSortTmp );
@@ -992,7 +1099,7 @@ extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const flo
 }
 
 extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int* awakeBodyId, const float* stateV,
-									const float* stateD, const float* params, const float* center0 )
+									const float* stateD, const float* params, const float* center0, const float* sleepTime )
 {
 	dw->topologyDirty = 1;
 	int cap0 = dw->awakeCap, capOut = 0;
@@ -1005,6 +1112,8 @@ extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int
 	CK2( upload( dw, &dw->center0, &cap0, (const float4*)center0, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
 	CK2( grow( dw, (void**)&dw->enlargedBody, &cap0, awakeCount, sizeof( int ) ) );
+	cap0 = dw->awakeCap;
+	CK2( upload( dw, &dw->sleepTime, &cap0, sleepTime, awakeCount, &capOut ) );
 	int pcap = dw->awakeCap * 8;
 	CK2( grow( dw, (void**)&dw->params, &pcap, 8 * awakeCount, sizeof( float ) ) );
 	if ( awakeCount > 0 ) CK( ( dw->h2dBytes += (long long)( (size_t)awakeCount * 8 * sizeof( float ) ), cudaMemcpy( dw->params, params, (size_t)awakeCount * 8 * sizeof( float ), cudaMemcpyHostToDevice ) ) );
@@ -1030,9 +1139,10 @@ static int drain( b2gDeviceWorld* dw );
 /* transforms, centers and flags of every body and velocities of the awake bodies, in one
    wait, into page-locked staging that stays valid until the next call */
 extern "C" int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awakeCount, const float** xf, const float** center,
-									 const uint32_t** flags, const float** stateV )
+									 const uint32_t** flags, const float** stateV, const float** sleepTime )
 {
 	int nb = bodyCount > 0 ? bodyCount : 1, na = awakeCount > 0 ? awakeCount : 1;
+	CK2( growHost( (void**)&dw->hSleepTime, &dw->hSleepTimeCap, na, sizeof( float ) ) );
 	CK2( growHost( (void**)&dw->hXf, &dw->hXfCap, nb, sizeof( float4 ) ) );
 	CK2( growHost( (void**)&dw->hCenter, &dw->hCenterCap, nb, sizeof( float2 ) ) );
 	CK2( growHost( (void**)&dw->hFlags, &dw->hFlagsCap, nb, sizeof( uint32_t ) ) );
@@ -1044,13 +1154,17 @@ extern "C" int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awak
 		CK( cudaMemcpyAsync( dw->hFlags, dw->bodyFlags, (size_t)bodyCount * sizeof( uint32_t ), cudaMemcpyDeviceToHost, dw->stream ) );
 	}
 	if ( awakeCount > 0 )
+	{
 		CK( cudaMemcpyAsync( dw->hStateV, dw->stateV, (size_t)awakeCount * sizeof( float4 ), cudaMemcpyDeviceToHost, dw->stream ) );
-	dw->d2hBytes += (long long)bodyCount * 28 + (long long)awakeCount * 16;
+		CK( cudaMemcpyAsync( dw->hSleepTime, dw->sleepTime, (size_t)awakeCount * sizeof( float ), cudaMemcpyDeviceToHost, dw->stream ) );
+	}
+	dw->d2hBytes += (long long)bodyCount * 28 + (long long)awakeCount * 20;
 	CK2( drain( dw ) );
 	*xf = (const float*)dw->hXf;
 	*center = (const float*)dw->hCenter;
 	*flags = dw->hFlags;
 	*stateV = (const float*)dw->hStateV;
+	*sleepTime = dw->hSleepTime;
 	return 0;
 }
 
@@ -1193,6 +1307,132 @@ extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int coun
 	CK2( uploadStaged( dw, ids, (size_t)count * sizeof( int ), &d ) );
 	d_contactListArgs a = { dw->contacts, d, count };
 	return dev_launch<d_contactListArgs, b_killContacts>( dw, DK_KILL_CONTACTS, blocks( count ), a );
+}
+
+static d_islandOpArgs islandArgs( b2gDeviceWorld* dw, int mode, int n, const void* list )
+{
+	d_islandOpArgs a;
+	memset( &a, 0, sizeof( a ) );
+	a.mode = mode;
+	a.n = n;
+	a.list = (const int*)list;
+	a.awakeBodyId = dw->awakeBodyId;
+	a.awakeIndex = dw->awakeIndex;
+	a.sv = dw->stateV;
+	a.sd = dw->stateD;
+	a.params = dw->params;
+	a.center0 = dw->center0;
+	a.sleepTime = dw->sleepTime;
+	a.bodyFlags = dw->bodyFlags;
+	a.center = dw->center;
+	a.xf = dw->xf;
+	a.contacts = dw->contacts;
+	a.colorIds = dw->colorIds;
+	a.shapes = dw->shapes;
+	return a;
+}
+
+/* the awake arrays hold `count` bodies (contents kept) */
+static int growAwake( b2gDeviceWorld* dw, int count )
+{
+	if ( count <= dw->awakeCap && dw->awakeBodyId != NULL ) return 0;
+	int capOut = 0, cap = dw->awakeCap;
+	CK2( grow( dw, (void**)&dw->awakeBodyId, &cap, count, sizeof( int ) ) );
+	capOut = cap;
+	cap = dw->awakeCap;
+	CK2( grow( dw, (void**)&dw->stateV, &cap, count, sizeof( float4 ) ) );
+	cap = dw->awakeCap;
+	CK2( grow( dw, (void**)&dw->stateD, &cap, count, sizeof( float4 ) ) );
+	cap = dw->awakeCap;
+	CK2( grow( dw, (void**)&dw->center0, &cap, count, sizeof( float4 ) ) );
+	cap = dw->awakeCap;
+	CK2( grow( dw, (void**)&dw->enlargedBody, &cap, count, sizeof( int ) ) );
+	cap = dw->awakeCap;
+	CK2( grow( dw, (void**)&dw->sleepTime, &cap, count, sizeof( float ) ) );
+	int pcap = dw->awakeCap * 8;
+	CK2( grow( dw, (void**)&dw->params, &pcap, 8 * count, sizeof( float ) ) );
+	dw->awakeCap = capOut;
+	return 0;
+}
+
+extern "C" int b2gDev_WakeBodies( b2gDeviceWorld* dw, int newAwakeCount, const int* records, int count )
+{
+	if ( count <= 0 ) return 0;
+	CK2( growAwake( dw, newAwakeCount ) );
+	void* d = NULL;
+	CK2( uploadStaged( dw, records, (size_t)count * 10 * sizeof( int ), &d ) );
+	d_islandOpArgs a = islandArgs( dw, D_ISLAND_WAKE, count, d );
+	CK2( ( dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( count ), a ) ) );
+	dw->awakeCount = newAwakeCount;
+	dw->topologyDirty = 1;
+	return 0;
+}
+
+extern "C" int b2gDev_SleepBodies( b2gDeviceWorld* dw, int newAwakeCount, const int* slept, int sleptCount, const int* pairs,
+								   int pairCount )
+{
+	if ( sleptCount > 0 )
+	{
+		void* d = NULL;
+		CK2( uploadStaged( dw, slept, (size_t)sleptCount * sizeof( int ), &d ) );
+		d_islandOpArgs a = islandArgs( dw, D_ISLAND_SLEEP, sleptCount, d );
+		CK2( ( dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( sleptCount ), a ) ) );
+	}
+	if ( pairCount > 0 )
+	{
+		void* d = NULL;
+		CK2( uploadStaged( dw, pairs, (size_t)pairCount * 2 * sizeof( int ), &d ) );
+		d_islandOpArgs a = islandArgs( dw, D_ISLAND_GATHER, pairCount, d );
+		CK2( ( dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( pairCount ), a ) ) );
+	}
+	dw->awakeCount = newAwakeCount;
+	dw->topologyDirty = 1;
+	return 0;
+}
+
+extern "C" int b2gDev_SetContactsAsleep( b2gDeviceWorld* dw, const int* contactIds, int count, int asleep )
+{
+	if ( count <= 0 ) return 0;
+	void* d = NULL;
+	CK2( uploadStaged( dw, contactIds, (size_t)count * sizeof( int ), &d ) );
+	d_islandOpArgs a = islandArgs( dw, D_ISLAND_CONTACTS, count, d );
+	a.value = asleep ? 1 : 0;
+	return dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( count ), a );
+}
+
+extern "C" int b2gDev_RefreshContactBodies( b2gDeviceWorld* dw )
+{
+	int total = dw->colorOffsets[B2_GRAPH_COLOR_COUNT];
+	if ( total <= 0 ) return 0;
+	d_islandOpArgs a = islandArgs( dw, D_ISLAND_REFRESH, total, NULL );
+	return dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( total ), a );
+}
+
+extern "C" int b2gDev_UploadIslands( b2gDeviceWorld* dw, const int* islandLocal, int awakeCount, const int* islandInfo,
+									 int islandCount )
+{
+	if ( islandCount < 0 )
+	{
+		dw->islandsOn = 0;
+		dw->islandCount = 0;
+		return 0;
+	}
+	CK2( grow( dw, (void**)&dw->islandLocal, &dw->islandLocalCap, awakeCount > 0 ? awakeCount : 1, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->islandInfo, &dw->islandInfoCap, islandCount > 0 ? islandCount : 1, sizeof( int2 ) ) );
+	if ( awakeCount > 0 ) CK2( uploadTo( dw, dw->islandLocal, islandLocal, (size_t)awakeCount * sizeof( int ) ) );
+	if ( islandCount > 0 ) CK2( uploadTo( dw, dw->islandInfo, islandInfo, (size_t)islandCount * sizeof( int2 ) ) );
+	dw->islandsOn = 1;
+	dw->islandCount = islandCount;
+	return 0;
+}
+
+extern "C" int b2gDev_IslandResults( b2gDeviceWorld* dw, const uint32_t** awakeIslandBits, int* islandCount,
+									  unsigned long long* splitKey )
+{
+	*awakeIslandBits = dw->pendingIslandWords > 0 ? dw->hIslandBits : NULL;
+	*islandCount = dw->pendingIslandWords > 0 ? dw->islandCount : 0;
+	*splitKey = dw->hCounters->splitKey;
+	return 0;
 }
 
 extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const int* offsets, int total )
@@ -1827,6 +2067,20 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	f.ccd.partnerList = dw->partnerCount > 0 ? dw->partnerList : NULL;
 	f.toi = dw->tapeToi;
 	dw->tapeToi = NULL;
+	f.sleepTime = dw->sleepTime;
+	f.islandLocal = NULL;
+	f.islandInfo = NULL;
+	f.awakeIslandBits = NULL;
+	int islandWords = 0;
+	if ( dw->islandsOn && dw->islandCount > 0 )
+	{
+		islandWords = ( dw->islandCount + 31 ) / 32;
+		CK2( grow( dw, (void**)&dw->islandBits, &dw->islandBitsCap, islandWords, sizeof( unsigned int ) ) );
+		CK2( dev_memset( dw, dw->islandBits, 0, (size_t)islandWords * sizeof( unsigned int ) ) );
+		f.islandLocal = dw->islandLocal;
+		f.islandInfo = dw->islandInfo;
+		f.awakeIslandBits = dw->islandBits;
+	}
 	int ovJointBegin0 = dw->jointOffsets[B2G_OVERFLOW_INDEX];
 	int ovJointCount0 = dw->jointOffsets[B2_GRAPH_COLOR_COUNT] - ovJointBegin0;
 	int ovCount0 = total - overflowBegin;
@@ -2038,6 +2292,12 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 		CK2( dev_d2h( dw, dw->hRecsRaw, dw->enlargedRecs, (size_t)recWindow * 4 * sizeof( int ) ) );
 		CK2( dev_d2h( dw, dw->hBoxesRaw, dw->enlargedBoxes, (size_t)recWindow * sizeof( float4 ) ) );
 	}
+	if ( islandWords > 0 )
+	{
+		CK2( growHost( (void**)&dw->hIslandBits, &dw->hIslandBitsCap, islandWords, sizeof( unsigned int ) ) );
+		CK2( dev_d2h( dw, dw->hIslandBits, dw->islandBits, (size_t)islandWords * sizeof( unsigned int ) ) );
+	}
+	dw->pendingIslandWords = islandWords;
 	dw->pendingRecWindow = recWindow;
 	dw->pendingShapeTotal = shapeTotal;
 	dw->pendingSolved = solved ? 1 : 0;
@@ -2520,6 +2780,7 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 		CK2( ( d_launchBatched<d_collideArgs, b_collide, 1>( b, L, DK_COLLIDE ) ) );
 		CK2( ( d_launchBatched<d_finalizeArgs, b_finalize, 8>( b, L, DK_FINALIZE ) ) );
 		CK2( ( d_launchBatched<d_captureArgs, b_capture, 1>( b, L, DK_CAPTURE ) ) );
+		CK2( ( d_launchBatched<d_islandOpArgs, b_islandOp, 1>( b, L, DK_ISLAND_OP ) ) );
 		if ( L.recCount[DK_SOLVE_BIN] > 0 )
 		{
 			CK2( b2gDev_SolveWorldBinBatch( (const long long*)( b->dBlob + L.recs[DK_SOLVE_BIN] ), b->dBlob, (int)L.recCount[DK_SOLVE_BIN],

@@ -19,7 +19,11 @@ enum
 	H_STATIC_SET = 0,
 	H_DISABLED_SET = 1,
 	H_AWAKE_SET = 2,
+	H_FIRST_SLEEPING_SET = 3,
 };
+
+/* constants.h B2_TIME_TO_SLEEP: seconds a body must be still before its island can sleep */
+#define H_TIME_TO_SLEEP 0.5f
 
 typedef struct h_body
 {
@@ -28,6 +32,8 @@ typedef struct h_body
 	int headContactKey, contactCount;
 	int headShapeId, shapeCount;
 	int headJointKey, jointCount;
+	int islandId, islandIndex; /* island of a non-static body and its index in the island */
+	int bodyMoveIndex;		   /* its move event in the last step while the sleep pass runs */
 	float mass, inertia;
 	float sleepThreshold, sleepTime, safetyFactor;
 	int id;
@@ -75,6 +81,7 @@ typedef struct h_contact
 {
 	h_contactEdge edges[2];
 	int setIndex, colorIndex, localIndex;
+	int islandId, islandIndex;
 	int shapeIdA, shapeIdB, contactId;
 	uint32_t flags, generation;
 } h_contact;
@@ -89,11 +96,37 @@ typedef struct h_joint
 	void* userData;
 	int setIndex, colorIndex, localIndex;
 	h_jointEdge edges[2];
+	int islandId, islandIndex;
 	int jointId;
 	b2JointType type;
 	uint16_t generation;
 	int collideConnected;
 } h_joint;
+
+/* a contact or joint of an island with its two bodies (island.h b2ContactLink, b2JointLink) */
+typedef struct h_link
+{
+	int id, bodyIdA, bodyIdB;
+} h_link;
+typedef H_ARRAY( h_link ) h_linkArray;
+
+/* a persistent island (island.h b2Island): touching contacts and joints connect its bodies */
+typedef struct h_island
+{
+	int setIndex, localIndex, islandId;
+	int constraintRemoveCount;
+	h_intArray bodies;
+	h_linkArray contacts;
+	h_linkArray joints;
+} h_island;
+
+/* a sleeping solver set (solver_set.h b2SolverSet, set index >= H_FIRST_SLEEPING_SET): the
+   ids of its bodies, touching contacts, joints and islands, in the reference's array orders */
+typedef struct h_sleepSet
+{
+	int setIndex; /* B2_NULL_INDEX when the slot is free */
+	h_intArray bodyIds, contactIds, jointIds, islandIds;
+} h_sleepSet;
 
 typedef struct h_color
 {
@@ -115,6 +148,21 @@ typedef struct h_world
 	h_intArray awakeBodyIds;		  /* awake index -> body id */
 	int staticCount;
 	h_intArray awakeContactIds;		  /* non-touching contacts, reference array order */
+	h_intArray disabledContactIds;	  /* non-touching contacts between sleeping bodies */
+	/* islands and sleeping (island.c) */
+	H_ARRAY( h_island ) islands;
+	h_idPool islandIdPool;
+	h_intArray awakeIslandIds; /* the awake set's islands, reference array order */
+	H_ARRAY( h_sleepSet ) sets; /* by solver set id; slots below H_FIRST_SLEEPING_SET unused */
+	h_idPool setIdPool;
+	int splitIslandId;
+	int islandsDirty;	  /* the finalize's island table must be sent again */
+	int setChangeCount;	  /* islands put to sleep or woken since the world was created */
+	int* sleepPerm;		  /* while the sleep pass runs: original awake index per awake slot */
+	h_intArray pendingWake;	   /* device records (10 ints) of bodies woken inside the step */
+	h_intArray pendingContacts; /* contacts whose solver set changed: collided or not */
+	h_intArray sleptBodies;	   /* bodies put to sleep by the sleep pass in progress */
+	int wokeInStep;			   /* a set woke inside the step: refresh the colored contacts */
 	h_color colors[B2_GRAPH_COLOR_COUNT];
 	h_tree trees[3];
 	h_bitSet movedProxies[3];
@@ -167,6 +215,29 @@ int h_stepCollide( h_world* w, int oneBlockOnly );
 int h_stepSolveIssue( h_world* w );
 void h_stepFinish( h_world* w );
 void h_tapeDetach( h_world* w );
+
+/* islands and solver sets (island.c: island.c, solver_set.c and the sleep pass of
+   solver.c:2024-2080 in the reference) */
+void h_islandsInit( h_world* w );
+void h_islandsFree( h_world* w );
+void h_createIslandForBody( h_world* w, int setIndex, h_body* body );
+void h_linkContact( h_world* w, h_contact* contact );
+void h_unlinkContact( h_world* w, h_contact* contact );
+void h_linkJoint( h_world* w, h_joint* joint );
+void h_splitIsland( h_world* w, int baseId );
+void h_wakeSolverSet( h_world* w, int setIndex );
+void h_trySleepIsland( h_world* w, int islandId );
+void h_mergeSolverSets( h_world* w, int setId1, int setId2 );
+int h_wakeBody( h_world* w, h_body* body );
+int h_allocSleepingSet( h_world* w );
+void h_removeJointFromGraph( h_world* w, int bodyIdA, int bodyIdB, int colorIndex, int localIndex );
+void h_addJointToGraph( h_world* w, h_joint* joint );
+/* per step: the split before the finalize, the finalize's island table, and the sleep pass
+   over the finalize's awake-island bits and split candidate */
+void h_stepIslands( h_world* w );
+void h_sleepPass( h_world* w, const uint32_t* awakeIslandBits, uint64_t splitKey );
+/* device work of sets that slept or woke: sent inside a step, or before the next one */
+void h_flushSleepOps( h_world* w );
 h_world* h_worldByIndex( int index );
 
 /* geometry helpers (geometry.c) */
@@ -178,6 +249,10 @@ void h_computeShapeExtent( const h_shape* shape, b2Vec2 localCenter, float* minE
 
 /* world.c internals used by step.c and joint.c */
 void h_syncFromDevice( h_world* w );
+/* the host records become authoritative: the device is refilled before the next step */
+void h_markHostChanged( h_world* w );
+/* the last step's move events, one per body awake at its finalize (solver.c:608-622) */
+void h_buildMoveEvents( h_world* w );
 void h_syncJointsFromDevice( h_world* w );
 void h_ensureDevice( h_world* w );
 void h_createContact( h_world* w, h_shape* a, h_shape* b );

@@ -18,6 +18,7 @@ typedef struct h_tapeWorld
 	int stepCount, offsetCapacity;
 	int maxAwake, maxSlots, maxSubsteps;
 	int bodyCount, shapeCount;
+	int setChanges; /* the world's set-change count at the first recorded step */
 } h_tapeWorld;
 
 struct b2DiffTape
@@ -115,6 +116,7 @@ void h_tapeCapture( h_world* w, const b2gStepParams* params )
 	int slots = 0;
 	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i ) slots += w->colors[i].contactIds.count;
 	long long offset = 0;
+	if ( tw->stepCount == 0 ) tw->setChanges = w->setChangeCount;
 	int rc = b2gDev_CaptureTape( w->dev, params, w->bodies.count, awake, w->joints.count, &tw->arena, &tw->capacity, &tw->used,
 								 &offset );
 	if ( rc != 0 ) h_fail( w, "tape capture", rc );
@@ -142,6 +144,7 @@ int b2Diff_Backward( b2DiffTape* t, const float* adjCenter, const float* adjRota
 	if ( t == NULL || adjCenter == NULL || gradVelocity == NULL ) return B2_DIFF_BAD_ARGUMENT;
 	int steps = b2Diff_StepCount( t );
 	if ( steps == 0 ) return B2_DIFF_EMPTY;
+	memset( t->lastFailure, 0, sizeof( t->lastFailure ) );
 	int n = t->worldCount;
 	b2gAdjointWorld* aw = calloc( (size_t)n, sizeof( b2gAdjointWorld ) );
 	int* bodyOffsets = malloc( (size_t)( n + 1 ) * sizeof( int ) );
@@ -155,6 +158,16 @@ int b2Diff_Backward( b2DiffTape* t, const float* adjCenter, const float* adjRota
 		if ( tw->world == NULL || tw->stepCount != steps )
 		{
 			rc = B2_DIFF_BAD_ARGUMENT;
+			break;
+		}
+		if ( tw->world->setChangeCount != tw->setChanges )
+		{
+			/* an island fell asleep or woke while recording: the awake set of the recorded
+			   steps no longer describes one trajectory */
+			rc = B2_DIFF_UNSUPPORTED;
+			t->lastFailure[0] = rc;
+			t->lastFailure[1] = i;
+			t->lastFailure[3] = 6;
 			break;
 		}
 		int shapeCount = 0;

@@ -116,7 +116,8 @@ static void h_destroyContactsBetweenBodies( h_world* w, h_body* bodyA, h_body* b
 	}
 }
 
-/* joint.c:204-398 (awake and static placements; no sleeping sets) */
+/* joint.c:204-398: the joint goes to the static set, the graph colors (waking a sleeping
+   body), or the sleeping set of its bodies, then links their islands */
 static b2gJoint* h_createJoint( h_world* w, const b2JointDef* def, b2JointType type, b2JointId* outId )
 {
 	h_syncFromDevice( w );
@@ -160,17 +161,30 @@ static b2gJoint* h_createJoint( h_world* w, const b2JointDef* def, b2JointType t
 		w->joints.data[bodyB->headJointKey >> 1].edges[bodyB->headJointKey & 1].prevKey = keyB;
 	bodyB->headJointKey = keyB;
 	bodyB->jointCount += 1;
+	j->islandId = B2_NULL_INDEX;
+	j->islandIndex = B2_NULL_INDEX;
+	int maxSetIndex = bodyA->setIndex > bodyB->setIndex ? bodyA->setIndex : bodyB->setIndex;
 	if ( bodyA->type != b2_dynamicBody && bodyB->type != b2_dynamicBody )
 	{
 		j->setIndex = H_STATIC_SET;
 	}
+	else if ( bodyA->setIndex == H_AWAKE_SET || bodyB->setIndex == H_AWAKE_SET )
+	{
+		/* a sleeping body of the pair wakes */
+		if ( maxSetIndex >= H_FIRST_SLEEPING_SET ) h_wakeSolverSet( w, maxSetIndex );
+		j->setIndex = H_AWAKE_SET;
+		h_addJointToGraph( w, j );
+	}
 	else
 	{
-		j->setIndex = H_AWAKE_SET;
-		int colorIndex = h_assignJointColor( w, bodyIdA, bodyIdB, bodyA->type, bodyB->type );
-		h_push( w->colors[colorIndex].jointIds, jointId );
-		j->colorIndex = colorIndex;
-		j->localIndex = w->colors[colorIndex].jointIds.count - 1;
+		/* between sleeping (and static) bodies: the joint sleeps with them; two sleeping
+		   sets merge */
+		j->setIndex = maxSetIndex;
+		j->localIndex = w->sets.data[maxSetIndex].jointIds.count;
+		h_push( w->sets.data[maxSetIndex].jointIds, jointId );
+		if ( bodyA->setIndex != bodyB->setIndex && bodyA->setIndex >= H_FIRST_SLEEPING_SET &&
+			 bodyB->setIndex >= H_FIRST_SLEEPING_SET )
+			h_mergeSolverSets( w, bodyA->setIndex, bodyB->setIndex );
 	}
 	b2gJoint* r = w->jointRecords.data + jointId;
 	memset( r, 0, sizeof( *r ) );
@@ -186,6 +200,7 @@ static b2gJoint* h_createJoint( h_world* w, const b2JointDef* def, b2JointType t
 	r->softImpulse = 0.0f;
 	r->jointId = jointId;
 	w->jointsDirty = 1;
+	if ( j->setIndex > H_DISABLED_SET ) h_linkJoint( w, j );
 	outId->index1 = jointId + 1;
 	outId->world0 = w->worldId;
 	outId->generation = j->generation;

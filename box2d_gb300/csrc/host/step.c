@@ -354,7 +354,10 @@ static void h_contactStatePass( h_world* w, const int* changes, int count )
 				b2ContactBeginTouchEvent ev = { shapeIdA, shapeIdB, fullId };
 				h_push( w->beginEvents, ev );
 			}
+			/* link first: this wakes a sleeping partner (island.c:172-230), which appends to
+			   the awake arrays and leaves this contact's slot in place */
 			contact->flags |= B2G_C_TOUCHING;
+			h_linkContact( w, contact );
 			h_addContactToGraph( w, contact );
 			int moved = h_removeSwap( w->awakeContactIds, localIndex );
 			if ( moved != B2_NULL_INDEX ) w->contacts.data[w->awakeContactIds.data[localIndex]].localIndex = localIndex;
@@ -367,6 +370,7 @@ static void h_contactStatePass( h_world* w, const int* changes, int count )
 				b2ContactEndTouchEvent ev = { shapeIdA, shapeIdB, fullId };
 				h_push( w->endEvents[endEventArrayIndex], ev );
 			}
+			h_unlinkContact( w, contact );
 			int bodyIdA = contact->edges[0].bodyId, bodyIdB = contact->edges[1].bodyId;
 			contact->colorIndex = B2_NULL_INDEX;
 			contact->localIndex = w->awakeContactIds.count;
@@ -417,6 +421,9 @@ int h_stepBegin( h_world* w, float timeStep, int subStepCount )
 	w->stepTimeStep = timeStep;
 
 	h_ensureDevice( w );
+	/* contacts whose solver set the API changed since the last step */
+	w->wokeInStep = 0;
+	h_flushSleepOps( w );
 
 	b2gStepParams* p = &w->stepParams;
 	memset( p, 0, sizeof( *p ) );
@@ -484,6 +491,8 @@ int h_stepCollide( h_world* w, int oneBlockOnly )
 	h_contactStatePass( w, changes, changeCount );
 	h_lap( w, H_PHASE_STATE_PASS, &lap );
 	h_flushContacts( w );
+	/* sets woken by contacts that started touching join the device awake set */
+	h_flushSleepOps( w );
 	h_lap( w, H_PHASE_UPLOADS, &lap );
 	w->profile.collide = h_ms( w->stepT0 );
 	w->stepSolveIssued = 0;
@@ -494,11 +503,19 @@ int h_stepCollide( h_world* w, int oneBlockOnly )
 	w->stepIndex += 1;
 	h_uploadColors( w );
 	h_uploadJoints( w );
+	if ( w->wokeInStep )
+	{
+		/* contacts that re-entered the colors take their bodies' new awake indices */
+		int rc = b2gDev_RefreshContactBodies( w->dev );
+		if ( rc != 0 ) h_fail( w, "contact refresh", rc );
+		w->wokeInStep = 0;
+	}
 	h_lap( w, H_PHASE_UPLOADS, &lap );
 	/* fast bodies sweep against the static tree in the finalize stage */
 	if ( w->enableContinuous ) h_uploadTree( w, b2_staticBody );
 	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
 	if ( w->awakeBodyIds.count == 0 ) return 0;
+	h_stepIslands( w );
 	if ( oneBlockOnly && b2gDev_SolveFitsOneBlock( w->dev, w->awakeBodyIds.count ) == 0 )
 	{
 		w->stepSolveLate = 1;
@@ -547,6 +564,14 @@ void h_stepFinish( h_world* w )
 		if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
 		h_enlargeProxies( w, recs, boxes, enlargedCount );
 		h_lap( w, H_PHASE_ENLARGE, &lap );
+		{
+			/* island sleeping comes last (solver.c:2024-2080) */
+			const uint32_t* bits = NULL;
+			int islandCount = 0;
+			unsigned long long splitKey = 0;
+			b2gDev_IslandResults( w->dev, &bits, &islandCount, &splitKey );
+			h_sleepPass( w, bits, splitKey );
+		}
 	}
 	if ( w->stepTimeStep > 0.0f ) w->profile.solve = h_ms( w->stepT0 );
 	h_joinRebuild( w );

@@ -193,6 +193,7 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 	memset( w, 0, sizeof( *w ) );
 	w->worldId = (uint16_t)index;
 	w->generation = generation;
+	h_islandsInit( w );
 	int rc = b2gDev_Create( &w->dev );
 	if ( rc != 0 )
 	{
@@ -259,6 +260,7 @@ void b2DestroyWorld( b2WorldId worldId )
 	h_free( w->endEvents[1] );
 	h_free( w->pendingInits );
 	h_free( w->pendingKills );
+	h_islandsFree( w );
 	uint16_t generation = w->generation;
 	memset( w, 0, sizeof( *w ) );
 	w->generation = generation + 1;
@@ -266,9 +268,15 @@ void b2DestroyWorld( b2WorldId worldId )
 
 bool b2World_IsValid( b2WorldId id ) { return h_worldFromId( id ) != NULL; }
 
+/* physics_world.c:1704-1734: switching sleep off wakes every sleeping set */
 void b2World_EnableSleeping( b2WorldId worldId, bool flag )
 {
 	h_world* w = h_worldFromId( worldId );
+	if ( w && w->locked == 0 && flag == false && w->enableSleep )
+	{
+		for ( int i = H_FIRST_SLEEPING_SET; i < w->sets.count; ++i )
+			if ( w->sets.data[i].setIndex != B2_NULL_INDEX && w->sets.data[i].bodyIds.count > 0 ) h_wakeSolverSet( w, i );
+	}
 	if ( w ) w->enableSleep = flag;
 }
 
@@ -314,6 +322,8 @@ b2Counters b2World_GetCounters( b2WorldId worldId )
 	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
 		c.colorCounts[i] = w->colors[i].contactIds.count + w->colors[i].jointIds.count;
 	c.awakeContactCount = w->awakeContactIds.count;
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i ) c.awakeContactCount += w->colors[i].contactIds.count;
+	c.islandCount = w->islandIdPool.nextIndex - w->islandIdPool.freeArray.count;
 	c.recycledContactCount = w->recycledContactCount;
 	return c;
 }
@@ -321,29 +331,33 @@ b2Counters b2World_GetCounters( b2WorldId worldId )
 b2BodyEvents b2World_GetBodyEvents( b2WorldId worldId )
 {
 	h_world* w = h_worldFromId( worldId );
-	if ( w->moveEventsValid == 0 && w->stepIndex > 0 )
-	{
-		/* materialize the move events of the last step from the device state
-		   (solver.c:608-612 fills one per awake body) */
-		h_syncFromDevice( w );
-		int n = w->awakeBodyIds.count;
-		h_reserve( w->moveEvents, n );
-		w->moveEvents.count = n;
-		for ( int i = 0; i < n; ++i )
-		{
-			h_body* b = w->bodies.data + w->awakeBodyIds.data[i];
-			b2BodyMoveEvent* ev = w->moveEvents.data + i;
-			ev->transform = b->transform;
-			ev->bodyId.index1 = b->id + 1;
-			ev->bodyId.world0 = w->worldId;
-			ev->bodyId.generation = b->generation;
-			ev->userData = b->userData;
-			ev->fellAsleep = false;
-		}
-		w->moveEventsValid = 1;
-	}
+	if ( w->moveEventsValid == 0 && w->stepIndex > 0 ) h_buildMoveEvents( w );
 	b2BodyEvents e = { w->moveEvents.data, w->moveEvents.count };
 	return e;
+}
+
+/* materialize the move events of the last step from the device state: one per body of
+   the awake set as the finalize saw it (solver.c:608-622); the sleep pass builds them
+   before it moves bodies out of the awake set */
+void h_buildMoveEvents( h_world* w )
+{
+	h_syncFromDevice( w );
+	int n = w->awakeBodyIds.count;
+	h_reserve( w->moveEvents, n );
+	w->moveEvents.count = n;
+	for ( int i = 0; i < n; ++i )
+	{
+		h_body* b = w->bodies.data + w->awakeBodyIds.data[i];
+		b2BodyMoveEvent* ev = w->moveEvents.data + i;
+		ev->transform = b->transform;
+		ev->bodyId.index1 = b->id + 1;
+		ev->bodyId.world0 = w->worldId;
+		ev->bodyId.generation = b->generation;
+		ev->userData = b->userData;
+		ev->fellAsleep = false;
+		b->bodyMoveIndex = i;
+	}
+	w->moveEventsValid = 1;
 }
 
 b2ContactEvents b2World_GetContactEvents( b2WorldId worldId )
@@ -369,9 +383,9 @@ void h_syncFromDevice( h_world* w )
 	if ( w->hostStateValid || w->devReady == 0 ) return;
 	int nb = w->bodies.count;
 	int na = w->awakeBodyIds.count;
-	const float *xf = NULL, *center = NULL, *sv = NULL;
+	const float *xf = NULL, *center = NULL, *sv = NULL, *sleepTime = NULL;
 	const uint32_t* typeFlags = NULL;
-	int rc = b2gDev_DownloadState( w->dev, nb, na, &xf, &center, &typeFlags, &sv );
+	int rc = b2gDev_DownloadState( w->dev, nb, na, &xf, &center, &typeFlags, &sv, &sleepTime );
 	if ( rc != 0 ) h_fail( w, "device download", rc );
 	for ( int i = 0; i < nb; ++i )
 	{
@@ -388,6 +402,7 @@ void h_syncFromDevice( h_world* w )
 		h_body* b = w->bodies.data + w->awakeBodyIds.data[a];
 		b->linearVelocity = h_v( sv[4 * a], sv[4 * a + 1] );
 		b->angularVelocity = sv[4 * a + 2];
+		b->sleepTime = sleepTime[a];
 	}
 	w->hostStateValid = 1;
 }
@@ -403,7 +418,7 @@ void h_syncJointsFromDevice( h_world* w )
 	w->jointsHostValid = 1;
 }
 
-static void h_markHostChanged( h_world* w )
+void h_markHostChanged( h_world* w )
 {
 	h_syncFromDevice( w );
 	h_syncJointsFromDevice( w );
@@ -468,9 +483,11 @@ void h_ensureDevice( h_world* w )
 	float* sd = calloc( nac * 4, sizeof( float ) );
 	float* params = calloc( nac * 8, sizeof( float ) );
 	float* c0 = calloc( nac * 4, sizeof( float ) );
+	float* sleepTimes = calloc( nac, sizeof( float ) );
 	for ( int a = 0; a < na; ++a )
 	{
 		h_body* b = w->bodies.data + awakeBodyId[a];
+		sleepTimes[a] = b->sleepTime;
 		uint32_t fl = b->simFlags;
 		float flBits;
 		memcpy( &flBits, &fl, 4 );
@@ -563,7 +580,7 @@ void h_ensureDevice( h_world* w )
 	int rc = b2gDev_UploadBodies( w->dev, nb, xf, center, localCenter, invMass, invI, minExtent, maxExtent, sleepThreshold, safetyFactor,
 								  awakeIndex, typeFlags,
 								  shapeStart, shapeCount, shapeList, listCount );
-	if ( rc == 0 ) rc = b2gDev_UploadAwake( w->dev, na, awakeBodyId, sv, sd, params, c0 );
+	if ( rc == 0 ) rc = b2gDev_UploadAwake( w->dev, na, awakeBodyId, sv, sd, params, c0, sleepTimes );
 	if ( rc == 0 ) rc = b2gDev_UploadShapes( w->dev, shapes, aabbs, fats, ns );
 	if ( rc != 0 ) h_fail( w, "device upload", rc );
 	free( xf );
@@ -584,12 +601,14 @@ void h_ensureDevice( h_world* w )
 	free( sd );
 	free( params );
 	free( c0 );
+	free( sleepTimes );
 	free( shapes );
 	free( aabbs );
 	free( fats );
 	w->jointsDirty = 1;
 
 	w->colorsDirty = 1;
+	w->islandsDirty = 1;
 	w->devReady = 1;
 }
 
@@ -633,17 +652,32 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	b->linearVelocity = def->linearVelocity;
 	b->angularVelocity = def->angularVelocity;
 	b->userData = def->userData;
+	/* body.c:194-226: a body created asleep gets a sleeping set of its own and no state */
+	int isAwake = def->isAwake || def->enableSleep == false;
 	if ( def->type == b2_staticBody )
 	{
 		b->setIndex = H_STATIC_SET;
 		b->localIndex = w->staticCount++;
 	}
-	else
+	else if ( isAwake )
 	{
 		b->setIndex = H_AWAKE_SET;
 		b->localIndex = w->awakeBodyIds.count;
 		h_push( w->awakeBodyIds, bodyId );
 	}
+	else
+	{
+		int setId = h_allocSleepingSet( w );
+		h_sleepSet* set = w->sets.data + setId;
+		b->setIndex = setId;
+		b->localIndex = set->bodyIds.count;
+		h_push( set->bodyIds, bodyId );
+		b->linearVelocity = h_v( 0.0f, 0.0f );
+		b->angularVelocity = 0.0f;
+	}
+	b->islandId = B2_NULL_INDEX;
+	b->islandIndex = B2_NULL_INDEX;
+	b->bodyMoveIndex = B2_NULL_INDEX;
 	b->generation = generation + 1;
 	b->headShapeId = B2_NULL_INDEX;
 	b->headContactKey = B2_NULL_INDEX;
@@ -653,7 +687,9 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	b->safetyFactor = def->safetyFactor;
 	b->type = def->type;
 	b->flags = flags;
-	b2BodyId id = { bodyId + 1, w->worldId, b->generation };
+	/* dynamic and kinematic bodies get an island (body.c:319-323) */
+	if ( b->setIndex >= H_AWAKE_SET ) h_createIslandForBody( w, b->setIndex, b );
+	b2BodyId id = { bodyId + 1, w->worldId, w->bodies.data[bodyId].generation };
 	return id;
 }
 
@@ -702,12 +738,15 @@ float b2Body_GetAngularVelocity( b2BodyId bodyId )
 	return b->setIndex == H_AWAKE_SET ? b->angularVelocity : 0.0f;
 }
 
-/* body.c:790-840: the new velocity goes to the host record and straight to the device */
+/* body.c:790-840: a nonzero velocity wakes a sleeping body; the new velocity of an awake
+   body goes to the host record and straight to the device */
 void b2Body_SetLinearVelocity( b2BodyId bodyId, b2Vec2 v )
 {
 	h_world* w = h_worlds + bodyId.world0;
 	h_body* b = h_getBody( bodyId );
 	if ( b->type == b2_staticBody ) return;
+	if ( v.x * v.x + v.y * v.y > 0.0f ) h_wakeBody( w, b );
+	if ( b->setIndex != H_AWAKE_SET ) return;
 	b->linearVelocity = v;
 	if ( w->devReady )
 	{
@@ -720,7 +759,9 @@ void b2Body_SetAngularVelocity( b2BodyId bodyId, float av )
 {
 	h_world* w = h_worlds + bodyId.world0;
 	h_body* b = h_getBody( bodyId );
-	if ( b->type == b2_staticBody ) return;
+	if ( b->type == b2_staticBody || ( b->flags & B2G_LOCK_Z ) ) return;
+	if ( av != 0.0f ) h_wakeBody( w, b );
+	if ( b->setIndex != H_AWAKE_SET ) return;
 	b->angularVelocity = av;
 	if ( w->devReady )
 	{
@@ -742,6 +783,28 @@ b2Pos b2Body_GetWorldCenter( b2BodyId bodyId )
 }
 
 bool b2Body_IsAwake( b2BodyId bodyId ) { return h_getBody( bodyId )->setIndex == H_AWAKE_SET; }
+
+/* body.c:1550-1575: wake the body's set, or put its island to sleep (split first when
+   constraints were removed from it) */
+void b2Body_SetAwake( b2BodyId bodyId, bool awake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	if ( w->inUse == 0 || w->locked ) return;
+	h_body* b = h_getBody( bodyId );
+	if ( awake && b->setIndex >= H_FIRST_SLEEPING_SET )
+	{
+		h_wakeBody( w, b );
+	}
+	else if ( awake == false && b->setIndex == H_AWAKE_SET )
+	{
+		h_markHostChanged( w );
+		if ( w->islands.data[b->islandId].constraintRemoveCount > 0 ) h_splitIsland( w, b->islandId );
+		h_trySleepIsland( w, b->islandId );
+	}
+}
+
+/* body.c b2Body_GetSleepThreshold / b2Body_SetSleepThreshold */
+float b2Body_GetSleepThreshold( b2BodyId bodyId ) { return h_getBody( bodyId )->sleepThreshold; }
 
 /* body.c b2Body_GetShapeCount / b2Body_GetShapes: the body's shape list, head first */
 int b2Body_GetShapeCount( b2BodyId bodyId ) { return h_getBody( bodyId )->shapeCount; }
@@ -1007,9 +1070,13 @@ void h_createContact( h_world* w, h_shape* shapeA, h_shape* shapeB )
 	h_contact* c = w->contacts.data + contactId;
 	c->contactId = contactId;
 	c->generation += 1;
-	c->setIndex = H_AWAKE_SET;
+	/* contact.c:241-252: in the awake set when a body is awake, else in the disabled set */
+	int awake = bodyA->setIndex == H_AWAKE_SET || bodyB->setIndex == H_AWAKE_SET;
+	c->setIndex = awake ? H_AWAKE_SET : H_DISABLED_SET;
 	c->colorIndex = B2_NULL_INDEX;
-	c->localIndex = w->awakeContactIds.count;
+	c->localIndex = awake ? w->awakeContactIds.count : w->disabledContactIds.count;
+	c->islandId = B2_NULL_INDEX;
+	c->islandIndex = B2_NULL_INDEX;
 	c->shapeIdA = shapeA->id;
 	c->shapeIdB = shapeB->id;
 	c->flags = 0;
@@ -1036,12 +1103,13 @@ void h_createContact( h_world* w, h_shape* shapeA, h_shape* shapeB )
 		bodyB->contactCount += 1;
 	}
 	h_pairSetAdd( &w->pairSet, H_SHAPE_PAIR_KEY( shapeA->id, shapeB->id ) );
-	h_push( w->awakeContactIds, contactId );
+	if ( awake ) h_push( w->awakeContactIds, contactId );
+	else h_push( w->disabledContactIds, contactId );
 	b2gContactInit init;
 	init.contactId = contactId;
 	init.shapeIdA = shapeA->id;
 	init.shapeIdB = shapeB->id;
-	init.simFlags = c->flags;
+	init.simFlags = c->flags | ( awake ? 0u : (uint32_t)B2G_S_ASLEEP );
 	init.friction = sqrtf( shapeA->material.friction * shapeB->material.friction );
 	init.restitution = h_max( shapeA->material.restitution, shapeB->material.restitution );
 	h_push( w->pendingInits, init );
@@ -1088,14 +1156,29 @@ void h_destroyContact( h_world* w, h_contact* c )
 	if ( eB->nextKey != B2_NULL_INDEX ) w->contacts.data[eB->nextKey >> 1].edges[eB->nextKey & 1].prevKey = eB->prevKey;
 	if ( bodyB->headContactKey == ( ( contactId << 1 ) | 1 ) ) bodyB->headContactKey = eB->nextKey;
 	bodyB->contactCount -= 1;
+	/* contact.c:462-500: leave the island, then the array that holds the contact */
+	if ( c->islandId != B2_NULL_INDEX ) h_unlinkContact( w, c );
 	if ( c->colorIndex != B2_NULL_INDEX ) h_removeContactFromGraph( w, bodyIdA, bodyIdB, c->colorIndex, c->localIndex );
-	else h_removeNonTouchingContact( w, c->localIndex );
+	else if ( c->setIndex == H_AWAKE_SET ) h_removeNonTouchingContact( w, c->localIndex );
+	else
+	{
+		h_intArray* list = c->setIndex == H_DISABLED_SET ? &w->disabledContactIds : &w->sets.data[c->setIndex].contactIds;
+		int localIndex = c->localIndex;
+		int moved = h_removeSwap( *list, localIndex );
+		if ( moved != B2_NULL_INDEX ) w->contacts.data[list->data[localIndex]].localIndex = localIndex;
+	}
 	c->contactId = B2_NULL_INDEX;
 	c->setIndex = B2_NULL_INDEX;
 	c->colorIndex = B2_NULL_INDEX;
 	c->localIndex = B2_NULL_INDEX;
 	h_freeId( &w->contactIdPool, contactId );
 	h_push( w->pendingKills, contactId );
+	/* a touching contact that goes away wakes its bodies */
+	if ( flags & B2G_C_TOUCHING )
+	{
+		h_wakeBody( w, w->bodies.data + bodyIdA );
+		h_wakeBody( w, w->bodies.data + bodyIdB );
+	}
 }
 
 /* ---------------- graph coloring (constraint_graph.c:66-291) ---------------- */

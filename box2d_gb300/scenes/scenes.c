@@ -690,6 +690,97 @@ static void b2sJointZoo( b2sScene* s, int count, b2sRng* rng )
 	}
 }
 
+/* Falling hinges: the scene of the reference's determinism test (shared/determinism.c:11-108,
+   test/test_determinism.c): a 40 x 1 ground box, four columns of twenty 0.25 m squares tilted
+   by +-0.1 rad, each pair joined by a revolute joint with limit, spring and motor. Sleeping
+   stays on: the test runs until every island is asleep. */
+static void b2sFallingHinges( b2sScene* s )
+{
+	{
+		b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, -1.0f );
+		b2Polygon box = b2MakeBox( 40.0f, 1.0f );
+		b2ShapeDef sd = b2DefaultShapeDef();
+		b2CreatePolygonShape( ground, &sd, &box );
+	}
+	const int columnCount = 4, rowCount = 20;
+	const float h = 0.25f;
+	b2Polygon square = b2MakeSquare( h );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2RevoluteJointDef jd = b2DefaultRevoluteJointDef();
+	jd.enableLimit = true;
+	jd.lowerAngle = -0.1f * B2_PI;
+	jd.upperAngle = 0.2f * B2_PI;
+	jd.enableSpring = true;
+	jd.hertz = 1.0f;
+	jd.dampingRatio = 1.0f;
+	jd.enableMotor = true;
+	jd.maxMotorTorque = 0.25f;
+	jd.base.localFrameA.p.x = -h;
+	jd.base.localFrameA.p.y = h;
+	jd.base.localFrameB.p.x = -h;
+	jd.base.localFrameB.p.y = -h;
+	jd.base.constraintHertz = 60.0f;
+	jd.base.constraintDampingRatio = 0.0f;
+	jd.base.drawScale = 0.5f;
+	float offset = 0.4f * h;
+	float dx = 10.0f * h;
+	float xBase = -0.5f * dx * ( columnCount - 1.0f );
+	for ( int j = 0; j < columnCount; ++j )
+	{
+		float x = xBase + j * dx;
+		b2BodyId prev = { 0 };
+		for ( int i = 0; i < rowCount; ++i )
+		{
+			b2BodyDef bd = b2DefaultBodyDef();
+			bd.type = b2_dynamicBody;
+			bd.position.x = x + offset * i;
+			bd.position.y = h + 2.0f * h * i;
+			float angle = ( i & 1 ) == 0 ? -0.1f : 0.1f;
+			bd.rotation = b2MakeRot( angle );
+			b2BodyId body = b2CreateBody( s->worldId, &bd );
+			b2sAddBody( s, body, 1 );
+			if ( ( i & 1 ) == 0 )
+			{
+				prev = body;
+			}
+			else
+			{
+				jd.base.bodyIdA = prev;
+				jd.base.bodyIdB = body;
+				b2CreateRevoluteJoint( s->worldId, &jd );
+				prev = ( b2BodyId ){ 0 };
+			}
+			b2CreatePolygonShape( body, &sd, &square );
+		}
+	}
+}
+
+/* Sleeping pyramids: `a` pyramids of `b` rows (0.5 m boxes on one ground box, sleeping on)
+   and one box dropped from height `c` onto the first pyramid after the stacks have gone to
+   sleep, which wakes them through a contact that starts touching. */
+static void b2sSleepPyramids( b2sScene* s, int pyramidCount, int rows, int dropHeight )
+{
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	b2Polygon groundBox = b2MakeOffsetBox( 40.0f, 1.0f, ( b2Vec2 ){ 0.0f, -1.0f }, b2MakeRot( 0.0f ) );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2CreatePolygonShape( ground, &sd, &groundBox );
+	b2Polygon box = b2MakeSquare( 0.5f );
+	for ( int p = 0; p < pyramidCount; ++p )
+	{
+		float x0 = -30.0f + 12.0f * p;
+		for ( int i = 0; i < rows; ++i )
+		{
+			for ( int k = 0; k < rows - i; ++k )
+			{
+				b2BodyId body = b2sBody( s, b2_dynamicBody, x0 + 0.5f * i + 1.0f * k, 0.5f + 1.0f * i );
+				b2CreatePolygonShape( body, &sd, &box );
+			}
+		}
+	}
+	b2BodyId drop = b2sBody( s, b2_dynamicBody, -30.0f + 0.5f * ( rows - 1 ) + 0.3f, (float)dropHeight );
+	b2CreatePolygonShape( drop, &sd, &box );
+}
+
 enum
 {
 	B2S_LARGE_PYRAMID = 0,
@@ -702,6 +793,8 @@ enum
 	B2S_HELLO_WORLD = 7,
 	B2S_SHAPE_ZOO = 8,
 	B2S_JOINT_ZOO = 9,
+	B2S_FALLING_HINGES = 10,
+	B2S_SLEEP_PYRAMIDS = 11,
 };
 
 /* Create a scene. kind selects the builder; a, b, c are its size parameters; seed feeds
@@ -741,6 +834,8 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 		case B2S_HELLO_WORLD: b2sHelloWorld( s ); break;
 		case B2S_SHAPE_ZOO: b2sShapeZoo( s, a, &rng ); break;
 		case B2S_JOINT_ZOO: b2sJointZoo( s, a, &rng ); break;
+		case B2S_FALLING_HINGES: b2sFallingHinges( s ); break;
+		case B2S_SLEEP_PYRAMIDS: b2sSleepPyramids( s, a, b, c ); break;
 		default: break;
 	}
 	return h;
@@ -776,6 +871,60 @@ B2S_EXPORT void b2s_destroy( int h )
 B2S_EXPORT void b2s_step( int h, float dt, int subSteps, int count )
 {
 	for ( int i = 0; i < count; ++i ) b2World_Step( b2s_scenes[h].worldId, dt, subSteps );
+}
+
+/* The determinism test's loop (test/test_determinism.c:28-50, shared/determinism.c:110-134):
+   step until a step reports no body move events (every island asleep), then hash the
+   transforms of the scene's dynamic bodies in creation order with b2Hash. Returns the step
+   count at that moment (the test's sleepStep) and the hash, or -1 within `stepLimit`. */
+B2S_EXPORT int b2s_run_until_asleep( int h, int stepLimit, uint32_t* hashOut )
+{
+	b2sScene* s = b2s_scenes + h;
+	*hashOut = 0;
+	for ( int stepCount = 0; stepCount < stepLimit; ++stepCount )
+	{
+		b2World_Step( s->worldId, 1.0f / 60.0f, 4 );
+		b2BodyEvents events = b2World_GetBodyEvents( s->worldId );
+		if ( events.moveCount == 0 )
+		{
+			uint32_t hash = 5381; /* B2_HASH_INIT */
+			for ( int i = 0; i < s->bodyCount; ++i )
+			{
+				if ( b2Body_GetType( s->bodies[i] ) == b2_staticBody ) continue;
+				b2WorldTransform xf = b2Body_GetTransform( s->bodies[i] );
+				hash = b2Hash( hash, (const uint8_t*)&xf, (int)sizeof( b2WorldTransform ) );
+			}
+			*hashOut = hash;
+			return stepCount;
+		}
+	}
+	return -1;
+}
+
+/* scripted changes between steps (sleeping scenes): a body's velocity, which wakes it when
+   nonzero; putting a body's island to sleep or waking it; switching sleeping off */
+B2S_EXPORT void b2s_set_body_velocity( int h, int bodyIndex, float vx, float vy, float w )
+{
+	b2BodyId id = b2s_scenes[h].bodies[bodyIndex];
+	b2Body_SetLinearVelocity( id, ( b2Vec2 ){ vx, vy } );
+	b2Body_SetAngularVelocity( id, w );
+}
+
+#ifndef B2S_NO_ISLANDS
+B2S_EXPORT void b2s_set_awake( int h, int bodyIndex, int awake )
+{
+	b2Body_SetAwake( b2s_scenes[h].bodies[bodyIndex], awake != 0 );
+}
+#endif
+
+B2S_EXPORT void b2s_enable_sleep( int h, int flag ) { b2World_EnableSleeping( b2s_scenes[h].worldId, flag != 0 ); }
+
+/* awake body count and the per-body awake flags (creation order) */
+B2S_EXPORT int b2s_awake( int h, int* out )
+{
+	b2sScene* s = b2s_scenes + h;
+	for ( int i = 0; i < s->bodyCount; ++i ) out[i] = b2Body_IsAwake( s->bodies[i] ) ? 1 : 0;
+	return b2World_GetAwakeBodyCount( s->worldId );
 }
 
 B2S_EXPORT int b2s_body_count( int h ) { return b2s_scenes[h].bodyCount; }

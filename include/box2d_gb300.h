@@ -590,6 +590,11 @@ B2G_API float b2Body_GetRotationalInertia( b2BodyId bodyId );
 B2G_API b2Vec2 b2Body_GetLocalCenter( b2BodyId bodyId );
 B2G_API b2Pos b2Body_GetWorldCenter( b2BodyId bodyId );
 B2G_API bool b2Body_IsAwake( b2BodyId bodyId );
+/* body.c b2Body_SetAwake (box2d.h:552): wake the body's sleeping set, or put its island
+   to sleep */
+B2G_API void b2Body_SetAwake( b2BodyId bodyId, bool awake );
+/* body.c b2Body_GetSleepThreshold (box2d.h:567) */
+B2G_API float b2Body_GetSleepThreshold( b2BodyId bodyId );
 
 /* ---- API: shapes (box2d.h:659-724) ---- */
 B2G_API b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Circle* circle );

@@ -297,7 +297,9 @@ b2Counters b2World_GetCounters( b2WorldId worldId )
 	c.treeHeight = o_treeHeight( w->trees + b2_dynamicBody );
 	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
 		c.colorCounts[i] = w->colors[i].contactSims.count + w->colors[i].jointSims.count;
+	/* physics_world.c:1920-1927: colored contacts plus the awake set's non-touching ones */
 	c.awakeContactCount = w->awakeContactSims.count;
+	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i ) c.awakeContactCount += w->colors[i].contactSims.count;
 	c.recycledContactCount = w->recycledContactCount;
 	return c;
 }

@@ -40,6 +40,23 @@ SCENES = [
     ("batch_world_continuous", B.BATCH_WORLD, 0, 0, 0, 21, 0, 300, [1, 300]),
 ]
 
+# sleeping on: islands fall asleep and wake; per step also the awake body count. The
+# oracle does not restate islands, so only the GB300 library is checked against these.
+SLEEP_SCENES = [
+    ("falling_hinges", B.FALLING_HINGES, 0, 0, 0, 0, 0, 300, [1, 100, 274, 300]),
+    ("sleep_pyramids_3x8", B.SLEEP_PYRAMIDS, 3, 8, 80, 0, 0, 700, [1, 200, 400, 700]),
+    ("sleep_api_pyramids", B.SLEEP_PYRAMIDS, 2, 6, 1000, 0, 0, 330, [1, 56, 131, 201, 330]),
+]
+# changes applied after the given step (Scene.apply): wake by velocity, put an island to
+# sleep and wake one through b2Body_SetAwake, switch sleeping off and on again
+SCRIPTS = {
+    "sleep_api_pyramids": [[40, "velocity", 3, 0.0, 6.0, 0.0], [41, "velocity", 25, 2.0, 0.0, 1.0],
+                           [55, "awake", 10, 0], [130, "awake", 30, 1], [200, "sleeping", 0], [260, "sleeping", 1]],
+}
+# test/test_determinism.c:21-22
+DETERMINISM_SLEEP_STEP = 274
+DETERMINISM_HASH = 0xE86690F4
+
 
 def contact_digest(table) -> str:
     return hashlib.sha256(table.astype("<i4").tobytes()).hexdigest()
@@ -48,12 +65,19 @@ def contact_digest(table) -> str:
 def main() -> None:
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"], check=True)
     ref = B.load_library(ROOT / "oracle" / "_ref" / "libref.so")
-    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES:
+    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES + SLEEP_SCENES:
+        sleeping = (name, kind, a, b, c, seed, flags, steps, digest_steps) in SLEEP_SCENES
+        script = SCRIPTS.get(name, [])
         with B.Scene(ref, kind, a, b, c, seed, flags) as s:
-            hashes, digests = [], {}
+            hashes, digests, awake = [], {}, []
             for k in range(1, steps + 1):
                 s.step()
+                for action in script:
+                    if action[0] == k:
+                        s.apply(action[1:])
                 hashes.append(f"{s.state_hash():016x}")
+                if sleeping:
+                    awake.append(s.awake()[0])
                 if k in digest_steps:
                     table = s.contacts()
                     digests[str(k)] = {"count": int(table.shape[0]), "sha256": contact_digest(table),
@@ -61,6 +85,17 @@ def main() -> None:
             data = {"scene": name, "kind": kind, "a": a, "b": b, "c": c, "seed": seed, "flags": flags,
                     "dt": 1.0 / 60.0, "substeps": 4, "bodies": s.body_count, "state_hashes": hashes,
                     "contact_digests": digests, "source": "reference built from its own sources (oracle/Makefile ref)"}
+            if sleeping:
+                data["requires"] = "islands"
+                data["awake_counts"] = awake
+                if script:
+                    data["script"] = script
+        if kind == B.FALLING_HINGES:
+            # the reference's own determinism test, rerun here: it must give the test's constants
+            with B.Scene(ref, kind, a, b, c, seed, flags) as s:
+                sleep_step, digest = s.run_until_asleep(500)
+            assert (sleep_step, digest) == (DETERMINISM_SLEEP_STEP, DETERMINISM_HASH), (sleep_step, hex(digest))
+            data["run_until_asleep"] = {"sleep_step": sleep_step, "hash": f"{digest:08x}"}
         (Path(__file__).parent / f"{name}.json").write_text(json.dumps(data, indent=1))
         print(name, steps, "steps", s.body_count, "bodies")
 

@@ -41,7 +41,10 @@ def test_library_exports_every_declared_function():
 
 def test_oracle_exports_the_public_api(oracle):
     skip = {"b2p_status", "b2p_timings", "b2p_stream", "b2p_host_profile", "b2p_contacts_noalloc", "b2World_StepBatch",
-            "b2p_batch_profile"}
+            "b2p_batch_profile",
+            # islands and sleeping are pinned against fixtures of the reference itself
+            # (tests/golden/make_golden.py), not restated in the oracle
+            "b2Body_SetAwake", "b2Body_GetSleepThreshold"}
     # differentiable stepping (box2d_gb300_diff.h) is an extension of the GB300 library; its
     # checker is the host tangent-linear code, not the oracle's public API
     missing = [n for n in sorted(declared_functions())

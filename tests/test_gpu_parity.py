@@ -20,9 +20,15 @@ def test_gpu_matches_reference_fixture(gpu_lib, name):
     g = load_golden(name)
     with B.Scene(gpu_lib, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
         assert s.body_count == g["bodies"]
+        script = g.get("script", [])
         for k, expected in enumerate(g["state_hashes"], start=1):
             s.step(1, g["dt"], g["substeps"])
+            for action in script:
+                if action[0] == k:
+                    s.apply(action[1:])
             assert f"{s.state_hash():016x}" == expected, f"{name}: body state differs from the reference at step {k}"
+            if "awake_counts" in g:
+                assert s.awake()[0] == g["awake_counts"][k - 1], f"{name}: awake body count at step {k}"
             d = g["contact_digests"].get(str(k))
             if d is not None:
                 table = s.contacts()
