@@ -333,7 +333,7 @@ def run_cpu_batch(args, budget_s: float, max_steps: int) -> dict:
     kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
     lib = B.load_library(ROOT / "oracle" / "liboracle.so")
     threads = max(1, os.cpu_count() or 1)
-    sample = min(args.worlds, 16 * threads)
+    sample = min(args.worlds, 16 * threads, 120)  # the oracle holds at most 128 worlds
     scenes = [B.Scene(lib, kind, a, b, c, seed + i, flags) for i in range(sample)]
     dyn = sum(s.dynamic_count for s in scenes)
     with ThreadPoolExecutor(threads) as ex:
