@@ -21,12 +21,23 @@
 
 #include <cooperative_groups.h>
 #include <pthread.h>
+#include <stddef.h>
 #include <string.h>
 
 namespace cg = cooperative_groups;
 
 #define B2G_CLUSTER_THREADS 512
 #define B2G_CLUSTER_SMEM_MAX ( 220 * 1024 )
+#define B2G_CLUSTER_MAX_RANKS 16
+/* clusterCounts, by [k * 16 + rank] for active color k: the contact lanes claimed from a
+   CTA and given to it, the joints claimed and given; then per CTA the lanes claimed over all
+   colors */
+#define B2G_CLUSTER_CLAIMS 0
+#define B2G_CLUSTER_FILLS ( B2_GRAPH_COLOR_COUNT * B2G_CLUSTER_MAX_RANKS )
+#define B2G_CLUSTER_JCLAIMS ( 2 * B2_GRAPH_COLOR_COUNT * B2G_CLUSTER_MAX_RANKS )
+#define B2G_CLUSTER_JFILLS ( 3 * B2_GRAPH_COLOR_COUNT * B2G_CLUSTER_MAX_RANKS )
+#define B2G_CLUSTER_TOTALS ( 4 * B2_GRAPH_COLOR_COUNT * B2G_CLUSTER_MAX_RANKS )
+#define B2G_CLUSTER_COUNT_WORDS ( ( 4 * B2_GRAPH_COLOR_COUNT + 1 ) * B2G_CLUSTER_MAX_RANKS )
 
 struct d_clusterPlan
 {
@@ -40,23 +51,44 @@ struct d_clusterPlan
 	const int* positionOf; /* awake index -> position in bodyList (lists only) */
 	const b2gCompSummary* summary;
 	int bodyCount;
-	int rankShift; /* ranks = 1 << rankShift */
-	int slotsPerRank;
+	int ranks;
+	int slotsPerRank; /* bodies per CTA: position p lives in CTA p / slotsPerRank */
+	int laneCap;	  /* contact lanes one CTA's shared memory holds */
+	int colorCap[B2_GRAPH_COLOR_COUNT]; /* lanes of an active color a CTA takes in one pass */
+	int jointCap[B2_GRAPH_COLOR_COUNT]; /* joints of an active color a CTA takes in one pass */
+	int* assignedJoints;				/* color c, CTA r: joints at [jointOffset(c) * ranks + r * count(c)] */
+	int* assigned;	  /* color c, CTA r: slots at assigned[offset(c) * ranks + r * count(c)] */
+	int* counts;	  /* B2G_CLUSTER_COUNT_WORDS assignment counters */
+	int* status;	  /* B2G_STATUS_CAPACITY if a CTA was given more lanes than it holds */
 };
 
-/* body state in distributed shared memory: position p -> CTA p & mask, slot p >> shift */
+/* A body reference inside the cluster is (owning CTA << 16 | slot in that CTA). Positions
+   are split in contiguous blocks, so bodies that touch each other -- neighbours in the
+   awake order -- mostly share a CTA, and a contact is solved by the CTA that owns its first
+   dynamic body: most body accesses stay in the CTA's own shared memory. */
+static __device__ __forceinline__ int d_clusterKey( const d_clusterPlan& plan, int p )
+{
+	int r = p / plan.slotsPerRank;
+	return ( r << 16 ) | ( p - r * plan.slotsPerRank );
+}
+
+static __device__ __forceinline__ int d_clusterPosition( const d_clusterPlan& plan, int key )
+{
+	return ( key >> 16 ) * plan.slotsPerRank + ( key & 0xffff );
+}
+
+/* body state in distributed shared memory, addressed by cluster key */
 struct d_clusterBodies
 {
 	float4* sv;
 	float4* sd;
-	int shift, mask;
-	__device__ __forceinline__ float4& v( int i ) const
+	__device__ __forceinline__ float4& v( int key ) const
 	{
-		return *cg::this_cluster().map_shared_rank( sv + ( i >> shift ), (unsigned)( i & mask ) );
+		return *cg::this_cluster().map_shared_rank( sv + ( key & 0xffff ), (unsigned)( key >> 16 ) );
 	}
-	__device__ __forceinline__ float4& d( int i ) const
+	__device__ __forceinline__ float4& d( int key ) const
 	{
-		return *cg::this_cluster().map_shared_rank( sd + ( i >> shift ), (unsigned)( i & mask ) );
+		return *cg::this_cluster().map_shared_rank( sd + ( key & 0xffff ), (unsigned)( key >> 16 ) );
 	}
 };
 
@@ -70,47 +102,167 @@ static __device__ __forceinline__ int d_planJointCount( const d_clusterPlan& pla
 	return plan.useLists ? plan.summary->bigJointCount[color] : plan.jointOffsets[color + 1] - plan.jointOffsets[color];
 }
 
-__global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solveArgs a, d_jointBodies jb, d_clusterPlan plan )
+/* one claim on CTA r for active color k: a lane slot within the color's one-pass share
+   (unless `anyShare`) and within the CTA's shared memory */
+static __device__ __forceinline__ bool d_clusterClaim( const d_clusterPlan& plan, int k, int r, bool anyShare )
+{
+	if ( anyShare == false && atomicAdd( plan.counts + B2G_CLUSTER_CLAIMS + k * B2G_CLUSTER_MAX_RANKS + r, 1 ) >= plan.colorCap[k] )
+		return false;
+	return atomicAdd( plan.counts + B2G_CLUSTER_TOTALS + r, 1 ) < plan.laneCap;
+}
+
+/* Give each contact of the solve to the CTA owning its first dynamic body, else to the
+   owner of the other body, else to the next CTA with room: a CTA takes at most one pass of
+   lanes per color while another has room, and never more lanes than its shared memory
+   holds (the host checks that all lanes fit the cluster). Grid: x over a color's contacts,
+   y over the active colors. Within a color the order of the lanes does not matter: they
+   touch disjoint bodies. */
+static __device__ void d_clusterAssignJoint( const d_clusterPlan& plan, const b2gJoint* joints, int k, int i );
+
+__global__ void k_clusterAssign( d_solveArgs a, d_clusterPlan plan )
+{
+	const int k = blockIdx.y;
+	const int color = plan.colors[k];
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( blockIdx.z == 1 )
+	{
+		if ( i < d_planJointCount( plan, color ) ) d_clusterAssignJoint( plan, a.joints, k, i );
+		return;
+	}
+	if ( i >= d_planContactCount( a, plan, color ) ) return;
+	const int begin = a.colorOffsets[color], colorSize = a.colorOffsets[color + 1] - begin;
+	const int slot = plan.useLists ? plan.slotList[begin + i] : begin + i;
+	const b2gContact* cs = a.contacts + a.colorIds[slot];
+	int owners[2] = { -1, -1 };
+	int bodies[2] = { cs->bodySimIndexA, cs->bodySimIndexB };
+	for ( int j = 0; j < 2; ++j )
+	{
+		if ( bodies[j] < 0 ) continue;
+		int p = plan.positionOf ? plan.positionOf[bodies[j]] : bodies[j];
+		owners[j] = min( p / plan.slotsPerRank, plan.ranks - 1 );
+	}
+	if ( owners[0] < 0 ) owners[0] = owners[1] >= 0 ? owners[1] : 0;
+	int r = -1;
+	if ( d_clusterClaim( plan, k, owners[0], false ) ) r = owners[0];
+	else if ( owners[1] >= 0 && owners[1] != owners[0] && d_clusterClaim( plan, k, owners[1], false ) ) r = owners[1];
+	for ( int pass = 0; pass < 2 && r < 0; ++pass )
+	{
+		for ( int j = 1; j <= plan.ranks && r < 0; ++j )
+		{
+			int c = owners[0] + j < plan.ranks ? owners[0] + j : owners[0] + j - plan.ranks;
+			if ( d_clusterClaim( plan, k, c, pass == 1 ) ) r = c;
+		}
+	}
+	if ( r < 0 )
+	{
+		atomicExch( plan.status, B2G_STATUS_CAPACITY );
+		return;
+	}
+	int idx = atomicAdd( plan.counts + B2G_CLUSTER_FILLS + k * B2G_CLUSTER_MAX_RANKS + r, 1 );
+	plan.assigned[(long long)begin * plan.ranks + (long long)r * colorSize + idx] = slot;
+}
+
+/* joints likewise, without a shared-memory limit (joints stay in global memory) */
+static __device__ void d_clusterAssignJoint( const d_clusterPlan& plan, const b2gJoint* joints, int k, int i )
+{
+	const int color = plan.colors[k];
+	const int begin = plan.jointOffsets[color], colorSize = plan.jointOffsets[color + 1] - begin;
+	const int index = plan.useLists ? plan.jointList[begin + i] : begin + i;
+	const b2gJoint* J = joints + index;
+	int bodies[2] = { J->indexA, J->indexB };
+	int owners[2] = { -1, -1 };
+	for ( int j = 0; j < 2; ++j )
+	{
+		if ( bodies[j] < 0 ) continue;
+		int p = plan.positionOf ? plan.positionOf[bodies[j]] : bodies[j];
+		owners[j] = min( p / plan.slotsPerRank, plan.ranks - 1 );
+	}
+	if ( owners[0] < 0 ) owners[0] = owners[1] >= 0 ? owners[1] : 0;
+	int* claims = plan.counts + B2G_CLUSTER_JCLAIMS + k * B2G_CLUSTER_MAX_RANKS;
+	int r = -1;
+	if ( atomicAdd( claims + owners[0], 1 ) < plan.jointCap[k] ) r = owners[0];
+	else if ( owners[1] >= 0 && owners[1] != owners[0] && atomicAdd( claims + owners[1], 1 ) < plan.jointCap[k] ) r = owners[1];
+	for ( int j = 1; j <= plan.ranks && r < 0; ++j )
+	{
+		int c = owners[0] + j < plan.ranks ? owners[0] + j : owners[0] + j - plan.ranks;
+		if ( atomicAdd( claims + c, 1 ) < plan.jointCap[k] ) r = c;
+	}
+	if ( r < 0 ) r = owners[0]; /* every CTA has its one-pass share: the owner loops */
+	int idx = atomicAdd( plan.counts + B2G_CLUSTER_JFILLS + k * B2G_CLUSTER_MAX_RANKS + r, 1 );
+	plan.assignedJoints[(long long)begin * plan.ranks + (long long)r * colorSize + idx] = index;
+}
+
+/* A joint stage on a copy of the record: the record is read in one burst of 16-byte loads
+   and only the accumulated impulses (s[], the only fields a stage writes) are stored back.
+   Working on global memory directly would turn every body store, which may alias the record
+   for the compiler, into another round trip to L2 before the next field load. */
+static __device__ __forceinline__ void d_clusterJointStage( const b2gStepParams& P, b2gJoint* J, d_clusterBodies& bodies,
+															 int stage )
+{
+	static_assert( sizeof( b2gJoint ) % 16 == 0 && offsetof( b2gJoint, s ) % 16 == 0, "joint record layout" );
+	union
+	{
+		b2gJoint j;
+		float4 w[sizeof( b2gJoint ) / 16];
+	} copy;
+	const float4* src = (const float4*)J;
+#pragma unroll
+	for ( int i = 0; i < (int)( sizeof( b2gJoint ) / 16 ); ++i ) copy.w[i] = __ldcg( src + i );
+	d_jointStageT( P, &copy.j, bodies, stage );
+	float4* dst = (float4*)J->s;
+	const float4* s4 = (const float4*)copy.j.s;
+#pragma unroll
+	for ( int i = 0; i < 4; ++i ) dst[i] = s4[i];
+}
+
+__global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies jb, d_clusterPlan plan )
 {
 	cg::cluster_group cluster = cg::this_cluster();
 	const int rank = (int)cluster.block_rank();
-	const int ranks = 1 << plan.rankShift;
-	const int mask = ranks - 1;
+	const int ranks = plan.ranks;
 	extern __shared__ float4 s_mem[];
 	float4* sv = s_mem;
 	float4* sd = sv + plan.slotsPerRank;
 	b2gContactLane* lanes = (b2gContactLane*)( sd + plan.slotsPerRank );
-	__shared__ int s_cBegin[B2_GRAPH_COLOR_COUNT], s_cCount[B2_GRAPH_COLOR_COUNT];
+	__shared__ int s_cCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_jBegin[B2_GRAPH_COLOR_COUNT], s_jCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_laneOffset[B2_GRAPH_COLOR_COUNT];
+	__shared__ int s_restitution;
 	const int tid = threadIdx.x, nt = blockDim.x;
 	const b2gStepParams& P = a.p;
 	const int overflowBegin = a.colorOffsets[B2G_OVERFLOW_INDEX];
-	d_clusterBodies bodies = { sv, sd, plan.rankShift, mask };
-	/* this CTA's bodies: positions rank, rank + ranks, ... */
-	const int localCount = plan.bodyCount > rank ? ( plan.bodyCount - rank + ranks - 1 ) >> plan.rankShift : 0;
+	d_clusterBodies bodies = { sv, sd };
+	/* this CTA's bodies: positions [base, base + localCount) */
+	const int base = rank * plan.slotsPerRank;
+	const int localCount = max( 0, min( plan.slotsPerRank, plan.bodyCount - base ) );
 
-	/* this CTA's share of every color */
+	/* this CTA's lanes and joints of every color; s_jBegin is where the CTA's joint list of
+	   the color starts */
 	if ( tid == 0 )
 	{
 		int offset = 0;
 		for ( int k = 0; k < plan.colorCount; ++k )
 		{
 			int color = plan.colors[k];
-			int nc = d_planContactCount( a, plan, color ), nj = d_planJointCount( plan, color );
-			int cb = (int)( ( (long long)nc * rank ) / ranks ), ce = (int)( ( (long long)nc * ( rank + 1 ) ) / ranks );
-			int jb0 = (int)( ( (long long)nj * rank ) / ranks ), je = (int)( ( (long long)nj * ( rank + 1 ) ) / ranks );
-			s_cBegin[k] = cb;
-			s_cCount[k] = ce - cb;
-			s_jBegin[k] = jb0;
-			s_jCount[k] = je - jb0;
+			int nc = plan.counts[B2G_CLUSTER_FILLS + k * B2G_CLUSTER_MAX_RANKS + rank];
+			if ( offset + nc > plan.laneCap )
+			{
+				atomicExch( plan.status, B2G_STATUS_CAPACITY );
+				nc = max( 0, plan.laneCap - offset );
+			}
+			int nj = plan.counts[B2G_CLUSTER_JFILLS + k * B2G_CLUSTER_MAX_RANKS + rank];
+			int jbegin = plan.jointOffsets[color];
+			s_cCount[k] = nc;
+			s_jBegin[k] = jbegin * ranks + rank * ( plan.jointOffsets[color + 1] - jbegin );
+			s_jCount[k] = nj;
 			s_laneOffset[k] = offset;
-			offset += ce - cb;
+			offset += nc;
 		}
+		s_restitution = 0;
 	}
 	for ( int s = tid; s < localCount; s += nt )
 	{
-		int p = ( s << plan.rankShift ) + rank;
+		int p = base + s;
 		int ai = plan.bodyList ? plan.bodyList[p] : p;
 		sv[s] = a.sv[ai];
 		sd[s] = a.sd[ai];
@@ -118,40 +270,47 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 	__syncthreads();
 
 	/* prepare: joints in place (global), contacts into this CTA's shared memory; body
-	   references become positions */
+	   references become cluster keys */
+	int restitution = 0;
 	for ( int k = 0; k < plan.colorCount; ++k )
 	{
 		int color = plan.colors[k];
 		for ( int t = tid; t < s_jCount[k]; t += nt )
 		{
-			int idx = plan.jointOffsets[color] + s_jBegin[k] + t;
-			b2gJoint* J = a.joints + ( plan.useLists ? plan.jointList[idx] : idx );
+			b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k] + t];
 			d_prepareJoint( J, &jb, P.h, P.inv_h, P.enableWarmStarting != 0 );
-			if ( plan.positionOf )
-			{
-				J->indexA = J->indexA >= 0 ? plan.positionOf[J->indexA] : -1;
-				J->indexB = J->indexB >= 0 ? plan.positionOf[J->indexB] : -1;
-			}
+			int pa = J->indexA >= 0 ? ( plan.positionOf ? plan.positionOf[J->indexA] : J->indexA ) : -1;
+			int pb = J->indexB >= 0 ? ( plan.positionOf ? plan.positionOf[J->indexB] : J->indexB ) : -1;
+			J->indexA = pa >= 0 ? d_clusterKey( plan, pa ) : -1;
+			J->indexB = pb >= 0 ? d_clusterKey( plan, pb ) : -1;
 		}
+		const int begin = a.colorOffsets[color];
+		const int* mine = plan.assigned + (long long)begin * ranks + (long long)rank * ( a.colorOffsets[color + 1] - begin );
 		for ( int t = tid; t < s_cCount[k]; t += nt )
 		{
-			int idx = a.colorOffsets[color] + s_cBegin[k] + t;
 			b2gContactLane* L = lanes + s_laneOffset[k] + t;
-			d_prepareContactLane( a, plan.useLists ? plan.slotList[idx] : idx, overflowBegin, L );
-			if ( plan.positionOf )
-			{
-				L->indexA = L->indexA != 0 ? plan.positionOf[L->indexA - 1] + 1 : 0;
-				L->indexB = L->indexB != 0 ? plan.positionOf[L->indexB - 1] + 1 : 0;
-			}
+			d_prepareContactLane( a, mine[t], overflowBegin, L );
+			int pa = L->indexA != 0 ? ( plan.positionOf ? plan.positionOf[L->indexA - 1] : L->indexA - 1 ) : -1;
+			int pb = L->indexB != 0 ? ( plan.positionOf ? plan.positionOf[L->indexB - 1] : L->indexB - 1 ) : -1;
+			L->indexA = pa >= 0 ? d_clusterKey( plan, pa ) + 1 : 0;
+			L->indexB = pb >= 0 ? d_clusterKey( plan, pb ) + 1 : 0;
+			restitution |= L->groupFlags & 2;
 		}
 	}
+	if ( restitution ) s_restitution = 1;
 	cluster.sync();
+	/* the restitution stage only changes lanes whose 4-wide group has restitution
+	   (contact_solver.c:2131); without any in the cluster its color phases are skipped */
+	{
+		int any = tid < ranks ? *cluster.map_shared_rank( &s_restitution, (unsigned)tid ) : 0;
+		restitution = __syncthreads_or( any );
+	}
 
 	for ( int sub = 0; sub < P.subStepCount; ++sub )
 	{
 		for ( int s = tid; s < localCount; s += nt )
 		{
-			int p = ( s << plan.rankShift ) + rank;
+			int p = base + s;
 			int ai = plan.bodyList ? plan.bodyList[p] : p;
 			d_integrateVelocitiesState( P, sv, s, a.params + 8 * ai );
 		}
@@ -165,14 +324,12 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 			}
 			for ( int k = 0; k < plan.colorCount; ++k )
 			{
-				int color = plan.colors[k];
 				int nj = s_jCount[k], n = nj + s_cCount[k];
 				for ( int t = tid; t < n; t += nt )
 				{
 					if ( t < nj )
 					{
-						int idx = plan.jointOffsets[color] + s_jBegin[k] + t;
-						d_jointStageT( P, a.joints + ( plan.useLists ? plan.jointList[idx] : idx ), bodies, stage );
+						d_clusterJointStage( P, a.joints + plan.assignedJoints[s_jBegin[k] + t], bodies, stage );
 					}
 					else
 					{
@@ -183,11 +340,14 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 			}
 		}
 	}
-	for ( int k = 0; k < plan.colorCount; ++k )
+	if ( restitution )
 	{
-		for ( int t = tid; t < s_cCount[k]; t += nt )
-			d_laneStageT( P, lanes + s_laneOffset[k] + t, bodies, STAGE_RESTITUTION );
-		cluster.sync();
+		for ( int k = 0; k < plan.colorCount; ++k )
+		{
+			for ( int t = tid; t < s_cCount[k]; t += nt )
+				d_laneStageT( P, lanes + s_laneOffset[k] + t, bodies, STAGE_RESTITUTION );
+			cluster.sync();
+		}
 	}
 
 	/* store impulses (contact_solver.c:2238-2331), restore joint body indices, write the
@@ -195,47 +355,36 @@ __global__ void __launch_bounds__( B2G_CLUSTER_THREADS ) k_solveCluster( d_solve
 	for ( int k = 0; k < plan.colorCount; ++k )
 	{
 		int color = plan.colors[k];
+		const int begin = a.colorOffsets[color];
+		const int* mine = plan.assigned + (long long)begin * ranks + (long long)rank * ( a.colorOffsets[color + 1] - begin );
 		for ( int t = tid; t < s_cCount[k]; t += nt )
+			d_storeLane( lanes + s_laneOffset[k] + t, &a.contacts[a.colorIds[mine[t]]].manifold, false );
+		for ( int t = tid; t < s_jCount[k]; t += nt )
 		{
-			int idx = a.colorOffsets[color] + s_cBegin[k] + t;
-			int slot = plan.useLists ? plan.slotList[idx] : idx;
-			d_storeLane( lanes + s_laneOffset[k] + t, &a.contacts[a.colorIds[slot]].manifold, false );
-		}
-		if ( plan.positionOf )
-		{
-			for ( int t = tid; t < s_jCount[k]; t += nt )
-			{
-				int idx = plan.jointOffsets[color] + s_jBegin[k] + t;
-				b2gJoint* J = a.joints + plan.jointList[idx];
-				J->indexA = J->indexA >= 0 ? plan.bodyList[J->indexA] : -1;
-				J->indexB = J->indexB >= 0 ? plan.bodyList[J->indexB] : -1;
-			}
+			b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k] + t];
+			int pa = J->indexA >= 0 ? d_clusterPosition( plan, J->indexA ) : -1;
+			int pb = J->indexB >= 0 ? d_clusterPosition( plan, J->indexB ) : -1;
+			J->indexA = pa >= 0 ? ( plan.bodyList ? plan.bodyList[pa] : pa ) : -1;
+			J->indexB = pb >= 0 ? ( plan.bodyList ? plan.bodyList[pb] : pb ) : -1;
 		}
 	}
 	for ( int s = tid; s < localCount; s += nt )
 	{
-		int p = ( s << plan.rankShift ) + rank;
+		int p = base + s;
 		int ai = plan.bodyList ? plan.bodyList[p] : p;
 		a.sv[ai] = sv[s];
 		a.sd[ai] = sd[s];
 	}
 }
 
-/* shared memory one CTA needs for its share of `counts` contacts per color */
-static size_t clusterSmem( const int* contactCounts, int colorCount, int ranks )
-{
-	size_t lanes = 0;
-	for ( int k = 0; k < colorCount; ++k ) lanes += (size_t)( contactCounts[k] + ranks - 1 ) / ranks;
-	return lanes * sizeof( b2gContactLane );
-}
-
 /* Launch the cluster solver over the active colors. useLists selects the big-component
    lists of `b` (and its big body list); otherwise every constraint and awake body. Returns
    0 when launched, -1 when the constraints do not fit a cluster (the caller then uses the
-   per-color launches), or a CUDA error code. */
+   per-color launches), or a CUDA error code. A CTA given more lanes than it holds (never
+   expected: the host checks the total) sets B2G_STATUS_CAPACITY in *status. */
 extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
-									const int* activeColors, int activeColorCount, int useLists, int bodyCount,
-									cudaStream_t stream, long long* launches )
+									const int* activeColors, int activeColorCount, int useLists, int bodyCount, int* status,
+									long long epoch, cudaStream_t stream, long long* launches )
 {
 	static pthread_mutex_t s_lock = PTHREAD_MUTEX_INITIALIZER;
 	static int s_ranks = -1;
@@ -251,7 +400,7 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 			pthread_mutex_unlock( &s_lock );
 			return -1;
 		}
-		for ( int ranks = 16; ranks >= 8 && s_ranks == 0; ranks /= 2 )
+		for ( int ranks = B2G_CLUSTER_MAX_RANKS; ranks >= 8 && s_ranks == 0; ranks /= 2 )
 		{
 			cudaLaunchConfig_t cfg;
 			memset( &cfg, 0, sizeof( cfg ) );
@@ -272,15 +421,55 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	}
 	int ranks = s_ranks;
 	pthread_mutex_unlock( &s_lock );
-	if ( ranks == 0 ) return -1;
+	if ( ranks == 0 || bodyCount <= 0 ) return -1;
 	int counts[B2_GRAPH_COLOR_COUNT];
+	long long lanesTotal = 0;
 	for ( int k = 0; k < activeColorCount; ++k )
+	{
 		counts[k] = useLists ? b->hSummary->bigContactCount[activeColors[k]]
 							 : a->colorOffsets[activeColors[k] + 1] - a->colorOffsets[activeColors[k]];
-	int rankShift = ranks == 16 ? 4 : 3;
+		lanesTotal += counts[k];
+	}
 	int slotsPerRank = ( bodyCount + ranks - 1 ) / ranks;
-	size_t smem = clusterSmem( counts, activeColorCount, ranks ) + (size_t)slotsPerRank * 2 * sizeof( float4 );
-	if ( smem > B2G_CLUSTER_SMEM_MAX ) return -1;
+	long long laneBytes = (long long)B2G_CLUSTER_SMEM_MAX - (long long)slotsPerRank * 2 * sizeof( float4 );
+	if ( slotsPerRank > 0xffff || laneBytes <= 0 ) return -1;
+	int laneCap = (int)( laneBytes / sizeof( b2gContactLane ) );
+	if ( lanesTotal > (long long)laneCap * ranks ) return -1;
+
+	/* assignment lists: 16 entries per colored slot and colored joint */
+	long long need = (long long)B2G_CLUSTER_MAX_RANKS * ( a->colorOffsets[B2G_OVERFLOW_INDEX] > 0 ? a->colorOffsets[B2G_OVERFLOW_INDEX] : 1 );
+	if ( need > b->clusterCap || b->clusterAssigned == NULL )
+	{
+		long long cap = b->clusterCap > 0 ? b->clusterCap : 1024;
+		while ( cap < need ) cap *= 2;
+		if ( b->clusterAssigned ) cudaFree( b->clusterAssigned );
+		b->clusterAssigned = NULL;
+		b->clusterEpoch = -1;
+		b->clusterCap = 0;
+		cudaError_t e = cudaMalloc( (void**)&b->clusterAssigned, (size_t)cap * sizeof( int ) );
+		if ( e != cudaSuccess ) return (int)e;
+		b->clusterCap = cap;
+	}
+	long long needJ = (long long)B2G_CLUSTER_MAX_RANKS * ( jointOffsets[B2G_OVERFLOW_INDEX] > 0 ? jointOffsets[B2G_OVERFLOW_INDEX] : 1 );
+	if ( needJ > b->clusterJointCap || b->clusterJoints == NULL )
+	{
+		long long cap = b->clusterJointCap > 0 ? b->clusterJointCap : 1024;
+		while ( cap < needJ ) cap *= 2;
+		if ( b->clusterJoints ) cudaFree( b->clusterJoints );
+		b->clusterJoints = NULL;
+		b->clusterEpoch = -1;
+		b->clusterJointCap = 0;
+		cudaError_t e = cudaMalloc( (void**)&b->clusterJoints, (size_t)cap * sizeof( int ) );
+		if ( e != cudaSuccess ) return (int)e;
+		b->clusterJointCap = cap;
+	}
+	if ( b->clusterCounts == NULL )
+	{
+		cudaError_t e = cudaMalloc( (void**)&b->clusterCounts, B2G_CLUSTER_COUNT_WORDS * sizeof( int ) );
+		if ( e != cudaSuccess ) return (int)e;
+		b->clusterEpoch = -1;
+	}
+
 	d_clusterPlan plan;
 	memset( &plan, 0, sizeof( plan ) );
 	plan.colorCount = activeColorCount;
@@ -293,22 +482,66 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	plan.positionOf = useLists ? b->localIndex : NULL;
 	plan.summary = b->summary;
 	plan.bodyCount = bodyCount;
-	plan.rankShift = rankShift;
+	plan.ranks = ranks;
 	plan.slotsPerRank = slotsPerRank;
+	plan.laneCap = laneCap;
+	plan.assigned = b->clusterAssigned;
+	plan.counts = b->clusterCounts;
+	plan.status = status;
+	plan.assignedJoints = b->clusterJoints;
 
-	/* threads per CTA: the largest per-CTA share of one color (joints + contacts), rounded to
-	   warps, so a color phase is one pass and no more warps than needed meet at each barrier */
-	int share = 1;
+	/* threads per CTA: the even share of the largest color (joints + contacts) with a
+	   quarter more for locality, rounded to warps; a color's constraints go to a CTA past its
+	   one-pass share only when every CTA has its share */
+	int share = 1, maxCount = 1;
+	int jointCounts[B2_GRAPH_COLOR_COUNT];
 	for ( int k = 0; k < activeColorCount; ++k )
 	{
 		int color = activeColors[k];
-		int joints = useLists ? b->hSummary->bigJointCount[color] : jointOffsets[color + 1] - jointOffsets[color];
-		int items = ( joints + ranks - 1 ) / ranks + ( counts[k] + ranks - 1 ) / ranks;
+		jointCounts[k] = useLists ? b->hSummary->bigJointCount[color] : jointOffsets[color + 1] - jointOffsets[color];
+		int evenC = ( counts[k] + ranks - 1 ) / ranks, evenJ = ( jointCounts[k] + ranks - 1 ) / ranks;
+		int items = evenC + evenC / 4 + evenJ + evenJ / 4;
 		if ( items > share ) share = items;
+		int range = a->colorOffsets[color + 1] - a->colorOffsets[color];
+		if ( range > maxCount ) maxCount = range;
+		range = jointOffsets[color + 1] - jointOffsets[color];
+		if ( range > maxCount ) maxCount = range;
 	}
 	int threads = ( ( share + 31 ) / 32 ) * 32;
 	if ( threads < 128 ) threads = 128;
 	if ( threads > B2G_CLUSTER_THREADS ) threads = B2G_CLUSTER_THREADS;
+	for ( int k = 0; k < activeColorCount; ++k )
+	{
+		int evenC = ( counts[k] + ranks - 1 ) / ranks, evenJ = ( jointCounts[k] + ranks - 1 ) / ranks;
+		plan.jointCap[k] = evenJ + evenJ / 4;
+		plan.colorCap[k] = threads - plan.jointCap[k] > evenC + evenC / 4 ? threads - plan.jointCap[k] : evenC + evenC / 4;
+		if ( evenC + evenJ > 0 && plan.colorCap[k] + plan.jointCap[k] > threads )
+		{
+			/* the color needs more than one pass anyway: shares in proportion */
+			plan.colorCap[k] = evenC + (int)( (long long)( threads > evenC + evenJ ? threads - evenC - evenJ : 0 ) * evenC / ( evenC + evenJ ) );
+			plan.jointCap[k] = evenJ + ( threads > evenC + evenJ ? threads - evenC - evenJ : 0 ) - ( plan.colorCap[k] - evenC );
+		}
+	}
+
+	/* the assignment holds while the constraint graph, the awake set and the solved body
+	   list are unchanged (the caller's epoch) and the launch shape is the same */
+	bool reuse = epoch >= 0 && b->clusterEpoch == epoch && b->clusterUseLists == useLists && b->clusterBodyCount == bodyCount &&
+				 b->clusterThreads == threads && b->clusterRanks == ranks;
+	if ( reuse == false )
+	{
+		cudaError_t e = cudaMemsetAsync( b->clusterCounts, 0, B2G_CLUSTER_COUNT_WORDS * sizeof( int ), stream );
+		if ( e != cudaSuccess ) return (int)e;
+		dim3 grid( (unsigned)( ( maxCount + 255 ) / 256 ), (unsigned)activeColorCount, 2 );
+		k_clusterAssign<<<grid, 256, 0, stream>>>( *a, plan );
+		*launches += 1;
+		e = cudaGetLastError();
+		if ( e != cudaSuccess ) return (int)e;
+		b->clusterEpoch = epoch;
+		b->clusterUseLists = useLists;
+		b->clusterBodyCount = bodyCount;
+		b->clusterThreads = threads;
+		b->clusterRanks = ranks;
+	}
 
 	cudaLaunchConfig_t cfg;
 	memset( &cfg, 0, sizeof( cfg ) );
@@ -319,7 +552,7 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	attr.val.clusterDim.z = 1;
 	cfg.gridDim = dim3( ranks );
 	cfg.blockDim = dim3( threads );
-	cfg.dynamicSmemBytes = smem > 0 ? smem : 16;
+	cfg.dynamicSmemBytes = B2G_CLUSTER_SMEM_MAX;
 	cfg.stream = stream;
 	cfg.attrs = &attr;
 	cfg.numAttrs = 1;

@@ -548,7 +548,8 @@ extern "C" int b2gDev_CompReserve( b2gCompBuffers* b, int awake, int slots, int 
 extern "C" void b2gDev_CompFree( b2gCompBuffers* b )
 {
 	void* ptrs[] = { b->parent,		 b->compData,	 b->bodyList,	 b->localIndex,	  b->slotList, b->jointList,
-					 b->binRange,	 b->bigBodyList, b->bigSlotList, b->bigJointList, b->summary };
+					 b->binRange,	 b->bigBodyList, b->bigSlotList, b->bigJointList, b->summary,
+					 b->clusterAssigned, b->clusterCounts, b->clusterJoints };
 	for ( size_t i = 0; i < sizeof( ptrs ) / sizeof( ptrs[0] ); ++i )
 		if ( ptrs[i] ) cudaFree( ptrs[i] );
 	if ( b->hSummary ) cudaFreeHost( b->hSummary );

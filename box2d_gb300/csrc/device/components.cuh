@@ -62,6 +62,16 @@ struct b2gCompBuffers
 	/* sizes of the last analysis */
 	int n, total, jointTotal;
 	const int* awakeIndex;
+	/* cluster solver: per color and CTA, the contact slots the CTA solves (16 times the
+	   colored slots), the counters that assign them, an error word */
+	int* clusterAssigned;
+	long long clusterCap;
+	int* clusterJoints; /* the same for joints (16 times the colored joints) */
+	long long clusterJointCap;
+	/* what the lists were assigned for: the caller's epoch and the launch shape */
+	long long clusterEpoch;
+	int clusterUseLists, clusterBodyCount, clusterThreads, clusterRanks;
+	int* clusterCounts;
 };
 
 extern "C" int b2gDev_CompReserve( b2gCompBuffers* b, int awake, int slots, int joints );
@@ -84,10 +94,12 @@ extern "C" int b2gDev_CompSolveBig( b2gCompBuffers* b, const d_solveArgs* a, con
 									cudaStream_t stream, long long* launches );
 
 /* cluster solver (cluster.cu) over every constraint (useLists = 0) or the big-component
-   lists; 0 = launched, -1 = does not fit a cluster, else a CUDA error */
+   lists; 0 = launched, -1 = does not fit a cluster, else a CUDA error. `epoch` changes
+   whenever colors, joints, the awake set or the component lists change (-1: unknown); the
+   assignment of constraints to the cluster's CTAs is reused while it stays the same. */
 extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
-									const int* activeColors, int activeColorCount, int useLists, int bodyCount,
-									cudaStream_t stream, long long* launches );
+									const int* activeColors, int activeColorCount, int useLists, int bodyCount, int* status,
+									long long epoch, cudaStream_t stream, long long* launches );
 
 /* the arguments of the one-CTA world solve, for a batched launch (out may be NULL to get
    the size), and the batched launch itself: CTA r solves the world whose arguments are at

@@ -99,6 +99,7 @@ struct b2gDeviceWorld
 	int compSkip;								   /* steps left before the next component analysis */
 	int compValid;								   /* the component lists match the current constraint graph */
 	int topologyDirty;							   /* colors, joints or the awake set changed since the analysis */
+	long long topologyEpoch;					   /* counts those changes and every component analysis */
 	b2gCompBuffers comp;						   /* component solver scratch */
 	void* persistentScratch;					   /* barrier counter, generation, error, restitution flag */
 	/* bodies by id */
@@ -1054,6 +1055,7 @@ extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const flo
 									 const int* shapeCount, const int* shapeList, int shapeListCount )
 {
 	dw->topologyDirty = 1;
+	dw->topologyEpoch += 1;
 	int cap0 = dw->bodyCap, capOut = 0;
 	CK2( upload( dw, &dw->xf, &cap0, (const float4*)xf, bodyCount, &capOut ) );
 	cap0 = dw->bodyCap;
@@ -1102,6 +1104,7 @@ extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int
 									const float* stateD, const float* params, const float* center0, const float* sleepTime )
 {
 	dw->topologyDirty = 1;
+	dw->topologyEpoch += 1;
 	int cap0 = dw->awakeCap, capOut = 0;
 	CK2( upload( dw, &dw->awakeBodyId, &cap0, awakeBodyId, awakeCount, &capOut ) );
 	cap0 = dw->awakeCap;
@@ -1365,6 +1368,7 @@ extern "C" int b2gDev_WakeBodies( b2gDeviceWorld* dw, int newAwakeCount, const i
 	CK2( ( dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( count ), a ) ) );
 	dw->awakeCount = newAwakeCount;
 	dw->topologyDirty = 1;
+	dw->topologyEpoch += 1;
 	return 0;
 }
 
@@ -1387,6 +1391,7 @@ extern "C" int b2gDev_SleepBodies( b2gDeviceWorld* dw, int newAwakeCount, const 
 	}
 	dw->awakeCount = newAwakeCount;
 	dw->topologyDirty = 1;
+	dw->topologyEpoch += 1;
 	return 0;
 }
 
@@ -1403,6 +1408,7 @@ extern "C" int b2gDev_SetContactsAsleep( b2gDeviceWorld* dw, const int* contactI
 extern "C" int b2gDev_RefreshContactBodies( b2gDeviceWorld* dw )
 {
 	int total = dw->colorOffsets[B2_GRAPH_COLOR_COUNT];
+	dw->topologyEpoch += 1;
 	if ( total <= 0 ) return 0;
 	d_islandOpArgs a = islandArgs( dw, D_ISLAND_REFRESH, total, NULL );
 	return dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( total ), a );
@@ -1438,6 +1444,7 @@ extern "C" int b2gDev_IslandResults( b2gDeviceWorld* dw, const uint32_t** awakeI
 extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const int* offsets, int total )
 {
 	dw->topologyDirty = 1;
+	dw->topologyEpoch += 1;
 	CK2( grow( dw, (void**)&dw->colorIds, &dw->colorIdsCap, total > 0 ? total : 1, sizeof( int ) ) );
 	CK2( uploadTo( dw, dw->colorIds, ids, (size_t)total * sizeof( int ) ) );
 	memcpy( dw->colorOffsets, offsets, sizeof( dw->colorOffsets ) );
@@ -1464,6 +1471,7 @@ extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int
 extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* offsets )
 {
 	dw->topologyDirty = 1;
+	dw->topologyEpoch += 1;
 	CK2( grow( dw, (void**)&dw->joints, &dw->jointCap, count > 0 ? count : 1, sizeof( b2gJoint ) ) );
 	CK2( uploadTo( dw, dw->joints, joints, (size_t)count * sizeof( b2gJoint ) ) );
 	memcpy( dw->jointOffsets, offsets, sizeof( dw->jointOffsets ) );
@@ -2142,6 +2150,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 			int forceBig = ovJointCount0 + ovCount0 > 0;
 			CK2( b2gDev_CompAnalyze( &dw->comp, &a, dw->jointOffsets, dw->awakeIndex, total, jointTotal, forceBig, dw->stream,
 									 &dw->launches ) );
+			dw->topologyEpoch += 1;
 			dw->topologyDirty = 0;
 			dw->compValid = 0;
 		}
@@ -2153,7 +2162,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 			if ( hs->bigComponents > 0 )
 			{
 				int rc = b2gDev_ClusterSolve( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, 1,
-											  hs->bigBodies, dw->stream, &dw->launches );
+											  hs->bigBodies, &dw->counters->status, dw->topologyEpoch, dw->stream, &dw->launches );
 				if ( rc > 0 ) return rc;
 				if ( rc < 0 )
 					CK2( b2gDev_CompSolveBig( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, total,
@@ -2168,7 +2177,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	if ( solved == false && dw->solverMode == B2G_SOLVER_COMPONENTS && ovJointCount0 + ovCount0 == 0 )
 	{
 		int rc = b2gDev_ClusterSolve( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, 0, awakeCount,
-									  dw->stream, &dw->launches );
+									  &dw->counters->status, dw->topologyEpoch, dw->stream, &dw->launches );
 		if ( rc > 0 ) return rc;
 		solved = rc == 0;
 	}
