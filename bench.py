@@ -220,7 +220,7 @@ def run_batch(args) -> dict:
     plain_s = time.perf_counter() - t0
     for s in scenes:
         s.timings(reset=True)
-    prof = np.zeros(12, np.float32)
+    prof = np.zeros(17, np.float32)
     lib.b2p_batch_profile(prof.ctypes.data, 1)
     launches0 = float(prof[5])
     with ClockSampler(0) as clocks:
@@ -235,15 +235,16 @@ def run_batch(args) -> dict:
         d2h += int(traffic[1])
     launches = int(prof[5] - launches0)
     profile = {k: float(v) / args.steps for k, v in
-               zip(["begin", "pairs", "collide", "finish", "flush", "_", "flush_assembly", "flush_wait"], prof) if k != "_"}
+               zip(["begin", "pairs", "collide", "finish", "flush", "_", "flush_assembly", "flush_wait", "_", "_", "_", "_",
+                       "flush_plan", "flush_layout", "flush_stage", "flush_issue", "flush_deliver"], prof) if k != "_"}
     # end to end: the batched step plus every world's move events
-    events = __import__("numpy").zeros((max(s.body_count for s in scenes), 4), "float32")
+    cap = sum(s.body_count for s in scenes)
+    events = np.zeros((cap, 4), np.float32)
     e2e_steps = max(1, min(args.steps, 20))
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         lib.b2s_step_batch(handles, n, dt, 4, 1, threads)
-        for s in scenes:
-            s.move_events(events)
+        lib.b2s_move_events_many(handles, n, events.ctypes.data, cap)
     e2e_s = time.perf_counter() - t0
     for s in scenes:
         s.close()
@@ -302,7 +303,7 @@ def run_diff(args) -> dict:
         forward(warm_steps)
         backward()
     plain_s = forward(args.steps, record=False)
-    prof = np.zeros(12, np.float32)
+    prof = np.zeros(17, np.float32)
     lib.b2p_batch_profile(prof.ctypes.data, 1)
     launches0 = float(prof[5])
     with ClockSampler(0) as clocks:
@@ -311,7 +312,8 @@ def run_diff(args) -> dict:
         bwd_s, gv, gf = backward()
     fwd_launches = int(prof[5] - launches0)
     profile = {k: float(v) / args.steps for k, v in
-               zip(["begin", "pairs", "collide", "finish", "flush", "_", "flush_assembly", "flush_wait"], prof) if k != "_"}
+               zip(["begin", "pairs", "collide", "finish", "flush", "_", "flush_assembly", "flush_wait", "_", "_", "_", "_",
+                       "flush_plan", "flush_layout", "flush_stage", "flush_issue", "flush_deliver"], prof) if k != "_"}
     adj_ms, launches = batch.backward_ms()
     tape_bytes = 0
     for w in range(min(n, 8)):

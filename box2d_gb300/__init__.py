@@ -48,6 +48,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2s_world_id": (c_u32, [c_int]),
         "b2s_get_state": (None, [c_int, c_p]),
         "b2s_move_events": (c_int, [c_int, c_p, c_int]),
+        "b2s_move_events_many": (c_int, [c_p, c_int, c_p, c_int]),
         "b2s_state_hash": (c_u64, [c_int]),
         "b2s_set_velocities": (None, [c_int, c_p]),
         "b2s_target": (None, [c_int, c_p]),

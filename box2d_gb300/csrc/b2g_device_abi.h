@@ -276,6 +276,8 @@ int b2gDev_DownloadAwake( b2gDeviceWorld* dw, int awakeCount, float* stateV, flo
 int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* center, uint32_t* typeFlags );
 /* body transforms (4 floats), centers (2), flags and awake velocities (4) in one wait;
    the pointers refer to page-locked staging valid until the next call */
+/* send the host-mirrored body state down behind the step's work, without waiting */
+int b2gDev_PrefetchState( b2gDeviceWorld* dw, int bodyCount, int awakeCount );
 int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awakeCount, const float** xf, const float** center,
 						  const uint32_t** flags, const float** stateV, const float** sleepTime );
 
@@ -397,6 +399,7 @@ int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on );
 typedef void ( *b2gParallelFor )( void* pool, int count, void ( *fn )( void* ctx, int index ), void* ctx );
 int b2gDev_BatchFlush( b2gDevBatch* batch, b2gDeviceWorld* const* worlds, int count, b2gParallelFor parallelFor, void* pool );
 long long b2gDev_BatchLaunches( b2gDevBatch* batch );
+void b2gDev_BatchPartTimes( b2gDevBatch* b, double* out, int reset );
 void b2gDev_BatchTimes( b2gDevBatch* batch, double* assembleMs, double* waitMs, int reset );
 
 /* bookkeeping for profiles */

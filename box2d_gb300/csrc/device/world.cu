@@ -232,6 +232,9 @@ struct b2gDeviceWorld
 	uint32_t* hFlags;
 	float4* hStateV;
 	int hXfCap, hCenterCap, hFlagsCap, hStateVCap;
+	/* the host mirrors above hold (or will hold after the next wait) the state as of the
+	   last prefetch, and no device work was issued or recorded since */
+	int prefetchValid, prefetchBodies, prefetchAwake;
 	float* hSleepTime;
 	int hSleepTimeCap;
 };
@@ -335,6 +338,7 @@ static long long d_alignArgs( long long x ) { return ( x + 15 ) & ~15LL; }
 /* upload: `src` is copied at once (recorded) or sent from pinned memory (issued) */
 static int dev_h2d( b2gDeviceWorld* dw, void* dst, const void* src, size_t bytes )
 {
+	dw->prefetchValid = 0;
 	if ( bytes == 0 ) return 0;
 	dw->h2dBytes += (long long)bytes;
 	if ( dw->defer )
@@ -375,6 +379,7 @@ static int dev_d2h( b2gDeviceWorld* dw, void* dst, const void* src, size_t bytes
 
 static int dev_memset( b2gDeviceWorld* dw, void* dst, int value, size_t bytes )
 {
+	dw->prefetchValid = 0;
 	if ( dw->defer )
 	{
 		d_deferredOp op;
@@ -393,6 +398,7 @@ template <class Args, void ( *Body )( const Args&, int, int ), int MinBlocks = 1
 static int dev_launch( b2gDeviceWorld* dw, int kernel, int grid, const Args& a )
 {
 	if ( grid <= 0 ) return 0;
+	dw->prefetchValid = 0;
 	dw->launches += 1;
 	if ( dw->defer )
 	{
@@ -1041,6 +1047,7 @@ extern "C" int b2gDev_UploadShapes( b2gDeviceWorld* dw, const b2gShape* shapes, 
 
 template <typename T> static int upload( b2gDeviceWorld* dw, T** dptr, int* cap, const T* src, int n, int* capOut )
 {
+	dw->prefetchValid = 0;
 	int c = *cap;
 	CK2( grow( dw, (void**)dptr, &c, n, sizeof( T ) ) );
 	*capOut = c;
@@ -1144,6 +1151,18 @@ static int drain( b2gDeviceWorld* dw );
 extern "C" int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awakeCount, const float** xf, const float** center,
 									 const uint32_t** flags, const float** stateV, const float** sleepTime )
 {
+	if ( dw->prefetchValid && dw->prefetchBodies == bodyCount && dw->prefetchAwake == awakeCount )
+	{
+		/* the step already sent the state down: wait for it */
+		dw->prefetchValid = 0;
+		CK2( drain( dw ) );
+		*xf = (const float*)dw->hXf;
+		*center = (const float*)dw->hCenter;
+		*flags = dw->hFlags;
+		*stateV = (const float*)dw->hStateV;
+		*sleepTime = dw->hSleepTime;
+		return 0;
+	}
 	int nb = bodyCount > 0 ? bodyCount : 1, na = awakeCount > 0 ? awakeCount : 1;
 	CK2( growHost( (void**)&dw->hSleepTime, &dw->hSleepTimeCap, na, sizeof( float ) ) );
 	CK2( growHost( (void**)&dw->hXf, &dw->hXfCap, nb, sizeof( float4 ) ) );
@@ -1171,6 +1190,35 @@ extern "C" int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awak
 	return 0;
 }
 
+/* Send the body state the host mirrors hold (transforms, centers and flags of all bodies,
+   velocities and sleep times of the awake set) down behind the step's work without waiting:
+   the step's move events and body getters then cost one wait instead of a round trip. In a
+   batched step the copies are recorded and land with the last flush. */
+extern "C" int b2gDev_PrefetchState( b2gDeviceWorld* dw, int bodyCount, int awakeCount )
+{
+	int nb = bodyCount > 0 ? bodyCount : 1, na = awakeCount > 0 ? awakeCount : 1;
+	CK2( growHost( (void**)&dw->hSleepTime, &dw->hSleepTimeCap, na, sizeof( float ) ) );
+	CK2( growHost( (void**)&dw->hXf, &dw->hXfCap, nb, sizeof( float4 ) ) );
+	CK2( growHost( (void**)&dw->hCenter, &dw->hCenterCap, nb, sizeof( float2 ) ) );
+	CK2( growHost( (void**)&dw->hFlags, &dw->hFlagsCap, nb, sizeof( uint32_t ) ) );
+	CK2( growHost( (void**)&dw->hStateV, &dw->hStateVCap, na, sizeof( float4 ) ) );
+	if ( bodyCount > 0 )
+	{
+		CK2( dev_d2h( dw, dw->hXf, dw->xf, (size_t)bodyCount * sizeof( float4 ) ) );
+		CK2( dev_d2h( dw, dw->hCenter, dw->center, (size_t)bodyCount * sizeof( float2 ) ) );
+		CK2( dev_d2h( dw, dw->hFlags, dw->bodyFlags, (size_t)bodyCount * sizeof( uint32_t ) ) );
+	}
+	if ( awakeCount > 0 )
+	{
+		CK2( dev_d2h( dw, dw->hStateV, dw->stateV, (size_t)awakeCount * sizeof( float4 ) ) );
+		CK2( dev_d2h( dw, dw->hSleepTime, dw->sleepTime, (size_t)awakeCount * sizeof( float ) ) );
+	}
+	dw->prefetchValid = 1;
+	dw->prefetchBodies = bodyCount;
+	dw->prefetchAwake = awakeCount;
+	return 0;
+}
+
 extern "C" int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* center, uint32_t* flags )
 {
 	if ( bodyCount == 0 ) return 0;
@@ -1192,6 +1240,7 @@ extern "C" int b2gDev_DownloadShapeBoxes( b2gDeviceWorld* dw, int shapeCount, fl
 
 extern "C" int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float vx, float vy, float w, int which )
 {
+	dw->prefetchValid = 0;
 	k_setVelocity<<<1, 1, 0, dw->stream>>>( dw->stateV, awakeIndex, vx, vy, w, which );
 	dw->launches += 1;
 	return (int)cudaGetLastError();
@@ -2467,14 +2516,28 @@ __global__ void k_batchCopy( const d_copyOp* __restrict__ ops, int count, const 
 	}
 }
 
+/* A world's part of a flush. Its records split into units -- a run of consecutive uploads,
+   a run of consecutive downloads, or one other record -- and unit l of every world runs in
+   level l of the replay. `slot` is where unit l sits in its level's table (the first copy,
+   the kernel record or the one-CTA solve), `blockBase` a kernel unit's first block. */
+struct d_worldFlush
+{
+	std::vector<int> unitEnd;
+	std::vector<long long> downAt; /* per record: download offset within the world's part */
+	std::vector<long long> slot;
+	std::vector<int> blockBase;
+	long long upBase, argBase, downBase, downBytes;
+};
+
 struct b2gDevBatch
 {
 	cudaStream_t stream;
 	unsigned char *hBlob, *dBlob, *hDown, *dDown;
 	long long blobCap, downCap;
-	std::vector<unsigned char> blob;
+	std::vector<d_worldFlush> plans; /* per world, reused across flushes */
 	long long launches;
 	double assembleMs, waitMs;
+	double partMs[5]; /* plan, layout, stage, issue, deliver */
 };
 
 static double d_nowMs( void )
@@ -2482,6 +2545,15 @@ static double d_nowMs( void )
 	struct timespec ts;
 	clock_gettime( CLOCK_MONOTONIC, &ts );
 	return ts.tv_sec * 1e3 + ts.tv_nsec * 1e-6;
+}
+
+extern "C" void b2gDev_BatchPartTimes( b2gDevBatch* b, double* out, int reset )
+{
+	for ( int k = 0; k < 5; ++k )
+	{
+		out[k] = b->partMs[k];
+		if ( reset ) b->partMs[k] = 0.0;
+	}
 }
 
 extern "C" void b2gDev_BatchTimes( b2gDevBatch* b, double* assembleMs, double* waitMs, int reset )
@@ -2557,14 +2629,6 @@ struct d_levelPlan
 	int smem;											  /* largest one-CTA world solve */
 };
 
-template <class T> static long long d_blobPush( std::vector<unsigned char>& blob, const T* items, long long count )
-{
-	long long at = d_alignArgs( (long long)blob.size() );
-	blob.resize( (size_t)( at + count * (long long)sizeof( T ) ) );
-	if ( count > 0 ) memcpy( blob.data() + at, items, (size_t)count * sizeof( T ) );
-	return at;
-}
-
 template <class Args, void ( *Body )( const Args&, int, int ), int MinBlocks>
 static int d_launchBatched( b2gDevBatch* b, const d_levelPlan& L, int kind )
 {
@@ -2575,37 +2639,128 @@ static int d_launchBatched( b2gDevBatch* b, const d_levelPlan& L, int kind )
 	return (int)cudaGetLastError();
 }
 
-/* replay the recorded work of `n` worlds: every world's records run in order; records of
-   different worlds at the same position run in one launch per kind. One upload, one
-   download and one wait in all. */
-struct d_flushCopy
+struct d_flushCtx
 {
 	b2gDevBatch* b;
 	b2gDeviceWorld* const* worlds;
-	const long long* upBase;
-	const long long* argBase;
-	const std::vector<long long>* downAt;
+	d_worldFlush* plan;
+	const d_levelPlan* levels;
 };
 
-/* world w's upload bytes and kernel arguments into the pinned staging */
-static void d_stageWorld( void* ctx, int w )
+static bool d_isCopy( int kind ) { return kind != D_OP_KERNEL; }
+
+/* pass 1, per world: units and download layout */
+static void d_planWorld( void* ctx, int w )
 {
-	const d_flushCopy* c = (const d_flushCopy*)ctx;
+	const d_flushCtx* c = (const d_flushCtx*)ctx;
+	d_worldFlush& P = c->plan[w];
+	P.unitEnd.clear();
+	P.downBytes = 0;
 	const d_deferred* d = c->worlds[w]->defer;
 	if ( d == NULL ) return;
-	if ( d->up.size() > 0 ) memcpy( c->b->hBlob + c->upBase[w], d->up.data(), d->up.size() );
-	if ( d->args.size() > 0 ) memcpy( c->b->hBlob + c->argBase[w], d->args.data(), d->args.size() );
+	int count = (int)d->ops.size();
+	P.downAt.assign( (size_t)count, -1 );
+	for ( int i = 0; i < count; )
+	{
+		int k = d->ops[i].kind;
+		int j = i + 1;
+		if ( k == D_OP_H2D || k == D_OP_D2H )
+			while ( j < count && d->ops[j].kind == k ) ++j;
+		P.unitEnd.push_back( j );
+		i = j;
+	}
+	for ( int i = 0; i < count; ++i )
+	{
+		if ( d->ops[i].kind != D_OP_D2H ) continue;
+		P.downAt[i] = P.downBytes;
+		P.downBytes = d_alignArgs( P.downBytes + d->ops[i].bytes );
+	}
+	P.slot.assign( P.unitEnd.size(), 0 );
+	P.blockBase.assign( P.unitEnd.size(), 0 );
+}
+
+/* pass 2, per world: upload bytes and kernel arguments into the pinned staging, and the
+   world's entries of every level's copy and record tables */
+static void d_stageWorld( void* ctx, int w )
+{
+	const d_flushCtx* c = (const d_flushCtx*)ctx;
+	const d_worldFlush& P = c->plan[w];
+	const d_deferred* d = c->worlds[w]->defer;
+	if ( d == NULL ) return;
+	unsigned char* h = c->b->hBlob;
+	if ( d->up.size() > 0 ) memcpy( h + P.upBase, d->up.data(), d->up.size() );
+	if ( d->args.size() > 0 ) memcpy( h + P.argBase, d->args.data(), d->args.size() );
+	int begin = 0;
+	for ( size_t l = 0; l < P.unitEnd.size(); ++l )
+	{
+		const d_levelPlan& L = c->levels[l];
+		int end = P.unitEnd[l];
+		if ( d_isCopy( d->ops[begin].kind ) )
+		{
+			d_copyOp* table = (d_copyOp*)( h + L.copies ) + P.slot[l];
+			for ( int i = begin; i < end; ++i )
+			{
+				const d_deferredOp& op = d->ops[(size_t)i];
+				d_copyOp cp;
+				cp.value = -1;
+				cp.fromStaging = 0;
+				cp.bytes = op.bytes;
+				if ( op.kind == D_OP_H2D )
+				{
+					cp.dst = (unsigned char*)op.dev;
+					cp.src = (const unsigned char*)(uintptr_t)( P.upBase + op.at );
+					cp.fromStaging = 1;
+				}
+				else if ( op.kind == D_OP_D2D )
+				{
+					cp.dst = (unsigned char*)op.dev;
+					cp.src = (const unsigned char*)op.host;
+				}
+				else if ( op.kind == D_OP_D2H )
+				{
+					cp.dst = c->b->dDown + P.downBase + P.downAt[(size_t)i];
+					cp.src = (const unsigned char*)op.dev;
+				}
+				else
+				{
+					cp.dst = (unsigned char*)op.dev;
+					cp.src = NULL;
+					cp.value = op.value & 0xff;
+				}
+				table[i - begin] = cp;
+			}
+		}
+		else
+		{
+			const d_deferredOp& op = d->ops[(size_t)begin];
+			if ( op.kernel == DK_SOLVE_BIN )
+			{
+				( (long long*)( h + L.recs[DK_SOLVE_BIN] ) )[P.slot[l]] = P.argBase + op.at;
+			}
+			else
+			{
+				d_batchRec r;
+				r.args = P.argBase + op.at;
+				r.blockBase = P.blockBase[l];
+				r.blocks = op.grid;
+				( (d_batchRec*)( h + L.recs[op.kernel] ) )[P.slot[l]] = r;
+			}
+		}
+		begin = end;
+	}
 }
 
 /* world w's downloads to where its records asked, then its records are spent */
 static void d_deliverWorld( void* ctx, int w )
 {
-	const d_flushCopy* c = (const d_flushCopy*)ctx;
+	const d_flushCtx* c = (const d_flushCtx*)ctx;
 	b2gDeviceWorld* dw = c->worlds[w];
 	d_deferred* d = dw->defer;
 	if ( d == NULL ) return;
+	const d_worldFlush& P = c->plan[w];
 	for ( size_t i = 0; i < d->ops.size(); ++i )
-		if ( d->ops[i].kind == D_OP_D2H ) memcpy( d->ops[i].host, c->b->hDown + c->downAt[w][i], (size_t)d->ops[i].bytes );
+		if ( d->ops[i].kind == D_OP_D2H )
+			memcpy( d->ops[i].host, c->b->hDown + P.downBase + P.downAt[i], (size_t)d->ops[i].bytes );
 	d->ops.clear();
 	d->up.clear();
 	d->args.clear();
@@ -2620,154 +2775,92 @@ static void d_serialFor( void* pool, int count, void ( *fn )( void*, int ), void
 
 /* replay the recorded work of `n` worlds: every world's records run in order; records of
    different worlds at the same position run in one launch per kind. One upload, one
-   download and one wait in all. `pf` runs the per-world staging and delivery copies on the
-   caller's threads (NULL: serially). */
+   download and one wait in all. `pf` runs the per-world planning, staging and delivery on
+   the caller's threads (NULL: serially); only the table layout is serial. */
 extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds, int n, b2gParallelFor pf, void* pool )
 {
 	if ( pf == NULL ) pf = d_serialFor;
 	double t0 = d_nowMs();
-	/* units: a run of consecutive uploads, a run of consecutive downloads, or one other record */
-	std::vector<std::vector<std::pair<int, int>>> units( (size_t)n );
+	if ( b->plans.size() < (size_t)n ) b->plans.resize( (size_t)n );
+	d_worldFlush* plan = b->plans.data();
+	d_flushCtx fc = { b, worlds, plan, NULL };
+	pf( pool, n, d_planWorld, &fc );
+	double tPlan = d_nowMs();
+	b->partMs[0] += tPlan - t0;
+	/* staging layout: every world's upload bytes and kernel arguments, then the tables;
+	   download layout */
 	size_t levels = 0;
+	long long at = 0, down = 0;
 	for ( int w = 0; w < n; ++w )
 	{
 		const d_deferred* d = worlds[w]->defer;
+		d_worldFlush& P = plan[w];
+		P.upBase = P.argBase = P.downBase = 0;
 		if ( d == NULL ) continue;
-		int count = (int)d->ops.size();
-		for ( int i = 0; i < count; )
-		{
-			int k = d->ops[i].kind;
-			int j = i + 1;
-			if ( k == D_OP_H2D || k == D_OP_D2H )
-				while ( j < count && d->ops[j].kind == k ) ++j;
-			units[w].push_back( std::make_pair( i, j ) );
-			i = j;
-		}
-		levels = units[w].size() > levels ? units[w].size() : levels;
+		levels = P.unitEnd.size() > levels ? P.unitEnd.size() : levels;
+		P.upBase = at;
+		at = d_alignArgs( at + (long long)d->up.size() );
+		P.argBase = at;
+		at = d_alignArgs( at + (long long)d->args.size() );
+		P.downBase = down;
+		down += P.downBytes;
 	}
 	if ( levels == 0 ) return 0;
-	/* staging layout: every world's upload bytes and kernel arguments, then the tables */
-	std::vector<long long> upBase( (size_t)n, 0 ), argBase( (size_t)n, 0 );
-	long long at = 0;
-	for ( int w = 0; w < n; ++w )
-	{
-		const d_deferred* d = worlds[w]->defer;
-		if ( d == NULL ) continue;
-		upBase[w] = at;
-		at = d_alignArgs( at + (long long)d->up.size() );
-		argBase[w] = at;
-		at = d_alignArgs( at + (long long)d->args.size() );
-	}
 	const long long tableBase = at;
-	/* download layout */
-	long long down = 0;
-	std::vector<std::vector<long long>> downAt( (size_t)n );
+	CK2( d_reserve( &b->hDown, &b->dDown, &b->downCap, down > 0 ? down : 16 ) );
+	/* each world's place in every level's tables, in world order (kernel records stay
+	   sorted by their first block) */
+	std::vector<d_levelPlan> plans( levels );
+	for ( size_t l = 0; l < levels; ++l ) memset( &plans[l], 0, sizeof( d_levelPlan ) );
 	for ( int w = 0; w < n; ++w )
 	{
 		const d_deferred* d = worlds[w]->defer;
 		if ( d == NULL ) continue;
-		downAt[w].assign( d->ops.size(), -1 );
-		for ( size_t i = 0; i < d->ops.size(); ++i )
+		d_worldFlush& P = plan[w];
+		int begin = 0;
+		for ( size_t l = 0; l < P.unitEnd.size(); ++l )
 		{
-			if ( d->ops[i].kind != D_OP_D2H ) continue;
-			downAt[w][i] = down;
-			down = d_alignArgs( down + d->ops[i].bytes );
-		}
-	}
-	CK2( d_reserve( &b->hDown, &b->dDown, &b->downCap, down > 0 ? down : 16 ) );
-	/* the level tables (offsets relative to the staging base) */
-	std::vector<unsigned char>& blob = b->blob;
-	blob.clear();
-	std::vector<d_levelPlan> plans( levels );
-	std::vector<d_copyOp> copies;
-	std::vector<d_batchRec> recs[DK_COUNT];
-	std::vector<long long> binOffsets;
-	for ( size_t l = 0; l < levels; ++l )
-	{
-		d_levelPlan& L = plans[l];
-		memset( &L, 0, sizeof( L ) );
-		copies.clear();
-		for ( int k = 0; k < DK_COUNT; ++k ) recs[k].clear();
-		binOffsets.clear();
-		for ( int w = 0; w < n; ++w )
-		{
-			const d_deferred* d = worlds[w]->defer;
-			if ( d == NULL || l >= units[w].size() ) continue;
-			for ( int i = units[w][l].first; i < units[w][l].second; ++i )
+			d_levelPlan& L = plans[l];
+			const d_deferredOp& op = d->ops[(size_t)begin];
+			if ( d_isCopy( op.kind ) )
 			{
-				const d_deferredOp& op = d->ops[(size_t)i];
-				d_copyOp c;
-				c.value = -1;
-				c.fromStaging = 0;
-				c.bytes = op.bytes;
-				switch ( op.kind )
-				{
-					case D_OP_H2D:
-						c.dst = (unsigned char*)op.dev;
-						c.src = (const unsigned char*)(uintptr_t)( upBase[w] + op.at );
-						c.fromStaging = 1;
-						copies.push_back( c );
-						break;
-					case D_OP_D2D:
-						c.dst = (unsigned char*)op.dev;
-						c.src = (const unsigned char*)op.host;
-						copies.push_back( c );
-						break;
-					case D_OP_D2H:
-						c.dst = b->dDown + downAt[w][(size_t)i];
-						c.src = (const unsigned char*)op.dev;
-						copies.push_back( c );
-						break;
-					case D_OP_MEMSET:
-						c.dst = (unsigned char*)op.dev;
-						c.src = NULL;
-						c.value = op.value & 0xff;
-						copies.push_back( c );
-						break;
-					default:
-					{
-						int k = op.kernel;
-						if ( k == DK_SOLVE_BIN )
-						{
-							binOffsets.push_back( argBase[w] + op.at );
-							L.smem = op.smem > L.smem ? op.smem : L.smem;
-						}
-						else
-						{
-							d_batchRec r;
-							r.args = argBase[w] + op.at;
-							r.blockBase = L.blocks[k];
-							r.blocks = op.grid;
-							recs[k].push_back( r );
-							L.blocks[k] += op.grid;
-						}
-						break;
-					}
-				}
+				P.slot[l] = L.copyCount;
+				L.copyCount += P.unitEnd[l] - begin;
 			}
-		}
-		L.copyCount = (long long)copies.size();
-		L.copies = tableBase + d_blobPush( blob, copies.data(), L.copyCount );
-		for ( int k = 0; k < DK_COUNT; ++k )
-		{
-			if ( k == DK_SOLVE_BIN )
+			else if ( op.kernel == DK_SOLVE_BIN )
 			{
-				L.recCount[k] = (long long)binOffsets.size();
-				L.recs[k] = tableBase + d_blobPush( blob, binOffsets.data(), L.recCount[k] );
+				P.slot[l] = L.recCount[DK_SOLVE_BIN]++;
+				L.smem = op.smem > L.smem ? op.smem : L.smem;
 			}
 			else
 			{
-				L.recCount[k] = (long long)recs[k].size();
-				L.recs[k] = tableBase + d_blobPush( blob, recs[k].data(), L.recCount[k] );
+				P.slot[l] = L.recCount[op.kernel]++;
+				P.blockBase[l] = L.blocks[op.kernel];
+				L.blocks[op.kernel] += op.grid;
 			}
+			begin = P.unitEnd[l];
 		}
 	}
-	long long total = tableBase + (long long)blob.size();
+	long long total = tableBase;
+	for ( size_t l = 0; l < levels; ++l )
+	{
+		d_levelPlan& L = plans[l];
+		L.copies = total;
+		total = d_alignArgs( total + L.copyCount * (long long)sizeof( d_copyOp ) );
+		for ( int k = 0; k < DK_COUNT; ++k )
+		{
+			L.recs[k] = total;
+			long long entry = k == DK_SOLVE_BIN ? (long long)sizeof( long long ) : (long long)sizeof( d_batchRec );
+			total = d_alignArgs( total + L.recCount[k] * entry );
+		}
+	}
 	CK2( d_reserve( &b->hBlob, &b->dBlob, &b->blobCap, total ) );
-	d_flushCopy fc = { b, worlds, upBase.data(), argBase.data(), downAt.data() };
+	fc.levels = plans.data();
+	double tLayout = d_nowMs();
+	b->partMs[1] += tLayout - tPlan;
 	pf( pool, n, d_stageWorld, &fc );
-	memcpy( b->hBlob + tableBase, blob.data(), blob.size() );
 	double t1 = d_nowMs();
+	b->partMs[2] += t1 - tLayout;
 	b->assembleMs += t1 - t0;
 	CK( cudaMemcpyAsync( b->dBlob, b->hBlob, (size_t)total, cudaMemcpyHostToDevice, b->stream ) );
 	for ( size_t l = 0; l < levels; ++l )
@@ -2798,9 +2891,13 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 		}
 	}
 	if ( down > 0 ) CK( cudaMemcpyAsync( b->hDown, b->dDown, (size_t)down, cudaMemcpyDeviceToHost, b->stream ) );
+	double tIssue = d_nowMs();
+	b->partMs[3] += tIssue - t1;
 	CK( cudaStreamSynchronize( b->stream ) );
-	b->waitMs += d_nowMs() - t1;
+	double tWait = d_nowMs();
+	b->waitMs += tWait - t1;
 	pf( pool, n, d_deliverWorld, &fc );
+	b->partMs[4] += d_nowMs() - tWait;
 	for ( int w = 0; w < n; ++w )
 	{
 		b2gDeviceWorld* dw = worlds[w];

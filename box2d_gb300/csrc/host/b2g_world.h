@@ -186,6 +186,12 @@ typedef struct h_world
 	b2gDeviceWorld* dev;
 	int devReady;			/* device arrays hold the current world */
 	int hostStateValid;		/* host body transforms/velocities match the device */
+	/* the device's state arrays as downloaded after the last step (valid until the next
+	   step's end): transforms and centers by body id, velocities and sleep times by awake
+	   index */
+	int mirrorValid;
+	const float *mirrorXf, *mirrorCenter, *mirrorV, *mirrorSleep;
+	const uint32_t* mirrorFlags;
 	int jointsHostValid;	/* host joint records (impulses) match the device */
 	int moveEventsValid;	/* move event array matches the last step */
 	int colorsDirty, jointsDirty;

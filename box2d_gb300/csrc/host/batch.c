@@ -250,7 +250,9 @@ void b2World_StepBatch( const b2WorldId* worldIds, int worldCount, float timeSte
 
 /* milliseconds spent by batched stepping since the last reset: begin, pairs, collide and
    finish phases (host), flushes (host assembly, copies and device work); out[5] = kernels
-   launched by flushes since the library loaded */
+   launched by flushes since the library loaded; out[6..7] flush assembly and wait, out[8..11]
+   thread-time of the four phases, out[12..16] the flush's planning, layout, staging, issue
+   and delivery (17 floats) */
 __attribute__( ( visibility( "default" ) ) ) void b2p_batch_profile( float* out, int reset )
 {
 	pthread_mutex_lock( &h_batchMu );
@@ -261,6 +263,9 @@ __attribute__( ( visibility( "default" ) ) ) void b2p_batch_profile( float* out,
 	out[6] = (float)assembleMs;
 	out[7] = (float)waitMs;
 	for ( int k = 0; k < 4; ++k ) out[8 + k] = (float)( 1e-3 * (double)atomic_load( &h_phaseThreadUs[k] ) );
+	double parts[5] = { 0.0, 0.0, 0.0, 0.0, 0.0 };
+	if ( h_batchDevice ) b2gDev_BatchPartTimes( h_batchDevice, parts, reset );
+	for ( int k = 0; k < 5; ++k ) out[12 + k] = (float)parts[k];
 	if ( reset )
 	{
 		for ( int k = 0; k < 5; ++k ) h_batchMs[k] = 0.0;

@@ -424,6 +424,9 @@ int h_stepBegin( h_world* w, float timeStep, int subStepCount )
 	/* contacts whose solver set the API changed since the last step */
 	w->wokeInStep = 0;
 	h_flushSleepOps( w );
+	/* from here on the device state moves on: host copies read before the step are stale */
+	w->hostStateValid = 0;
+	w->mirrorValid = 0;
 
 	b2gStepParams* p = &w->stepParams;
 	memset( p, 0, sizeof( *p ) );
@@ -576,7 +579,16 @@ void h_stepFinish( h_world* w )
 	if ( w->stepTimeStep > 0.0f ) w->profile.solve = h_ms( w->stepT0 );
 	h_joinRebuild( w );
 	w->hostStateValid = 0;
+	w->mirrorValid = 0;
 	w->jointsHostValid = 0;
+	/* the step's body state follows its work down, so move events and body getters wait
+	   for it instead of asking for it (physics_world.c:863-867 makes move events part of
+	   the step's output) */
+	if ( w->devReady )
+	{
+		int rc = b2gDev_PrefetchState( w->dev, w->bodies.count, w->awakeBodyIds.count );
+		if ( rc != 0 ) h_fail( w, "state prefetch", rc );
+	}
 	w->profile.step = h_ms( w->stepTicks );
 	w->endEventArrayIndex = 1 - w->endEventArrayIndex;
 	w->endEvents[w->endEventArrayIndex].count = 0;

@@ -339,9 +339,24 @@ b2BodyEvents b2World_GetBodyEvents( b2WorldId worldId )
 /* materialize the move events of the last step from the device state: one per body of
    the awake set as the finalize saw it (solver.c:608-622); the sleep pass builds them
    before it moves bodies out of the awake set */
+static void h_fetchMirror( h_world* w )
+{
+	if ( w->mirrorValid ) return;
+	int rc = b2gDev_DownloadState( w->dev, w->bodies.count, w->awakeBodyIds.count, &w->mirrorXf, &w->mirrorCenter,
+								   &w->mirrorFlags, &w->mirrorV, &w->mirrorSleep );
+	if ( rc != 0 ) h_fail( w, "device download", rc );
+	w->mirrorValid = 1;
+}
+
 void h_buildMoveEvents( h_world* w )
 {
-	h_syncFromDevice( w );
+	/* transforms straight from the downloaded state when the host bodies are stale */
+	const float* xf = NULL;
+	if ( w->hostStateValid == 0 && w->devReady )
+	{
+		h_fetchMirror( w );
+		xf = w->mirrorXf;
+	}
 	int n = w->awakeBodyIds.count;
 	h_reserve( w->moveEvents, n );
 	w->moveEvents.count = n;
@@ -349,7 +364,17 @@ void h_buildMoveEvents( h_world* w )
 	{
 		h_body* b = w->bodies.data + w->awakeBodyIds.data[i];
 		b2BodyMoveEvent* ev = w->moveEvents.data + i;
-		ev->transform = b->transform;
+		if ( xf != NULL )
+		{
+			const float* x = xf + 4 * b->id;
+			ev->transform.p = h_v( x[0], x[1] );
+			ev->transform.q.c = x[2];
+			ev->transform.q.s = x[3];
+		}
+		else
+		{
+			ev->transform = b->transform;
+		}
 		ev->bodyId.index1 = b->id + 1;
 		ev->bodyId.world0 = w->worldId;
 		ev->bodyId.generation = b->generation;
@@ -383,10 +408,9 @@ void h_syncFromDevice( h_world* w )
 	if ( w->hostStateValid || w->devReady == 0 ) return;
 	int nb = w->bodies.count;
 	int na = w->awakeBodyIds.count;
-	const float *xf = NULL, *center = NULL, *sv = NULL, *sleepTime = NULL;
-	const uint32_t* typeFlags = NULL;
-	int rc = b2gDev_DownloadState( w->dev, nb, na, &xf, &center, &typeFlags, &sv, &sleepTime );
-	if ( rc != 0 ) h_fail( w, "device download", rc );
+	h_fetchMirror( w );
+	const float *xf = w->mirrorXf, *center = w->mirrorCenter, *sv = w->mirrorV, *sleepTime = w->mirrorSleep;
+	const uint32_t* typeFlags = w->mirrorFlags;
 	for ( int i = 0; i < nb; ++i )
 	{
 		h_body* b = w->bodies.data + i;

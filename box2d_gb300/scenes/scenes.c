@@ -955,6 +955,27 @@ B2S_EXPORT int b2s_move_events( int handle, float* out, int capacity )
 	return ev.moveCount;
 }
 
+/* the move events of `count` scenes after a batched step, one world after the other
+   through b2World_GetBodyEvents, as a C program stepping a batch reads them; 4 floats per
+   event up to `capacity` events in all; returns the event count */
+B2S_EXPORT int b2s_move_events_many( const int* handles, int count, float* out, int capacity )
+{
+	int total = 0;
+	for ( int k = 0; k < count; ++k )
+	{
+		b2BodyEvents ev = b2World_GetBodyEvents( b2s_scenes[handles[k]].worldId );
+		for ( int i = 0; i < ev.moveCount && total < capacity; ++i, ++total )
+		{
+			b2Transform xf = ev.moveEvents[i].transform;
+			out[4 * total] = xf.p.x;
+			out[4 * total + 1] = xf.p.y;
+			out[4 * total + 2] = xf.q.c;
+			out[4 * total + 3] = xf.q.s;
+		}
+	}
+	return total;
+}
+
 B2S_EXPORT void b2s_get_state( int h, float* out )
 {
 	b2sScene* s = b2s_scenes + h;

@@ -54,7 +54,8 @@ void* b2p_stream( uint32_t packedWorldId );
    the begin, pairs, collide and finish phases on the host threads, out[4] the flushes;
    out[5] the kernels the flushes launched since the library loaded; out[6], out[7] the
    flushes' host assembly and their wait for the device; out[8..11] the four phases' thread
-   time summed over worlds (12 floats). */
+   time summed over worlds; out[12..16] the flushes' planning, table layout, staging, issue
+   and delivery (17 floats). */
 void b2p_batch_profile( float* out, int reset );
 
 /* Continuous collision of one world since its creation: out[0] = fast non-bullet bodies
@@ -82,6 +83,9 @@ void b2s_get_state( int handle, float* out );
 /* the last step's body move events (b2World_GetBodyEvents), 4 floats per event:
    p.x, p.y, q.c, q.s, up to capacity; returns the event count */
 int b2s_move_events( int handle, float* out, int capacity );
+/* the same for `count` scenes, their events one after the other (capacity events in all);
+   returns the event count */
+int b2s_move_events_many( const int* handles, int count, float* out, int capacity );
 /* FNV-1a 64 over the bit patterns of b2s_get_state */
 uint64_t b2s_state_hash( int handle );
 void b2s_set_velocities( int handle, const float* in );

@@ -37,6 +37,25 @@ def test_batch_step_equals_single_steps(gpu_lib, threads):
             s.close()
 
 
+def test_move_events_of_a_batch(gpu_lib):
+    """The move events read for a whole batch are each world's events in turn."""
+    import numpy as np
+
+    batch = _scenes(gpu_lib, list(range(301, 309)))
+    try:
+        handles = (ctypes.c_int * len(batch))(*[s.handle for s in batch])
+        gpu_lib.b2s_step_batch(handles, len(batch), 1.0 / 60.0, 4, 5, 4)
+        cap = sum(s.body_count for s in batch)
+        many = np.zeros((cap, 4), np.float32)
+        n = gpu_lib.b2s_move_events_many(handles, len(batch), many.ctypes.data, cap)
+        each = np.concatenate([s.move_events().copy() for s in batch])
+        assert n == len(each) > 0
+        assert (many[:n] == each).all()
+    finally:
+        for s in batch:
+            s.close()
+
+
 def test_batch_worlds_match_oracle(gpu_lib, oracle):
     for seed in (12345, 12346):
         lockstep(gpu_lib, oracle, B.BATCH_WORLD, 0, 0, 0, seed, B.NO_CONTINUOUS, 120)
