@@ -30,6 +30,7 @@ SHAPE_ZOO = 8
 JOINT_ZOO = 9
 FALLING_HINGES = 10
 SLEEP_PYRAMIDS = 11
+JOINT_MIX = 12
 
 NO_CONTINUOUS = 1
 NO_WARM_STARTING = 2

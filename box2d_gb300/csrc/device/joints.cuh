@@ -2,7 +2,8 @@
  * Device joint solvers: prepare / warm start / solve per joint, one thread per joint of a
  * graph color, with the reference's operation order: revolute_joint.c:217-500,
  * prismatic_joint.c:295-667, weld_joint.c:148-454 (non-block solver), wheel_joint.c:197-525,
- * distance_joint.c:250-543. The parameter slots of b2gJoint are documented in host/joint.c.
+ * distance_joint.c:250-543, motor_joint.c:180-436 and pogo_joint.c:98-281. The parameter slots
+ * of b2gJoint are documented in host/joint.c.
  */
 #pragma once
 
@@ -906,6 +907,244 @@ template <class TBodies> static __device__ void d_solveDistance( b2gJoint* j, TB
 	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
 }
 
+/* ---- motor (motor_joint.c:180-436)
+   p: linearVelocity (2), maxVelocityForce, angularVelocity, maxVelocityTorque, linearHertz,
+      linearDampingRatio, maxSpringForce, angularHertz, angularDampingRatio, maxSpringTorque,
+      angular spring softness (3, written by prepare)
+   s: linearVelocityImpulse (2), angularVelocityImpulse, linearSpringImpulse (2),
+      angularSpringImpulse, linearMass (b2Mat22 cx, cy), angularMass, linear spring softness (3) ---- */
+static __device__ __forceinline__ void d_motorLinearMass( b2gJoint* j, float mA, float mB, float iA, float iB, b2Vec2 rA, b2Vec2 rB )
+{
+	/* math_functions.h b2GetInverse22 of the point-to-point mass */
+	float a = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+	float c = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+	float b = c;
+	float d = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+	float det = a * d - b * c;
+	if ( det != 0.0f ) det = 1.0f / det;
+	j->s[6] = det * d;
+	j->s[7] = -det * c;
+	j->s[8] = -det * b;
+	j->s[9] = det * a;
+}
+
+/* math_functions.h b2MulMV with the stored linear mass */
+static __device__ __forceinline__ b2Vec2 d_motorMulMass( const b2gJoint* j, b2Vec2 v )
+{
+	return d_v( j->s[6] * v.x + j->s[8] * v.y, j->s[7] * v.x + j->s[9] * v.y );
+}
+
+static __device__ void d_prepareMotor( b2gJoint* j, const d_jointBodies* bodies, float h, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	d_makeSoftInto( j->p[5], j->p[6], h, j->s + 11, j->s + 12, j->s + 13 );
+	d_makeSoftInto( j->p[8], j->p[9], h, j->p + 11, j->p + 12, j->p + 13 );
+	d_motorLinearMass( j, j->invMassA, j->invMassB, j->invIA, j->invIB, j->frameA.p, j->frameB.p );
+	float ka = j->invIA + j->invIB;
+	j->s[10] = ka > 0.0f ? 1.0f / ka : 0.0f;
+	if ( warmStart == false )
+	{
+		for ( int i = 0; i < 6; ++i ) j->s[i] = 0.0f;
+	}
+}
+
+template <class TBodies> static __device__ void d_warmStartMotor( b2gJoint* j, TBodies& bodies )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 linearImpulse = d_add( d_v( j->s[0], j->s[1] ), d_v( j->s[3], j->s[4] ) );
+	float angularImpulse = j->s[2] + j->s[5];
+	if ( A.dynamic )
+	{
+		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, linearImpulse );
+		float w = A.v.z - iA * ( d_cross( rA, linearImpulse ) + angularImpulse );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, w, A.v.w );
+	}
+	if ( B.dynamic )
+	{
+		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, linearImpulse );
+		float w = B.v.z + iB * ( d_cross( rB, linearImpulse ) + angularImpulse );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, w, B.v.w );
+	}
+}
+
+/* add `impulse` to the accumulated impulse at s[k], s[k + 1] and clamp its length to
+   maxImpulse (motor_joint.c:383-392); returns the applied change */
+static __device__ __forceinline__ b2Vec2 d_motorAccumulate( b2gJoint* j, int k, b2Vec2 impulse, float maxImpulse )
+{
+	b2Vec2 old = d_v( j->s[k], j->s[k + 1] );
+	b2Vec2 acc = d_add( old, impulse );
+	if ( d_lengthSq( acc ) > maxImpulse * maxImpulse )
+	{
+		acc = d_normalize( acc );
+		acc.x *= maxImpulse;
+		acc.y *= maxImpulse;
+	}
+	j->s[k] = acc.x;
+	j->s[k + 1] = acc.y;
+	return d_sub( acc, old );
+}
+
+/* solve and relax are the same pass for the motor joint (joint.c:1506-1508) */
+template <class TBodies> static __device__ void d_solveMotor( b2gJoint* j, TBodies& bodies, float h )
+{
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
+	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
+	float wA = A.v.z, wB = B.v.z;
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	if ( j->p[10] > 0.0f && j->p[8] > 0.0f )
+	{
+		b2Rot qA = d_mulRot( dqA, j->frameA.q );
+		b2Rot qB = d_mulRot( dqB, j->frameB.q );
+		b2Rot relQ = d_invMulRot( qA, qB );
+		float c = d_atan2( relQ.s, relQ.c );
+		float bias = j->p[11] * c;
+		float massScale = j->p[12];
+		float impulseScale = j->p[13];
+		float cdot = wB - wA;
+		float maxImpulse = h * j->p[10];
+		float oldImpulse = j->s[5];
+		float impulse = -massScale * j->s[10] * ( cdot + bias ) - impulseScale * oldImpulse;
+		j->s[5] = d_clamp( oldImpulse + impulse, -maxImpulse, maxImpulse );
+		impulse = j->s[5] - oldImpulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	if ( j->p[4] > 0.0f )
+	{
+		float cdot = wB - wA - j->p[3];
+		float impulse = -j->s[10] * cdot;
+		float maxImpulse = h * j->p[4];
+		float oldImpulse = j->s[2];
+		j->s[2] = d_clamp( oldImpulse + impulse, -maxImpulse, maxImpulse );
+		impulse = j->s[2] - oldImpulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	if ( j->p[7] > 0.0f && j->p[5] > 0.0f )
+	{
+		b2Vec2 dcA = { A.d.x, A.d.y }, dcB = { B.d.x, B.d.y };
+		b2Vec2 c = d_add( d_add( d_sub( dcB, dcA ), d_sub( rB, rA ) ), j->deltaCenter );
+		b2Vec2 bias = d_mulSV( j->s[11], c );
+		float massScale = j->s[12];
+		float impulseScale = j->s[13];
+		b2Vec2 cdot = d_sub( d_add( vB, d_crossSV( wB, rB ) ), d_add( vA, d_crossSV( wA, rA ) ) );
+		cdot = d_add( cdot, bias );
+		d_motorLinearMass( j, mA, mB, iA, iB, rA, rB );
+		b2Vec2 b = d_motorMulMass( j, cdot );
+		b2Vec2 impulse = d_v( -massScale * b.x - impulseScale * j->s[3], -massScale * b.y - impulseScale * j->s[4] );
+		impulse = d_motorAccumulate( j, 3, impulse, h * j->p[7] );
+		vA = d_mulSub( vA, mA, impulse );
+		wA -= iA * d_cross( rA, impulse );
+		vB = d_mulAdd( vB, mB, impulse );
+		wB += iB * d_cross( rB, impulse );
+	}
+	if ( j->p[2] > 0.0f )
+	{
+		b2Vec2 cdot = d_sub( d_add( vB, d_crossSV( wB, rB ) ), d_add( vA, d_crossSV( wA, rA ) ) );
+		cdot = d_sub( cdot, d_v( j->p[0], j->p[1] ) );
+		b2Vec2 b = d_motorMulMass( j, cdot );
+		b2Vec2 impulse = d_motorAccumulate( j, 0, d_v( -b.x, -b.y ), h * j->p[2] );
+		vA = d_mulSub( vA, mA, impulse );
+		wA -= iA * d_cross( rA, impulse );
+		vB = d_mulAdd( vB, mB, impulse );
+		wB += iB * d_cross( rB, impulse );
+	}
+	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
+}
+
+/* ---- pogo (pogo_joint.c:98-281)
+   p: normal (2), hertz, dampingRatio, restLength, maxTensionForce, maxCompressionForce
+   s: impulse, velocity (the spring's internal velocity), linearMass ---- */
+static __device__ void d_preparePogo( b2gJoint* j, const d_jointBodies* bodies, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	b2Vec2 normal = { j->p[0], j->p[1] };
+	float crA = d_cross( j->frameA.p, normal );
+	float crB = d_cross( j->frameB.p, normal );
+	float k = j->invMassA + j->invMassB + j->invIA * crA * crA + j->invIB * crB * crB;
+	j->s[2] = k > 0.0f ? 1.0f / k : 0.0f;
+	if ( warmStart == false ) j->s[0] = 0.0f;
+}
+
+template <class TBodies> static __device__ void d_warmStartPogo( b2gJoint* j, TBodies& bodies )
+{
+	if ( j->p[2] == 0.0f )
+	{
+		j->s[0] = 0.0f;
+		return;
+	}
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 P = d_mulSV( j->s[0], d_v( j->p[0], j->p[1] ) );
+	if ( A.dynamic )
+	{
+		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), mA, P );
+		float w = A.v.z - iA * d_cross( rA, P );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, w, A.v.w );
+	}
+	if ( B.dynamic )
+	{
+		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), mB, P );
+		float w = B.v.z + iB * d_cross( rB, P );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, w, B.v.w );
+	}
+}
+
+template <class TBodies> static __device__ void d_solvePogo( b2gJoint* j, TBodies& bodies, float h, bool useBias )
+{
+	if ( j->p[2] == 0.0f )
+	{
+		j->s[0] = 0.0f;
+		return;
+	}
+	float mA = j->invMassA, mB = j->invMassB, iA = j->invIA, iB = j->invIB;
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
+	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
+	float wA = A.v.z, wB = B.v.z;
+	b2Rot dqA = { A.d.z, A.d.w }, dqB = { B.d.z, B.d.w };
+	b2Vec2 rA = d_rotate( dqA, j->frameA.p );
+	b2Vec2 rB = d_rotate( dqB, j->frameB.p );
+	b2Vec2 normal = { j->p[0], j->p[1] };
+	float bias = 0.0f;
+	if ( useBias )
+	{
+		b2Vec2 dcA = { A.d.x, A.d.y }, dcB = { B.d.x, B.d.y };
+		b2Vec2 d = d_add( d_add( d_sub( dcB, dcA ), d_sub( rB, rA ) ), j->deltaCenter );
+		/* the pogo axis is frame B's y axis (pogo_joint.c:14) */
+		b2Vec2 pogoAxis = d_rotate( j->frameB.q, d_v( 0.0f, 1.0f ) );
+		float c = d_dot( pogoAxis, d ) - j->p[4];
+		/* math_functions.h b2SpringDamper */
+		float omega = 2.0f * B2_PI * j->p[2];
+		float omegaH = omega * h;
+		j->s[1] = ( j->s[1] - omega * omegaH * c ) / ( 1.0f + 2.0f * j->p[3] * omegaH + omegaH * omegaH );
+		bias = -j->s[1];
+	}
+	b2Vec2 vr = d_sub( d_add( vB, d_crossSV( wB, rB ) ), d_add( vA, d_crossSV( wA, rA ) ) );
+	float cdot = d_dot( normal, vr );
+	float maxTensionImpulse = h * j->p[5];
+	float maxCompressionImpulse = h * j->p[6];
+	float oldImpulse = j->s[0];
+	float impulse = -j->s[2] * ( cdot + bias );
+	j->s[0] = d_clamp( j->s[0] + impulse, -maxTensionImpulse, maxCompressionImpulse );
+	impulse = j->s[0] - oldImpulse;
+	b2Vec2 P = d_mulSV( impulse, normal );
+	vA = d_mulSub( vA, mA, P );
+	wA -= iA * d_cross( rA, P );
+	vB = d_mulAdd( vB, mB, P );
+	wB += iB * d_cross( rB, P );
+	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
+}
+
 /* joint.c:1406-1540 dispatch */
 static __device__ void d_prepareJoint( b2gJoint* j, const d_jointBodies* bodies, float h, float inv_h, bool warmStart )
 {
@@ -918,7 +1157,9 @@ static __device__ void d_prepareJoint( b2gJoint* j, const d_jointBodies* bodies,
 		case b2_revoluteJoint: d_prepareRevolute( j, bodies, h, warmStart ); break;
 		case b2_weldJoint: d_prepareWeld( j, bodies, h, warmStart ); break;
 		case b2_wheelJoint: d_prepareWheel( j, bodies, h, warmStart ); break;
-		default: break;
+		case b2_motorJoint: d_prepareMotor( j, bodies, h, warmStart ); break;
+		case b2_pogoJoint: d_preparePogo( j, bodies, warmStart ); break;
+		default: break; /* filter joints have no constraint */
 	}
 }
 
@@ -931,6 +1172,8 @@ template <class TBodies> static __device__ void d_warmStartJoint( b2gJoint* j, T
 		case b2_revoluteJoint: d_warmStartRevolute( j, bodies ); break;
 		case b2_weldJoint: d_warmStartWeld( j, bodies ); break;
 		case b2_wheelJoint: d_warmStartWheel( j, bodies ); break;
+		case b2_motorJoint: d_warmStartMotor( j, bodies ); break;
+		case b2_pogoJoint: d_warmStartPogo( j, bodies ); break;
 		default: break;
 	}
 }
@@ -944,6 +1187,8 @@ template <class TBodies> static __device__ void d_solveJoint( b2gJoint* j, TBodi
 		case b2_revoluteJoint: d_solveRevolute( j, bodies, h, inv_h, useBias ); break;
 		case b2_weldJoint: d_solveWeld( j, bodies, useBias ); break;
 		case b2_wheelJoint: d_solveWheel( j, bodies, h, inv_h, useBias ); break;
+		case b2_motorJoint: d_solveMotor( j, bodies, h ); break;
+		case b2_pogoJoint: d_solvePogo( j, bodies, h, useBias ); break;
 		default: break;
 	}
 }

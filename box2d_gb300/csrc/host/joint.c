@@ -23,6 +23,17 @@
  *                  minLength, maxLength, maxMotorForce, motorSpeed
  *              s = impulse, lowerImpulse, upperImpulse, motorImpulse, axialMass,
  *                  distance softness (3); the anchors are frameA.p and frameB.p
+ *   motor    : p = linearVelocity (2), maxVelocityForce, angularVelocity,
+ *                  maxVelocityTorque, linearHertz, linearDampingRatio, maxSpringForce,
+ *                  angularHertz, angularDampingRatio, maxSpringTorque, angular spring
+ *                  softness (3, written by the prepare stage)
+ *              s = linearVelocityImpulse (2), angularVelocityImpulse, linearSpringImpulse
+ *                  (2), angularSpringImpulse, linearMass (2x2, columns), angularMass,
+ *                  linear spring softness (3)
+ *   pogo     : p = normal (2), hertz, dampingRatio, restLength, maxTensionForce,
+ *                  maxCompressionForce
+ *              s = impulse, spring velocity, linearMass
+ *   filter   : no parameters; colored like any joint, no constraint
  */
 #include "b2g_world.h"
 
@@ -291,6 +302,81 @@ b2JointId b2CreateDistanceJoint( b2WorldId worldId, const b2DistanceJointDef* de
 	r->enableSpring = def->enableSpring;
 	r->enableLimit = def->enableLimit;
 	r->enableMotor = def->enableMotor;
+	return id;
+}
+
+/* joint.c:50-62, :72-78 */
+b2FilterJointDef b2DefaultFilterJointDef( void )
+{
+	b2FilterJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = h_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+b2MotorJointDef b2DefaultMotorJointDef( void )
+{
+	b2MotorJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = h_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+b2PogoJointDef b2DefaultPogoJointDef( void )
+{
+	b2PogoJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = h_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+/* joint.c:436-459 */
+b2JointId b2CreateFilterJoint( b2WorldId worldId, const b2FilterJointDef* def )
+{
+	h_world* w = h_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	h_createJoint( w, &def->base, b2_filterJoint, &id );
+	return id;
+}
+
+/* joint.c:461-491 */
+b2JointId b2CreateMotorJoint( b2WorldId worldId, const b2MotorJointDef* def )
+{
+	h_world* w = h_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	b2gJoint* r = h_createJoint( w, &def->base, b2_motorJoint, &id );
+	r->p[0] = def->linearVelocity.x;
+	r->p[1] = def->linearVelocity.y;
+	r->p[2] = def->maxVelocityForce;
+	r->p[3] = def->angularVelocity;
+	r->p[4] = def->maxVelocityTorque;
+	r->p[5] = def->linearHertz;
+	r->p[6] = def->linearDampingRatio;
+	r->p[7] = def->maxSpringForce;
+	r->p[8] = def->angularHertz;
+	r->p[9] = def->angularDampingRatio;
+	r->p[10] = def->maxSpringTorque;
+	return id;
+}
+
+/* joint.c:521-560 */
+b2JointId b2CreatePogoJoint( b2WorldId worldId, const b2PogoJointDef* def )
+{
+	h_world* w = h_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	b2gJoint* r = h_createJoint( w, &def->base, b2_pogoJoint, &id );
+	r->p[0] = def->normal.x;
+	r->p[1] = def->normal.y;
+	r->p[2] = def->hertz;
+	r->p[3] = def->dampingRatio;
+	r->p[4] = def->restLength;
+	r->p[5] = def->maxTensionForce;
+	r->p[6] = def->maxCompressionForce;
+	r->s[0] = def->impulse;
+	r->s[1] = def->velocity;
 	return id;
 }
 

@@ -520,6 +520,97 @@ static b2JointDef b2sJointBase( b2BodyId a, b2BodyId b, float ax, float ay, floa
 	return j;
 }
 
+/* Motor, pogo and filter joints (motor_joint.c, pogo_joint.c, joint.c:436-459): per cell a
+   box driven by a motor joint to the ground (velocity control in even cells, spring
+   control in odd ones) with a circle dropped on it, a pair of boxes with a motor joint as
+   top-down friction, a box held up by a pogo joint, and two overlapping boxes whose filter
+   joint keeps them from colliding. */
+static void b2sJointMix( b2sScene* s, int count, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	{
+		b2ShapeDef sd = b2DefaultShapeDef();
+		b2Segment seg = { { -10.0f, 0.0f }, { 12.0f * count + 10.0f, 0.0f } };
+		b2CreateSegmentShape( ground, &sd, &seg );
+	}
+	b2ShapeDef sd = b2DefaultShapeDef();
+	for ( int k = 0; k < count; ++k )
+	{
+		float x0 = 12.0f * k;
+		int variant = k % 2;
+		{
+			float bx = x0 + b2sRandomFloatRange( rng, -0.5f, 0.5f ), by = 3.0f;
+			b2BodyId box = b2sBody( s, b2_dynamicBody, bx, by );
+			b2Polygon p = b2MakeBox( 0.6f, 0.3f );
+			b2CreatePolygonShape( box, &sd, &p );
+			b2MotorJointDef jd = b2DefaultMotorJointDef();
+			jd.base = b2sJointBase( ground, box, x0, 2.0f, 0.0f, 0.0f );
+			if ( variant == 0 )
+			{
+				jd.linearVelocity.x = b2sRandomFloatRange( rng, -1.0f, 1.0f );
+				jd.linearVelocity.y = 0.5f;
+				jd.maxVelocityForce = 40.0f;
+				jd.angularVelocity = b2sRandomFloatRange( rng, -1.0f, 1.0f );
+				jd.maxVelocityTorque = 10.0f;
+			}
+			else
+			{
+				jd.linearHertz = 3.0f;
+				jd.linearDampingRatio = 0.7f;
+				jd.maxSpringForce = 200.0f;
+				jd.angularHertz = 2.0f;
+				jd.angularDampingRatio = 0.5f;
+				jd.maxSpringTorque = 50.0f;
+				jd.maxVelocityForce = 2.0f;
+			}
+			b2CreateMotorJoint( s->worldId, &jd );
+			b2BodyId ball = b2sBody( s, b2_dynamicBody, bx + 0.2f, by + 1.5f );
+			b2Circle c = { { 0.0f, 0.0f }, 0.25f };
+			b2CreateCircleShape( ball, &sd, &c );
+		}
+		{
+			b2BodyId a = b2sBody( s, b2_dynamicBody, x0 + 3.0f, 0.5f );
+			b2BodyId b = b2sBody( s, b2_dynamicBody, x0 + 4.5f, 0.5f );
+			b2Polygon p = b2MakeBox( 0.5f, 0.5f );
+			b2CreatePolygonShape( a, &sd, &p );
+			b2CreatePolygonShape( b, &sd, &p );
+			b2MotorJointDef jd = b2DefaultMotorJointDef();
+			jd.base = b2sJointBase( a, b, 0.0f, 0.0f, 0.0f, 0.0f );
+			jd.base.collideConnected = true;
+			jd.maxVelocityForce = 5.0f;
+			jd.maxVelocityTorque = 2.0f;
+			b2CreateMotorJoint( s->worldId, &jd );
+			b2Body_SetLinearVelocity( a, ( b2Vec2 ){ 2.0f, 0.0f } );
+		}
+		{
+			b2BodyId mover = b2sBody( s, b2_dynamicBody, x0 + 7.0f, 1.6f );
+			b2Polygon p = b2MakeBox( 0.3f, 0.5f );
+			b2CreatePolygonShape( mover, &sd, &p );
+			b2PogoJointDef jd = b2DefaultPogoJointDef();
+			jd.base = b2sJointBase( ground, mover, x0 + 7.0f, 0.0f, 0.0f, -0.5f );
+			jd.normal.x = 0.0f;
+			jd.normal.y = 1.0f;
+			jd.hertz = variant == 0 ? 5.0f : 2.0f;
+			jd.dampingRatio = 0.7f;
+			jd.restLength = 0.8f;
+			jd.maxTensionForce = 20.0f;
+			jd.maxCompressionForce = 400.0f;
+			b2CreatePogoJoint( s->worldId, &jd );
+		}
+		{
+			b2BodyId a = b2sBody( s, b2_dynamicBody, x0 + 9.5f, 0.5f );
+			b2BodyId b = b2sBody( s, b2_dynamicBody, x0 + 9.8f, 0.9f );
+			b2Polygon p = b2MakeBox( 0.5f, 0.5f );
+			b2CreatePolygonShape( a, &sd, &p );
+			b2CreatePolygonShape( b, &sd, &p );
+			b2FilterJointDef jd = b2DefaultFilterJointDef();
+			jd.base = b2sJointBase( a, b, 0.0f, 0.0f, 0.0f, 0.0f );
+			b2CreateFilterJoint( s->worldId, &jd );
+		}
+	}
+}
+
 static void b2sJointZoo( b2sScene* s, int count, b2sRng* rng )
 {
 	b2World_EnableSleeping( s->worldId, false );
@@ -795,6 +886,7 @@ enum
 	B2S_JOINT_ZOO = 9,
 	B2S_FALLING_HINGES = 10,
 	B2S_SLEEP_PYRAMIDS = 11,
+	B2S_JOINT_MIX = 12,
 };
 
 /* Create a scene. kind selects the builder; a, b, c are its size parameters; seed feeds
@@ -836,6 +928,7 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 		case B2S_JOINT_ZOO: b2sJointZoo( s, a, &rng ); break;
 		case B2S_FALLING_HINGES: b2sFallingHinges( s ); break;
 		case B2S_SLEEP_PYRAMIDS: b2sSleepPyramids( s, a, b, c ); break;
+		case B2S_JOINT_MIX: b2sJointMix( s, a, &rng ); break;
 		default: break;
 	}
 	return h;

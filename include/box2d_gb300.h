@@ -461,6 +461,45 @@ typedef struct b2WheelJointDef
 	int internalValue;
 } b2WheelJointDef;
 
+/* types.h:694-701: disables collision between two bodies, no constraint */
+typedef struct b2FilterJointDef
+{
+	b2JointDef base;
+	int internalValue;
+} b2FilterJointDef;
+
+/* types.h:710-747: relative velocity and spring control between two bodies */
+typedef struct b2MotorJointDef
+{
+	b2JointDef base;
+	b2Vec2 linearVelocity;
+	float maxVelocityForce;
+	float angularVelocity;
+	float maxVelocityTorque;
+	float linearHertz;
+	float linearDampingRatio;
+	float maxSpringForce;
+	float angularHertz;
+	float angularDampingRatio;
+	float maxSpringTorque;
+	int internalValue;
+} b2MotorJointDef;
+
+/* types.h:777-810: one-sided spring along a normal (character movers) */
+typedef struct b2PogoJointDef
+{
+	b2JointDef base;
+	b2Vec2 normal;
+	float hertz;
+	float dampingRatio;
+	float restLength;
+	float maxTensionForce;
+	float maxCompressionForce;
+	float impulse;
+	float velocity;
+	int internalValue;
+} b2PogoJointDef;
+
 /* ---- events (types.h) ---- */
 typedef struct b2ContactBeginTouchEvent
 {
@@ -617,6 +656,13 @@ B2G_API b2JointId b2CreatePrismaticJoint( b2WorldId worldId, const b2PrismaticJo
 B2G_API b2JointId b2CreateRevoluteJoint( b2WorldId worldId, const b2RevoluteJointDef* def );
 B2G_API b2JointId b2CreateWeldJoint( b2WorldId worldId, const b2WeldJointDef* def );
 B2G_API b2JointId b2CreateWheelJoint( b2WorldId worldId, const b2WheelJointDef* def );
+/* types.h:705, :751, :814 and box2d.h:1091, :1109, :1207 */
+B2G_API b2FilterJointDef b2DefaultFilterJointDef( void );
+B2G_API b2MotorJointDef b2DefaultMotorJointDef( void );
+B2G_API b2PogoJointDef b2DefaultPogoJointDef( void );
+B2G_API b2JointId b2CreateFilterJoint( b2WorldId worldId, const b2FilterJointDef* def );
+B2G_API b2JointId b2CreateMotorJoint( b2WorldId worldId, const b2MotorJointDef* def );
+B2G_API b2JointId b2CreatePogoJoint( b2WorldId worldId, const b2PogoJointDef* def );
 B2G_API b2JointType b2Joint_GetType( b2JointId jointId );
 B2G_API float b2RevoluteJoint_GetAngle( b2JointId jointId );
 

@@ -568,6 +568,36 @@ typedef struct o_wheelJoint
 	int enableSpring, enableMotor, enableLimit;
 } o_wheelJoint;
 
+/* joint.h b2MotorJoint */
+typedef struct o_motorJoint
+{
+	b2Vec2 linearVelocity;
+	float maxVelocityForce, angularVelocity, maxVelocityTorque;
+	float linearHertz, linearDampingRatio, maxSpringForce, angularHertz, angularDampingRatio, maxSpringTorque;
+	b2Vec2 linearVelocityImpulse;
+	float angularVelocityImpulse;
+	b2Vec2 linearSpringImpulse;
+	float angularSpringImpulse;
+	o_softness linearSpring, angularSpring;
+	int indexA, indexB;
+	b2Transform frameA, frameB;
+	b2Vec2 deltaCenter;
+	b2Vec2 linearMassCx, linearMassCy; /* b2Mat22 columns */
+	float angularMass;
+} o_motorJoint;
+
+/* joint.h b2PogoJoint */
+typedef struct o_pogoJoint
+{
+	b2Vec2 normal;
+	float hertz, dampingRatio, restLength, maxTensionForce, maxCompressionForce;
+	float impulse, velocity;
+	int indexA, indexB;
+	b2Transform frameA, frameB;
+	b2Vec2 deltaCenter;
+	float linearMass;
+} o_pogoJoint;
+
 struct o_jointSim
 {
 	int jointId, bodyIdA, bodyIdB;
@@ -584,6 +614,8 @@ struct o_jointSim
 		o_revoluteJoint revoluteJoint;
 		o_weldJoint weldJoint;
 		o_wheelJoint wheelJoint;
+		o_motorJoint motorJoint;
+		o_pogoJoint pogoJoint;
 	};
 };
 

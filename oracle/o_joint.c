@@ -278,6 +278,83 @@ b2JointId b2CreateWheelJoint( b2WorldId worldId, const b2WheelJointDef* def )
 	return id;
 }
 
+/* joint.c:50-62, :72-78 */
+b2FilterJointDef b2DefaultFilterJointDef( void )
+{
+	b2FilterJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = o_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+b2MotorJointDef b2DefaultMotorJointDef( void )
+{
+	b2MotorJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = o_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+b2PogoJointDef b2DefaultPogoJointDef( void )
+{
+	b2PogoJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = o_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+/* joint.c:436-459: a graph edge and a colored constraint that does nothing */
+b2JointId b2CreateFilterJoint( b2WorldId worldId, const b2FilterJointDef* def )
+{
+	o_world* w = o_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	o_createJoint( w, &def->base, b2_filterJoint, &id );
+	return id;
+}
+
+/* joint.c:461-491 */
+b2JointId b2CreateMotorJoint( b2WorldId worldId, const b2MotorJointDef* def )
+{
+	o_world* w = o_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	o_jointSim* j = o_createJoint( w, &def->base, b2_motorJoint, &id );
+	memset( &j->motorJoint, 0, sizeof( j->motorJoint ) );
+	o_motorJoint* m = &j->motorJoint;
+	m->linearVelocity = def->linearVelocity;
+	m->maxVelocityForce = def->maxVelocityForce;
+	m->angularVelocity = def->angularVelocity;
+	m->maxVelocityTorque = def->maxVelocityTorque;
+	m->linearHertz = def->linearHertz;
+	m->linearDampingRatio = def->linearDampingRatio;
+	m->maxSpringForce = def->maxSpringForce;
+	m->angularHertz = def->angularHertz;
+	m->angularDampingRatio = def->angularDampingRatio;
+	m->maxSpringTorque = def->maxSpringTorque;
+	return id;
+}
+
+/* joint.c:521-560 */
+b2JointId b2CreatePogoJoint( b2WorldId worldId, const b2PogoJointDef* def )
+{
+	o_world* w = o_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	o_jointSim* j = o_createJoint( w, &def->base, b2_pogoJoint, &id );
+	memset( &j->pogoJoint, 0, sizeof( j->pogoJoint ) );
+	o_pogoJoint* q = &j->pogoJoint;
+	q->restLength = def->restLength;
+	q->hertz = def->hertz;
+	q->dampingRatio = def->dampingRatio;
+	q->maxTensionForce = def->maxTensionForce;
+	q->maxCompressionForce = def->maxCompressionForce;
+	q->normal = def->normal;
+	q->impulse = def->impulse;
+	q->velocity = def->velocity;
+	return id;
+}
+
 /* ---------------- shared helpers ---------------- */
 static o_bodySim* o_jointBodySim( o_world* w, int bodyId, int* awakeIndex )
 {
@@ -1195,6 +1272,296 @@ static void o_solveDistance( o_world* w, o_stepContext* ctx, o_jointSim* base, i
 	}
 }
 
+/* ---------------- motor (motor_joint.c:180-436) ---------------- */
+/* math_functions.h b2GetInverse22 and b2MulMV, columns cx, cy */
+static void o_inverse22( b2Vec2 cx, b2Vec2 cy, b2Vec2* ox, b2Vec2* oy )
+{
+	float a = cx.x, b = cy.x, c = cx.y, d = cy.y;
+	float det = a * d - b * c;
+	if ( det != 0.0f ) det = 1.0f / det;
+	*ox = o_v( det * d, -det * c );
+	*oy = o_v( -det * b, det * a );
+}
+
+static b2Vec2 o_mulMV( b2Vec2 cx, b2Vec2 cy, b2Vec2 v ) { return o_v( cx.x * v.x + cy.x * v.y, cx.y * v.x + cy.y * v.y ); }
+
+static void o_motorLinearMass( o_motorJoint* j, float mA, float mB, float iA, float iB, b2Vec2 rA, b2Vec2 rB )
+{
+	b2Vec2 kx, ky;
+	kx.x = mA + mB + rA.y * rA.y * iA + rB.y * rB.y * iB;
+	kx.y = -rA.y * rA.x * iA - rB.y * rB.x * iB;
+	ky.x = kx.y;
+	ky.y = mA + mB + rA.x * rA.x * iA + rB.x * rB.x * iB;
+	o_inverse22( kx, ky, &j->linearMassCx, &j->linearMassCy );
+}
+
+static void o_prepareMotor( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	int ia, ib;
+	o_bodySim* simA = o_jointBodySim( w, base->bodyIdA, &ia );
+	o_bodySim* simB = o_jointBodySim( w, base->bodyIdB, &ib );
+	float mA = simA->invMass, iA = simA->invInertia, mB = simB->invMass, iB = simB->invInertia;
+	base->invMassA = mA;
+	base->invMassB = mB;
+	base->invIA = iA;
+	base->invIB = iB;
+	o_motorJoint* j = &base->motorJoint;
+	j->indexA = ia;
+	j->indexB = ib;
+	j->frameA.q = o_mulRot( simA->transform.q, base->localFrameA.q );
+	j->frameA.p = o_rotate( simA->transform.q, o_sub( base->localFrameA.p, simA->localCenter ) );
+	j->frameB.q = o_mulRot( simB->transform.q, base->localFrameB.q );
+	j->frameB.p = o_rotate( simB->transform.q, o_sub( base->localFrameB.p, simB->localCenter ) );
+	j->deltaCenter = o_v( simB->center.x - simA->center.x, simB->center.y - simA->center.y );
+	j->linearSpring = o_makeSoft( j->linearHertz, j->linearDampingRatio, ctx->h );
+	j->angularSpring = o_makeSoft( j->angularHertz, j->angularDampingRatio, ctx->h );
+	o_motorLinearMass( j, mA, mB, iA, iB, j->frameA.p, j->frameB.p );
+	float ka = iA + iB;
+	j->angularMass = ka > 0.0f ? 1.0f / ka : 0.0f;
+	if ( ctx->enableWarmStarting == 0 )
+	{
+		j->linearVelocityImpulse = o_v( 0.0f, 0.0f );
+		j->angularVelocityImpulse = 0.0f;
+		j->linearSpringImpulse = o_v( 0.0f, 0.0f );
+		j->angularSpringImpulse = 0.0f;
+	}
+}
+
+static void o_warmStartMotor( o_world* w, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_motorJoint* j = &base->motorJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	b2Vec2 linearImpulse = o_add( j->linearVelocityImpulse, j->linearSpringImpulse );
+	float angularImpulse = j->angularVelocityImpulse + j->angularSpringImpulse;
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = o_mulSub( sA->linearVelocity, mA, linearImpulse );
+		sA->angularVelocity -= iA * ( o_cross( rA, linearImpulse ) + angularImpulse );
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = o_mulAdd( sB->linearVelocity, mB, linearImpulse );
+		sB->angularVelocity += iB * ( o_cross( rB, linearImpulse ) + angularImpulse );
+	}
+}
+
+/* accumulate `impulse` into `*acc` and clamp the total's length to maxImpulse
+   (motor_joint.c:383-392); returns the applied change */
+static b2Vec2 o_clampedAccumulate( b2Vec2* acc, b2Vec2 impulse, float maxImpulse )
+{
+	b2Vec2 old = *acc;
+	*acc = o_add( *acc, impulse );
+	if ( o_lengthSq( *acc ) > maxImpulse * maxImpulse )
+	{
+		*acc = o_normalize( *acc );
+		acc->x *= maxImpulse;
+		acc->y *= maxImpulse;
+	}
+	return o_sub( *acc, old );
+}
+
+/* the motor joint ignores useBias: solve and relax are the same pass (joint.c:1506-1508) */
+static void o_solveMotor( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_bodyState dummy = o_dummyState;
+	o_motorJoint* j = &base->motorJoint;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 vA = sA->linearVelocity, vB = sB->linearVelocity;
+	float wA = sA->angularVelocity, wB = sB->angularVelocity;
+	if ( j->maxSpringTorque > 0.0f && j->angularHertz > 0.0f )
+	{
+		b2Rot qA = o_mulRot( sA->deltaRotation, j->frameA.q );
+		b2Rot qB = o_mulRot( sB->deltaRotation, j->frameB.q );
+		b2Rot relQ = o_invMulRot( qA, qB );
+		float c = b2Atan2( relQ.s, relQ.c );
+		float bias = j->angularSpring.biasRate * c;
+		float massScale = j->angularSpring.massScale;
+		float impulseScale = j->angularSpring.impulseScale;
+		float cdot = wB - wA;
+		float maxImpulse = ctx->h * j->maxSpringTorque;
+		float oldImpulse = j->angularSpringImpulse;
+		float impulse = -massScale * j->angularMass * ( cdot + bias ) - impulseScale * oldImpulse;
+		j->angularSpringImpulse = o_clamp( oldImpulse + impulse, -maxImpulse, maxImpulse );
+		impulse = j->angularSpringImpulse - oldImpulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	if ( j->maxVelocityTorque > 0.0f )
+	{
+		float cdot = wB - wA - j->angularVelocity;
+		float impulse = -j->angularMass * cdot;
+		float maxImpulse = ctx->h * j->maxVelocityTorque;
+		float oldImpulse = j->angularVelocityImpulse;
+		j->angularVelocityImpulse = o_clamp( oldImpulse + impulse, -maxImpulse, maxImpulse );
+		impulse = j->angularVelocityImpulse - oldImpulse;
+		wA -= iA * impulse;
+		wB += iB * impulse;
+	}
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	if ( j->maxSpringForce > 0.0f && j->linearHertz > 0.0f )
+	{
+		b2Vec2 dcA = sA->deltaPosition, dcB = sB->deltaPosition;
+		b2Vec2 c = o_add( o_add( o_sub( dcB, dcA ), o_sub( rB, rA ) ), j->deltaCenter );
+		b2Vec2 bias = o_mulSV( j->linearSpring.biasRate, c );
+		float massScale = j->linearSpring.massScale;
+		float impulseScale = j->linearSpring.impulseScale;
+		b2Vec2 cdot = o_sub( o_add( vB, o_crossSV( wB, rB ) ), o_add( vA, o_crossSV( wA, rA ) ) );
+		cdot = o_add( cdot, bias );
+		o_motorLinearMass( j, mA, mB, iA, iB, rA, rB );
+		b2Vec2 b = o_mulMV( j->linearMassCx, j->linearMassCy, cdot );
+		b2Vec2 old = j->linearSpringImpulse;
+		b2Vec2 impulse = o_v( -massScale * b.x - impulseScale * old.x, -massScale * b.y - impulseScale * old.y );
+		impulse = o_clampedAccumulate( &j->linearSpringImpulse, impulse, ctx->h * j->maxSpringForce );
+		vA = o_mulSub( vA, mA, impulse );
+		wA -= iA * o_cross( rA, impulse );
+		vB = o_mulAdd( vB, mB, impulse );
+		wB += iB * o_cross( rB, impulse );
+	}
+	if ( j->maxVelocityForce > 0.0f )
+	{
+		b2Vec2 cdot = o_sub( o_add( vB, o_crossSV( wB, rB ) ), o_add( vA, o_crossSV( wA, rA ) ) );
+		cdot = o_sub( cdot, j->linearVelocity );
+		b2Vec2 b = o_mulMV( j->linearMassCx, j->linearMassCy, cdot );
+		b2Vec2 impulse = o_v( -b.x, -b.y );
+		impulse = o_clampedAccumulate( &j->linearVelocityImpulse, impulse, ctx->h * j->maxVelocityForce );
+		vA = o_mulSub( vA, mA, impulse );
+		wA -= iA * o_cross( rA, impulse );
+		vB = o_mulAdd( vB, mB, impulse );
+		wB += iB * o_cross( rB, impulse );
+	}
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = vA;
+		sA->angularVelocity = wA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = vB;
+		sB->angularVelocity = wB;
+	}
+}
+
+/* ---------------- pogo (pogo_joint.c:98-281) ---------------- */
+static void o_preparePogo( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	int ia, ib;
+	o_bodySim* simA = o_jointBodySim( w, base->bodyIdA, &ia );
+	o_bodySim* simB = o_jointBodySim( w, base->bodyIdB, &ib );
+	float mA = simA->invMass, iA = simA->invInertia, mB = simB->invMass, iB = simB->invInertia;
+	base->invMassA = mA;
+	base->invMassB = mB;
+	base->invIA = iA;
+	base->invIB = iB;
+	o_pogoJoint* j = &base->pogoJoint;
+	j->indexA = ia;
+	j->indexB = ib;
+	j->frameA.q = o_mulRot( simA->transform.q, base->localFrameA.q );
+	j->frameA.p = o_rotate( simA->transform.q, o_sub( base->localFrameA.p, simA->localCenter ) );
+	j->frameB.q = o_mulRot( simB->transform.q, base->localFrameB.q );
+	j->frameB.p = o_rotate( simB->transform.q, o_sub( base->localFrameB.p, simB->localCenter ) );
+	j->deltaCenter = o_v( simB->center.x - simA->center.x, simB->center.y - simA->center.y );
+	float crA = o_cross( j->frameA.p, j->normal );
+	float crB = o_cross( j->frameB.p, j->normal );
+	float k = mA + mB + iA * crA * crA + iB * crB * crB;
+	j->linearMass = k > 0.0f ? 1.0f / k : 0.0f;
+	if ( ctx->enableWarmStarting == 0 ) j->impulse = 0.0f;
+}
+
+static void o_warmStartPogo( o_world* w, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_pogoJoint* j = &base->pogoJoint;
+	if ( j->hertz == 0.0f )
+	{
+		j->impulse = 0.0f;
+		return;
+	}
+	o_bodyState dummy = o_dummyState;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	b2Vec2 P = o_mulSV( j->impulse, j->normal );
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = o_mulSub( sA->linearVelocity, mA, P );
+		sA->angularVelocity -= iA * o_cross( rA, P );
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = o_mulAdd( sB->linearVelocity, mB, P );
+		sB->angularVelocity += iB * o_cross( rB, P );
+	}
+}
+
+/* math_functions.h b2SpringDamper: implicit spring-damper velocity update */
+static float o_springDamper( float hertz, float dampingRatio, float position, float velocity, float timeStep )
+{
+	float omega = 2.0f * B2_PI * hertz;
+	float omegaH = omega * timeStep;
+	return ( velocity - omega * omegaH * position ) / ( 1.0f + 2.0f * dampingRatio * omegaH + omegaH * omegaH );
+}
+
+static void o_solvePogo( o_world* w, o_stepContext* ctx, o_jointSim* base, int useBias )
+{
+	float mA = base->invMassA, mB = base->invMassB, iA = base->invIA, iB = base->invIB;
+	o_pogoJoint* j = &base->pogoJoint;
+	if ( j->hertz == 0.0f )
+	{
+		j->impulse = 0.0f;
+		return;
+	}
+	o_bodyState dummy = o_dummyState;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 vA = sA->linearVelocity, vB = sB->linearVelocity;
+	float wA = sA->angularVelocity, wB = sB->angularVelocity;
+	b2Vec2 rA = o_rotate( sA->deltaRotation, j->frameA.p );
+	b2Vec2 rB = o_rotate( sB->deltaRotation, j->frameB.p );
+	float bias = 0.0f;
+	if ( useBias )
+	{
+		b2Vec2 dcA = sA->deltaPosition, dcB = sB->deltaPosition;
+		b2Vec2 d = o_add( o_add( o_sub( dcB, dcA ), o_sub( rB, rA ) ), j->deltaCenter );
+		/* the pogo axis is frame B's y axis (pogo_joint.c:14) */
+		b2Vec2 pogoAxis = o_rotate( j->frameB.q, o_v( 0.0f, 1.0f ) );
+		float c = o_dot( pogoAxis, d ) - j->restLength;
+		j->velocity = o_springDamper( j->hertz, j->dampingRatio, c, j->velocity, ctx->h );
+		bias = -j->velocity;
+	}
+	b2Vec2 vr = o_sub( o_add( vB, o_crossSV( wB, rB ) ), o_add( vA, o_crossSV( wA, rA ) ) );
+	float cdot = o_dot( j->normal, vr );
+	float maxTensionImpulse = ctx->h * j->maxTensionForce;
+	float maxCompressionImpulse = ctx->h * j->maxCompressionForce;
+	float oldImpulse = j->impulse;
+	float impulse = -j->linearMass * ( cdot + bias );
+	j->impulse = o_clamp( j->impulse + impulse, -maxTensionImpulse, maxCompressionImpulse );
+	impulse = j->impulse - oldImpulse;
+	b2Vec2 P = o_mulSV( impulse, j->normal );
+	vA = o_mulSub( vA, mA, P );
+	wA -= iA * o_cross( rA, P );
+	vB = o_mulAdd( vB, mB, P );
+	wB += iB * o_cross( rB, P );
+	if ( sA->flags & O_DYNAMIC_FLAG )
+	{
+		sA->linearVelocity = vA;
+		sA->angularVelocity = wA;
+	}
+	if ( sB->flags & O_DYNAMIC_FLAG )
+	{
+		sB->linearVelocity = vB;
+		sB->angularVelocity = wB;
+	}
+}
+
 /* ---------------- dispatch (joint.c:1406-1540) ---------------- */
 int o_unsupportedJoints = 0;
 
@@ -1209,6 +1576,9 @@ void o_prepareJoint( o_world* w, o_stepContext* ctx, o_jointSim* j )
 		case b2_revoluteJoint: o_prepareRevolute( w, ctx, j ); break;
 		case b2_weldJoint: o_prepareWeld( w, ctx, j ); break;
 		case b2_wheelJoint: o_prepareWheel( w, ctx, j ); break;
+		case b2_motorJoint: o_prepareMotor( w, ctx, j ); break;
+		case b2_pogoJoint: o_preparePogo( w, ctx, j ); break;
+		case b2_filterJoint: break;
 		default: o_unsupportedJoints += 1; break;
 	}
 }
@@ -1223,6 +1593,8 @@ void o_warmStartJoint( o_world* w, o_stepContext* ctx, o_jointSim* j )
 		case b2_revoluteJoint: o_warmStartRevolute( w, j ); break;
 		case b2_weldJoint: o_warmStartWeld( w, j ); break;
 		case b2_wheelJoint: o_warmStartWheel( w, j ); break;
+		case b2_motorJoint: o_warmStartMotor( w, j ); break;
+		case b2_pogoJoint: o_warmStartPogo( w, j ); break;
 		default: break;
 	}
 }
@@ -1236,6 +1608,8 @@ void o_solveJoint( o_world* w, o_stepContext* ctx, o_jointSim* j, int useBias )
 		case b2_revoluteJoint: o_solveRevolute( w, ctx, j, useBias ); break;
 		case b2_weldJoint: o_solveWeld( w, j, useBias ); break;
 		case b2_wheelJoint: o_solveWheel( w, ctx, j, useBias ); break;
+		case b2_motorJoint: o_solveMotor( w, ctx, j ); break;
+		case b2_pogoJoint: o_solvePogo( w, ctx, j, useBias ); break;
 		default: break;
 	}
 }

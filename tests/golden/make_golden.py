@@ -8,7 +8,7 @@ table (contact id, shape pair, graph color, point count, feature ids, touching) 
 steps. The committed JSON files are what tests compare the oracle and the GB300 library
 against on machines without the reference.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [scene names]   (all scenes without names)
 """
 from __future__ import annotations
 
@@ -34,6 +34,7 @@ SCENES = [
     ("batch_world_60", B.BATCH_WORLD, 60, 0, 0, 11, B.NO_CONTINUOUS, 200, [1, 200]),
     ("ramp_world_4x4", B.RAMP_WORLD, 4, 4, 0, 5, B.NO_CONTINUOUS, 120, [1, 120]),
     ("joint_zoo_4", B.JOINT_ZOO, 4, 0, 0, 3, B.NO_CONTINUOUS, 300, [1, 150, 300]),
+    ("joint_mix_4", B.JOINT_MIX, 4, 0, 0, 5, B.NO_CONTINUOUS, 300, [1, 150, 300]),
     # continuous collision on: fast bodies are swept against static shapes
     ("shape_zoo_200_continuous", B.SHAPE_ZOO, 200, 0, 0, 7, 0, 300, [1, 150, 300]),
     ("many_pyramids_rain_3x3_continuous", B.MANY_PYRAMIDS_RAIN, 3, 10, 100, 0, 0, 300, [1, 150, 300]),
@@ -65,7 +66,10 @@ def contact_digest(table) -> str:
 def main() -> None:
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"], check=True)
     ref = B.load_library(ROOT / "oracle" / "_ref" / "libref.so")
+    only = set(sys.argv[1:])
     for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES + SLEEP_SCENES:
+        if only and name not in only:
+            continue
         sleeping = (name, kind, a, b, c, seed, flags, steps, digest_steps) in SLEEP_SCENES
         script = SCRIPTS.get(name, [])
         with B.Scene(ref, kind, a, b, c, seed, flags) as s:

@@ -23,6 +23,7 @@ CASES = [
     ("shape_zoo_restitution", B.SHAPE_ZOO, 150, 0, 0, 2, B.NO_CONTINUOUS, 100),
     ("batch_world", B.BATCH_WORLD, 0, 0, 0, 22, B.NO_CONTINUOUS, 100),
     ("joint_zoo", B.JOINT_ZOO, 6, 0, 0, 4, B.NO_CONTINUOUS, 150),
+    ("joint_mix", B.JOINT_MIX, 6, 0, 0, 4, B.NO_CONTINUOUS, 150),
 ]
 
 
