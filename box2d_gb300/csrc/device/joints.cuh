@@ -1059,6 +1059,69 @@ template <class TBodies> static __device__ void d_solveMotor( b2gJoint* j, TBodi
 	d_storeVelocities( bodies, j, A, B, vA, wA, vB, wB );
 }
 
+/* ---- mover (mover_joint.c:43-170): linear velocity only, the bodies' rotation untouched
+   p: linearVelocity (2), maxVelocityForce (2)
+   s: linearVelocityImpulse (2), linearMass ---- */
+static __device__ void d_prepareMover( b2gJoint* j, const d_jointBodies* bodies, bool warmStart )
+{
+	d_prepareJointFrames( j, bodies );
+	j->invIA = 0.0f;
+	j->invIB = 0.0f;
+	float k = j->invMassA + j->invMassB;
+	j->s[2] = k > 0.0f ? 1.0f / k : 0.0f;
+	if ( warmStart == false )
+	{
+		j->s[0] = 0.0f;
+		j->s[1] = 0.0f;
+	}
+}
+
+template <class TBodies> static __device__ void d_warmStartMover( b2gJoint* j, TBodies& bodies )
+{
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
+	b2Vec2 P = { j->s[0], j->s[1] };
+	if ( A.dynamic )
+	{
+		b2Vec2 v = d_mulSub( d_v( A.v.x, A.v.y ), j->invMassA, P );
+		bodies.v( j->indexA ) = make_float4( v.x, v.y, A.v.z, A.v.w );
+	}
+	if ( B.dynamic )
+	{
+		b2Vec2 v = d_mulAdd( d_v( B.v.x, B.v.y ), j->invMassB, P );
+		bodies.v( j->indexB ) = make_float4( v.x, v.y, B.v.z, B.v.w );
+	}
+}
+
+template <class TBodies> static __device__ void d_solveMover( b2gJoint* j, TBodies& bodies, float h )
+{
+	float mA = j->invMassA, mB = j->invMassB;
+	d_stateRef A = d_loadState( bodies, j->indexA ), B = d_loadState( bodies, j->indexB );
+	b2Vec2 vA = { A.v.x, A.v.y }, vB = { B.v.x, B.v.y };
+	if ( j->p[2] > 0.0f || j->p[3] > 0.0f )
+	{
+		b2Vec2 cdot = d_sub( d_sub( vB, vA ), d_v( j->p[0], j->p[1] ) );
+		b2Vec2 b = d_mulSV( j->s[2], cdot );
+		b2Vec2 old = { j->s[0], j->s[1] };
+		b2Vec2 acc = d_add( old, d_v( -b.x, -b.y ) );
+		/* x and y clamped separately (math_functions.h b2Clamp) */
+		float mx = h * j->p[2], my = h * j->p[3];
+		acc.x = d_clamp( acc.x, -mx, mx );
+		acc.y = d_clamp( acc.y, -my, my );
+		j->s[0] = acc.x;
+		j->s[1] = acc.y;
+		b2Vec2 impulse = d_sub( acc, old );
+		vA = d_mulSub( vA, mA, impulse );
+		vB = d_mulAdd( vB, mB, impulse );
+	}
+	else
+	{
+		j->s[0] = 0.0f;
+		j->s[1] = 0.0f;
+	}
+	if ( A.dynamic ) bodies.v( j->indexA ) = make_float4( vA.x, vA.y, A.v.z, A.v.w );
+	if ( B.dynamic ) bodies.v( j->indexB ) = make_float4( vB.x, vB.y, B.v.z, B.v.w );
+}
+
 /* ---- pogo (pogo_joint.c:98-281)
    p: normal (2), hertz, dampingRatio, restLength, maxTensionForce, maxCompressionForce
    s: impulse, velocity (the spring's internal velocity), linearMass ---- */
@@ -1159,6 +1222,7 @@ static __device__ void d_prepareJoint( b2gJoint* j, const d_jointBodies* bodies,
 		case b2_wheelJoint: d_prepareWheel( j, bodies, h, warmStart ); break;
 		case b2_motorJoint: d_prepareMotor( j, bodies, h, warmStart ); break;
 		case b2_pogoJoint: d_preparePogo( j, bodies, warmStart ); break;
+		case b2_moverJoint: d_prepareMover( j, bodies, warmStart ); break;
 		default: break; /* filter joints have no constraint */
 	}
 }
@@ -1174,6 +1238,7 @@ template <class TBodies> static __device__ void d_warmStartJoint( b2gJoint* j, T
 		case b2_wheelJoint: d_warmStartWheel( j, bodies ); break;
 		case b2_motorJoint: d_warmStartMotor( j, bodies ); break;
 		case b2_pogoJoint: d_warmStartPogo( j, bodies ); break;
+		case b2_moverJoint: d_warmStartMover( j, bodies ); break;
 		default: break;
 	}
 }
@@ -1189,6 +1254,7 @@ template <class TBodies> static __device__ void d_solveJoint( b2gJoint* j, TBodi
 		case b2_wheelJoint: d_solveWheel( j, bodies, h, inv_h, useBias ); break;
 		case b2_motorJoint: d_solveMotor( j, bodies, h ); break;
 		case b2_pogoJoint: d_solvePogo( j, bodies, h, useBias ); break;
+		case b2_moverJoint: d_solveMover( j, bodies, h ); break;
 		default: break;
 	}
 }

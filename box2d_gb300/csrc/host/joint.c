@@ -33,6 +33,8 @@
  *   pogo     : p = normal (2), hertz, dampingRatio, restLength, maxTensionForce,
  *                  maxCompressionForce
  *              s = impulse, spring velocity, linearMass
+ *   mover    : p = linearVelocity (2), maxVelocityForce (2)
+ *              s = linearVelocityImpulse (2), linearMass
  *   filter   : no parameters; colored like any joint, no constraint
  */
 #include "b2g_world.h"
@@ -331,6 +333,28 @@ b2PogoJointDef b2DefaultPogoJointDef( void )
 	def.base = h_defaultJointDef();
 	def.internalValue = 1152023;
 	return def;
+}
+
+b2MoverJointDef b2DefaultMoverJointDef( void )
+{
+	b2MoverJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = h_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+/* joint.c b2CreateMoverJoint */
+b2JointId b2CreateMoverJoint( b2WorldId worldId, const b2MoverJointDef* def )
+{
+	h_world* w = h_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	b2gJoint* r = h_createJoint( w, &def->base, b2_moverJoint, &id );
+	r->p[0] = def->linearVelocity.x;
+	r->p[1] = def->linearVelocity.y;
+	r->p[2] = def->maxVelocityForce.x;
+	r->p[3] = def->maxVelocityForce.y;
+	return id;
 }
 
 /* joint.c:436-459 */

@@ -520,11 +520,11 @@ static b2JointDef b2sJointBase( b2BodyId a, b2BodyId b, float ax, float ay, floa
 	return j;
 }
 
-/* Motor, pogo and filter joints (motor_joint.c, pogo_joint.c, joint.c:436-459): per cell a
-   box driven by a motor joint to the ground (velocity control in even cells, spring
-   control in odd ones) with a circle dropped on it, a pair of boxes with a motor joint as
-   top-down friction, a box held up by a pogo joint, and two overlapping boxes whose filter
-   joint keeps them from colliding. */
+/* Motor, pogo, mover and filter joints (motor_joint.c, pogo_joint.c, mover_joint.c,
+   joint.c:436-459): per cell a box driven by a motor joint to the ground (velocity control
+   in even cells, spring control in odd ones) with a circle dropped on it, a pair of boxes
+   with a motor joint as top-down friction, a box held up by a pogo joint, a box walked by
+   a mover joint, and two overlapping boxes whose filter joint keeps them from colliding. */
 static void b2sJointMix( b2sScene* s, int count, b2sRng* rng )
 {
 	b2World_EnableSleeping( s->worldId, false );
@@ -597,6 +597,18 @@ static void b2sJointMix( b2sScene* s, int count, b2sRng* rng )
 			jd.maxTensionForce = 20.0f;
 			jd.maxCompressionForce = 400.0f;
 			b2CreatePogoJoint( s->worldId, &jd );
+		}
+		{
+			b2BodyId walker = b2sBody( s, b2_dynamicBody, x0 + 5.5f, 2.0f );
+			b2Polygon p = b2MakeBox( 0.3f, 0.3f );
+			b2CreatePolygonShape( walker, &sd, &p );
+			b2MoverJointDef jd = b2DefaultMoverJointDef();
+			jd.base = b2sJointBase( ground, walker, x0 + 5.5f, 2.0f, 0.0f, 0.0f );
+			jd.linearVelocity.x = variant == 0 ? 1.5f : -1.0f;
+			jd.linearVelocity.y = 0.0f;
+			jd.maxVelocityForce.x = 30.0f;
+			jd.maxVelocityForce.y = variant == 0 ? 0.0f : 5.0f;
+			b2CreateMoverJoint( s->worldId, &jd );
 		}
 		{
 			b2BodyId a = b2sBody( s, b2_dynamicBody, x0 + 9.5f, 0.5f );

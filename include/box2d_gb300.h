@@ -485,6 +485,15 @@ typedef struct b2MotorJointDef
 	int internalValue;
 } b2MotorJointDef;
 
+/* types.h:756-769: linear velocity control, x and y separately, no rotation */
+typedef struct b2MoverJointDef
+{
+	b2JointDef base;
+	b2Vec2 linearVelocity;
+	b2Vec2 maxVelocityForce;
+	int internalValue;
+} b2MoverJointDef;
+
 /* types.h:777-810: one-sided spring along a normal (character movers) */
 typedef struct b2PogoJointDef
 {
@@ -660,6 +669,9 @@ B2G_API b2JointId b2CreateWheelJoint( b2WorldId worldId, const b2WheelJointDef* 
 B2G_API b2FilterJointDef b2DefaultFilterJointDef( void );
 B2G_API b2MotorJointDef b2DefaultMotorJointDef( void );
 B2G_API b2PogoJointDef b2DefaultPogoJointDef( void );
+/* types.h:773 and box2d.h b2CreateMoverJoint */
+B2G_API b2MoverJointDef b2DefaultMoverJointDef( void );
+B2G_API b2JointId b2CreateMoverJoint( b2WorldId worldId, const b2MoverJointDef* def );
 B2G_API b2JointId b2CreateFilterJoint( b2WorldId worldId, const b2FilterJointDef* def );
 B2G_API b2JointId b2CreateMotorJoint( b2WorldId worldId, const b2MotorJointDef* def );
 B2G_API b2JointId b2CreatePogoJoint( b2WorldId worldId, const b2PogoJointDef* def );

@@ -586,6 +586,14 @@ typedef struct o_motorJoint
 	float angularMass;
 } o_motorJoint;
 
+/* joint.h b2MoverJoint */
+typedef struct o_moverJoint
+{
+	b2Vec2 linearVelocity, maxVelocityForce, linearVelocityImpulse;
+	float linearMass;
+	int indexA, indexB;
+} o_moverJoint;
+
 /* joint.h b2PogoJoint */
 typedef struct o_pogoJoint
 {
@@ -616,6 +624,7 @@ struct o_jointSim
 		o_wheelJoint wheelJoint;
 		o_motorJoint motorJoint;
 		o_pogoJoint pogoJoint;
+		o_moverJoint moverJoint;
 	};
 };
 

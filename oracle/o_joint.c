@@ -306,6 +306,27 @@ b2PogoJointDef b2DefaultPogoJointDef( void )
 	return def;
 }
 
+b2MoverJointDef b2DefaultMoverJointDef( void )
+{
+	b2MoverJointDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.base = o_defaultJointDef();
+	def.internalValue = 1152023;
+	return def;
+}
+
+/* joint.c b2CreateMoverJoint */
+b2JointId b2CreateMoverJoint( b2WorldId worldId, const b2MoverJointDef* def )
+{
+	o_world* w = o_worldFromId( worldId );
+	b2JointId id = { 0, 0, 0 };
+	o_jointSim* j = o_createJoint( w, &def->base, b2_moverJoint, &id );
+	memset( &j->moverJoint, 0, sizeof( j->moverJoint ) );
+	j->moverJoint.linearVelocity = def->linearVelocity;
+	j->moverJoint.maxVelocityForce = def->maxVelocityForce;
+	return id;
+}
+
 /* joint.c:436-459: a graph edge and a colored constraint that does nothing */
 b2JointId b2CreateFilterJoint( b2WorldId worldId, const b2FilterJointDef* def )
 {
@@ -1449,6 +1470,67 @@ static void o_solveMotor( o_world* w, o_stepContext* ctx, o_jointSim* base )
 	}
 }
 
+/* ---------------- mover (mover_joint.c:43-170): linear only, rotation untouched ---------------- */
+static void o_prepareMover( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	int ia, ib;
+	o_bodySim* simA = o_jointBodySim( w, base->bodyIdA, &ia );
+	o_bodySim* simB = o_jointBodySim( w, base->bodyIdB, &ib );
+	float mA = simA->invMass, mB = simB->invMass;
+	base->invMassA = mA;
+	base->invMassB = mB;
+	base->invIA = 0.0f;
+	base->invIB = 0.0f;
+	o_moverJoint* j = &base->moverJoint;
+	j->indexA = ia;
+	j->indexB = ib;
+	float k = mA + mB;
+	j->linearMass = k > 0.0f ? 1.0f / k : 0.0f;
+	if ( ctx->enableWarmStarting == 0 ) j->linearVelocityImpulse = o_v( 0.0f, 0.0f );
+}
+
+static void o_warmStartMover( o_world* w, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB;
+	o_moverJoint* j = &base->moverJoint;
+	o_bodyState dummy = o_dummyState;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	if ( sA->flags & O_DYNAMIC_FLAG ) sA->linearVelocity = o_mulSub( sA->linearVelocity, mA, j->linearVelocityImpulse );
+	if ( sB->flags & O_DYNAMIC_FLAG ) sB->linearVelocity = o_mulAdd( sB->linearVelocity, mB, j->linearVelocityImpulse );
+}
+
+static void o_solveMover( o_world* w, o_stepContext* ctx, o_jointSim* base )
+{
+	float mA = base->invMassA, mB = base->invMassB;
+	o_moverJoint* j = &base->moverJoint;
+	o_bodyState dummy = o_dummyState;
+	o_bodyState* sA = j->indexA == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexA;
+	o_bodyState* sB = j->indexB == B2_NULL_INDEX ? &dummy : w->awakeStates.data + j->indexB;
+	b2Vec2 vA = sA->linearVelocity, vB = sB->linearVelocity;
+	if ( j->maxVelocityForce.x > 0.0f || j->maxVelocityForce.y > 0.0f )
+	{
+		b2Vec2 cdot = o_sub( o_sub( vB, vA ), j->linearVelocity );
+		b2Vec2 b = o_mulSV( j->linearMass, cdot );
+		b2Vec2 impulse = o_v( -b.x, -b.y );
+		b2Vec2 old = j->linearVelocityImpulse;
+		j->linearVelocityImpulse = o_add( j->linearVelocityImpulse, impulse );
+		b2Vec2 maxImpulse = o_mulSV( ctx->h, j->maxVelocityForce );
+		/* x and y clamped separately (math_functions.h b2Clamp) */
+		j->linearVelocityImpulse.x = o_clamp( j->linearVelocityImpulse.x, -maxImpulse.x, maxImpulse.x );
+		j->linearVelocityImpulse.y = o_clamp( j->linearVelocityImpulse.y, -maxImpulse.y, maxImpulse.y );
+		impulse = o_sub( j->linearVelocityImpulse, old );
+		vA = o_mulSub( vA, mA, impulse );
+		vB = o_mulAdd( vB, mB, impulse );
+	}
+	else
+	{
+		j->linearVelocityImpulse = o_v( 0.0f, 0.0f );
+	}
+	if ( sA->flags & O_DYNAMIC_FLAG ) sA->linearVelocity = vA;
+	if ( sB->flags & O_DYNAMIC_FLAG ) sB->linearVelocity = vB;
+}
+
 /* ---------------- pogo (pogo_joint.c:98-281) ---------------- */
 static void o_preparePogo( o_world* w, o_stepContext* ctx, o_jointSim* base )
 {
@@ -1578,6 +1660,7 @@ void o_prepareJoint( o_world* w, o_stepContext* ctx, o_jointSim* j )
 		case b2_wheelJoint: o_prepareWheel( w, ctx, j ); break;
 		case b2_motorJoint: o_prepareMotor( w, ctx, j ); break;
 		case b2_pogoJoint: o_preparePogo( w, ctx, j ); break;
+		case b2_moverJoint: o_prepareMover( w, ctx, j ); break;
 		case b2_filterJoint: break;
 		default: o_unsupportedJoints += 1; break;
 	}
@@ -1595,6 +1678,7 @@ void o_warmStartJoint( o_world* w, o_stepContext* ctx, o_jointSim* j )
 		case b2_wheelJoint: o_warmStartWheel( w, j ); break;
 		case b2_motorJoint: o_warmStartMotor( w, j ); break;
 		case b2_pogoJoint: o_warmStartPogo( w, j ); break;
+		case b2_moverJoint: o_warmStartMover( w, j ); break;
 		default: break;
 	}
 }
@@ -1610,6 +1694,7 @@ void o_solveJoint( o_world* w, o_stepContext* ctx, o_jointSim* j, int useBias )
 		case b2_wheelJoint: o_solveWheel( w, ctx, j, useBias ); break;
 		case b2_motorJoint: o_solveMotor( w, ctx, j ); break;
 		case b2_pogoJoint: o_solvePogo( w, ctx, j, useBias ); break;
+		case b2_moverJoint: o_solveMover( w, ctx, j ); break;
 		default: break;
 	}
 }

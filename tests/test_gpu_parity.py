@@ -59,8 +59,8 @@ def test_gpu_vs_oracle_joint_zoo(gpu_lib, oracle, seed):
 
 @pytest.mark.parametrize("seed", [5, 6])
 def test_gpu_vs_oracle_joint_mix(gpu_lib, oracle, seed):
-    """Motor joints (velocity and spring control, between two dynamic bodies), pogo joints
-    and filter joints, with contacts on the motor-driven bodies."""
+    """Motor joints (velocity and spring control, between two dynamic bodies), pogo,
+    mover and filter joints, with contacts on the motor-driven bodies."""
     _lockstep(gpu_lib, oracle, B.JOINT_MIX, 8, 0, 0, seed, B.NO_CONTINUOUS, 200)
 
 
@@ -71,10 +71,10 @@ def test_gpu_filter_joint_stops_collision(gpu_lib):
         s.step(30)
         table = s.contacts()
     # cell 0: ground segment shape 0, motor box 1, ball 2, friction pair 3-4, pogo mover 5,
-    # filtered pair 6-7 (shape ids in creation order)
+    # mover-walked box 6, filtered pair 7-8 (shape ids in creation order)
     pairs = {tuple(sorted((int(r[1]), int(r[2])))) for r in table}
-    assert (6, 7) not in pairs
-    assert any(6 in p or 7 in p for p in pairs)  # they still touch the ground
+    assert (7, 8) not in pairs
+    assert any(7 in p or 8 in p for p in pairs)  # they still touch the ground
 
 
 def test_gpu_vs_oracle_joint_grid_mixed(gpu_lib, oracle):
