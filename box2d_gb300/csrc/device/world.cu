@@ -235,6 +235,7 @@ struct b2gDeviceWorld
 	/* the host mirrors above hold (or will hold after the next wait) the state as of the
 	   last prefetch, and no device work was issued or recorded since */
 	int prefetchValid, prefetchBodies, prefetchAwake;
+	int prefetchWait; /* the prefetch copies were issued on the world's stream (not delivered by a flush) */
 	float* hSleepTime;
 	int hSleepTimeCap;
 };
@@ -1153,9 +1154,10 @@ extern "C" int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awak
 {
 	if ( dw->prefetchValid && dw->prefetchBodies == bodyCount && dw->prefetchAwake == awakeCount )
 	{
-		/* the step already sent the state down: wait for it */
+		/* the step already sent the state down: wait for it (a batched step's flush has
+		   delivered it already) */
 		dw->prefetchValid = 0;
-		CK2( drain( dw ) );
+		if ( dw->prefetchWait ) CK2( drain( dw ) );
 		*xf = (const float*)dw->hXf;
 		*center = (const float*)dw->hCenter;
 		*flags = dw->hFlags;
@@ -1214,6 +1216,7 @@ extern "C" int b2gDev_PrefetchState( b2gDeviceWorld* dw, int bodyCount, int awak
 		CK2( dev_d2h( dw, dw->hSleepTime, dw->sleepTime, (size_t)awakeCount * sizeof( float ) ) );
 	}
 	dw->prefetchValid = 1;
+	dw->prefetchWait = dw->defer == NULL;
 	dw->prefetchBodies = bodyCount;
 	dw->prefetchAwake = awakeCount;
 	return 0;

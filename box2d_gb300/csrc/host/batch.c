@@ -151,6 +151,13 @@ static void h_phaseFinishWorld( h_lockstep* L, int i )
 	h_stepFinish( w );
 }
 
+static void h_phaseEvents( void* ctx, int i )
+{
+	h_lockstep* L = ctx;
+	h_world* w = L->worlds[i];
+	if ( w->moveEventsValid == 0 && w->stepIndex > 0 ) h_buildMoveEvents( w );
+}
+
 static pthread_mutex_t h_batchMu = PTHREAD_MUTEX_INITIALIZER;
 static b2gDevBatch* h_batchDevice = NULL;
 
@@ -242,6 +249,11 @@ void b2World_StepBatch( const b2WorldId* worldIds, int worldCount, float timeSte
 		}
 		h_batchFlushLaunches = b2gDev_BatchLaunches( h_batchDevice );
 		for ( int i = 0; i < n; ++i ) b2gDev_BatchRecord( devs[i], 0 );
+		/* the move events of every world, from the state the last flush delivered, as the
+		   reference's finalize builds them inside the step */
+		uint64_t t0 = b2GetTicks();
+		h_poolRun( threads, h_phaseEvents, &L, n );
+		h_batchMs[3] += b2GetMilliseconds( t0 );
 		pthread_mutex_unlock( &h_batchMu );
 	}
 	free( worlds );
