@@ -68,7 +68,8 @@ def test_mixed_batch_equals_single_steps(gpu_lib, mode, flags):
     batched flush), a jointed world, and a pyramid too heavy for one CTA (solved on its own
     stream in the last phase)."""
     specs = [(B.BATCH_WORLD, 0, 0, 0, s) for s in range(201, 213)]
-    specs += [(B.JOINT_ZOO, 4, 0, 0, 3), (B.SHAPE_ZOO, 60, 0, 0, 4), (B.LARGE_PYRAMID, 40, 0, 0, 0)]
+    specs += [(B.JOINT_ZOO, 4, 0, 0, 3), (B.JOINT_MIX, 3, 0, 0, 6), (B.SHAPE_ZOO, 60, 0, 0, 4),
+              (B.LARGE_PYRAMID, 40, 0, 0, 0)]
     batch = [B.Scene(gpu_lib, k, a, b, c, seed, flags) for k, a, b, c, seed in specs]
     single = [B.Scene(gpu_lib, k, a, b, c, seed, flags) for k, a, b, c, seed in specs]
     old = os.environ.get("B2G_BATCH")
