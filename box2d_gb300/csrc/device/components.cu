@@ -117,6 +117,15 @@ __global__ void k_compUnion( d_solveArgs a, const int* awakeIndex, int* parent, 
 	if ( ia >= 0 && ib >= 0 ) d_unite( parent, ia, ib );
 }
 
+/* one atomic add of `1` per distinct address in the warp: lanes with the same address
+   combine, and the lowest of them adds their count (a big component otherwise sends every
+   one of its bodies or constraints to the same counter) */
+static __device__ __forceinline__ void d_warpCountAdd( int* counter )
+{
+	unsigned peers = __match_any_sync( __activemask(), (unsigned long long)(uintptr_t)counter );
+	if ( ( threadIdx.x & 31 ) == __ffs( peers ) - 1 ) atomicAdd( counter, __popc( peers ) );
+}
+
 /* the root goes to its own field: path halving by other threads may still rewrite parent[i]
    with a non-root ancestor during this kernel */
 __global__ void k_compRoots( int* parent, int* compData, int n )
@@ -124,7 +133,7 @@ __global__ void k_compRoots( int* parent, int* compData, int n )
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if ( i >= n ) return;
 	int r = d_find( parent, i );
-	atomicAdd( compData + CD_STRIDE * r + CD_COUNT, 1 );
+	d_warpCountAdd( compData + CD_STRIDE * r + CD_COUNT );
 	compData[CD_STRIDE * i + CD_ROOT] = r;
 }
 
@@ -137,7 +146,7 @@ __global__ void k_compCountCons( d_solveArgs a, const int* awakeIndex, int* comp
 	int x = ia >= 0 ? ia : ib;
 	if ( x < 0 ) return;
 	int r = compData[CD_STRIDE * x + CD_ROOT];
-	atomicAdd( compData + CD_STRIDE * r + ( i < total ? 1 : 2 ), 1 );
+	d_warpCountAdd( compData + CD_STRIDE * r + ( i < total ? 1 : 2 ) );
 }
 
 __global__ void k_compAssign( int* compData, int* binRange, int binCap, b2gCompSummary* summary, int n, int forceBig )
