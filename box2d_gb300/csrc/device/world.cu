@@ -2647,7 +2647,8 @@ struct d_flushCtx
 	b2gDevBatch* b;
 	b2gDeviceWorld* const* worlds;
 	d_worldFlush* plan;
-	const d_levelPlan* levels;
+	d_levelPlan* levels;
+	int count;
 };
 
 static bool d_isCopy( int kind ) { return kind != D_OP_KERNEL; }
@@ -2680,6 +2681,37 @@ static void d_planWorld( void* ctx, int w )
 	}
 	P.slot.assign( P.unitEnd.size(), 0 );
 	P.blockBase.assign( P.unitEnd.size(), 0 );
+}
+
+/* layout, per level: the level's table sizes and every world's slot in them */
+static void d_layoutLevel( void* ctx, int l )
+{
+	const d_flushCtx* c = (const d_flushCtx*)ctx;
+	d_levelPlan& L = c->levels[l];
+	for ( int w = 0; w < c->count; ++w )
+	{
+		const d_deferred* d = c->worlds[w]->defer;
+		d_worldFlush& P = c->plan[w];
+		if ( d == NULL || (size_t)l >= P.unitEnd.size() ) continue;
+		int begin = l > 0 ? P.unitEnd[(size_t)l - 1] : 0;
+		const d_deferredOp& op = d->ops[(size_t)begin];
+		if ( d_isCopy( op.kind ) )
+		{
+			P.slot[(size_t)l] = L.copyCount;
+			L.copyCount += P.unitEnd[(size_t)l] - begin;
+		}
+		else if ( op.kernel == DK_SOLVE_BIN )
+		{
+			P.slot[(size_t)l] = L.recCount[DK_SOLVE_BIN]++;
+			L.smem = op.smem > L.smem ? op.smem : L.smem;
+		}
+		else
+		{
+			P.slot[(size_t)l] = L.recCount[op.kernel]++;
+			P.blockBase[(size_t)l] = L.blocks[op.kernel];
+			L.blocks[op.kernel] += op.grid;
+		}
+	}
 }
 
 /* pass 2, per world: upload bytes and kernel arguments into the pinned staging, and the
@@ -2786,7 +2818,7 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 	double t0 = d_nowMs();
 	if ( b->plans.size() < (size_t)n ) b->plans.resize( (size_t)n );
 	d_worldFlush* plan = b->plans.data();
-	d_flushCtx fc = { b, worlds, plan, NULL };
+	d_flushCtx fc = { b, worlds, plan, NULL, n };
 	pf( pool, n, d_planWorld, &fc );
 	double tPlan = d_nowMs();
 	b->partMs[0] += tPlan - t0;
@@ -2812,38 +2844,12 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 	const long long tableBase = at;
 	CK2( d_reserve( &b->hDown, &b->dDown, &b->downCap, down > 0 ? down : 16 ) );
 	/* each world's place in every level's tables, in world order (kernel records stay
-	   sorted by their first block) */
+	   sorted by their first block); the levels are independent, one task each */
 	std::vector<d_levelPlan> plans( levels );
 	for ( size_t l = 0; l < levels; ++l ) memset( &plans[l], 0, sizeof( d_levelPlan ) );
-	for ( int w = 0; w < n; ++w )
-	{
-		const d_deferred* d = worlds[w]->defer;
-		if ( d == NULL ) continue;
-		d_worldFlush& P = plan[w];
-		int begin = 0;
-		for ( size_t l = 0; l < P.unitEnd.size(); ++l )
-		{
-			d_levelPlan& L = plans[l];
-			const d_deferredOp& op = d->ops[(size_t)begin];
-			if ( d_isCopy( op.kind ) )
-			{
-				P.slot[l] = L.copyCount;
-				L.copyCount += P.unitEnd[l] - begin;
-			}
-			else if ( op.kernel == DK_SOLVE_BIN )
-			{
-				P.slot[l] = L.recCount[DK_SOLVE_BIN]++;
-				L.smem = op.smem > L.smem ? op.smem : L.smem;
-			}
-			else
-			{
-				P.slot[l] = L.recCount[op.kernel]++;
-				P.blockBase[l] = L.blocks[op.kernel];
-				L.blocks[op.kernel] += op.grid;
-			}
-			begin = P.unitEnd[l];
-		}
-	}
+	fc.levels = plans.data();
+	fc.count = n;
+	pf( pool, (int)levels, d_layoutLevel, &fc );
 	long long total = tableBase;
 	for ( size_t l = 0; l < levels; ++l )
 	{
@@ -2858,7 +2864,6 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 		}
 	}
 	CK2( d_reserve( &b->hBlob, &b->dBlob, &b->blobCap, total ) );
-	fc.levels = plans.data();
 	double tLayout = d_nowMs();
 	b->partMs[1] += tLayout - tPlan;
 	pf( pool, n, d_stageWorld, &fc );
