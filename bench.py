@@ -14,8 +14,13 @@ library's stream, and L2 is flushed (a 256 MiB write) between timed steps, outsi
 dominant device stage: algorithmic bytes from the reference data layout
 (S*(120 Nb + 708 Nc + 604 Nj) + 364 Nc per step; +260 Nc with restitution) over its
 CUDA-event time, against the measured HBM copy bandwidth.
-`cpu_baseline` times the CPU oracle (a serial restatement of the reference step) on a
-bounded sample of the same workload on this machine's host.
+`cpu_baseline` times the reference itself -- its own sources compiled on this machine
+(oracle/_ref/libref.so, Release flags, the SIMD its core.h picks) with its built-in
+scheduler on one worker per host core -- on a bounded sample of the same workload, and
+`cpu_port` the CPU oracle (the C restatement) beside it. Where the reference build is
+missing the oracle stands in and `cpu_baseline.kind` says "port".
+`pose_error` compares the GPU world with the reference world after the same number of
+steps (the end of the timed window): largest position and rotation difference.
 
 --impl reference runs that CPU step alone with the same line format.
 Multi-GPU: independent replicas per rank (the step of one world does not shard).
@@ -159,6 +164,7 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     stage_ms, traffic = scene.timings(reset=True)
     host_ms = scene.host_profile(reset=True)
+    window_state = scene.state()  # at the end of the timed window, for the CPU comparison
     total_ms = float(sum(step_ms))
     solver_ms = float(stage_ms[2])
     launches = int(traffic[2])
@@ -190,7 +196,7 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
         "e2e_d2h": float(e2e_traffic[1]) / e2e_steps, "counters": counters.tolist(),
         "stage_ms": stage_ms.tolist(), "desc": desc, "counters_before": counters_before.tolist(),
         "host_ms": host_ms.tolist(), "e2e_step_ms": 1e3 * step_s / e2e_steps,
-        "e2e_read_ms": 1e3 * (e2e_s - step_s) / e2e_steps,
+        "e2e_read_ms": 1e3 * (e2e_s - step_s) / e2e_steps, "window_state": window_state,
     }
 
 
@@ -206,18 +212,28 @@ def run_batch(args) -> dict:
     torch.cuda.set_device(0)
     lib = B.load_library()
     n = args.worlds
-    scenes = [B.Scene(lib, B.BATCH_WORLD, 0, 0, 0, 12345 + i, 0) for i in range(n)]
-    handles = (ctypes.c_int * n)(*[s.handle for s in scenes])
-    dyn = sum(s.dynamic_count for s in scenes)
     threads = args.threads if args.threads > 0 else 4 * max(1, os.cpu_count() or 1)
     dt = 1.0 / 60.0
+
+    def make_worlds():
+        return [B.Scene(lib, B.BATCH_WORLD, 0, 0, 0, 12345 + i, 0) for i in range(n)]
+
+    # the plain per-world loop: b2World_Step on each world in turn, over the same window
+    # (warm-up steps, then `steps` timed) as the batched run below, on worlds built anew
+    scenes = make_worlds()
+    handles = (ctypes.c_int * n)(*[s.handle for s in scenes])
     lib.b2s_step_batch(handles, n, dt, 4, args.warmup, threads)
-    # the plain per-world loop: b2World_Step on each world in turn
-    plain_steps = max(1, min(args.steps, 5))
+    plain_steps = args.steps
     t0 = time.perf_counter()
     for s in scenes:
         s.step(plain_steps)
     plain_s = time.perf_counter() - t0
+    for s in scenes:
+        s.close()
+    scenes = make_worlds()
+    handles = (ctypes.c_int * n)(*[s.handle for s in scenes])
+    dyn = sum(s.dynamic_count for s in scenes)
+    lib.b2s_step_batch(handles, n, dt, 4, args.warmup, threads)
     for s in scenes:
         s.timings(reset=True)
     prof = np.zeros(17, np.float32)
@@ -228,6 +244,8 @@ def run_batch(args) -> dict:
         lib.b2s_step_batch(handles, n, dt, 4, args.steps, threads)
         batch_s = time.perf_counter() - t0
     lib.b2p_batch_profile(prof.ctypes.data, 1)
+    # state of the first worlds after warm-up + timed steps, for the CPU comparison
+    states = {i: scenes[i].state() for i in range(min(n, 120))}
     h2d = d2h = 0
     for s in scenes:
         _, traffic = s.timings(reset=True)
@@ -250,7 +268,7 @@ def run_batch(args) -> dict:
         s.close()
     return {"dyn": dyn, "batch_s": batch_s, "plain_s": plain_s, "plain_steps": plain_steps, "threads": threads,
             "launches": launches, "h2d": h2d / args.steps, "d2h": d2h / args.steps, "clocks": clocks.summary,
-            "e2e_value": dyn * e2e_steps / e2e_s, "profile": profile}
+            "e2e_value": dyn * e2e_steps / e2e_s, "profile": profile, "states": states}
 
 
 def run_diff(args) -> dict:
@@ -326,56 +344,124 @@ def run_diff(args) -> dict:
             "finite": finite, "profile": profile}
 
 
-def run_cpu_batch(args, budget_s: float, max_steps: int) -> dict:
-    """The oracle on a sample of the batched workload's worlds (the first `sample` seeds),
-    every host core stepping whole worlds in parallel, as a batch of independent reference
-    worlds would run on a CPU. ctypes releases the interpreter lock during each call."""
+REF_LIB = ROOT / "oracle" / "_ref" / "libref.so"
+ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
+
+
+def cpu_impl() -> str:
+    """'reference' when the reference build exists on this machine, else 'port' (oracle)."""
+    return "reference" if REF_LIB.exists() else "port"
+
+
+def cpu_threads() -> int:
+    # the reference caps its worker count at B2_MAX_WORKERS = 32 (constants.h:18)
+    return max(1, min(os.cpu_count() or 1, 32))
+
+
+def _cpu_lib(impl: str):
+    import ctypes
+
+    lib = B.load_library(REF_LIB if impl == "reference" else ORACLE_LIB)
+    if impl == "port":
+        lib.b2o_set_threads.argtypes = [ctypes.c_int]
+    return lib
+
+
+def pose_error(a: np.ndarray, b: np.ndarray) -> dict:
+    """Largest position (m) and rotation (cos/sin component) difference between two
+    b2s_get_state snapshots, and whether the snapshots are bit-identical."""
+    dp = float(np.abs(a[:, 0:2].astype(np.float64) - b[:, 0:2]).max()) if a.size else 0.0
+    dq = float(np.abs(a[:, 2:4].astype(np.float64) - b[:, 2:4]).max()) if a.size else 0.0
+    return {"max_position_m": dp, "max_rotation": dq, "bit_exact": bool(a.tobytes() == b.tobytes())}
+
+
+def run_cpu_batch(args, budget_s: float, max_steps: int, impl: str, gpu_states=None) -> dict:
+    """A CPU library on a sample of the batched workload's worlds (the first `sample` seeds),
+    every host core stepping whole worlds in parallel, one world per task (each world
+    single-threaded), as a batch of independent worlds runs on a CPU. ctypes releases the
+    interpreter lock during each call. `gpu_states` (world index -> b2s_get_state after
+    warm-up + steps) are compared with the CPU worlds after the same number of steps."""
     from concurrent.futures import ThreadPoolExecutor
 
     kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
-    lib = B.load_library(ROOT / "oracle" / "liboracle.so")
-    threads = max(1, os.cpu_count() or 1)
-    sample = min(args.worlds, 16 * threads, 120)  # the oracle holds at most 128 worlds
+    lib = _cpu_lib(impl)
+    if impl == "port":
+        lib.b2o_set_threads(1)
+    threads = cpu_threads()
+    sample = min(args.worlds, 16 * threads, 120)  # both CPU libraries hold at most 128 worlds
     scenes = [B.Scene(lib, kind, a, b, c, seed + i, flags) for i in range(sample)]
     dyn = sum(s.dynamic_count for s in scenes)
+    err = None
     with ThreadPoolExecutor(threads) as ex:
         list(ex.map(lambda s: s.step(max(1, args.warmup)), scenes))
         t0 = time.perf_counter()
         n = 0
+        paused = 0.0
         while n < max_steps and time.perf_counter() - t0 < budget_s:
             list(ex.map(lambda s: s.step(), scenes))
             n += 1
-        dt = time.perf_counter() - t0
+            if gpu_states is not None and n == args.steps:
+                t1 = time.perf_counter()
+                errs = [pose_error(gpu_states[i], scenes[i].state()) for i in range(sample) if i in gpu_states]
+                if errs:
+                    err = {"max_position_m": max(e["max_position_m"] for e in errs),
+                           "max_rotation": max(e["max_rotation"] for e in errs),
+                           "bit_exact": all(e["bit_exact"] for e in errs), "worlds": len(errs)}
+                paused += time.perf_counter() - t1
+        dt = time.perf_counter() - t0 - paused
     for s in scenes:
         s.close()
-    return {"value": dyn * n / dt, "steps": n, "seconds": dt, "dyn": dyn, "threads": threads, "worlds": sample}
+    return {"value": dyn * n / dt, "steps": n, "seconds": dt, "dyn": dyn, "threads": threads, "worlds": sample,
+            "pose_error": err}
 
 
-def run_cpu_sample(args, budget_s: float, max_steps: int) -> dict:
-    """The oracle (CPU restatement of the reference step) on the same workload, with its
-    data-parallel loops (narrowphase, solver stages, integration, finalize) on every host
-    core, as the reference runs them on its worker threads."""
-    import ctypes
-
+def run_cpu_sample(args, budget_s: float, max_steps: int, impl: str, gpu_state=None) -> dict:
+    """A CPU library on the same workload, bounded by `max_steps` and `budget_s`:
+    impl 'reference' -- the reference build with its built-in scheduler on one worker per
+    host core (b2WorldDef.workerCount; physics_world.c:307-314); impl 'port' -- the oracle
+    with its data-parallel loops on every host core. Timing starts after the same untimed
+    steps as the GPU run's timed window; `gpu_state` (b2s_get_state at the window's end) is
+    compared with the CPU world after the same step count, outside the timed region."""
     kind, a, b, c, seed, flags, desc = WORKLOADS[args.workload]
-    lib = B.load_library(ROOT / "oracle" / "liboracle.so")
-    threads = max(1, os.cpu_count() or 1)
-    lib.b2o_set_threads.argtypes = [ctypes.c_int]
-    lib.b2o_set_threads(threads)
+    lib = _cpu_lib(impl)
+    threads = cpu_threads()
+    if impl == "reference":
+        lib.b2s_set_workers(threads)
+    else:
+        lib.b2o_set_threads(threads)
     scene = B.Scene(lib, kind, a, b, c, seed, flags)
+    if impl == "reference":
+        lib.b2s_set_workers(0)
     scene.step(args.start_step)
-    for _ in range(max(1, args.warmup)):
+    for _ in range(args.warmup):
         scene.step()
+    err = None
     t0 = time.perf_counter()
     n = 0
+    paused = 0.0
     while n < max_steps and time.perf_counter() - t0 < budget_s:
         scene.step()
         n += 1
-    dt = time.perf_counter() - t0
+        if gpu_state is not None and n == args.steps:
+            t1 = time.perf_counter()
+            err = pose_error(gpu_state, scene.state())
+            err["step"] = args.start_step + args.warmup + args.steps
+            paused += time.perf_counter() - t1
+    dt = time.perf_counter() - t0 - paused
     dyn = scene.dynamic_count
     scene.close()
-    lib.b2o_set_threads(1)
-    return {"value": dyn * n / dt, "steps": n, "seconds": dt, "dyn": dyn, "threads": threads}
+    if impl == "port":
+        lib.b2o_set_threads(1)
+    return {"value": dyn * n / dt, "steps": n, "seconds": dt, "dyn": dyn, "threads": threads, "pose_error": err}
+
+
+def cpu_description(impl: str, threads: int, batched: bool) -> str:
+    if impl == "reference":
+        who = ("the reference built from its sources (-O3, NEON/SSE2 as its core.h selects), "
+               + ("one single-threaded world per task" if batched else "built-in scheduler, workerCount"))
+    else:
+        who = "C oracle (restatement of the reference step)" + (", one world per task" if batched else "")
+    return f"{who} on {threads} threads"
 
 
 def main() -> None:
@@ -413,17 +499,23 @@ def main() -> None:
         if rank != 0:
             return
         batched = args.workload in ("batch_worlds", "diff_batch")
-        r = run_cpu_batch(args, 60.0, args.steps) if batched else run_cpu_sample(args, budget_s=60.0, max_steps=args.steps)
+        impl = cpu_impl()
+        if batched:
+            r = run_cpu_batch(args, 60.0, args.steps, impl)
+            sample = f"{r['steps']} steps of {r['worlds']} worlds after {args.warmup} untimed steps"
+        else:
+            r = run_cpu_sample(args, budget_s=60.0, max_steps=args.steps, impl=impl)
+            sample = f"{r['steps']} steps after {args.start_step + args.warmup} untimed steps"
         cores = r["threads"]
-        sample = (f"{r['steps']} steps of {r['worlds']} worlds, one world per task on {cores} threads, C oracle"
-                  if batched else
-                  f"{r['steps']} steps after {args.start_step + args.warmup} untimed steps, C oracle on {cores} threads")
+        sample += ", " + cpu_description(impl, cores, batched)
         line = {"metric": "body-steps/s", "value": r["value"], "unit": "body-steps/s", "n_gpus": args.gpus,
                 "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / max(1, r["steps"]),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded scene builders)", "config": config, "impl": "reference",
-                "cpu_baseline": {"value": r["value"], "unit": "body-steps/s", "cores": cores, "kind": "port",
-                                 "sample": sample},
+                "cpu_baseline": {"value": r["value"], "unit": "body-steps/s", "cores": cores, "kind": impl,
+                                 "sample": sample,
+                                 "library": str(REF_LIB.relative_to(ROOT)) if impl == "reference" else
+                                 str(ORACLE_LIB.relative_to(ROOT))},
                 "e2e": {"value": r["value"], "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -438,11 +530,12 @@ def main() -> None:
         achieved = r["tape_bytes"] / (r["adj_ms"] * 1e-3) / 1e9 if r["adj_ms"] > 0 else 0.0
         cpu = None
         if not args.no_cpu_baseline:
-            c = run_cpu_batch(args, 20.0, args.steps)
+            impl = cpu_impl()
+            c = run_cpu_batch(args, 20.0, args.steps, impl)
             cpu = {"value": c["value"], "unit": "body-steps/s (forward only: the reference has no adjoint)",
-                   "cores": c["threads"], "kind": "port",
-                   "sample": f"{c['steps']} forward steps of {c['worlds']} ramp worlds, one world per task on "
-                             f"{c['threads']} threads, C oracle"}
+                   "cores": c["threads"], "kind": impl,
+                   "sample": f"{c['steps']} forward steps of {c['worlds']} ramp worlds, "
+                             + cpu_description(impl, c["threads"], True)}
         config.update({"worlds": args.worlds, "host_threads": r["threads"], "steps_per_pass": args.steps,
                        "l2": "inputs larger than L2 (every world's tape), no flush",
                        "timing": "wall clock of the forward pass (recording) and of the adjoint through the public API"})
@@ -471,11 +564,14 @@ def main() -> None:
             return
         r = run_batch(args)
         r["cpu"] = None
+        r["pose_error"] = None
         if not args.no_cpu_baseline:
-            c = run_cpu_batch(args, 20.0, args.steps)
-            r["cpu"] = {"value": c["value"], "unit": "body-steps/s", "cores": c["threads"], "kind": "port",
-                        "sample": f"{c['steps']} steps of {c['worlds']} worlds, one world per task on "
-                                  f"{c['threads']} threads, C oracle"}
+            impl = cpu_impl()
+            c = run_cpu_batch(args, 20.0, args.steps, impl, gpu_states=r["states"])
+            r["cpu"] = {"value": c["value"], "unit": "body-steps/s", "cores": c["threads"], "kind": impl,
+                        "sample": f"{c['steps']} steps of {c['worlds']} worlds after {args.warmup} untimed steps, "
+                                  + cpu_description(impl, c["threads"], True)}
+            r["pose_error"] = c["pose_error"]
         value = r["dyn"] * args.steps / r["batch_s"]
         plain = r["dyn"] * r["plain_steps"] / r["plain_s"]
         config.update({"worlds": args.worlds, "host_threads": r["threads"],
@@ -487,6 +583,8 @@ def main() -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene builders)",
             "config": config, "plain_loop": {"value": plain, "steps": r["plain_steps"], "speedup": value / plain},
             "roofline": None, "cpu_baseline": r["cpu"],
+            "pose_error": r["pose_error"] and dict(r["pose_error"], against=r["cpu"]["kind"],
+                                                   after_steps=args.warmup + args.steps),
             "e2e": {"value": r["e2e_value"], "unit": "body-steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "read": "every world's move events after every batched step"},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
@@ -511,12 +609,19 @@ def main() -> None:
     if rank != 0:
         return
     value = world_size * r["dyn"] * args.steps / (total_ms * 1e-3)
-    cpu = None
+    cpu = port = err = None
     if not args.no_cpu_baseline:
-        c = run_cpu_sample(args, budget_s=20.0, max_steps=400)
-        cpu = {"value": c["value"], "unit": "body-steps/s", "cores": c["threads"], "kind": "port",
+        impl = cpu_impl()
+        c = run_cpu_sample(args, budget_s=20.0, max_steps=400, impl=impl, gpu_state=r["window_state"])
+        cpu = {"value": c["value"], "unit": "body-steps/s", "cores": c["threads"], "kind": impl,
                "sample": f"{c['steps']} steps ({c['seconds']:.1f} s) of the same world after "
-                         f"{args.start_step + args.warmup} untimed steps, C oracle on {c['threads']} threads"}
+                         f"{args.start_step + args.warmup} untimed steps, " + cpu_description(impl, c["threads"], False)}
+        err = c["pose_error"] and dict(c["pose_error"], against=impl)
+        if impl == "reference":
+            o = run_cpu_sample(args, budget_s=10.0, max_steps=400, impl="port", gpu_state=r["window_state"])
+            port = {"value": o["value"], "unit": "body-steps/s", "cores": o["threads"], "kind": "port",
+                    "sample": f"{o['steps']} steps ({o['seconds']:.1f} s), " + cpu_description("port", o["threads"], False),
+                    "pose_error": o["pose_error"]}
     pk = r["peak"]
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": world_size, "steps": args.steps,
@@ -528,6 +633,8 @@ def main() -> None:
                      "alg_bytes_per_step": r["alg_bytes"] / args.steps,
                      "solver_ms_per_step": r["solver_ms"] / args.steps},
         "cpu_baseline": cpu,
+        "cpu_port": port,
+        "pose_error": err,
         "e2e": {"value": r["e2e_value"] * world_size, "unit": "body-steps/s", "h2d_bytes_per_step": r["e2e_h2d"],
                 "d2h_bytes_per_step": r["e2e_d2h"], "step_ms": r["e2e_step_ms"], "read_ms": r["e2e_read_ms"],
                 "read": "b2World_GetBodyEvents after every step (transforms of all awake bodies)"},

@@ -31,6 +31,7 @@ JOINT_ZOO = 9
 FALLING_HINGES = 10
 SLEEP_PYRAMIDS = 11
 JOINT_MIX = 12
+OVERFLOW = 13
 
 NO_CONTINUOUS = 1
 NO_WARM_STARTING = 2
@@ -61,6 +62,8 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     }
     optional = {
         "b2s_set_body_velocity": (None, [c_int, c_int, c_f, c_f, c_f]),
+        "b2s_set_workers": (None, [c_int]),
+        "b2s_contact_events": (c_int, [c_int, c_p, c_int]),
         "b2s_set_awake": (None, [c_int, c_int, c_int]),
         "b2s_enable_sleep": (None, [c_int, c_int]),
         "b2p_timings": (c_int, [c_u32, c_p, c_p, c_int]),
@@ -154,6 +157,17 @@ class Scene:
         while True:
             buf = np.zeros((cap, 12), np.float32)
             n = self.lib.b2p_contact_floats(self.world_id, buf.ctypes.data, cap)
+            if n <= cap:
+                return buf[:n]
+            cap = n
+
+    def contact_events(self) -> np.ndarray:
+        """The last step's contact begin/end touch events, one row each: kind (0 begin,
+        1 end), shape A, shape B, contact id, contact generation."""
+        cap = 4096
+        while True:
+            buf = np.zeros((cap, 5), np.int32)
+            n = self.lib.b2s_contact_events(self.handle, buf.ctypes.data, cap)
             if n <= cap:
                 return buf[:n]
             cap = n

@@ -85,16 +85,24 @@ def build_library(force: bool = False) -> Path:
 
 
 def build_oracle(with_reference: bool = True) -> None:
-    """Build the CPU oracle and, where the reference sources exist, the reference itself."""
-    _run(["make", "-s", "-C", str(ROOT / "oracle"), "liboracle.so", "libtangent.so"])
-    ref = Path(os.environ.get("B2G_REFERENCE_DIR", "/root/reference"))
-    if with_reference and (ref / "src").is_dir():
-        _run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={ref}"])
+    """Build the CPU oracle and, where the reference sources can be found (its checkout, or
+    the git-ignored copy the oracle Makefile stages beside the repository), the reference
+    itself. The checkout's location comes from the Makefile, or B2G_REFERENCE_DIR."""
+    oracle = ROOT / "oracle"
+    _run(["make", "-s", "-C", str(oracle), "liboracle.so", "libtangent.so"])
+    if with_reference:
+        ref = os.environ.get("B2G_REFERENCE_DIR")
+        extra = [f"REF={ref}"] if ref else []
+        _run(["make", "-s", "-C", str(oracle), "stage", *extra])
+        _run(["make", "-s", f"-j{max(2, os.cpu_count() or 2)}", "-C", str(oracle), "ref", *extra])
 
 
 def build_all(force: bool = False) -> None:
-    build_library(force)
-    build_oracle()
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        lib = ex.submit(build_library, force)
+        orc = ex.submit(build_oracle)
+        lib.result()
+        orc.result()
 
 
 if __name__ == "__main__":

@@ -388,7 +388,9 @@ void h_buildMoveEvents( h_world* w )
 b2ContactEvents b2World_GetContactEvents( b2WorldId worldId )
 {
 	h_world* w = h_worldFromId( worldId );
-	int endIndex = w->endEventArrayIndex;
+	/* the step flips the end-event buffers when it ends: the events of the last step (and of
+	   changes made before it) are in the previous buffer (physics_world.c:1486-1487) */
+	int endIndex = 1 - w->endEventArrayIndex;
 	b2ContactEvents e;
 	memset( &e, 0, sizeof( e ) );
 	e.beginEvents = w->beginEvents.data;

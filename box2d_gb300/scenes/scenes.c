@@ -459,6 +459,7 @@ static void b2sShapeZoo( b2sScene* s, int count, b2sRng* rng )
 		b2ShapeDef sd = b2DefaultShapeDef();
 		sd.material.friction = b2sRandomFloatRange( rng, 0.1f, 0.9f );
 		sd.material.restitution = b2sRandomFloatRange( rng, 0.0f, 0.4f );
+		sd.enableContactEvents = ( k & 1 ) == 0; /* begin/end touch events for half the shapes */
 		int kind = b2sRandomIntRange( rng, 0, 3 );
 		if ( kind == 0 )
 		{
@@ -884,6 +885,60 @@ static void b2sSleepPyramids( b2sScene* s, int pyramidCount, int rows, int dropH
 	b2CreatePolygonShape( drop, &sd, &box );
 }
 
+/* Overflow scene: bodies with more constraints than the graph has colors, so the solver's
+   overflow path (constraints past the colors, solved one by one before the colors in each
+   stage; contact_solver.c:24-545, joint.c:1542-1591) runs. Per cell: a 24 m plank resting
+   on the ground under 40 small boxes (40 dynamic-vs-dynamic contacts on one body: the
+   first 20 get the 20 dynamic colors, the rest overflow; every other box has restitution),
+   and a hub falling with 28 satellites held by distance joints (28 joints on one body). */
+static void b2sOverflowScene( b2sScene* s, int count, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, -1.0f );
+	{
+		b2ShapeDef sd = b2DefaultShapeDef();
+		b2Polygon box = b2MakeOffsetBox( 40.0f * count + 20.0f, 1.0f, ( b2Vec2 ){ 20.0f * count, 0.0f }, b2MakeRot( 0.0f ) );
+		b2CreatePolygonShape( ground, &sd, &box );
+	}
+	for ( int k = 0; k < count; ++k )
+	{
+		float x0 = 40.0f * k;
+		b2ShapeDef sd = b2DefaultShapeDef();
+		b2BodyId plank = b2sBody( s, b2_dynamicBody, x0, 0.25f );
+		b2Polygon p = b2MakeBox( 12.0f, 0.25f );
+		b2CreatePolygonShape( plank, &sd, &p );
+		b2Polygon small = b2MakeBox( 0.25f, 0.25f );
+		for ( int i = 0; i < 40; ++i )
+		{
+			float jitter = b2sRandomFloatRange( rng, -0.02f, 0.02f );
+			b2BodyId b = b2sBody( s, b2_dynamicBody, x0 - 10.75f + 0.55f * i + jitter, 0.76f );
+			b2ShapeDef bs = b2DefaultShapeDef();
+			bs.material.restitution = ( i & 1 ) ? 0.3f : 0.0f;
+			bs.enableContactEvents = true;
+			b2CreatePolygonShape( b, &bs, &small );
+		}
+		float hx = x0 + b2sRandomFloatRange( rng, -1.0f, 1.0f ), hy = 9.0f;
+		b2BodyId hub = b2sBody( s, b2_dynamicBody, hx, hy );
+		b2Circle hc = { { 0.0f, 0.0f }, 0.5f };
+		b2CreateCircleShape( hub, &sd, &hc );
+		for ( int i = 0; i < 28; ++i )
+		{
+			float angle = 6.2831853f * (float)i / 28.0f + b2sRandomFloatRange( rng, -0.05f, 0.05f );
+			b2CosSin cs = b2ComputeCosSin( angle );
+			b2BodyId sat = b2sBody( s, b2_dynamicBody, hx + 2.5f * cs.cosine, hy + 2.5f * cs.sine );
+			b2Circle c = { { 0.0f, 0.0f }, 0.15f };
+			b2CreateCircleShape( sat, &sd, &c );
+			b2DistanceJointDef jd = b2DefaultDistanceJointDef();
+			jd.base = b2sJointBase( hub, sat, 0.0f, 0.0f, 0.0f, 0.0f );
+			jd.length = 2.5f;
+			jd.enableSpring = ( i % 3 ) == 0;
+			jd.hertz = 4.0f;
+			jd.dampingRatio = 0.5f;
+			b2CreateDistanceJoint( s->worldId, &jd );
+		}
+	}
+}
+
 enum
 {
 	B2S_LARGE_PYRAMID = 0,
@@ -899,7 +954,18 @@ enum
 	B2S_FALLING_HINGES = 10,
 	B2S_SLEEP_PYRAMIDS = 11,
 	B2S_JOINT_MIX = 12,
+	B2S_OVERFLOW = 13,
 };
+
+/* Worker threads requested in the world definition of scenes created from now on (0 keeps
+   the default). A library with a built-in task system (the reference: workerCount > 1
+   starts its scheduler, physics_world.c:307-314) uses them; the GB300 library ignores it. */
+static int b2s_workerCount = 0;
+
+B2S_EXPORT void b2s_set_workers( int count )
+{
+	b2s_workerCount = count > 0 ? count : 0;
+}
 
 /* Create a scene. kind selects the builder; a, b, c are its size parameters; seed feeds
    the random stream (0 means 12345). flags bit 0 disables continuous collision.
@@ -919,6 +985,7 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 	b2sScene* s = b2s_scenes + h;
 	memset( s, 0, sizeof( *s ) );
 	b2WorldDef wd = b2DefaultWorldDef();
+	if ( b2s_workerCount > 0 ) wd.workerCount = b2s_workerCount;
 	if ( flags & 1 ) wd.enableContinuous = false;
 	s->worldId = b2CreateWorld( &wd );
 	if ( s->worldId.index1 == 0 ) return -1;
@@ -941,6 +1008,7 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 		case B2S_FALLING_HINGES: b2sFallingHinges( s ); break;
 		case B2S_SLEEP_PYRAMIDS: b2sSleepPyramids( s, a, b, c ); break;
 		case B2S_JOINT_MIX: b2sJointMix( s, a, &rng ); break;
+		case B2S_OVERFLOW: b2sOverflowScene( s, a, &rng ); break;
 		default: break;
 	}
 	return h;
@@ -1098,6 +1166,37 @@ B2S_EXPORT void b2s_get_state( int h, float* out )
 		o[5] = v.y;
 		o[6] = w;
 	}
+}
+
+/* The last step's contact begin/end touch events (b2World_GetContactEvents), 5 ints per
+   event in the library's order, begin events first: kind (0 begin, 1 end), shape A id,
+   shape B id (index1 - 1), contact id index1 - 1 and its generation, up to capacity.
+   Returns the event count. */
+B2S_EXPORT int b2s_contact_events( int h, int* out, int capacity )
+{
+	b2ContactEvents e = b2World_GetContactEvents( b2s_scenes[h].worldId );
+	int n = 0;
+	for ( int i = 0; i < e.beginCount; ++i, ++n )
+	{
+		if ( n >= capacity ) continue;
+		int* o = out + 5 * n;
+		o[0] = 0;
+		o[1] = e.beginEvents[i].shapeIdA.index1 - 1;
+		o[2] = e.beginEvents[i].shapeIdB.index1 - 1;
+		o[3] = e.beginEvents[i].contactId.index1 - 1;
+		o[4] = (int)e.beginEvents[i].contactId.generation;
+	}
+	for ( int i = 0; i < e.endCount; ++i, ++n )
+	{
+		if ( n >= capacity ) continue;
+		int* o = out + 5 * n;
+		o[0] = 1;
+		o[1] = e.endEvents[i].shapeIdA.index1 - 1;
+		o[2] = e.endEvents[i].shapeIdB.index1 - 1;
+		o[3] = e.endEvents[i].contactId.index1 - 1;
+		o[4] = (int)e.endEvents[i].contactId.generation;
+	}
+	return n;
 }
 
 /* FNV-1a 64 over the bit patterns of b2s_get_state */

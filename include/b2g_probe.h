@@ -70,6 +70,9 @@ void b2p_continuous_counts( uint32_t packedWorldId, int* out );
    flags bit 0 disables continuous collision, bit 1 warm starting, bit 2 contact recycling
    (ramp scene). Returns a handle or -1. */
 int b2s_create( int kind, int a, int b, int c, uint32_t seed, int flags );
+/* worker threads put in the world definition (b2WorldDef.workerCount) of scenes created
+   afterwards; 0 keeps the default. Only a library with its own task system uses it. */
+void b2s_set_workers( int count );
 void b2s_destroy( int handle );
 void b2s_step( int handle, float timeStep, int subStepCount, int count );
 /* step `count` scenes `steps` times, one b2World_StepBatch call (up to `threads` host
@@ -86,6 +89,10 @@ int b2s_move_events( int handle, float* out, int capacity );
 /* the same for `count` scenes, their events one after the other (capacity events in all);
    returns the event count */
 int b2s_move_events_many( const int* handles, int count, float* out, int capacity );
+/* the last step's contact begin/end touch events (b2World_GetContactEvents), 5 ints per
+   event, begin events first: kind (0 begin, 1 end), shape A id, shape B id, contact id
+   (index1 - 1), contact generation, up to capacity; returns the event count */
+int b2s_contact_events( int handle, int* out, int capacity );
 /* FNV-1a 64 over the bit patterns of b2s_get_state */
 uint64_t b2s_state_hash( int handle );
 void b2s_set_velocities( int handle, const float* in );

@@ -19,6 +19,18 @@ ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 REF_LIB = ROOT / "oracle" / "_ref" / "libref.so"
 
 
+def reference_dir() -> Path | None:
+    """The reference's sources: B2G_REFERENCE_DIR when set, else the git-ignored copy the
+    oracle Makefile stages (`make stage`) beside the repository; None where neither is."""
+    import os
+
+    env = os.environ.get("B2G_REFERENCE_DIR")
+    for cand in ([Path(env)] if env else []) + [ROOT / "baseline" / "_ref"]:
+        if (cand / "include" / "box2d" / "box2d.h").is_file():
+            return cand
+    return None
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU and the built libbox2d_gb300.so")
 
@@ -62,6 +74,32 @@ def tangent():
 def gpu_lib():
     """The GB300 library; fails (does not skip) when it is missing on a GPU run."""
     return B.load_library()
+
+
+class EventCheck:
+    """Checks a scene's contact begin/end touch events step by step against a fixture's
+    `contact_events` record (per-step counts, one sha256 over every step's rows)."""
+
+    def __init__(self, g: dict):
+        import hashlib
+
+        self.rec = g.get("contact_events")
+        self.h = hashlib.sha256()
+        self.name = g.get("scene", "")
+
+    def step(self, scene, k: int) -> None:
+        if self.rec is None:
+            return
+        ev = scene.contact_events()
+        self.h.update(len(ev).to_bytes(4, "little"))
+        self.h.update(ev.astype("<i4").tobytes())
+        begin, end = int((ev[:, 0] == 0).sum()), int((ev[:, 0] == 1).sum())
+        assert (begin, end) == (self.rec["begin_per_step"][k - 1], self.rec["end_per_step"][k - 1]), \
+            f"{self.name}: contact begin/end event counts at step {k}"
+
+    def finish(self, steps: int) -> None:
+        if self.rec is not None and steps == len(self.rec["begin_per_step"]):
+            assert self.h.hexdigest() == self.rec["sha256"], f"{self.name}: contact begin/end events differ"
 
 
 def lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps, check_every=1):

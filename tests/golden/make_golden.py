@@ -39,6 +39,9 @@ SCENES = [
     ("shape_zoo_200_continuous", B.SHAPE_ZOO, 200, 0, 0, 7, 0, 300, [1, 150, 300]),
     ("many_pyramids_rain_3x3_continuous", B.MANY_PYRAMIDS_RAIN, 3, 10, 100, 0, 0, 300, [1, 150, 300]),
     ("batch_world_continuous", B.BATCH_WORLD, 0, 0, 0, 21, 0, 300, [1, 300]),
+    # more constraints on one body than the graph has colors: the overflow color (23) holds
+    # contacts and joints, solved by the overflow path
+    ("overflow_2", B.OVERFLOW, 2, 0, 0, 4, 0, 240, [1, 60, 240]),
 ]
 
 # sleeping on: islands fall asleep and wake; per step also the awake body count. The
@@ -63,6 +66,24 @@ def contact_digest(table) -> str:
     return hashlib.sha256(table.astype("<i4").tobytes()).hexdigest()
 
 
+class EventDigest:
+    """Contact begin/end touch events of every step: per-step counts and one sha256 over
+    every step's event rows (kind, shape A, shape B, contact id, generation) in order."""
+
+    def __init__(self):
+        self.h = hashlib.sha256()
+        self.begin, self.end = [], []
+
+    def add(self, events) -> None:
+        self.h.update(len(events).to_bytes(4, "little"))
+        self.h.update(events.astype("<i4").tobytes())
+        self.begin.append(int((events[:, 0] == 0).sum()))
+        self.end.append(int((events[:, 0] == 1).sum()))
+
+    def record(self) -> dict:
+        return {"sha256": self.h.hexdigest(), "begin_per_step": self.begin, "end_per_step": self.end}
+
+
 def main() -> None:
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"], check=True)
     ref = B.load_library(ROOT / "oracle" / "_ref" / "libref.so")
@@ -74,8 +95,10 @@ def main() -> None:
         script = SCRIPTS.get(name, [])
         with B.Scene(ref, kind, a, b, c, seed, flags) as s:
             hashes, digests, awake = [], {}, []
+            events = EventDigest()
             for k in range(1, steps + 1):
                 s.step()
+                events.add(s.contact_events())
                 for action in script:
                     if action[0] == k:
                         s.apply(action[1:])
@@ -88,7 +111,8 @@ def main() -> None:
                                        "touching": int(table[:, 7].sum()) if len(table) else 0}
             data = {"scene": name, "kind": kind, "a": a, "b": b, "c": c, "seed": seed, "flags": flags,
                     "dt": 1.0 / 60.0, "substeps": 4, "bodies": s.body_count, "state_hashes": hashes,
-                    "contact_digests": digests, "source": "reference built from its own sources (oracle/Makefile ref)"}
+                    "contact_digests": digests, "contact_events": events.record(),
+                    "source": "reference built from its own sources (oracle/Makefile ref)"}
             if sleeping:
                 data["requires"] = "islands"
                 data["awake_counts"] = awake

@@ -12,6 +12,7 @@ from pathlib import Path
 import pytest
 
 import box2d_gb300 as B
+from conftest import reference_dir
 
 ROOT = Path(__file__).resolve().parents[1]
 
@@ -52,7 +53,8 @@ def test_oracle_exports_the_public_api(oracle):
     assert not missing, missing
 
 
-REF_INCLUDE = Path("/root/reference/include")
+_REF = reference_dir()
+REF_INCLUDE = _REF / "include" if _REF else ROOT / "baseline" / "_ref" / "include"
 
 
 @pytest.mark.skipif(not REF_INCLUDE.is_dir(), reason="reference headers not present on this machine")

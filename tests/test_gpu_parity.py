@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import box2d_gb300 as B
-from conftest import golden_cases, load_golden, lockstep
+from conftest import EventCheck, golden_cases, load_golden, lockstep
 
 pytestmark = pytest.mark.gpu
 
@@ -21,8 +21,10 @@ def test_gpu_matches_reference_fixture(gpu_lib, name):
     with B.Scene(gpu_lib, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
         assert s.body_count == g["bodies"]
         script = g.get("script", [])
+        events = EventCheck(g)
         for k, expected in enumerate(g["state_hashes"], start=1):
             s.step(1, g["dt"], g["substeps"])
+            events.step(s, k)
             for action in script:
                 if action[0] == k:
                     s.apply(action[1:])
@@ -35,6 +37,7 @@ def test_gpu_matches_reference_fixture(gpu_lib, name):
                 assert table.shape[0] == d["count"], f"{name}: contact count at step {k}"
                 assert hashlib.sha256(table.astype("<i4").tobytes()).hexdigest() == d["sha256"], \
                     f"{name}: contact table (ids, pairs, colors, feature ids) at step {k}"
+        events.finish(len(g["state_hashes"]))
 
 
 def _lockstep(*args, **kw):

@@ -7,7 +7,7 @@ import hashlib
 import pytest
 
 import box2d_gb300 as B
-from conftest import golden_cases, load_golden
+from conftest import EventCheck, golden_cases, load_golden
 
 
 @pytest.mark.parametrize("name", golden_cases())
@@ -18,8 +18,10 @@ def test_oracle_matches_reference_fixture(oracle, name):
                     "checked against this reference fixture directly")
     with B.Scene(oracle, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
         assert s.body_count == g["bodies"]
+        events = EventCheck(g)
         for k, expected in enumerate(g["state_hashes"], start=1):
             s.step(1, g["dt"], g["substeps"])
+            events.step(s, k)
             assert f"{s.state_hash():016x}" == expected, f"{name}: state diverged at step {k}"
             d = g["contact_digests"].get(str(k))
             if d is not None:
@@ -27,6 +29,7 @@ def test_oracle_matches_reference_fixture(oracle, name):
                 assert table.shape[0] == d["count"], f"{name}: contact count at step {k}"
                 assert hashlib.sha256(table.astype("<i4").tobytes()).hexdigest() == d["sha256"], \
                     f"{name}: contact table (ids, pairs, colors, feature ids) at step {k}"
+        events.finish(len(g["state_hashes"]))
 
 
 @pytest.mark.parametrize("name", ["large_pyramid_20", "joint_zoo_4", "many_pyramids_rain_3x3"])
