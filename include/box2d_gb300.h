@@ -73,6 +73,12 @@ typedef struct b2AABB
 	b2Vec2 upperBound;
 } b2AABB;
 
+typedef struct b2Plane
+{
+	b2Vec2 normal;
+	float offset;
+} b2Plane;
+
 /* ---- ids (id.h:37-81) ---- */
 typedef struct b2WorldId
 {
@@ -100,6 +106,13 @@ typedef struct b2JointId
 	uint16_t world0;
 	uint16_t generation;
 } b2JointId;
+
+typedef struct b2ChainId
+{
+	int32_t index1;
+	uint16_t world0;
+	uint16_t generation;
+} b2ChainId;
 
 typedef struct b2ContactId
 {
@@ -558,16 +571,6 @@ typedef struct b2BodyEvents
 	int moveCount;
 } b2BodyEvents;
 
-/* ---- inline math used by callers (math_functions.h) ---- */
-B2G_INLINE b2Vec2 b2Add( b2Vec2 a, b2Vec2 b )
-{
-	return B2G_LITERAL( b2Vec2 ){ a.x + b.x, a.y + b.y };
-}
-
-B2G_INLINE b2Vec2 b2Sub( b2Vec2 a, b2Vec2 b )
-{
-	return B2G_LITERAL( b2Vec2 ){ a.x - b.x, a.y - b.y };
-}
 
 /* ---- API: base (base.h:150-164) ---- */
 B2G_API uint64_t b2GetTicks( void );
@@ -578,6 +581,9 @@ B2G_API uint32_t b2Hash( uint32_t hash, const uint8_t* data, int count );
 B2G_API float b2Atan2( float y, float x );
 B2G_API b2CosSin b2ComputeCosSin( float radians );
 B2G_API b2Rot b2MakeRot( float radians );
+
+/* the reference's inline math, id helpers and constants */
+#include "box2d_gb300_math.h"
 
 /* ---- API: geometry (collision.h:160-230, geometry.c, hull.c) ---- */
 B2G_API b2Hull b2ComputeHull( const b2Vec2* points, int count );
