@@ -33,6 +33,10 @@ SLEEP_PYRAMIDS = 11
 JOINT_MIX = 12
 OVERFLOW = 13
 
+# scripted body changes (Scene.apply): name -> b2s_body_action kind
+BODY_ACTIONS = {"force": 0, "force_center": 1, "torque": 2, "impulse": 3, "impulse_center": 4, "angular_impulse": 5,
+                "transform": 6, "target": 7}
+
 NO_CONTINUOUS = 1
 NO_WARM_STARTING = 2
 NO_RECYCLING = 4
@@ -63,7 +67,9 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     optional = {
         "b2s_set_body_velocity": (None, [c_int, c_int, c_f, c_f, c_f]),
         "b2s_set_workers": (None, [c_int]),
+        "b2s_body_action": (None, [c_int, c_int, c_int, c_f, c_f, c_f, c_f]),
         "b2s_contact_events": (c_int, [c_int, c_p, c_int]),
+        "b2s_world_state_hash": (c_u64, [c_int]),
         "b2s_set_awake": (None, [c_int, c_int, c_int]),
         "b2s_enable_sleep": (None, [c_int, c_int]),
         "b2p_timings": (c_int, [c_u32, c_p, c_p, c_int]),
@@ -143,6 +149,10 @@ class Scene:
     def state_hash(self) -> int:
         return int(self.lib.b2s_state_hash(self.handle))
 
+    def world_state_hash(self) -> int:
+        """b2World_GetStateHash of the scene's world (libraries that export it)."""
+        return int(self.lib.b2s_world_state_hash(self.handle))
+
     def contacts(self) -> np.ndarray:
         cap = 1 << 16
         while True:
@@ -204,7 +214,8 @@ class Scene:
 
     def apply(self, action: list) -> None:
         """One scripted change between steps: ["velocity", body, vx, vy, w], ["awake", body,
-        flag] or ["sleeping", flag]."""
+        flag], ["sleeping", flag], or a body action of BODY_ACTIONS with its body index and up
+        to four numbers (see b2s_body_action)."""
         kind = action[0]
         if kind == "velocity":
             self.lib.b2s_set_body_velocity(self.handle, int(action[1]), float(action[2]), float(action[3]),
@@ -213,6 +224,9 @@ class Scene:
             self.lib.b2s_set_awake(self.handle, int(action[1]), int(action[2]))
         elif kind == "sleeping":
             self.lib.b2s_enable_sleep(self.handle, int(action[1]))
+        elif kind in BODY_ACTIONS:
+            args = [float(x) for x in action[2:]] + [0.0] * (4 - len(action[2:]))
+            self.lib.b2s_body_action(self.handle, BODY_ACTIONS[kind], int(action[1]), *args[:4])
         else:
             raise ValueError(f"unknown scene action {kind!r}")
 

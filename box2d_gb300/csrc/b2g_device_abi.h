@@ -303,6 +303,7 @@ int b2gDev_IslandResults( b2gDeviceWorld* dw, const uint32_t** awakeIslandBits, 
 						  unsigned long long* splitKey );
 int b2gDev_DownloadShapeBoxes( b2gDeviceWorld* dw, int shapeCount, float* aabbs, float* fatAABBs );
 int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float vx, float vy, float w, int which );
+int b2gDev_SetBodyForce( b2gDeviceWorld* dw, int awakeIndex, float fx, float fy, float torque );
 
 /* contacts */
 int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity );

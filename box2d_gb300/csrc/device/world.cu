@@ -1249,6 +1249,23 @@ extern "C" int b2gDev_SetBodyVelocity( b2gDeviceWorld* dw, int awakeIndex, float
 	return (int)cudaGetLastError();
 }
 
+__global__ void k_setForce( float* params, int index, float fx, float fy, float torque )
+{
+	float* pr = params + 8 * index;
+	pr[0] = fx;
+	pr[1] = fy;
+	pr[2] = torque;
+}
+
+/* the accumulated external force and torque of one awake body (its first three integration
+   parameters; the finalize kernel clears them after the step that applies them) */
+extern "C" int b2gDev_SetBodyForce( b2gDeviceWorld* dw, int awakeIndex, float fx, float fy, float torque )
+{
+	k_setForce<<<1, 1, 0, dw->stream>>>( dw->params, awakeIndex, fx, fy, torque );
+	dw->launches += 1;
+	return (int)cudaGetLastError();
+}
+
 extern "C" int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity )
 {
 	CK2( grow( dw, (void**)&dw->contacts, &dw->contactCap, capacity > 0 ? capacity : 1, sizeof( b2gContact ) ) );

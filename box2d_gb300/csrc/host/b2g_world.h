@@ -48,6 +48,8 @@ typedef struct h_body
 	uint32_t simFlags;
 	b2Vec2 linearVelocity;
 	float angularVelocity;
+	b2Vec2 force; /* external force and torque accumulated for the next step (cleared by it) */
+	float torque;
 } h_body;
 
 typedef struct h_shape
@@ -139,7 +141,7 @@ typedef struct h_world
 {
 	int inUse;
 	uint16_t worldId, generation;
-	h_idPool bodyIdPool, shapeIdPool, contactIdPool, jointIdPool;
+	h_idPool bodyIdPool, shapeIdPool, contactIdPool, jointIdPool, chainIdPool;
 	H_ARRAY( h_body ) bodies;
 	H_ARRAY( h_shape ) shapes;
 	H_ARRAY( h_contact ) contacts;
@@ -199,6 +201,7 @@ typedef struct h_world
 	const void* uploadedTreeNodes[3]; /* node array it was sent from */
 	H_ARRAY( b2gContactInit ) pendingInits;
 	h_intArray pendingKills;
+	h_intArray forcedBodies; /* bodies given a force or torque since the last step */
 	int lastStatus;
 	int continuousSweeps, continuousHits; /* accumulated device continuous-collision counters */
 	struct h_tapeWorld* tape;			  /* differentiable-stepping recorder (diff.c), or NULL */

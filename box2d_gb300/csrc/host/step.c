@@ -565,6 +565,14 @@ void h_stepFinish( h_world* w )
 			w->continuousHits += sc.continuousHits;
 		}
 		if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
+		/* the finalize kernel cleared the force and torque of every awake body (solver.c:710-712) */
+		for ( int i = 0; i < w->forcedBodies.count; ++i )
+		{
+			h_body* fb = w->bodies.data + w->forcedBodies.data[i];
+			fb->force = h_v( 0.0f, 0.0f );
+			fb->torque = 0.0f;
+		}
+		w->forcedBodies.count = 0;
 		h_enlargeProxies( w, recs, boxes, enlargedCount );
 		h_lap( w, H_PHASE_ENLARGE, &lap );
 		{

@@ -237,6 +237,7 @@ void b2DestroyWorld( b2WorldId worldId )
 	}
 	h_free( w->bodyIdPool.freeArray );
 	h_free( w->shapeIdPool.freeArray );
+	h_free( w->chainIdPool.freeArray );
 	h_free( w->contactIdPool.freeArray );
 	h_free( w->jointIdPool.freeArray );
 	h_free( w->bodies );
@@ -260,6 +261,7 @@ void b2DestroyWorld( b2WorldId worldId )
 	h_free( w->endEvents[1] );
 	h_free( w->pendingInits );
 	h_free( w->pendingKills );
+	h_free( w->forcedBodies );
 	h_islandsFree( w );
 	uint16_t generation = w->generation;
 	memset( w, 0, sizeof( *w ) );
@@ -305,6 +307,136 @@ void b2World_SetGravity( b2WorldId worldId, b2Vec2 gravity )
 b2Vec2 b2World_GetGravity( b2WorldId worldId ) { return h_worldFromId( worldId )->gravity; }
 
 int b2World_GetAwakeBodyCount( b2WorldId worldId ) { return h_worldFromId( worldId )->awakeBodyIds.count; }
+
+/* ---- state hash (world_snapshot.c:1003-1187, b2World_GetStateHash) ----
+   FNV-1a 64 over every live body's transform, its velocity when awake and its solver-set
+   slot; every live contact's set, color and slot and its manifold impulses; every live
+   joint's set, color, slot and accumulated impulses; the id pools and the solver-set count.
+   Two worlds that simulate identically, with identical bookkeeping, give the same value. */
+#define H_FNV_INIT 14695981039346656037ull
+#define H_FNV_PRIME 1099511628211ull
+
+static uint64_t h_fnvWord( uint64_t hash, uint32_t bits ) { return ( hash ^ (uint64_t)bits ) * H_FNV_PRIME; }
+static uint64_t h_fnvFloat( uint64_t hash, float f )
+{
+	uint32_t bits;
+	memcpy( &bits, &f, 4 );
+	return h_fnvWord( hash, bits );
+}
+static uint64_t h_fnvInt( uint64_t hash, int v ) { return h_fnvWord( hash, (uint32_t)v ); }
+static uint64_t h_fnvBytes( uint64_t hash, const void* data, int n )
+{
+	const uint8_t* b = (const uint8_t*)data;
+	for ( int i = 0; i < n; ++i ) hash = ( hash ^ (uint64_t)b[i] ) * H_FNV_PRIME;
+	return hash;
+}
+static uint64_t h_fnvPool( uint64_t hash, const h_idPool* pool )
+{
+	hash = h_fnvInt( hash, pool->nextIndex );
+	return h_fnvInt( hash, pool->nextIndex - pool->freeArray.count );
+}
+
+uint64_t b2World_GetStateHash( b2WorldId worldId )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w == NULL ) return 0;
+	h_syncFromDevice( w );
+	h_syncJointsFromDevice( w );
+	uint64_t hash = H_FNV_INIT;
+	for ( int i = 0; i < w->bodies.count; ++i )
+	{
+		const h_body* b = w->bodies.data + i;
+		if ( b->id != i ) continue;
+		hash = h_fnvFloat( hash, b->transform.p.x );
+		hash = h_fnvFloat( hash, b->transform.p.y );
+		hash = h_fnvFloat( hash, b->transform.q.c );
+		hash = h_fnvFloat( hash, b->transform.q.s );
+		if ( b->setIndex == H_AWAKE_SET )
+		{
+			hash = h_fnvFloat( hash, b->linearVelocity.x );
+			hash = h_fnvFloat( hash, b->linearVelocity.y );
+			hash = h_fnvFloat( hash, b->angularVelocity );
+		}
+		hash = h_fnvInt( hash, b->setIndex );
+		hash = h_fnvInt( hash, b->localIndex );
+	}
+	int nc = w->contacts.count;
+	b2gContact* dc = NULL;
+	if ( nc > 0 && w->dev != NULL )
+	{
+		dc = malloc( (size_t)nc * sizeof( b2gContact ) );
+		int rc = b2gDev_DownloadContacts( w->dev, dc, nc );
+		if ( rc != 0 ) h_fail( w, "contact download", rc );
+	}
+	for ( int i = 0; i < nc; ++i )
+	{
+		const h_contact* c = w->contacts.data + i;
+		if ( c->contactId != i ) continue;
+		hash = h_fnvInt( hash, c->setIndex );
+		hash = h_fnvInt( hash, c->colorIndex );
+		hash = h_fnvInt( hash, c->localIndex );
+		const b2Manifold* m = dc != NULL ? &dc[i].manifold : NULL;
+		int pointCount = m != NULL ? m->pointCount : 0;
+		hash = h_fnvInt( hash, pointCount );
+		for ( int k = 0; k < pointCount; ++k )
+		{
+			hash = h_fnvFloat( hash, m->points[k].normalImpulse );
+			hash = h_fnvFloat( hash, m->points[k].tangentImpulse );
+			hash = h_fnvFloat( hash, m->points[k].totalNormalImpulse );
+		}
+	}
+	free( dc );
+	for ( int i = 0; i < w->joints.count; ++i )
+	{
+		const h_joint* j = w->joints.data + i;
+		if ( j->jointId != i ) continue;
+		hash = h_fnvInt( hash, j->setIndex );
+		hash = h_fnvInt( hash, j->colorIndex );
+		hash = h_fnvInt( hash, j->localIndex );
+		const float* s = w->jointRecords.data[i].s;
+		/* the accumulated impulses of each type, in the slots host/joint.c lists */
+		switch ( j->type )
+		{
+			case b2_distanceJoint:
+			case b2_wheelJoint:
+			case b2_revoluteJoint:
+			case b2_prismaticJoint:
+			{
+				int first = 0, count = j->type == b2_distanceJoint ? 4 : ( j->type == b2_wheelJoint ? 5 : 6 );
+				if ( j->type == b2_revoluteJoint || j->type == b2_prismaticJoint )
+				{
+					hash = h_fnvBytes( hash, s, 2 * (int)sizeof( float ) );
+					first = 2;
+				}
+				for ( int k = first; k < count; ++k ) hash = h_fnvFloat( hash, s[k] );
+				break;
+			}
+			case b2_weldJoint:
+				hash = h_fnvBytes( hash, s, 2 * (int)sizeof( float ) );
+				hash = h_fnvFloat( hash, s[2] );
+				break;
+			case b2_moverJoint:
+			case b2_pogoJoint:
+				hash = h_fnvFloat( hash, s[0] );
+				hash = h_fnvFloat( hash, s[1] );
+				break;
+			case b2_motorJoint:
+				for ( int k = 0; k < 6; ++k ) hash = h_fnvFloat( hash, s[k] );
+				break;
+			default:
+				break;
+		}
+	}
+	hash = h_fnvPool( hash, &w->bodyIdPool );
+	hash = h_fnvPool( hash, &w->shapeIdPool );
+	hash = h_fnvPool( hash, &w->chainIdPool );
+	hash = h_fnvPool( hash, &w->contactIdPool );
+	hash = h_fnvPool( hash, &w->jointIdPool );
+	hash = h_fnvPool( hash, &w->islandIdPool );
+	hash = h_fnvPool( hash, &w->setIdPool );
+	hash = h_fnvInt( hash, w->sets.count );
+	return hash;
+}
 
 b2Profile b2World_GetProfile( b2WorldId worldId ) { return h_worldFromId( worldId )->profile; }
 
@@ -522,9 +654,9 @@ void h_ensureDevice( h_world* w )
 		sv[4 * a + 2] = b->angularVelocity;
 		sv[4 * a + 3] = flBits;
 		sd[4 * a + 2] = 1.0f;
-		params[8 * a + 0] = 0.0f; /* force.x */
-		params[8 * a + 1] = 0.0f; /* force.y */
-		params[8 * a + 2] = 0.0f; /* torque */
+		params[8 * a + 0] = b->force.x;
+		params[8 * a + 1] = b->force.y;
+		params[8 * a + 2] = b->torque;
 		params[8 * a + 3] = b->linearDamping;
 		params[8 * a + 4] = b->angularDamping;
 		params[8 * a + 5] = b->gravityScale;
@@ -794,6 +926,170 @@ void b2Body_SetAngularVelocity( b2BodyId bodyId, float av )
 		int rc = b2gDev_SetBodyVelocity( w->dev, b->localIndex, 0.0f, 0.0f, av, 2 );
 		if ( rc != 0 ) h_fail( w, "set velocity", rc );
 	}
+}
+
+/* body.c:713-768: teleport; shapes get new boxes and move in the broadphase when they
+   leave their fat box */
+void b2Body_SetTransform( b2BodyId bodyId, b2Pos position, b2Rot rotation )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	if ( w->locked ) return;
+	h_markHostChanged( w );
+	h_body* b = h_getBody( bodyId );
+	b->transform.p = position;
+	b->transform.q = rotation;
+	b->center = h_transformWorldPoint( b->transform, b->localCenter );
+	for ( int sid = b->headShapeId; sid != B2_NULL_INDEX; sid = w->shapes.data[sid].nextShapeId )
+	{
+		h_shape* s = w->shapes.data + sid;
+		b2AABB aabb = h_computeFatShapeAABB( s, b->transform, H_SPECULATIVE_DISTANCE );
+		s->aabb = aabb;
+		if ( h_aabbContains( s->fatAABB, aabb ) ) continue;
+		float margin = s->aabbMargin;
+		b2AABB fat = { { aabb.lowerBound.x - margin, aabb.lowerBound.y - margin },
+					   { aabb.upperBound.x + margin, aabb.upperBound.y + margin } };
+		s->fatAABB = fat;
+		if ( s->proxyKey != B2_NULL_INDEX )
+		{
+			h_treeMoveProxy( w->trees + H_PROXY_TYPE( s->proxyKey ), H_PROXY_ID( s->proxyKey ), fat );
+			h_bufferMove( w, s->proxyKey );
+		}
+	}
+}
+
+/* ---- forces and impulses (body.c:935-1090) ---- */
+
+/* a force, torque or impulse reaches a dynamic body that is awake (after waking it when
+   asked); returns whether it applies */
+static int h_applyTarget( h_world* w, h_body* b, bool wake )
+{
+	if ( b->type != b2_dynamicBody || b->setIndex == H_DISABLED_SET ) return 0;
+	if ( wake && b->setIndex >= H_FIRST_SLEEPING_SET ) h_wakeBody( w, b );
+	return b->setIndex == H_AWAKE_SET;
+}
+
+static void h_pushForce( h_world* w, h_body* b )
+{
+	h_push( w->forcedBodies, b->id );
+	if ( w->devReady )
+	{
+		int rc = b2gDev_SetBodyForce( w->dev, b->localIndex, b->force.x, b->force.y, b->torque );
+		if ( rc != 0 ) h_fail( w, "set force", rc );
+	}
+}
+
+void b2Body_ApplyForce( b2BodyId bodyId, b2Vec2 force, b2Pos point, bool wake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( h_applyTarget( w, b, wake ) == 0 ) return;
+	h_syncFromDevice( w );
+	b->force = h_add( b->force, force );
+	b->torque += h_cross( h_sub( point, b->center ), force );
+	h_pushForce( w, b );
+}
+
+void b2Body_ApplyForceToCenter( b2BodyId bodyId, b2Vec2 force, bool wake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( h_applyTarget( w, b, wake ) == 0 ) return;
+	b->force = h_add( b->force, force );
+	h_pushForce( w, b );
+}
+
+void b2Body_ApplyTorque( b2BodyId bodyId, float torque, bool wake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( h_applyTarget( w, b, wake ) == 0 ) return;
+	b->torque += torque;
+	h_pushForce( w, b );
+}
+
+void b2Body_ClearForces( b2BodyId bodyId )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	b->force = h_v( 0.0f, 0.0f );
+	b->torque = 0.0f;
+	if ( b->setIndex == H_AWAKE_SET ) h_pushForce( w, b );
+}
+
+/* new velocities of an awake body: host record and device state */
+static void h_setVelocities( h_world* w, h_body* b, b2Vec2 v, float av )
+{
+	b->linearVelocity = v;
+	b->angularVelocity = av;
+	if ( w->devReady )
+	{
+		int rc = b2gDev_SetBodyVelocity( w->dev, b->localIndex, v.x, v.y, 0.0f, 1 );
+		if ( rc == 0 ) rc = b2gDev_SetBodyVelocity( w->dev, b->localIndex, 0.0f, 0.0f, av, 2 );
+		if ( rc != 0 ) h_fail( w, "set velocity", rc );
+	}
+}
+
+/* body.h b2LimitVelocity: clamp the linear speed to the world's maximum */
+static b2Vec2 h_limitVelocity( b2Vec2 v, float maxLinearSpeed )
+{
+	float v2 = h_lengthSq( v );
+	if ( v2 > maxLinearSpeed * maxLinearSpeed ) v = h_mulSV( maxLinearSpeed / sqrtf( v2 ), v );
+	return v;
+}
+
+void b2Body_ApplyLinearImpulse( b2BodyId bodyId, b2Vec2 impulse, b2Pos point, bool wake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( h_applyTarget( w, b, wake ) == 0 ) return;
+	h_syncFromDevice( w );
+	b2Vec2 v = h_mulAdd( b->linearVelocity, b->invMass, impulse );
+	float av = b->angularVelocity + b->invInertia * h_cross( h_sub( point, b->center ), impulse );
+	h_setVelocities( w, b, h_limitVelocity( v, w->maxLinearSpeed ), av );
+}
+
+void b2Body_ApplyLinearImpulseToCenter( b2BodyId bodyId, b2Vec2 impulse, bool wake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( h_applyTarget( w, b, wake ) == 0 ) return;
+	h_syncFromDevice( w );
+	b2Vec2 v = h_mulAdd( b->linearVelocity, b->invMass, impulse );
+	h_setVelocities( w, b, h_limitVelocity( v, w->maxLinearSpeed ), b->angularVelocity );
+}
+
+void b2Body_ApplyAngularImpulse( b2BodyId bodyId, float impulse, bool wake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( h_applyTarget( w, b, wake ) == 0 ) return;
+	h_syncFromDevice( w );
+	h_setVelocities( w, b, b->linearVelocity, b->angularVelocity + b->invInertia * impulse );
+}
+
+/* body.c:842-920: velocities that carry the body to the target transform over timeStep */
+void b2Body_SetTargetTransform( b2BodyId bodyId, b2WorldTransform target, float timeStep, bool wake )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	h_body* b = h_getBody( bodyId );
+	if ( b->setIndex == H_DISABLED_SET || b->type == b2_staticBody || timeStep <= 0.0f ) return;
+	if ( b->setIndex != H_AWAKE_SET && wake == false ) return;
+	h_syncFromDevice( w );
+	b2Vec2 targetCenter = h_transformWorldPoint( target, b->localCenter );
+	b2Vec2 delta = h_sub( targetCenter, b->center );
+	float invTimeStep = 1.0f / timeStep;
+	b2Vec2 v = h_mulSV( invTimeStep, delta );
+	b2Rot q1 = b->transform.q, q2 = target.q;
+	float s = q1.c * q2.s - q1.s * q2.c;
+	float c = q1.c * q2.c + q1.s * q2.s;
+	float av = invTimeStep * b2Atan2( s, c );
+	if ( b->setIndex != H_AWAKE_SET )
+	{
+		float maxVelocity = h_length( v ) + h_abs( av ) * b->maxExtent;
+		if ( maxVelocity < b->sleepThreshold ) return;
+		h_wakeBody( w, b );
+	}
+	h_setVelocities( w, b, v, av );
 }
 
 float b2Body_GetMass( b2BodyId bodyId ) { return h_getBody( bodyId )->mass; }

@@ -1090,6 +1090,37 @@ B2S_EXPORT void b2s_set_awake( int h, int bodyIndex, int awake )
 }
 #endif
 
+/* One scripted change to a scene body between steps, through the public body API:
+   kind 0 b2Body_ApplyForce (force (a, b) at the center of mass + (c, d)), 1 ApplyForceToCenter,
+   2 ApplyTorque (a), 3 ApplyLinearImpulse (impulse (a, b) at the center + (c, d)),
+   4 ApplyLinearImpulseToCenter, 5 ApplyAngularImpulse (a), 6 SetTransform (position (a, b),
+   angle c), 7 SetTargetTransform (position (a, b), angle c, time step d). Forces and
+   impulses wake the body. */
+B2S_EXPORT void b2s_body_action( int h, int kind, int bodyIndex, float a, float b, float c, float d )
+{
+	b2BodyId id = b2s_scenes[h].bodies[bodyIndex];
+	b2Vec2 v = { a, b };
+	b2Vec2 center = b2Body_GetWorldCenter( id );
+	b2Vec2 point = { center.x + c, center.y + d };
+	switch ( kind )
+	{
+		case 0: b2Body_ApplyForce( id, v, point, true ); break;
+		case 1: b2Body_ApplyForceToCenter( id, v, true ); break;
+		case 2: b2Body_ApplyTorque( id, a, true ); break;
+		case 3: b2Body_ApplyLinearImpulse( id, v, point, true ); break;
+		case 4: b2Body_ApplyLinearImpulseToCenter( id, v, true ); break;
+		case 5: b2Body_ApplyAngularImpulse( id, a, true ); break;
+		case 6: b2Body_SetTransform( id, v, b2MakeRot( c ) ); break;
+		case 7:
+		{
+			b2Transform target = { v, b2MakeRot( c ) };
+			b2Body_SetTargetTransform( id, target, d, true );
+			break;
+		}
+		default: break;
+	}
+}
+
 B2S_EXPORT void b2s_enable_sleep( int h, int flag ) { b2World_EnableSleeping( b2s_scenes[h].worldId, flag != 0 ); }
 
 /* awake body count and the per-body awake flags (creation order) */
@@ -1198,6 +1229,14 @@ B2S_EXPORT int b2s_contact_events( int h, int* out, int capacity )
 	}
 	return n;
 }
+
+#ifndef B2S_NO_ISLANDS
+/* the library's own b2World_GetStateHash of the scene's world */
+B2S_EXPORT uint64_t b2s_world_state_hash( int h )
+{
+	return b2World_GetStateHash( b2s_scenes[h].worldId );
+}
+#endif
 
 /* FNV-1a 64 over the bit patterns of b2s_get_state */
 B2S_EXPORT uint64_t b2s_state_hash( int h )

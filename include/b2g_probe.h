@@ -74,6 +74,11 @@ int b2s_create( int kind, int a, int b, int c, uint32_t seed, int flags );
    afterwards; 0 keeps the default. Only a library with its own task system uses it. */
 void b2s_set_workers( int count );
 void b2s_destroy( int handle );
+/* a scripted change to scene body `bodyIndex` between steps: 0 b2Body_ApplyForce (force
+   (a, b) at the center of mass + (c, d)), 1 ApplyForceToCenter, 2 ApplyTorque (a),
+   3 ApplyLinearImpulse, 4 ApplyLinearImpulseToCenter, 5 ApplyAngularImpulse (a),
+   6 SetTransform (position (a, b), angle c), 7 SetTargetTransform (also time step d) */
+void b2s_body_action( int handle, int kind, int bodyIndex, float a, float b, float c, float d );
 void b2s_step( int handle, float timeStep, int subStepCount, int count );
 /* step `count` scenes `steps` times, one b2World_StepBatch call (up to `threads` host
    threads) per step on the GB300 library, one world after the other elsewhere */
@@ -93,6 +98,8 @@ int b2s_move_events_many( const int* handles, int count, float* out, int capacit
    event, begin events first: kind (0 begin, 1 end), shape A id, shape B id, contact id
    (index1 - 1), contact generation, up to capacity; returns the event count */
 int b2s_contact_events( int handle, int* out, int capacity );
+/* b2World_GetStateHash of the scene's world (not in the oracle, which has no islands) */
+uint64_t b2s_world_state_hash( int handle );
 /* FNV-1a 64 over the bit patterns of b2s_get_state */
 uint64_t b2s_state_hash( int handle );
 void b2s_set_velocities( int handle, const float* in );

@@ -625,6 +625,8 @@ B2G_API b2Vec2 b2World_GetGravity( b2WorldId worldId );
 B2G_API int b2World_GetAwakeBodyCount( b2WorldId worldId );
 B2G_API b2Profile b2World_GetProfile( b2WorldId worldId );
 B2G_API b2Counters b2World_GetCounters( b2WorldId worldId );
+/* world_snapshot.c:1183 (box2d.h:235): FNV-1a 64 of the simulation state and bookkeeping */
+B2G_API uint64_t b2World_GetStateHash( b2WorldId worldId );
 
 /* ---- API: bodies (box2d.h:355-550) ---- */
 B2G_API b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def );
@@ -639,6 +641,16 @@ B2G_API b2Vec2 b2Body_GetLinearVelocity( b2BodyId bodyId );
 B2G_API float b2Body_GetAngularVelocity( b2BodyId bodyId );
 B2G_API void b2Body_SetLinearVelocity( b2BodyId bodyId, b2Vec2 linearVelocity );
 B2G_API void b2Body_SetAngularVelocity( b2BodyId bodyId, float angularVelocity );
+/* body.c:713, :842 and :935-1090 (box2d.h:396-490) */
+B2G_API void b2Body_SetTransform( b2BodyId bodyId, b2Pos position, b2Rot rotation );
+B2G_API void b2Body_SetTargetTransform( b2BodyId bodyId, b2WorldTransform target, float timeStep, bool wake );
+B2G_API void b2Body_ApplyForce( b2BodyId bodyId, b2Vec2 force, b2Pos point, bool wake );
+B2G_API void b2Body_ApplyForceToCenter( b2BodyId bodyId, b2Vec2 force, bool wake );
+B2G_API void b2Body_ApplyTorque( b2BodyId bodyId, float torque, bool wake );
+B2G_API void b2Body_ClearForces( b2BodyId bodyId );
+B2G_API void b2Body_ApplyLinearImpulse( b2BodyId bodyId, b2Vec2 impulse, b2Pos point, bool wake );
+B2G_API void b2Body_ApplyLinearImpulseToCenter( b2BodyId bodyId, b2Vec2 impulse, bool wake );
+B2G_API void b2Body_ApplyAngularImpulse( b2BodyId bodyId, float impulse, bool wake );
 B2G_API float b2Body_GetMass( b2BodyId bodyId );
 B2G_API float b2Body_GetRotationalInertia( b2BodyId bodyId );
 B2G_API b2Vec2 b2Body_GetLocalCenter( b2BodyId bodyId );

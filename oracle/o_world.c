@@ -486,6 +486,135 @@ void b2Body_SetAngularVelocity( b2BodyId bodyId, float av )
 	if ( s ) s->angularVelocity = av;
 }
 
+/* body.c:713-768 */
+void b2Body_SetTransform( b2BodyId bodyId, b2Pos position, b2Rot rotation )
+{
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_body* b = o_getBody( bodyId );
+	o_bodySim* sim = o_getBodySim( w, b );
+	sim->transform.p = position;
+	sim->transform.q = rotation;
+	sim->center = o_transformWorldPoint( sim->transform, sim->localCenter );
+	sim->rotation0 = sim->transform.q;
+	sim->center0 = sim->center;
+	for ( int sid = b->headShapeId; sid != B2_NULL_INDEX; sid = w->shapes.data[sid].nextShapeId )
+	{
+		o_shape* s = w->shapes.data + sid;
+		b2AABB aabb = o_computeFatShapeAABB( s, sim->transform, O_SPECULATIVE_DISTANCE );
+		s->aabb = aabb;
+		if ( o_aabbContains( s->fatAABB, aabb ) ) continue;
+		float margin = s->aabbMargin;
+		b2AABB fat = { { aabb.lowerBound.x - margin, aabb.lowerBound.y - margin },
+					   { aabb.upperBound.x + margin, aabb.upperBound.y + margin } };
+		s->fatAABB = fat;
+		if ( s->proxyKey != B2_NULL_INDEX )
+		{
+			o_treeMoveProxy( w->trees + O_PROXY_TYPE( s->proxyKey ), O_PROXY_ID( s->proxyKey ), fat );
+			o_bufferMove( w, s->proxyKey );
+		}
+	}
+}
+
+/* body.c:935-1090; the oracle has no sleeping sets, so every dynamic body is awake */
+static o_bodySim* o_forceTarget( o_world* w, o_body* b )
+{
+	if ( b->type != b2_dynamicBody ) return NULL;
+	return o_getBodySim( w, b );
+}
+
+void b2Body_ApplyForce( b2BodyId bodyId, b2Vec2 force, b2Pos point, bool wake )
+{
+	(void)wake;
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_bodySim* sim = o_forceTarget( w, o_getBody( bodyId ) );
+	if ( sim == NULL ) return;
+	sim->force = o_add( sim->force, force );
+	sim->torque += o_cross( o_sub( point, sim->center ), force );
+}
+
+void b2Body_ApplyForceToCenter( b2BodyId bodyId, b2Vec2 force, bool wake )
+{
+	(void)wake;
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_bodySim* sim = o_forceTarget( w, o_getBody( bodyId ) );
+	if ( sim != NULL ) sim->force = o_add( sim->force, force );
+}
+
+void b2Body_ApplyTorque( b2BodyId bodyId, float torque, bool wake )
+{
+	(void)wake;
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_bodySim* sim = o_forceTarget( w, o_getBody( bodyId ) );
+	if ( sim != NULL ) sim->torque += torque;
+}
+
+void b2Body_ClearForces( b2BodyId bodyId )
+{
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_bodySim* sim = o_getBodySim( w, o_getBody( bodyId ) );
+	sim->force = o_v( 0.0f, 0.0f );
+	sim->torque = 0.0f;
+}
+
+static b2Vec2 o_limitVelocity( b2Vec2 v, float maxLinearSpeed )
+{
+	float v2 = o_lengthSq( v );
+	if ( v2 > maxLinearSpeed * maxLinearSpeed ) v = o_mulSV( maxLinearSpeed / sqrtf( v2 ), v );
+	return v;
+}
+
+void b2Body_ApplyLinearImpulse( b2BodyId bodyId, b2Vec2 impulse, b2Pos point, bool wake )
+{
+	(void)wake;
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_body* b = o_getBody( bodyId );
+	o_bodySim* sim = o_forceTarget( w, b );
+	if ( sim == NULL ) return;
+	o_bodyState* st = o_getBodyState( w, b );
+	st->linearVelocity = o_mulAdd( st->linearVelocity, sim->invMass, impulse );
+	st->angularVelocity += sim->invInertia * o_cross( o_sub( point, sim->center ), impulse );
+	st->linearVelocity = o_limitVelocity( st->linearVelocity, w->maxLinearSpeed );
+}
+
+void b2Body_ApplyLinearImpulseToCenter( b2BodyId bodyId, b2Vec2 impulse, bool wake )
+{
+	(void)wake;
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_body* b = o_getBody( bodyId );
+	o_bodySim* sim = o_forceTarget( w, b );
+	if ( sim == NULL ) return;
+	o_bodyState* st = o_getBodyState( w, b );
+	st->linearVelocity = o_limitVelocity( o_mulAdd( st->linearVelocity, sim->invMass, impulse ), w->maxLinearSpeed );
+}
+
+void b2Body_ApplyAngularImpulse( b2BodyId bodyId, float impulse, bool wake )
+{
+	(void)wake;
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_body* b = o_getBody( bodyId );
+	o_bodySim* sim = o_forceTarget( w, b );
+	if ( sim == NULL ) return;
+	o_getBodyState( w, b )->angularVelocity += sim->invInertia * impulse;
+}
+
+/* body.c:842-920 */
+void b2Body_SetTargetTransform( b2BodyId bodyId, b2WorldTransform target, float timeStep, bool wake )
+{
+	(void)wake;
+	o_world* w = o_worldByIndex( bodyId.world0 );
+	o_body* b = o_getBody( bodyId );
+	if ( b->type == b2_staticBody || timeStep <= 0.0f ) return;
+	o_bodySim* sim = o_getBodySim( w, b );
+	b2Vec2 delta = o_sub( o_transformWorldPoint( target, sim->localCenter ), sim->center );
+	float invTimeStep = 1.0f / timeStep;
+	b2Rot q1 = sim->transform.q, q2 = target.q;
+	float s = q1.c * q2.s - q1.s * q2.c;
+	float c = q1.c * q2.c + q1.s * q2.s;
+	o_bodyState* st = o_getBodyState( w, b );
+	st->linearVelocity = o_mulSV( invTimeStep, delta );
+	st->angularVelocity = invTimeStep * b2Atan2( s, c );
+}
+
 float b2Body_GetMass( b2BodyId bodyId ) { return o_getBody( bodyId )->mass; }
 
 float b2Body_GetRotationalInertia( b2BodyId bodyId ) { return o_getBody( bodyId )->inertia; }

@@ -42,6 +42,8 @@ SCENES = [
     # more constraints on one body than the graph has colors: the overflow color (23) holds
     # contacts and joints, solved by the overflow path
     ("overflow_2", B.OVERFLOW, 2, 0, 0, 4, 0, 240, [1, 60, 240]),
+    # forces, torques, impulses, teleports and target transforms applied between steps
+    ("body_api_zoo", B.SHAPE_ZOO, 60, 0, 0, 9, 0, 150, [1, 75, 150]),
 ]
 
 # sleeping on: islands fall asleep and wake; per step also the awake body count. The
@@ -57,6 +59,14 @@ SCRIPTS = {
     "sleep_api_pyramids": [[40, "velocity", 3, 0.0, 6.0, 0.0], [41, "velocity", 25, 2.0, 0.0, 1.0],
                            [55, "awake", 10, 0], [130, "awake", 30, 1], [200, "sleeping", 0], [260, "sleeping", 1]],
 }
+SCRIPTS["body_api_zoo"] = (
+    [[5, "force", 3, 50.0, 100.0, 0.1, 0.2], [5, "force_center", 3, -20.0, 0.0], [6, "torque", 4, 30.0],
+     [10, "impulse", 5, 2.0, 5.0, 0.1, 0.0], [11, "impulse_center", 6, -3.0, 1.0], [12, "angular_impulse", 7, 2.0],
+     [13, "impulse_center", 11, 1.0e5, 0.0], [14, "force", 0, 100.0, 100.0, 0.0, 0.0],
+     [20, "transform", 8, 0.0, 12.0, 0.5], [30, "target", 9, 3.0, 5.0, 0.3, 1.0 / 60.0]]
+    + [[k, "force_center", 10, 0.0, 40.0] for k in range(40, 61)]
+    + [[k, "torque", 12, -5.0] for k in range(50, 56)])
+
 # test/test_determinism.c:21-22
 DETERMINISM_SLEEP_STEP = 274
 DETERMINISM_HASH = 0xE86690F4
@@ -94,7 +104,7 @@ def main() -> None:
         sleeping = (name, kind, a, b, c, seed, flags, steps, digest_steps) in SLEEP_SCENES
         script = SCRIPTS.get(name, [])
         with B.Scene(ref, kind, a, b, c, seed, flags) as s:
-            hashes, digests, awake = [], {}, []
+            hashes, digests, awake, world_hashes = [], {}, [], []
             events = EventDigest()
             for k in range(1, steps + 1):
                 s.step()
@@ -103,6 +113,7 @@ def main() -> None:
                     if action[0] == k:
                         s.apply(action[1:])
                 hashes.append(f"{s.state_hash():016x}")
+                world_hashes.append(f"{s.world_state_hash():016x}")
                 if sleeping:
                     awake.append(s.awake()[0])
                 if k in digest_steps:
@@ -112,12 +123,13 @@ def main() -> None:
             data = {"scene": name, "kind": kind, "a": a, "b": b, "c": c, "seed": seed, "flags": flags,
                     "dt": 1.0 / 60.0, "substeps": 4, "bodies": s.body_count, "state_hashes": hashes,
                     "contact_digests": digests, "contact_events": events.record(),
+                    "world_state_hashes": world_hashes,
                     "source": "reference built from its own sources (oracle/Makefile ref)"}
             if sleeping:
                 data["requires"] = "islands"
                 data["awake_counts"] = awake
-                if script:
-                    data["script"] = script
+            if script:
+                data["script"] = script
         if kind == B.FALLING_HINGES:
             # the reference's own determinism test, rerun here: it must give the test's constants
             with B.Scene(ref, kind, a, b, c, seed, flags) as s:

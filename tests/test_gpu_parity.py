@@ -29,6 +29,9 @@ def test_gpu_matches_reference_fixture(gpu_lib, name):
                 if action[0] == k:
                     s.apply(action[1:])
             assert f"{s.state_hash():016x}" == expected, f"{name}: body state differs from the reference at step {k}"
+            if "world_state_hashes" in g:
+                assert f"{s.world_state_hash():016x}" == g["world_state_hashes"][k - 1], \
+                    f"{name}: b2World_GetStateHash (state and bookkeeping) differs from the reference at step {k}"
             if "awake_counts" in g:
                 assert s.awake()[0] == g["awake_counts"][k - 1], f"{name}: awake body count at step {k}"
             d = g["contact_digests"].get(str(k))

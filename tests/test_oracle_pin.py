@@ -19,9 +19,13 @@ def test_oracle_matches_reference_fixture(oracle, name):
     with B.Scene(oracle, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
         assert s.body_count == g["bodies"]
         events = EventCheck(g)
+        script = g.get("script", [])
         for k, expected in enumerate(g["state_hashes"], start=1):
             s.step(1, g["dt"], g["substeps"])
             events.step(s, k)
+            for action in script:
+                if action[0] == k:
+                    s.apply(action[1:])
             assert f"{s.state_hash():016x}" == expected, f"{name}: state diverged at step {k}"
             d = g["contact_digests"].get(str(k))
             if d is not None:
