@@ -32,6 +32,7 @@ FALLING_HINGES = 10
 SLEEP_PYRAMIDS = 11
 JOINT_MIX = 12
 OVERFLOW = 13
+SENSOR_ZOO = 14
 
 # scripted body changes (Scene.apply): name -> b2s_body_action kind
 BODY_ACTIONS = {"force": 0, "force_center": 1, "torque": 2, "impulse": 3, "impulse_center": 4, "angular_impulse": 5,
@@ -70,6 +71,7 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2s_body_action": (None, [c_int, c_int, c_int, c_f, c_f, c_f, c_f]),
         "b2s_contact_events": (c_int, [c_int, c_p, c_int]),
         "b2s_world_state_hash": (c_u64, [c_int]),
+        "b2s_sensor_events": (c_int, [c_int, c_p, c_int]),
         "b2s_set_awake": (None, [c_int, c_int, c_int]),
         "b2s_enable_sleep": (None, [c_int, c_int]),
         "b2p_timings": (c_int, [c_u32, c_p, c_p, c_int]),
@@ -178,6 +180,17 @@ class Scene:
         while True:
             buf = np.zeros((cap, 5), np.int32)
             n = self.lib.b2s_contact_events(self.handle, buf.ctypes.data, cap)
+            if n <= cap:
+                return buf[:n]
+            cap = n
+
+    def sensor_events(self) -> np.ndarray:
+        """The last step's sensor begin/end touch events, one row each: kind (0 begin,
+        1 end), sensor shape, visitor shape, sensor generation, visitor generation."""
+        cap = 4096
+        while True:
+            buf = np.zeros((cap, 5), np.int32)
+            n = self.lib.b2s_sensor_events(self.handle, buf.ctypes.data, cap)
             if n <= cap:
                 return buf[:n]
             cap = n

@@ -84,6 +84,7 @@ typedef struct b2gShape
 	int isSensor;
 	b2Vec2 ccdCentroid;
 	float ccdCoreRadius;
+	int enableSensorEvents; /* the shape is seen by sensors (and a sensor reports events) */
 } b2gShape;
 
 /* contact record (contact.h:103-142 b2ContactSim without ids kept on the host) */
@@ -312,10 +313,16 @@ int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* contactIds, int count );
 int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* colorContactIds, const int* colorContactOffsets,
 						 int totalContacts );
 int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count );
-/* device addresses of the contact records and the color lists, the color offsets and the
-   world's stream (cudaStream_t), for kernels outside world.cu */
+/* device addresses of the contact records and the color lists, the color offsets, the
+   world's stream (cudaStream_t) and its CUDA device, for kernels outside world.cu */
 void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const int** colorIds, int* colorOffsets,
-						 void** stream );
+						 void** stream, int* device );
+/* sensor.c:43-270 b2SensorQueryCallback for every sensor at the end of a step: the
+   (sensor index, shape id) pairs whose shapes overlap (GJK distance with radii below
+   10 FLT_EPSILON), unordered. sensorShapeIds[i] < 0 skips sensor i. Waits for the device;
+   the returned array is valid until the next call. */
+int b2gDev_SensorOverlaps( b2gDeviceWorld* dw, const int* sensorShapeIds, int sensorCount, int shapeCount,
+						   const int** outPairs, int* outCount );
 /* the contact table of b2p_contacts built without allocating (noalloc.cu) */
 int b2gDev_ContactTableNoAlloc( b2gDeviceWorld* dw, int capacity, int* out, int outCapacity );
 
@@ -396,6 +403,8 @@ typedef struct b2gDevBatch b2gDevBatch;
 int b2gDev_BatchCreate( b2gDevBatch** out );
 void b2gDev_BatchDestroy( b2gDevBatch* batch );
 int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on );
+/* whether the world's device work is being recorded for a batched flush */
+int b2gDev_IsRecording( b2gDeviceWorld* dw );
 /* runs fn(ctx, i) for i in [0, count) on the caller's threads */
 typedef void ( *b2gParallelFor )( void* pool, int count, void ( *fn )( void* ctx, int index ), void* ctx );
 int b2gDev_BatchFlush( b2gDevBatch* batch, b2gDeviceWorld* const* worlds, int count, b2gParallelFor parallelFor, void* pool );

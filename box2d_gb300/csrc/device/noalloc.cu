@@ -12,8 +12,10 @@
  *     larger worlds are refused with -2 and a message;
  *   - the scratch is shared by every caller in the process: calls whose GPU work overlaps
  *     (two threads, two streams) race on it and must be serialized by the caller;
- *   - the first call on each device resolves the scratch address (cudaGetSymbolAddress)
- *     and must therefore happen before any stream capture that should contain later calls;
+ *   - the first call on each device resolves the scratch address (cudaGetSymbolAddress,
+ *     with the world's device current);
+ *   - a call waits for the world's stream and copies the table into the caller's (pageable)
+ *     host array, so it must be made outside any CUDA stream capture;
  *   - the kernel writes every scratch word it reads (the color map is reset inside the
  *     kernel, the row count is stored, not accumulated), so nothing has to be zeroed
  *     between calls.
@@ -86,7 +88,9 @@ __global__ void __launch_bounds__( B2G_NOALLOC_THREADS )
 		o[0] = i;
 		o[1] = c->shapeIdA;
 		o[2] = c->shapeIdB;
-		o[3] = colorOf[i];
+		/* a contact of a sleeping island is in no graph color (its id may still sit in a
+		   color list that is refreshed at the next step) */
+		o[3] = ( c->simFlags & B2G_S_ASLEEP ) ? B2_NULL_INDEX : colorOf[i];
 		o[4] = m->pointCount;
 		o[5] = m->pointCount > 0 ? (int)m->points[0].id : -1;
 		o[6] = m->pointCount > 1 ? (int)m->points[1].id : -1;
@@ -99,13 +103,11 @@ __global__ void __launch_bounds__( B2G_NOALLOC_THREADS )
 static pthread_mutex_t s_setupLock = PTHREAD_MUTEX_INITIALIZER;
 static unsigned char* s_scratch[B2G_NOALLOC_MAX_DEVICES];
 
-/* the scratch address on the current device, resolved once per device */
-static int noallocScratch( unsigned char** out )
+/* the scratch address on `dev` (the current device), resolved once per device */
+static int noallocScratch( int dev, unsigned char** out )
 {
-	int dev = 0;
-	cudaError_t e = cudaGetDevice( &dev );
-	if ( e != cudaSuccess ) return (int)e;
 	if ( dev < 0 || dev >= B2G_NOALLOC_MAX_DEVICES ) return (int)cudaErrorInvalidDevice;
+	cudaError_t e = cudaSuccess;
 	pthread_mutex_lock( &s_setupLock );
 	if ( s_scratch[dev] == NULL )
 	{
@@ -131,14 +133,23 @@ extern "C" int b2gDev_ContactTableNoAlloc( b2gDeviceWorld* dw, int capacity, int
 	const int* colorIds = NULL;
 	d_colorOffsets offsets;
 	void* stream = NULL;
-	b2gDev_ContactView( dw, &contacts, &colorIds, offsets.v, &stream );
+	int device = 0, current = 0;
+	b2gDev_ContactView( dw, &contacts, &colorIds, offsets.v, &stream, &device );
+	/* the world's device is current for the call (the scratch symbol and the kernel are
+	   per device); the caller's current device is restored afterwards */
+	cudaError_t e = cudaGetDevice( &current );
+	if ( e == cudaSuccess && current != device ) e = cudaSetDevice( device );
+	if ( e != cudaSuccess ) return -( 1000 + (int)e );
 	unsigned char* scratch = NULL;
-	int rc = noallocScratch( &scratch );
-	if ( rc != 0 ) return -( 1000 + rc );
-	cudaStream_t s = (cudaStream_t)stream;
-	k_contactTableNoAlloc<<<1, B2G_NOALLOC_THREADS, 0, s>>>( contacts, capacity, colorIds, offsets, scratch );
-	cudaError_t e = cudaGetLastError();
+	int rc = noallocScratch( device, &scratch );
 	int count = 0;
+	if ( rc != 0 ) e = (cudaError_t)rc;
+	cudaStream_t s = (cudaStream_t)stream;
+	if ( e == cudaSuccess )
+	{
+		k_contactTableNoAlloc<<<1, B2G_NOALLOC_THREADS, 0, s>>>( contacts, capacity, colorIds, offsets, scratch );
+		e = cudaGetLastError();
+	}
 	if ( e == cudaSuccess ) e = cudaMemcpyAsync( &count, scratch, sizeof( int ), cudaMemcpyDeviceToHost, s );
 	if ( e == cudaSuccess ) e = cudaStreamSynchronize( s );
 	int copy = count < outCapacity ? count : outCapacity;
@@ -146,6 +157,7 @@ extern "C" int b2gDev_ContactTableNoAlloc( b2gDeviceWorld* dw, int capacity, int
 		e = cudaMemcpyAsync( out, scratch + B2G_NOALLOC_HEADER_BYTES + (size_t)B2G_NOALLOC_MAX_CONTACT_IDS * 4,
 							 (size_t)copy * 8 * sizeof( int ), cudaMemcpyDeviceToHost, s );
 	if ( e == cudaSuccess ) e = cudaStreamSynchronize( s );
+	if ( current != device ) cudaSetDevice( current );
 	if ( e != cudaSuccess ) return -( 1000 + (int)e );
 	return count;
 }

@@ -89,6 +89,7 @@ struct d_deferred
 struct b2gDeviceWorld
 {
 	cudaStream_t stream;
+	int device; /* the CUDA device the world's buffers and stream live on */
 	d_deferred* defer;			 /* non-NULL: record device work for a batched flush */
 	std::vector<void*> retired; /* device buffers recorded work may name, freed after the flush */
 	cudaEvent_t ev[10];
@@ -194,6 +195,14 @@ struct b2gDeviceWorld
 	int pairsTimingPending;
 	cudaEvent_t syncEvent; /* blocking-sync event for waits of batched steps */
 	int blockingSync;
+	/* sensor overlap pass: sensor shape ids in, (sensor, shape) pairs out */
+	int* sensorIds;
+	int sensorIdsCap;
+	int2* sensorPairs;
+	int sensorPairsCap;
+	int* sensorCount;
+	int2* hSensorPairs;
+	int hSensorPairsCap;
 	/* upload arena (page-locked host + device) */
 	void* upHost;
 	void* upDev;
@@ -965,6 +974,7 @@ extern "C" int b2gDev_Create( b2gDeviceWorld** out )
 	if ( e != cudaSuccess ) return (int)e;
 	if ( count == 0 ) return (int)cudaErrorNoDevice;
 	b2gDeviceWorld* dw = new b2gDeviceWorld(); /* value-initialized: every field zero */
+	CK( cudaGetDevice( &dw->device ) );
 	/* a blocking stream: buffer growth (cudaMalloc + cudaMemset / cudaMemcpy on the legacy
 	   default stream) is then ordered before every kernel of this world */
 	CK( cudaStreamCreate( &dw->stream ) );
@@ -997,7 +1007,8 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->tree[1],	  dw->tree[2], dw->treeRaw[0], dw->treeRaw[1], dw->treeRaw[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  
 					  dw->moveStage, dw->pairPacked, dw->pairOffsets, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
 					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList,
-					  dw->sleepTime, dw->islandLocal, dw->islandInfo, dw->islandBits };
+					  dw->sleepTime, dw->islandLocal, dw->islandInfo, dw->islandBits, dw->sensorIds, dw->sensorPairs,
+					  dw->sensorCount };
 	b2gDev_CompFree( &dw->comp );
 	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
 		if ( dptrs[i] ) cudaFree( dptrs[i] );
@@ -1005,7 +1016,8 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	if ( dw->upHost ) cudaFreeHost( dw->upHost );
 	void* hptrs[] = { dw->hCounters, dw->hChanges,	   dw->hRecs,	   dw->hBoxes,	   dw->hPairs,	  dw->hPairCounts,
 					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw, dw->hSortKeys,
-					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV, dw->hSleepTime, dw->hIslandBits };
+					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV, dw->hSleepTime, dw->hIslandBits,
+					  dw->hSensorPairs };
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
 		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
 	free( dw->hSortTmp );
@@ -1521,8 +1533,9 @@ extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const in
 }
 
 extern "C" void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const int** colorIds, int* colorOffsets,
-									void** stream )
+									void** stream, int* device )
 {
+	*device = dw->device;
 	*contacts = dw->contacts;
 	*colorIds = dw->colorIds;
 	memcpy( colorOffsets, dw->colorOffsets, sizeof( dw->colorOffsets ) );
@@ -2622,6 +2635,86 @@ extern "C" int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on )
 		delete dw->defer;
 		dw->defer = NULL;
 	}
+	return 0;
+}
+
+extern "C" int b2gDev_IsRecording( b2gDeviceWorld* dw ) { return dw->defer != NULL; }
+
+/* sensor.c:43-120 b2SensorQueryCallback, one block per sensor over every shape: the tree
+   query's tests (the shape's fat box meets the sensor's box, its category meets the
+   sensor's mask), then the callback's (not the sensor itself, sensor events enabled on the
+   shape, another body, the shape filter), then GJK distance with radii in the sensor's
+   frame below 10 FLT_EPSILON */
+__global__ void k_sensorOverlaps( const int* __restrict__ sensorIds, int sensorCount, const b2gShape* __restrict__ shapes,
+								  const float4* __restrict__ aabb, const float4* __restrict__ fat, const float4* __restrict__ xf,
+								  int shapeCount, int2* out, int outCap, int* outCount )
+{
+	int sensorIndex = blockIdx.x;
+	if ( sensorIndex >= sensorCount ) return;
+	int sensorShapeId = sensorIds[sensorIndex];
+	if ( sensorShapeId < 0 ) return;
+	const b2gShape* sensor = shapes + sensorShapeId;
+	float4 q = aabb[sensorShapeId];
+	b2AABB query = { { q.x, q.y }, { q.z, q.w } };
+	float4 xs = xf[sensor->bodyId];
+	b2Transform sensorXf = { { xs.x, xs.y }, { xs.z, xs.w } };
+	d_proxy proxyA = d_shapeProxy( sensor );
+	for ( int shapeId = threadIdx.x; shapeId < shapeCount; shapeId += blockDim.x )
+	{
+		if ( shapeId == sensorShapeId ) continue;
+		const b2gShape* other = shapes + shapeId;
+		if ( other->type < 0 || ( other->categoryBits & sensor->maskBits ) == 0 ) continue;
+		if ( d_overlaps( query, fat[shapeId] ) == false ) continue;
+		if ( other->enableSensorEvents == 0 || other->bodyId == sensor->bodyId ) continue;
+		if ( d_shouldShapesCollide( sensor, other ) == false ) continue;
+		float4 xo = xf[other->bodyId];
+		b2Transform otherXf = { { xo.x, xo.y }, { xo.z, xo.w } };
+		d_proxy proxyB = d_shapeProxy( other );
+		d_simplexCache cache;
+		cache.count = 0;
+		float distance = d_shapeDistance( &proxyA, &proxyB, d_invMulTransforms( sensorXf, otherXf ), &cache );
+		distance = d_max( 0.0f, distance - proxyA.radius - proxyB.radius );
+		if ( distance < 10.0f * FLT_EPSILON )
+		{
+			int k = atomicAdd( outCount, 1 );
+			if ( k < outCap ) out[k] = make_int2( sensorIndex, shapeId );
+		}
+	}
+}
+
+extern "C" int b2gDev_SensorOverlaps( b2gDeviceWorld* dw, const int* sensorShapeIds, int sensorCount, int shapeCount,
+									  const int** outPairs, int* outCount )
+{
+	*outPairs = NULL;
+	*outCount = 0;
+	if ( sensorCount <= 0 ) return 0;
+	CK2( grow( dw, (void**)&dw->sensorIds, &dw->sensorIdsCap, sensorCount, sizeof( int ) ) );
+	if ( dw->sensorCount == NULL ) CK( cudaMalloc( &dw->sensorCount, sizeof( int ) ) );
+	if ( dw->sensorPairsCap == 0 ) CK2( grow( dw, (void**)&dw->sensorPairs, &dw->sensorPairsCap, 4 * sensorCount + 64, sizeof( int2 ) ) );
+	CK( cudaMemcpyAsync( dw->sensorIds, sensorShapeIds, (size_t)sensorCount * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) );
+	dw->h2dBytes += (long long)sensorCount * (long long)sizeof( int );
+	int count = 0;
+	for ( int attempt = 0; attempt < 2; ++attempt )
+	{
+		CK( cudaMemsetAsync( dw->sensorCount, 0, sizeof( int ), dw->stream ) );
+		k_sensorOverlaps<<<sensorCount, 128, 0, dw->stream>>>( dw->sensorIds, sensorCount, dw->shapes, dw->aabb, dw->fat, dw->xf,
+															   shapeCount, dw->sensorPairs, dw->sensorPairsCap, dw->sensorCount );
+		dw->launches += 1;
+		CK( cudaGetLastError() );
+		CK( cudaMemcpyAsync( &count, dw->sensorCount, sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaStreamSynchronize( dw->stream ) );
+		if ( count <= dw->sensorPairsCap ) break;
+		/* more overlaps than the output holds: grow it and run the pass again */
+		CK2( grow( dw, (void**)&dw->sensorPairs, &dw->sensorPairsCap, count, sizeof( int2 ) ) );
+	}
+	CK2( growHost( (void**)&dw->hSensorPairs, &dw->hSensorPairsCap, count > 0 ? count : 1, sizeof( int2 ) ) );
+	if ( count > 0 )
+	{
+		CK( cudaMemcpy( dw->hSensorPairs, dw->sensorPairs, (size_t)count * sizeof( int2 ), cudaMemcpyDeviceToHost ) );
+		dw->d2hBytes += (long long)count * (long long)sizeof( int2 );
+	}
+	*outPairs = (const int*)dw->hSensorPairs;
+	*outCount = count;
 	return 0;
 }
 

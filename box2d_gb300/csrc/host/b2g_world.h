@@ -72,7 +72,24 @@ typedef struct h_shape
 	};
 	uint16_t generation;
 	int enableContactEvents, enableHitEvents, isSensor;
+	int enableSensorEvents, sensorIndex; /* sensorIndex: its slot in the world's sensors, or -1 */
 } h_shape;
+
+/* a shape seen by a sensor (sensor.h b2Visitor) */
+typedef struct h_visitor
+{
+	int shapeId;
+	uint16_t generation;
+} h_visitor;
+typedef H_ARRAY( h_visitor ) h_visitorArray;
+
+/* a sensor shape's overlaps (sensor.h b2Sensor): the previous and current step's sorted
+   visitors, and the visitors continuous sweeps hit during the step */
+typedef struct h_sensor
+{
+	int shapeId;
+	h_visitorArray overlaps1, overlaps2, hits;
+} h_sensor;
 
 typedef struct h_contactEdge
 {
@@ -149,6 +166,7 @@ typedef struct h_world
 	H_ARRAY( b2gJoint ) jointRecords; /* by joint id; device copy is authoritative */
 	h_intArray awakeBodyIds;		  /* awake index -> body id */
 	int staticCount;
+	int staticJointCount; /* joints of the static set (between two non-dynamic bodies) */
 	h_intArray awakeContactIds;		  /* non-touching contacts, reference array order */
 	h_intArray disabledContactIds;	  /* non-touching contacts between sleeping bodies */
 	/* islands and sleeping (island.c) */
@@ -174,6 +192,11 @@ typedef struct h_world
 	b2Vec2 gravity;
 	float hitEventThreshold, restitutionThreshold, maxLinearSpeed, contactSpeed, contactHertz, contactDampingRatio;
 	int enableSleep, enableWarmStarting, enableContactSoftening, enableContinuous, locked;
+	/* sensors, in creation order (swap-removed) */
+	H_ARRAY( h_sensor ) sensors;
+	int sensorStep; /* stepIndex of the last sensor overlap pass */
+	H_ARRAY( b2SensorBeginTouchEvent ) sensorBeginEvents;
+	H_ARRAY( b2SensorEndTouchEvent ) sensorEndEvents[2];
 	/* events */
 	H_ARRAY( b2BodyMoveEvent ) moveEvents;
 	H_ARRAY( b2ContactBeginTouchEvent ) beginEvents;
@@ -248,6 +271,14 @@ void h_sleepPass( h_world* w, const uint32_t* awakeIslandBits, uint64_t splitKey
 /* device work of sets that slept or woke: sent inside a step, or before the next one */
 void h_flushSleepOps( h_world* w );
 h_world* h_worldByIndex( int index );
+/* the values b2World_GetStateHash mixes, in order, up to capacity; returns their count */
+int h_stateHashWords( h_world* w, uint32_t* words, int capacity );
+
+/* sensors (sensor.c): a new sensor shape's record; the overlap pass at the end of a step,
+   its end events going to sensorEndEvents[endIndex]; records freed with the world */
+void h_createSensor( h_world* w, h_shape* shape );
+void h_overlapSensors( h_world* w, int endIndex );
+void h_freeSensors( h_world* w );
 
 /* geometry helpers (geometry.c) */
 b2AABB h_computeFatShapeAABB( const h_shape* shape, b2Transform xf, float extra );

@@ -249,6 +249,11 @@ void b2World_StepBatch( const b2WorldId* worldIds, int worldCount, float timeSte
 		}
 		h_batchFlushLaunches = b2gDev_BatchLaunches( h_batchDevice );
 		for ( int i = 0; i < n; ++i ) b2gDev_BatchRecord( devs[i], 0 );
+		/* sensor overlaps of the worlds that have sensors, on the final state; their end
+		   events go to the buffer the step just completed (the one the reader uses) */
+		for ( int i = 0; i < n; ++i )
+			if ( worlds[i]->sensors.count > 0 && worlds[i]->sensorStep != worlds[i]->stepIndex )
+				h_overlapSensors( worlds[i], 1 - worlds[i]->endEventArrayIndex );
 		/* the move events of every world, from the state the last flush delivered, as the
 		   reference's finalize builds them inside the step */
 		uint64_t t0 = b2GetTicks();

@@ -179,7 +179,10 @@ static b2gJoint* h_createJoint( h_world* w, const b2JointDef* def, b2JointType t
 	int maxSetIndex = bodyA->setIndex > bodyB->setIndex ? bodyA->setIndex : bodyB->setIndex;
 	if ( bodyA->type != b2_dynamicBody && bodyB->type != b2_dynamicBody )
 	{
+		/* joint.c:265-275: the static set holds it, at the end of its joint array */
 		j->setIndex = H_STATIC_SET;
+		j->colorIndex = B2_NULL_INDEX;
+		j->localIndex = w->staticJointCount++;
 	}
 	else if ( bodyA->setIndex == H_AWAKE_SET || bodyB->setIndex == H_AWAKE_SET )
 	{

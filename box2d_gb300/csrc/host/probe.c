@@ -83,6 +83,14 @@ B2P_EXPORT int b2p_contact_floats( uint32_t packedWorldId, float* out, int capac
 	return n;
 }
 
+/* the values b2World_GetStateHash mixes, in order (to locate a bookkeeping difference) */
+B2P_EXPORT int b2p_state_words( uint32_t packedWorldId, uint32_t* out, int capacity )
+{
+	b2WorldId id = { (uint16_t)( packedWorldId >> 16 ), (uint16_t)( packedWorldId & 0xFFFF ) };
+	h_world* w = h_worldFromId( id );
+	return w == NULL ? -1 : h_stateHashWords( w, out, capacity );
+}
+
 /* device status of the last step (0 ok, 1 non-finite velocity, 2 capacity) */
 B2P_EXPORT int b2p_status( uint32_t packedWorldId )
 {

@@ -415,6 +415,7 @@ int h_stepBegin( h_world* w, float timeStep, int subStepCount )
 	w->moveEvents.count = 0;
 	w->moveEventsValid = 0;
 	w->beginEvents.count = 0;
+	w->sensorBeginEvents.count = 0;
 	memset( &w->profile, 0, sizeof( w->profile ) );
 	w->locked = 1;
 	w->stepTicks = b2GetTicks();
@@ -586,6 +587,14 @@ void h_stepFinish( h_world* w )
 	}
 	if ( w->stepTimeStep > 0.0f ) w->profile.solve = h_ms( w->stepT0 );
 	h_joinRebuild( w );
+	/* sensor overlaps come last (physics_world.c:961-966); a batched step runs them after
+	   its last flush, when the device state is final */
+	if ( w->sensors.count > 0 && b2gDev_IsRecording( w->dev ) == 0 )
+	{
+		uint64_t sensorTicks = b2GetTicks();
+		h_overlapSensors( w, w->endEventArrayIndex );
+		w->profile.sensors = h_ms( sensorTicks );
+	}
 	w->hostStateValid = 0;
 	w->mirrorValid = 0;
 	w->jointsHostValid = 0;
@@ -600,6 +609,7 @@ void h_stepFinish( h_world* w )
 	w->profile.step = h_ms( w->stepTicks );
 	w->endEventArrayIndex = 1 - w->endEventArrayIndex;
 	w->endEvents[w->endEventArrayIndex].count = 0;
+	w->sensorEndEvents[w->endEventArrayIndex].count = 0;
 	w->locked = 0;
 	(void)h_cmpInt;
 }

@@ -256,6 +256,7 @@ void b2DestroyWorld( b2WorldId worldId )
 	h_free( w->moveArray );
 	h_pairSetFree( &w->pairSet );
 	h_free( w->moveEvents );
+	h_freeSensors( w );
 	h_free( w->beginEvents );
 	h_free( w->endEvents[0] );
 	h_free( w->endEvents[1] );
@@ -316,49 +317,59 @@ int b2World_GetAwakeBodyCount( b2WorldId worldId ) { return h_worldFromId( world
 #define H_FNV_INIT 14695981039346656037ull
 #define H_FNV_PRIME 1099511628211ull
 
-static uint64_t h_fnvWord( uint64_t hash, uint32_t bits ) { return ( hash ^ (uint64_t)bits ) * H_FNV_PRIME; }
-static uint64_t h_fnvFloat( uint64_t hash, float f )
+/* the hash under construction; `words`, when set, also receives every value mixed in (a
+   probe for locating where two worlds' bookkeeping differs) */
+typedef struct h_fnv
+{
+	uint64_t hash;
+	uint32_t* words;
+	int count, capacity;
+} h_fnv;
+
+static void h_fnvWord( h_fnv* f, uint32_t bits )
+{
+	f->hash = ( f->hash ^ (uint64_t)bits ) * H_FNV_PRIME;
+	if ( f->words != NULL && f->count < f->capacity ) f->words[f->count] = bits;
+	f->count += 1;
+}
+static void h_fnvFloat( h_fnv* f, float v )
 {
 	uint32_t bits;
-	memcpy( &bits, &f, 4 );
-	return h_fnvWord( hash, bits );
+	memcpy( &bits, &v, 4 );
+	h_fnvWord( f, bits );
 }
-static uint64_t h_fnvInt( uint64_t hash, int v ) { return h_fnvWord( hash, (uint32_t)v ); }
-static uint64_t h_fnvBytes( uint64_t hash, const void* data, int n )
+static void h_fnvInt( h_fnv* f, int v ) { h_fnvWord( f, (uint32_t)v ); }
+static void h_fnvBytes( h_fnv* f, const void* data, int n )
 {
 	const uint8_t* b = (const uint8_t*)data;
-	for ( int i = 0; i < n; ++i ) hash = ( hash ^ (uint64_t)b[i] ) * H_FNV_PRIME;
-	return hash;
+	for ( int i = 0; i < n; ++i ) h_fnvWord( f, b[i] );
 }
-static uint64_t h_fnvPool( uint64_t hash, const h_idPool* pool )
+static void h_fnvPool( h_fnv* f, const h_idPool* pool )
 {
-	hash = h_fnvInt( hash, pool->nextIndex );
-	return h_fnvInt( hash, pool->nextIndex - pool->freeArray.count );
+	h_fnvInt( f, pool->nextIndex );
+	h_fnvInt( f, pool->nextIndex - pool->freeArray.count );
 }
 
-uint64_t b2World_GetStateHash( b2WorldId worldId )
+static void h_stateHash( h_world* w, h_fnv* f )
 {
-	h_world* w = h_worldFromId( worldId );
-	if ( w == NULL ) return 0;
 	h_syncFromDevice( w );
 	h_syncJointsFromDevice( w );
-	uint64_t hash = H_FNV_INIT;
 	for ( int i = 0; i < w->bodies.count; ++i )
 	{
 		const h_body* b = w->bodies.data + i;
 		if ( b->id != i ) continue;
-		hash = h_fnvFloat( hash, b->transform.p.x );
-		hash = h_fnvFloat( hash, b->transform.p.y );
-		hash = h_fnvFloat( hash, b->transform.q.c );
-		hash = h_fnvFloat( hash, b->transform.q.s );
+		h_fnvFloat( f, b->transform.p.x );
+		h_fnvFloat( f, b->transform.p.y );
+		h_fnvFloat( f, b->transform.q.c );
+		h_fnvFloat( f, b->transform.q.s );
 		if ( b->setIndex == H_AWAKE_SET )
 		{
-			hash = h_fnvFloat( hash, b->linearVelocity.x );
-			hash = h_fnvFloat( hash, b->linearVelocity.y );
-			hash = h_fnvFloat( hash, b->angularVelocity );
+			h_fnvFloat( f, b->linearVelocity.x );
+			h_fnvFloat( f, b->linearVelocity.y );
+			h_fnvFloat( f, b->angularVelocity );
 		}
-		hash = h_fnvInt( hash, b->setIndex );
-		hash = h_fnvInt( hash, b->localIndex );
+		h_fnvInt( f, b->setIndex );
+		h_fnvInt( f, b->localIndex );
 	}
 	int nc = w->contacts.count;
 	b2gContact* dc = NULL;
@@ -372,17 +383,17 @@ uint64_t b2World_GetStateHash( b2WorldId worldId )
 	{
 		const h_contact* c = w->contacts.data + i;
 		if ( c->contactId != i ) continue;
-		hash = h_fnvInt( hash, c->setIndex );
-		hash = h_fnvInt( hash, c->colorIndex );
-		hash = h_fnvInt( hash, c->localIndex );
+		h_fnvInt( f, c->setIndex );
+		h_fnvInt( f, c->colorIndex );
+		h_fnvInt( f, c->localIndex );
 		const b2Manifold* m = dc != NULL ? &dc[i].manifold : NULL;
 		int pointCount = m != NULL ? m->pointCount : 0;
-		hash = h_fnvInt( hash, pointCount );
+		h_fnvInt( f, pointCount );
 		for ( int k = 0; k < pointCount; ++k )
 		{
-			hash = h_fnvFloat( hash, m->points[k].normalImpulse );
-			hash = h_fnvFloat( hash, m->points[k].tangentImpulse );
-			hash = h_fnvFloat( hash, m->points[k].totalNormalImpulse );
+			h_fnvFloat( f, m->points[k].normalImpulse );
+			h_fnvFloat( f, m->points[k].tangentImpulse );
+			h_fnvFloat( f, m->points[k].totalNormalImpulse );
 		}
 	}
 	free( dc );
@@ -390,9 +401,9 @@ uint64_t b2World_GetStateHash( b2WorldId worldId )
 	{
 		const h_joint* j = w->joints.data + i;
 		if ( j->jointId != i ) continue;
-		hash = h_fnvInt( hash, j->setIndex );
-		hash = h_fnvInt( hash, j->colorIndex );
-		hash = h_fnvInt( hash, j->localIndex );
+		h_fnvInt( f, j->setIndex );
+		h_fnvInt( f, j->colorIndex );
+		h_fnvInt( f, j->localIndex );
 		const float* s = w->jointRecords.data[i].s;
 		/* the accumulated impulses of each type, in the slots host/joint.c lists */
 		switch ( j->type )
@@ -405,37 +416,53 @@ uint64_t b2World_GetStateHash( b2WorldId worldId )
 				int first = 0, count = j->type == b2_distanceJoint ? 4 : ( j->type == b2_wheelJoint ? 5 : 6 );
 				if ( j->type == b2_revoluteJoint || j->type == b2_prismaticJoint )
 				{
-					hash = h_fnvBytes( hash, s, 2 * (int)sizeof( float ) );
+					h_fnvBytes( f, s, 2 * (int)sizeof( float ) );
 					first = 2;
 				}
-				for ( int k = first; k < count; ++k ) hash = h_fnvFloat( hash, s[k] );
+				for ( int k = first; k < count; ++k ) h_fnvFloat( f, s[k] );
 				break;
 			}
 			case b2_weldJoint:
-				hash = h_fnvBytes( hash, s, 2 * (int)sizeof( float ) );
-				hash = h_fnvFloat( hash, s[2] );
+				h_fnvBytes( f, s, 2 * (int)sizeof( float ) );
+				h_fnvFloat( f, s[2] );
 				break;
 			case b2_moverJoint:
 			case b2_pogoJoint:
-				hash = h_fnvFloat( hash, s[0] );
-				hash = h_fnvFloat( hash, s[1] );
+				h_fnvFloat( f, s[0] );
+				h_fnvFloat( f, s[1] );
 				break;
 			case b2_motorJoint:
-				for ( int k = 0; k < 6; ++k ) hash = h_fnvFloat( hash, s[k] );
+				for ( int k = 0; k < 6; ++k ) h_fnvFloat( f, s[k] );
 				break;
 			default:
 				break;
 		}
 	}
-	hash = h_fnvPool( hash, &w->bodyIdPool );
-	hash = h_fnvPool( hash, &w->shapeIdPool );
-	hash = h_fnvPool( hash, &w->chainIdPool );
-	hash = h_fnvPool( hash, &w->contactIdPool );
-	hash = h_fnvPool( hash, &w->jointIdPool );
-	hash = h_fnvPool( hash, &w->islandIdPool );
-	hash = h_fnvPool( hash, &w->setIdPool );
-	hash = h_fnvInt( hash, w->sets.count );
-	return hash;
+	h_fnvPool( f, &w->bodyIdPool );
+	h_fnvPool( f, &w->shapeIdPool );
+	h_fnvPool( f, &w->chainIdPool );
+	h_fnvPool( f, &w->contactIdPool );
+	h_fnvPool( f, &w->jointIdPool );
+	h_fnvPool( f, &w->islandIdPool );
+	h_fnvPool( f, &w->setIdPool );
+	h_fnvInt( f, w->sets.count );
+}
+
+uint64_t b2World_GetStateHash( b2WorldId worldId )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w == NULL ) return 0;
+	h_fnv f = { H_FNV_INIT, NULL, 0, 0 };
+	h_stateHash( w, &f );
+	return f.hash;
+}
+
+/* the values b2World_GetStateHash mixes, in order (probe); returns their count */
+int h_stateHashWords( h_world* w, uint32_t* words, int capacity )
+{
+	h_fnv f = { H_FNV_INIT, words, 0, capacity };
+	h_stateHash( w, &f );
+	return f.count;
 }
 
 b2Profile b2World_GetProfile( b2WorldId worldId ) { return h_worldFromId( worldId )->profile; }
@@ -719,6 +746,7 @@ void h_ensureDevice( h_world* w )
 		d->maskBits = s->filter.maskBits;
 		d->groupIndex = s->filter.groupIndex;
 		d->isSensor = s->isSensor;
+		d->enableSensorEvents = s->enableSensorEvents;
 		{
 			b2Vec2 centroid = h_getShapeCentroid( s );
 			float minExtent, maxExtent;
@@ -1281,6 +1309,8 @@ static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const vo
 	s->enableContactEvents = def->enableContactEvents;
 	s->enableHitEvents = def->enableHitEvents;
 	s->isSensor = def->isSensor;
+	s->enableSensorEvents = def->enableSensorEvents;
+	s->sensorIndex = B2_NULL_INDEX;
 	s->proxyKey = B2_NULL_INDEX;
 	s->localCentroid = h_getShapeCentroid( s );
 	s->aabbMargin = h_computeShapeMargin( s );
@@ -1303,6 +1333,7 @@ static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const vo
 	s->nextShapeId = body->headShapeId;
 	body->headShapeId = shapeId;
 	body->shapeCount += 1;
+	if ( def->isSensor ) h_createSensor( w, s );
 	if ( def->updateBodyMass ) h_updateBodyMassData( w, body );
 	else body->flags |= B2G_DIRTY_MASS;
 	b2ShapeId id = { s->id + 1, bodyId.world0, s->generation };

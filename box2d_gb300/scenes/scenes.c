@@ -939,6 +939,90 @@ static void b2sOverflowScene( b2sScene* s, int count, b2sRng* rng )
 	}
 }
 
+/* Sensor scene (sensor.c, shape.c:180-205): static sensor boxes on the floor and a static
+   sensor circle in the air, a kinematic body carrying a sensor capsule across the scene, a
+   dynamic body whose sensor circle rides on its own solid box (a sensor never sees shapes
+   of its own body), a static sensor whose sensor events are off, and `count` falling
+   shapes of which two in three report to sensors and every fifth is in a category the
+   sensors' mask excludes. Sleeping is off. */
+static void b2sSensorZoo( b2sScene* s, int count, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	b2ShapeDef gd = b2DefaultShapeDef();
+	b2Polygon gbox = b2MakeOffsetBox( 20.0f, 0.5f, ( b2Vec2 ){ 0.0f, -0.5f }, b2MakeRot( 0.0f ) );
+	b2CreatePolygonShape( ground, &gd, &gbox );
+	b2Segment w1 = { { -20.0f, 0.0f }, { -20.0f, 20.0f } };
+	b2Segment w2 = { { 20.0f, 0.0f }, { 20.0f, 20.0f } };
+	b2CreateSegmentShape( ground, &gd, &w1 );
+	b2CreateSegmentShape( ground, &gd, &w2 );
+	b2ShapeDef sensorDef = b2DefaultShapeDef();
+	sensorDef.isSensor = true;
+	sensorDef.enableSensorEvents = true;
+	sensorDef.filter.maskBits = ~(uint64_t)4;
+	for ( int i = 0; i < 3; ++i )
+	{
+		b2Polygon zone = b2MakeOffsetBox( 2.0f, 1.0f, ( b2Vec2 ){ -12.0f + 12.0f * i, 1.0f }, b2MakeRot( 0.0f ) );
+		b2CreatePolygonShape( ground, &sensorDef, &zone );
+	}
+	{
+		b2Circle zone = { { 5.0f, 4.0f }, 1.5f };
+		b2CreateCircleShape( ground, &sensorDef, &zone );
+		b2ShapeDef quiet = sensorDef;
+		quiet.enableSensorEvents = false;
+		b2Circle silent = { { -5.0f, 4.0f }, 1.5f };
+		b2CreateCircleShape( ground, &quiet, &silent );
+	}
+	{
+		b2BodyDef bd = b2DefaultBodyDef();
+		bd.type = b2_kinematicBody;
+		bd.position.x = -18.0f;
+		bd.position.y = 6.0f;
+		bd.linearVelocity.x = 1.5f;
+		b2BodyId mover = b2CreateBody( s->worldId, &bd );
+		b2sAddBody( s, mover, 0 );
+		b2Capsule cap = { { -1.0f, 0.0f }, { 1.0f, 0.0f }, 0.5f };
+		b2CreateCapsuleShape( mover, &sensorDef, &cap );
+	}
+	{
+		b2BodyId carrier = b2sBody( s, b2_dynamicBody, 0.0f, 9.0f );
+		b2ShapeDef solid = b2DefaultShapeDef();
+		solid.enableSensorEvents = true;
+		b2Polygon box = b2MakeBox( 0.5f, 0.5f );
+		b2CreatePolygonShape( carrier, &solid, &box );
+		b2Circle ring = { { 0.0f, 0.0f }, 1.2f };
+		b2CreateCircleShape( carrier, &sensorDef, &ring );
+	}
+	for ( int k = 0; k < count; ++k )
+	{
+		float x = b2sRandomFloatRange( rng, -18.0f, 18.0f );
+		float y = b2sRandomFloatRange( rng, 2.0f, 14.0f );
+		b2BodyId body = b2sBody( s, b2_dynamicBody, x, y );
+		b2ShapeDef sd = b2DefaultShapeDef();
+		sd.enableSensorEvents = ( k % 3 ) != 0;
+		if ( k % 5 == 4 ) sd.filter.categoryBits = 4;
+		int kind = b2sRandomIntRange( rng, 0, 2 );
+		if ( kind == 0 )
+		{
+			b2Circle c = { { 0.0f, 0.0f }, b2sRandomFloatRange( rng, 0.2f, 0.5f ) };
+			b2CreateCircleShape( body, &sd, &c );
+		}
+		else if ( kind == 1 )
+		{
+			float hx = b2sRandomFloatRange( rng, 0.2f, 0.5f );
+			float hy = b2sRandomFloatRange( rng, 0.2f, 0.5f );
+			b2Polygon p = b2MakeBox( hx, hy );
+			b2CreatePolygonShape( body, &sd, &p );
+		}
+		else
+		{
+			float r = b2sRandomFloatRange( rng, 0.15f, 0.3f );
+			b2Capsule c = { { -0.3f, 0.0f }, { 0.3f, 0.0f }, r };
+			b2CreateCapsuleShape( body, &sd, &c );
+		}
+	}
+}
+
 enum
 {
 	B2S_LARGE_PYRAMID = 0,
@@ -955,6 +1039,7 @@ enum
 	B2S_SLEEP_PYRAMIDS = 11,
 	B2S_JOINT_MIX = 12,
 	B2S_OVERFLOW = 13,
+	B2S_SENSOR_ZOO = 14,
 };
 
 /* Worker threads requested in the world definition of scenes created from now on (0 keeps
@@ -1009,6 +1094,7 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 		case B2S_SLEEP_PYRAMIDS: b2sSleepPyramids( s, a, b, c ); break;
 		case B2S_JOINT_MIX: b2sJointMix( s, a, &rng ); break;
 		case B2S_OVERFLOW: b2sOverflowScene( s, a, &rng ); break;
+		case B2S_SENSOR_ZOO: b2sSensorZoo( s, a, &rng ); break;
 		default: break;
 	}
 	return h;
@@ -1229,6 +1315,31 @@ B2S_EXPORT int b2s_contact_events( int h, int* out, int capacity )
 	}
 	return n;
 }
+
+#ifndef B2S_NO_SENSORS
+/* The last step's sensor begin/end touch events (b2World_GetSensorEvents), 5 ints per event,
+   begin events first: kind (0 begin, 1 end), sensor shape id, visitor shape id (index1 - 1),
+   sensor shape generation, visitor shape generation. Returns the event count. */
+B2S_EXPORT int b2s_sensor_events( int h, int* out, int capacity )
+{
+	b2SensorEvents e = b2World_GetSensorEvents( b2s_scenes[h].worldId );
+	int n = 0;
+	for ( int i = 0; i < e.beginCount + e.endCount; ++i, ++n )
+	{
+		if ( n >= capacity ) continue;
+		int end = i >= e.beginCount;
+		b2ShapeId sensor = end ? e.endEvents[i - e.beginCount].sensorShapeId : e.beginEvents[i].sensorShapeId;
+		b2ShapeId visitor = end ? e.endEvents[i - e.beginCount].visitorShapeId : e.beginEvents[i].visitorShapeId;
+		int* o = out + 5 * n;
+		o[0] = end;
+		o[1] = sensor.index1 - 1;
+		o[2] = visitor.index1 - 1;
+		o[3] = sensor.generation;
+		o[4] = visitor.generation;
+	}
+	return n;
+}
+#endif
 
 #ifndef B2S_NO_ISLANDS
 /* the library's own b2World_GetStateHash of the scene's world */

@@ -20,18 +20,25 @@ extern "C"
 int b2p_contacts( uint32_t packedWorldId, int* out, int capacity );
 
 /* The table of b2p_contacts built without allocating anything (no counterpart in the
-   reference). For callers that may not allocate while they run -- a real-time loop or a
-   capture of a CUDA stream, where cudaMalloc/cudaFree and host malloc would stall or be
-   illegal. Limit: 32768 contact ids per world (-2 and a message above it). The scratch is
-   one fixed device array per process: calls whose GPU work overlaps race on it, and the
-   first call on a device (which resolves that array) must precede any stream capture.
-   Returns the row count (may exceed capacity), -1 for an unknown or never-stepped world,
-   or -(1000 + CUDA error code). */
+   reference). For callers that may not allocate while they run, such as a real-time loop
+   that must not stall in cudaMalloc/cudaFree or host malloc. Limit: 32768 contact ids per
+   world (-2 and a message above it). The scratch is one fixed device array per device:
+   calls whose GPU work overlaps race on it. A call waits for the world's stream and copies
+   into the caller's host array, so it cannot be made inside a CUDA stream capture.
+   Returns the row count (may exceed capacity); -1 for an unknown world or one that has not
+   been stepped with a positive time step since its last change made through the API (a
+   body, shape or joint created or destroyed, a body woken, moved or given a velocity while
+   asleep); or -(1000 + CUDA error code). */
 int b2p_contacts_noalloc( uint32_t packedWorldId, int* out, int capacity );
 
 /* 12 floats per live contact: normal (2), then per point: separation, normalImpulse,
    tangentImpulse, anchorA (2). Returns the row count. */
 int b2p_contact_floats( uint32_t packedWorldId, float* out, int capacity );
+
+/* The 32-bit values b2World_GetStateHash mixes into its hash, in order, up to capacity
+   (bytes mixed one by one appear one per value); returns their count. For locating where
+   two worlds' state or bookkeeping differ. */
+int b2p_state_words( uint32_t packedWorldId, uint32_t* out, int capacity );
 
 /* Device status of the last step: 0 ok, 1 non-finite body velocity, 2 capacity exceeded. */
 int b2p_status( uint32_t packedWorldId );
@@ -98,6 +105,10 @@ int b2s_move_events_many( const int* handles, int count, float* out, int capacit
    event, begin events first: kind (0 begin, 1 end), shape A id, shape B id, contact id
    (index1 - 1), contact generation, up to capacity; returns the event count */
 int b2s_contact_events( int handle, int* out, int capacity );
+/* the last step's sensor begin/end touch events (b2World_GetSensorEvents), 5 ints per
+   event, begin events first: kind (0 begin, 1 end), sensor shape id, visitor shape id,
+   sensor generation, visitor generation; returns the event count (not in the oracle) */
+int b2s_sensor_events( int handle, int* out, int capacity );
 /* b2World_GetStateHash of the scene's world (not in the oracle, which has no islands) */
 uint64_t b2s_world_state_hash( int handle );
 /* FNV-1a 64 over the bit patterns of b2s_get_state */

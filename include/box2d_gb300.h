@@ -557,6 +557,27 @@ typedef struct b2ContactEvents
 	int hitCount;
 } b2ContactEvents;
 
+/* sensor events (types.h:1030-1073) */
+typedef struct b2SensorBeginTouchEvent
+{
+	b2ShapeId sensorShapeId;
+	b2ShapeId visitorShapeId;
+} b2SensorBeginTouchEvent;
+
+typedef struct b2SensorEndTouchEvent
+{
+	b2ShapeId sensorShapeId;
+	b2ShapeId visitorShapeId;
+} b2SensorEndTouchEvent;
+
+typedef struct b2SensorEvents
+{
+	b2SensorBeginTouchEvent* beginEvents;
+	b2SensorEndTouchEvent* endEvents;
+	int beginCount;
+	int endCount;
+} b2SensorEvents;
+
 typedef struct b2BodyMoveEvent
 {
 	void* userData;
@@ -615,6 +636,7 @@ B2G_API void b2World_Step( b2WorldId worldId, float timeStep, int subStepCount )
 B2G_API void b2World_StepBatch( const b2WorldId* worldIds, int worldCount, float timeStep, int subStepCount, int threadCount );
 B2G_API b2BodyEvents b2World_GetBodyEvents( b2WorldId worldId );
 B2G_API b2ContactEvents b2World_GetContactEvents( b2WorldId worldId );
+B2G_API b2SensorEvents b2World_GetSensorEvents( b2WorldId worldId );
 B2G_API void b2World_EnableSleeping( b2WorldId worldId, bool flag );
 B2G_API bool b2World_IsSleepingEnabled( b2WorldId worldId );
 B2G_API void b2World_EnableContinuous( b2WorldId worldId, bool flag );
@@ -668,6 +690,12 @@ B2G_API b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, 
 B2G_API b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Capsule* capsule );
 B2G_API b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon );
 B2G_API void b2Shape_SetFriction( b2ShapeId shapeId, float friction );
+/* sensors (shape.c:1109, :1400-1415, :1780-1825; box2d.h:703-856) */
+B2G_API bool b2Shape_IsSensor( b2ShapeId shapeId );
+B2G_API void b2Shape_EnableSensorEvents( b2ShapeId shapeId, bool flag );
+B2G_API bool b2Shape_AreSensorEventsEnabled( b2ShapeId shapeId );
+B2G_API int b2Shape_GetSensorCapacity( b2ShapeId shapeId );
+B2G_API int b2Shape_GetSensorData( b2ShapeId shapeId, b2ShapeId* visitorIds, int capacity );
 B2G_API float b2Shape_GetFriction( b2ShapeId shapeId );
 B2G_API int b2Body_GetShapeCount( b2BodyId bodyId );
 B2G_API int b2Body_GetShapes( b2BodyId bodyId, b2ShapeId* shapeArray, int capacity );

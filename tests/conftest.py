@@ -77,29 +77,31 @@ def gpu_lib():
 
 
 class EventCheck:
-    """Checks a scene's contact begin/end touch events step by step against a fixture's
-    `contact_events` record (per-step counts, one sha256 over every step's rows)."""
+    """Checks a scene's contact (or sensor) begin/end touch events step by step against a
+    fixture's `contact_events` (`sensor_events`) record: per-step counts and one sha256 over
+    every step's rows."""
 
-    def __init__(self, g: dict):
+    def __init__(self, g: dict, key: str = "contact_events"):
         import hashlib
 
-        self.rec = g.get("contact_events")
+        self.rec = g.get(key)
+        self.key = key
         self.h = hashlib.sha256()
         self.name = g.get("scene", "")
 
     def step(self, scene, k: int) -> None:
         if self.rec is None:
             return
-        ev = scene.contact_events()
+        ev = scene.contact_events() if self.key == "contact_events" else scene.sensor_events()
         self.h.update(len(ev).to_bytes(4, "little"))
         self.h.update(ev.astype("<i4").tobytes())
         begin, end = int((ev[:, 0] == 0).sum()), int((ev[:, 0] == 1).sum())
         assert (begin, end) == (self.rec["begin_per_step"][k - 1], self.rec["end_per_step"][k - 1]), \
-            f"{self.name}: contact begin/end event counts at step {k}"
+            f"{self.name}: {self.key} begin/end counts at step {k}"
 
     def finish(self, steps: int) -> None:
         if self.rec is not None and steps == len(self.rec["begin_per_step"]):
-            assert self.h.hexdigest() == self.rec["sha256"], f"{self.name}: contact begin/end events differ"
+            assert self.h.hexdigest() == self.rec["sha256"], f"{self.name}: {self.key} differ"
 
 
 def lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps, check_every=1):

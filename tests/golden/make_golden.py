@@ -44,6 +44,8 @@ SCENES = [
     ("overflow_2", B.OVERFLOW, 2, 0, 0, 4, 0, 240, [1, 60, 240]),
     # forces, torques, impulses, teleports and target transforms applied between steps
     ("body_api_zoo", B.SHAPE_ZOO, 60, 0, 0, 9, 0, 150, [1, 75, 150]),
+    # sensors: begin/end overlap events of static, kinematic and dynamic sensor shapes
+    ("sensor_zoo_60", B.SENSOR_ZOO, 60, 0, 0, 5, B.NO_CONTINUOUS, 240, [1, 120, 240]),
 ]
 
 # sleeping on: islands fall asleep and wake; per step also the awake body count. The
@@ -106,9 +108,11 @@ def main() -> None:
         with B.Scene(ref, kind, a, b, c, seed, flags) as s:
             hashes, digests, awake, world_hashes = [], {}, [], []
             events = EventDigest()
+            sensor_events = EventDigest()
             for k in range(1, steps + 1):
                 s.step()
                 events.add(s.contact_events())
+                sensor_events.add(s.sensor_events())
                 for action in script:
                     if action[0] == k:
                         s.apply(action[1:])
@@ -123,6 +127,7 @@ def main() -> None:
             data = {"scene": name, "kind": kind, "a": a, "b": b, "c": c, "seed": seed, "flags": flags,
                     "dt": 1.0 / 60.0, "substeps": 4, "bodies": s.body_count, "state_hashes": hashes,
                     "contact_digests": digests, "contact_events": events.record(),
+                    "sensor_events": sensor_events.record(),
                     "world_state_hashes": world_hashes,
                     "source": "reference built from its own sources (oracle/Makefile ref)"}
             if sleeping:

@@ -48,7 +48,11 @@ def test_oracle_exports_the_public_api(oracle):
             "b2Body_SetAwake", "b2Body_GetSleepThreshold",
             # the state hash covers island and solver-set bookkeeping the oracle does not
             # restate; the GB300 library is checked against the reference's values directly
-            "b2World_GetStateHash", "b2s_world_state_hash"}
+            "b2World_GetStateHash", "b2s_world_state_hash", "b2p_state_words",
+            # sensors are checked against fixtures recorded from the reference itself
+            "b2World_GetSensorEvents", "b2Shape_IsSensor", "b2Shape_EnableSensorEvents",
+            "b2Shape_AreSensorEventsEnabled", "b2Shape_GetSensorCapacity", "b2Shape_GetSensorData",
+            "b2s_sensor_events"}
     # differentiable stepping (box2d_gb300_diff.h) is an extension of the GB300 library; its
     # checker is the host tangent-linear code, not the oracle's public API
     missing = [n for n in sorted(declared_functions())

@@ -22,9 +22,11 @@ def test_gpu_matches_reference_fixture(gpu_lib, name):
         assert s.body_count == g["bodies"]
         script = g.get("script", [])
         events = EventCheck(g)
+        sensor_events = EventCheck(g, "sensor_events")
         for k, expected in enumerate(g["state_hashes"], start=1):
             s.step(1, g["dt"], g["substeps"])
             events.step(s, k)
+            sensor_events.step(s, k)
             for action in script:
                 if action[0] == k:
                     s.apply(action[1:])
@@ -41,6 +43,7 @@ def test_gpu_matches_reference_fixture(gpu_lib, name):
                 assert hashlib.sha256(table.astype("<i4").tobytes()).hexdigest() == d["sha256"], \
                     f"{name}: contact table (ids, pairs, colors, feature ids) at step {k}"
         events.finish(len(g["state_hashes"]))
+        sensor_events.finish(len(g["state_hashes"]))
 
 
 def _lockstep(*args, **kw):

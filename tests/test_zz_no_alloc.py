@@ -38,6 +38,32 @@ def test_noalloc_contact_table_matches_b2p_contacts(gpu_lib, kind, a, b, c, seed
                 assert (table[n:] == -7).all(), "rows past the count must stay untouched"
 
 
+def test_noalloc_contact_table_in_a_sleeping_world(gpu_lib):
+    """Islands fall asleep at the end of a step: their contacts leave the graph colors (the
+    table reports color -1 for them) while the device color lists are refreshed only at
+    the next step. A world woken between steps is refused until it is stepped again."""
+    with B.Scene(gpu_lib, B.SLEEP_PYRAMIDS, 3, 8, 80) as s:
+        saw_sleeping = False
+        for _ in range(14):
+            s.step(25)
+            expected = s.contacts()
+            n, table = _noalloc_table(gpu_lib, s.world_id, max(1, expected.shape[0]) + 4)
+            assert n == expected.shape[0]
+            assert (table[:n] == expected).all()
+            saw_sleeping |= bool(((expected[:, 7] == 1) & (expected[:, 3] == -1)).any())
+        assert saw_sleeping, "no touching contact of a sleeping island was seen"
+        _, awake = s.awake()
+        asleep = [i for i in range(1, len(awake)) if awake[i] == 0]
+        assert asleep
+        s.apply(["velocity", asleep[-1], 0.0, 3.0, 0.0])  # wakes that body's island between steps
+        n, _ = _noalloc_table(gpu_lib, s.world_id, 16)
+        assert n == -1
+        s.step(1)
+        expected = s.contacts()
+        n, table = _noalloc_table(gpu_lib, s.world_id, max(1, expected.shape[0]))
+        assert n == expected.shape[0] and (table[:n] == expected).all()
+
+
 def test_noalloc_contact_table_small_capacity_reports_full_count(gpu_lib):
     with B.Scene(gpu_lib, B.LARGE_PYRAMID, 10, 0) as s:
         s.step(5)
