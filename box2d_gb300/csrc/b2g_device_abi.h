@@ -98,6 +98,9 @@ typedef struct b2gContact
 	b2Rot cachedRotationA, cachedRotationB;
 	b2Transform cachedRelativePose;
 	b2Manifold manifold;
+	/* GJK simplex cache (contact.h b2ContactSim cache): vertex count and the vertex indices
+	   on each shape; warm-starts the distance query of chain-segment manifolds */
+	uint8_t cacheCount, cacheA[3], cacheB[3], cachePad;
 } b2gContact;
 
 /* new contact written by the host into the contact slot of its id */

@@ -68,6 +68,7 @@ static __device__ d_proxy d_shapeProxy( const b2gShape* s )
 			p.radius = s->radius;
 			break;
 		case b2_segmentShape:
+		case b2_chainSegmentShape:
 			p.points[0] = s->v[0];
 			p.points[1] = s->v[1];
 			p.count = 2;
@@ -230,9 +231,11 @@ static __device__ b2Vec2 d_solveSimplex3( d_simplex* s )
 	return d_v( 0.0f, 0.0f );
 }
 
-/* distance.c:424-612 without radii: the distance only, in the frame of proxy A, with proxy
-   B placed by `transform`; the simplex cache is updated */
-static __device__ float d_shapeDistance( const d_proxy* proxyA, const d_proxy* proxyB, b2Transform transform, d_simplexCache* cache )
+/* distance.c:424-612 without radii: the distance in the frame of proxy A, with proxy B
+   placed by `transform`, and the witness points on both (when pointA is not null); the
+   simplex cache is updated */
+static __device__ float d_shapeDistanceWitness( const d_proxy* proxyA, const d_proxy* proxyB, b2Transform transform,
+												 d_simplexCache* cache, b2Vec2* pointA, b2Vec2* pointB )
 {
 	d_proxy localB;
 	localB.count = proxyB->count;
@@ -301,11 +304,16 @@ static __device__ float d_shapeDistance( const d_proxy* proxyA, const d_proxy* p
 		if ( duplicate ) break;
 		s.count += 1;
 	}
-	if ( overlapped == false )
+	if ( overlapped == false || pointA != nullptr )
 	{
-		b2Vec2 pointA, pointB;
-		d_witnessPoints( &s, &pointA, &pointB );
-		distance = d_distance( pointA, pointB );
+		b2Vec2 wA, wB;
+		d_witnessPoints( &s, &wA, &wB );
+		if ( overlapped == false ) distance = d_distance( wA, wB );
+		if ( pointA != nullptr )
+		{
+			*pointA = wA;
+			*pointB = wB;
+		}
 	}
 	cache->count = s.count;
 	for ( int i = 0; i < s.count; ++i )
@@ -314,6 +322,11 @@ static __device__ float d_shapeDistance( const d_proxy* proxyA, const d_proxy* p
 		cache->indexB[i] = s.v[i].indexB;
 	}
 	return distance;
+}
+
+static __device__ float d_shapeDistance( const d_proxy* proxyA, const d_proxy* proxyB, b2Transform transform, d_simplexCache* cache )
+{
+	return d_shapeDistanceWitness( proxyA, proxyB, transform, cache, nullptr, nullptr );
 }
 
 enum
@@ -591,10 +604,19 @@ static __device__ bool d_jointAllowsCollision( const d_ccdWorld& cw, int bodyA, 
 	return true;
 }
 
+/* the fast shape's centroid at the sweep's start and end (in the base frame) and the core
+   distance (B2_CORE_FRACTION of the fast body's minimum extent) */
+struct d_fastShape
+{
+	b2Vec2 centroid1, centroid2;
+	float coreDistance;
+};
+
 /* solver.c:183-376 b2ContinuousQueryCallback for one static candidate; returns the new
    fraction (unchanged when there is no hit) */
 static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId, int fastShapeId, const b2gShape* fastShape,
-											   const d_sweep& fastSweep, b2Vec2 base, float fraction, bool* hit )
+											   const d_sweep& fastSweep, b2Vec2 base, float fraction, bool* hit,
+											   const d_fastShape& fast )
 {
 	if ( shapeId == fastShapeId ) return fraction;
 	const b2gShape* shape = cw.shapes + shapeId;
@@ -604,6 +626,23 @@ static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId
 	int bodyId = shape->bodyId;
 	if ( cw.bodyFlags[bodyId] & B2G_IS_BULLET ) return fraction;
 	if ( d_jointAllowsCollision( cw, fastShape->bodyId, bodyId ) == false ) return fraction;
+	if ( shape->type == b2_chainSegmentShape )
+	{
+		/* solver.c:258-281: early out on fast movement parallel to, or from behind, a chain */
+		float4 xb = cw.xf[bodyId];
+		b2Transform transform = { { xb.x - base.x, xb.y - base.y }, { xb.z, xb.w } };
+		b2Vec2 p1 = d_transformPoint( transform, shape->v[0] );
+		b2Vec2 p2 = d_transformPoint( transform, shape->v[1] );
+		float length;
+		b2Vec2 e = d_getLengthAndNormalize( &length, d_sub( p2, p1 ) );
+		if ( length > D_LINEAR_SLOP )
+		{
+			float separation1 = d_cross( d_sub( fast.centroid1, p1 ), e );
+			float separation2 = d_cross( d_sub( fast.centroid2, p1 ), e );
+			if ( separation1 < 0.0f || ( separation1 - separation2 < fast.coreDistance && separation2 > fast.coreDistance ) )
+				return fraction;
+		}
+	}
 	d_proxy proxyA = d_shapeProxy( shape );
 	d_proxy proxyB = d_shapeProxy( fastShape );
 	/* a static body's sweep is at rest: center0 = center, rotation0 = rotation */
@@ -637,7 +676,8 @@ static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId
 /* dynamic_tree.c b2DynamicTree_Query over the static tree with the swept box, visiting
    overlapping leaves in the reference's order (children pushed child1 then child2) */
 static __device__ float d_continuousQuery( const d_ccdWorld& cw, float4 box, int fastShapeId, const b2gShape* fastShape,
-										   const d_sweep& fastSweep, b2Vec2 base, float fraction, bool* hit, bool* overflow )
+										   const d_sweep& fastSweep, b2Vec2 base, float fraction, bool* hit, bool* overflow,
+										   const d_fastShape& fast )
 {
 	int root = cw.staticRoot;
 	if ( root < 0 ) return fraction;
@@ -653,7 +693,7 @@ static __device__ float d_continuousQuery( const d_ccdWorld& cw, float4 box, int
 		int2 e = stack[--sp];
 		if ( e.x < 0 )
 		{
-			fraction = d_continuousCandidate( cw, e.y, fastShapeId, fastShape, fastSweep, base, fraction, hit );
+			fraction = d_continuousCandidate( cw, e.y, fastShapeId, fastShape, fastSweep, base, fraction, hit, fast );
 			continue;
 		}
 		const b2gTreeNode c1 = cw.staticTree[e.x];

@@ -6,6 +6,7 @@
 #pragma once
 
 #include "math.cuh"
+#include "ccd.cuh"
 
 #define D_MAKE_ID( A, B ) ( (uint16_t)( ( (uint8_t)( A ) << 8 ) | (uint8_t)( B ) ) )
 
@@ -587,11 +588,366 @@ static __device__ b2Polygon d_shapePolygon( const b2gShape* s )
 	return p;
 }
 
+
+/* ---- chain segments (manifold.c:1042-1641): one-sided segments with ghost vertices that
+   smooth the collision across the chain's joints. A chain segment keeps its points in v[0],
+   v[1] and its ghost vertices in v[2] (before point 1) and v[3] (after point 2). ---- */
+
+/* manifold.c:1042-1122 */
+static __device__ b2LocalManifold d_collideChainSegmentAndCircle( const b2gShape* seg, const b2Circle* circleB, b2Transform xf )
+{
+	b2LocalManifold manifold = d_emptyManifold();
+	b2Vec2 pB = d_transformPoint( xf, circleB->center );
+	b2Vec2 p1 = seg->v[0], p2 = seg->v[1];
+	b2Vec2 e = d_sub( p2, p1 );
+	float offset = d_dot( d_rightPerp( e ), d_sub( pB, p1 ) );
+	if ( offset < 0.0f ) return manifold;
+	float u = d_dot( e, d_sub( p2, pB ) );
+	float v = d_dot( e, d_sub( pB, p1 ) );
+	b2Vec2 pA;
+	if ( v <= 0.0f )
+	{
+		b2Vec2 prevEdge = d_sub( p1, seg->v[2] );
+		float uPrev = d_dot( prevEdge, d_sub( pB, p1 ) );
+		if ( uPrev <= 0.0f ) return manifold;
+		pA = p1;
+	}
+	else if ( u <= 0.0f )
+	{
+		b2Vec2 nextEdge = d_sub( seg->v[3], p2 );
+		float vNext = d_dot( nextEdge, d_sub( pB, p2 ) );
+		if ( vNext > 0.0f ) return manifold;
+		pA = p2;
+	}
+	else
+	{
+		float ee = d_dot( e, e );
+		pA = d_v( u * p1.x + v * p2.x, u * p1.y + v * p2.y );
+		pA = ee > 0.0f ? d_mulSV( 1.0f / ee, pA ) : p1;
+	}
+	float distance;
+	b2Vec2 normal = d_getLengthAndNormalize( &distance, d_sub( pB, pA ) );
+	float radius = circleB->radius;
+	float separation = distance - radius;
+	if ( separation > D_SPECULATIVE_DISTANCE ) return manifold;
+	b2Vec2 cA = pA;
+	b2Vec2 cB = d_mulAdd( pB, -radius, normal );
+	manifold.normal = normal;
+	manifold.points[0].point = d_lerp( cA, cB, 0.5f );
+	manifold.points[0].separation = separation;
+	manifold.points[0].id = 0;
+	manifold.pointCount = 1;
+	return manifold;
+}
+
+/* manifold.c:1131-1196: two-point manifold from the overlap of edge (a1, a2) with the
+   incident edge (b1, b2) along `normal` */
+static __device__ b2LocalManifold d_clipSegments( b2Vec2 a1, b2Vec2 a2, b2Vec2 b1, b2Vec2 b2, b2Vec2 normal, float ra, float rb,
+												  uint16_t id1, uint16_t id2 )
+{
+	b2LocalManifold manifold = d_emptyManifold();
+	b2Vec2 tangent = d_leftPerp( normal );
+	float lower1 = 0.0f;
+	float upper1 = d_dot( d_sub( a2, a1 ), tangent );
+	float upper2 = d_dot( d_sub( b1, a1 ), tangent );
+	float lower2 = d_dot( d_sub( b2, a1 ), tangent );
+	if ( upper2 < lower1 || upper1 < lower2 ) return manifold;
+	b2Vec2 vLower;
+	if ( lower2 < lower1 && upper2 - lower2 > FLT_EPSILON ) vLower = d_lerp( b2, b1, ( lower1 - lower2 ) / ( upper2 - lower2 ) );
+	else vLower = b2;
+	b2Vec2 vUpper;
+	if ( upper2 > upper1 && upper2 - lower2 > FLT_EPSILON ) vUpper = d_lerp( b2, b1, ( upper1 - lower2 ) / ( upper2 - lower2 ) );
+	else vUpper = b1;
+	float separationLower = d_dot( d_sub( vLower, a1 ), normal );
+	float separationUpper = d_dot( d_sub( vUpper, a1 ), normal );
+	vLower = d_mulAdd( vLower, 0.5f * ( ra - rb - separationLower ), normal );
+	vUpper = d_mulAdd( vUpper, 0.5f * ( ra - rb - separationUpper ), normal );
+	float radius = ra + rb;
+	manifold.normal = normal;
+	manifold.points[0].point = vLower;
+	manifold.points[0].separation = separationLower - radius;
+	manifold.points[0].id = id1;
+	manifold.points[1].point = vUpper;
+	manifold.points[1].separation = separationUpper - radius;
+	manifold.points[1].id = id2;
+	manifold.pointCount = 2;
+	return manifold;
+}
+
+enum
+{
+	D_NORMAL_SKIP = 0,
+	D_NORMAL_ADMIT = 1,
+	D_NORMAL_SNAP = 2,
+};
+
+struct d_chainParams
+{
+	b2Vec2 edge1, normal0, normal2;
+	bool convex1, convex2;
+};
+
+/* manifold.c:1219-1259: where a normal falls on the Gauss map of the segment's vertices */
+static __device__ int d_classifyNormal( const d_chainParams& params, b2Vec2 normal )
+{
+	const float sinTol = 0.01f;
+	if ( d_dot( normal, params.edge1 ) <= 0.0f )
+	{
+		if ( params.convex1 ) return d_cross( normal, params.normal0 ) > sinTol ? D_NORMAL_SKIP : D_NORMAL_ADMIT;
+		return D_NORMAL_SNAP;
+	}
+	if ( params.convex2 ) return d_cross( params.normal2, normal ) > sinTol ? D_NORMAL_SKIP : D_NORMAL_ADMIT;
+	return D_NORMAL_SNAP;
+}
+
+/* manifold.c:1261-1641 */
+static __device__ b2LocalManifold d_collideChainSegmentAndPolygon( const b2gShape* seg, const b2Polygon* polygonB, b2Transform xf,
+																   d_simplexCache* cache )
+{
+	b2LocalManifold manifold = d_emptyManifold();
+	b2Vec2 centroidB = d_transformPoint( xf, polygonB->centroid );
+	float radiusB = polygonB->radius;
+	b2Vec2 p1 = seg->v[0], p2 = seg->v[1];
+	b2Vec2 edge1 = d_normalize( d_sub( p2, p1 ) );
+	d_chainParams sp;
+	sp.edge1 = edge1;
+	const float convexTol = 0.01f;
+	b2Vec2 edge0 = d_normalize( d_sub( p1, seg->v[2] ) );
+	sp.normal0 = d_rightPerp( edge0 );
+	sp.convex1 = d_cross( edge0, edge1 ) >= convexTol;
+	b2Vec2 edge2 = d_normalize( d_sub( seg->v[3], p2 ) );
+	sp.normal2 = d_rightPerp( edge2 );
+	sp.convex2 = d_cross( edge1, edge2 ) >= convexTol;
+	b2Vec2 normal1 = d_rightPerp( edge1 );
+	bool behind1 = d_dot( normal1, d_sub( centroidB, p1 ) ) < 0.0f;
+	bool behind0 = true, behind2 = true;
+	if ( sp.convex1 ) behind0 = d_dot( sp.normal0, d_sub( centroidB, p1 ) ) < 0.0f;
+	if ( sp.convex2 ) behind2 = d_dot( sp.normal2, d_sub( centroidB, p2 ) ) < 0.0f;
+	if ( behind1 && behind0 && behind2 ) return manifold;
+
+	int count = polygonB->count;
+	b2Vec2 vertices[B2_MAX_POLYGON_VERTICES];
+	b2Vec2 normals[B2_MAX_POLYGON_VERTICES];
+	for ( int i = 0; i < count; ++i )
+	{
+		vertices[i] = d_transformPoint( xf, polygonB->vertices[i] );
+		normals[i] = d_rotate( xf.q, polygonB->normals[i] );
+	}
+	d_proxy proxyA, proxyB;
+	proxyA.points[0] = p1;
+	proxyA.points[1] = p2;
+	proxyA.count = 2;
+	proxyA.radius = 0.0f;
+	for ( int i = 0; i < count; ++i ) proxyB.points[i] = vertices[i];
+	proxyB.count = count;
+	proxyB.radius = 0.0f;
+	b2Transform identity = { { 0.0f, 0.0f }, { 1.0f, 0.0f } };
+	b2Vec2 outA, outB;
+	float outDistance = d_shapeDistanceWitness( &proxyA, &proxyB, identity, cache, &outA, &outB );
+	if ( outDistance > radiusB + D_SPECULATIVE_DISTANCE ) return manifold;
+
+	b2Vec2 n0 = sp.convex1 ? sp.normal0 : normal1;
+	b2Vec2 n2 = sp.convex2 ? sp.normal2 : normal1;
+	int incidentIndex = -1;
+	int incidentNormal = -1;
+	if ( behind1 == false && outDistance > 0.1f * D_LINEAR_SLOP )
+	{
+		if ( cache->count == 1 )
+		{
+			/* vertex-vertex */
+			b2Vec2 pA = outA, pB = outB;
+			b2Vec2 normal = d_normalize( d_sub( pB, pA ) );
+			int type = d_classifyNormal( sp, normal );
+			if ( type == D_NORMAL_SKIP ) return manifold;
+			if ( type == D_NORMAL_ADMIT )
+			{
+				manifold.normal = normal;
+				manifold.points[0].point = pA;
+				manifold.points[0].separation = outDistance - radiusB;
+				manifold.points[0].id = D_MAKE_ID( cache->indexA[0], cache->indexB[0] );
+				manifold.pointCount = 1;
+				return manifold;
+			}
+			incidentIndex = cache->indexB[0];
+		}
+		else
+		{
+			/* vertex-edge */
+			int ia1 = cache->indexA[0], ia2 = cache->indexA[1];
+			int ib1 = cache->indexB[0], ib2 = cache->indexB[1];
+			if ( ia1 == ia2 )
+			{
+				b2Vec2 normalB = d_sub( outA, outB );
+				float dot1 = d_dot( normalB, normals[ib1] );
+				float dot2 = d_dot( normalB, normals[ib2] );
+				int ib = dot1 > dot2 ? ib1 : ib2;
+				normalB = normals[ib];
+				int type = d_classifyNormal( sp, d_neg( normalB ) );
+				if ( type == D_NORMAL_SKIP ) return manifold;
+				if ( type == D_NORMAL_ADMIT )
+				{
+					ib1 = ib;
+					ib2 = ib < count - 1 ? ib + 1 : 0;
+					b2Vec2 b1 = vertices[ib1], b2 = vertices[ib2];
+					dot1 = d_dot( normalB, d_sub( p1, b1 ) );
+					dot2 = d_dot( normalB, d_sub( p2, b1 ) );
+					if ( dot1 < dot2 )
+					{
+						if ( d_dot( n0, normalB ) < d_dot( normal1, normalB ) ) return manifold;
+					}
+					else
+					{
+						if ( d_dot( n2, normalB ) < d_dot( normal1, normalB ) ) return manifold;
+					}
+					manifold = d_clipSegments( b1, b2, p1, p2, normalB, radiusB, 0.0f, D_MAKE_ID( ib1, 1 ), D_MAKE_ID( ib2, 0 ) );
+					if ( manifold.pointCount == 2 ) manifold.normal = d_neg( normalB );
+					return manifold;
+				}
+				incidentNormal = ib;
+			}
+			else
+			{
+				float dot1 = d_dot( normal1, d_sub( vertices[ib1], p1 ) );
+				float dot2 = d_dot( normal1, d_sub( vertices[ib2], p2 ) );
+				incidentIndex = dot1 < dot2 ? ib1 : ib2;
+			}
+		}
+	}
+	else
+	{
+		/* separating axes: the segment normal, the convex neighbors' normals, the polygon's */
+		float edgeSeparation = FLT_MAX;
+		for ( int i = 0; i < count; ++i )
+		{
+			float s = d_dot( normal1, d_sub( vertices[i], p1 ) );
+			if ( s < edgeSeparation )
+			{
+				edgeSeparation = s;
+				incidentIndex = i;
+			}
+		}
+		if ( sp.convex1 )
+		{
+			float s0 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float s = d_dot( sp.normal0, d_sub( vertices[i], p1 ) );
+				if ( s < s0 ) s0 = s;
+			}
+			if ( s0 > edgeSeparation )
+			{
+				edgeSeparation = s0;
+				incidentIndex = -1;
+			}
+		}
+		if ( sp.convex2 )
+		{
+			float s2 = FLT_MAX;
+			for ( int i = 0; i < count; ++i )
+			{
+				float s = d_dot( sp.normal2, d_sub( vertices[i], p2 ) );
+				if ( s < s2 ) s2 = s;
+			}
+			if ( s2 > edgeSeparation )
+			{
+				edgeSeparation = s2;
+				incidentIndex = -1;
+			}
+		}
+		float polygonSeparation = -FLT_MAX;
+		int referenceIndex = -1;
+		for ( int i = 0; i < count; ++i )
+		{
+			b2Vec2 n = normals[i];
+			if ( d_classifyNormal( sp, d_neg( n ) ) != D_NORMAL_ADMIT ) continue;
+			b2Vec2 pv = vertices[i];
+			float s = d_min( d_dot( n, d_sub( p2, pv ) ), d_dot( n, d_sub( p1, pv ) ) );
+			if ( s > polygonSeparation )
+			{
+				polygonSeparation = s;
+				referenceIndex = i;
+			}
+		}
+		if ( polygonSeparation > edgeSeparation )
+		{
+			int ia1 = referenceIndex;
+			int ia2 = ia1 < count - 1 ? ia1 + 1 : 0;
+			b2Vec2 a1 = vertices[ia1], a2 = vertices[ia2];
+			b2Vec2 n = normals[ia1];
+			float dot1 = d_dot( n, d_sub( p1, a1 ) );
+			float dot2 = d_dot( n, d_sub( p2, a1 ) );
+			if ( dot1 < dot2 )
+			{
+				if ( d_dot( n0, n ) < d_dot( normal1, n ) ) return manifold;
+			}
+			else
+			{
+				if ( d_dot( n2, n ) < d_dot( normal1, n ) ) return manifold;
+			}
+			manifold = d_clipSegments( a1, a2, p1, p2, normals[ia1], radiusB, 0.0f, D_MAKE_ID( ia1, 1 ), D_MAKE_ID( ia2, 0 ) );
+			if ( manifold.pointCount == 2 ) manifold.normal = d_neg( normals[ia1] );
+			return manifold;
+		}
+		if ( incidentIndex == -1 ) return manifold;
+	}
+
+	/* the segment normal: clip the polygon edge most anti-parallel to it */
+	b2Vec2 b1, b2;
+	int ib1, ib2;
+	if ( incidentNormal != -1 )
+	{
+		ib1 = incidentNormal;
+		ib2 = ib1 < count - 1 ? ib1 + 1 : 0;
+		b1 = vertices[ib1];
+		b2 = vertices[ib2];
+	}
+	else
+	{
+		int i2 = incidentIndex;
+		int i1 = i2 > 0 ? i2 - 1 : count - 1;
+		float d1 = d_dot( normal1, normals[i1] );
+		float d2 = d_dot( normal1, normals[i2] );
+		if ( d1 < d2 )
+		{
+			ib1 = i1;
+			ib2 = i2;
+		}
+		else
+		{
+			ib1 = i2;
+			ib2 = i2 < count - 1 ? i2 + 1 : 0;
+		}
+		b1 = vertices[ib1];
+		b2 = vertices[ib2];
+	}
+	return d_clipSegments( p1, p2, b1, b2, normal1, 0.0f, radiusB, D_MAKE_ID( 0, ib2 ), D_MAKE_ID( 1, ib1 ) );
+}
+
 /* dispatch in the primary order of the contact register table (contact.c:188-206):
-   circle 0, capsule 1, segment 2, polygon 3 */
-static __device__ b2LocalManifold d_collideShapes( const b2gShape* a, const b2gShape* b, b2Transform xf )
+   circle 0, capsule 1, segment 2, polygon 3, chain segment 4 (always shape A). `cache` is
+   the contact's GJK simplex cache, read and updated by the chain-segment manifolds. */
+static __device__ b2LocalManifold d_collideShapes( const b2gShape* a, const b2gShape* b, b2Transform xf, d_simplexCache* cache )
 {
 	int ta = a->type, tb = b->type;
+	if ( ta == b2_chainSegmentShape )
+	{
+		if ( tb == b2_circleShape )
+		{
+			b2Circle cb = { b->v[0], b->radius };
+			return d_collideChainSegmentAndCircle( a, &cb, xf );
+		}
+		if ( tb == b2_capsuleShape )
+		{
+			b2Polygon pb = d_makeCapsule( b->v[0], b->v[1], b->radius );
+			return d_collideChainSegmentAndPolygon( a, &pb, xf, cache );
+		}
+		if ( tb == b2_polygonShape )
+		{
+			b2Polygon pb = d_shapePolygon( b );
+			return d_collideChainSegmentAndPolygon( a, &pb, xf, cache );
+		}
+		return d_emptyManifold();
+	}
 	if ( ta == b2_circleShape && tb == b2_circleShape )
 	{
 		b2Circle ca = { a->v[0], a->radius }, cb = { b->v[0], b->radius };

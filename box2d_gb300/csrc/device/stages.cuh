@@ -351,6 +351,7 @@ static __device__ float4 d_computeFatShapeAABB( const b2gShape* s, b2Transform x
 		}
 		case b2_capsuleShape:
 		case b2_segmentShape:
+		case b2_chainSegmentShape:
 		{
 			b2Vec2 v1 = d_transformWorldPoint( xf, s->v[0] );
 			b2Vec2 v2 = d_transformWorldPoint( xf, s->v[1] );
@@ -431,6 +432,9 @@ static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, 
 	float2 lc2 = a.localCenter[bodyId];
 	b2Vec2 localCenter = { lc2.x, lc2.y };
 	d_sweep sweep = d_relativeSweep( base, b2Rot{ c0.z, c0.w }, center, q, localCenter, base );
+	b2Transform xf1;
+	xf1.q = sweep.q1;
+	xf1.p = d_sub( sweep.c1, d_rotate( sweep.q1, sweep.localCenter ) );
 	b2Transform xf2;
 	xf2.q = sweep.q2;
 	xf2.p = d_sub( sweep.c2, d_rotate( sweep.q2, sweep.localCenter ) );
@@ -447,7 +451,11 @@ static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, 
 		if ( fastShape->isSensor ) continue;
 		float4 swept = make_float4( d_min( box1.x, box2.x ), d_min( box1.y, box2.y ), d_max( box1.z, box2.z ),
 									d_max( box1.w, box2.w ) );
-		fraction = d_continuousQuery( a.ccd, swept, shapeId, fastShape, sweep, base, fraction, &hit, &overflow );
+		d_fastShape fast;
+		fast.centroid1 = d_transformPoint( xf1, fastShape->ccdCentroid );
+		fast.centroid2 = d_transformPoint( xf2, fastShape->ccdCentroid );
+		fast.coreDistance = D_CORE_FRACTION * a.minExtent[bodyId];
+		fraction = d_continuousQuery( a.ccd, swept, shapeId, fastShape, sweep, base, fraction, &hit, &overflow, fast );
 	}
 	atomicAdd( &a.counters->continuousSweeps, 1 );
 	if ( overflow ) atomicOr( &a.counters->status, B2G_STATUS_CAPACITY );

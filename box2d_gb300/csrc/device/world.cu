@@ -808,7 +808,20 @@ static __device__ void b_collide( const d_collideArgs& a, int block, int grid )
 	/* b2UpdateContact */
 	b2Manifold oldManifold = cs->manifold;
 	b2Transform rel = d_invMulTransforms( xfA, xfB );
-	b2LocalManifold local = d_collideShapes( shapeA, shapeB, rel );
+	d_simplexCache cache;
+	cache.count = cs->cacheCount;
+	for ( int k = 0; k < 3; ++k )
+	{
+		cache.indexA[k] = cs->cacheA[k];
+		cache.indexB[k] = cs->cacheB[k];
+	}
+	b2LocalManifold local = d_collideShapes( shapeA, shapeB, rel, &cache );
+	cs->cacheCount = (uint8_t)cache.count;
+	for ( int k = 0; k < 3; ++k )
+	{
+		cs->cacheA[k] = (uint8_t)cache.indexA[k];
+		cs->cacheB[k] = (uint8_t)cache.indexB[k];
+	}
 	b2Manifold m;
 	memset( &m, 0, sizeof( m ) );
 	m.normal = d_rotate( xfA.q, local.normal );

@@ -32,6 +32,7 @@ typedef struct h_body
 	int headContactKey, contactCount;
 	int headShapeId, shapeCount;
 	int headJointKey, jointCount;
+	int headChainId;
 	int islandId, islandIndex; /* island of a non-static body and its index in the island */
 	int bodyMoveIndex;		   /* its move event in the last step while the sleep pass runs */
 	float mass, inertia;
@@ -69,11 +70,21 @@ typedef struct h_shape
 		b2Circle circle;
 		b2Polygon polygon;
 		b2Segment segment;
+		b2ChainSegment chainSegment;
 	};
 	uint16_t generation;
 	int enableContactEvents, enableHitEvents, isSensor;
 	int enableSensorEvents, sensorIndex; /* sensorIndex: its slot in the world's sensors, or -1 */
 } h_shape;
+
+/* a chain of segment shapes on one body (shape.h b2ChainShape) */
+typedef struct h_chain
+{
+	int id, bodyId, nextChainId;
+	int count; /* segment shapes */
+	int* shapeIndices;
+	uint16_t generation;
+} h_chain;
 
 /* a shape seen by a sensor (sensor.h b2Visitor) */
 typedef struct h_visitor
@@ -193,6 +204,7 @@ typedef struct h_world
 	float hitEventThreshold, restitutionThreshold, maxLinearSpeed, contactSpeed, contactHertz, contactDampingRatio;
 	int enableSleep, enableWarmStarting, enableContactSoftening, enableContinuous, locked;
 	/* sensors, in creation order (swap-removed) */
+	H_ARRAY( h_chain ) chains; /* by chain id */
 	H_ARRAY( h_sensor ) sensors;
 	int sensorStep; /* stepIndex of the last sensor overlap pass */
 	H_ARRAY( b2SensorBeginTouchEvent ) sensorBeginEvents;

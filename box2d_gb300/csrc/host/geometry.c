@@ -457,9 +457,11 @@ b2AABB h_computeFatShapeAABB( const h_shape* shape, b2Transform xf, float extra 
 			return h_fatBox( lx, ly, ux, uy, r );
 		}
 		case b2_segmentShape:
+		case b2_chainSegmentShape:
 		{
-			b2Vec2 v1 = h_transformWorldPoint( xf, shape->segment.point1 );
-			b2Vec2 v2 = h_transformWorldPoint( xf, shape->segment.point2 );
+			const b2Segment* seg = shape->type == b2_segmentShape ? &shape->segment : &shape->chainSegment.segment;
+			b2Vec2 v1 = h_transformWorldPoint( xf, seg->point1 );
+			b2Vec2 v2 = h_transformWorldPoint( xf, seg->point2 );
 			double e = (double)extra;
 			return h_fatBox( v1.x < v2.x ? v1.x : v2.x, v1.y < v2.y ? v1.y : v2.y, v1.x > v2.x ? v1.x : v2.x,
 							 v1.y > v2.y ? v1.y : v2.y, e );
@@ -481,6 +483,7 @@ b2Vec2 h_getShapeCentroid( const h_shape* s )
 		case b2_circleShape: return s->circle.center;
 		case b2_polygonShape: return s->polygon.centroid;
 		case b2_segmentShape: return h_lerp( s->segment.point1, s->segment.point2, 0.5f );
+		case b2_chainSegmentShape: return h_lerp( s->chainSegment.segment.point1, s->chainSegment.segment.point2, 0.5f );
 		default: return h_v( 0.0f, 0.0f );
 	}
 }
@@ -507,6 +510,9 @@ float h_computeShapeMargin( const h_shape* s )
 		break;
 		case b2_segmentShape:
 			margin = 0.5f * h_distance( s->segment.point1, s->segment.point2 );
+			break;
+		case b2_chainSegmentShape:
+			margin = 0.5f * h_distance( s->chainSegment.segment.point1, s->chainSegment.segment.point2 );
 			break;
 		default:
 			return H_AABB_MARGIN;
@@ -570,6 +576,12 @@ void h_computeShapeExtent( const h_shape* s, b2Vec2 lc, float* minExtent, float*
 		case b2_segmentShape:
 		{
 			b2Vec2 c1 = h_sub( s->segment.point1, lc ), c2 = h_sub( s->segment.point2, lc );
+			*maxExtent = sqrtf( h_max( h_lengthSq( c1 ), h_lengthSq( c2 ) ) );
+		}
+		break;
+		case b2_chainSegmentShape:
+		{
+			b2Vec2 c1 = h_sub( s->chainSegment.segment.point1, lc ), c2 = h_sub( s->chainSegment.segment.point2, lc );
 			*maxExtent = sqrtf( h_max( h_lengthSq( c1 ), h_lengthSq( c2 ) ) );
 		}
 		break;

@@ -257,6 +257,8 @@ void b2DestroyWorld( b2WorldId worldId )
 	h_pairSetFree( &w->pairSet );
 	h_free( w->moveEvents );
 	h_freeSensors( w );
+	for ( int i = 0; i < w->chains.count; ++i ) free( w->chains.data[i].shapeIndices );
+	h_free( w->chains );
 	h_free( w->beginEvents );
 	h_free( w->endEvents[0] );
 	h_free( w->endEvents[1] );
@@ -727,6 +729,14 @@ void h_ensureDevice( h_world* w )
 				d->v[1] = s->segment.point2;
 				d->count = 2;
 				break;
+			case b2_chainSegmentShape:
+				/* the segment in v[0], v[1]; its ghost vertices in v[2] (before) and v[3] (after) */
+				d->v[0] = s->chainSegment.segment.point1;
+				d->v[1] = s->chainSegment.segment.point2;
+				d->v[2] = s->chainSegment.ghost1;
+				d->v[3] = s->chainSegment.ghost2;
+				d->count = 2;
+				break;
 			case b2_polygonShape:
 				memcpy( d->v, s->polygon.vertices, sizeof( d->v ) );
 				memcpy( d->n, s->polygon.normals, sizeof( d->n ) );
@@ -868,6 +878,7 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	b->headShapeId = B2_NULL_INDEX;
 	b->headContactKey = B2_NULL_INDEX;
 	b->headJointKey = B2_NULL_INDEX;
+	b->headChainId = B2_NULL_INDEX;
 	b->id = bodyId;
 	b->sleepThreshold = def->sleepThreshold;
 	b->safetyFactor = def->safetyFactor;
@@ -1275,7 +1286,10 @@ void h_bufferMove( h_world* w, int proxyKey )
 }
 
 /* ---------------- shapes (shape.c:85-270, :1034-1044) ---------------- */
-static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const void* geometry, b2ShapeType type )
+/* shape.c:115-205 b2CreateShapeInternal, plus the mass update or dirty-mass mark of
+   b2CreateShape (shape.c:207-240) unless `internal` (a chain's segments) */
+static b2ShapeId h_createShapeImpl( b2BodyId bodyId, const b2ShapeDef* def, const void* geometry, b2ShapeType type,
+									int internal )
 {
 	h_world* w = h_worlds + bodyId.world0;
 	h_markHostChanged( w );
@@ -1297,6 +1311,7 @@ static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const vo
 		case b2_circleShape: s->circle = *(const b2Circle*)geometry; break;
 		case b2_polygonShape: s->polygon = *(const b2Polygon*)geometry; break;
 		case b2_segmentShape: s->segment = *(const b2Segment*)geometry; break;
+		case b2_chainSegmentShape: s->chainSegment = *(const b2ChainSegment*)geometry; break;
 		default: break;
 	}
 	s->id = shapeId;
@@ -1334,10 +1349,18 @@ static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const vo
 	body->headShapeId = shapeId;
 	body->shapeCount += 1;
 	if ( def->isSensor ) h_createSensor( w, s );
-	if ( def->updateBodyMass ) h_updateBodyMassData( w, body );
-	else body->flags |= B2G_DIRTY_MASS;
+	if ( internal == 0 )
+	{
+		if ( def->updateBodyMass ) h_updateBodyMassData( w, body );
+		else body->flags |= B2G_DIRTY_MASS;
+	}
 	b2ShapeId id = { s->id + 1, bodyId.world0, s->generation };
 	return id;
+}
+
+static b2ShapeId h_createShape( b2BodyId bodyId, const b2ShapeDef* def, const void* geometry, b2ShapeType type )
+{
+	return h_createShapeImpl( bodyId, def, geometry, type, 0 );
 }
 
 b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Circle* circle )
@@ -1370,6 +1393,146 @@ b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2
 	return h_createShape( bodyId, def, segment, b2_segmentShape );
 }
 
+/* ---- chains (shape.c:300-315, 439-640) ---- */
+
+b2ChainDef b2DefaultChainDef( void )
+{
+	static const b2SurfaceMaterial defaultMaterial = { 0.6f, 0.0f, 0.0f, 0.0f, 0, 0 };
+	b2ChainDef def;
+	memset( &def, 0, sizeof( def ) );
+	def.materials = &defaultMaterial;
+	def.materialCount = 1;
+	def.filter = b2DefaultFilter();
+	def.internalValue = 1152023;
+	return def;
+}
+
+b2ShapeId b2CreateChainSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2ChainSegment* chainSegment )
+{
+	if ( h_distanceSq( chainSegment->segment.point1, chainSegment->segment.point2 ) <= H_LINEAR_SLOP * H_LINEAR_SLOP )
+	{
+		b2ShapeId nullId = { 0, 0, 0 };
+		return nullId;
+	}
+	b2ChainSegment local = *chainSegment;
+	local.chainId = B2_NULL_INDEX;
+	return h_createShape( bodyId, def, &local, b2_chainSegmentShape );
+}
+
+/* one segment of a chain: the chain's filter and sensor flag, the segment's material, no
+   contact or hit events, the body's mass left as it is */
+static int h_chainSegmentShape( b2BodyId bodyId, const b2ChainDef* def, int materialIndex, b2Vec2 g1, b2Vec2 p1, b2Vec2 p2,
+								b2Vec2 g2, int chainId )
+{
+	b2ShapeDef shapeDef = b2DefaultShapeDef();
+	shapeDef.userData = def->userData;
+	shapeDef.filter = def->filter;
+	shapeDef.enableSensorEvents = def->enableSensorEvents;
+	shapeDef.enableContactEvents = false;
+	shapeDef.enableHitEvents = false;
+	shapeDef.updateBodyMass = false;
+	shapeDef.material = def->materials[materialIndex];
+	b2ChainSegment seg = { g1, { p1, p2 }, g2, chainId };
+	b2ShapeId id = h_createShapeImpl( bodyId, &shapeDef, &seg, b2_chainSegmentShape, 1 );
+	return id.index1 - 1;
+}
+
+b2ChainId b2CreateChain( b2BodyId bodyId, const b2ChainDef* def )
+{
+	b2ChainId nullId = { 0, 0, 0 };
+	h_world* w = h_worlds + bodyId.world0;
+	if ( w->locked || def->count < 4 ) return nullId;
+	h_markHostChanged( w );
+	h_body* body = h_getBody( bodyId );
+	int chainId = h_allocId( &w->chainIdPool );
+	if ( chainId == w->chains.count )
+	{
+		h_chain z;
+		memset( &z, 0, sizeof( z ) );
+		h_push( w->chains, z );
+	}
+	h_chain* chain = w->chains.data + chainId;
+	chain->id = chainId;
+	chain->bodyId = body->id;
+	chain->nextChainId = body->headChainId;
+	chain->generation += 1;
+	body->headChainId = chainId;
+	const b2Vec2* pts = def->points;
+	int n = def->count;
+	int one = def->materialCount == 1;
+	if ( def->isLoop )
+	{
+		chain->count = n;
+		chain->shapeIndices = malloc( (size_t)n * sizeof( int ) );
+		int prev = n - 1;
+		for ( int i = 0; i < n - 2; ++i )
+		{
+			chain->shapeIndices[i] =
+				h_chainSegmentShape( bodyId, def, one ? 0 : i, pts[prev], pts[i], pts[i + 1], pts[i + 2], chainId );
+			prev = i;
+		}
+		chain->shapeIndices[n - 2] =
+			h_chainSegmentShape( bodyId, def, one ? 0 : n - 2, pts[n - 3], pts[n - 2], pts[n - 1], pts[0], chainId );
+		chain->shapeIndices[n - 1] =
+			h_chainSegmentShape( bodyId, def, one ? 0 : n - 1, pts[n - 2], pts[n - 1], pts[0], pts[1], chainId );
+	}
+	else
+	{
+		/* the first and last points only shape the ends (ghost vertices); the material of a
+		   segment is that of its leading point */
+		chain->count = n - 3;
+		chain->shapeIndices = malloc( (size_t)( n - 3 ) * sizeof( int ) );
+		for ( int i = 0; i < n - 3; ++i )
+			chain->shapeIndices[i] =
+				h_chainSegmentShape( bodyId, def, one ? 0 : i + 1, pts[i], pts[i + 1], pts[i + 2], pts[i + 3], chainId );
+	}
+	b2ChainId id = { chainId + 1, w->worldId, chain->generation };
+	return id;
+}
+
+bool b2Chain_IsValid( b2ChainId id )
+{
+	if ( id.world0 >= H_MAX_WORLDS ) return false;
+	h_world* w = h_worlds + id.world0;
+	if ( w->inUse == 0 || id.index1 < 1 || id.index1 > w->chains.count ) return false;
+	const h_chain* chain = w->chains.data + ( id.index1 - 1 );
+	return chain->id == id.index1 - 1 && chain->generation == id.generation;
+}
+
+int b2Chain_GetSegmentCount( b2ChainId chainId ) { return h_worlds[chainId.world0].chains.data[chainId.index1 - 1].count; }
+
+int b2Chain_GetSegments( b2ChainId chainId, b2ShapeId* segmentArray, int capacity )
+{
+	h_world* w = h_worlds + chainId.world0;
+	const h_chain* chain = w->chains.data + ( chainId.index1 - 1 );
+	int count = chain->count < capacity ? chain->count : capacity;
+	for ( int i = 0; i < count; ++i )
+	{
+		const h_shape* s = w->shapes.data + chain->shapeIndices[i];
+		b2ShapeId id = { s->id + 1, chainId.world0, s->generation };
+		segmentArray[i] = id;
+	}
+	return count;
+}
+
+b2ShapeType b2Shape_GetType( b2ShapeId shapeId ) { return h_worlds[shapeId.world0].shapes.data[shapeId.index1 - 1].type; }
+
+b2ChainSegment b2Shape_GetChainSegment( b2ShapeId shapeId )
+{
+	return h_worlds[shapeId.world0].shapes.data[shapeId.index1 - 1].chainSegment;
+}
+
+b2ChainId b2Shape_GetParentChain( b2ShapeId shapeId )
+{
+	h_world* w = h_worlds + shapeId.world0;
+	const h_shape* s = w->shapes.data + ( shapeId.index1 - 1 );
+	b2ChainId nullId = { 0, 0, 0 };
+	if ( s->type != b2_chainSegmentShape || s->chainSegment.chainId == B2_NULL_INDEX ) return nullId;
+	int chainId = s->chainSegment.chainId;
+	b2ChainId id = { chainId + 1, shapeId.world0, w->chains.data[chainId].generation };
+	return id;
+}
+
 void b2Shape_SetFriction( b2ShapeId shapeId, float friction )
 {
 	h_world* w = h_worlds + shapeId.world0;
@@ -1383,22 +1546,26 @@ float b2Shape_GetFriction( b2ShapeId shapeId )
 }
 
 /* ---------------- contact register table (contact.c:188-206) ---------------- */
-/* shape types: circle 0, capsule 1, segment 2, polygon 3 */
+/* shape types: circle 0, capsule 1, segment 2, polygon 3, chain segment 4. Segments and
+   chain segments collide with circles, capsules and polygons only, as shape A. */
 int h_canCollide( b2ShapeType a, b2ShapeType b )
 {
-	if ( (int)a > 3 || (int)b > 3 ) return 0;
-	return !( a == b2_segmentShape && b == b2_segmentShape );
+	if ( (int)a > 4 || (int)b > 4 ) return 0;
+	int lineA = a == b2_segmentShape || a == b2_chainSegmentShape;
+	int lineB = b == b2_segmentShape || b == b2_chainSegmentShape;
+	return !( lineA && lineB );
 }
 
 int h_isPrimary( b2ShapeType a, b2ShapeType b )
 {
-	static const int prim[4][4] = {
-		{ 1, 0, 0, 0 },
-		{ 1, 1, 0, 0 },
-		{ 1, 1, 0, 1 },
-		{ 1, 1, 0, 1 },
+	static const int prim[5][5] = {
+		{ 1, 0, 0, 0, 0 },
+		{ 1, 1, 0, 0, 0 },
+		{ 1, 1, 0, 1, 0 },
+		{ 1, 1, 0, 1, 0 },
+		{ 1, 1, 0, 1, 0 },
 	};
-	if ( (int)a > 3 || (int)b > 3 ) return 0;
+	if ( (int)a > 4 || (int)b > 4 ) return 0;
 	return prim[a][b];
 }
 

@@ -1023,6 +1023,112 @@ static void b2sSensorZoo( b2sScene* s, int count, b2sRng* rng )
 	}
 }
 
+#ifndef B2S_NO_CHAINS
+/* Chain scene (shape.c:439-640, manifold.c:1042-1641): a closed chain forming a container
+   with a wavy floor (clockwise, so every segment's one-sided normal points inward), an open
+   chain ramp inside it, a loose chain segment shape, and `count` circles, capsules, boxes and
+   rounded convex polygons dropped from up to 18 m. Per-segment materials on the floor. */
+static void b2sChainZoo( b2sScene* s, int count, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	{
+		enum { floorCount = 31 };
+		b2Vec2 pts[floorCount + 3];
+		b2SurfaceMaterial mats[floorCount + 3];
+		int n = 0;
+		for ( int i = 0; i < floorCount; ++i )
+		{
+			float x = 15.0f - 1.0f * (float)i;
+			b2CosSin cs = b2ComputeCosSin( 0.6f * x );
+			pts[n].x = x;
+			pts[n].y = 0.8f * cs.sine + 1.0f;
+			n += 1;
+		}
+		pts[n].x = -15.0f;
+		pts[n].y = 22.0f;
+		n += 1;
+		pts[n].x = 15.0f;
+		pts[n].y = 22.0f;
+		n += 1;
+		for ( int i = 0; i < n; ++i )
+		{
+			memset( mats + i, 0, sizeof( b2SurfaceMaterial ) );
+			mats[i].friction = ( i % 3 ) == 0 ? 0.2f : 0.7f;
+			mats[i].restitution = ( i % 4 ) == 0 ? 0.3f : 0.0f;
+		}
+		b2ChainDef cd = b2DefaultChainDef();
+		cd.points = pts;
+		cd.count = n;
+		cd.materials = mats;
+		cd.materialCount = n;
+		cd.isLoop = true;
+		b2CreateChain( ground, &cd );
+	}
+	{
+		b2Vec2 ramp[6] = { { 9.0f, 9.0f }, { 7.0f, 8.0f }, { 4.0f, 7.0f }, { 1.0f, 6.5f }, { -2.0f, 6.8f }, { -4.0f, 7.8f } };
+		b2ChainDef cd = b2DefaultChainDef();
+		cd.points = ramp;
+		cd.count = 6;
+		b2CreateChain( ground, &cd );
+	}
+	{
+		b2ShapeDef sd = b2DefaultShapeDef();
+		b2ChainSegment seg = { { -6.0f, 12.0f }, { { -8.0f, 12.0f }, { -12.0f, 11.0f } }, { -14.0f, 11.0f }, -1 };
+		b2CreateChainSegmentShape( ground, &sd, &seg );
+	}
+	for ( int k = 0; k < count; ++k )
+	{
+		float x = b2sRandomFloatRange( rng, -13.0f, 13.0f );
+		float y = b2sRandomFloatRange( rng, 4.0f, 18.0f );
+		b2BodyDef bd = b2DefaultBodyDef();
+		bd.type = b2_dynamicBody;
+		bd.position.x = x;
+		bd.position.y = y;
+		bd.rotation = b2MakeRot( b2sRandomFloatRange( rng, -3.0f, 3.0f ) );
+		b2BodyId body = b2CreateBody( s->worldId, &bd );
+		b2sAddBody( s, body, 1 );
+		b2ShapeDef sd = b2DefaultShapeDef();
+		sd.material.friction = b2sRandomFloatRange( rng, 0.2f, 0.9f );
+		int kind = b2sRandomIntRange( rng, 0, 3 );
+		if ( kind == 0 )
+		{
+			b2Circle c = { { 0.0f, 0.0f }, b2sRandomFloatRange( rng, 0.2f, 0.5f ) };
+			b2CreateCircleShape( body, &sd, &c );
+		}
+		else if ( kind == 1 )
+		{
+			float half = b2sRandomFloatRange( rng, 0.2f, 0.6f );
+			b2Capsule c = { { -half, 0.0f }, { half, 0.0f }, b2sRandomFloatRange( rng, 0.1f, 0.3f ) };
+			b2CreateCapsuleShape( body, &sd, &c );
+		}
+		else if ( kind == 2 )
+		{
+			float hx = b2sRandomFloatRange( rng, 0.2f, 0.6f );
+			float hy = b2sRandomFloatRange( rng, 0.2f, 0.6f );
+			b2Polygon p = b2MakeBox( hx, hy );
+			b2CreatePolygonShape( body, &sd, &p );
+		}
+		else
+		{
+			int nv = b2sRandomIntRange( rng, 3, 7 );
+			b2Vec2 pts[8];
+			float radius = b2sRandomFloatRange( rng, 0.3f, 0.6f );
+			for ( int i = 0; i < nv; ++i )
+			{
+				float a = 6.2831853f * (float)i / (float)nv;
+				b2CosSin cs = b2ComputeCosSin( a );
+				pts[i].x = radius * cs.cosine;
+				pts[i].y = radius * cs.sine;
+			}
+			b2Hull hull = b2ComputeHull( pts, nv );
+			b2Polygon p = b2MakePolygon( &hull, b2sRandomFloatRange( rng, 0.0f, 0.05f ) );
+			b2CreatePolygonShape( body, &sd, &p );
+		}
+	}
+}
+#endif
+
 enum
 {
 	B2S_LARGE_PYRAMID = 0,
@@ -1040,6 +1146,7 @@ enum
 	B2S_JOINT_MIX = 12,
 	B2S_OVERFLOW = 13,
 	B2S_SENSOR_ZOO = 14,
+	B2S_CHAIN_ZOO = 15,
 };
 
 /* Worker threads requested in the world definition of scenes created from now on (0 keeps
@@ -1095,6 +1202,9 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 		case B2S_JOINT_MIX: b2sJointMix( s, a, &rng ); break;
 		case B2S_OVERFLOW: b2sOverflowScene( s, a, &rng ); break;
 		case B2S_SENSOR_ZOO: b2sSensorZoo( s, a, &rng ); break;
+#ifndef B2S_NO_CHAINS
+		case B2S_CHAIN_ZOO: b2sChainZoo( s, a, &rng ); break;
+#endif
 		default: break;
 	}
 	return h;

@@ -161,6 +161,15 @@ typedef struct b2Segment
 	b2Vec2 point2;
 } b2Segment;
 
+/* collision.h:184-197: a one-sided segment of a chain with its neighbors' far points */
+typedef struct b2ChainSegment
+{
+	b2Vec2 ghost1;
+	b2Segment segment;
+	b2Vec2 ghost2;
+	int chainId;
+} b2ChainSegment;
+
 typedef struct b2Hull
 {
 	b2Vec2 points[B2_MAX_POLYGON_VERTICES];
@@ -325,6 +334,20 @@ typedef struct b2ShapeDef
 	bool updateBodyMass;
 	int internalValue;
 } b2ShapeDef;
+
+/* types.h:488-518 */
+typedef struct b2ChainDef
+{
+	void* userData;
+	const b2Vec2* points;
+	int count;
+	const b2SurfaceMaterial* materials;
+	int materialCount;
+	b2Filter filter;
+	bool isLoop;
+	bool enableSensorEvents;
+	int internalValue;
+} b2ChainDef;
 
 typedef struct b2Profile
 {
@@ -687,6 +710,16 @@ B2G_API float b2Body_GetSleepThreshold( b2BodyId bodyId );
 /* ---- API: shapes (box2d.h:659-724) ---- */
 B2G_API b2ShapeId b2CreateCircleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Circle* circle );
 B2G_API b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Segment* segment );
+/* chains (shape.c:300-315, :439-640; box2d.h:860-900) */
+B2G_API b2ChainDef b2DefaultChainDef( void );
+B2G_API b2ChainId b2CreateChain( b2BodyId bodyId, const b2ChainDef* def );
+B2G_API bool b2Chain_IsValid( b2ChainId id );
+B2G_API int b2Chain_GetSegmentCount( b2ChainId chainId );
+B2G_API int b2Chain_GetSegments( b2ChainId chainId, b2ShapeId* segmentArray, int capacity );
+B2G_API b2ShapeId b2CreateChainSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2ChainSegment* chainSegment );
+B2G_API b2ShapeType b2Shape_GetType( b2ShapeId shapeId );
+B2G_API b2ChainSegment b2Shape_GetChainSegment( b2ShapeId shapeId );
+B2G_API b2ChainId b2Shape_GetParentChain( b2ShapeId shapeId );
 B2G_API b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Capsule* capsule );
 B2G_API b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon );
 B2G_API void b2Shape_SetFriction( b2ShapeId shapeId, float friction );

@@ -48,6 +48,13 @@ SCENES = [
     ("sensor_zoo_60", B.SENSOR_ZOO, 60, 0, 0, 5, B.NO_CONTINUOUS, 240, [1, 120, 240]),
 ]
 
+# chain shapes (one-sided segments with ghost vertices), with continuous collision on and
+# off; the oracle does not restate chains, so only the GB300 library is checked against these
+CHAIN_SCENES = [
+    ("chain_zoo_80", B.CHAIN_ZOO, 80, 0, 0, 3, 0, 300, [1, 100, 300]),
+    ("chain_zoo_80_discrete", B.CHAIN_ZOO, 80, 0, 0, 4, B.NO_CONTINUOUS, 300, [1, 150, 300]),
+]
+
 # sleeping on: islands fall asleep and wake; per step also the awake body count. The
 # oracle does not restate islands, so only the GB300 library is checked against these.
 SLEEP_SCENES = [
@@ -100,7 +107,7 @@ def main() -> None:
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"], check=True)
     ref = B.load_library(ROOT / "oracle" / "_ref" / "libref.so")
     only = set(sys.argv[1:])
-    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES + SLEEP_SCENES:
+    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES + CHAIN_SCENES + SLEEP_SCENES:
         if only and name not in only:
             continue
         sleeping = (name, kind, a, b, c, seed, flags, steps, digest_steps) in SLEEP_SCENES
@@ -130,6 +137,8 @@ def main() -> None:
                     "sensor_events": sensor_events.record(),
                     "world_state_hashes": world_hashes,
                     "source": "reference built from its own sources (oracle/Makefile ref)"}
+            if (name, kind, a, b, c, seed, flags, steps, digest_steps) in CHAIN_SCENES:
+                data["requires"] = "chains"
             if sleeping:
                 data["requires"] = "islands"
                 data["awake_counts"] = awake

@@ -52,7 +52,10 @@ def test_oracle_exports_the_public_api(oracle):
             # sensors are checked against fixtures recorded from the reference itself
             "b2World_GetSensorEvents", "b2Shape_IsSensor", "b2Shape_EnableSensorEvents",
             "b2Shape_AreSensorEventsEnabled", "b2Shape_GetSensorCapacity", "b2Shape_GetSensorData",
-            "b2s_sensor_events"}
+            "b2s_sensor_events",
+            # chain shapes are checked against fixtures recorded from the reference itself
+            "b2DefaultChainDef", "b2CreateChain", "b2Chain_IsValid", "b2Chain_GetSegmentCount", "b2Chain_GetSegments",
+            "b2CreateChainSegmentShape", "b2Shape_GetType", "b2Shape_GetChainSegment", "b2Shape_GetParentChain"}
     # differentiable stepping (box2d_gb300_diff.h) is an extension of the GB300 library; its
     # checker is the host tangent-linear code, not the oracle's public API
     missing = [n for n in sorted(declared_functions())

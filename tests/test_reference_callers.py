@@ -63,6 +63,19 @@ def test_reference_determinism_scene_builds_and_links(tmp_path):
     _build_driver(tmp_path)
 
 
+@pytest.mark.parametrize("source", ["shared/benchmarks.c", "benchmark/main.c", "test/test_determinism.c"])
+def test_reference_benchmark_sources_compile(source):
+    """The reference's benchmark scenes (chains, target transforms, the inline math) and its
+    benchmark driver compile unchanged against the public headers."""
+    ref = reference_dir()
+    if ref is None or not (ref / source).is_file():
+        pytest.skip("reference sources not present (set B2G_REFERENCE_DIR or run make -C oracle stage)")
+    cmd = ["gcc", "-std=gnu17", "-fsyntax-only", "-Werror=implicit-function-declaration", "-I", str(ROOT / "include"),
+           "-I", str(ref / "shared"), "-I", str(ref / "test"), str(ref / source)]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr
+
+
 @pytest.mark.gpu
 def test_reference_determinism_scene_runs_to_the_reference_constants(tmp_path):
     exe = _build_driver(tmp_path)
