@@ -34,6 +34,7 @@ JOINT_MIX = 12
 OVERFLOW = 13
 SENSOR_ZOO = 14
 CHAIN_ZOO = 15
+BULLET_ZOO = 16
 
 # scripted body changes (Scene.apply): name -> b2s_body_action kind
 BODY_ACTIONS = {"force": 0, "force_center": 1, "torque": 2, "impulse": 3, "impulse_center": 4, "angular_impulse": 5,

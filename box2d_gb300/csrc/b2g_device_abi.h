@@ -326,6 +326,11 @@ void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const 
    the returned array is valid until the next call. */
 int b2gDev_SensorOverlaps( b2gDeviceWorld* dw, const int* sensorShapeIds, int sensorCount, int shapeCount,
 						   const int** outPairs, int* outCount );
+/* solver.c:1917-1989: sweep the fast bullet bodies (awake slots) against the static,
+   kinematic and dynamic trees as last uploaded; per bullet shape a record (shape id,
+   enlarged) and its fat box. Waits for the device; results valid until the next call. */
+int b2gDev_SolveBullets( b2gDeviceWorld* dw, const b2gStepParams* params, int awakeCount, const int* bulletSims, int count,
+						 const int** outRecs, const float** outBoxes, int* outCount );
 /* the contact table of b2p_contacts built without allocating (noalloc.cu) */
 int b2gDev_ContactTableNoAlloc( b2gDeviceWorld* dw, int capacity, int* out, int outCapacity );
 
@@ -408,6 +413,8 @@ void b2gDev_BatchDestroy( b2gDevBatch* batch );
 int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on );
 /* whether the world's device work is being recorded for a batched flush */
 int b2gDev_IsRecording( b2gDeviceWorld* dw );
+/* device operations recorded since recording began */
+int b2gDev_RecordedCount( b2gDeviceWorld* dw );
 /* runs fn(ctx, i) for i in [0, count) on the caller's threads */
 typedef void ( *b2gParallelFor )( void* pool, int count, void ( *fn )( void* ctx, int index ), void* ctx );
 int b2gDev_BatchFlush( b2gDevBatch* batch, b2gDeviceWorld* const* worlds, int count, b2gParallelFor parallelFor, void* pool );

@@ -577,6 +577,12 @@ struct d_ccdWorld
 {
 	const b2gTreeNode* staticTree;
 	int staticRoot;
+	/* for bullets (solver.c:443-447): the kinematic and dynamic trees after this step's
+	   enlargement, or null */
+	const b2gTreeNode* kinematicTree;
+	int kinematicRoot;
+	const b2gTreeNode* dynamicTree;
+	int dynamicRoot;
 	const b2gShape* shapes;
 	const float4* xf;
 	const float2* center;
@@ -645,7 +651,8 @@ static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId
 	}
 	d_proxy proxyA = d_shapeProxy( shape );
 	d_proxy proxyB = d_shapeProxy( fastShape );
-	/* a static body's sweep is at rest: center0 = center, rotation0 = rotation */
+	/* the candidate's sweep is at rest: a static body's, and (for bullets) a kinematic or
+	   non-bullet dynamic body's, whose center0 and rotation0 the finalize set to its pose */
 	float2 c = cw.center[bodyId];
 	float4 x = cw.xf[bodyId];
 	float2 lc = cw.localCenter[bodyId];
@@ -673,18 +680,17 @@ static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId
 	return fraction;
 }
 
-/* dynamic_tree.c b2DynamicTree_Query over the static tree with the swept box, visiting
+/* dynamic_tree.c b2DynamicTree_Query over one tree with the swept box, visiting
    overlapping leaves in the reference's order (children pushed child1 then child2) */
-static __device__ float d_continuousQuery( const d_ccdWorld& cw, float4 box, int fastShapeId, const b2gShape* fastShape,
-										   const d_sweep& fastSweep, b2Vec2 base, float fraction, bool* hit, bool* overflow,
-										   const d_fastShape& fast )
+static __device__ float d_continuousQuery( const d_ccdWorld& cw, const b2gTreeNode* tree, int root, float4 box, int fastShapeId,
+										   const b2gShape* fastShape, const d_sweep& fastSweep, b2Vec2 base, float fraction,
+										   bool* hit, bool* overflow, const d_fastShape& fast )
 {
-	int root = cw.staticRoot;
-	if ( root < 0 ) return fraction;
+	if ( tree == nullptr || root < 0 ) return fraction;
 	int2 stack[D_CCD_STACK];
 	int sp = 0;
 	{
-		const b2gTreeNode r = cw.staticTree[root];
+		const b2gTreeNode r = tree[root];
 		if ( d_overlaps( r.aabb, box ) == false || r.categoryNonZero == 0 ) return fraction;
 		stack[sp++] = r.isLeaf ? make_int2( ~root, r.child1 ) : make_int2( r.child1, r.child2 );
 	}
@@ -696,8 +702,8 @@ static __device__ float d_continuousQuery( const d_ccdWorld& cw, float4 box, int
 			fraction = d_continuousCandidate( cw, e.y, fastShapeId, fastShape, fastSweep, base, fraction, hit, fast );
 			continue;
 		}
-		const b2gTreeNode c1 = cw.staticTree[e.x];
-		const b2gTreeNode c2 = cw.staticTree[e.y];
+		const b2gTreeNode c1 = tree[e.x];
+		const b2gTreeNode c2 = tree[e.y];
 		bool hit1 = d_overlaps( c1.aabb, box ) && c1.categoryNonZero != 0;
 		bool hit2 = d_overlaps( c2.aabb, box ) && c2.categoryNonZero != 0;
 		if ( sp + 2 > D_CCD_STACK )

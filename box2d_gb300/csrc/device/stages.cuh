@@ -425,7 +425,8 @@ struct d_finalizeArgs
    static tree, move the body back to the earliest time of impact, and refresh the shape
    boxes. Kept out of line: fast bodies are rare and the sweep needs a deep stack.
    Returns whether a shape's fat box was enlarged. */
-static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, int simIndex, int bodyId, b2Vec2 center, b2Rot q )
+static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, int simIndex, int bodyId, b2Vec2 center, b2Rot q,
+														bool isBullet )
 {
 	float4 c0 = a.center0[simIndex];
 	b2Vec2 base = { c0.x, c0.y };
@@ -455,7 +456,15 @@ static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, 
 		fast.centroid1 = d_transformPoint( xf1, fastShape->ccdCentroid );
 		fast.centroid2 = d_transformPoint( xf2, fastShape->ccdCentroid );
 		fast.coreDistance = D_CORE_FRACTION * a.minExtent[bodyId];
-		fraction = d_continuousQuery( a.ccd, swept, shapeId, fastShape, sweep, base, fraction, &hit, &overflow, fast );
+		fraction = d_continuousQuery( a.ccd, a.ccd.staticTree, a.ccd.staticRoot, swept, shapeId, fastShape, sweep, base, fraction,
+									  &hit, &overflow, fast );
+		if ( isBullet )
+		{
+			fraction = d_continuousQuery( a.ccd, a.ccd.kinematicTree, a.ccd.kinematicRoot, swept, shapeId, fastShape, sweep, base,
+										  fraction, &hit, &overflow, fast );
+			fraction = d_continuousQuery( a.ccd, a.ccd.dynamicTree, a.ccd.dynamicRoot, swept, shapeId, fastShape, sweep, base,
+										  fraction, &hit, &overflow, fast );
+		}
 	}
 	atomicAdd( &a.counters->continuousSweeps, 1 );
 	if ( overflow ) atomicOr( &a.counters->status, B2G_STATUS_CAPACITY );
@@ -596,8 +605,11 @@ static __device__ void d_finalizeBody( const d_finalizeArgs& a, int simIndex )
 	if ( a.toi != nullptr ) a.toi[simIndex] = 1.0f;
 	int start = a.shapeStart[bodyId], count = a.shapeCount[bodyId];
 	bool anyEnlarged = false;
-	if ( sweep ) anyEnlarged = d_solveContinuous( a, simIndex, bodyId, center, q );
-	else a.center0[simIndex] = make_float4( center.x, center.y, q.c, q.s );
+	bool fastBullet = ( bodyFlags & B2G_IS_FAST ) != 0 && isBullet;
+	if ( sweep ) anyEnlarged = d_solveContinuous( a, simIndex, bodyId, center, q, false );
+	else if ( fastBullet == false ) a.center0[simIndex] = make_float4( center.x, center.y, q.c, q.s );
+	/* a fast bullet keeps its sweep start (center0) for the bullet pass after the broadphase
+	   enlargement (solver.c:1917-1928) */
 	bool isFast = ( bodyFlags & B2G_IS_FAST ) != 0;
 	b2Transform transform = { p, q };
 	for ( int k = 0; k < count && sweep == false; ++k )
@@ -621,7 +633,6 @@ static __device__ void d_finalizeBody( const d_finalizeArgs& a, int simIndex )
 		}
 		a.shapeEnlarged[shapeId] = enlarged;
 	}
-	bool fastBullet = isFast && isBullet;
 	if ( anyEnlarged || fastBullet )
 	{
 		int base = atomicAdd( &a.counters->enlargedBodyCount, count );

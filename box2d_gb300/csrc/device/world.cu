@@ -195,6 +195,18 @@ struct b2gDeviceWorld
 	int pairsTimingPending;
 	cudaEvent_t syncEvent; /* blocking-sync event for waits of batched steps */
 	int blockingSync;
+	/* bullet pass: bullet body slots in, shape records out */
+	int* bulletSims;
+	int bulletSimsCap;
+	int* bulletRecs; /* 2 ints per bullet shape: shape id, enlarged */
+	int bulletRecsCap;
+	float4* bulletBoxes;
+	int bulletBoxesCap;
+	int* bulletCount;
+	int* hBulletRecs;
+	int hBulletRecsCap;
+	float4* hBulletBoxes;
+	int hBulletBoxesCap;
 	/* sensor overlap pass: sensor shape ids in, (sensor, shape) pairs out */
 	int* sensorIds;
 	int sensorIdsCap;
@@ -1021,7 +1033,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->moveStage, dw->pairPacked, dw->pairOffsets, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
 					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList,
 					  dw->sleepTime, dw->islandLocal, dw->islandInfo, dw->islandBits, dw->sensorIds, dw->sensorPairs,
-					  dw->sensorCount };
+					  dw->sensorCount, dw->bulletSims, dw->bulletRecs, dw->bulletBoxes, dw->bulletCount };
 	b2gDev_CompFree( &dw->comp );
 	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
 		if ( dptrs[i] ) cudaFree( dptrs[i] );
@@ -1030,7 +1042,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	void* hptrs[] = { dw->hCounters, dw->hChanges,	   dw->hRecs,	   dw->hBoxes,	   dw->hPairs,	  dw->hPairCounts,
 					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw, dw->hSortKeys,
 					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV, dw->hSleepTime, dw->hIslandBits,
-					  dw->hSensorPairs };
+					  dw->hSensorPairs, dw->hBulletRecs, dw->hBulletBoxes };
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
 		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
 	free( dw->hSortTmp );
@@ -2104,6 +2116,127 @@ static int cmpRec( const void* a, const void* b )
 
 /* the solver and finalize of one step, issued (or recorded: one-CTA worlds only); the
    counters and the first `window` enlarged-proxy records arrive with the world's next wait */
+/* the finalize arguments of this world's current state (solver.c b2FinalizeBodiesTask and
+   b2SolveContinuous read and write these arrays); trees beyond the static one are off */
+static void finalizeArgsFor( b2gDeviceWorld* dw, const b2gStepParams* p, int awakeCount, int shapeTotal, d_finalizeArgs* f )
+{
+	f->sv = dw->stateV;
+	f->sd = dw->stateD;
+	f->params = dw->params;
+	f->center0 = dw->center0;
+	f->awakeBodyId = dw->awakeBodyId;
+	f->awakeCount = awakeCount;
+	f->xf = dw->xf;
+	f->center = dw->center;
+	f->localCenter = dw->localCenter;
+	f->minExtent = dw->minExtent;
+	f->maxExtent = dw->maxExtent;
+	f->sleepThreshold = dw->sleepThreshold;
+	f->safetyFactor = dw->safetyFactor;
+	f->bodyType = dw->bodyType;
+	f->bodyFlags = dw->bodyFlags;
+	f->shapeStart = dw->shapeStart;
+	f->shapeCount = dw->shapeCount;
+	f->shapeList = dw->shapeList;
+	f->shapes = dw->shapes;
+	f->aabb = dw->aabb;
+	f->fat = dw->fat;
+	f->shapeEnlarged = dw->shapeEnlarged;
+	f->enlargedRecs = dw->enlargedRecs;
+	f->enlargedBoxes = dw->enlargedBoxes;
+	f->enlargedCap = shapeTotal;
+	f->counters = dw->counters;
+	f->dt = p->dt;
+	f->inv_dt = p->inv_dt;
+	f->enableSleep = p->enableSleep;
+	f->enableContinuous = p->enableContinuous;
+	f->ccd.staticTree = dw->tree[b2_staticBody];
+	f->ccd.staticRoot = dw->tree[b2_staticBody] != NULL ? dw->treeRoot[b2_staticBody] : -1;
+	f->ccd.kinematicTree = NULL;
+	f->ccd.kinematicRoot = -1;
+	f->ccd.dynamicTree = NULL;
+	f->ccd.dynamicRoot = -1;
+	f->ccd.shapes = dw->shapes;
+	f->ccd.xf = dw->xf;
+	f->ccd.center = dw->center;
+	f->ccd.localCenter = dw->localCenter;
+	f->ccd.bodyFlags = dw->bodyFlags;
+	f->ccd.partnerOffsets = dw->partnerCount > 0 ? dw->partnerOffsets : NULL;
+	f->ccd.partnerList = dw->partnerCount > 0 ? dw->partnerList : NULL;
+}
+
+/* solver.c:1917-1928 b2BulletBodyTask: each fast bullet body swept against the static,
+   kinematic and dynamic trees (the latter two as the host left them after this step's
+   broadphase enlargement), moved back to its earliest time of impact, its shapes' boxes
+   refreshed; one record (shape id, enlarged) and fat box per bullet shape */
+__global__ void k_bullets( d_finalizeArgs f, const int* bulletSims, int count, int* recs, float4* boxes, int* recCount, int recCap )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= count ) return;
+	int simIndex = bulletSims[i];
+	int bodyId = f.awakeBodyId[simIndex];
+	float2 c = f.center[bodyId];
+	float4 x = f.xf[bodyId];
+	d_solveContinuous( f, simIndex, bodyId, d_v( c.x, c.y ), b2Rot{ x.z, x.w }, true );
+	int start = f.shapeStart[bodyId], n = f.shapeCount[bodyId];
+	int base = atomicAdd( recCount, n );
+	for ( int k = 0; k < n && base + k < recCap; ++k )
+	{
+		int shapeId = f.shapeList[start + k];
+		recs[2 * ( base + k )] = shapeId;
+		recs[2 * ( base + k ) + 1] = f.shapeEnlarged[shapeId];
+		boxes[base + k] = f.fat[shapeId];
+	}
+}
+
+extern "C" int b2gDev_SolveBullets( b2gDeviceWorld* dw, const b2gStepParams* p, int awakeCount, const int* bulletSims, int count,
+									const int** outRecs, const float** outBoxes, int* outCount )
+{
+	*outRecs = NULL;
+	*outBoxes = NULL;
+	*outCount = 0;
+	if ( count <= 0 ) return 0;
+	int shapeTotal = dw->shapeCountTotal;
+	int cap = shapeTotal > 0 ? shapeTotal : 1;
+	CK2( grow( dw, (void**)&dw->bulletSims, &dw->bulletSimsCap, count, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->bulletRecs, &dw->bulletRecsCap, 2 * cap, sizeof( int ) ) );
+	CK2( grow( dw, (void**)&dw->bulletBoxes, &dw->bulletBoxesCap, cap, sizeof( float4 ) ) );
+	if ( dw->bulletCount == NULL ) CK( cudaMalloc( &dw->bulletCount, sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hBulletRecs, &dw->hBulletRecsCap, 2 * cap, sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hBulletBoxes, &dw->hBulletBoxesCap, cap, sizeof( float4 ) ) );
+	d_finalizeArgs f;
+	memset( &f, 0, sizeof( f ) );
+	finalizeArgsFor( dw, p, awakeCount, shapeTotal, &f );
+	f.ccd.kinematicTree = dw->tree[b2_kinematicBody];
+	f.ccd.kinematicRoot = dw->tree[b2_kinematicBody] != NULL ? dw->treeRoot[b2_kinematicBody] : -1;
+	f.ccd.dynamicTree = dw->tree[b2_dynamicBody];
+	f.ccd.dynamicRoot = dw->tree[b2_dynamicBody] != NULL ? dw->treeRoot[b2_dynamicBody] : -1;
+	f.toi = NULL;
+	f.sleepTime = dw->sleepTime;
+	CK( cudaMemcpyAsync( dw->bulletSims, bulletSims, (size_t)count * sizeof( int ), cudaMemcpyHostToDevice, dw->stream ) );
+	dw->h2dBytes += (long long)count * (long long)sizeof( int );
+	CK( cudaMemsetAsync( dw->bulletCount, 0, sizeof( int ), dw->stream ) );
+	k_bullets<<<( count + 63 ) / 64, 64, 0, dw->stream>>>( f, dw->bulletSims, count, dw->bulletRecs, dw->bulletBoxes, dw->bulletCount, cap );
+	dw->launches += 1;
+	CK( cudaGetLastError() );
+	int n = 0;
+	CK( cudaMemcpyAsync( &n, dw->bulletCount, sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	if ( n > cap ) n = cap;
+	if ( n > 0 )
+	{
+		CK( cudaMemcpyAsync( dw->hBulletRecs, dw->bulletRecs, (size_t)n * 2 * sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaMemcpyAsync( dw->hBulletBoxes, dw->bulletBoxes, (size_t)n * sizeof( float4 ), cudaMemcpyDeviceToHost, dw->stream ) );
+		CK( cudaStreamSynchronize( dw->stream ) );
+		dw->d2hBytes += (long long)n * (long long)( 2 * sizeof( int ) + sizeof( float4 ) );
+	}
+	*outRecs = dw->hBulletRecs;
+	*outBoxes = (const float*)dw->hBulletBoxes;
+	*outCount = n;
+	dw->prefetchValid = 0;
+	return 0;
+}
+
 extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, const int* activeColors, int activeColorCount,
 								   int awakeCount )
 {
@@ -2129,45 +2262,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	CK2( grow( dw, (void**)&dw->enlargedRecs, &dw->enlargedCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( int ) ) );
 	CK2( grow( dw, (void**)&dw->enlargedBoxes, &dw->enlargedBoxesCap, shapeTotal > 0 ? shapeTotal : 1, sizeof( float4 ) ) );
 	d_finalizeArgs f;
-	f.sv = dw->stateV;
-	f.sd = dw->stateD;
-	f.params = dw->params;
-	f.center0 = dw->center0;
-	f.awakeBodyId = dw->awakeBodyId;
-	f.awakeCount = awakeCount;
-	f.xf = dw->xf;
-	f.center = dw->center;
-	f.localCenter = dw->localCenter;
-	f.minExtent = dw->minExtent;
-	f.maxExtent = dw->maxExtent;
-	f.sleepThreshold = dw->sleepThreshold;
-	f.safetyFactor = dw->safetyFactor;
-	f.bodyType = dw->bodyType;
-	f.bodyFlags = dw->bodyFlags;
-	f.shapeStart = dw->shapeStart;
-	f.shapeCount = dw->shapeCount;
-	f.shapeList = dw->shapeList;
-	f.shapes = dw->shapes;
-	f.aabb = dw->aabb;
-	f.fat = dw->fat;
-	f.shapeEnlarged = dw->shapeEnlarged;
-	f.enlargedRecs = dw->enlargedRecs;
-	f.enlargedBoxes = dw->enlargedBoxes;
-	f.enlargedCap = shapeTotal;
-	f.counters = dw->counters;
-	f.dt = p->dt;
-	f.inv_dt = p->inv_dt;
-	f.enableSleep = p->enableSleep;
-	f.enableContinuous = p->enableContinuous;
-	f.ccd.staticTree = dw->tree[b2_staticBody];
-	f.ccd.staticRoot = dw->tree[b2_staticBody] != NULL ? dw->treeRoot[b2_staticBody] : -1;
-	f.ccd.shapes = dw->shapes;
-	f.ccd.xf = dw->xf;
-	f.ccd.center = dw->center;
-	f.ccd.localCenter = dw->localCenter;
-	f.ccd.bodyFlags = dw->bodyFlags;
-	f.ccd.partnerOffsets = dw->partnerCount > 0 ? dw->partnerOffsets : NULL;
-	f.ccd.partnerList = dw->partnerCount > 0 ? dw->partnerList : NULL;
+	finalizeArgsFor( dw, p, awakeCount, shapeTotal, &f );
 	f.toi = dw->tapeToi;
 	dw->tapeToi = NULL;
 	f.sleepTime = dw->sleepTime;
@@ -2652,6 +2747,8 @@ extern "C" int b2gDev_BatchRecord( b2gDeviceWorld* dw, int on )
 }
 
 extern "C" int b2gDev_IsRecording( b2gDeviceWorld* dw ) { return dw->defer != NULL; }
+
+extern "C" int b2gDev_RecordedCount( b2gDeviceWorld* dw ) { return dw->defer != NULL ? (int)dw->defer->ops.size() : 0; }
 
 /* sensor.c:43-120 b2SensorQueryCallback, one block per sensor over every shape: the tree
    query's tests (the shape's fat box meets the sensor's box, its category meets the

@@ -405,7 +405,51 @@ static void h_enlargeProxies( h_world* w, const int* recs, const float* boxes, i
 	}
 }
 
-/* ---- the step in four phases, split at its three waits (pair query, narrowphase,
+/* solver.c:1917-1989: fast bullet bodies are swept after the broadphase enlargement,
+   against the static, kinematic and dynamic trees as it left them; their shapes' grown
+   boxes then enlarge the dynamic tree (their moves were buffered by the enlargement) */
+static void h_solveBullets( h_world* w, const int* recs, int count )
+{
+	int* sims = NULL;
+	int n = 0, last = -1;
+	for ( int i = 0; i < count; ++i )
+	{
+		if ( recs[4 * i + 3] == 0 || recs[4 * i] == last ) continue;
+		last = recs[4 * i];
+		if ( sims == NULL ) sims = malloc( (size_t)count * sizeof( int ) );
+		sims[n++] = last;
+	}
+	if ( n == 0 ) return;
+	/* a batched step records device work for its flushes; the bullet pass waits for its
+	   results, so it runs on the world's own stream (the world's earlier work has been
+	   flushed by now and nothing of this phase is recorded yet) */
+	int recording = b2gDev_IsRecording( w->dev );
+	if ( recording )
+	{
+		if ( b2gDev_RecordedCount( w->dev ) != 0 ) h_fail( w, "bullets inside a batched flush", -1 );
+		b2gDev_BatchRecord( w->dev, 0 );
+	}
+	h_uploadTree( w, b2_kinematicBody );
+	h_uploadTree( w, b2_dynamicBody );
+	const int* brecs = NULL;
+	const float* bboxes = NULL;
+	int bcount = 0;
+	int rc = b2gDev_SolveBullets( w->dev, &w->stepParams, w->awakeBodyIds.count, sims, n, &brecs, &bboxes, &bcount );
+	free( sims );
+	if ( recording ) b2gDev_BatchRecord( w->dev, 1 );
+	if ( rc != 0 ) h_fail( w, "bullets", rc );
+	h_tree* dynamicTree = w->trees + b2_dynamicBody;
+	for ( int i = 0; i < bcount; ++i )
+	{
+		if ( brecs[2 * i + 1] == 0 ) continue;
+		h_shape* s = w->shapes.data + brecs[2 * i];
+		b2AABB fat = { { bboxes[4 * i], bboxes[4 * i + 1] }, { bboxes[4 * i + 2], bboxes[4 * i + 3] } };
+		s->fatAABB = fat;
+		h_treeEnlargeProxy( dynamicTree, H_PROXY_ID( s->proxyKey ), fat );
+	}
+}
+
+/* ---- the step in four phases, split at its three waits/* ---- the step in four phases, split at its three waits (pair query, narrowphase,
    solver); b2World_Step runs them back to back, b2World_StepBatch runs each phase over
    many worlds and replaces the waits by one batched flush ---- */
 
@@ -575,6 +619,7 @@ void h_stepFinish( h_world* w )
 		}
 		w->forcedBodies.count = 0;
 		h_enlargeProxies( w, recs, boxes, enlargedCount );
+		h_solveBullets( w, recs, enlargedCount );
 		h_lap( w, H_PHASE_ENLARGE, &lap );
 		{
 			/* island sleeping comes last (solver.c:2024-2080) */

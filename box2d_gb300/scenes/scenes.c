@@ -1129,6 +1129,58 @@ static void b2sChainZoo( b2sScene* s, int count, b2sRng* rng )
 }
 #endif
 
+/* Bullet scene (solver.c:1917-1989): a wall of boxes and a stack of thin planks on the
+   ground, hit by `count` bullet bodies (small circles and boxes flagged isBullet) fired at
+   80-250 m/s from both sides at staggered heights, so that they are swept against dynamic
+   bodies as well as static ones. */
+static void b2sBulletZoo( b2sScene* s, int count, b2sRng* rng )
+{
+	b2World_EnableSleeping( s->worldId, false );
+	b2BodyId ground = b2sBody( s, b2_staticBody, 0.0f, 0.0f );
+	b2ShapeDef gd = b2DefaultShapeDef();
+	b2Polygon gbox = b2MakeOffsetBox( 60.0f, 0.5f, ( b2Vec2 ){ 0.0f, -0.5f }, b2MakeRot( 0.0f ) );
+	b2CreatePolygonShape( ground, &gd, &gbox );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2Polygon brick = b2MakeBox( 0.25f, 0.25f );
+	for ( int i = 0; i < 12; ++i )
+		for ( int j = 0; j < 4; ++j )
+		{
+			b2BodyId b = b2sBody( s, b2_dynamicBody, -1.0f + 0.5f * j, 0.25f + 0.5f * i );
+			b2CreatePolygonShape( b, &sd, &brick );
+		}
+	b2Polygon plank = b2MakeBox( 0.05f, 1.0f );
+	for ( int k = 0; k < 6; ++k )
+	{
+		b2BodyId b = b2sBody( s, b2_dynamicBody, 8.0f + 0.4f * k, 1.0f );
+		b2CreatePolygonShape( b, &sd, &plank );
+	}
+	for ( int k = 0; k < count; ++k )
+	{
+		float side = ( k & 1 ) ? 1.0f : -1.0f;
+		b2BodyDef bd = b2DefaultBodyDef();
+		bd.type = b2_dynamicBody;
+		bd.isBullet = true;
+		bd.position.x = side * b2sRandomFloatRange( rng, 20.0f, 40.0f );
+		bd.position.y = b2sRandomFloatRange( rng, 0.3f, 5.5f );
+		bd.linearVelocity.x = -side * b2sRandomFloatRange( rng, 80.0f, 250.0f );
+		bd.linearVelocity.y = b2sRandomFloatRange( rng, -2.0f, 2.0f );
+		b2BodyId b = b2CreateBody( s->worldId, &bd );
+		b2sAddBody( s, b, 1 );
+		b2ShapeDef bs = b2DefaultShapeDef();
+		bs.density = 4.0f;
+		if ( k % 3 == 0 )
+		{
+			b2Polygon p = b2MakeBox( 0.08f, 0.08f );
+			b2CreatePolygonShape( b, &bs, &p );
+		}
+		else
+		{
+			b2Circle c = { { 0.0f, 0.0f }, b2sRandomFloatRange( rng, 0.05f, 0.12f ) };
+			b2CreateCircleShape( b, &bs, &c );
+		}
+	}
+}
+
 enum
 {
 	B2S_LARGE_PYRAMID = 0,
@@ -1147,6 +1199,7 @@ enum
 	B2S_OVERFLOW = 13,
 	B2S_SENSOR_ZOO = 14,
 	B2S_CHAIN_ZOO = 15,
+	B2S_BULLET_ZOO = 16,
 };
 
 /* Worker threads requested in the world definition of scenes created from now on (0 keeps
@@ -1205,6 +1258,7 @@ B2S_EXPORT int b2s_create( int kind, int a, int b, int c, uint32_t seed, int fla
 #ifndef B2S_NO_CHAINS
 		case B2S_CHAIN_ZOO: b2sChainZoo( s, a, &rng ); break;
 #endif
+		case B2S_BULLET_ZOO: b2sBulletZoo( s, a, &rng ); break;
 		default: break;
 	}
 	return h;

@@ -55,6 +55,12 @@ CHAIN_SCENES = [
     ("chain_zoo_80_discrete", B.CHAIN_ZOO, 80, 0, 0, 4, B.NO_CONTINUOUS, 300, [1, 150, 300]),
 ]
 
+# bullets swept against dynamic bodies; the oracle advances bullets like other fast bodies
+# (static sweeps only), so only the GB300 library is checked against these
+BULLET_SCENES = [
+    ("bullet_zoo_24", B.BULLET_ZOO, 24, 0, 0, 7, 0, 200, [1, 20, 200]),
+]
+
 # sleeping on: islands fall asleep and wake; per step also the awake body count. The
 # oracle does not restate islands, so only the GB300 library is checked against these.
 SLEEP_SCENES = [
@@ -107,7 +113,7 @@ def main() -> None:
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"], check=True)
     ref = B.load_library(ROOT / "oracle" / "_ref" / "libref.so")
     only = set(sys.argv[1:])
-    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES + CHAIN_SCENES + SLEEP_SCENES:
+    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES + CHAIN_SCENES + BULLET_SCENES + SLEEP_SCENES:
         if only and name not in only:
             continue
         sleeping = (name, kind, a, b, c, seed, flags, steps, digest_steps) in SLEEP_SCENES
@@ -139,6 +145,8 @@ def main() -> None:
                     "source": "reference built from its own sources (oracle/Makefile ref)"}
             if (name, kind, a, b, c, seed, flags, steps, digest_steps) in CHAIN_SCENES:
                 data["requires"] = "chains"
+            if (name, kind, a, b, c, seed, flags, steps, digest_steps) in BULLET_SCENES:
+                data["requires"] = "bullets"
             if sleeping:
                 data["requires"] = "islands"
                 data["awake_counts"] = awake
