@@ -19,6 +19,8 @@
 
 #define B2G_BARRIER_SPIN_LIMIT ( 1u << 22 )
 
+#include <stdlib.h>
+
 struct d_colorRange
 {
 	int jointBegin, jointCount, laneBegin, laneCount;
@@ -32,6 +34,7 @@ struct d_persistentPlan
 	int total, jointTotal, awakeCount, substeps;
 	d_jointBodies jb;
 	unsigned int* barrier; /* [0] arrivals, [1] generation */
+	unsigned int spinLimit; /* polls before a barrier gives up */
 	int* error;
 	int* anyRestitution;
 };
@@ -65,7 +68,7 @@ static __device__ bool d_gridBarrier( const d_persistentPlan& plan )
 			unsigned int polls = 0;
 			while ( *gen == myGen )
 			{
-				if ( ++polls > B2G_BARRIER_SPIN_LIMIT )
+				if ( ++polls > plan.spinLimit )
 				{
 					atomicOr( plan.error, B2G_PERSISTENT_TIMEOUT );
 					break;
@@ -185,6 +188,13 @@ extern "C" int b2gDev_LaunchPersistent( const d_solveArgs* a, const d_finalizeAr
 	plan.substeps = substeps;
 	plan.jb = *jb;
 	plan.barrier = barrier;
+	/* B2G_PERSISTENT_SPIN_LIMIT shortens the barrier's patience, so that a test can make a
+	   barrier give up and check the reported status */
+	plan.spinLimit = B2G_BARRIER_SPIN_LIMIT;
+	{
+		const char* limit = getenv( "B2G_PERSISTENT_SPIN_LIMIT" );
+		if ( limit != NULL && atoi( limit ) > 0 ) plan.spinLimit = (unsigned int)atoi( limit );
+	}
 	plan.error = error;
 	plan.anyRestitution = anyRestitution;
 	int maxWork = total > awakeCount ? total : awakeCount;

@@ -27,6 +27,11 @@
 #define B2G_THREADS 128
 #define B2G_PAIR_STACK 256
 
+/* the pair query's traversal stack depth in use (at most B2G_PAIR_STACK); the environment
+   variable B2G_PAIR_STACK_LIMIT lowers it so that a test can exhaust it and check the
+   capacity status */
+static __device__ int d_pairStackLimit = B2G_PAIR_STACK;
+
 /* solver strategies, chosen per world from the B2G_SOLVER environment variable at creation:
    "components" (default) solves small connected components one CTA each out of shared
    memory and the rest in one thread-block cluster (or, when they do not fit one, with one
@@ -573,7 +578,7 @@ static __device__ void b_findPairs( const d_findPairsArgs& fa, int block, int gr
 			const b2gTreeNode c2 = nodes[e.y];
 			bool hit1 = d_overlaps( c1.aabb, box ) && c1.categoryNonZero != 0;
 			bool hit2 = d_overlaps( c2.aabb, box ) && c2.categoryNonZero != 0;
-			if ( sp + 2 > B2G_PAIR_STACK )
+			if ( sp + 2 > d_pairStackLimit )
 			{
 				full = true;
 				break;
@@ -1000,6 +1005,11 @@ extern "C" int b2gDev_Create( b2gDeviceWorld** out )
 	if ( count == 0 ) return (int)cudaErrorNoDevice;
 	b2gDeviceWorld* dw = new b2gDeviceWorld(); /* value-initialized: every field zero */
 	CK( cudaGetDevice( &dw->device ) );
+	{
+		const char* limit = getenv( "B2G_PAIR_STACK_LIMIT" );
+		int v = limit != NULL ? atoi( limit ) : 0;
+		if ( v >= 2 && v <= B2G_PAIR_STACK ) CK( cudaMemcpyToSymbol( d_pairStackLimit, &v, sizeof( int ) ) );
+	}
 	/* a blocking stream: buffer growth (cudaMalloc + cudaMemset / cudaMemcpy on the legacy
 	   default stream) is then ordered before every kernel of this world */
 	CK( cudaStreamCreate( &dw->stream ) );
