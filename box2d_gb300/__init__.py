@@ -38,7 +38,7 @@ BULLET_ZOO = 16
 
 # scripted body changes (Scene.apply): name -> b2s_body_action kind
 BODY_ACTIONS = {"force": 0, "force_center": 1, "torque": 2, "impulse": 3, "impulse_center": 4, "angular_impulse": 5,
-                "transform": 6, "target": 7}
+                "transform": 6, "target": 7, "destroy_body": 8, "destroy_shape": 9}
 
 NO_CONTINUOUS = 1
 NO_WARM_STARTING = 2

@@ -177,7 +177,9 @@ typedef struct h_world
 	H_ARRAY( b2gJoint ) jointRecords; /* by joint id; device copy is authoritative */
 	h_intArray awakeBodyIds;		  /* awake index -> body id */
 	int staticCount;
-	int staticJointCount; /* joints of the static set (between two non-dynamic bodies) */
+	h_intArray staticBodyIds;  /* the static set's bodies, reference array order */
+	int staticJointCount;	   /* joints of the static set (between two non-dynamic bodies) */
+	h_intArray staticJointIds; /* those joints, reference array order */
 	h_intArray awakeContactIds;		  /* non-touching contacts, reference array order */
 	h_intArray disabledContactIds;	  /* non-touching contacts between sleeping bodies */
 	/* islands and sleeping (island.c) */
@@ -268,6 +270,9 @@ void h_createIslandForBody( h_world* w, int setIndex, h_body* body );
 void h_linkContact( h_world* w, h_contact* contact );
 void h_unlinkContact( h_world* w, h_contact* contact );
 void h_linkJoint( h_world* w, h_joint* joint );
+void h_unlinkJoint( h_world* w, h_joint* joint );
+void h_removeBodyFromIsland( h_world* w, h_body* body );
+void h_freeSleepingSet( h_world* w, int setIndex );
 void h_splitIsland( h_world* w, int baseId );
 void h_wakeSolverSet( h_world* w, int setIndex );
 void h_trySleepIsland( h_world* w, int islandId );

@@ -100,6 +100,8 @@ static h_island* h_createIsland( h_world* w, int setIndex )
 }
 
 /* island.c:49-80: swap-remove from the set's island list, free the id */
+static void h_destroySleepingSet( h_world* w, int setIndex );
+
 static void h_destroyIsland( h_world* w, int islandId )
 {
 	if ( w->splitIslandId == islandId ) w->splitIslandId = B2_NULL_INDEX;
@@ -204,6 +206,41 @@ void h_unlinkContact( h_world* w, h_contact* contact )
 	island->constraintRemoveCount += 1;
 	w->islandsDirty = 1;
 }
+
+/* island.c:311-340 */
+void h_unlinkJoint( h_world* w, h_joint* joint )
+{
+	if ( joint->islandId == B2_NULL_INDEX ) return;
+	h_island* island = w->islands.data + joint->islandId;
+	int removeIndex = joint->islandIndex;
+	int moved = h_removeSwap( island->joints, removeIndex );
+	if ( moved != B2_NULL_INDEX ) w->joints.data[island->joints.data[removeIndex].id].islandIndex = removeIndex;
+	joint->islandId = B2_NULL_INDEX;
+	joint->islandIndex = B2_NULL_INDEX;
+	island->constraintRemoveCount += 1;
+	w->islandsDirty = 1;
+}
+
+/* body.c:120-155: the body leaves its island (the last body takes its slot); an island
+   left without bodies is destroyed */
+void h_removeBodyFromIsland( h_world* w, h_body* body )
+{
+	if ( body->islandId == B2_NULL_INDEX ) return;
+	int islandId = body->islandId;
+	h_island* island = w->islands.data + islandId;
+	int localIndex = body->islandIndex;
+	int movedBodyId = island->bodies.data[island->bodies.count - 1];
+	island->bodies.data[localIndex] = movedBodyId;
+	w->bodies.data[movedBodyId].islandIndex = localIndex;
+	island->bodies.count -= 1;
+	if ( island->bodies.count == 0 ) h_destroyIsland( w, islandId );
+	w->islandsDirty = 1;
+	body->islandId = B2_NULL_INDEX;
+	body->islandIndex = B2_NULL_INDEX;
+}
+
+/* solver_set.c:16-27 for a sleeping set left empty */
+void h_freeSleepingSet( h_world* w, int setIndex ) { h_destroySleepingSet( w, setIndex ); }
 
 /* island.c:280-307 */
 void h_linkJoint( h_world* w, h_joint* joint )

@@ -183,6 +183,7 @@ static b2gJoint* h_createJoint( h_world* w, const b2JointDef* def, b2JointType t
 		j->setIndex = H_STATIC_SET;
 		j->colorIndex = B2_NULL_INDEX;
 		j->localIndex = w->staticJointCount++;
+		h_push( w->staticJointIds, jointId );
 	}
 	else if ( bodyA->setIndex == H_AWAKE_SET || bodyB->setIndex == H_AWAKE_SET )
 	{

@@ -265,6 +265,8 @@ void b2DestroyWorld( b2WorldId worldId )
 	h_free( w->pendingInits );
 	h_free( w->pendingKills );
 	h_free( w->forcedBodies );
+	h_free( w->staticBodyIds );
+	h_free( w->staticJointIds );
 	h_islandsFree( w );
 	uint16_t generation = w->generation;
 	memset( w, 0, sizeof( *w ) );
@@ -854,6 +856,7 @@ b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def )
 	{
 		b->setIndex = H_STATIC_SET;
 		b->localIndex = w->staticCount++;
+		h_push( w->staticBodyIds, bodyId );
 	}
 	else if ( isAwake )
 	{
@@ -994,6 +997,204 @@ void b2Body_SetTransform( b2BodyId bodyId, b2Pos position, b2Rot rotation )
 			h_bufferMove( w, s->proxyKey );
 		}
 	}
+}
+
+/* ---- destruction (body.c:346-430, shape.c:322-437, joint.c:721-840, shape.c:582-640) ---- */
+
+static void h_updateBodyMassData( h_world* w, h_body* body );
+
+/* broad_phase.c:80-126: the proxy leaves the move buffer (swap-removal, as the reference
+   does) and its tree */
+static void h_destroyProxy( h_world* w, h_shape* s )
+{
+	if ( s->proxyKey == B2_NULL_INDEX ) return;
+	int type = H_PROXY_TYPE( s->proxyKey ), id = H_PROXY_ID( s->proxyKey );
+	if ( h_bitGet( w->movedProxies + type, id ) )
+	{
+		h_bitClear( w->movedProxies + type, id );
+		for ( int i = 0; i < w->moveArray.count; ++i )
+			if ( w->moveArray.data[i] == s->proxyKey )
+			{
+				h_removeSwap( w->moveArray, i );
+				break;
+			}
+	}
+	h_treeDestroyProxy( w->trees + type, id );
+	s->proxyKey = B2_NULL_INDEX;
+}
+
+/* sensor.c:388-420: a destroyed sensor ends its overlaps; the last sensor takes its slot */
+static void h_destroySensor( h_world* w, h_shape* s )
+{
+	h_sensor* sensor = w->sensors.data + s->sensorIndex;
+	for ( int i = 0; i < sensor->overlaps2.count; ++i )
+	{
+		b2SensorEndTouchEvent ev = { { s->id + 1, w->worldId, s->generation },
+									 { sensor->overlaps2.data[i].shapeId + 1, w->worldId, sensor->overlaps2.data[i].generation } };
+		h_push( w->sensorEndEvents[w->endEventArrayIndex], ev );
+	}
+	h_free( sensor->overlaps1 );
+	h_free( sensor->overlaps2 );
+	h_free( sensor->hits );
+	int slot = s->sensorIndex;
+	int moved = h_removeSwap( w->sensors, slot );
+	if ( moved != B2_NULL_INDEX ) w->shapes.data[w->sensors.data[slot].shapeId].sensorIndex = slot;
+	s->sensorIndex = B2_NULL_INDEX;
+}
+
+/* shape.c:322-410 */
+static void h_destroyShapeInternal( h_world* w, h_shape* s, h_body* body )
+{
+	int shapeId = s->id;
+	if ( s->prevShapeId != B2_NULL_INDEX ) w->shapes.data[s->prevShapeId].nextShapeId = s->nextShapeId;
+	if ( s->nextShapeId != B2_NULL_INDEX ) w->shapes.data[s->nextShapeId].prevShapeId = s->prevShapeId;
+	if ( shapeId == body->headShapeId ) body->headShapeId = s->nextShapeId;
+	body->shapeCount -= 1;
+	h_destroyProxy( w, s );
+	int key = body->headContactKey;
+	while ( key != B2_NULL_INDEX )
+	{
+		h_contact* c = w->contacts.data + ( key >> 1 );
+		key = c->edges[key & 1].nextKey;
+		if ( c->shapeIdA == shapeId || c->shapeIdB == shapeId ) h_destroyContact( w, c );
+	}
+	if ( s->sensorIndex != B2_NULL_INDEX ) h_destroySensor( w, s );
+	h_freeId( &w->shapeIdPool, shapeId );
+	s->id = B2_NULL_INDEX;
+}
+
+void b2DestroyShape( b2ShapeId shapeId, bool updateBodyMass )
+{
+	h_world* w = h_worlds + shapeId.world0;
+	if ( w->locked ) return;
+	h_shape* s = w->shapes.data + ( shapeId.index1 - 1 );
+	/* a segment of a chain goes with its chain (shape.c:421-426) */
+	if ( s->type == b2_chainSegmentShape && s->chainSegment.chainId != B2_NULL_INDEX ) return;
+	h_markHostChanged( w );
+	h_body* body = w->bodies.data + s->bodyId;
+	h_destroyShapeInternal( w, s, body );
+	if ( updateBodyMass ) h_updateBodyMassData( w, body );
+}
+
+void b2DestroyChain( b2ChainId chainId )
+{
+	h_world* w = h_worlds + chainId.world0;
+	if ( w->locked ) return;
+	h_markHostChanged( w );
+	h_chain* chain = w->chains.data + ( chainId.index1 - 1 );
+	h_body* body = w->bodies.data + chain->bodyId;
+	int* link = &body->headChainId;
+	while ( *link != B2_NULL_INDEX && *link != chain->id ) link = &w->chains.data[*link].nextChainId;
+	if ( *link == B2_NULL_INDEX ) return;
+	*link = chain->nextChainId;
+	for ( int i = 0; i < chain->count; ++i ) h_destroyShapeInternal( w, w->shapes.data + chain->shapeIndices[i], body );
+	free( chain->shapeIndices );
+	chain->shapeIndices = NULL;
+	h_freeId( &w->chainIdPool, chain->id );
+	chain->id = B2_NULL_INDEX;
+}
+
+/* joint.c:721-821 */
+static void h_destroyJointInternal( h_world* w, h_joint* j )
+{
+	int jointId = j->jointId;
+	h_body* bodies[2];
+	for ( int e = 0; e < 2; ++e )
+	{
+		h_jointEdge* edge = j->edges + e;
+		h_body* body = w->bodies.data + edge->bodyId;
+		bodies[e] = body;
+		if ( edge->prevKey != B2_NULL_INDEX ) w->joints.data[edge->prevKey >> 1].edges[edge->prevKey & 1].nextKey = edge->nextKey;
+		if ( edge->nextKey != B2_NULL_INDEX ) w->joints.data[edge->nextKey >> 1].edges[edge->nextKey & 1].prevKey = edge->prevKey;
+		if ( body->headJointKey == ( ( jointId << 1 ) | e ) ) body->headJointKey = edge->nextKey;
+		body->jointCount -= 1;
+	}
+	if ( j->islandId != B2_NULL_INDEX ) h_unlinkJoint( w, j );
+	if ( j->setIndex == H_AWAKE_SET )
+	{
+		h_removeJointFromGraph( w, j->edges[0].bodyId, j->edges[1].bodyId, j->colorIndex, j->localIndex );
+	}
+	else
+	{
+		h_intArray* list = j->setIndex == H_STATIC_SET ? &w->staticJointIds : &w->sets.data[j->setIndex].jointIds;
+		int localIndex = j->localIndex;
+		int moved = h_removeSwap( *list, localIndex );
+		if ( moved != B2_NULL_INDEX ) w->joints.data[list->data[localIndex]].localIndex = localIndex;
+		if ( j->setIndex == H_STATIC_SET ) w->staticJointCount -= 1;
+	}
+	j->setIndex = B2_NULL_INDEX;
+	j->localIndex = B2_NULL_INDEX;
+	j->colorIndex = B2_NULL_INDEX;
+	j->jointId = B2_NULL_INDEX;
+	h_freeId( &w->jointIdPool, jointId );
+	w->jointsDirty = 1;
+	h_wakeBody( w, bodies[0] );
+	h_wakeBody( w, bodies[1] );
+}
+
+void b2DestroyJoint( b2JointId jointId )
+{
+	h_world* w = h_worlds + jointId.world0;
+	if ( w->locked ) return;
+	h_markHostChanged( w );
+	h_destroyJointInternal( w, w->joints.data + ( jointId.index1 - 1 ) );
+}
+
+/* body.c:346-430 */
+void b2DestroyBody( b2BodyId bodyId )
+{
+	h_world* w = h_worlds + bodyId.world0;
+	if ( w->locked ) return;
+	h_markHostChanged( w );
+	h_body* body = h_getBody( bodyId );
+	int key = body->headJointKey;
+	while ( key != B2_NULL_INDEX )
+	{
+		h_joint* j = w->joints.data + ( key >> 1 );
+		key = j->edges[key & 1].nextKey;
+		h_destroyJointInternal( w, j );
+	}
+	key = body->headContactKey;
+	while ( key != B2_NULL_INDEX )
+	{
+		h_contact* c = w->contacts.data + ( key >> 1 );
+		key = c->edges[key & 1].nextKey;
+		h_destroyContact( w, c );
+	}
+	for ( int sid = body->headShapeId; sid != B2_NULL_INDEX; )
+	{
+		h_shape* s = w->shapes.data + sid;
+		if ( s->sensorIndex != B2_NULL_INDEX ) h_destroySensor( w, s );
+		h_destroyProxy( w, s );
+		h_freeId( &w->shapeIdPool, sid );
+		s->id = B2_NULL_INDEX;
+		sid = s->nextShapeId;
+	}
+	for ( int cid = body->headChainId; cid != B2_NULL_INDEX; )
+	{
+		h_chain* chain = w->chains.data + cid;
+		free( chain->shapeIndices );
+		chain->shapeIndices = NULL;
+		h_freeId( &w->chainIdPool, cid );
+		chain->id = B2_NULL_INDEX;
+		cid = chain->nextChainId;
+	}
+	h_removeBodyFromIsland( w, body );
+	int localIndex = body->localIndex;
+	if ( body->setIndex == H_AWAKE_SET || body->setIndex == H_STATIC_SET || body->setIndex >= H_FIRST_SLEEPING_SET )
+	{
+		h_intArray* list = body->setIndex == H_AWAKE_SET	 ? &w->awakeBodyIds
+						   : body->setIndex == H_STATIC_SET ? &w->staticBodyIds
+															 : &w->sets.data[body->setIndex].bodyIds;
+		int moved = h_removeSwap( *list, localIndex );
+		if ( moved != B2_NULL_INDEX ) w->bodies.data[list->data[localIndex]].localIndex = localIndex;
+		if ( body->setIndex == H_STATIC_SET ) w->staticCount -= 1;
+		if ( body->setIndex >= H_FIRST_SLEEPING_SET && list->count == 0 ) h_freeSleepingSet( w, body->setIndex );
+	}
+	h_freeId( &w->bodyIdPool, body->id );
+	body->setIndex = B2_NULL_INDEX;
+	body->localIndex = B2_NULL_INDEX;
+	body->id = B2_NULL_INDEX;
 }
 
 /* ---- forces and impulses (body.c:935-1090) ---- */

@@ -1344,8 +1344,9 @@ B2S_EXPORT void b2s_set_awake( int h, int bodyIndex, int awake )
    kind 0 b2Body_ApplyForce (force (a, b) at the center of mass + (c, d)), 1 ApplyForceToCenter,
    2 ApplyTorque (a), 3 ApplyLinearImpulse (impulse (a, b) at the center + (c, d)),
    4 ApplyLinearImpulseToCenter, 5 ApplyAngularImpulse (a), 6 SetTransform (position (a, b),
-   angle c), 7 SetTargetTransform (position (a, b), angle c, time step d). Forces and
-   impulses wake the body. */
+   angle c), 7 SetTargetTransform (position (a, b), angle c, time step d), 8 b2DestroyBody
+   (the scene then reports the body as zeros), 9 b2DestroyShape of its first shape with a
+   mass update. Forces and impulses wake the body. */
 B2S_EXPORT void b2s_body_action( int h, int kind, int bodyIndex, float a, float b, float c, float d )
 {
 	b2BodyId id = b2s_scenes[h].bodies[bodyIndex];
@@ -1367,6 +1368,19 @@ B2S_EXPORT void b2s_body_action( int h, int kind, int bodyIndex, float a, float 
 			b2Body_SetTargetTransform( id, target, d, true );
 			break;
 		}
+#ifndef B2S_NO_DESTROY
+		case 8:
+			b2DestroyBody( id );
+			b2s_scenes[h].bodies[bodyIndex] = b2_nullBodyId;
+			break;
+		case 9:
+		{
+			b2ShapeId shapes[16];
+			int n = b2Body_GetShapes( id, shapes, 16 );
+			if ( n > 0 ) b2DestroyShape( shapes[0], true );
+			break;
+		}
+#endif
 		default: break;
 	}
 }
@@ -1377,7 +1391,7 @@ B2S_EXPORT void b2s_enable_sleep( int h, int flag ) { b2World_EnableSleeping( b2
 B2S_EXPORT int b2s_awake( int h, int* out )
 {
 	b2sScene* s = b2s_scenes + h;
-	for ( int i = 0; i < s->bodyCount; ++i ) out[i] = b2Body_IsAwake( s->bodies[i] ) ? 1 : 0;
+	for ( int i = 0; i < s->bodyCount; ++i ) out[i] = B2_IS_NON_NULL( s->bodies[i] ) && b2Body_IsAwake( s->bodies[i] ) ? 1 : 0;
 	return b2World_GetAwakeBodyCount( s->worldId );
 }
 
@@ -1435,10 +1449,16 @@ B2S_EXPORT void b2s_get_state( int h, float* out )
 	b2sScene* s = b2s_scenes + h;
 	for ( int i = 0; i < s->bodyCount; ++i )
 	{
+		float* o = out + 7 * i;
+		if ( B2_IS_NULL( s->bodies[i] ) )
+		{
+			/* a body destroyed by a scripted change */
+			memset( o, 0, 7 * sizeof( float ) );
+			continue;
+		}
 		b2Transform xf = b2Body_GetTransform( s->bodies[i] );
 		b2Vec2 v = b2Body_GetLinearVelocity( s->bodies[i] );
 		float w = b2Body_GetAngularVelocity( s->bodies[i] );
-		float* o = out + 7 * i;
 		o[0] = (float)xf.p.x;
 		o[1] = (float)xf.p.y;
 		o[2] = xf.q.c;
@@ -1521,6 +1541,12 @@ B2S_EXPORT uint64_t b2s_state_hash( int h )
 	float buf[7];
 	for ( int i = 0; i < s->bodyCount; ++i )
 	{
+		if ( B2_IS_NULL( s->bodies[i] ) )
+		{
+			memset( buf, 0, sizeof( buf ) );
+			for ( int k = 0; k < 7; ++k ) hash = hash * 1099511628211ull;
+			continue;
+		}
 		b2Transform xf = b2Body_GetTransform( s->bodies[i] );
 		b2Vec2 v = b2Body_GetLinearVelocity( s->bodies[i] );
 		buf[0] = (float)xf.p.x;

@@ -84,7 +84,8 @@ void b2s_destroy( int handle );
 /* a scripted change to scene body `bodyIndex` between steps: 0 b2Body_ApplyForce (force
    (a, b) at the center of mass + (c, d)), 1 ApplyForceToCenter, 2 ApplyTorque (a),
    3 ApplyLinearImpulse, 4 ApplyLinearImpulseToCenter, 5 ApplyAngularImpulse (a),
-   6 SetTransform (position (a, b), angle c), 7 SetTargetTransform (also time step d) */
+   6 SetTransform (position (a, b), angle c), 7 SetTargetTransform (also time step d),
+   8 b2DestroyBody, 9 b2DestroyShape of its first shape */
 void b2s_body_action( int handle, int kind, int bodyIndex, float a, float b, float c, float d );
 void b2s_step( int handle, float timeStep, int subStepCount, int count );
 /* step `count` scenes `steps` times, one b2World_StepBatch call (up to `threads` host

@@ -675,6 +675,8 @@ B2G_API uint64_t b2World_GetStateHash( b2WorldId worldId );
 
 /* ---- API: bodies (box2d.h:355-550) ---- */
 B2G_API b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def );
+/* body.c:346 (box2d.h:359): its joints, contacts, shapes and chains go with it */
+B2G_API void b2DestroyBody( b2BodyId bodyId );
 B2G_API bool b2Body_IsValid( b2BodyId id );
 B2G_API b2BodyType b2Body_GetType( b2BodyId bodyId );
 B2G_API b2Pos b2Body_GetPosition( b2BodyId bodyId );
@@ -713,6 +715,7 @@ B2G_API b2ShapeId b2CreateSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, 
 /* chains (shape.c:300-315, :439-640; box2d.h:860-900) */
 B2G_API b2ChainDef b2DefaultChainDef( void );
 B2G_API b2ChainId b2CreateChain( b2BodyId bodyId, const b2ChainDef* def );
+B2G_API void b2DestroyChain( b2ChainId chainId );
 B2G_API bool b2Chain_IsValid( b2ChainId id );
 B2G_API int b2Chain_GetSegmentCount( b2ChainId chainId );
 B2G_API int b2Chain_GetSegments( b2ChainId chainId, b2ShapeId* segmentArray, int capacity );
@@ -722,6 +725,8 @@ B2G_API b2ChainSegment b2Shape_GetChainSegment( b2ShapeId shapeId );
 B2G_API b2ChainId b2Shape_GetParentChain( b2ShapeId shapeId );
 B2G_API b2ShapeId b2CreateCapsuleShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Capsule* capsule );
 B2G_API b2ShapeId b2CreatePolygonShape( b2BodyId bodyId, const b2ShapeDef* def, const b2Polygon* polygon );
+/* shape.c:411 (box2d.h:686) */
+B2G_API void b2DestroyShape( b2ShapeId shapeId, bool updateBodyMass );
 B2G_API void b2Shape_SetFriction( b2ShapeId shapeId, float friction );
 /* sensors (shape.c:1109, :1400-1415, :1780-1825; box2d.h:703-856) */
 B2G_API bool b2Shape_IsSensor( b2ShapeId shapeId );
@@ -754,6 +759,8 @@ B2G_API b2JointId b2CreateMoverJoint( b2WorldId worldId, const b2MoverJointDef* 
 B2G_API b2JointId b2CreateFilterJoint( b2WorldId worldId, const b2FilterJointDef* def );
 B2G_API b2JointId b2CreateMotorJoint( b2WorldId worldId, const b2MotorJointDef* def );
 B2G_API b2JointId b2CreatePogoJoint( b2WorldId worldId, const b2PogoJointDef* def );
+/* joint.c:823 (box2d.h:919) */
+B2G_API void b2DestroyJoint( b2JointId jointId );
 B2G_API b2JointType b2Joint_GetType( b2JointId jointId );
 B2G_API float b2RevoluteJoint_GetAngle( b2JointId jointId );
 

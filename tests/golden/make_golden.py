@@ -67,6 +67,9 @@ SLEEP_SCENES = [
     ("falling_hinges", B.FALLING_HINGES, 0, 0, 0, 0, 0, 300, [1, 100, 274, 300]),
     ("sleep_pyramids_3x8", B.SLEEP_PYRAMIDS, 3, 8, 80, 0, 0, 700, [1, 200, 400, 700]),
     ("sleep_api_pyramids", B.SLEEP_PYRAMIDS, 2, 6, 1000, 0, 0, 330, [1, 56, 131, 201, 330]),
+    # bodies and shapes destroyed between steps, awake and asleep
+    ("destroy_pyramids", B.SLEEP_PYRAMIDS, 2, 6, 1000, 0, 0, 300, [1, 60, 160, 300]),
+    ("destroy_joint_zoo", B.JOINT_ZOO, 4, 0, 0, 3, 0, 200, [1, 50, 100, 200]),
 ]
 # changes applied after the given step (Scene.apply): wake by velocity, put an island to
 # sleep and wake one through b2Body_SetAwake, switch sleeping off and on again
@@ -74,6 +77,10 @@ SCRIPTS = {
     "sleep_api_pyramids": [[40, "velocity", 3, 0.0, 6.0, 0.0], [41, "velocity", 25, 2.0, 0.0, 1.0],
                            [55, "awake", 10, 0], [130, "awake", 30, 1], [200, "sleeping", 0], [260, "sleeping", 1]],
 }
+SCRIPTS["destroy_pyramids"] = [[20, "destroy_body", 3], [40, "destroy_shape", 7], [120, "destroy_body", 12],
+                                [121, "destroy_body", 30], [150, "destroy_shape", 25], [200, "destroy_body", 40]]
+SCRIPTS["destroy_joint_zoo"] = [[30, "destroy_body", 5], [31, "destroy_body", 9], [60, "destroy_body", 14],
+                                 [61, "destroy_shape", 20], [90, "destroy_body", 2]]
 SCRIPTS["body_api_zoo"] = (
     [[5, "force", 3, 50.0, 100.0, 0.1, 0.2], [5, "force_center", 3, -20.0, 0.0], [6, "torque", 4, 30.0],
      [10, "impulse", 5, 2.0, 5.0, 0.1, 0.0], [11, "impulse_center", 6, -3.0, 1.0], [12, "angular_impulse", 7, 2.0],
