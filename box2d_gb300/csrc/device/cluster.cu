@@ -54,6 +54,7 @@ struct d_clusterPlan
 	int ranks;
 	int slotsPerRank; /* bodies per CTA: position p lives in CTA p / slotsPerRank */
 	int laneCap;	  /* contact lanes one CTA's shared memory holds */
+	int jointSlotCap; /* joints whose accumulated impulses (s[]) a CTA keeps in shared memory */
 	int colorCap[B2_GRAPH_COLOR_COUNT]; /* lanes of an active color a CTA takes in one pass */
 	int jointCap[B2_GRAPH_COLOR_COUNT]; /* joints of an active color a CTA takes in one pass */
 	int* assignedJoints;				/* color c, CTA r: joints at [jointOffset(c) * ranks + r * count(c)] */
@@ -215,6 +216,30 @@ static __device__ __forceinline__ void d_clusterJointStage( const b2gStepParams&
 	for ( int i = 0; i < 4; ++i ) dst[i] = s4[i];
 }
 
+/* The same stage with the joint's accumulated impulses and solver constants (s[]) kept in
+   the CTA's shared memory for the whole step: the constant part of the record comes from
+   global memory, s[] from and back to `slot`. With no global store in the phase, the
+   cluster barrier that ends it waits for no store to reach L2. */
+static __device__ __forceinline__ void d_clusterJointStageShared( const b2gStepParams& P, const b2gJoint* J, float4* slot,
+																   d_clusterBodies& bodies, int stage )
+{
+	union
+	{
+		b2gJoint j;
+		float4 w[sizeof( b2gJoint ) / 16];
+	} copy;
+	const float4* src = (const float4*)J;
+	const int sBegin = (int)( offsetof( b2gJoint, s ) / 16 );
+#pragma unroll
+	for ( int i = 0; i < (int)( sizeof( b2gJoint ) / 16 ); ++i )
+		if ( i < sBegin || i >= sBegin + 4 ) copy.w[i] = __ldcg( src + i );
+#pragma unroll
+	for ( int i = 0; i < 4; ++i ) copy.w[sBegin + i] = slot[i];
+	d_jointStageT( P, &copy.j, bodies, stage );
+#pragma unroll
+	for ( int i = 0; i < 4; ++i ) slot[i] = copy.w[sBegin + i];
+}
+
 __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies jb, d_clusterPlan plan )
 {
 	cg::cluster_group cluster = cg::this_cluster();
@@ -223,9 +248,11 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 	extern __shared__ float4 s_mem[];
 	float4* sv = s_mem;
 	float4* sd = sv + plan.slotsPerRank;
-	b2gContactLane* lanes = (b2gContactLane*)( sd + plan.slotsPerRank );
+	float4* jimp = sd + plan.slotsPerRank; /* 4 float4 (s[]) per joint slot */
+	b2gContactLane* lanes = (b2gContactLane*)( jimp + 4 * plan.jointSlotCap );
 	__shared__ int s_cCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_jBegin[B2_GRAPH_COLOR_COUNT], s_jCount[B2_GRAPH_COLOR_COUNT];
+	__shared__ int s_jSlot[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_laneOffset[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_restitution;
 	const int tid = threadIdx.x, nt = blockDim.x;
@@ -240,7 +267,7 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 	   the color starts */
 	if ( tid == 0 )
 	{
-		int offset = 0;
+		int offset = 0, jslot = 0;
 		for ( int k = 0; k < plan.colorCount; ++k )
 		{
 			int color = plan.colors[k];
@@ -255,6 +282,8 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 			s_cCount[k] = nc;
 			s_jBegin[k] = jbegin * ranks + rank * ( plan.jointOffsets[color + 1] - jbegin );
 			s_jCount[k] = nj;
+			s_jSlot[k] = jslot;
+			jslot += nj;
 			s_laneOffset[k] = offset;
 			offset += nc;
 		}
@@ -283,6 +312,13 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 			int pb = J->indexB >= 0 ? ( plan.positionOf ? plan.positionOf[J->indexB] : J->indexB ) : -1;
 			J->indexA = pa >= 0 ? d_clusterKey( plan, pa ) : -1;
 			J->indexB = pb >= 0 ? d_clusterKey( plan, pb ) : -1;
+			int slot = s_jSlot[k] + t;
+			if ( slot < plan.jointSlotCap )
+			{
+				const float4* s4 = (const float4*)J->s;
+#pragma unroll
+				for ( int i = 0; i < 4; ++i ) jimp[4 * slot + i] = s4[i];
+			}
 		}
 		const int begin = a.colorOffsets[color];
 		const int* mine = plan.assigned + (long long)begin * ranks + (long long)rank * ( a.colorOffsets[color + 1] - begin );
@@ -329,7 +365,10 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 				{
 					if ( t < nj )
 					{
-						d_clusterJointStage( P, a.joints + plan.assignedJoints[s_jBegin[k] + t], bodies, stage );
+						int slot = s_jSlot[k] + t;
+						b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k] + t];
+						if ( slot < plan.jointSlotCap ) d_clusterJointStageShared( P, J, jimp + 4 * slot, bodies, stage );
+						else d_clusterJointStage( P, J, bodies, stage );
 					}
 					else
 					{
@@ -362,6 +401,13 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 		for ( int t = tid; t < s_jCount[k]; t += nt )
 		{
 			b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k] + t];
+			int slot = s_jSlot[k] + t;
+			if ( slot < plan.jointSlotCap )
+			{
+				float4* d4 = (float4*)J->s;
+#pragma unroll
+				for ( int i = 0; i < 4; ++i ) d4[i] = jimp[4 * slot + i];
+			}
 			int pa = J->indexA >= 0 ? d_clusterPosition( plan, J->indexA ) : -1;
 			int pb = J->indexB >= 0 ? d_clusterPosition( plan, J->indexB ) : -1;
 			J->indexA = pa >= 0 ? ( plan.bodyList ? plan.bodyList[pa] : pa ) : -1;
@@ -431,9 +477,27 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 		lanesTotal += counts[k];
 	}
 	int slotsPerRank = ( bodyCount + ranks - 1 ) / ranks;
-	long long laneBytes = (long long)B2G_CLUSTER_SMEM_MAX - (long long)slotsPerRank * 2 * sizeof( float4 );
-	if ( slotsPerRank > 0xffff || laneBytes <= 0 ) return -1;
-	int laneCap = (int)( laneBytes / sizeof( b2gContactLane ) );
+	long long bodyBytes = (long long)slotsPerRank * 2 * sizeof( float4 );
+	if ( slotsPerRank > 0xffff || bodyBytes >= (long long)B2G_CLUSTER_SMEM_MAX ) return -1;
+	/* joint impulses in shared memory: a CTA's even share of the joints with a quarter more,
+	   as long as the contact lanes still fit; joints past the slots keep theirs in global */
+	long long jointsTotal = 0;
+	for ( int k = 0; k < activeColorCount; ++k )
+	{
+		int color = activeColors[k];
+		jointsTotal += useLists ? b->hSummary->bigJointCount[color] : jointOffsets[color + 1] - jointOffsets[color];
+	}
+	const long long jointSlotBytes = 4 * (long long)sizeof( float4 );
+	long long evenJoints = ( jointsTotal + ranks - 1 ) / ranks;
+	int jointSlotCap = jointsTotal > 0 ? (int)( evenJoints + evenJoints / 4 + 32 ) : 0;
+	int laneCap = 0;
+	for ( ;; )
+	{
+		long long laneBytes = (long long)B2G_CLUSTER_SMEM_MAX - bodyBytes - (long long)jointSlotCap * jointSlotBytes;
+		laneCap = laneBytes > 0 ? (int)( laneBytes / sizeof( b2gContactLane ) ) : 0;
+		if ( lanesTotal <= (long long)laneCap * ranks || jointSlotCap == 0 ) break;
+		jointSlotCap = jointSlotCap > 64 ? jointSlotCap / 2 : 0;
+	}
 	if ( lanesTotal > (long long)laneCap * ranks ) return -1;
 
 	/* assignment lists: 16 entries per colored slot and colored joint */
@@ -485,6 +549,7 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	plan.ranks = ranks;
 	plan.slotsPerRank = slotsPerRank;
 	plan.laneCap = laneCap;
+	plan.jointSlotCap = jointSlotCap;
 	plan.assigned = b->clusterAssigned;
 	plan.counts = b->clusterCounts;
 	plan.status = status;
