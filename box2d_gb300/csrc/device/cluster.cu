@@ -193,51 +193,41 @@ static __device__ void d_clusterAssignJoint( const d_clusterPlan& plan, const b2
 	plan.assignedJoints[(long long)begin * plan.ranks + (long long)r * colorSize + idx] = index;
 }
 
-/* A joint stage on a copy of the record: the record is read in one burst of 16-byte loads
-   and only the accumulated impulses (s[], the only fields a stage writes) are stored back.
-   Working on global memory directly would turn every body store, which may alias the record
-   for the compiler, into another round trip to L2 before the next field load. */
-static __device__ __forceinline__ void d_clusterJointStage( const b2gStepParams& P, b2gJoint* J, d_clusterBodies& bodies,
-															 int stage )
+/* A joint record held in registers between its load and its stage. */
+union d_jointCopy
 {
-	static_assert( sizeof( b2gJoint ) % 16 == 0 && offsetof( b2gJoint, s ) % 16 == 0, "joint record layout" );
-	union
-	{
-		b2gJoint j;
-		float4 w[sizeof( b2gJoint ) / 16];
-	} copy;
-	const float4* src = (const float4*)J;
-#pragma unroll
-	for ( int i = 0; i < (int)( sizeof( b2gJoint ) / 16 ); ++i ) copy.w[i] = __ldcg( src + i );
-	d_jointStageT( P, &copy.j, bodies, stage );
-	float4* dst = (float4*)J->s;
-	const float4* s4 = (const float4*)copy.j.s;
-#pragma unroll
-	for ( int i = 0; i < 4; ++i ) dst[i] = s4[i];
-}
+	b2gJoint j;
+	float4 w[sizeof( b2gJoint ) / 16];
+};
 
-/* The same stage with the joint's accumulated impulses and solver constants (s[]) kept in
-   the CTA's shared memory for the whole step: the constant part of the record comes from
-   global memory, s[] from and back to `slot`. With no global store in the phase, the
-   cluster barrier that ends it waits for no store to reach L2. */
-static __device__ __forceinline__ void d_clusterJointStageShared( const b2gStepParams& P, const b2gJoint* J, float4* slot,
-																   d_clusterBodies& bodies, int stage )
+/* Load a joint for a stage: the constant part of the record from global memory, the
+   accumulated impulses and solver constants (s[]) from the CTA's shared-memory slot when it
+   has one, else from the record. */
+static __device__ __forceinline__ void d_clusterJointLoad( const b2gJoint* J, const float4* slot, d_jointCopy& copy )
 {
-	union
-	{
-		b2gJoint j;
-		float4 w[sizeof( b2gJoint ) / 16];
-	} copy;
 	const float4* src = (const float4*)J;
 	const int sBegin = (int)( offsetof( b2gJoint, s ) / 16 );
 #pragma unroll
 	for ( int i = 0; i < (int)( sizeof( b2gJoint ) / 16 ); ++i )
-		if ( i < sBegin || i >= sBegin + 4 ) copy.w[i] = __ldcg( src + i );
+		if ( slot == nullptr || i < sBegin || i >= sBegin + 4 ) copy.w[i] = __ldcg( src + i );
+	if ( slot != nullptr )
+	{
 #pragma unroll
-	for ( int i = 0; i < 4; ++i ) copy.w[sBegin + i] = slot[i];
+		for ( int i = 0; i < 4; ++i ) copy.w[sBegin + i] = slot[i];
+	}
+}
+
+/* Run a stage on a loaded joint and keep its s[]: in the shared-memory slot (no global store
+   in the phase, so the cluster barrier that ends it waits for no store to reach L2), or
+   back in the record. */
+static __device__ __forceinline__ void d_clusterJointRun( const b2gStepParams& P, b2gJoint* J, float4* slot, d_jointCopy& copy,
+														  d_clusterBodies& bodies, int stage )
+{
+	const int sBegin = (int)( offsetof( b2gJoint, s ) / 16 );
 	d_jointStageT( P, &copy.j, bodies, stage );
+	float4* dst = slot != nullptr ? slot : (float4*)J->s;
 #pragma unroll
-	for ( int i = 0; i < 4; ++i ) slot[i] = copy.w[sBegin + i];
+	for ( int i = 0; i < 4; ++i ) dst[i] = copy.w[sBegin + i];
 }
 
 __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies jb, d_clusterPlan plan )
@@ -358,6 +348,11 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 				for ( int s = tid; s < localCount; s += nt ) d_integratePositionsState( P, sv, sd, s );
 				cluster.sync();
 			}
+			/* a thread's first joint of the next color is loaded while the cluster barrier
+			   ending the current color completes: arrive, load, wait. Safe because a color's
+			   records change only in that color's phases, all before earlier barriers. */
+			d_jointCopy next;
+			bool haveNext = false;
 			for ( int k = 0; k < plan.colorCount; ++k )
 			{
 				int nj = s_jCount[k], n = nj + s_cCount[k];
@@ -367,15 +362,24 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 					{
 						int slot = s_jSlot[k] + t;
 						b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k] + t];
-						if ( slot < plan.jointSlotCap ) d_clusterJointStageShared( P, J, jimp + 4 * slot, bodies, stage );
-						else d_clusterJointStage( P, J, bodies, stage );
+						float4* sp = slot < plan.jointSlotCap ? jimp + 4 * slot : nullptr;
+						if ( t != tid || haveNext == false ) d_clusterJointLoad( J, sp, next );
+						d_clusterJointRun( P, J, sp, next, bodies, stage );
 					}
 					else
 					{
 						d_laneStageT( P, lanes + s_laneOffset[k] + ( t - nj ), bodies, stage );
 					}
 				}
-				cluster.sync();
+				auto token = cluster.barrier_arrive();
+				haveNext = k + 1 < plan.colorCount && tid < s_jCount[k + 1];
+				if ( haveNext )
+				{
+					int slot = s_jSlot[k + 1] + tid;
+					const b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k + 1] + tid];
+					d_clusterJointLoad( J, slot < plan.jointSlotCap ? jimp + 4 * slot : nullptr, next );
+				}
+				cluster.barrier_wait( std::move( token ) );
 			}
 		}
 	}
