@@ -172,6 +172,7 @@ typedef struct b2gStepCounters
 	int pairOverflow;
 	int fastBodyCount;
 	int status;			/* nonzero: a device check failed (see B2G_STATUS_*) */
+	int sensorHitCount; /* sensor shapes hit by continuous sweeps this step */
 	int continuousSweeps; /* fast non-bullet bodies swept against static shapes */
 	int continuousHits;	  /* sweeps that moved the body back to its time of impact */
 	int pad;
@@ -326,6 +327,9 @@ void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const 
    the returned array is valid until the next call. */
 int b2gDev_SensorOverlaps( b2gDeviceWorld* dw, const int* sensorShapeIds, int sensorCount, int shapeCount,
 						   const int** outPairs, int* outCount );
+/* solver.c:321-335, :539-547: the (sensor shape, visitor shape) pairs continuous sweeps of
+   the last step hit before their solid time of impact. Waits for the device. */
+int b2gDev_SensorHits( b2gDeviceWorld* dw, const int** outPairs, int* outCount );
 /* solver.c:1917-1989: sweep the fast bullet bodies (awake slots) against the static,
    kinematic and dynamic trees as last uploaded; per bullet shape a record (shape id,
    enlarged) and its fat box. Waits for the device; results valid until the next call. */

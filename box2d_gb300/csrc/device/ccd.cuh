@@ -590,6 +590,20 @@ struct d_ccdWorld
 	const uint32_t* bodyFlags;
 	const int* partnerOffsets; /* per body: joint partners that must not collide (NULL: none) */
 	const int* partnerList;
+	/* sensors hit by the sweeps: (sensor shape, visitor shape), counted in *sensorHitCount */
+	int2* sensorHits;
+	int sensorHitCap;
+	int* sensorHitCount;
+};
+
+#define D_MAX_SENSOR_HITS 8
+
+/* solver.c:164-177: the sensors one fast body's sweep hits, with their fractions */
+struct d_sensorHits
+{
+	int sensor[D_MAX_SENSOR_HITS], visitor[D_MAX_SENSOR_HITS];
+	float fraction[D_MAX_SENSOR_HITS];
+	int count;
 };
 
 /* shape.c b2ShouldShapesCollide */
@@ -622,12 +636,14 @@ struct d_fastShape
    fraction (unchanged when there is no hit) */
 static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId, int fastShapeId, const b2gShape* fastShape,
 											   const d_sweep& fastSweep, b2Vec2 base, float fraction, bool* hit,
-											   const d_fastShape& fast )
+											   const d_fastShape& fast, d_sensorHits* hits )
 {
 	if ( shapeId == fastShapeId ) return fraction;
 	const b2gShape* shape = cw.shapes + shapeId;
 	if ( shape->bodyId == fastShape->bodyId ) return fraction;
-	if ( shape->isSensor ) return fraction;
+	/* a sensor is swept only for its events, when both shapes want them */
+	bool isSensor = shape->isSensor != 0;
+	if ( isSensor && ( shape->enableSensorEvents == 0 || fastShape->enableSensorEvents == 0 ) ) return fraction;
 	if ( d_shouldShapesCollide( fastShape, shape ) == false ) return fraction;
 	int bodyId = shape->bodyId;
 	if ( cw.bodyFlags[bodyId] & B2G_IS_BULLET ) return fraction;
@@ -659,6 +675,19 @@ static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId
 	b2Rot q = { x.z, x.w };
 	d_sweep sweepA = d_relativeSweep( d_v( c.x, c.y ), q, d_v( c.x, c.y ), q, d_v( lc.x, lc.y ), base );
 	float f = d_timeOfImpact( &proxyA, &sweepA, &proxyB, &fastSweep, fraction );
+	if ( isSensor )
+	{
+		/* solver.c:319-335: a sensor hit no later than the solid hit so far; it never
+		   moves the body */
+		if ( f <= fraction && hits->count < D_MAX_SENSOR_HITS )
+		{
+			hits->sensor[hits->count] = shapeId;
+			hits->visitor[hits->count] = fastShapeId;
+			hits->fraction[hits->count] = f;
+			hits->count += 1;
+		}
+		return fraction;
+	}
 	if ( 0.0f < f && f < fraction )
 	{
 		*hit = true;
@@ -684,7 +713,7 @@ static __device__ float d_continuousCandidate( const d_ccdWorld& cw, int shapeId
    overlapping leaves in the reference's order (children pushed child1 then child2) */
 static __device__ float d_continuousQuery( const d_ccdWorld& cw, const b2gTreeNode* tree, int root, float4 box, int fastShapeId,
 										   const b2gShape* fastShape, const d_sweep& fastSweep, b2Vec2 base, float fraction,
-										   bool* hit, bool* overflow, const d_fastShape& fast )
+										   bool* hit, bool* overflow, const d_fastShape& fast, d_sensorHits* hits )
 {
 	if ( tree == nullptr || root < 0 ) return fraction;
 	int2 stack[D_CCD_STACK];
@@ -699,7 +728,7 @@ static __device__ float d_continuousQuery( const d_ccdWorld& cw, const b2gTreeNo
 		int2 e = stack[--sp];
 		if ( e.x < 0 )
 		{
-			fraction = d_continuousCandidate( cw, e.y, fastShapeId, fastShape, fastSweep, base, fraction, hit, fast );
+			fraction = d_continuousCandidate( cw, e.y, fastShapeId, fastShape, fastSweep, base, fraction, hit, fast, hits );
 			continue;
 		}
 		const b2gTreeNode c1 = tree[e.x];

@@ -441,6 +441,8 @@ static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, 
 	xf2.p = d_sub( sweep.c2, d_rotate( sweep.q2, sweep.localCenter ) );
 	float fraction = 1.0f;
 	bool hit = false, overflow = false;
+	d_sensorHits sensorHits;
+	sensorHits.count = 0;
 	int start = a.shapeStart[bodyId], count = a.shapeCount[bodyId];
 	for ( int k = 0; k < count; ++k )
 	{
@@ -457,14 +459,22 @@ static __device__ __noinline__ bool d_solveContinuous( const d_finalizeArgs& a, 
 		fast.centroid2 = d_transformPoint( xf2, fastShape->ccdCentroid );
 		fast.coreDistance = D_CORE_FRACTION * a.minExtent[bodyId];
 		fraction = d_continuousQuery( a.ccd, a.ccd.staticTree, a.ccd.staticRoot, swept, shapeId, fastShape, sweep, base, fraction,
-									  &hit, &overflow, fast );
+									  &hit, &overflow, fast, &sensorHits );
 		if ( isBullet )
 		{
 			fraction = d_continuousQuery( a.ccd, a.ccd.kinematicTree, a.ccd.kinematicRoot, swept, shapeId, fastShape, sweep, base,
-										  fraction, &hit, &overflow, fast );
+										  fraction, &hit, &overflow, fast, &sensorHits );
 			fraction = d_continuousQuery( a.ccd, a.ccd.dynamicTree, a.ccd.dynamicRoot, swept, shapeId, fastShape, sweep, base,
-										  fraction, &hit, &overflow, fast );
+										  fraction, &hit, &overflow, fast, &sensorHits );
 		}
+	}
+	/* solver.c:539-547: the sensor hits before the solid time of impact */
+	for ( int i = 0; i < sensorHits.count; ++i )
+	{
+		if ( sensorHits.fraction[i] >= fraction || a.ccd.sensorHits == nullptr ) continue;
+		int k = atomicAdd( a.ccd.sensorHitCount, 1 );
+		if ( k < a.ccd.sensorHitCap ) a.ccd.sensorHits[k] = make_int2( sensorHits.sensor[i], sensorHits.visitor[i] );
+		else atomicOr( &a.counters->status, B2G_STATUS_CAPACITY );
 	}
 	atomicAdd( &a.counters->continuousSweeps, 1 );
 	if ( overflow ) atomicOr( &a.counters->status, B2G_STATUS_CAPACITY );

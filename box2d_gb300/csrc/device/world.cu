@@ -212,6 +212,11 @@ struct b2gDeviceWorld
 	int hBulletRecsCap;
 	float4* hBulletBoxes;
 	int hBulletBoxesCap;
+	/* sensor hits of the continuous sweeps, (sensor shape, visitor shape) */
+	int2* sensorHits;
+	int sensorHitsCap;
+	int2* hSensorHits;
+	int hSensorHitsCap;
 	/* sensor overlap pass: sensor shape ids in, (sensor, shape) pairs out */
 	int* sensorIds;
 	int sensorIdsCap;
@@ -1043,7 +1048,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->moveStage, dw->pairPacked, dw->pairOffsets, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
 					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList,
 					  dw->sleepTime, dw->islandLocal, dw->islandInfo, dw->islandBits, dw->sensorIds, dw->sensorPairs,
-					  dw->sensorCount, dw->bulletSims, dw->bulletRecs, dw->bulletBoxes, dw->bulletCount };
+					  dw->sensorCount, dw->bulletSims, dw->bulletRecs, dw->bulletBoxes, dw->bulletCount, dw->sensorHits };
 	b2gDev_CompFree( &dw->comp );
 	for ( size_t i = 0; i < sizeof( dptrs ) / sizeof( dptrs[0] ); ++i )
 		if ( dptrs[i] ) cudaFree( dptrs[i] );
@@ -1052,7 +1057,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	void* hptrs[] = { dw->hCounters, dw->hChanges,	   dw->hRecs,	   dw->hBoxes,	   dw->hPairs,	  dw->hPairCounts,
 					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw, dw->hSortKeys,
 					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV, dw->hSleepTime, dw->hIslandBits,
-					  dw->hSensorPairs, dw->hBulletRecs, dw->hBulletBoxes };
+					  dw->hSensorPairs, dw->hBulletRecs, dw->hBulletBoxes, dw->hSensorHits };
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
 		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
 	free( dw->hSortTmp );
@@ -2173,6 +2178,9 @@ static void finalizeArgsFor( b2gDeviceWorld* dw, const b2gStepParams* p, int awa
 	f->ccd.bodyFlags = dw->bodyFlags;
 	f->ccd.partnerOffsets = dw->partnerCount > 0 ? dw->partnerOffsets : NULL;
 	f->ccd.partnerList = dw->partnerCount > 0 ? dw->partnerList : NULL;
+	f->ccd.sensorHits = dw->sensorHits;
+	f->ccd.sensorHitCap = dw->sensorHitsCap;
+	f->ccd.sensorHitCount = &dw->counters->sensorHitCount;
 }
 
 /* solver.c:1917-1928 b2BulletBodyTask: each fast bullet body swept against the static,
@@ -2271,6 +2279,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	int shapeTotal = dw->shapeCountTotal;
 	CK2( grow( dw, (void**)&dw->enlargedRecs, &dw->enlargedCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( int ) ) );
 	CK2( grow( dw, (void**)&dw->enlargedBoxes, &dw->enlargedBoxesCap, shapeTotal > 0 ? shapeTotal : 1, sizeof( float4 ) ) );
+	CK2( grow( dw, (void**)&dw->sensorHits, &dw->sensorHitsCap, 1024, sizeof( int2 ) ) );
 	d_finalizeArgs f;
 	finalizeArgsFor( dw, p, awakeCount, shapeTotal, &f );
 	f.toi = dw->tapeToi;
@@ -2800,6 +2809,26 @@ __global__ void k_sensorOverlaps( const int* __restrict__ sensorIds, int sensorC
 			if ( k < outCap ) out[k] = make_int2( sensorIndex, shapeId );
 		}
 	}
+}
+
+extern "C" int b2gDev_SensorHits( b2gDeviceWorld* dw, const int** outPairs, int* outCount )
+{
+	*outPairs = NULL;
+	*outCount = 0;
+	if ( dw->sensorHits == NULL ) return 0;
+	int count = 0;
+	CK( cudaMemcpyAsync( &count, &dw->counters->sensorHitCount, sizeof( int ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	if ( count > dw->sensorHitsCap ) count = dw->sensorHitsCap;
+	CK2( growHost( (void**)&dw->hSensorHits, &dw->hSensorHitsCap, count > 0 ? count : 1, sizeof( int2 ) ) );
+	if ( count > 0 )
+	{
+		CK( cudaMemcpy( dw->hSensorHits, dw->sensorHits, (size_t)count * sizeof( int2 ), cudaMemcpyDeviceToHost ) );
+		dw->d2hBytes += (long long)count * (long long)sizeof( int2 );
+	}
+	*outPairs = (const int*)dw->hSensorHits;
+	*outCount = count;
+	return 0;
 }
 
 extern "C" int b2gDev_SensorOverlaps( b2gDeviceWorld* dw, const int* sensorShapeIds, int sensorCount, int shapeCount,

@@ -59,6 +59,21 @@ void h_overlapSensors( h_world* w, int endIndex )
 	int n = w->sensors.count;
 	w->sensorStep = w->stepIndex;
 	if ( n == 0 ) return;
+	/* solver.c:1991-2017: the sweeps' sensor hits join the sensors' hit lists */
+	if ( w->devReady )
+	{
+		const int* hits = NULL;
+		int hitCount = 0;
+		int rc = b2gDev_SensorHits( w->dev, &hits, &hitCount );
+		if ( rc != 0 ) h_fail( w, "sensor hits", rc );
+		for ( int k = 0; k < hitCount; ++k )
+		{
+			const h_shape* sensorShape = w->shapes.data + hits[2 * k];
+			if ( sensorShape->sensorIndex == B2_NULL_INDEX ) continue;
+			h_visitor v = { hits[2 * k + 1], w->shapes.data[hits[2 * k + 1]].generation };
+			h_push( w->sensors.data[sensorShape->sensorIndex].hits, v );
+		}
+	}
 	int* query = malloc( (size_t)n * sizeof( int ) );
 	unsigned char* changed = calloc( (size_t)n, 1 );
 	/* sensor.c:145-175: swap the overlap lists, start the new one with the sweep hits */

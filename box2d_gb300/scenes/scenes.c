@@ -939,8 +939,8 @@ static void b2sOverflowScene( b2sScene* s, int count, b2sRng* rng )
 	}
 }
 
-/* Sensor scene (sensor.c, shape.c:180-205): static sensor boxes on the floor and a static
-   sensor circle in the air, a kinematic body carrying a sensor capsule across the scene, a
+/* Sensor scene (sensor.c, shape.c:180-205): static sensor boxes on the floor, a thin static
+   sensor gate at 6 m and a static sensor circle in the air, a kinematic body carrying a sensor capsule across the scene, a
    dynamic body whose sensor circle rides on its own solid box (a sensor never sees shapes
    of its own body), a static sensor whose sensor events are off, and `count` falling
    shapes of which two in three report to sensors and every fifth is in a category the
@@ -964,6 +964,11 @@ static void b2sSensorZoo( b2sScene* s, int count, b2sRng* rng )
 	{
 		b2Polygon zone = b2MakeOffsetBox( 2.0f, 1.0f, ( b2Vec2 ){ -12.0f + 12.0f * i, 1.0f }, b2MakeRot( 0.0f ) );
 		b2CreatePolygonShape( ground, &sensorDef, &zone );
+	}
+	{
+		/* a thin gate the falling shapes cross within one step: seen by continuous sweeps */
+		b2Polygon gate = b2MakeOffsetBox( 18.0f, 0.02f, ( b2Vec2 ){ 0.0f, 6.0f }, b2MakeRot( 0.0f ) );
+		b2CreatePolygonShape( ground, &sensorDef, &gate );
 	}
 	{
 		b2Circle zone = { { 5.0f, 4.0f }, 1.5f };

@@ -46,6 +46,9 @@ SCENES = [
     ("body_api_zoo", B.SHAPE_ZOO, 60, 0, 0, 9, 0, 150, [1, 75, 150]),
     # sensors: begin/end overlap events of static, kinematic and dynamic sensor shapes
     ("sensor_zoo_60", B.SENSOR_ZOO, 60, 0, 0, 5, B.NO_CONTINUOUS, 240, [1, 120, 240]),
+    ("sensor_zoo_60_continuous", B.SENSOR_ZOO, 60, 0, 0, 6, 0, 240, [1, 120, 240]),
+    # shapes dropped from high up cross the thin gate within one step: continuous sensor hits
+    ("sensor_gate_120", B.SENSOR_ZOO, 120, 0, 0, 8, 0, 120, [1, 60, 120]),
 ]
 
 # chain shapes (one-sided segments with ghost vertices), with continuous collision on and
