@@ -146,6 +146,7 @@ struct b2gDeviceWorld
 	unsigned int* hIslandBits;
 	int hIslandBitsCap;
 	int pendingIslandWords; /* island bits the solve awaiting its results reads back */
+	int stageStatus;		/* status bits of the step's pair query, reported with the solve's */
 	/* shapes */
 	int shapeCap, shapeCountTotal;
 	b2gShape* shapes;
@@ -251,13 +252,11 @@ struct b2gDeviceWorld
 	int* hPairs;
 	int* hPairCounts;
 	int hPairsCap, hPairCountsCap;
-	int* hSortTmp;
+	int* hSortTmp; /* counting-sort buckets of the enlarged-proxy records (malloc) */
 	int hSortTmpCap;
 	int* hRecsRaw;
 	float* hBoxesRaw;
 	int hRecsRawCap, hBoxesRawCap;
-	void* hSortKeys;
-	int hSortKeysCap;
 	float4* hXf;
 	float2* hCenter;
 	uint32_t* hFlags;
@@ -1055,7 +1054,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	if ( dw->upDev ) cudaFree( dw->upDev );
 	if ( dw->upHost ) cudaFreeHost( dw->upHost );
 	void* hptrs[] = { dw->hCounters, dw->hChanges,	   dw->hRecs,	   dw->hBoxes,	   dw->hPairs,	  dw->hPairCounts,
-					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw, dw->hSortKeys,
+					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw,
 					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV, dw->hSleepTime, dw->hIslandBits,
 					  dw->hSensorPairs, dw->hBulletRecs, dw->hBulletBoxes, dw->hSensorHits };
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
@@ -1975,16 +1974,14 @@ extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int*
 	dw->defer = NULL;
 	for ( int attempt = 0; attempt < 8; ++attempt )
 	{
-		if ( dw->hCounters->status != 0 )
-		{
-			dw->defer = deferred;
-			return (int)cudaErrorIllegalState;
-		}
 		if ( dw->hCounters->pairOverflow <= dw->pairPerMove ) break;
 		while ( dw->pairPerMove < dw->hCounters->pairOverflow ) dw->pairPerMove *= 2;
 		CK2( findPairsIssue( dw, n ) );
 		CK2( drain( dw ) );
 	}
+	/* a query that ran out of traversal stack kept the pairs it found; the status goes out
+	   with the step's */
+	dw->stageStatus |= dw->hCounters->status;
 	int total = dw->hCounters->pairCount;
 	int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
 	if ( total > window )
@@ -2114,19 +2111,6 @@ extern "C" int b2gDev_Collide( b2gDeviceWorld* dw, const b2gStepParams* p, int c
 	CK2( b2gDev_CollideIssue( dw, p, contactIdCapacity ) );
 	CK2( drain( dw ) );
 	return b2gDev_CollideCollect( dw, outChanges, outChangeCount, outRecycled );
-}
-
-struct recKey
-{
-	int simIndex, order;
-};
-
-static int cmpRec( const void* a, const void* b )
-{
-	const recKey* x = (const recKey*)a;
-	const recKey* y = (const recKey*)b;
-	if ( x->simIndex != y->simIndex ) return ( x->simIndex > y->simIndex ) - ( x->simIndex < y->simIndex );
-	return ( x->order > y->order ) - ( x->order < y->order );
 }
 
 /* the solver and finalize of one step, issued (or recorded: one-CTA worlds only); the
@@ -2564,20 +2548,30 @@ extern "C" int b2gDev_SolveCollect( b2gDeviceWorld* dw, const int** outRecs, int
 	dw->recWindow = 2 * n > 64 ? 2 * n : 64;
 	if ( n > 0 )
 	{
+		/* records into ascending awake index, keeping the arrival order of a body's shapes
+		   (one body's records are contiguous): a counting sort over the awake indices */
 		const int* recs = dw->hRecsRaw;
 		const float* boxes = dw->hBoxesRaw;
-		CK2( growHost( (void**)&dw->hSortKeys, &dw->hSortKeysCap, n, sizeof( recKey ) ) );
-		recKey* keys = (recKey*)dw->hSortKeys;
-		for ( int i = 0; i < n; ++i )
+		int top = 0;
+		for ( int i = 0; i < n; ++i ) top = recs[4 * i] > top ? recs[4 * i] : top;
+		if ( top + 2 > dw->hSortTmpCap )
 		{
-			keys[i].simIndex = recs[4 * i];
-			keys[i].order = i;
+			int cap = dw->hSortTmpCap > 0 ? dw->hSortTmpCap : 1024;
+			while ( cap < top + 2 ) cap *= 2;
+			int* grown = (int*)realloc( dw->hSortTmp, (size_t)cap * sizeof( int ) );
+			if ( grown == NULL ) return (int)cudaErrorMemoryAllocation;
+			dw->hSortTmp = grown;
+			dw->hSortTmpCap = cap;
 		}
-		qsort( keys, (size_t)n, sizeof( recKey ), cmpRec );
+		int* start = dw->hSortTmp;
+		memset( start, 0, (size_t)( top + 2 ) * sizeof( int ) );
+		for ( int i = 0; i < n; ++i ) start[recs[4 * i] + 1] += 1;
+		for ( int s = 1; s <= top + 1; ++s ) start[s] += start[s - 1];
 		for ( int i = 0; i < n; ++i )
 		{
-			memcpy( dw->hRecs + 4 * i, recs + 4 * keys[i].order, 4 * sizeof( int ) );
-			memcpy( dw->hBoxes + 4 * i, boxes + 4 * keys[i].order, 4 * sizeof( float ) );
+			int dst = start[recs[4 * i]]++;
+			memcpy( dw->hRecs + 4 * dst, recs + 4 * i, 4 * sizeof( int ) );
+			memcpy( dw->hBoxes + 4 * dst, boxes + 4 * i, 4 * sizeof( float ) );
 		}
 	}
 	dw->defer = deferred;
@@ -2585,7 +2579,8 @@ extern "C" int b2gDev_SolveCollect( b2gDeviceWorld* dw, const int** outRecs, int
 	*outRecs = dw->hRecs;
 	*outBoxes = dw->hBoxes;
 	*outCount = n;
-	*outStatus = dw->hCounters->status;
+	*outStatus = dw->hCounters->status | dw->stageStatus;
+	dw->stageStatus = 0;
 	return 0;
 }
 

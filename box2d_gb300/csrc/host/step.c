@@ -610,6 +610,8 @@ void h_stepFinish( h_world* w )
 			w->continuousHits += sc.continuousHits;
 		}
 		if ( status & B2G_STATUS_NAN ) fprintf( stderr, "box2d_gb300: unstable body state (NaN or infinite velocity)\n" );
+		if ( status & B2G_STATUS_CAPACITY )
+			fprintf( stderr, "box2d_gb300: a device query ran out of traversal stack; this step missed some pairs or sweeps\n" );
 		/* the finalize kernel cleared the force and torque of every awake body (solver.c:710-712) */
 		for ( int i = 0; i < w->forcedBodies.count; ++i )
 		{
