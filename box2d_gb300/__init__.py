@@ -45,6 +45,15 @@ NO_WARM_STARTING = 2
 NO_RECYCLING = 4
 
 
+class WorldId(ctypes.Structure):
+    """b2WorldId (id.h): world slot + 1 and generation, passed by value."""
+    _fields_ = [("index1", ctypes.c_uint16), ("generation", ctypes.c_uint16)]
+
+    @classmethod
+    def unpack(cls, packed: int) -> "WorldId":
+        return cls(packed >> 16, packed & 0xFFFF)
+
+
 def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
     c_int, c_u32, c_u64, c_f, c_p = ctypes.c_int, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_float, ctypes.c_void_p
     sig = {
@@ -75,6 +84,16 @@ def _bind(lib: ctypes.CDLL) -> ctypes.CDLL:
         "b2s_world_state_hash": (c_u64, [c_int]),
         "b2s_sensor_events": (c_int, [c_int, c_p, c_int]),
         "b2s_set_awake": (None, [c_int, c_int, c_int]),
+        "b2s_snapshot": (c_int, [c_int]),
+        "b2s_restore": (c_int, [c_int]),
+        "b2s_from_snapshot": (c_int, [c_int]),
+        "b2s_add_box": (c_int, [c_int, c_f, c_f]),
+        "b2s_body_valid": (c_int, [c_int, c_int]),
+        "b2World_Snapshot": (c_int, [WorldId, c_p, c_int]),
+        "b2World_Restore": (ctypes.c_bool, [WorldId, c_p, c_int]),
+        "b2CreateWorldFromSnapshot": (WorldId, [c_p, c_int, c_int]),
+        "b2World_GetStateHash": (c_u64, [WorldId]),
+        "b2World_IsValid": (ctypes.c_bool, [WorldId]),
         "b2s_enable_sleep": (None, [c_int, c_int]),
         "b2p_timings": (c_int, [c_u32, c_p, c_p, c_int]),
         "b2p_stream": (c_p, [c_u32]),
@@ -130,6 +149,58 @@ class Scene:
             raise RuntimeError("scene creation failed (no world slot, or no usable CUDA device for the GB300 library)")
         self.body_count = lib.b2s_body_count(self.handle)
         self.dynamic_count = lib.b2s_dynamic_count(self.handle)
+
+    @classmethod
+    def _from_handle(cls, lib: ctypes.CDLL, handle: int) -> "Scene":
+        scene = cls.__new__(cls)
+        scene.lib = lib
+        scene.handle = handle
+        scene.body_count = lib.b2s_body_count(handle)
+        scene.dynamic_count = lib.b2s_dynamic_count(handle)
+        return scene
+
+    # ---- snapshots (b2World_Snapshot, b2World_Restore, b2CreateWorldFromSnapshot) ----
+    def snapshot(self) -> int:
+        """Snapshot the world into an image the scene keeps (with its body list); returns
+        the image size."""
+        return self.lib.b2s_snapshot(self.handle)
+
+    def restore(self) -> bool:
+        """Restore the world (and the body list) from the scene's kept image."""
+        ok = self.lib.b2s_restore(self.handle) == 1
+        self.body_count = self.lib.b2s_body_count(self.handle)
+        return ok
+
+    def from_snapshot(self) -> "Scene":
+        """A new scene whose world is created from the kept image."""
+        handle = self.lib.b2s_from_snapshot(self.handle)
+        if handle < 0:
+            raise RuntimeError("b2CreateWorldFromSnapshot failed")
+        return Scene._from_handle(self.lib, handle)
+
+    def snapshot_image(self) -> bytes:
+        """The world's snapshot image through the public API (size query, then fill)."""
+        wid = WorldId.unpack(self.world_id)
+        size = self.lib.b2World_Snapshot(wid, None, 0)
+        buf = ctypes.create_string_buffer(max(size, 1))
+        written = self.lib.b2World_Snapshot(wid, buf, size)
+        assert written == size
+        return buf.raw[:size]
+
+    def restore_image(self, image: bytes | None) -> bool:
+        wid = WorldId.unpack(self.world_id)
+        if image is None:
+            return bool(self.lib.b2World_Restore(wid, None, 0))
+        buf = ctypes.create_string_buffer(image, len(image))
+        return bool(self.lib.b2World_Restore(wid, buf, len(image)))
+
+    def add_box(self, x: float, y: float) -> int:
+        index = self.lib.b2s_add_box(self.handle, x, y)
+        self.body_count = self.lib.b2s_body_count(self.handle)
+        return index
+
+    def body_valid(self, index: int) -> bool:
+        return self.lib.b2s_body_valid(self.handle, index) == 1
 
     @property
     def world_id(self) -> int:
@@ -229,7 +300,7 @@ class Scene:
 
     def apply(self, action: list) -> None:
         """One scripted change between steps: ["velocity", body, vx, vy, w], ["awake", body,
-        flag], ["sleeping", flag], or a body action of BODY_ACTIONS with its body index and up
+        flag], ["sleeping", flag], ["snapshot"], ["restore"], or a body action of BODY_ACTIONS with its body index and up
         to four numbers (see b2s_body_action)."""
         kind = action[0]
         if kind == "velocity":
@@ -239,6 +310,12 @@ class Scene:
             self.lib.b2s_set_awake(self.handle, int(action[1]), int(action[2]))
         elif kind == "sleeping":
             self.lib.b2s_enable_sleep(self.handle, int(action[1]))
+        elif kind == "snapshot":
+            if self.snapshot() <= 0:
+                raise RuntimeError("b2World_Snapshot failed")
+        elif kind == "restore":
+            if not self.restore():
+                raise RuntimeError("b2World_Restore refused the scene's image")
         elif kind in BODY_ACTIONS:
             args = [float(x) for x in action[2:]] + [0.0] * (4 - len(action[2:]))
             self.lib.b2s_body_action(self.handle, BODY_ACTIONS[kind], int(action[1]), *args[:4])

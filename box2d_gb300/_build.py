@@ -21,7 +21,7 @@ LIB = PKG / "libbox2d_gb300.so"
 
 HOST_SOURCES = ["csrc/host/world.c", "csrc/host/step.c", "csrc/host/joint.c", "csrc/host/tree.c",
                 "csrc/host/geometry.c", "csrc/host/probe.c", "csrc/host/batch.c", "csrc/host/diff.c", "csrc/host/island.c",
-                "csrc/host/sensor.c",
+                "csrc/host/sensor.c", "csrc/host/snapshot.c",
                 "scenes/scenes.c"]
 # (source, extra nvcc flags). The cluster and persistent solvers read state written by
 # other SMs between barriers, so their global loads bypass L1 (-dlcm=cg).

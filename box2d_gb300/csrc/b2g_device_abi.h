@@ -316,7 +316,10 @@ int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* inits, int co
 int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* contactIds, int count );
 int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* colorContactIds, const int* colorContactOffsets,
 						 int totalContacts );
+/* contact slots [0, count) to the host (slots the device never held read as zeros), and
+   back (a world snapshot's restore) */
 int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count );
+int b2gDev_UploadContacts( b2gDeviceWorld* dw, const b2gContact* in, int count );
 /* device addresses of the contact records and the color lists, the color offsets, the
    world's stream (cudaStream_t) and its CUDA device, for kernels outside world.cu */
 void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const int** colorIds, int* colorOffsets,

@@ -1326,6 +1326,31 @@ extern "C" int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity )
 	return 0;
 }
 
+/* every contact slot below `count` (manifolds, impulses, flags, simplex caches) to or from
+   the host, for world snapshots; slots the device never held read as zeros */
+extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count )
+{
+	if ( count <= 0 ) return 0;
+	int held = dw->contacts != NULL ? ( count < dw->contactCap ? count : dw->contactCap ) : 0;
+	if ( held < count ) memset( out + held, 0, (size_t)( count - held ) * sizeof( b2gContact ) );
+	if ( held == 0 ) return 0;
+	dw->d2hBytes += (long long)held * (long long)sizeof( b2gContact );
+	CK( cudaMemcpyAsync( out, dw->contacts, (size_t)held * sizeof( b2gContact ), cudaMemcpyDeviceToHost, dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	return 0;
+}
+
+extern "C" int b2gDev_UploadContacts( b2gDeviceWorld* dw, const b2gContact* in, int count )
+{
+	CK2( b2gDev_ReserveContacts( dw, count ) );
+	dw->prefetchValid = 0;
+	if ( count <= 0 ) return 0;
+	dw->h2dBytes += (long long)count * (long long)sizeof( b2gContact );
+	CK( cudaMemcpyAsync( dw->contacts, in, (size_t)count * sizeof( b2gContact ), cudaMemcpyHostToDevice, dw->stream ) );
+	CK( cudaStreamSynchronize( dw->stream ) );
+	return 0;
+}
+
 /* Upload arena: small per-step uploads are copied into page-locked host memory and sent
    with cudaMemcpyAsync on the world stream, so they need no wait. Arena space is reused
    only after the stream has been drained (every step drains it at its readbacks). */
@@ -1579,14 +1604,6 @@ extern "C" void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** conta
 	*colorIds = dw->colorIds;
 	memcpy( colorOffsets, dw->colorOffsets, sizeof( dw->colorOffsets ) );
 	*stream = (void*)dw->stream;
-}
-
-extern "C" int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count )
-{
-	if ( count == 0 ) return 0;
-	CK( cudaStreamSynchronize( dw->stream ) );
-	CK( ( dw->d2hBytes += (long long)( (size_t)count * sizeof( b2gContact ) ), cudaMemcpy( out, dw->contacts, (size_t)count * sizeof( b2gContact ), cudaMemcpyDeviceToHost ) ) );
-	return 0;
 }
 
 extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* offsets )

@@ -232,6 +232,7 @@ typedef struct h_world
 	const float *mirrorXf, *mirrorCenter, *mirrorV, *mirrorSleep;
 	const uint32_t* mirrorFlags;
 	int jointsHostValid;	/* host joint records (impulses) match the device */
+	int shapeBoxesValid;	/* host shape boxes (aabb) match the device */
 	int moveEventsValid;	/* move event array matches the last step */
 	int colorsDirty, jointsDirty;
 	int uploadedTreeVersion[3];		 /* tree version last sent to the device */
@@ -311,6 +312,11 @@ void h_markHostChanged( h_world* w );
 /* the last step's move events, one per body awake at its finalize (solver.c:608-622) */
 void h_buildMoveEvents( h_world* w );
 void h_syncJointsFromDevice( h_world* w );
+/* the shapes' tight boxes as the last finalize left them on the device */
+void h_syncShapeBoxes( h_world* w );
+/* frees every array of the world's simulation state; the device world, the rebuild worker
+   and the tape stay (world.c) */
+void h_freeWorldArrays( h_world* w );
 void h_ensureDevice( h_world* w );
 void h_createContact( h_world* w, h_shape* a, h_shape* b );
 void h_destroyContact( h_world* w, h_contact* c );

@@ -458,6 +458,7 @@ int h_stepBegin( h_world* w, float timeStep, int subStepCount )
 {
 	w->moveEvents.count = 0;
 	w->moveEventsValid = 0;
+	w->shapeBoxesValid = 0;
 	w->beginEvents.count = 0;
 	w->sensorBeginEvents.count = 0;
 	memset( &w->profile, 0, sizeof( w->profile ) );

@@ -223,13 +223,10 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
 	return id;
 }
 
-void b2DestroyWorld( b2WorldId worldId )
+/* frees every array of the world's simulation state (what a snapshot holds); the device
+   world, the rebuild worker and the tape stay */
+void h_freeWorldArrays( h_world* w )
 {
-	h_world* w = h_worldFromId( worldId );
-	if ( w == NULL ) return;
-	h_stopRebuildWorker( w );
-	h_tapeDetach( w );
-	b2gDev_Destroy( w->dev );
 	for ( int i = 0; i < 3; ++i )
 	{
 		h_treeDestroy( w->trees + i );
@@ -268,6 +265,16 @@ void b2DestroyWorld( b2WorldId worldId )
 	h_free( w->staticBodyIds );
 	h_free( w->staticJointIds );
 	h_islandsFree( w );
+}
+
+void b2DestroyWorld( b2WorldId worldId )
+{
+	h_world* w = h_worldFromId( worldId );
+	if ( w == NULL ) return;
+	h_stopRebuildWorker( w );
+	h_tapeDetach( w );
+	b2gDev_Destroy( w->dev );
+	h_freeWorldArrays( w );
 	uint16_t generation = w->generation;
 	memset( w, 0, sizeof( *w ) );
 	w->generation = generation + 1;
@@ -607,10 +614,33 @@ void h_syncJointsFromDevice( h_world* w )
 	w->jointsHostValid = 1;
 }
 
+void h_syncShapeBoxes( h_world* w )
+{
+	if ( w->shapeBoxesValid || w->devReady == 0 ) return;
+	int ns = w->shapes.count;
+	if ( ns > 0 )
+	{
+		float* boxes = malloc( (size_t)ns * 8 * sizeof( float ) );
+		int rc = b2gDev_DownloadShapeBoxes( w->dev, ns, boxes, boxes + 4 * (size_t)ns );
+		if ( rc != 0 ) h_fail( w, "shape box download", rc );
+		for ( int i = 0; i < ns; ++i )
+		{
+			h_shape* s = w->shapes.data + i;
+			if ( s->id != i ) continue;
+			b2AABB box = { { boxes[4 * i], boxes[4 * i + 1] }, { boxes[4 * i + 2], boxes[4 * i + 3] } };
+			s->aabb = box;
+		}
+		free( boxes );
+	}
+	w->shapeBoxesValid = 1;
+}
+
 void h_markHostChanged( h_world* w )
 {
 	h_syncFromDevice( w );
 	h_syncJointsFromDevice( w );
+	/* the device boxes are sent again from the host's before the next step */
+	h_syncShapeBoxes( w );
 	w->devReady = 0;
 }
 
@@ -900,6 +930,35 @@ bool b2Body_IsValid( b2BodyId id )
 	if ( w->inUse == 0 || id.index1 < 1 || id.index1 > w->bodies.count ) return false;
 	h_body* b = w->bodies.data + id.index1 - 1;
 	return b->id == id.index1 - 1 && b->generation == id.generation;
+}
+
+/* shape.c b2Shape_IsValid, joint.c b2Joint_IsValid: the slot is live and of the same generation */
+bool b2Shape_IsValid( b2ShapeId id )
+{
+	if ( id.world0 >= H_MAX_WORLDS ) return false;
+	h_world* w = h_worlds + id.world0;
+	if ( w->inUse == 0 || id.index1 < 1 || id.index1 > w->shapes.count ) return false;
+	const h_shape* s = w->shapes.data + id.index1 - 1;
+	return s->id == id.index1 - 1 && s->generation == id.generation;
+}
+
+bool b2Joint_IsValid( b2JointId id )
+{
+	if ( id.world0 >= H_MAX_WORLDS ) return false;
+	h_world* w = h_worlds + id.world0;
+	if ( w->inUse == 0 || id.index1 < 1 || id.index1 > w->joints.count ) return false;
+	const h_joint* j = w->joints.data + id.index1 - 1;
+	return j->jointId == id.index1 - 1 && j->generation == id.generation;
+}
+
+/* shape.c b2Shape_GetAABB: the shape's box as the last step's finalize computed it */
+b2AABB b2Shape_GetAABB( b2ShapeId id )
+{
+	b2AABB empty = { { 0.0f, 0.0f }, { 0.0f, 0.0f } };
+	if ( b2Shape_IsValid( id ) == false ) return empty;
+	h_world* w = h_worlds + id.world0;
+	h_syncShapeBoxes( w );
+	return w->shapes.data[id.index1 - 1].aabb;
 }
 
 b2BodyType b2Body_GetType( b2BodyId bodyId ) { return h_getBody( bodyId )->type; }

@@ -75,6 +75,10 @@ typedef struct b2sScene
 	int dynamicCount;
 	float targetX, targetY;
 	int flags; /* creation flags: 1 no continuous, 2 no warm starting, 4 no contact recycling (ramp) */
+	uint8_t* image;		  /* the last b2s_snapshot image */
+	int imageSize;
+	b2BodyId* imageBodies; /* the scene's body list when that image was taken */
+	int imageBodyCount;
 } b2sScene;
 
 #define B2S_MAX_SCENES 4096
@@ -1293,6 +1297,8 @@ B2S_EXPORT void b2s_destroy( int h )
 	if ( s->inUse == 0 ) return;
 	b2DestroyWorld( s->worldId );
 	free( s->bodies );
+	free( s->image );
+	free( s->imageBodies );
 	memset( s, 0, sizeof( *s ) );
 }
 
@@ -1337,6 +1343,94 @@ B2S_EXPORT void b2s_set_body_velocity( int h, int bodyIndex, float vx, float vy,
 	b2Body_SetLinearVelocity( id, ( b2Vec2 ){ vx, vy } );
 	b2Body_SetAngularVelocity( id, w );
 }
+
+#ifndef B2S_NO_SNAPSHOT
+/* b2World_Snapshot of the scene's world into an image the scene keeps, with a copy of its
+   body list; returns the image size */
+B2S_EXPORT int b2s_snapshot( int h )
+{
+	b2sScene* s = b2s_scenes + h;
+	int size = b2World_Snapshot( s->worldId, NULL, 0 );
+	if ( size <= 0 ) return size;
+	free( s->image );
+	s->image = malloc( (size_t)size );
+	s->imageSize = b2World_Snapshot( s->worldId, s->image, size );
+	free( s->imageBodies );
+	s->imageBodies = malloc( (size_t)( s->bodyCount > 0 ? s->bodyCount : 1 ) * sizeof( b2BodyId ) );
+	memcpy( s->imageBodies, s->bodies, (size_t)s->bodyCount * sizeof( b2BodyId ) );
+	s->imageBodyCount = s->bodyCount;
+	return s->imageSize;
+}
+
+/* b2World_Restore of the scene's world from its kept image, and the body list of that
+   instant; returns 1 when the restore succeeded */
+B2S_EXPORT int b2s_restore( int h )
+{
+	b2sScene* s = b2s_scenes + h;
+	if ( s->image == NULL ) return 0;
+	if ( b2World_Restore( s->worldId, s->image, s->imageSize ) == false ) return 0;
+	memcpy( s->bodies, s->imageBodies, (size_t)s->imageBodyCount * sizeof( b2BodyId ) );
+	s->bodyCount = s->imageBodyCount;
+	return 1;
+}
+
+/* a new scene whose world is b2CreateWorldFromSnapshot of the scene's kept image, with the
+   body list of that instant pointed at the new world; returns its handle, or -1 */
+B2S_EXPORT int b2s_from_snapshot( int h )
+{
+	b2sScene* s = b2s_scenes + h;
+	if ( s->image == NULL ) return -1;
+	int n = -1;
+	for ( int i = 0; i < B2S_MAX_SCENES; ++i )
+	{
+		if ( b2s_scenes[i].inUse == 0 )
+		{
+			n = i;
+			break;
+		}
+	}
+	if ( n < 0 ) return -1;
+	b2WorldId id = b2CreateWorldFromSnapshot( s->image, s->imageSize, b2s_workerCount );
+	if ( b2World_IsValid( id ) == false ) return -1;
+	b2sScene* t = b2s_scenes + n;
+	memset( t, 0, sizeof( *t ) );
+	t->inUse = 1;
+	t->worldId = id;
+	t->flags = s->flags;
+	t->dynamicCount = s->dynamicCount;
+	t->targetX = s->targetX;
+	t->targetY = s->targetY;
+	t->bodyCapacity = s->imageBodyCount > 0 ? s->imageBodyCount : 1;
+	t->bodies = malloc( (size_t)t->bodyCapacity * sizeof( b2BodyId ) );
+	t->bodyCount = s->imageBodyCount;
+	for ( int i = 0; i < t->bodyCount; ++i )
+	{
+		t->bodies[i] = s->imageBodies[i];
+		if ( B2_IS_NON_NULL( t->bodies[i] ) ) t->bodies[i].world0 = (uint16_t)( id.index1 - 1 );
+	}
+	return n;
+}
+
+/* a dynamic 0.5 m box at (x, y) added to the scene; returns its index in the body list */
+B2S_EXPORT int b2s_add_box( int h, float x, float y )
+{
+	b2sScene* s = b2s_scenes + h;
+	b2BodyDef bd = b2DefaultBodyDef();
+	bd.type = b2_dynamicBody;
+	bd.position = ( b2Vec2 ){ x, y };
+	b2BodyId id = b2CreateBody( s->worldId, &bd );
+	b2ShapeDef sd = b2DefaultShapeDef();
+	b2Polygon box = b2MakeBox( 0.5f, 0.5f );
+	b2CreatePolygonShape( id, &sd, &box );
+	b2sAddBody( s, id, 1 );
+	return s->bodyCount - 1;
+}
+
+B2S_EXPORT int b2s_body_valid( int h, int bodyIndex )
+{
+	return b2Body_IsValid( b2s_scenes[h].bodies[bodyIndex] ) ? 1 : 0;
+}
+#endif
 
 #ifndef B2S_NO_ISLANDS
 B2S_EXPORT void b2s_set_awake( int h, int bodyIndex, int awake )

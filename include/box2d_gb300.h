@@ -673,6 +673,19 @@ B2G_API b2Counters b2World_GetCounters( b2WorldId worldId );
 /* world_snapshot.c:1183 (box2d.h:235): FNV-1a 64 of the simulation state and bookkeeping */
 B2G_API uint64_t b2World_GetStateHash( b2WorldId worldId );
 
+/* ---- API: snapshots (world_snapshot.c; box2d.h:286-338) ----
+   The world's simulation state at a step boundary as a caller-owned byte image. Call
+   b2World_Snapshot with image == NULL for the size, then with a buffer of that size; it
+   returns the size needed (nothing is written when capacity is smaller) and 0 inside a
+   step. b2World_Restore rolls a world back to an image in place (ids held from that
+   instant stay valid, ids minted later fail validation); a rejected image (bad magic,
+   version, layout or checksum) leaves the world unchanged and returns false.
+   b2CreateWorldFromSnapshot builds a new world from an image. Object user data is not
+   stored and reads back as NULL. Images are for this library on the same machine type. */
+B2G_API int b2World_Snapshot( b2WorldId worldId, uint8_t* image, int capacity );
+B2G_API bool b2World_Restore( b2WorldId worldId, const uint8_t* image, int size );
+B2G_API b2WorldId b2CreateWorldFromSnapshot( const uint8_t* image, int size, int workerCount );
+
 /* ---- API: bodies (box2d.h:355-550) ---- */
 B2G_API b2BodyId b2CreateBody( b2WorldId worldId, const b2BodyDef* def );
 /* body.c:346 (box2d.h:359): its joints, contacts, shapes and chains go with it */
@@ -720,6 +733,9 @@ B2G_API bool b2Chain_IsValid( b2ChainId id );
 B2G_API int b2Chain_GetSegmentCount( b2ChainId chainId );
 B2G_API int b2Chain_GetSegments( b2ChainId chainId, b2ShapeId* segmentArray, int capacity );
 B2G_API b2ShapeId b2CreateChainSegmentShape( b2BodyId bodyId, const b2ShapeDef* def, const b2ChainSegment* chainSegment );
+/* shape.c (box2d.h:689, :859) */
+B2G_API bool b2Shape_IsValid( b2ShapeId id );
+B2G_API b2AABB b2Shape_GetAABB( b2ShapeId shapeId );
 B2G_API b2ShapeType b2Shape_GetType( b2ShapeId shapeId );
 B2G_API b2ChainSegment b2Shape_GetChainSegment( b2ShapeId shapeId );
 B2G_API b2ChainId b2Shape_GetParentChain( b2ShapeId shapeId );
@@ -761,6 +777,8 @@ B2G_API b2JointId b2CreateMotorJoint( b2WorldId worldId, const b2MotorJointDef* 
 B2G_API b2JointId b2CreatePogoJoint( b2WorldId worldId, const b2PogoJointDef* def );
 /* joint.c:823 (box2d.h:919) */
 B2G_API void b2DestroyJoint( b2JointId jointId );
+/* joint.c (box2d.h:922) */
+B2G_API bool b2Joint_IsValid( b2JointId id );
 B2G_API b2JointType b2Joint_GetType( b2JointId jointId );
 B2G_API float b2RevoluteJoint_GetAngle( b2JointId jointId );
 

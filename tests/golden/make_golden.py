@@ -74,6 +74,15 @@ SLEEP_SCENES = [
     ("destroy_pyramids", B.SLEEP_PYRAMIDS, 2, 6, 1000, 0, 0, 300, [1, 60, 160, 300]),
     ("destroy_joint_zoo", B.JOINT_ZOO, 4, 0, 0, 3, 0, 200, [1, 50, 100, 200]),
 ]
+# snapshots taken and restored between steps (b2World_Snapshot / b2World_Restore), with
+# changes made between them that the restore rolls back; per step also the awake count.
+# The oracle does not restate snapshots, so only the GB300 library is checked against these.
+SNAPSHOT_SCENES = [
+    ("snapshot_sleep_pyramids", B.SLEEP_PYRAMIDS, 2, 6, 1000, 0, 0, 300, [1, 96, 141, 221, 300]),
+    ("snapshot_joint_zoo", B.JOINT_ZOO, 4, 0, 0, 3, 0, 200, [1, 61, 141, 200]),
+    ("snapshot_sensor_zoo", B.SENSOR_ZOO, 60, 0, 0, 6, 0, 160, [1, 91, 160]),
+    ("snapshot_chain_zoo", B.CHAIN_ZOO, 80, 0, 0, 3, 0, 200, [1, 101, 200]),
+]
 # changes applied after the given step (Scene.apply): wake by velocity, put an island to
 # sleep and wake one through b2Body_SetAwake, switch sleeping off and on again
 SCRIPTS = {
@@ -84,6 +93,14 @@ SCRIPTS["destroy_pyramids"] = [[20, "destroy_body", 3], [40, "destroy_shape", 7]
                                 [121, "destroy_body", 30], [150, "destroy_shape", 25], [200, "destroy_body", 40]]
 SCRIPTS["destroy_joint_zoo"] = [[30, "destroy_body", 5], [31, "destroy_body", 9], [60, "destroy_body", 14],
                                  [61, "destroy_shape", 20], [90, "destroy_body", 2]]
+SCRIPTS["snapshot_sleep_pyramids"] = [[95, "snapshot"], [100, "velocity", 3, 0.0, 6.0, 0.0], [110, "destroy_body", 12],
+                                       [140, "restore"], [170, "snapshot"], [175, "impulse_center", 20, 5.0, 10.0],
+                                       [220, "restore"], [230, "restore"]]
+SCRIPTS["snapshot_joint_zoo"] = [[30, "snapshot"], [31, "impulse_center", 6, 3.0, 8.0], [60, "restore"],
+                                  [100, "snapshot"], [101, "destroy_body", 5], [140, "restore"]]
+SCRIPTS["snapshot_sensor_zoo"] = [[50, "snapshot"], [51, "impulse_center", 10, 0.0, 20.0], [90, "restore"],
+                                   [120, "snapshot"], [121, "destroy_body", 7], [150, "restore"]]
+SCRIPTS["snapshot_chain_zoo"] = [[60, "snapshot"], [61, "impulse_center", 10, 4.0, 9.0], [100, "restore"]]
 SCRIPTS["body_api_zoo"] = (
     [[5, "force", 3, 50.0, 100.0, 0.1, 0.2], [5, "force_center", 3, -20.0, 0.0], [6, "torque", 4, 30.0],
      [10, "impulse", 5, 2.0, 5.0, 0.1, 0.0], [11, "impulse_center", 6, -3.0, 1.0], [12, "angular_impulse", 7, 2.0],
@@ -123,10 +140,12 @@ def main() -> None:
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref"], check=True)
     ref = B.load_library(ROOT / "oracle" / "_ref" / "libref.so")
     only = set(sys.argv[1:])
-    for name, kind, a, b, c, seed, flags, steps, digest_steps in SCENES + CHAIN_SCENES + BULLET_SCENES + SLEEP_SCENES:
+    for name, kind, a, b, c, seed, flags, steps, digest_steps in (SCENES + CHAIN_SCENES + BULLET_SCENES + SLEEP_SCENES
+                                                                   + SNAPSHOT_SCENES):
         if only and name not in only:
             continue
-        sleeping = (name, kind, a, b, c, seed, flags, steps, digest_steps) in SLEEP_SCENES
+        entry = (name, kind, a, b, c, seed, flags, steps, digest_steps)
+        sleeping = entry in SLEEP_SCENES or entry in SNAPSHOT_SCENES
         script = SCRIPTS.get(name, [])
         with B.Scene(ref, kind, a, b, c, seed, flags) as s:
             hashes, digests, awake, world_hashes = [], {}, [], []
@@ -160,6 +179,8 @@ def main() -> None:
             if sleeping:
                 data["requires"] = "islands"
                 data["awake_counts"] = awake
+            if entry in SNAPSHOT_SCENES:
+                data["requires"] = "snapshots"
             if script:
                 data["script"] = script
         if kind == B.FALLING_HINGES:

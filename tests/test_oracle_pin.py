@@ -13,7 +13,7 @@ from conftest import EventCheck, golden_cases, load_golden
 @pytest.mark.parametrize("name", golden_cases())
 def test_oracle_matches_reference_fixture(oracle, name):
     g = load_golden(name)
-    if g.get("requires") in ("islands", "chains", "bullets"):
+    if g.get("requires") in ("islands", "chains", "bullets", "snapshots"):
         pytest.skip(f"{g['requires']} are not restated in the oracle; the GB300 library is checked against "
                     "this reference fixture directly")
     with B.Scene(oracle, g["kind"], g["a"], g["b"], g["c"], g["seed"], g["flags"]) as s:
