@@ -108,13 +108,32 @@ __global__ void k_compInit( int* parent, int* compData, int n )
 	for ( int k = 0; k < CD_STRIDE; ++k ) compData[CD_STRIDE * i + k] = 0;
 }
 
-__global__ void k_compUnion( d_solveArgs a, const int* awakeIndex, int* parent, int total, int count )
+/* unions of the constraints [begin, end) (contact slots, then joints) */
+__global__ void k_compUnion( d_solveArgs a, const int* awakeIndex, int* parent, int total, int begin, int end )
 {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if ( i >= count ) return;
+	int i = begin + blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= end ) return;
 	int ia, ib;
 	d_constraintBodies( a, awakeIndex, total, i, &ia, &ib );
 	if ( ia >= 0 && ib >= 0 ) d_unite( parent, ia, ib );
+}
+
+/* the forest over the joints, every body pointing at its root (no union runs meanwhile, so
+   each root is final), kept for later analyses */
+__global__ void k_compFlatten( int* parent, int* forest, int n )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	forest[i] = d_find( parent, i );
+}
+
+/* the union-find starts from the kept joint forest */
+__global__ void k_compInitFrom( int* parent, const int* forest, int* compData, int n )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	parent[i] = forest[i];
+	for ( int k = 0; k < CD_STRIDE; ++k ) compData[CD_STRIDE * i + k] = 0;
 }
 
 /* one atomic add of `1` per distinct address in the warp: lanes with the same address
@@ -558,7 +577,7 @@ extern "C" void b2gDev_CompFree( b2gCompBuffers* b )
 {
 	void* ptrs[] = { b->parent,		 b->compData,	 b->bodyList,	 b->localIndex,	  b->slotList, b->jointList,
 					 b->binRange,	 b->bigBodyList, b->bigSlotList, b->bigJointList, b->summary,
-					 b->clusterAssigned, b->clusterCounts, b->clusterJoints };
+					 b->clusterAssigned, b->clusterCounts, b->clusterJoints, b->jointForest };
 	for ( size_t i = 0; i < sizeof( ptrs ) / sizeof( ptrs[0] ); ++i )
 		if ( ptrs[i] ) cudaFree( ptrs[i] );
 	if ( b->hSummary ) cudaFreeHost( b->hSummary );
@@ -586,7 +605,8 @@ static d_compArgs compArgs( b2gCompBuffers* b, const int* jointOffsets, const in
 }
 
 extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const int* awakeIndex,
-								   int total, int jointTotal, int forceBig, cudaStream_t stream, long long* launches )
+								   int total, int jointTotal, int forceBig, long long jointEpoch, cudaStream_t stream,
+								   long long* launches )
 {
 	int n = a->awakeCount;
 	int rc = b2gDev_CompReserve( b, n, total, jointTotal );
@@ -607,12 +627,46 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 	CKC( cudaMemsetAsync( b->binRange + 3 * b->binCap, 0, (size_t)3 * b->binCap * sizeof( int ), stream ) );
 	CKC( cudaMemsetAsync( b->summary, 0, sizeof( b2gCompSummary ), stream ) );
 	int cons = total + jointTotal;
-	k_compInit<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
-	*launches += 1;
-	if ( cons > 0 )
+	/* Roots are the smallest index of each component whatever the order of the unions, so
+	   the joints' unions can be done once and kept: later analyses start from that forest
+	   and add the contacts. Joints change rarely; contacts begin and end every step. */
+	bool keptForest = jointTotal > 0 && jointEpoch >= 0 && b->jointForest != NULL && b->jointForestEpoch == jointEpoch &&
+					  b->jointForestN == n && b->jointForestJoints == jointTotal;
+	if ( keptForest == false && jointTotal > 0 && jointEpoch >= 0 )
 	{
-		k_compUnion<<<compBlocks( cons ), B2G_COMP_THREADS, 0, stream>>>( *a, awakeIndex, b->parent, total, cons );
+		if ( n > b->jointForestCap || b->jointForest == NULL )
+		{
+			int rc2 = growPair( &b->jointForest, NULL, &b->jointForestCap, n, 1 );
+			if ( rc2 ) return rc2;
+		}
+		k_compInit<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
+		k_compUnion<<<compBlocks( jointTotal ), B2G_COMP_THREADS, 0, stream>>>( *a, awakeIndex, b->parent, total, total, cons );
+		k_compFlatten<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->jointForest, n );
+		*launches += 3;
+		b->jointForestEpoch = jointEpoch;
+		b->jointForestN = n;
+		b->jointForestJoints = jointTotal;
+		keptForest = true;
+	}
+	if ( keptForest )
+	{
+		k_compInitFrom<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->jointForest, b->compData, n );
 		*launches += 1;
+		if ( total > 0 )
+		{
+			k_compUnion<<<compBlocks( total ), B2G_COMP_THREADS, 0, stream>>>( *a, awakeIndex, b->parent, total, 0, total );
+			*launches += 1;
+		}
+	}
+	else
+	{
+		k_compInit<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
+		*launches += 1;
+		if ( cons > 0 )
+		{
+			k_compUnion<<<compBlocks( cons ), B2G_COMP_THREADS, 0, stream>>>( *a, awakeIndex, b->parent, total, 0, cons );
+			*launches += 1;
+		}
 	}
 	k_compRoots<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
 	*launches += 1;

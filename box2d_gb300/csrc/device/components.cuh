@@ -72,6 +72,11 @@ struct b2gCompBuffers
 	long long clusterEpoch;
 	int clusterUseLists, clusterBodyCount, clusterThreads, clusterRanks;
 	int* clusterCounts;
+	/* the roots of the awake bodies over joints alone (every body points at its root), kept
+	   while the joints and the awake set are unchanged (jointEpoch) */
+	int* jointForest;
+	int jointForestCap, jointForestN, jointForestJoints;
+	long long jointForestEpoch;
 };
 
 extern "C" int b2gDev_CompReserve( b2gCompBuffers* b, int awake, int slots, int joints );
@@ -79,9 +84,12 @@ extern "C" void b2gDev_CompFree( b2gCompBuffers* b );
 
 /* find components, pack the small ones into bins and build the component-contiguous and
    big-component lists; waits for the summary. forceBig puts every component on the
-   global path (an overflow color exists). */
+   global path (an overflow color exists). `jointEpoch` changes whenever the joints or the
+   awake set change (-1: unknown): the joints' part of the union-find is kept while it
+   stays the same. */
 extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const int* awakeIndex,
-								   int total, int jointTotal, int forceBig, cudaStream_t stream, long long* launches );
+								   int total, int jointTotal, int forceBig, long long jointEpoch, cudaStream_t stream,
+								   long long* launches );
 
 /* solve every bin (small components) */
 extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets,

@@ -106,6 +106,7 @@ struct b2gDeviceWorld
 	int compValid;								   /* the component lists match the current constraint graph */
 	int topologyDirty;							   /* colors, joints or the awake set changed since the analysis */
 	long long topologyEpoch;					   /* counts those changes and every component analysis */
+	long long jointEpoch;						   /* counts changes of the joints or the awake set */
 	b2gCompBuffers comp;						   /* component solver scratch */
 	void* persistentScratch;					   /* barrier counter, generation, error, restitution flag */
 	/* bodies by id */
@@ -1114,6 +1115,7 @@ extern "C" int b2gDev_UploadBodies( b2gDeviceWorld* dw, int bodyCount, const flo
 									 const int* shapeCount, const int* shapeList, int shapeListCount )
 {
 	dw->topologyDirty = 1;
+	dw->jointEpoch += 1; /* the awake set or the joints changed */
 	dw->topologyEpoch += 1;
 	int cap0 = dw->bodyCap, capOut = 0;
 	CK2( upload( dw, &dw->xf, &cap0, (const float4*)xf, bodyCount, &capOut ) );
@@ -1163,6 +1165,7 @@ extern "C" int b2gDev_UploadAwake( b2gDeviceWorld* dw, int awakeCount, const int
 									const float* stateD, const float* params, const float* center0, const float* sleepTime )
 {
 	dw->topologyDirty = 1;
+	dw->jointEpoch += 1; /* the awake set or the joints changed */
 	dw->topologyEpoch += 1;
 	int cap0 = dw->awakeCap, capOut = 0;
 	CK2( upload( dw, &dw->awakeBodyId, &cap0, awakeBodyId, awakeCount, &capOut ) );
@@ -1513,6 +1516,7 @@ extern "C" int b2gDev_WakeBodies( b2gDeviceWorld* dw, int newAwakeCount, const i
 	CK2( ( dev_launch<d_islandOpArgs, b_islandOp>( dw, DK_ISLAND_OP, blocks( count ), a ) ) );
 	dw->awakeCount = newAwakeCount;
 	dw->topologyDirty = 1;
+	dw->jointEpoch += 1; /* the awake set or the joints changed */
 	dw->topologyEpoch += 1;
 	return 0;
 }
@@ -1536,6 +1540,7 @@ extern "C" int b2gDev_SleepBodies( b2gDeviceWorld* dw, int newAwakeCount, const 
 	}
 	dw->awakeCount = newAwakeCount;
 	dw->topologyDirty = 1;
+	dw->jointEpoch += 1; /* the awake set or the joints changed */
 	dw->topologyEpoch += 1;
 	return 0;
 }
@@ -1609,6 +1614,7 @@ extern "C" void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** conta
 extern "C" int b2gDev_UploadJoints( b2gDeviceWorld* dw, const b2gJoint* joints, int count, const int* offsets )
 {
 	dw->topologyDirty = 1;
+	dw->jointEpoch += 1; /* the awake set or the joints changed */
 	dw->topologyEpoch += 1;
 	CK2( grow( dw, (void**)&dw->joints, &dw->jointCap, count > 0 ? count : 1, sizeof( b2gJoint ) ) );
 	CK2( uploadTo( dw, dw->joints, joints, (size_t)count * sizeof( b2gJoint ) ) );
@@ -2358,7 +2364,8 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 		if ( reuse == false )
 		{
 			int forceBig = ovJointCount0 + ovCount0 > 0;
-			CK2( b2gDev_CompAnalyze( &dw->comp, &a, dw->jointOffsets, dw->awakeIndex, total, jointTotal, forceBig, dw->stream,
+			CK2( b2gDev_CompAnalyze( &dw->comp, &a, dw->jointOffsets, dw->awakeIndex, total, jointTotal, forceBig, dw->jointEpoch,
+									 dw->stream,
 									 &dw->launches ) );
 			dw->topologyEpoch += 1;
 			dw->topologyDirty = 0;

@@ -335,6 +335,9 @@ int h_treeCreateProxy( h_tree* t, b2AABB aabb, uint64_t categoryBits, uint64_t u
 void h_treeDestroyProxy( h_tree* t, int proxyId );
 void h_treeMoveProxy( h_tree* t, int proxyId, b2AABB aabb );
 void h_treeEnlargeProxy( h_tree* t, int proxyId, b2AABB aabb );
+/* h_treeEnlargeProxy for threads that enlarge different proxies of one tree at once (the
+   result is that of the enlargements one after another); the caller bumps the version */
+void h_treeEnlargeProxyShared( h_tree* t, int proxyId, b2AABB aabb );
 int h_treeRebuild( h_tree* t, int fullBuild );
 typedef int h_treeQueryFcn( int proxyId, uint64_t userData, void* ctx );
 void h_treeQuery( const h_tree* t, b2AABB aabb, uint64_t maskBits, h_treeQueryFcn* fcn, void* ctx );

@@ -317,6 +317,13 @@ void h_syncShapeBoxes( h_world* w );
 /* frees every array of the world's simulation state; the device world, the rebuild worker
    and the tape stay (world.c) */
 void h_freeWorldArrays( h_world* w );
+/* the host thread pool (batch.c): fn(ctx, i) for i in [0, count) on up to `threads` threads,
+   the caller among them; returns 0 without running anything when the pool is taken (by
+   another thread, or by the caller itself inside a pool task): the caller then runs the
+   loop alone */
+int h_parallelFor( int threads, void ( *fn )( void*, int ), void* ctx, int count );
+/* threads a step's host loops use: the online cores, at most 8 */
+int h_hostThreads( void );
 void h_ensureDevice( h_world* w );
 void h_createContact( h_world* w, h_shape* a, h_shape* b );
 void h_destroyContact( h_world* w, h_contact* c );

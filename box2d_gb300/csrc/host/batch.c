@@ -22,6 +22,7 @@
 /* ---- a fork-join pool of host threads, kept across calls ---- */
 typedef struct h_pool
 {
+	pthread_mutex_t runMu; /* held by the thread that runs the pool */
 	pthread_mutex_t mu;
 	pthread_cond_t start, done;
 	pthread_t threads[256];
@@ -34,7 +35,10 @@ typedef struct h_pool
 	atomic_int next;
 } h_pool;
 
-static h_pool h_thePool = { .mu = PTHREAD_MUTEX_INITIALIZER, .start = PTHREAD_COND_INITIALIZER, .done = PTHREAD_COND_INITIALIZER };
+static h_pool h_thePool = { .runMu = PTHREAD_MUTEX_INITIALIZER,
+							 .mu = PTHREAD_MUTEX_INITIALIZER,
+							 .start = PTHREAD_COND_INITIALIZER,
+							 .done = PTHREAD_COND_INITIALIZER };
 
 static void h_poolDrain( h_pool* p )
 {
@@ -64,10 +68,8 @@ static void* h_poolMain( void* arg )
 	return NULL;
 }
 
-/* run fn(ctx, i) for i in [0, count) on `threads` threads (the caller is one of them) */
-static void h_poolRun( int threads, void ( *fn )( void*, int ), void* ctx, int count )
+static void h_poolRunLocked( h_pool* p, int threads, void ( *fn )( void*, int ), void* ctx, int count )
 {
-	h_pool* p = &h_thePool;
 	pthread_mutex_lock( &p->mu );
 	while ( p->threadCount < threads - 1 && p->threadCount < 256 )
 	{
@@ -88,6 +90,35 @@ static void h_poolRun( int threads, void ( *fn )( void*, int ), void* ctx, int c
 	pthread_mutex_lock( &p->mu );
 	while ( p->finished < helpers ) pthread_cond_wait( &p->done, &p->mu );
 	pthread_mutex_unlock( &p->mu );
+}
+
+/* run fn(ctx, i) for i in [0, count) on `threads` threads (the caller is one of them) */
+static void h_poolRun( int threads, void ( *fn )( void*, int ), void* ctx, int count )
+{
+	h_pool* p = &h_thePool;
+	pthread_mutex_lock( &p->runMu );
+	h_poolRunLocked( p, threads, fn, ctx, count );
+	pthread_mutex_unlock( &p->runMu );
+}
+
+int h_parallelFor( int threads, void ( *fn )( void*, int ), void* ctx, int count )
+{
+	h_pool* p = &h_thePool;
+	if ( pthread_mutex_trylock( &p->runMu ) != 0 ) return 0;
+	h_poolRunLocked( p, threads, fn, ctx, count );
+	pthread_mutex_unlock( &p->runMu );
+	return 1;
+}
+
+int h_hostThreads( void )
+{
+	static int threads = 0;
+	if ( threads == 0 )
+	{
+		long n = sysconf( _SC_NPROCESSORS_ONLN );
+		threads = n > 8 ? 8 : ( n < 1 ? 1 : (int)n );
+	}
+	return threads;
 }
 
 /* ---- batched stepping ---- */

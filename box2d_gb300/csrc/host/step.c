@@ -382,8 +382,50 @@ static void h_contactStatePass( h_world* w, const int* changes, int count )
 
 /* solver.c:1837-1909: enlarge proxies in ascending awake index; this builds the next move
    array. Each record is (awakeIndex, shapeId, enlargedFlag, bodyFast) + fat box. */
+typedef struct h_enlargeJob
+{
+	h_world* w;
+	const int* recs;
+	const float* boxes;
+	int count;
+} h_enlargeJob;
+
+#define H_ENLARGE_CHUNK 512
+
+/* one chunk of records: the shapes' fat boxes and the tree enlargements (every shape is
+   in one record at most, so only tree ancestors are shared between chunks) */
+static void h_enlargeChunk( void* ctx, int chunk )
+{
+	const h_enlargeJob* job = ctx;
+	int end = ( chunk + 1 ) * H_ENLARGE_CHUNK < job->count ? ( chunk + 1 ) * H_ENLARGE_CHUNK : job->count;
+	for ( int i = chunk * H_ENLARGE_CHUNK; i < end; ++i )
+	{
+		const int* r = job->recs + 4 * i;
+		if ( r[3] != 0 || r[2] == 0 ) continue;
+		h_shape* s = job->w->shapes.data + r[1];
+		const float* f = job->boxes + 4 * i;
+		b2AABB fat = { { f[0], f[1] }, { f[2], f[3] } };
+		s->fatAABB = fat;
+		h_treeEnlargeProxyShared( job->w->trees + H_PROXY_TYPE( s->proxyKey ), H_PROXY_ID( s->proxyKey ), fat );
+	}
+}
+
 static void h_enlargeProxies( h_world* w, const int* recs, const float* boxes, int count )
 {
+	/* many records: the tree enlargements on the host pool, then the move buffer in order */
+	if ( count >= 4 * H_ENLARGE_CHUNK )
+	{
+		h_enlargeJob job = { w, recs, boxes, count };
+		int chunks = ( count + H_ENLARGE_CHUNK - 1 ) / H_ENLARGE_CHUNK;
+		if ( h_parallelFor( h_hostThreads(), h_enlargeChunk, &job, chunks ) )
+		{
+			w->trees[b2_dynamicBody].version += 1;
+			w->trees[b2_kinematicBody].version += 1;
+			for ( int i = 0; i < count; ++i )
+				if ( recs[4 * i + 3] != 0 || recs[4 * i + 2] != 0 ) h_bufferMove( w, w->shapes.data[recs[4 * i + 1]].proxyKey );
+			return;
+		}
+	}
 	for ( int i = 0; i < count; ++i )
 	{
 		int shapeId = recs[4 * i + 1];
@@ -603,7 +645,7 @@ void h_stepFinish( h_world* w )
 		h_lap( w, H_PHASE_SOLVE, &lap );
 		h_joinRebuild( w );
 		h_lap( w, H_PHASE_TREE_REBUILD, &lap );
-		w->lastStatus = status;
+		w->lastStatus |= status; /* sticky: every step's failures since the world was created */
 		{
 			b2gStepCounters sc;
 			b2gDev_LastCounters( w->dev, &sc );

@@ -470,6 +470,56 @@ void h_treeEnlargeProxy( h_tree* t, int proxyId, b2AABB aabb )
 	}
 }
 
+/* h_treeEnlargeProxy for threads enlarging different proxies of one tree at once: box
+   growth and flags are atomic. Every ancestor ends up with its old box grown by the new
+   boxes of the enlarged leaves below it and flagged enlarged, whatever the order in which
+   the threads reach it, so the tree is bit for bit what the enlargements one after another
+   give. A walk may stop at an ancestor that already holds the box, since that ancestor's
+   own ancestors hold it too or are being grown by the thread that grew it. The caller bumps
+   the tree's version. */
+static int h_atomicLower( float* p, float v )
+{
+	float cur;
+	__atomic_load( p, &cur, __ATOMIC_RELAXED );
+	while ( v < cur )
+		if ( __atomic_compare_exchange( p, &cur, &v, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED ) ) return 1;
+	return 0;
+}
+
+static int h_atomicRaise( float* p, float v )
+{
+	float cur;
+	__atomic_load( p, &cur, __ATOMIC_RELAXED );
+	while ( cur < v )
+		if ( __atomic_compare_exchange( p, &cur, &v, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED ) ) return 1;
+	return 0;
+}
+
+void h_treeEnlargeProxyShared( h_tree* t, int proxyId, b2AABB aabb )
+{
+	h_treeNode* nodes = t->nodes;
+	nodes[proxyId].aabb = aabb;
+	int parentIndex = nodes[proxyId].parent;
+	while ( parentIndex != B2_NULL_INDEX )
+	{
+		b2AABB* box = &nodes[parentIndex].aabb;
+		int changed = h_atomicLower( &box->lowerBound.x, aabb.lowerBound.x );
+		changed |= h_atomicLower( &box->lowerBound.y, aabb.lowerBound.y );
+		changed |= h_atomicRaise( &box->upperBound.x, aabb.upperBound.x );
+		changed |= h_atomicRaise( &box->upperBound.y, aabb.upperBound.y );
+		if ( ( __atomic_load_n( &nodes[parentIndex].flags, __ATOMIC_RELAXED ) & H_NODE_ENLARGED ) == 0 )
+			__atomic_fetch_or( &nodes[parentIndex].flags, (uint16_t)H_NODE_ENLARGED, __ATOMIC_RELAXED );
+		parentIndex = nodes[parentIndex].parent;
+		if ( changed == 0 ) break;
+	}
+	while ( parentIndex != B2_NULL_INDEX )
+	{
+		if ( __atomic_load_n( &nodes[parentIndex].flags, __ATOMIC_RELAXED ) & H_NODE_ENLARGED ) break;
+		__atomic_fetch_or( &nodes[parentIndex].flags, (uint16_t)H_NODE_ENLARGED, __ATOMIC_RELAXED );
+		parentIndex = nodes[parentIndex].parent;
+	}
+}
+
 int h_treeHeight( const h_tree* t )
 {
 	return t->root == B2_NULL_INDEX ? 0 : t->nodes[t->root].height;

@@ -40,7 +40,9 @@ int b2p_contact_floats( uint32_t packedWorldId, float* out, int capacity );
    two worlds' state or bookkeeping differ. */
 int b2p_state_words( uint32_t packedWorldId, uint32_t* out, int capacity );
 
-/* Device status of the last step: 0 ok, 1 non-finite body velocity, 2 capacity exceeded. */
+/* Device status bits of every step since the world was created (or restored from a
+   snapshot): 0 ok, 1 non-finite body velocity, 2 a query ran out of traversal stack,
+   4 the persistent solver's grid barrier gave up. */
 int b2p_status( uint32_t packedWorldId );
 
 /* Accumulated device time per stage since the last reset, in ms: pair query, narrowphase

@@ -1,5 +1,6 @@
 """Failure detection without a GPU fault: each device check reports through the world's
-status word (b2p_status), which a step sets and the host reads, and the device stays usable.
+status word (b2p_status: the status bits of every step since the world was created), which
+the host reads, and the device stays usable.
 
 - a body given a non-finite velocity through b2Body_SetLinearVelocity: B2G_STATUS_NAN (1);
 - the pair query's traversal stack made too small for the tree (B2G_PAIR_STACK_LIMIT):
