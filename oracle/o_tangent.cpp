@@ -9,29 +9,435 @@
  * cone, speed cap, clip and edge choice) is the recorded one; each float carries one tangent
  * in double, propagated forward from a direction in (initial velocity, friction) space.
  * Every step's replay must land bit for bit on the next recorded step.
+ *
+ * Nothing of the product's differentiation code is used here: the dual numbers, the vector
+ * math and the polygon contact (manifold.c:511-1028) are this file's own, restated from the
+ * reference; only the tape's record layout (b2g_device_abi.h) is shared.
  */
 #include "../box2d_gb300/csrc/b2g_device_abi.h"
-#include "../box2d_gb300/csrc/device/diff_collide.h"
 
+#include <float.h>
+#include <math.h>
 #include <string.h>
 
 #include <vector>
 
-typedef b2dDual<double, 1> T1;
-typedef b2dVec2<T1> V1;
-typedef b2dRot<T1> R1;
-
-static inline T1 t_c( float x ) { return T1::make( x ); }
-static inline T1 t_v( float x, double d )
+/* ---- dual numbers: the float value as the step computes it, one double tangent ----
+   Every value operation is the plain float operation in the order the expression is
+   written (this file is compiled with -ffp-contract=off), so the value of a computation
+   equals the step's float result bit for bit; the tangent follows the chain rule in
+   double. */
+struct T1
 {
-	T1 r = T1::make( x );
+	float v;
+	double d[1];
+	static T1 make( float x )
+	{
+		T1 r;
+		r.v = x;
+		r.d[0] = 0.0;
+		return r;
+	}
+};
+
+static inline T1 t_num( float v, double d )
+{
+	T1 r;
+	r.v = v;
 	r.d[0] = d;
 	return r;
 }
-static inline V1 t_vec( b2Vec2 a ) { return b2dV( t_c( a.x ), t_c( a.y ) ); }
+static inline T1 operator+( const T1& a, const T1& b ) { return t_num( a.v + b.v, a.d[0] + b.d[0] ); }
+static inline T1 operator-( const T1& a, const T1& b ) { return t_num( a.v - b.v, a.d[0] - b.d[0] ); }
+static inline T1 operator-( const T1& a ) { return t_num( -a.v, -a.d[0] ); }
+static inline T1 operator*( const T1& a, const T1& b )
+{
+	return t_num( a.v * b.v, a.d[0] * (double)b.v + (double)a.v * b.d[0] );
+}
+static inline T1 operator/( const T1& a, const T1& b )
+{
+	float q = a.v / b.v;
+	return t_num( q, ( a.d[0] - (double)q * b.d[0] ) / (double)b.v );
+}
+static inline T1 operator+( float a, const T1& b ) { return t_num( a + b.v, b.d[0] ); }
+static inline T1 operator+( const T1& a, float b ) { return t_num( a.v + b, a.d[0] ); }
+static inline T1 operator-( float a, const T1& b ) { return t_num( a - b.v, -b.d[0] ); }
+static inline T1 operator-( const T1& a, float b ) { return t_num( a.v - b, a.d[0] ); }
+static inline T1 operator*( float a, const T1& b ) { return t_num( a * b.v, (double)a * b.d[0] ); }
+static inline T1 operator*( const T1& a, float b ) { return t_num( a.v * b, a.d[0] * (double)b ); }
+static inline T1 operator/( float a, const T1& b )
+{
+	float q = a / b.v;
+	return t_num( q, -(double)q * b.d[0] / (double)b.v );
+}
+static inline T1 operator/( const T1& a, float b ) { return t_num( a.v / b, a.d[0] / (double)b ); }
+static inline T1 t_sqrt( const T1& a )
+{
+	float r = sqrtf( a.v );
+	return t_num( r, r > 0.0f ? a.d[0] / ( 2.0 * (double)r ) : 0.0 );
+}
+
+struct V1
+{
+	T1 x, y;
+};
+struct R1
+{
+	T1 c, s;
+};
+struct t_xf
+{
+	V1 p;
+	R1 q;
+};
+
+static inline T1 t_c( float x ) { return T1::make( x ); }
+static inline T1 t_v( float x, double d ) { return t_num( x, d ); }
+static inline V1 t_v2( T1 x, T1 y )
+{
+	V1 r = { x, y };
+	return r;
+}
+static inline V1 t_vec( b2Vec2 a ) { return t_v2( t_c( a.x ), t_c( a.y ) ); }
+static inline V1 t_add( V1 a, V1 b ) { return t_v2( a.x + b.x, a.y + b.y ); }
+static inline V1 t_sub( V1 a, V1 b ) { return t_v2( a.x - b.x, a.y - b.y ); }
+static inline T1 t_dot( V1 a, V1 b ) { return a.x * b.x + a.y * b.y; }
+static inline T1 t_cross( V1 a, V1 b ) { return a.x * b.y - a.y * b.x; }
+/* math_functions.h b2RotateVector, b2InvRotateVector, b2InvMulRot, b2TransformPoint, b2Lerp */
+static inline V1 t_rotate( R1 q, V1 v ) { return t_v2( q.c * v.x - q.s * v.y, q.s * v.x + q.c * v.y ); }
+static inline V1 t_invRotate( R1 q, V1 v ) { return t_v2( q.c * v.x + q.s * v.y, -q.s * v.x + q.c * v.y ); }
+static inline R1 t_invMulRot( R1 a, R1 b )
+{
+	R1 r = { a.c * b.c + a.s * b.s, a.c * b.s - a.s * b.c };
+	return r;
+}
+static inline V1 t_transformPoint( const t_xf& t, V1 p )
+{
+	return t_v2( ( t.q.c * p.x - t.q.s * p.y ) + t.p.x, ( t.q.s * p.x + t.q.c * p.y ) + t.p.y );
+}
+static inline V1 t_lerp( V1 a, V1 b, float t )
+{
+	return t_v2( ( 1.0f - t ) * a.x + t * b.x, ( 1.0f - t ) * a.y + t * b.y );
+}
+static inline V1 t_lerpT( V1 a, V1 b, T1 t ) { return t_v2( ( 1.0f - t ) * a.x + t * b.x, ( 1.0f - t ) * a.y + t * b.y ); }
+static inline V1 t_mulAdd( V1 a, T1 s, V1 b ) { return t_v2( a.x + s * b.x, a.y + s * b.y ); }
 static inline T1 t_max( const T1& a, const T1& b ) { return a.v > b.v ? a : b; }
 static inline T1 t_min( const T1& a, const T1& b ) { return a.v < b.v ? a : b; }
-static inline T1 t_cross( V1 a, V1 b ) { return a.x * b.y - a.y * b.x; }
+static inline T1 t_clamp( const T1& a, float lo, float hi ) { return a.v < lo ? t_c( lo ) : ( a.v > hi ? t_c( hi ) : a ); }
+
+/* ---- polygon contact in duals (manifold.c:511-1028 b2CollidePolygons with its clip and
+   edge search, contact.c:519-545 and physics_world.c:568-569 for the world anchors) ----
+   Written here for the checker alone: the value path is the reference's float operation
+   order, so the recorded feature ids, edge choices and clip branches come out again, and
+   the tangents are the Jacobian of the manifold with respect to both poses. */
+#define T_LINEAR_SLOP 0.005f
+#define T_SPECULATIVE_DISTANCE ( 4.0f * T_LINEAR_SLOP )
+#define T_MAKE_ID( A, B ) ( (uint16_t)( (uint8_t)( A ) << 8 | (uint8_t)( B ) ) )
+
+struct t_polygon
+{
+	int count;
+	float radius;
+	V1 v[B2_MAX_POLYGON_VERTICES], n[B2_MAX_POLYGON_VERTICES];
+};
+
+struct t_local
+{
+	int count;
+	V1 normal;
+	V1 point[2];
+	T1 separation[2];
+	uint16_t id[2];
+};
+
+/* the contact geometry the solver reads: world normal, anchors relative to the centers of
+   mass, separations and feature ids */
+struct t_geometry
+{
+	int count;
+	V1 normal;
+	V1 anchorA[2], anchorB[2];
+	T1 separation[2];
+	uint16_t id[2];
+};
+
+/* manifold.c:646-682 */
+static T1 t_findMaxSeparation( int* edgeIndex, const t_polygon& poly1, const t_polygon& poly2 )
+{
+	int bestIndex = 0;
+	T1 maxSeparation = t_c( -FLT_MAX );
+	for ( int i = 0; i < poly1.count; ++i )
+	{
+		V1 n = poly1.n[i];
+		V1 v1 = poly1.v[i];
+		T1 si = t_c( FLT_MAX );
+		for ( int j = 0; j < poly2.count; ++j )
+		{
+			T1 sij = t_dot( n, t_sub( poly2.v[j], v1 ) );
+			if ( sij.v < si.v ) si = sij;
+		}
+		if ( si.v > maxSeparation.v )
+		{
+			maxSeparation = si;
+			bestIndex = i;
+		}
+	}
+	*edgeIndex = bestIndex;
+	return maxSeparation;
+}
+
+/* manifold.c:511-643 */
+static t_local t_clipPolygons( const t_polygon& polyA, const t_polygon& polyB, int edgeA, int edgeB, bool flip )
+{
+	t_local m;
+	memset( &m, 0, sizeof( m ) );
+	const t_polygon* poly1 = flip ? &polyB : &polyA;
+	const t_polygon* poly2 = flip ? &polyA : &polyB;
+	int i11 = flip ? edgeB : edgeA;
+	int i12 = i11 + 1 < poly1->count ? i11 + 1 : 0;
+	int i21 = flip ? edgeA : edgeB;
+	int i22 = i21 + 1 < poly2->count ? i21 + 1 : 0;
+	V1 normal = poly1->n[i11];
+	V1 v11 = poly1->v[i11], v12 = poly1->v[i12];
+	V1 v21 = poly2->v[i21], v22 = poly2->v[i22];
+	V1 tangent = t_v2( -1.0f * normal.y, 1.0f * normal.x );
+	T1 lower1 = t_c( 0.0f );
+	T1 upper1 = t_dot( t_sub( v12, v11 ), tangent );
+	T1 upper2 = t_dot( t_sub( v21, v11 ), tangent );
+	T1 lower2 = t_dot( t_sub( v22, v11 ), tangent );
+	if ( upper2.v < lower1.v || upper1.v < lower2.v ) return m;
+	V1 vLower;
+	if ( lower2.v < lower1.v && ( upper2 - lower2 ).v > FLT_EPSILON )
+		vLower = t_lerpT( v22, v21, ( lower1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vLower = v22;
+	V1 vUpper;
+	if ( upper2.v > upper1.v && ( upper2 - lower2 ).v > FLT_EPSILON )
+		vUpper = t_lerpT( v22, v21, ( upper1 - lower2 ) / ( upper2 - lower2 ) );
+	else
+		vUpper = v21;
+	T1 separationLower = t_dot( t_sub( vLower, v11 ), normal );
+	T1 separationUpper = t_dot( t_sub( vUpper, v11 ), normal );
+	float r1 = poly1->radius, r2 = poly2->radius;
+	vLower = t_mulAdd( vLower, 0.5f * ( r1 - r2 - separationLower ), normal );
+	vUpper = t_mulAdd( vUpper, 0.5f * ( r1 - r2 - separationUpper ), normal );
+	float radius = r1 + r2;
+	m.count = 2;
+	if ( flip == false )
+	{
+		m.normal = normal;
+		m.point[0] = vLower;
+		m.separation[0] = separationLower - radius;
+		m.id[0] = T_MAKE_ID( i11, i22 );
+		m.point[1] = vUpper;
+		m.separation[1] = separationUpper - radius;
+		m.id[1] = T_MAKE_ID( i12, i21 );
+	}
+	else
+	{
+		m.normal = t_v2( -normal.x, -normal.y );
+		m.point[0] = vUpper;
+		m.separation[0] = separationUpper - radius;
+		m.id[0] = T_MAKE_ID( i21, i12 );
+		m.point[1] = vLower;
+		m.separation[1] = separationLower - radius;
+		m.id[1] = T_MAKE_ID( i22, i11 );
+	}
+	return m;
+}
+
+/* distance.c:33-106 b2SegmentDistance */
+struct t_segmentDistance
+{
+	T1 fraction1, fraction2, distanceSquared;
+};
+
+static t_segmentDistance t_segDistance( V1 p1, V1 q1, V1 p2, V1 q2 )
+{
+	t_segmentDistance res;
+	V1 d1 = t_sub( q1, p1 ), d2 = t_sub( q2, p2 ), r = t_sub( p1, p2 );
+	T1 dd1 = t_dot( d1, d1 ), dd2 = t_dot( d2, d2 ), rd1 = t_dot( r, d1 ), rd2 = t_dot( r, d2 );
+	const float epsSqr = FLT_EPSILON * FLT_EPSILON;
+	T1 f1 = t_c( 0.0f ), f2 = t_c( 0.0f );
+	if ( dd1.v < epsSqr || dd2.v < epsSqr )
+	{
+		if ( dd1.v >= epsSqr ) f1 = t_clamp( -rd1 / dd1, 0.0f, 1.0f );
+		else if ( dd2.v >= epsSqr ) f2 = t_clamp( rd2 / dd2, 0.0f, 1.0f );
+	}
+	else
+	{
+		T1 d12 = t_dot( d1, d2 );
+		T1 denom = dd1 * dd2 - d12 * d12;
+		if ( denom.v != 0.0f ) f1 = t_clamp( ( d12 * rd2 - rd1 * dd2 ) / denom, 0.0f, 1.0f );
+		f2 = ( d12 * f1 + rd2 ) / dd2;
+		if ( f2.v < 0.0f )
+		{
+			f2 = t_c( 0.0f );
+			f1 = t_clamp( -rd1 / dd1, 0.0f, 1.0f );
+		}
+		else if ( f2.v > 1.0f )
+		{
+			f2 = t_c( 1.0f );
+			f1 = t_clamp( ( d12 - rd1 ) / dd1, 0.0f, 1.0f );
+		}
+	}
+	V1 closest1 = t_mulAdd( p1, f1, d1 );
+	V1 closest2 = t_mulAdd( p2, f2, d2 );
+	V1 dc = t_sub( closest2, closest1 );
+	res.fraction1 = f1;
+	res.fraction2 = f2;
+	res.distanceSquared = dc.x * dc.x + dc.y * dc.y;
+	return res;
+}
+
+/* manifold.c:702-1028, in frame A after the relative transform */
+static t_local t_collidePolygons( const t_polygon& polyA, const t_polygon& polyB, const t_xf& xf )
+{
+	t_local empty;
+	memset( &empty, 0, sizeof( empty ) );
+	V1 origin = polyA.v[0];
+	t_xf xfs = { t_sub( xf.p, origin ), xf.q };
+	t_polygon A, B;
+	A.count = polyA.count;
+	A.radius = polyA.radius;
+	A.v[0] = t_v2( t_c( 0.0f ), t_c( 0.0f ) );
+	A.n[0] = polyA.n[0];
+	for ( int i = 1; i < A.count; ++i )
+	{
+		A.v[i] = t_sub( polyA.v[i], origin );
+		A.n[i] = polyA.n[i];
+	}
+	B.count = polyB.count;
+	B.radius = polyB.radius;
+	for ( int i = 0; i < B.count; ++i )
+	{
+		B.v[i] = t_transformPoint( xfs, polyB.v[i] );
+		B.n[i] = t_rotate( xfs.q, polyB.n[i] );
+	}
+	int edgeA = 0;
+	T1 separationA = t_findMaxSeparation( &edgeA, A, B );
+	int edgeB = 0;
+	T1 separationB = t_findMaxSeparation( &edgeB, B, A );
+	float radius = A.radius + B.radius;
+	if ( separationA.v > T_SPECULATIVE_DISTANCE + radius || separationB.v > T_SPECULATIVE_DISTANCE + radius ) return empty;
+	bool flip;
+	if ( separationA.v >= separationB.v )
+	{
+		flip = false;
+		V1 search = A.n[edgeA];
+		edgeB = 0;
+		float minDot = FLT_MAX;
+		for ( int i = 0; i < B.count; ++i )
+		{
+			float d = t_dot( search, B.n[i] ).v;
+			if ( d < minDot )
+			{
+				minDot = d;
+				edgeB = i;
+			}
+		}
+	}
+	else
+	{
+		flip = true;
+		V1 search = B.n[edgeB];
+		edgeA = 0;
+		float minDot = FLT_MAX;
+		for ( int i = 0; i < A.count; ++i )
+		{
+			float d = t_dot( search, A.n[i] ).v;
+			if ( d < minDot )
+			{
+				minDot = d;
+				edgeA = i;
+			}
+		}
+	}
+	t_local m = empty;
+	if ( separationA.v > 0.1f * T_LINEAR_SLOP || separationB.v > 0.1f * T_LINEAR_SLOP )
+	{
+		int i11 = edgeA, i12 = edgeA + 1 < A.count ? edgeA + 1 : 0;
+		int i21 = edgeB, i22 = edgeB + 1 < B.count ? edgeB + 1 : 0;
+		V1 v11 = A.v[i11], v12 = A.v[i12], v21 = B.v[i21], v22 = B.v[i22];
+		t_segmentDistance res = t_segDistance( v11, v12, v21, v22 );
+		T1 distance = t_sqrt( res.distanceSquared );
+		T1 separation = distance - radius;
+		if ( ( distance - radius ).v > T_SPECULATIVE_DISTANCE ) return m;
+		m = t_clipPolygons( A, B, edgeA, edgeB, flip );
+		float minSeparation = FLT_MAX;
+		for ( int i = 0; i < m.count; ++i ) minSeparation = minSeparation < m.separation[i].v ? minSeparation : m.separation[i].v;
+		if ( ( separation + 0.1f * T_LINEAR_SLOP ).v < minSeparation )
+		{
+			float f1 = res.fraction1.v, f2 = res.fraction2.v;
+			bool hit = ( f1 == 0.0f || f1 == 1.0f ) && ( f2 == 0.0f || f2 == 1.0f );
+			if ( hit )
+			{
+				V1 va = f1 == 0.0f ? v11 : v12;
+				V1 vb = f2 == 0.0f ? v21 : v22;
+				int ia = f1 == 0.0f ? i11 : i12;
+				int ib = f2 == 0.0f ? i21 : i22;
+				V1 normal = t_sub( vb, va );
+				T1 invDistance = 1.0f / distance;
+				normal.x = normal.x * invDistance;
+				normal.y = normal.y * invDistance;
+				V1 c1 = t_mulAdd( va, t_c( A.radius ), normal );
+				V1 c2 = t_mulAdd( vb, t_c( -B.radius ), normal );
+				m.count = 1;
+				m.normal = normal;
+				m.point[0] = t_lerp( c1, c2, 0.5f );
+				m.separation[0] = distance - radius;
+				m.id[0] = T_MAKE_ID( ia, ib );
+			}
+		}
+	}
+	else
+	{
+		m = t_clipPolygons( A, B, edgeA, edgeB, flip );
+	}
+	for ( int i = 0; i < m.count; ++i ) m.point[i] = t_add( m.point[i], origin );
+	return m;
+}
+
+static t_polygon t_polygonOf( const b2gShape* s )
+{
+	t_polygon p;
+	p.count = s->count;
+	p.radius = s->radius;
+	for ( int i = 0; i < s->count; ++i )
+	{
+		p.v[i] = t_vec( s->v[i] );
+		p.n[i] = t_vec( s->n[i] );
+	}
+	return p;
+}
+
+/* contact.c:519-545 and :619-623: the manifold in frame A, then world anchors, then
+   anchors relative to the centers of mass (physics_world.c:568-569) */
+static t_geometry t_polygonContact( const b2gShape* shapeA, const b2gShape* shapeB, const t_xf& xfA, const t_xf& xfB, b2Vec2 lcA,
+								   b2Vec2 lcB )
+{
+	t_xf rel;
+	rel.q = t_invMulRot( xfA.q, xfB.q );
+	rel.p = t_invRotate( xfA.q, t_v2( xfB.p.x - xfA.p.x, xfB.p.y - xfA.p.y ) );
+	t_local local = t_collidePolygons( t_polygonOf( shapeA ), t_polygonOf( shapeB ), rel );
+	t_geometry g;
+	memset( &g, 0, sizeof( g ) );
+	g.count = local.count;
+	g.normal = t_rotate( xfA.q, local.normal );
+	V1 originDelta = t_v2( xfA.p.x - xfB.p.x, xfA.p.y - xfB.p.y );
+	V1 centerOffsetA = t_rotate( xfA.q, t_vec( lcA ) );
+	V1 centerOffsetB = t_rotate( xfB.q, t_vec( lcB ) );
+	for ( int i = 0; i < local.count; ++i )
+	{
+		V1 anchorA = t_rotate( xfA.q, local.point[i] );
+		V1 anchorB = t_add( anchorA, originDelta );
+		g.anchorA[i] = t_sub( anchorA, centerOffsetA );
+		g.anchorB[i] = t_sub( anchorB, centerOffsetB );
+		g.separation[i] = local.separation[i];
+		g.id[i] = local.id[i];
+	}
+	return g;
+}
 
 /* body state of the substep loop */
 struct t_body
@@ -232,7 +638,7 @@ static void t_integratePositions( const b2gStepParams& P, t_body* b )
 	T1 w = ( flags & B2G_LOCK_Z ) ? t_c( 0.0f ) : b->w;
 	if ( ( vx * vx + vy * vy ).v > maxLinearSq )
 	{
-		T1 ratio = maxLinearSpeed / b2dSqrt( vx * vx + vy * vy );
+		T1 ratio = maxLinearSpeed / t_sqrt( vx * vx + vy * vy );
 		vx = ratio * vx;
 		vy = ratio * vy;
 		flags |= B2G_SPEED_CAPPED;
@@ -248,7 +654,7 @@ static void t_integratePositions( const b2gStepParams& P, t_body* b )
 	b->dpy = b->dpy + h * vy;
 	T1 da = h * w;
 	T1 q2c = b->dqc - da * b->dqs, q2s = b->dqs + da * b->dqc;
-	T1 mag = b2dSqrt( q2s * q2s + q2c * q2c );
+	T1 mag = t_sqrt( q2s * q2s + q2c * q2c );
 	T1 inv = mag.v > 0.0f ? 1.0f / mag : t_c( 0.0f );
 	b->dqc = q2c * inv;
 	b->dqs = q2s * inv;
@@ -318,12 +724,12 @@ static t_lane t_prepare( const b2gStepParams& P, const b2gContact* cs, const t_m
 	c.massScale = massScale;
 	c.impulseScale = impulseScale;
 	c.pointCount = m.pointCount;
-	V1 tangent = b2dV( normal.y, -normal.x );
+	V1 tangent = t_v2( normal.y, -normal.x );
 	for ( int p = 0; p < 2; ++p )
 	{
 		if ( p >= m.pointCount )
 		{
-			c.anchorA[p] = b2dV( t_c( 0.0f ), t_c( 0.0f ) );
+			c.anchorA[p] = t_v2( t_c( 0.0f ), t_c( 0.0f ) );
 			c.anchorB[p] = c.anchorA[p];
 			c.baseSeparation[p] = t_c( 0.0f );
 			c.normalImpulse[p] = t_c( 0.0f );
@@ -337,7 +743,7 @@ static t_lane t_prepare( const b2gStepParams& P, const b2gContact* cs, const t_m
 		V1 rA = m.anchorA[p], rB = m.anchorB[p];
 		c.anchorA[p] = rA;
 		c.anchorB[p] = rB;
-		c.baseSeparation[p] = m.separation[p] - b2dDot( b2dSub( rB, rA ), normal );
+		c.baseSeparation[p] = m.separation[p] - t_dot( t_sub( rB, rA ), normal );
 		c.normalImpulse[p] = warmStartScale * m.normalImpulse[p];
 		c.tangentImpulse[p] = warmStartScale * m.tangentImpulse[p];
 		c.totalNormalImpulse[p] = t_c( 0.0f );
@@ -347,9 +753,9 @@ static t_lane t_prepare( const b2gStepParams& P, const b2gContact* cs, const t_m
 		T1 rtA = t_cross( rA, tangent ), rtB = t_cross( rB, tangent );
 		T1 kTangent = mA + mB + iA * rtA * rtA + iB * rtB * rtB;
 		c.tangentMass[p] = kTangent.v > 0.0f ? 1.0f / kTangent : t_c( 0.0f );
-		V1 vrA = b2dV( A.vx - A.w * rA.y, A.vy + A.w * rA.x );
-		V1 vrB = b2dV( B.vx - B.w * rB.y, B.vy + B.w * rB.x );
-		c.relativeVelocity[p] = b2dDot( normal, b2dSub( vrB, vrA ) );
+		V1 vrA = t_v2( A.vx - A.w * rA.y, A.vy + A.w * rA.x );
+		V1 vrB = t_v2( B.vx - B.w * rB.y, B.vy + B.w * rB.x );
+		c.relativeVelocity[p] = t_dot( normal, t_sub( vrB, vrA ) );
 	}
 	return c;
 }
@@ -361,12 +767,12 @@ struct t_pose
 	R1 q;
 };
 
-static b2dXf<T1> t_transform( const t_pose& b, b2Vec2 lc, b2Transform recorded )
+static t_xf t_transform( const t_pose& b, b2Vec2 lc, b2Transform recorded )
 {
-	b2dXf<T1> xf;
+	t_xf xf;
 	xf.q = b.q;
-	V1 off = b2dRotate( b.q, t_vec( lc ) );
-	xf.p = b2dV( b.c.x - off.x, b.c.y - off.y );
+	V1 off = t_rotate( b.q, t_vec( lc ) );
+	xf.p = t_v2( b.c.x - off.x, b.c.y - off.y );
 	/* the primal is the recorded transform (the step stores p, not c - R(q) lc) */
 	xf.p.x.v = recorded.p.x;
 	xf.p.y.v = recorded.p.y;
@@ -434,7 +840,7 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 		for ( int b = 0; b < nb; ++b )
 		{
 			const b2gTapeBody& T = bodies[b];
-			pose[b].c = b2dV( t_v( T.center.x, dC[2 * b] ), t_v( T.center.y, dC[2 * b + 1] ) );
+			pose[b].c = t_v2( t_v( T.center.x, dC[2 * b] ), t_v( T.center.y, dC[2 * b + 1] ) );
 			pose[b].q.c = t_v( T.xf.q.c, dQ[2 * b] );
 			pose[b].q.s = t_v( T.xf.q.s, dQ[2 * b + 1] );
 			if ( T.awakeIndex >= 0 )
@@ -470,26 +876,22 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 				R1 iA = { old.cachedA.c, -old.cachedA.s }, iB = { old.cachedB.c, -old.cachedB.s };
 				R1 dqA = { qA.c * iA.c - qA.s * iA.s, qA.s * iA.c + qA.c * iA.s };
 				R1 dqB = { qB.c * iB.c - qB.s * iB.s, qB.s * iB.c + qB.c * iB.s };
-				V1 dc = b2dV( pose[bB].c.x - pose[bA].c.x, pose[bB].c.y - pose[bA].c.y );
+				V1 dc = t_v2( pose[bB].c.x - pose[bA].c.x, pose[bB].c.y - pose[bA].c.y );
 				for ( int p = 0; p < m.pointCount; ++p )
 				{
-					V1 rA = b2dRotate( dqA, old.anchorA[p] );
-					V1 rB = b2dRotate( dqB, old.anchorB[p] );
-					V1 dp = b2dAdd( dc, b2dSub( rB, rA ) );
-					m.separation[p] = old.baseSeparation[p] + b2dDot( dp, old.normal );
+					V1 rA = t_rotate( dqA, old.anchorA[p] );
+					V1 rB = t_rotate( dqB, old.anchorB[p] );
+					V1 dp = t_add( dc, t_sub( rB, rA ) );
+					m.separation[p] = old.baseSeparation[p] + t_dot( dp, old.normal );
 					if ( t_same( m.separation[p].v, rm.points[p].separation ) == false ) return -2;
 				}
 			}
 			else if ( rm.pointCount > 0 )
 			{
 				if ( shapeA->type != b2_polygonShape || shapeB->type != b2_polygonShape ) return -1;
-				b2dPoly<T1> polyA, polyB;
-				b2dMakePoly( &polyA, &shapeA->v[0].x, &shapeA->n[0].x, shapeA->count, shapeA->radius );
-				b2dMakePoly( &polyB, &shapeB->v[0].x, &shapeB->n[0].x, shapeB->count, shapeB->radius );
-				b2dXf<T1> xfA = t_transform( pose[bA], bodies[bA].localCenter, bodies[bA].xf );
-				b2dXf<T1> xfB = t_transform( pose[bB], bodies[bB].localCenter, bodies[bB].xf );
-				b2dContactGeometry<T1> g = b2dContactManifold( &polyA, &polyB, xfA, xfB, bodies[bA].localCenter.x, bodies[bA].localCenter.y,
-															   bodies[bB].localCenter.x, bodies[bB].localCenter.y );
+				t_xf xfA = t_transform( pose[bA], bodies[bA].localCenter, bodies[bA].xf );
+				t_xf xfB = t_transform( pose[bB], bodies[bB].localCenter, bodies[bB].xf );
+				t_geometry g = t_polygonContact( shapeA, shapeB, xfA, xfB, bodies[bA].localCenter, bodies[bB].localCenter );
 				if ( g.count != rm.pointCount || t_same( g.normal.x.v, rm.normal.x ) == false || t_same( g.normal.y.v, rm.normal.y ) == false )
 					return -2;
 				m.normal = g.normal;
@@ -527,7 +929,7 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 			}
 			/* friction = sqrt(fA fB) (b2MixFriction) */
 			T1 fA = t_v( shapeA->friction, dirFriction[cs->shapeIdA] ), fB = t_v( shapeB->friction, dirFriction[cs->shapeIdB] );
-			T1 friction = b2dSqrt( fA * fB );
+			T1 friction = t_sqrt( fA * fB );
 			if ( t_same( friction.v, cs->friction ) == false ) return -2;
 			man[s] = m;
 			lanes[s] = t_prepare( P, cs, m, friction, v0 );
@@ -608,9 +1010,9 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 		{
 			int b = awakeBody[i];
 			const t_body& s = sb[i];
-			V1 c2 = b2dV( pose[b].c.x + s.dpx, pose[b].c.y + s.dpy );
+			V1 c2 = t_v2( pose[b].c.x + s.dpx, pose[b].c.y + s.dpy );
 			R1 r = { s.dqc * pose[b].q.c - s.dqs * pose[b].q.s, s.dqs * pose[b].q.c + s.dqc * pose[b].q.s };
-			T1 mag = b2dSqrt( r.s * r.s + r.c * r.c );
+			T1 mag = t_sqrt( r.s * r.s + r.c * r.c );
 			T1 inv = mag.v > 0.0f ? 1.0f / mag : t_c( 0.0f );
 			R1 q2 = { r.c * inv, r.s * inv };
 			float t = toi[i];
@@ -618,14 +1020,14 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 			{
 				/* solver.c:495-512 with the recorded fraction: the sweep is relative to the start center */
 				V1 base = pose[b].c;
-				V1 c1 = b2dSub( base, base ), cs2 = b2dSub( c2, base );
-				V1 ct = b2dLerpF( c1, cs2, t );
+				V1 c1 = t_sub( base, base ), cs2 = t_sub( c2, base );
+				V1 ct = t_lerp( c1, cs2, t );
 				float omt = 1.0f - t;
 				R1 qt = { omt * pose[b].q.c + t * q2.c, omt * pose[b].q.s + t * q2.s };
-				T1 m2 = b2dSqrt( qt.s * qt.s + qt.c * qt.c );
+				T1 m2 = t_sqrt( qt.s * qt.s + qt.c * qt.c );
 				T1 i2 = m2.v > 0.0f ? 1.0f / m2 : t_c( 0.0f );
 				q2 = { qt.c * i2, qt.s * i2 };
-				c2 = b2dAdd( base, ct );
+				c2 = t_add( base, ct );
 			}
 			if ( nextBodies != NULL )
 			{
