@@ -150,6 +150,8 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
     if world_size > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    if args.profile_timed:
+        torch.cuda.profiler.start()  # ncu --profile-from-start off captures the timed steps only
     with ClockSampler(dev) as clocks:
         for k in range(args.steps):
             flush.zero_()
@@ -159,6 +161,8 @@ def run_gpu(args, rank: int, world_size: int) -> dict:
             ends[k].record(stream)
             alg_bytes += algorithmic_bytes(scene.counters(), dyn, 4, False)
         torch.cuda.synchronize()
+    if args.profile_timed:
+        torch.cuda.profiler.stop()
     if world_size > 1:
         torch.distributed.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -472,6 +476,8 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="many_pyramids", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-timed", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--worlds", type=int, default=0,
                     help="world count of the batch_worlds (default 4096) and diff_batch (default 1024) workloads")
     ap.add_argument("--threads", type=int, default=0, help="host threads of the batch_worlds workload (0: 4 per core)")

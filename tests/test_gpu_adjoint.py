@@ -4,8 +4,13 @@ of mass to a seeded target. The gradient with respect to the initial velocities 
 shape frictions is checked against
   - the FP64 tangent-linear model of the same recorded steps (oracle/o_tangent.cpp):
     relative error of directional derivatives <= 1e-3;
-  - central finite differences (h = 1e-3) of the forward step over a few steps, where the
-    float32 trajectory is smooth enough for differences to mean something: <= 2e-2.
+  - central finite differences of the forward step: over 2 steps of the stacked boxes
+    (h = 1e-3), <= 2e-2, where contacts switching under the perturbation make differences
+    coarse; and for one box sliding on the ramp over 5 steps (h = 1e-2), a regime smooth
+    enough for differences to resolve the derivative, <= 1e-3.
+
+The tangent-linear checker is independent of the product: its dual numbers and its
+polygon contact Jacobian are its own, restated from the reference.
 """
 from __future__ import annotations
 
@@ -147,6 +152,42 @@ def test_adjoint_matches_finite_differences(gpu_lib):
         lm = functional()
         fd = (lp - lm) / (2 * h)
         assert abs(adjoint - fd) <= 2e-2 * max(abs(fd), 1e-3), (adjoint, fd)
+
+
+def test_adjoint_matches_finite_differences_in_a_smooth_regime(gpu_lib):
+    """One box on the ramp for 5 steps: the perturbation takes no other branch of the step
+    (contact, clip, friction cone), so central differences (h = 1e-2) of the forward step
+    resolve the derivative; the adjoint must match them to 1e-3 along a velocity direction,
+    a velocity-and-friction direction and a linear-velocity-only direction."""
+    batch, _ = _make(gpu_lib, [777], 1, 1)
+    rng = np.random.default_rng(5)
+    steps, h = 5, 1e-2
+    with batch:
+        v0, f0 = batch.velocities(), batch.friction()
+        weights = [rng.standard_normal((s.body_count, 2)).astype(np.float32) * batch.dynamic_masks[w][:, None]
+                   for w, s in enumerate(batch.scenes)]
+
+        def functional():
+            return sum(float((c.astype(np.float64) * wt).sum()) for c, wt in zip(batch.centers(), weights))
+
+        for kind in ("velocity", "velocity and friction", "linear velocity"):
+            du = [rng.standard_normal(v.shape).astype(np.float32) * batch.dynamic_masks[w][:, None] for w, v in enumerate(v0)]
+            if kind == "linear velocity":
+                for d in du:
+                    d[:, 2] = 0.0
+            scale = 1.0 if kind == "velocity and friction" else 0.0
+            df = [rng.standard_normal(f.shape).astype(np.float32) * scale for f in f0]
+            for f in df:
+                f[0] = 0.0
+            _run(batch, v0, f0, steps)
+            gv, _, gf = batch.backward(weights)
+            adjoint = float((gv[0].astype(np.float64) * du[0]).sum() + (gf[0].astype(np.float64) * df[0]).sum())
+            _run(batch, [v + h * d for v, d in zip(v0, du)], [f + h * d for f, d in zip(f0, df)], steps)
+            lp = functional()
+            _run(batch, [v - h * d for v, d in zip(v0, du)], [f - h * d for f, d in zip(f0, df)], steps)
+            lm = functional()
+            fd = (lp - lm) / (2 * h)
+            assert abs(adjoint - fd) <= 1e-3 * abs(fd), (kind, adjoint, fd)
 
 
 def test_torch_autograd_function(gpu_lib):
