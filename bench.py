@@ -62,6 +62,12 @@ WORKLOADS = {
 }
 
 
+# DRAM bytes (read + write) per step of the solver-stage kernels (component analysis, bins,
+# cluster assignment, cluster solve) in the timed window, from one ncu capture of each
+# workload's timed steps (profiles/solver_traffic_timed_steps.md: command and per-kernel split)
+SOLVER_TRAFFIC = {"many_pyramids": 43.21e6, "large_pyramid": 3.48e6, "joint_grid": 18.33e6}
+
+
 def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -635,7 +641,9 @@ def main() -> None:
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene builders)", "config": config,
         "roofline": {"bound": "hbm", "kernel": "solver (prepare..store)", "achieved": r["achieved_gbs"],
                      "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": r["achieved_gbs"] / pk["hbm_gbs"],
-                     "peak_source": pk["source"], "traffic": None,
+                     "peak_source": pk["source"], "traffic": SOLVER_TRAFFIC.get(args.workload),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the solver-stage kernels per "
+                                       "step, timed steps (profiles/solver_traffic_timed_steps.md)",
                      "alg_bytes_per_step": r["alg_bytes"] / args.steps,
                      "solver_ms_per_step": r["solver_ms"] / args.steps},
         "cpu_baseline": cpu,
