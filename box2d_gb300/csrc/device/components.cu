@@ -15,6 +15,7 @@
 
 #include <pthread.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #define B2G_COMP_THREADS 256
@@ -168,7 +169,20 @@ __global__ void k_compCountCons( d_solveArgs a, const int* awakeIndex, int* comp
 	d_warpCountAdd( compData + CD_STRIDE * r + ( i < total ? 1 : 2 ) );
 }
 
-__global__ void k_compAssign( int* compData, int* binRange, int binCap, b2gCompSummary* summary, int n, int forceBig )
+extern "C" int b2gBinCapBytes( void )
+{
+	static int cap = 0;
+	if ( cap == 0 )
+	{
+		const char* e = getenv( "B2G_BIN_CAP_KB" );
+		int kb = e != NULL ? atoi( e ) : 0;
+		cap = kb >= 16 && kb <= 100 ? kb * 1024 : B2G_BIN_CAP_BYTES;
+	}
+	return cap;
+}
+
+__global__ void k_compAssign( int* compData, int* binRange, int binCap, b2gCompSummary* summary, int n, int forceBig,
+							  long long capBytes )
 {
 	int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if ( i >= n ) return;
@@ -177,7 +191,7 @@ __global__ void k_compAssign( int* compData, int* binRange, int binCap, b2gCompS
 	int nb = cd[0], nc = cd[1], nj = cd[2];
 	long long weight = (long long)B2G_BIN_BODY_BYTES * nb + (long long)B2G_BIN_CONTACT_BYTES * nc +
 					   (long long)B2G_BIN_JOINT_BYTES * nj;
-	if ( forceBig || weight > B2G_BIN_CAP_BYTES )
+	if ( forceBig || weight > capBytes )
 	{
 		cd[CD_BIN] = -1;
 		atomicAdd( &summary->bigComponents, 1 );
@@ -195,7 +209,7 @@ __global__ void k_compAssign( int* compData, int* binRange, int binCap, b2gCompS
 	cd[CD_OFFSET + 2] = jo;
 	long long start = (long long)B2G_BIN_BODY_BYTES * bo + (long long)B2G_BIN_CONTACT_BYTES * co +
 					  (long long)B2G_BIN_JOINT_BYTES * jo;
-	int bin = (int)( start / B2G_BIN_CAP_BYTES );
+	int bin = (int)( start / capBytes );
 	cd[CD_BIN] = bin;
 	int* begin = binRange;
 	int* end = binRange + 3 * binCap;
@@ -613,7 +627,7 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 	if ( rc ) return rc;
 	long long upper = (long long)B2G_BIN_BODY_BYTES * n + (long long)B2G_BIN_CONTACT_BYTES * total +
 					  (long long)B2G_BIN_JOINT_BYTES * jointTotal;
-	int bins = (int)( upper / B2G_BIN_CAP_BYTES ) + 2;
+	int bins = (int)( upper / b2gBinCapBytes() ) + 2;
 	if ( bins > b->binCap || b->binRange == NULL )
 	{
 		rc = growPair( &b->binRange, NULL, &b->binCap, bins, 6 );
@@ -675,7 +689,8 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 		k_compCountCons<<<compBlocks( cons ), B2G_COMP_THREADS, 0, stream>>>( *a, awakeIndex, b->compData, total, cons );
 		*launches += 1;
 	}
-	k_compAssign<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->compData, b->binRange, b->binCap, b->summary, n, forceBig );
+	k_compAssign<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->compData, b->binRange, b->binCap, b->summary, n, forceBig,
+													  (long long)b2gBinCapBytes() );
 	*launches += 1;
 	CKC( cudaGetLastError() );
 	/* the lists now, so the summary read below carries the big components' per-color counts */
@@ -704,7 +719,7 @@ extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, co
 									 long long* launches )
 {
 	static pthread_once_t s_once = PTHREAD_ONCE_INIT;
-	const int smemBytes = 2 * B2G_BIN_CAP_BYTES;
+	const int smemBytes = 2 * b2gBinCapBytes();
 	pthread_once( &s_once, configureBins );
 	CKC( s_binsConfigured );
 	d_compArgs c = compArgs( b, jointOffsets, b->awakeIndex );
@@ -713,7 +728,7 @@ extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, co
 	long long co = (long long)( ( cur >> B2G_CURSOR_JOINT_BITS ) & ( ( 1ull << B2G_CURSOR_CONTACT_BITS ) - 1 ) );
 	long long jo = (long long)( cur & ( ( 1ull << B2G_CURSOR_JOINT_BITS ) - 1 ) );
 	long long weight = B2G_BIN_BODY_BYTES * bo + B2G_BIN_CONTACT_BYTES * co + B2G_BIN_JOINT_BYTES * jo;
-	int bins = (int)( weight / B2G_BIN_CAP_BYTES ) + 1;
+	int bins = (int)( weight / b2gBinCapBytes() ) + 1;
 	if ( bins > b->binCap ) bins = b->binCap;
 	k_solveBins<<<bins, B2G_BIN_THREADS, smemBytes, stream>>>( *a, c, *jb, counters, smemBytes );
 	*launches += 1;

@@ -23,8 +23,10 @@
 #define B2G_BIN_BODY_BYTES 32
 #define B2G_BIN_CONTACT_BYTES ( (int)sizeof( b2gContactLane ) + 4 )
 #define B2G_BIN_JOINT_BYTES ( (int)sizeof( b2gJoint ) + 4 )
-/* a component heavier than this is solved on the global path; a bin holds less than twice it */
+/* a component heavier than the bin cap is solved on the global path; a bin holds less than
+   twice it. The cap is B2G_BIN_CAP_BYTES unless B2G_BIN_CAP_KB (16 to 100) overrides it. */
 #define B2G_BIN_CAP_BYTES ( 40 * 1024 )
+extern "C" int b2gBinCapBytes( void );
 /* a whole world up to this weight is solved by one CTA without component analysis */
 #define B2G_WORLD_BIN_MAX_BYTES ( 200 * 1024 )
 /* field widths of the packed (bodies, contacts, joints) allocation cursor */
