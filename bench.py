@@ -246,6 +246,7 @@ def run_batch(args) -> dict:
     lib.b2s_step_batch(handles, n, dt, 4, args.warmup, threads)
     for s in scenes:
         s.timings(reset=True)
+        s.host_profile(reset=True)
     prof = np.zeros(17, np.float32)
     lib.b2p_batch_profile(prof.ctypes.data, 1)
     launches0 = float(prof[5])
@@ -262,6 +263,13 @@ def run_batch(args) -> dict:
         h2d += int(traffic[0])
         d2h += int(traffic[1])
     launches = int(prof[5] - launches0)
+    # host time of the step's phases summed over the worlds (thread time, not wall time)
+    host_cpu = np.zeros(10, np.float64)
+    for s in scenes:
+        host_cpu += s.host_profile(reset=True)
+    host_cpu_ms = {k: float(v) / args.steps for k, v in zip(
+        ["tree_upload", "pair_query", "contact_create", "tree_rebuild", "narrowphase", "state_pass", "uploads",
+         "solver", "enlarge"], host_cpu)}
     profile = {k: float(v) / args.steps for k, v in
                zip(["begin", "pairs", "collide", "finish", "flush", "_", "flush_assembly", "flush_wait", "_", "_", "_", "_",
                        "flush_plan", "flush_layout", "flush_stage", "flush_issue", "flush_deliver"], prof) if k != "_"}
@@ -278,7 +286,7 @@ def run_batch(args) -> dict:
         s.close()
     return {"dyn": dyn, "batch_s": batch_s, "plain_s": plain_s, "plain_steps": plain_steps, "threads": threads,
             "launches": launches, "h2d": h2d / args.steps, "d2h": d2h / args.steps, "clocks": clocks.summary,
-            "e2e_value": dyn * e2e_steps / e2e_s, "profile": profile, "states": states}
+            "e2e_value": dyn * e2e_steps / e2e_s, "profile": profile, "states": states, "host_cpu_ms": host_cpu_ms}
 
 
 def run_diff(args) -> dict:
@@ -600,7 +608,7 @@ def main() -> None:
             "e2e": {"value": r["e2e_value"], "unit": "body-steps/s", "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "read": "every world's move events after every batched step"},
             "gpu_launches": r["launches"], "clocks": r["clocks"],
-            "batch_ms_per_step": r["profile"],
+            "batch_ms_per_step": r["profile"], "host_cpu_ms_per_step": r["host_cpu_ms"],
         }
         print(json.dumps(line))
         return

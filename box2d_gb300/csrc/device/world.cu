@@ -278,11 +278,22 @@ struct b2gDeviceWorld
 		if ( e_ != cudaSuccess ) return (int)e_;                                                                                 \
 	} while ( 0 )
 
+/* capacity for `need` elements with room to grow: allocations (cudaMalloc, cudaMallocHost)
+   take a process-wide lock and cost far more than the step's own work, so a buffer that
+   grows gets twice what it needs */
+static int growCapacity( int cap, int need )
+{
+	int nc = cap > 0 ? cap : 64;
+	long long target = 2LL * need;
+	if ( target > 0x7fffffffLL ) target = need;
+	while ( nc < target && nc < 0x40000000 ) nc *= 2;
+	return nc < need ? need : nc;
+}
+
 static int grow( b2gDeviceWorld* dw, void** ptr, int* cap, int need, size_t elem )
 {
 	if ( need <= *cap && *ptr != NULL ) return 0;
-	int nc = *cap > 0 ? *cap : 64;
-	while ( nc < need ) nc *= 2;
+	int nc = growCapacity( *cap, need );
 	void* p = NULL;
 	CK( cudaMalloc( &p, (size_t)nc * elem ) );
 	CK( cudaMemset( p, 0, (size_t)nc * elem ) );
@@ -318,8 +329,7 @@ static int grow( b2gDeviceWorld* dw, void** ptr, int* cap, int need, size_t elem
 static int growHost( void** ptr, int* cap, int need, size_t elem )
 {
 	if ( need <= *cap && *ptr != NULL ) return 0;
-	int nc = *cap > 0 ? *cap : 64;
-	while ( nc < need ) nc *= 2;
+	int nc = growCapacity( *cap, need );
 	void* p = NULL;
 	CK( cudaMallocHost( &p, (size_t)nc * elem ) );
 	if ( *ptr != NULL )
@@ -2510,8 +2520,9 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	if ( dw->recWindow < 64 ) dw->recWindow = 64;
 	if ( dw->defer ) dw->recWindow = shapeTotal > 64 ? shapeTotal : 64;
 	int recWindow = dw->recWindow < shapeTotal ? dw->recWindow : shapeTotal;
-	CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( int ) ) );
-	CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * ( recWindow > 0 ? recWindow : 1 ), sizeof( float ) ) );
+	/* staging for every shape's record, so that a larger count later needs no allocation */
+	CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hBoxesRaw, &dw->hBoxesRawCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( float ) ) );
 	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
 	if ( recWindow > 0 )
 	{
