@@ -1939,8 +1939,9 @@ static int findPairsIssue( b2gDeviceWorld* dw, int n )
 {
 	CK2( grow( dw, (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
 	CK2( grow( dw, (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
-	/* recorded work reads everything back: a second wait would cost a flush */
-	if ( dw->defer ) dw->pairWindow = n * dw->pairPerMove;
+	/* the window follows the last count; recorded work (a batched flush) reads back twice
+	   that, and a world whose count still exceeds it copies the rest alone after the flush */
+	if ( dw->defer && dw->pairWindow < n * dw->pairPerMove ) dw->pairWindow = 2 * dw->pairWindow;
 	int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
 	CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * window, sizeof( int ) ) );
 	CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
@@ -2090,7 +2091,7 @@ extern "C" int b2gDev_CollideIssue( b2gDeviceWorld* dw, const b2gStepParams* p, 
 		dev_event( dw, dw->ev[3] );
 	}
 	if ( dw->changeWindow < 64 ) dw->changeWindow = 64;
-	if ( dw->defer ) dw->changeWindow = contactIdCapacity > 64 ? contactIdCapacity : 64;
+	if ( dw->defer && dw->changeWindow < contactIdCapacity ) dw->changeWindow = 2 * dw->changeWindow;
 	int window = dw->changeWindow < contactIdCapacity ? dw->changeWindow : contactIdCapacity;
 	CK2( growHost( (void**)&dw->hChanges, &dw->hChangesCap, 2 * ( window > 0 ? window : 1 ), sizeof( int ) ) );
 	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
@@ -2518,7 +2519,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	}
 	/* the counters and the first `window` enlarged-proxy records come back in one wait */
 	if ( dw->recWindow < 64 ) dw->recWindow = 64;
-	if ( dw->defer ) dw->recWindow = shapeTotal > 64 ? shapeTotal : 64;
+	if ( dw->defer && dw->recWindow < shapeTotal ) dw->recWindow = 2 * dw->recWindow;
 	int recWindow = dw->recWindow < shapeTotal ? dw->recWindow : shapeTotal;
 	/* staging for every shape's record, so that a larger count later needs no allocation */
 	CK2( growHost( (void**)&dw->hRecsRaw, &dw->hRecsRawCap, 4 * ( shapeTotal > 0 ? shapeTotal : 1 ), sizeof( int ) ) );
