@@ -85,6 +85,7 @@ typedef struct b2gShape
 	b2Vec2 ccdCentroid;
 	float ccdCoreRadius;
 	int enableSensorEvents; /* the shape is seen by sensors (and a sensor reports events) */
+	int proxyKey;			/* its broadphase proxy (proxy id << 2 | tree), -1 = none */
 } b2gShape;
 
 /* contact record (contact.h:103-142 b2ContactSim without ids kept on the host) */
@@ -377,6 +378,13 @@ typedef struct b2gHostTreeNode
    device. The host array must stay unchanged until the next pair query returns. */
 int b2gDev_UploadTree( b2gDeviceWorld* dw, int treeType, const b2gHostTreeNode* nodes, int nodeCount, int root,
 					   int hostPinned );
+/* the proxy enlargement of the last solve applied to the device's copies of the kinematic
+   and dynamic trees (the first `recordCount` enlarged-proxy records); the device copies must
+   hold the trees as the host left them before its own enlargement. Records an event after
+   the trees' uploads, which b2gDev_WaitTreeUploads waits for (the host node arrays may then
+   change). */
+int b2gDev_EnlargeTrees( b2gDeviceWorld* dw, int recordCount );
+int b2gDev_WaitTreeUploads( b2gDeviceWorld* dw );
 /* waits of this world block the calling thread (sleep) instead of spinning */
 void b2gDev_SetBlockingSync( b2gDeviceWorld* dw, int on );
 

@@ -201,6 +201,7 @@ struct b2gDeviceWorld
 	int recWindow;	  /* enlarged-proxy records copied back with the counters */
 	int pairsTimingPending;
 	cudaEvent_t syncEvent; /* blocking-sync event for waits of batched steps */
+	cudaEvent_t treeEvent; /* after the tree uploads that precede a device enlargement */
 	int blockingSync;
 	/* bullet pass: bullet body slots in, shape records out */
 	int* bulletSims;
@@ -1072,6 +1073,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 		if ( hptrs[i] ) cudaFreeHost( hptrs[i] );
 	free( dw->hSortTmp );
 	for ( int i = 0; i < 10; ++i ) cudaEventDestroy( dw->ev[i] );
+	if ( dw->treeEvent ) cudaEventDestroy( dw->treeEvent );
 	cudaStreamDestroy( dw->stream );
 	for ( void* r : dw->retired ) cudaFree( r );
 	delete dw->defer;
@@ -1892,6 +1894,87 @@ extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gHostTre
 	CK2( grow( dw, (void**)&dw->moved[type], &mc, need, 1 ) );
 	dw->movedCap[type] = mc;
 	dw->treeRoot[type] = root;
+	return 0;
+}
+
+/* grow a device tree node's box by `b` with atomic min / max (the result does not depend on
+   the order of the threads); returns whether it changed */
+static __device__ bool d_atomicLowerF( float* p, float v )
+{
+	int* ip = (int*)p;
+	int cur = *(volatile int*)ip;
+	while ( v < __int_as_float( cur ) )
+	{
+		int prev = atomicCAS( ip, cur, __float_as_int( v ) );
+		if ( prev == cur ) return true;
+		cur = prev;
+	}
+	return false;
+}
+
+static __device__ bool d_atomicRaiseF( float* p, float v )
+{
+	int* ip = (int*)p;
+	int cur = *(volatile int*)ip;
+	while ( __int_as_float( cur ) < v )
+	{
+		int prev = atomicCAS( ip, cur, __float_as_int( v ) );
+		if ( prev == cur ) return true;
+		cur = prev;
+	}
+	return false;
+}
+
+/* dynamic_tree.c:798-837 on the device's query trees: each enlarged proxy's leaf takes its
+   fat box and its ancestors grow until one already holds it. Every ancestor ends with its
+   old box grown by the new boxes of the enlarged leaves below it, as the host's serial
+   enlargement leaves it (the flags the host also sets are of no use to the queries). */
+__global__ void k_enlargeTrees( const int* __restrict__ recs, const float4* __restrict__ boxes, int n,
+								const b2gShape* __restrict__ shapes, b2gTreeNode* kinematicTree, b2gTreeNode* dynamicTree,
+								const b2gHostTreeNode* __restrict__ kinematicRaw, const b2gHostTreeNode* __restrict__ dynamicRaw )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= n ) return;
+	const int* r = recs + 4 * i;
+	if ( r[2] == 0 || r[3] != 0 ) return; /* not enlarged, or a fast bullet (the bullet pass handles it) */
+	int key = shapes[r[1]].proxyKey;
+	if ( key < 0 ) return;
+	int type = key & 3, id = key >> 2;
+	if ( type != b2_kinematicBody && type != b2_dynamicBody ) return;
+	b2gTreeNode* tree = type == b2_dynamicBody ? dynamicTree : kinematicTree;
+	const b2gHostTreeNode* raw = type == b2_dynamicBody ? dynamicRaw : kinematicRaw;
+	float4 f = boxes[i];
+	tree[id].aabb.lowerBound.x = f.x;
+	tree[id].aabb.lowerBound.y = f.y;
+	tree[id].aabb.upperBound.x = f.z;
+	tree[id].aabb.upperBound.y = f.w;
+	for ( int p = raw[id].parent; p >= 0; p = raw[p].parent )
+	{
+		b2AABB* box = &tree[p].aabb;
+		bool changed = d_atomicLowerF( &box->lowerBound.x, f.x );
+		changed = d_atomicLowerF( &box->lowerBound.y, f.y ) || changed;
+		changed = d_atomicRaiseF( &box->upperBound.x, f.z ) || changed;
+		changed = d_atomicRaiseF( &box->upperBound.y, f.w ) || changed;
+		if ( changed == false ) break;
+	}
+}
+
+extern "C" int b2gDev_EnlargeTrees( b2gDeviceWorld* dw, int recordCount )
+{
+	if ( dw->treeEvent == NULL ) CK( cudaEventCreateWithFlags( &dw->treeEvent, cudaEventDisableTiming ) );
+	CK( cudaEventRecord( dw->treeEvent, dw->stream ) );
+	int n = recordCount < dw->enlargedCap / 4 ? recordCount : dw->enlargedCap / 4;
+	if ( n <= 0 || dw->tree[b2_dynamicBody] == NULL || dw->treeRaw[b2_dynamicBody] == NULL ) return 0;
+	k_enlargeTrees<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->enlargedRecs, dw->enlargedBoxes, n, dw->shapes,
+																   dw->tree[b2_kinematicBody], dw->tree[b2_dynamicBody],
+																   dw->treeRaw[b2_kinematicBody], dw->treeRaw[b2_dynamicBody] );
+	dw->launches += 1;
+	return (int)cudaGetLastError();
+}
+
+extern "C" int b2gDev_WaitTreeUploads( b2gDeviceWorld* dw )
+{
+	if ( dw->treeEvent != NULL ) CK( cudaEventSynchronize( dw->treeEvent ) );
 	return 0;
 }
 

@@ -335,6 +335,8 @@ int h_treeCreateProxy( h_tree* t, b2AABB aabb, uint64_t categoryBits, uint64_t u
 void h_treeDestroyProxy( h_tree* t, int proxyId );
 void h_treeMoveProxy( h_tree* t, int proxyId, b2AABB aabb );
 void h_treeEnlargeProxy( h_tree* t, int proxyId, b2AABB aabb );
+/* h_treeEnlargeProxy of each proxy in turn, without touching the version (the caller bumps it) */
+void h_treeEnlargeProxies( h_tree* t, const int* proxyIds, const b2AABB* boxes, int count );
 /* h_treeEnlargeProxy for threads that enlarge different proxies of one tree at once (the
    result is that of the enlargements one after another); the caller bumps the version */
 void h_treeEnlargeProxyShared( h_tree* t, int proxyId, b2AABB aabb );

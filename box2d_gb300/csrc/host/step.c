@@ -28,14 +28,20 @@ static void h_lap( h_world* w, int phase, uint64_t* t )
 /* The partial tree rebuild after the pair query (b2UpdateTreesTask, broad_phase.c:401-410)
    touches only the trees, which nothing else uses until the proxies are enlarged at the
    end of the solve. The reference runs it as a task beside the narrowphase; here a
-   per-world host thread runs it while the device does the narrowphase and the solver. */
+   per-world host thread runs it while the device does the narrowphase and the solver.
+   The same thread applies the step's proxy enlargement to the host trees after the step
+   (the device enlarges its own copies, so the next pair query does not wait for it); its
+   jobs run in the order they were posted. */
 typedef struct h_rebuildWorker
 {
 	pthread_t thread;
 	pthread_mutex_t mu;
 	pthread_cond_t cv;
-	int pending, busy, quit;
+	int rebuildPending, enlargePending, busy, quit;
 	h_world* w;
+	/* the enlargement to apply: proxy ids and fat boxes, [0] kinematic tree, [1] dynamic */
+	h_intArray enlargeIds[2];
+	H_ARRAY( b2AABB ) enlargeBoxes[2];
 } h_rebuildWorker;
 
 static void h_rebuildTrees( h_world* w )
@@ -50,53 +56,77 @@ static void* h_rebuildMain( void* arg )
 	pthread_mutex_lock( &k->mu );
 	for ( ;; )
 	{
-		while ( k->pending == 0 && k->quit == 0 ) pthread_cond_wait( &k->cv, &k->mu );
+		while ( k->rebuildPending == 0 && k->enlargePending == 0 && k->quit == 0 ) pthread_cond_wait( &k->cv, &k->mu );
 		if ( k->quit ) break;
-		k->pending = 0;
-		pthread_mutex_unlock( &k->mu );
-		h_rebuildTrees( k->w );
-		pthread_mutex_lock( &k->mu );
-		k->busy = 0;
-		pthread_cond_broadcast( &k->cv );
+		if ( k->enlargePending )
+		{
+			k->enlargePending = 0;
+			pthread_mutex_unlock( &k->mu );
+			/* the device has copied the node arrays before they change */
+			int rc = b2gDev_WaitTreeUploads( k->w->dev );
+			if ( rc != 0 ) h_fail( k->w, "tree upload", rc );
+			h_treeEnlargeProxies( k->w->trees + b2_kinematicBody, k->enlargeIds[0].data, k->enlargeBoxes[0].data,
+								  k->enlargeIds[0].count );
+			h_treeEnlargeProxies( k->w->trees + b2_dynamicBody, k->enlargeIds[1].data, k->enlargeBoxes[1].data,
+								  k->enlargeIds[1].count );
+			pthread_mutex_lock( &k->mu );
+		}
+		else
+		{
+			k->rebuildPending = 0;
+			pthread_mutex_unlock( &k->mu );
+			h_rebuildTrees( k->w );
+			pthread_mutex_lock( &k->mu );
+		}
+		if ( k->rebuildPending == 0 && k->enlargePending == 0 )
+		{
+			k->busy = 0;
+			pthread_cond_broadcast( &k->cv );
+		}
 	}
 	pthread_mutex_unlock( &k->mu );
 	return NULL;
 }
 
-/* run the rebuild on the world's worker thread (started on first use); small trees are
-   rebuilt inline */
+/* the world's worker thread, started on first use; NULL if it cannot start */
+static h_rebuildWorker* h_startWorker( h_world* w )
+{
+	h_rebuildWorker* k = w->rebuildWorker;
+	if ( k != NULL ) return k;
+	k = calloc( 1, sizeof( h_rebuildWorker ) );
+	k->w = w;
+	pthread_mutex_init( &k->mu, NULL );
+	pthread_cond_init( &k->cv, NULL );
+	if ( pthread_create( &k->thread, NULL, h_rebuildMain, k ) != 0 )
+	{
+		pthread_mutex_destroy( &k->mu );
+		pthread_cond_destroy( &k->cv );
+		free( k );
+		return NULL;
+	}
+	w->rebuildWorker = k;
+	return k;
+}
+
+/* run the rebuild on the world's worker thread; small trees without a worker are rebuilt
+   inline */
 static void h_postRebuild( h_world* w )
 {
-	if ( w->trees[b2_dynamicBody].proxyCount < 2048 )
+	h_rebuildWorker* k = w->rebuildWorker;
+	if ( k == NULL && w->trees[b2_dynamicBody].proxyCount >= 2048 ) k = h_startWorker( w );
+	if ( k == NULL )
 	{
 		h_rebuildTrees( w );
 		return;
 	}
-	h_rebuildWorker* k = w->rebuildWorker;
-	if ( k == NULL )
-	{
-		k = calloc( 1, sizeof( h_rebuildWorker ) );
-		k->w = w;
-		pthread_mutex_init( &k->mu, NULL );
-		pthread_cond_init( &k->cv, NULL );
-		if ( pthread_create( &k->thread, NULL, h_rebuildMain, k ) != 0 )
-		{
-			pthread_mutex_destroy( &k->mu );
-			pthread_cond_destroy( &k->cv );
-			free( k );
-			h_rebuildTrees( w );
-			return;
-		}
-		w->rebuildWorker = k;
-	}
 	pthread_mutex_lock( &k->mu );
-	k->pending = 1;
+	k->rebuildPending = 1;
 	k->busy = 1;
 	pthread_cond_broadcast( &k->cv );
 	pthread_mutex_unlock( &k->mu );
 }
 
-/* wait for a posted rebuild; the trees are the main thread's again afterwards */
+/* wait for the posted jobs; the trees are the main thread's again afterwards */
 void h_joinRebuild( h_world* w )
 {
 	h_rebuildWorker* k = w->rebuildWorker;
@@ -118,6 +148,11 @@ void h_stopRebuildWorker( h_world* w )
 	pthread_join( k->thread, NULL );
 	pthread_mutex_destroy( &k->mu );
 	pthread_cond_destroy( &k->cv );
+	for ( int i = 0; i < 2; ++i )
+	{
+		h_free( k->enlargeIds[i] );
+		h_free( k->enlargeBoxes[i] );
+	}
 	free( k );
 	w->rebuildWorker = NULL;
 }
@@ -162,14 +197,17 @@ static int h_pairsIssue( h_world* w )
 	int* shapeIds = malloc( (size_t)moveCount * sizeof( int ) );
 	for ( int i = 0; i < moveCount; ++i )
 	{
+		/* a leaf's box is its shape's fat box; the shape's copy is read because the worker
+		   may still be enlarging the host tree after the last step */
 		int key = w->moveArray.data[i];
 		const h_tree* tree = w->trees + H_PROXY_TYPE( key );
-		const h_treeNode* node = tree->nodes + H_PROXY_ID( key );
-		boxes[4 * i] = node->aabb.lowerBound.x;
-		boxes[4 * i + 1] = node->aabb.lowerBound.y;
-		boxes[4 * i + 2] = node->aabb.upperBound.x;
-		boxes[4 * i + 3] = node->aabb.upperBound.y;
-		shapeIds[i] = (int)node->userData;
+		int shapeId = (int)tree->nodes[H_PROXY_ID( key )].userData;
+		const b2AABB fat = w->shapes.data[shapeId].fatAABB;
+		boxes[4 * i] = fat.lowerBound.x;
+		boxes[4 * i + 1] = fat.lowerBound.y;
+		boxes[4 * i + 2] = fat.upperBound.x;
+		boxes[4 * i + 3] = fat.upperBound.y;
+		shapeIds[i] = shapeId;
 	}
 	int rc = b2gDev_FindPairsIssue( w->dev, w->moveArray.data, boxes, shapeIds, moveCount );
 	free( boxes );
@@ -410,8 +448,63 @@ static void h_enlargeChunk( void* ctx, int chunk )
 	}
 }
 
+/* The enlargement split between the device and the worker: the trees as the rebuild left
+   them go to the device, which enlarges its copies at once (order-independent, so equal to
+   the host's serial enlargement); the move buffer is built here in record order; the host
+   trees are enlarged by the worker while the next step's pair query runs. Returns 0 when
+   the world has no worker or its device work is being recorded (a batched step). */
+static int h_enlargeOnDevice( h_world* w, const int* recs, const float* boxes, int count )
+{
+	h_rebuildWorker* k = w->rebuildWorker;
+	if ( k == NULL || b2gDev_IsRecording( w->dev ) ) return 0;
+	h_uploadTree( w, b2_kinematicBody );
+	h_uploadTree( w, b2_dynamicBody );
+	int rc = b2gDev_EnlargeTrees( w->dev, count );
+	if ( rc != 0 ) h_fail( w, "tree enlargement", rc );
+	for ( int t = 0; t < 2; ++t )
+	{
+		k->enlargeIds[t].count = 0;
+		k->enlargeBoxes[t].count = 0;
+	}
+	for ( int i = 0; i < count; ++i )
+	{
+		int shapeId = recs[4 * i + 1];
+		int enlarged = recs[4 * i + 2];
+		int fastBullet = recs[4 * i + 3];
+		h_shape* s = w->shapes.data + shapeId;
+		if ( fastBullet == 0 && enlarged )
+		{
+			b2AABB fat = { { boxes[4 * i], boxes[4 * i + 1] }, { boxes[4 * i + 2], boxes[4 * i + 3] } };
+			s->fatAABB = fat;
+			int t = H_PROXY_TYPE( s->proxyKey ) == b2_dynamicBody ? 1 : 0;
+			h_push( k->enlargeIds[t], H_PROXY_ID( s->proxyKey ) );
+			h_push( k->enlargeBoxes[t], fat );
+		}
+		if ( fastBullet || enlarged ) h_bufferMove( w, s->proxyKey );
+	}
+	/* the device copies already hold the enlarged trees: the next upload is due only when
+	   the host trees change again */
+	const int types[2] = { b2_kinematicBody, b2_dynamicBody };
+	for ( int t = 0; t < 2; ++t )
+	{
+		if ( k->enlargeIds[t].count == 0 ) continue;
+		w->trees[types[t]].version += 1;
+		w->uploadedTreeVersion[types[t]] = w->trees[types[t]].version;
+	}
+	if ( k->enlargeIds[0].count + k->enlargeIds[1].count > 0 )
+	{
+		pthread_mutex_lock( &k->mu );
+		k->enlargePending = 1;
+		k->busy = 1;
+		pthread_cond_broadcast( &k->cv );
+		pthread_mutex_unlock( &k->mu );
+	}
+	return 1;
+}
+
 static void h_enlargeProxies( h_world* w, const int* recs, const float* boxes, int count )
 {
+	if ( h_enlargeOnDevice( w, recs, boxes, count ) ) return;
 	/* many records: the tree enlargements on the host pool, then the move buffer in order */
 	if ( count >= 4 * H_ENLARGE_CHUNK )
 	{
@@ -462,6 +555,8 @@ static void h_solveBullets( h_world* w, const int* recs, int count )
 		sims[n++] = last;
 	}
 	if ( n == 0 ) return;
+	/* the host trees are swept as the enlargement left them */
+	h_joinRebuild( w );
 	/* a batched step records device work for its flushes; the bullet pass waits for its
 	   results, so it runs on the world's own stream (the world's earlier work has been
 	   flushed by now and nothing of this phase is recorded yet) */
@@ -676,7 +771,9 @@ void h_stepFinish( h_world* w )
 		}
 	}
 	if ( w->stepTimeStep > 0.0f ) w->profile.solve = h_ms( w->stepT0 );
-	h_joinRebuild( w );
+	/* a step that issued no solve still waits for its rebuild here; after a solve the worker
+	   may go on enlarging the host trees past the step's end */
+	if ( w->stepSolveIssued == 0 ) h_joinRebuild( w );
 	/* sensor overlaps come last (physics_world.c:961-966); a batched step runs them after
 	   its last flush, when the device state is final */
 	if ( w->sensors.count > 0 && b2gDev_IsRecording( w->dev ) == 0 )

@@ -449,10 +449,22 @@ void h_treeMoveProxy( h_tree* t, int proxyId, b2AABB aabb )
 }
 
 /* dynamic_tree.c:798-837 */
+static void h_treeEnlargeOne( h_tree* t, int proxyId, b2AABB aabb );
+
 void h_treeEnlargeProxy( h_tree* t, int proxyId, b2AABB aabb )
 {
-	h_treeNode* nodes = t->nodes;
 	t->version += 1;
+	h_treeEnlargeOne( t, proxyId, aabb );
+}
+
+void h_treeEnlargeProxies( h_tree* t, const int* proxyIds, const b2AABB* boxes, int count )
+{
+	for ( int i = 0; i < count; ++i ) h_treeEnlargeOne( t, proxyIds[i], boxes[i] );
+}
+
+static void h_treeEnlargeOne( h_tree* t, int proxyId, b2AABB aabb )
+{
+	h_treeNode* nodes = t->nodes;
 	nodes[proxyId].aabb = aabb;
 	int parentIndex = nodes[proxyId].parent;
 	while ( parentIndex != B2_NULL_INDEX )

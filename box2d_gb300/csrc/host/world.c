@@ -637,6 +637,8 @@ void h_syncShapeBoxes( h_world* w )
 
 void h_markHostChanged( h_world* w )
 {
+	/* the trees may still be in the rebuild worker's hands (the last step's enlargement) */
+	h_joinRebuild( w );
 	h_syncFromDevice( w );
 	h_syncJointsFromDevice( w );
 	/* the device boxes are sent again from the host's before the next step */
@@ -738,6 +740,7 @@ void h_ensureDevice( h_world* w )
 		if ( s->id != i )
 		{
 			d->type = -1;
+			d->proxyKey = -1;
 			continue;
 		}
 		d->type = s->type;
@@ -789,6 +792,7 @@ void h_ensureDevice( h_world* w )
 		d->groupIndex = s->filter.groupIndex;
 		d->isSensor = s->isSensor;
 		d->enableSensorEvents = s->enableSensorEvents;
+		d->proxyKey = s->proxyKey;
 		{
 			b2Vec2 centroid = h_getShapeCentroid( s );
 			float minExtent, maxExtent;
