@@ -61,6 +61,8 @@ struct d_clusterPlan
 	int* assigned;	  /* color c, CTA r: slots at assigned[offset(c) * ranks + r * count(c)] */
 	int* counts;	  /* B2G_CLUSTER_COUNT_WORDS assignment counters */
 	int* status;	  /* B2G_STATUS_CAPACITY if a CTA was given more lanes than it holds */
+	int* startFlag;	  /* host-visible word set to startToken once the cluster runs (or NULL) */
+	int startToken;
 };
 
 /* A body reference inside the cluster is (owning CTA << 16 | slot in that CTA). Positions
@@ -247,6 +249,12 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 	__shared__ int s_restitution;
 	const int tid = threadIdx.x, nt = blockDim.x;
 	const b2gStepParams& P = a.p;
+	/* the cluster is resident: the host may now start other work beside it on the GPU */
+	if ( plan.startFlag != nullptr && rank == 0 && tid == 0 )
+	{
+		*(volatile int*)plan.startFlag = plan.startToken;
+		__threadfence_system();
+	}
 	const int overflowBegin = a.colorOffsets[B2G_OVERFLOW_INDEX];
 	d_clusterBodies bodies = { sv, sd };
 	/* this CTA's bodies: positions [base, base + localCount) */
@@ -434,7 +442,7 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
    expected: the host checks the total) sets B2G_STATUS_CAPACITY in *status. */
 extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
 									const int* activeColors, int activeColorCount, int useLists, int bodyCount, int* status,
-									long long epoch, cudaStream_t stream, long long* launches )
+									long long epoch, int* startFlag, int startToken, cudaStream_t stream, long long* launches )
 {
 	static pthread_mutex_t s_lock = PTHREAD_MUTEX_INITIALIZER;
 	static int s_ranks = -1;
@@ -557,6 +565,8 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	plan.assigned = b->clusterAssigned;
 	plan.counts = b->clusterCounts;
 	plan.status = status;
+	plan.startFlag = startFlag;
+	plan.startToken = startToken;
 	plan.assignedJoints = b->clusterJoints;
 
 	/* threads per CTA: the even share of the largest color (joints + contacts) with a

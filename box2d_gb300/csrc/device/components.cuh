@@ -106,10 +106,13 @@ extern "C" int b2gDev_CompSolveBig( b2gCompBuffers* b, const d_solveArgs* a, con
 /* cluster solver (cluster.cu) over every constraint (useLists = 0) or the big-component
    lists; 0 = launched, -1 = does not fit a cluster, else a CUDA error. `epoch` changes
    whenever colors, joints, the awake set or the component lists change (-1: unknown); the
-   assignment of constraints to the cluster's CTAs is reused while it stays the same. */
+   assignment of constraints to the cluster's CTAs is reused while it stays the same.
+   startFlag (a word of mapped host memory, or NULL) is set to startToken once the cluster
+   is resident on the GPU. */
 extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const d_jointBodies* jb,
 									const int* activeColors, int activeColorCount, int useLists, int bodyCount, int* status,
-									long long epoch, cudaStream_t stream, long long* launches );
+									long long epoch, int* startFlag, int startToken, cudaStream_t stream,
+									long long* launches );
 
 /* the arguments of the one-CTA world solve, for a batched launch (out may be NULL to get
    the size), and the batched launch itself: CTA r solves the world whose arguments are at

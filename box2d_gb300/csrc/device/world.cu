@@ -202,6 +202,13 @@ struct b2gDeviceWorld
 	int pairsTimingPending;
 	cudaEvent_t syncEvent; /* blocking-sync event for waits of batched steps */
 	cudaEvent_t treeEvent; /* after the tree uploads that precede a device enlargement */
+	/* small components' bins solved beside the cluster: a second stream, its fork and join
+	   events, and the mapped word the cluster kernel sets once it is resident */
+	cudaStream_t sideStream;
+	cudaEvent_t forkEvent, joinEvent;
+	int* hClusterStarted;
+	int* dClusterStarted;
+	int clusterToken;
 	int blockingSync;
 	/* bullet pass: bullet body slots in, shape records out */
 	int* bulletSims;
@@ -1074,6 +1081,10 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	free( dw->hSortTmp );
 	for ( int i = 0; i < 10; ++i ) cudaEventDestroy( dw->ev[i] );
 	if ( dw->treeEvent ) cudaEventDestroy( dw->treeEvent );
+	if ( dw->forkEvent ) cudaEventDestroy( dw->forkEvent );
+	if ( dw->joinEvent ) cudaEventDestroy( dw->joinEvent );
+	if ( dw->sideStream ) cudaStreamDestroy( dw->sideStream );
+	if ( dw->hClusterStarted ) cudaFreeHost( dw->hClusterStarted );
 	cudaStreamDestroy( dw->stream );
 	for ( void* r : dw->retired ) cudaFree( r );
 	delete dw->defer;
@@ -2356,6 +2367,38 @@ extern "C" int b2gDev_SolveBullets( b2gDeviceWorld* dw, const b2gStepParams* p, 
 	return 0;
 }
 
+/* the second stream, its events and the mapped start word, created on first use; 0 when
+   ready */
+static int sideReady( b2gDeviceWorld* dw )
+{
+	if ( dw->sideStream != NULL ) return 0;
+	cudaStream_t side = NULL;
+	cudaEvent_t fork = NULL, join = NULL;
+	int* hFlag = NULL;
+	int* dFlag = NULL;
+	bool ok = cudaStreamCreateWithFlags( &side, cudaStreamNonBlocking ) == cudaSuccess &&
+			  cudaEventCreateWithFlags( &fork, cudaEventDisableTiming ) == cudaSuccess &&
+			  cudaEventCreateWithFlags( &join, cudaEventDisableTiming ) == cudaSuccess &&
+			  cudaHostAlloc( (void**)&hFlag, sizeof( int ), cudaHostAllocMapped ) == cudaSuccess &&
+			  cudaHostGetDevicePointer( (void**)&dFlag, hFlag, 0 ) == cudaSuccess;
+	if ( ok == false )
+	{
+		cudaGetLastError();
+		if ( hFlag ) cudaFreeHost( hFlag );
+		if ( join ) cudaEventDestroy( join );
+		if ( fork ) cudaEventDestroy( fork );
+		if ( side ) cudaStreamDestroy( side );
+		return 1;
+	}
+	*hFlag = 0;
+	dw->sideStream = side;
+	dw->forkEvent = fork;
+	dw->joinEvent = join;
+	dw->hClusterStarted = hFlag;
+	dw->dClusterStarted = dFlag;
+	return 0;
+}
+
 extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, const int* activeColors, int activeColorCount,
 								   int awakeCount )
 {
@@ -2466,14 +2509,47 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 			dw->compValid = 0;
 		}
 		const b2gCompSummary* hs = dw->comp.hSummary;
-		if ( hs->smallComponents > 0 )
+		if ( hs->smallComponents > 0 && hs->bigComponents > 0 && sideReady( dw ) == 0 )
+		{
+			/* The bins of the small components run beside the cluster solve of the big ones
+			   (they share no body or contact): the cluster is launched first, and once it is
+			   resident (it needs 16 whole SMs, which bins already placed would hold) the bins
+			   go to the other SMs from a second stream. */
+			dw->compValid = 1;
+			CK( cudaEventRecord( dw->forkEvent, dw->stream ) );
+			int token = ++dw->clusterToken;
+			int rc = b2gDev_ClusterSolve( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, 1,
+										  hs->bigBodies, &dw->counters->status, dw->topologyEpoch, dw->dClusterStarted, token,
+										  dw->stream, &dw->launches );
+			if ( rc > 0 ) return rc;
+			if ( rc == 0 )
+			{
+				/* bounded wait for the cluster to start; past it the bins go anyway (they
+				   may then delay the cluster, never change a result) */
+				uint64_t spins = 0;
+				while ( *(volatile int*)dw->hClusterStarted != token && spins < ( 1ull << 17 ) ) ++spins;
+				CK( cudaStreamWaitEvent( dw->sideStream, dw->forkEvent, 0 ) );
+				CK2( b2gDev_CompSolveBins( &dw->comp, &a, dw->jointOffsets, &jb0, dw->counters, dw->sideStream, &dw->launches ) );
+				CK( cudaEventRecord( dw->joinEvent, dw->sideStream ) );
+				CK( cudaStreamWaitEvent( dw->stream, dw->joinEvent, 0 ) );
+			}
+			else
+			{
+				CK2( b2gDev_CompSolveBins( &dw->comp, &a, dw->jointOffsets, &jb0, dw->counters, dw->stream, &dw->launches ) );
+				CK2( b2gDev_CompSolveBig( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, total,
+										  jointTotal, dw->stream, &dw->launches ) );
+			}
+			solved = true;
+		}
+		else if ( hs->smallComponents > 0 )
 		{
 			dw->compValid = 1;
 			CK2( b2gDev_CompSolveBins( &dw->comp, &a, dw->jointOffsets, &jb0, dw->counters, dw->stream, &dw->launches ) );
 			if ( hs->bigComponents > 0 )
 			{
 				int rc = b2gDev_ClusterSolve( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, 1,
-											  hs->bigBodies, &dw->counters->status, dw->topologyEpoch, dw->stream, &dw->launches );
+											  hs->bigBodies, &dw->counters->status, dw->topologyEpoch, NULL, 0, dw->stream,
+											  &dw->launches );
 				if ( rc > 0 ) return rc;
 				if ( rc < 0 )
 					CK2( b2gDev_CompSolveBig( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, total,
@@ -2488,7 +2564,7 @@ extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, co
 	if ( solved == false && dw->solverMode == B2G_SOLVER_COMPONENTS && ovJointCount0 + ovCount0 == 0 )
 	{
 		int rc = b2gDev_ClusterSolve( &dw->comp, &a, dw->jointOffsets, &jb0, activeColors, activeColorCount, 0, awakeCount,
-									  &dw->counters->status, dw->topologyEpoch, dw->stream, &dw->launches );
+									  &dw->counters->status, dw->topologyEpoch, NULL, 0, dw->stream, &dw->launches );
 		if ( rc > 0 ) return rc;
 		solved = rc == 0;
 	}
