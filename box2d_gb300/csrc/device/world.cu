@@ -206,6 +206,8 @@ struct b2gDeviceWorld
 	   events, and the mapped word the cluster kernel sets once it is resident */
 	cudaStream_t sideStream;
 	cudaEvent_t forkEvent, joinEvent;
+	cudaEvent_t enlargeEvent; /* after a tree enlargement run on the second stream */
+	int enlargeOnSide;		  /* that enlargement is not yet ordered before the world's stream */
 	int* hClusterStarted;
 	int* dClusterStarted;
 	int clusterToken;
@@ -1082,6 +1084,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	for ( int i = 0; i < 10; ++i ) cudaEventDestroy( dw->ev[i] );
 	if ( dw->treeEvent ) cudaEventDestroy( dw->treeEvent );
 	if ( dw->forkEvent ) cudaEventDestroy( dw->forkEvent );
+	if ( dw->enlargeEvent ) cudaEventDestroy( dw->enlargeEvent );
 	if ( dw->joinEvent ) cudaEventDestroy( dw->joinEvent );
 	if ( dw->sideStream ) cudaStreamDestroy( dw->sideStream );
 	if ( dw->hClusterStarted ) cudaFreeHost( dw->hClusterStarted );
@@ -1881,9 +1884,24 @@ static __device__ void b_convertTree( const d_convertTreeArgs& a, int block, int
 	out[i] = d;
 }
 
+static int sideReady( b2gDeviceWorld* dw );
+
+/* order a tree enlargement that ran on the second stream before the world's next use of
+   the trees (the pair query, the bullet sweeps, a tree upload); recorded work waits on
+   the host, since it replays on another stream */
+static int joinEnlarge( b2gDeviceWorld* dw )
+{
+	if ( dw->enlargeOnSide == 0 ) return 0;
+	if ( dw->defer ) CK( cudaEventSynchronize( dw->enlargeEvent ) );
+	else CK( cudaStreamWaitEvent( dw->stream, dw->enlargeEvent, 0 ) );
+	dw->enlargeOnSide = 0;
+	return 0;
+}
+
 extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gHostTreeNode* nodes, int nodeCount, int root,
 								   int hostPinned )
 {
+	CK2( joinEnlarge( dw ) );
 	int need = nodeCount > 0 ? nodeCount : 1;
 	CK2( grow( dw, (void**)&dw->tree[type], &dw->treeCap[type], need, sizeof( b2gTreeNode ) ) );
 	CK2( grow( dw, (void**)&dw->treeRaw[type], &dw->treeRawCap[type], need, sizeof( b2gHostTreeNode ) ) );
@@ -1973,14 +1991,31 @@ __global__ void k_enlargeTrees( const int* __restrict__ recs, const float4* __re
 extern "C" int b2gDev_EnlargeTrees( b2gDeviceWorld* dw, int recordCount )
 {
 	if ( dw->treeEvent == NULL ) CK( cudaEventCreateWithFlags( &dw->treeEvent, cudaEventDisableTiming ) );
+	CK2( joinEnlarge( dw ) );
 	CK( cudaEventRecord( dw->treeEvent, dw->stream ) );
 	int n = recordCount < dw->enlargedCap / 4 ? recordCount : dw->enlargedCap / 4;
 	if ( n <= 0 || dw->tree[b2_dynamicBody] == NULL || dw->treeRaw[b2_dynamicBody] == NULL ) return 0;
-	k_enlargeTrees<<<blocks( n ), B2G_THREADS, 0, dw->stream>>>( dw->enlargedRecs, dw->enlargedBoxes, n, dw->shapes,
-																   dw->tree[b2_kinematicBody], dw->tree[b2_dynamicBody],
-																   dw->treeRaw[b2_kinematicBody], dw->treeRaw[b2_dynamicBody] );
+	/* on the second stream, so that the step's state download (queued next on the world's
+	   stream) does not wait for it; the next use of the trees does */
+	cudaStream_t s = dw->stream;
+	if ( dw->enlargeEvent == NULL && sideReady( dw ) == 0 )
+		CK( cudaEventCreateWithFlags( &dw->enlargeEvent, cudaEventDisableTiming ) );
+	if ( dw->enlargeEvent != NULL )
+	{
+		s = dw->sideStream;
+		CK( cudaStreamWaitEvent( s, dw->treeEvent, 0 ) );
+	}
+	k_enlargeTrees<<<blocks( n ), B2G_THREADS, 0, s>>>( dw->enlargedRecs, dw->enlargedBoxes, n, dw->shapes,
+														dw->tree[b2_kinematicBody], dw->tree[b2_dynamicBody],
+														dw->treeRaw[b2_kinematicBody], dw->treeRaw[b2_dynamicBody] );
 	dw->launches += 1;
-	return (int)cudaGetLastError();
+	CK( cudaGetLastError() );
+	if ( s != dw->stream )
+	{
+		CK( cudaEventRecord( dw->enlargeEvent, s ) );
+		dw->enlargeOnSide = 1;
+	}
+	return 0;
 }
 
 extern "C" int b2gDev_WaitTreeUploads( b2gDeviceWorld* dw )
@@ -2031,6 +2066,7 @@ static __device__ void b_packPairs( const d_packPairsArgs& a, int block, int gri
    next wait: counters, per-move counts and offsets, and the first `window` packed pairs */
 static int findPairsIssue( b2gDeviceWorld* dw, int n )
 {
+	CK2( joinEnlarge( dw ) );
 	CK2( grow( dw, (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
 	CK2( grow( dw, (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
 	/* the window follows the last count; recorded work (a batched flush) reads back twice
@@ -2326,6 +2362,7 @@ extern "C" int b2gDev_SolveBullets( b2gDeviceWorld* dw, const b2gStepParams* p, 
 	*outBoxes = NULL;
 	*outCount = 0;
 	if ( count <= 0 ) return 0;
+	CK2( joinEnlarge( dw ) );
 	int shapeTotal = dw->shapeCountTotal;
 	int cap = shapeTotal > 0 ? shapeTotal : 1;
 	CK2( grow( dw, (void**)&dw->bulletSims, &dw->bulletSimsCap, count, sizeof( int ) ) );
