@@ -385,6 +385,8 @@ int b2gDev_UploadTree( b2gDeviceWorld* dw, int treeType, const b2gHostTreeNode* 
    change). */
 int b2gDev_EnlargeTrees( b2gDeviceWorld* dw, int recordCount );
 int b2gDev_WaitTreeUploads( b2gDeviceWorld* dw );
+/* create the enlargement's events and second stream and load its kernel ahead of use */
+int b2gDev_PrepareEnlarge( b2gDeviceWorld* dw );
 /* waits of this world block the calling thread (sleep) instead of spinning */
 void b2gDev_SetBlockingSync( b2gDeviceWorld* dw, int on );
 

@@ -5,11 +5,13 @@
  * color, restitution, store -- in one launch. Each color's constraints are split evenly
  * over the CTAs; a CTA keeps its contact constraints in its own shared memory for the whole
  * step. The body state lives in the cluster's distributed shared memory: body position p
- * (its index in the solved body list) sits in CTA p % ranks, slot p / ranks, and every
- * constraint reads and writes it there through the cluster's shared-memory window. Colors
- * are separated by the hardware cluster barrier, whose release/acquire semantics order the
- * body-state writes of one color before the reads of the next. Joints stay in global
- * memory; each joint is always processed by the same thread.
+ * (its index in the solved body list) sits in CTA p / slotsPerRank, slot p % slotsPerRank,
+ * and every constraint reads and writes it there through the cluster's shared-memory window.
+ * Colors are separated by the hardware cluster barrier, whose release/acquire semantics
+ * order the body-state writes of one color before the reads of the next. Joints stay in
+ * global memory; each joint is always processed by the same thread. In a cluster without
+ * joints the warm start runs per body, right after the body's integrate velocities, which
+ * takes the warm-start colors' barriers out of every substep.
  *
  * This file is compiled with -Xptxas -dlcm=cg: global loads bypass L1.
  *
@@ -22,6 +24,7 @@
 #include <cooperative_groups.h>
 #include <pthread.h>
 #include <stddef.h>
+#include <stdlib.h>
 #include <string.h>
 
 namespace cg = cooperative_groups;
@@ -56,6 +59,8 @@ struct d_clusterPlan
 	int laneCap;	  /* contact lanes one CTA's shared memory holds */
 	int jointSlotCap; /* joints whose accumulated impulses (s[]) a CTA keeps in shared memory */
 	int colorCap[B2_GRAPH_COLOR_COUNT]; /* lanes of an active color a CTA takes in one pass */
+	int bodyWarm;	/* warm start per body, fused with integrate velocities (contact-only clusters) */
+	int entryBytes; /* bytes of the per-body warm-start entries in each CTA's shared memory */
 	int jointCap[B2_GRAPH_COLOR_COUNT]; /* joints of an active color a CTA takes in one pass */
 	int* assignedJoints;				/* color c, CTA r: joints at [jointOffset(c) * ranks + r * count(c)] */
 	int* assigned;	  /* color c, CTA r: slots at assigned[offset(c) * ranks + r * count(c)] */
@@ -232,6 +237,60 @@ static __device__ __forceinline__ void d_clusterJointRun( const b2gStepParams& P
 	for ( int i = 0; i < 4; ++i ) dst[i] = copy.w[sBegin + i];
 }
 
+/* Warm start as seen by one body (contact_solver.c:1811-1871 read per body): a dynamic
+   body is in at most one constraint per graph color (constraint_graph.c:84-130), and a
+   lane's warm start changes each of its bodies from that body's own velocity and the
+   lane's stored impulses only. So applying the body's lanes in color order, with the
+   operations of d_warmStartLane for its side, gives its velocity after the warm-start
+   colors bit for bit, with no barrier between colors. ent[k] is the body's lane of active
+   color k: (lane index in its CTA << 6) | (32 if the body is side B) | CTA rank, or -1. */
+static __device__ __forceinline__ void d_clusterWarmBody( float4* sv, int s, const int* ent, int colorCount,
+														  const b2gContactLane* lanes )
+{
+	float4 v = sv[s];
+	if ( ( __float_as_uint( v.w ) & B2G_DYNAMIC_FLAG ) == 0 ) return;
+	float vx = v.x, vy = v.y, w = v.z;
+	for ( int k = 0; k < colorCount; ++k )
+	{
+		const int e = ent[k];
+		if ( e < 0 ) continue;
+		const b2gContactLane* c = cg::this_cluster().map_shared_rank( lanes + ( e >> 6 ), (unsigned)( e & 31 ) );
+		const float nx = c->normal.x, ny = c->normal.y;
+		const float tangentX = ny;
+		const float tangentY = 0.0f - nx;
+		const float ni1 = c->normalImpulse1, ti1 = c->tangentImpulse1;
+		const float ni2 = c->normalImpulse2, ti2 = c->tangentImpulse2;
+		const float roll = c->rollingImpulse;
+		const float Px1 = ni1 * nx + ti1 * tangentX, Py1 = ni1 * ny + ti1 * tangentY;
+		const float Px2 = ni2 * nx + ti2 * tangentX, Py2 = ni2 * ny + ti2 * tangentY;
+		if ( ( e & 32 ) == 0 )
+		{
+			const float invM = c->invMassA, invI = c->invIA;
+			const b2Vec2 r1 = c->anchorA1, r2 = c->anchorA2;
+			w = w - invI * ( r1.x * Py1 - r1.y * Px1 );
+			vx = vx - invM * Px1;
+			vy = vy - invM * Py1;
+			w = w - invI * ( r2.x * Py2 - r2.y * Px2 );
+			vx = vx - invM * Px2;
+			vy = vy - invM * Py2;
+			w = w - invI * roll;
+		}
+		else
+		{
+			const float invM = c->invMassB, invI = c->invIB;
+			const b2Vec2 r1 = c->anchorB1, r2 = c->anchorB2;
+			w = w + invI * ( r1.x * Py1 - r1.y * Px1 );
+			vx = vx + invM * Px1;
+			vy = vy + invM * Py1;
+			w = w + invI * ( r2.x * Py2 - r2.y * Px2 );
+			vx = vx + invM * Px2;
+			vy = vy + invM * Py2;
+			w = w + invI * roll;
+		}
+	}
+	sv[s] = make_float4( vx, vy, w, v.w );
+}
+
 __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies jb, d_clusterPlan plan )
 {
 	cg::cluster_group cluster = cg::this_cluster();
@@ -241,7 +300,8 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 	float4* sv = s_mem;
 	float4* sd = sv + plan.slotsPerRank;
 	float4* jimp = sd + plan.slotsPerRank; /* 4 float4 (s[]) per joint slot */
-	b2gContactLane* lanes = (b2gContactLane*)( jimp + 4 * plan.jointSlotCap );
+	int* entries = (int*)( jimp + 4 * plan.jointSlotCap ); /* [slot * colorCount + k] when bodyWarm */
+	b2gContactLane* lanes = (b2gContactLane*)( (char*)entries + plan.entryBytes );
 	__shared__ int s_cCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_jBegin[B2_GRAPH_COLOR_COUNT], s_jCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_jSlot[B2_GRAPH_COLOR_COUNT];
@@ -294,7 +354,16 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 		sv[s] = a.sv[ai];
 		sd[s] = a.sd[ai];
 	}
-	__syncthreads();
+	if ( plan.bodyWarm )
+	{
+		/* every CTA's entries are empty before any lane registers with its bodies */
+		for ( int i = tid; i < plan.slotsPerRank * plan.colorCount; i += nt ) entries[i] = -1;
+		cluster.sync();
+	}
+	else
+	{
+		__syncthreads();
+	}
 
 	/* prepare: joints in place (global), contacts into this CTA's shared memory; body
 	   references become cluster keys */
@@ -329,6 +398,22 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 			L->indexA = pa >= 0 ? d_clusterKey( plan, pa ) + 1 : 0;
 			L->indexB = pb >= 0 ? d_clusterKey( plan, pb ) + 1 : 0;
 			restitution |= L->groupFlags & 2;
+			if ( plan.bodyWarm )
+			{
+				/* register the lane with its bodies (kinematic bodies may take several lanes of
+				   a color; their entries are never read) */
+				const int ref = ( ( s_laneOffset[k] + t ) << 6 ) | rank;
+				if ( pa >= 0 )
+				{
+					int key = L->indexA - 1;
+					*cluster.map_shared_rank( entries + ( key & 0xffff ) * plan.colorCount + k, (unsigned)( key >> 16 ) ) = ref;
+				}
+				if ( pb >= 0 )
+				{
+					int key = L->indexB - 1;
+					*cluster.map_shared_rank( entries + ( key & 0xffff ) * plan.colorCount + k, (unsigned)( key >> 16 ) ) = ref | 32;
+				}
+			}
 		}
 	}
 	if ( restitution ) s_restitution = 1;
@@ -347,9 +432,21 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 			int p = base + s;
 			int ai = plan.bodyList ? plan.bodyList[p] : p;
 			d_integrateVelocitiesState( P, sv, s, a.params + 8 * ai );
+			if ( plan.bodyWarm ) d_clusterWarmBody( sv, s, entries + s * plan.colorCount, plan.colorCount, lanes );
+		}
+		if ( plan.bodyWarm && plan.colorCount > 0 )
+		{
+			/* the lanes' own part of the warm start (contact_solver.c:1846,1858) */
+			const int laneCount = s_laneOffset[plan.colorCount - 1] + s_cCount[plan.colorCount - 1];
+			for ( int i = tid; i < laneCount; i += nt )
+			{
+				b2gContactLane* c = lanes + i;
+				c->totalNormalImpulse1 = c->totalNormalImpulse1 + c->normalImpulse1;
+				c->totalNormalImpulse2 = c->totalNormalImpulse2 + c->normalImpulse2;
+			}
 		}
 		cluster.sync();
-		for ( int stage = STAGE_WARM; stage <= STAGE_RELAX; ++stage )
+		for ( int stage = plan.bodyWarm ? STAGE_SOLVE : STAGE_WARM; stage <= STAGE_RELAX; ++stage )
 		{
 			if ( stage == STAGE_RELAX )
 			{
@@ -502,13 +599,23 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	const long long jointSlotBytes = 4 * (long long)sizeof( float4 );
 	long long evenJoints = ( jointsTotal + ranks - 1 ) / ranks;
 	int jointSlotCap = jointsTotal > 0 ? (int)( evenJoints + evenJoints / 4 + 32 ) : 0;
+	/* without joints, the warm start runs per body with integrate velocities when the body
+	   entries fit beside the lanes (B2G_CLUSTER_BODY_WARM=0 keeps the per-color warm start) */
+	const char* bodyWarmEnv = getenv( "B2G_CLUSTER_BODY_WARM" );
+	int bodyWarm = jointsTotal == 0 && activeColorCount > 0 && ( bodyWarmEnv == NULL || atoi( bodyWarmEnv ) != 0 );
+	long long entryBytes = bodyWarm ? ( ( (long long)slotsPerRank * activeColorCount * (long long)sizeof( int ) + 15 ) / 16 ) * 16 : 0;
 	int laneCap = 0;
 	for ( ;; )
 	{
-		long long laneBytes = (long long)B2G_CLUSTER_SMEM_MAX - bodyBytes - (long long)jointSlotCap * jointSlotBytes;
+		long long laneBytes = (long long)B2G_CLUSTER_SMEM_MAX - bodyBytes - (long long)jointSlotCap * jointSlotBytes - entryBytes;
 		laneCap = laneBytes > 0 ? (int)( laneBytes / sizeof( b2gContactLane ) ) : 0;
-		if ( lanesTotal <= (long long)laneCap * ranks || jointSlotCap == 0 ) break;
-		jointSlotCap = jointSlotCap > 64 ? jointSlotCap / 2 : 0;
+		if ( lanesTotal <= (long long)laneCap * ranks ) break;
+		if ( jointSlotCap > 0 )
+			jointSlotCap = jointSlotCap > 64 ? jointSlotCap / 2 : 0;
+		else if ( entryBytes > 0 )
+			entryBytes = 0, bodyWarm = 0;
+		else
+			break;
 	}
 	if ( lanesTotal > (long long)laneCap * ranks ) return -1;
 
@@ -562,6 +669,8 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	plan.slotsPerRank = slotsPerRank;
 	plan.laneCap = laneCap;
 	plan.jointSlotCap = jointSlotCap;
+	plan.bodyWarm = bodyWarm;
+	plan.entryBytes = (int)entryBytes;
 	plan.assigned = b->clusterAssigned;
 	plan.counts = b->clusterCounts;
 	plan.status = status;

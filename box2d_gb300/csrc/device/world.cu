@@ -2018,6 +2018,19 @@ extern "C" int b2gDev_EnlargeTrees( b2gDeviceWorld* dw, int recordCount )
 	return 0;
 }
 
+/* create what the tree enlargement uses (events, the second stream) and load its kernel
+   ahead of the first step that needs them, so that none of these one-time costs falls in a
+   step */
+extern "C" int b2gDev_PrepareEnlarge( b2gDeviceWorld* dw )
+{
+	if ( dw->treeEvent == NULL ) CK( cudaEventCreateWithFlags( &dw->treeEvent, cudaEventDisableTiming ) );
+	if ( dw->enlargeEvent == NULL && sideReady( dw ) == 0 )
+		CK( cudaEventCreateWithFlags( &dw->enlargeEvent, cudaEventDisableTiming ) );
+	cudaFuncAttributes attr;
+	CK( cudaFuncGetAttributes( &attr, k_enlargeTrees ) );
+	return 0;
+}
+
 extern "C" int b2gDev_WaitTreeUploads( b2gDeviceWorld* dw )
 {
 	if ( dw->treeEvent != NULL ) CK( cudaEventSynchronize( dw->treeEvent ) );

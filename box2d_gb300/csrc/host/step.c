@@ -105,6 +105,10 @@ static h_rebuildWorker* h_startWorker( h_world* w )
 		return NULL;
 	}
 	w->rebuildWorker = k;
+	/* the device tree enlargement comes with the worker: its setup happens here, not in the
+	   first step that enlarges proxies */
+	int rc = b2gDev_PrepareEnlarge( w->dev );
+	if ( rc != 0 ) h_fail( w, "tree enlargement setup", rc );
 	return k;
 }
 

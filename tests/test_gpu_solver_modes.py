@@ -33,3 +33,23 @@ def test_solver_mode_matches_oracle(gpu_lib, oracle, monkeypatch, mode, case):
     monkeypatch.setenv("B2G_SOLVER", mode)
     _, kind, a, b, c, seed, flags, steps = case
     lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps)
+
+
+# The cluster solver of the big components runs the warm start per body (fused with
+# integrate velocities) when the cluster has no joints; B2G_CLUSTER_BODY_WARM=0 keeps the
+# per-color warm start. Both must match the oracle bit for bit.
+WARM_CASES = [
+    ("pyramids_big_and_small", B.MANY_PYRAMIDS_RAIN, 2, 30, 600, 0, B.NO_CONTINUOUS, 40),
+    ("pyramids_big_no_warm_start", B.MANY_PYRAMIDS_RAIN, 2, 30, 600, 0, B.NO_CONTINUOUS | B.NO_WARM_STARTING, 30),
+    ("large_pyramid", B.LARGE_PYRAMID, 40, 1, 0, 0, 0, 40),
+    ("shape_zoo_restitution", B.SHAPE_ZOO, 150, 0, 0, 2, B.NO_CONTINUOUS, 100),
+]
+
+
+@pytest.mark.parametrize("body_warm", ["1", "0"])
+@pytest.mark.parametrize("case", WARM_CASES, ids=[c[0] for c in WARM_CASES])
+def test_cluster_warm_start_per_body_matches_oracle(gpu_lib, oracle, monkeypatch, body_warm, case):
+    monkeypatch.setenv("B2G_SOLVER", "components")
+    monkeypatch.setenv("B2G_CLUSTER_BODY_WARM", body_warm)
+    _, kind, a, b, c, seed, flags, steps = case
+    lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps)
