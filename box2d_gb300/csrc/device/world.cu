@@ -61,7 +61,6 @@ enum
 {
 	DK_MARK_MOVED = 0,
 	DK_FIND_PAIRS,
-	DK_PACK_PAIRS,
 	DK_CONVERT_TREE,
 	DK_INIT_CONTACTS,
 	DK_KILL_CONTACTS,
@@ -191,11 +190,9 @@ struct b2gDeviceWorld
 	void* hMoveStage; /* pinned host staging of the same */
 	int hMoveStageCap;
 	int* pairPacked; /* pairs packed per move at atomically claimed offsets */
-	int* pairOffsets;
-	int pairPackedCap, pairOffsetsCap;
-	int* hPairOffsets;
+	int pairPackedCap;
 	int* hPairPacked;
-	int hPairOffsetsCap, hPairPackedCap;
+	int hPairPackedCap;
 	int pairWindow;	  /* pairs copied back with the counters */
 	int changeWindow; /* state changes copied back with the counters */
 	int recWindow;	  /* enlarged-proxy records copied back with the counters */
@@ -243,7 +240,7 @@ struct b2gDeviceWorld
 	int upCap;
 	size_t upUsed;
 	int* pairBuf;
-	int* pairCounts;
+	int* pairCounts; /* per move: pair counts at [0, n), packed offsets at [n, 2n) */
 	int pairPerMove;
 	int pairBufCap;
 	/* outputs */
@@ -484,11 +481,17 @@ struct d_markMovedArgs
 	const int* keys;
 	int n;
 	unsigned char value;
+	b2gStepCounters* reset; /* zeroed by the first thread (the query's counters), or NULL */
 };
 
 static __device__ void b_markMoved( const d_markMovedArgs& a, int block, int grid )
 {
 	int i = block * blockDim.x + threadIdx.x;
+	if ( i == 0 && a.reset != nullptr )
+	{
+		int* w = (int*)a.reset;
+		for ( int k = 0; k < (int)( sizeof( b2gStepCounters ) / sizeof( int ) ); ++k ) w[k] = 0;
+	}
 	if ( i >= a.n ) return;
 	int key = a.keys[i];
 	int type = key & 3, id = key >> 2;
@@ -515,6 +518,8 @@ struct d_findPairsArgs
 	int* counts;
 	int capPerMove;
 	b2gStepCounters* counters;
+	int* packed;  /* every move's pairs, one contiguous run per move */
+	int* offsets; /* where each move's run starts (in pairs) */
 };
 
 static __device__ void b_findPairs( const d_findPairsArgs& fa, int block, int grid )
@@ -619,6 +624,14 @@ static __device__ void b_findPairs( const d_findPairsArgs& fa, int block, int gr
 	}
 	counts[i] = count;
 	if ( count > capPerMove ) atomicMax( &counters->pairOverflow, count );
+	/* claim a contiguous run of the packed buffer and copy the move's pairs there: the host
+	   reads them back per move through the offsets, so the runs' order does not matter */
+	int c = count < capPerMove ? count : capPerMove;
+	int o = atomicAdd( &counters->pairCount, c );
+	fa.offsets[i] = o;
+	const int2* src = (const int2*)pairs + (size_t)i * capPerMove;
+	int2* dst = (int2*)fa.packed + o;
+	for ( int k = 0; k < c; ++k ) dst[k] = src[k];
 }
 
 /* ======================= contacts ======================= */
@@ -1065,7 +1078,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->params,	  dw->center0,	 dw->enlargedBody, dw->shapes,		dw->aabb,		  dw->fat,
 					  dw->shapeEnlarged, dw->contacts, dw->colorIds,	dw->lanes,		dw->joints,		  dw->tree[0],
 					  dw->tree[1],	  dw->tree[2], dw->treeRaw[0], dw->treeRaw[1], dw->treeRaw[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  
-					  dw->moveStage, dw->pairPacked, dw->pairOffsets, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
+					  dw->moveStage, dw->pairPacked, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
 					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList,
 					  dw->sleepTime, dw->islandLocal, dw->islandInfo, dw->islandBits, dw->sensorIds, dw->sensorPairs,
 					  dw->sensorCount, dw->bulletSims, dw->bulletRecs, dw->bulletBoxes, dw->bulletCount, dw->sensorHits };
@@ -1075,7 +1088,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	if ( dw->upDev ) cudaFree( dw->upDev );
 	if ( dw->upHost ) cudaFreeHost( dw->upHost );
 	void* hptrs[] = { dw->hCounters, dw->hChanges,	   dw->hRecs,	   dw->hBoxes,	   dw->hPairs,	  dw->hPairCounts,
-					  dw->hMoveStage, dw->hPairOffsets, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw,
+					  dw->hMoveStage, dw->hPairPacked, dw->hRecsRaw, dw->hBoxesRaw,
 					  dw->hXf,		  dw->hCenter,		dw->hFlags,		 dw->hStateV, dw->hSleepTime, dw->hIslandBits,
 					  dw->hSensorPairs, dw->hBulletRecs, dw->hBulletBoxes, dw->hSensorHits };
 	for ( size_t i = 0; i < sizeof( hptrs ) / sizeof( hptrs[0] ); ++i )
@@ -2049,35 +2062,9 @@ extern "C" void b2gDev_HostFree( void* p )
 	if ( p != NULL ) cudaFreeHost( p );
 }
 
-/* per move: claim a contiguous run of the packed pair buffer */
-struct d_packPairsArgs
-{
-	const int* pairs;
-	const int* counts;
-	int n, capPerMove;
-	int* packed;
-	int* offsets;
-	b2gStepCounters* counters;
-};
-
-static __device__ void b_packPairs( const d_packPairsArgs& a, int block, int grid )
-{
-	int i = block * blockDim.x + threadIdx.x;
-	if ( i >= a.n ) return;
-	int c = a.counts[i];
-	if ( c > a.capPerMove ) c = a.capPerMove;
-	int o = atomicAdd( &a.counters->pairCount, c );
-	a.offsets[i] = o;
-	for ( int k = 0; k < c; ++k )
-	{
-		a.packed[2 * ( o + k )] = a.pairs[2 * ( (size_t)i * a.capPerMove + k )];
-		a.packed[2 * ( o + k ) + 1] = a.pairs[2 * ( (size_t)i * a.capPerMove + k ) + 1];
-	}
-}
-
 /* the pair query of one step, issued (or recorded); its results arrive with the world's
    next wait: counters, per-move counts and offsets, and the first `window` packed pairs */
-static int findPairsIssue( b2gDeviceWorld* dw, int n )
+static int findPairsIssue( b2gDeviceWorld* dw, int n, bool countersReset )
 {
 	CK2( joinEnlarge( dw ) );
 	CK2( grow( dw, (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
@@ -2087,7 +2074,8 @@ static int findPairsIssue( b2gDeviceWorld* dw, int n )
 	if ( dw->defer && dw->pairWindow < n * dw->pairPerMove ) dw->pairWindow = 2 * dw->pairWindow;
 	int window = dw->pairWindow < n * dw->pairPerMove ? dw->pairWindow : n * dw->pairPerMove;
 	CK2( growHost( (void**)&dw->hPairPacked, &dw->hPairPackedCap, 2 * window, sizeof( int ) ) );
-	CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
+	if ( countersReset == false ) CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
+	int* offsets = dw->pairCounts + n;
 	d_findPairsArgs fa;
 	fa.tStat = dw->tree[b2_staticBody];
 	fa.tKin = dw->tree[b2_kinematicBody];
@@ -2104,12 +2092,12 @@ static int findPairsIssue( b2gDeviceWorld* dw, int n )
 	fa.counts = dw->pairCounts;
 	fa.capPerMove = dw->pairPerMove;
 	fa.counters = dw->counters;
+	fa.packed = dw->pairPacked;
+	fa.offsets = offsets;
 	CK2( ( dev_launch<d_findPairsArgs, b_findPairs>( dw, DK_FIND_PAIRS, blocks( n ), fa ) ) );
-	d_packPairsArgs pa = { dw->pairBuf, dw->pairCounts, n, dw->pairPerMove, dw->pairPacked, dw->pairOffsets, dw->counters };
-	CK2( ( dev_launch<d_packPairsArgs, b_packPairs>( dw, DK_PACK_PAIRS, blocks( n ), pa ) ) );
 	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
-	CK2( dev_d2h( dw, dw->hPairCounts, dw->pairCounts, (size_t)n * sizeof( int ) ) );
-	CK2( dev_d2h( dw, dw->hPairOffsets, dw->pairOffsets, (size_t)n * sizeof( int ) ) );
+	/* per-move counts and offsets are one array: one copy */
+	CK2( dev_d2h( dw, dw->hPairCounts, dw->pairCounts, (size_t)n * 2 * sizeof( int ) ) );
 	CK2( dev_d2h( dw, dw->hPairPacked, dw->pairPacked, (size_t)window * 2 * sizeof( int ) ) );
 	dw->pendingMoves = n;
 	return 0;
@@ -2132,14 +2120,14 @@ extern "C" int b2gDev_FindPairsIssue( b2gDeviceWorld* dw, const int* keys, const
 	dw->moveBoxes = (float4*)dw->moveStage;
 	dw->moveKeys = (int*)( dw->moveBoxes + n );
 	dw->moveShapes = dw->moveKeys + n;
-	CK2( grow( dw, (void**)&dw->pairCounts, &dw->moveCap, n, sizeof( int ) ) );
-	CK2( grow( dw, (void**)&dw->pairOffsets, &dw->pairOffsetsCap, n, sizeof( int ) ) );
-	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, n, sizeof( int ) ) );
-	CK2( growHost( (void**)&dw->hPairOffsets, &dw->hPairOffsetsCap, n, sizeof( int ) ) );
+	/* per-move counts at [0, n), offsets at [n, 2n) */
+	CK2( grow( dw, (void**)&dw->pairCounts, &dw->moveCap, 2 * n, sizeof( int ) ) );
+	CK2( growHost( (void**)&dw->hPairCounts, &dw->hPairCountsCap, 2 * n, sizeof( int ) ) );
 	if ( dw->pairWindow < 64 ) dw->pairWindow = 64;
-	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 1 };
+	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 1,
+						   dw->counters };
 	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
-	return findPairsIssue( dw, n );
+	return findPairsIssue( dw, n, true );
 }
 
 /* after the wait: the pairs of every move in move order. A per-move overflow or a window
@@ -2153,7 +2141,7 @@ extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int*
 	{
 		if ( dw->hCounters->pairOverflow <= dw->pairPerMove ) break;
 		while ( dw->pairPerMove < dw->hCounters->pairOverflow ) dw->pairPerMove *= 2;
-		CK2( findPairsIssue( dw, n ) );
+		CK2( findPairsIssue( dw, n, false ) );
 		CK2( drain( dw ) );
 	}
 	/* a query that ran out of traversal stack kept the pairs it found; the status goes out
@@ -2169,7 +2157,8 @@ extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int*
 	}
 	dw->defer = deferred;
 	/* clear the moved flags (recorded with the next batch when batching) */
-	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 0 };
+	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 0,
+						   nullptr };
 	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
 	/* next step's window follows this step's count, both ways */
 	dw->pairWindow = 2 * total > 64 ? 2 * total : 64;
@@ -2179,7 +2168,7 @@ extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int*
 	for ( int i = 0; i < n; ++i )
 	{
 		int c = dw->hPairCounts[i];
-		memcpy( dw->hPairs + 2 * o, dw->hPairPacked + 2 * (size_t)dw->hPairOffsets[i], (size_t)c * 2 * sizeof( int ) );
+		memcpy( dw->hPairs + 2 * o, dw->hPairPacked + 2 * (size_t)dw->hPairCounts[n + i], (size_t)c * 2 * sizeof( int ) );
 		o += c;
 	}
 	dev_event( dw, dw->ev[1] );
@@ -3382,7 +3371,6 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 		}
 		CK2( ( d_launchBatched<d_markMovedArgs, b_markMoved, 1>( b, L, DK_MARK_MOVED ) ) );
 		CK2( ( d_launchBatched<d_findPairsArgs, b_findPairs, 1>( b, L, DK_FIND_PAIRS ) ) );
-		CK2( ( d_launchBatched<d_packPairsArgs, b_packPairs, 1>( b, L, DK_PACK_PAIRS ) ) );
 		CK2( ( d_launchBatched<d_convertTreeArgs, b_convertTree, 1>( b, L, DK_CONVERT_TREE ) ) );
 		CK2( ( d_launchBatched<d_contactListArgs, b_initContacts, 1>( b, L, DK_INIT_CONTACTS ) ) );
 		CK2( ( d_launchBatched<d_contactListArgs, b_killContacts, 1>( b, L, DK_KILL_CONTACTS ) ) );
