@@ -177,6 +177,7 @@ struct b2gDeviceWorld
 	/* broadphase */
 	b2gTreeNode* tree[3];
 	int treeCap[3], treeRoot[3];
+	int treeNodes[3]; /* nodes of the last upload (the host tree's capacity) */
 	b2gHostTreeNode* treeRaw[3]; /* host node arrays as uploaded */
 	int treeRawCap[3];
 	unsigned char* moved[3];
@@ -482,6 +483,10 @@ struct d_markMovedArgs
 	int n;
 	unsigned char value;
 	b2gStepCounters* reset; /* zeroed by the first thread (the query's counters), or NULL */
+	/* the trees the query walks next: their nodes are prefetched into L2, so that the
+	   query's dependent node reads do not each wait on DRAM */
+	const b2gTreeNode* trees[3];
+	int treeNodes[3];
 };
 
 static __device__ void b_markMoved( const d_markMovedArgs& a, int block, int grid )
@@ -491,6 +496,13 @@ static __device__ void b_markMoved( const d_markMovedArgs& a, int block, int gri
 	{
 		int* w = (int*)a.reset;
 		for ( int k = 0; k < (int)( sizeof( b2gStepCounters ) / sizeof( int ) ); ++k ) w[k] = 0;
+	}
+	const int threads = grid * blockDim.x;
+	for ( int t = 0; t < 3; ++t )
+	{
+		const char* base = (const char*)a.trees[t];
+		const int lines = ( a.treeNodes[t] * (int)sizeof( b2gTreeNode ) + 127 ) / 128;
+		for ( int l = i; l < lines; l += threads ) asm volatile( "prefetch.global.L2 [%0];" ::"l"( base + 128 * (size_t)l ) );
 	}
 	if ( i >= a.n ) return;
 	int key = a.keys[i];
@@ -1936,6 +1948,7 @@ extern "C" int b2gDev_UploadTree( b2gDeviceWorld* dw, int type, const b2gHostTre
 	CK2( grow( dw, (void**)&dw->moved[type], &mc, need, 1 ) );
 	dw->movedCap[type] = mc;
 	dw->treeRoot[type] = root;
+	dw->treeNodes[type] = nodeCount;
 	return 0;
 }
 
@@ -2126,6 +2139,11 @@ extern "C" int b2gDev_FindPairsIssue( b2gDeviceWorld* dw, const int* keys, const
 	if ( dw->pairWindow < 64 ) dw->pairWindow = 64;
 	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 1,
 						   dw->counters };
+	for ( int t = 0; t < 3; ++t )
+	{
+		ma.trees[t] = dw->tree[t];
+		ma.treeNodes[t] = dw->tree[t] != NULL && dw->treeRoot[t] >= 0 ? dw->treeNodes[t] : 0;
+	}
 	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
 	return findPairsIssue( dw, n, true );
 }
@@ -2158,7 +2176,7 @@ extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int*
 	dw->defer = deferred;
 	/* clear the moved flags (recorded with the next batch when batching) */
 	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 0,
-						   nullptr };
+						   nullptr, { nullptr, nullptr, nullptr }, { 0, 0, 0 } };
 	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
 	/* next step's window follows this step's count, both ways */
 	dw->pairWindow = 2 * total > 64 ? 2 * total : 64;
