@@ -61,6 +61,7 @@ struct d_clusterPlan
 	int colorCap[B2_GRAPH_COLOR_COUNT]; /* lanes of an active color a CTA takes in one pass */
 	int bodyWarm;	/* warm start per body, fused with integrate velocities (contact-only clusters) */
 	int entryBytes; /* bytes of the per-body warm-start entries in each CTA's shared memory */
+	int jointConstants; /* plain revolute joints in slots read their constants from the slot */
 	int jointCap[B2_GRAPH_COLOR_COUNT]; /* joints of an active color a CTA takes in one pass */
 	int* assignedJoints;				/* color c, CTA r: joints at [jointOffset(c) * ranks + r * count(c)] */
 	int* assigned;	  /* color c, CTA r: slots at assigned[offset(c) * ranks + r * count(c)] */
@@ -207,13 +208,59 @@ union d_jointCopy
 	float4 w[sizeof( b2gJoint ) / 16];
 };
 
-/* Load a joint for a stage: the constant part of the record from global memory, the
-   accumulated impulses and solver constants (s[]) from the CTA's shared-memory slot when it
-   has one, else from the record. */
+/* A joint slot in a CTA's shared memory is 8 float4: the joint's s[] (accumulated impulses
+   and solver constants), then the constants a plain revolute joint (no spring, motor or
+   limit) reads in its warm start and solve, written at prepare:
+     [4] indexA, indexB (cluster keys, as int bits), invMassA, invMassB
+     [5] invIA, invIB, frameA.p
+     [6] frameB.p, deltaCenter
+     [7] softBias, softMass, softImpulse, 1 (plain revolute) or 0 (any other joint) */
+#define B2G_JOINT_SLOT_FLOAT4 8
+
+static __device__ __forceinline__ void d_clusterJointConstants( const b2gJoint* J, float4* slot, bool allow )
+{
+	bool plain = allow && J->type == b2_revoluteJoint && J->enableSpring == 0 && J->enableMotor == 0 && J->enableLimit == 0;
+	slot[4] = make_float4( __int_as_float( J->indexA ), __int_as_float( J->indexB ), J->invMassA, J->invMassB );
+	slot[5] = make_float4( J->invIA, J->invIB, J->frameA.p.x, J->frameA.p.y );
+	slot[6] = make_float4( J->frameB.p.x, J->frameB.p.y, J->deltaCenter.x, J->deltaCenter.y );
+	slot[7] = make_float4( J->softBias, J->softMass, J->softImpulse, __int_as_float( plain ? 1 : 0 ) );
+}
+
+/* Load a joint for a stage: the accumulated impulses and solver constants (s[]) from the
+   CTA's shared-memory slot when it has one, else from the record; a plain revolute joint's
+   constants from the slot too (revolute_joint.c:283-500 read nothing else with spring,
+   motor and limit off: the frames' rotations only feed the spring and the limit), any
+   other joint's constant part from global memory. */
 static __device__ __forceinline__ void d_clusterJointLoad( const b2gJoint* J, const float4* slot, d_jointCopy& copy )
 {
 	const float4* src = (const float4*)J;
 	const int sBegin = (int)( offsetof( b2gJoint, s ) / 16 );
+	if ( slot != nullptr && __float_as_int( slot[7].w ) == 1 )
+	{
+		const float4 c0 = slot[4], c1 = slot[5], c2 = slot[6], c3 = slot[7];
+		b2gJoint& j = copy.j;
+		j.type = b2_revoluteJoint;
+		j.indexA = __float_as_int( c0.x );
+		j.indexB = __float_as_int( c0.y );
+		j.invMassA = c0.z;
+		j.invMassB = c0.w;
+		j.invIA = c1.x;
+		j.invIB = c1.y;
+		j.frameA.p = b2Vec2{ c1.z, c1.w };
+		j.frameA.q = b2Rot{ 1.0f, 0.0f };
+		j.frameB.p = b2Vec2{ c2.x, c2.y };
+		j.frameB.q = b2Rot{ 1.0f, 0.0f };
+		j.deltaCenter = b2Vec2{ c2.z, c2.w };
+		j.softBias = c3.x;
+		j.softMass = c3.y;
+		j.softImpulse = c3.z;
+		j.enableSpring = 0;
+		j.enableMotor = 0;
+		j.enableLimit = 0;
+#pragma unroll
+		for ( int i = 0; i < 4; ++i ) copy.w[sBegin + i] = slot[i];
+		return;
+	}
 #pragma unroll
 	for ( int i = 0; i < (int)( sizeof( b2gJoint ) / 16 ); ++i )
 		if ( slot == nullptr || i < sBegin || i >= sBegin + 4 ) copy.w[i] = __ldcg( src + i );
@@ -299,8 +346,8 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 	extern __shared__ float4 s_mem[];
 	float4* sv = s_mem;
 	float4* sd = sv + plan.slotsPerRank;
-	float4* jimp = sd + plan.slotsPerRank; /* 4 float4 (s[]) per joint slot */
-	int* entries = (int*)( jimp + 4 * plan.jointSlotCap ); /* [slot * colorCount + k] when bodyWarm */
+	float4* jimp = sd + plan.slotsPerRank; /* B2G_JOINT_SLOT_FLOAT4 per joint slot */
+	int* entries = (int*)( jimp + B2G_JOINT_SLOT_FLOAT4 * plan.jointSlotCap ); /* [slot * colorCount + k] when bodyWarm */
 	b2gContactLane* lanes = (b2gContactLane*)( (char*)entries + plan.entryBytes );
 	__shared__ int s_cCount[B2_GRAPH_COLOR_COUNT];
 	__shared__ int s_jBegin[B2_GRAPH_COLOR_COUNT], s_jCount[B2_GRAPH_COLOR_COUNT];
@@ -383,8 +430,10 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 			if ( slot < plan.jointSlotCap )
 			{
 				const float4* s4 = (const float4*)J->s;
+				float4* js = jimp + B2G_JOINT_SLOT_FLOAT4 * slot;
 #pragma unroll
-				for ( int i = 0; i < 4; ++i ) jimp[4 * slot + i] = s4[i];
+				for ( int i = 0; i < 4; ++i ) js[i] = s4[i];
+				d_clusterJointConstants( J, js, plan.jointConstants != 0 );
 			}
 		}
 		const int begin = a.colorOffsets[color];
@@ -467,7 +516,7 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 					{
 						int slot = s_jSlot[k] + t;
 						b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k] + t];
-						float4* sp = slot < plan.jointSlotCap ? jimp + 4 * slot : nullptr;
+						float4* sp = slot < plan.jointSlotCap ? jimp + B2G_JOINT_SLOT_FLOAT4 * slot : nullptr;
 						if ( t != tid || haveNext == false ) d_clusterJointLoad( J, sp, next );
 						d_clusterJointRun( P, J, sp, next, bodies, stage );
 					}
@@ -482,7 +531,7 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 				{
 					int slot = s_jSlot[k + 1] + tid;
 					const b2gJoint* J = a.joints + plan.assignedJoints[s_jBegin[k + 1] + tid];
-					d_clusterJointLoad( J, slot < plan.jointSlotCap ? jimp + 4 * slot : nullptr, next );
+					d_clusterJointLoad( J, slot < plan.jointSlotCap ? jimp + B2G_JOINT_SLOT_FLOAT4 * slot : nullptr, next );
 				}
 				cluster.barrier_wait( std::move( token ) );
 			}
@@ -515,7 +564,7 @@ __global__ void __maxnreg__( 128 ) k_solveCluster( d_solveArgs a, d_jointBodies 
 			{
 				float4* d4 = (float4*)J->s;
 #pragma unroll
-				for ( int i = 0; i < 4; ++i ) d4[i] = jimp[4 * slot + i];
+				for ( int i = 0; i < 4; ++i ) d4[i] = jimp[B2G_JOINT_SLOT_FLOAT4 * slot + i];
 			}
 			int pa = J->indexA >= 0 ? d_clusterPosition( plan, J->indexA ) : -1;
 			int pb = J->indexB >= 0 ? d_clusterPosition( plan, J->indexB ) : -1;
@@ -596,7 +645,7 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 		int color = activeColors[k];
 		jointsTotal += useLists ? b->hSummary->bigJointCount[color] : jointOffsets[color + 1] - jointOffsets[color];
 	}
-	const long long jointSlotBytes = 4 * (long long)sizeof( float4 );
+	const long long jointSlotBytes = B2G_JOINT_SLOT_FLOAT4 * (long long)sizeof( float4 );
 	long long evenJoints = ( jointsTotal + ranks - 1 ) / ranks;
 	int jointSlotCap = jointsTotal > 0 ? (int)( evenJoints + evenJoints / 4 + 32 ) : 0;
 	/* without joints, the warm start runs per body with integrate velocities when the body
@@ -604,6 +653,16 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	const char* bodyWarmEnv = getenv( "B2G_CLUSTER_BODY_WARM" );
 	int bodyWarm = jointsTotal == 0 && activeColorCount > 0 && ( bodyWarmEnv == NULL || atoi( bodyWarmEnv ) != 0 );
 	long long entryBytes = bodyWarm ? ( ( (long long)slotsPerRank * activeColorCount * (long long)sizeof( int ) + 15 ) / 16 ) * 16 : 0;
+	/* joint slots take what the lanes leave: an even share of the lanes with an eighth more
+	   stays for them, the rest of the shared memory holds as many joints as it can */
+	if ( jointSlotCap > 0 )
+	{
+		long long laneNeed = ( lanesTotal + ranks - 1 ) / ranks;
+		laneNeed += laneNeed / 8 + 8;
+		long long room = (long long)B2G_CLUSTER_SMEM_MAX - bodyBytes - entryBytes - laneNeed * (long long)sizeof( b2gContactLane );
+		long long fit = room > 0 ? room / jointSlotBytes : 0;
+		if ( fit < jointSlotCap ) jointSlotCap = (int)fit;
+	}
 	int laneCap = 0;
 	for ( ;; )
 	{
@@ -670,6 +729,11 @@ extern "C" int b2gDev_ClusterSolve( b2gCompBuffers* b, const d_solveArgs* a, con
 	plan.laneCap = laneCap;
 	plan.jointSlotCap = jointSlotCap;
 	plan.bodyWarm = bodyWarm;
+	{
+		/* B2G_CLUSTER_JOINT_CONSTANTS=0: every joint's constant part from global memory */
+		const char* e = getenv( "B2G_CLUSTER_JOINT_CONSTANTS" );
+		plan.jointConstants = e == NULL || atoi( e ) != 0;
+	}
 	plan.entryBytes = (int)entryBytes;
 	plan.assigned = b->clusterAssigned;
 	plan.counts = b->clusterCounts;

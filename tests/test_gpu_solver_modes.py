@@ -53,3 +53,22 @@ def test_cluster_warm_start_per_body_matches_oracle(gpu_lib, oracle, monkeypatch
     monkeypatch.setenv("B2G_CLUSTER_BODY_WARM", body_warm)
     _, kind, a, b, c, seed, flags, steps = case
     lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps)
+
+
+# Plain revolute joints (no spring, motor or limit) kept in a cluster CTA's shared memory read
+# their constants from their slot; B2G_CLUSTER_JOINT_CONSTANTS=0 reads every joint's constant
+# part from global memory. Both must match the oracle bit for bit.
+JOINT_CONSTANT_CASES = [
+    ("joint_grid_big", B.JOINT_GRID_MIXED, 20, 60, 0, 5, B.NO_CONTINUOUS, 60),
+    ("joint_grid_no_warm_start", B.JOINT_GRID_MIXED, 20, 60, 0, 5, B.NO_CONTINUOUS | B.NO_WARM_STARTING, 30),
+    ("joint_zoo", B.JOINT_ZOO, 6, 0, 0, 4, B.NO_CONTINUOUS, 150),
+]
+
+
+@pytest.mark.parametrize("constants", ["1", "0"])
+@pytest.mark.parametrize("case", JOINT_CONSTANT_CASES, ids=[c[0] for c in JOINT_CONSTANT_CASES])
+def test_cluster_joint_constants_match_oracle(gpu_lib, oracle, monkeypatch, constants, case):
+    monkeypatch.setenv("B2G_SOLVER", "components")
+    monkeypatch.setenv("B2G_CLUSTER_JOINT_CONSTANTS", constants)
+    _, kind, a, b, c, seed, flags, steps = case
+    lockstep(gpu_lib, oracle, kind, a, b, c, seed, flags, steps)
