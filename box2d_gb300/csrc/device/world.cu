@@ -61,6 +61,7 @@ enum
 {
 	DK_MARK_MOVED = 0,
 	DK_FIND_PAIRS,
+	DK_PAIR_SET,
 	DK_CONVERT_TREE,
 	DK_INIT_CONTACTS,
 	DK_KILL_CONTACTS,
@@ -155,7 +156,14 @@ struct b2gDeviceWorld
 	int* shapeEnlarged;
 	/* contacts */
 	int contactCap;
+	int contactSlots; /* contact ids in use at most (the host's id pool high-water mark) */
 	b2gContact* contacts;
+	/* the shape-pair keys of the live contact slots (open addressing, linear probing, at
+	   most half full counting removed keys); the pair query drops pairs found here */
+	unsigned long long* pairSet;
+	int pairSetCap;		   /* a power of two, or 0 before the first contact */
+	long long pairSetUsed; /* keys written since the last rebuild, live or removed */
+	int pairSetStale;	   /* the slots changed behind the set (a snapshot restore) */
 	int* colorIds;
 	int colorIdsCap;
 	int colorOffsets[B2_GRAPH_COLOR_COUNT + 1];
@@ -475,6 +483,72 @@ static void dev_event( b2gDeviceWorld* dw, cudaEvent_t ev )
 	if ( dw->defer == NULL ) cudaEventRecord( ev, dw->stream );
 }
 
+/* ---- the device pair set: the host's pair set (broad_phase.c b2PairQueryCallback's
+   b2ContainsKey) kept beside the contact slots, so that the query returns new pairs only ---- */
+#define D_PAIR_EMPTY 0xffffffffffffffffull
+#define D_PAIR_REMOVED 0xfffffffffffffffeull
+
+static __device__ __forceinline__ unsigned long long d_pairKey( int a, int b )
+{
+	return a < b ? ( (unsigned long long)(unsigned)a << 32 ) | (unsigned)b : ( (unsigned long long)(unsigned)b << 32 ) | (unsigned)a;
+}
+
+static __device__ __forceinline__ unsigned long long d_pairMix( unsigned long long k )
+{
+	k ^= k >> 33;
+	k *= 0xff51afd7ed558ccdull;
+	k ^= k >> 33;
+	return k;
+}
+
+/* probes are bounded by the capacity: the set is at most half full, so a probe meets an
+   empty slot long before */
+static __device__ void d_pairSetInsert( unsigned long long* set, int cap, unsigned long long key )
+{
+	if ( cap <= 0 ) return;
+	unsigned mask = (unsigned)cap - 1u;
+	unsigned i = (unsigned)d_pairMix( key ) & mask;
+	for ( int probe = 0; probe < cap; ++probe )
+	{
+		unsigned long long old = atomicCAS( set + i, D_PAIR_EMPTY, key );
+		if ( old == D_PAIR_EMPTY || old == key ) return;
+		i = ( i + 1u ) & mask;
+	}
+}
+
+static __device__ bool d_pairSetContains( const unsigned long long* __restrict__ set, int cap, unsigned long long key )
+{
+	if ( cap <= 0 ) return false;
+	unsigned mask = (unsigned)cap - 1u;
+	unsigned i = (unsigned)d_pairMix( key ) & mask;
+	for ( int probe = 0; probe < cap; ++probe )
+	{
+		unsigned long long v = set[i];
+		if ( v == key ) return true;
+		if ( v == D_PAIR_EMPTY ) return false;
+		i = ( i + 1u ) & mask;
+	}
+	return false;
+}
+
+static __device__ void d_pairSetRemove( unsigned long long* set, int cap, unsigned long long key )
+{
+	if ( cap <= 0 ) return;
+	unsigned mask = (unsigned)cap - 1u;
+	unsigned i = (unsigned)d_pairMix( key ) & mask;
+	for ( int probe = 0; probe < cap; ++probe )
+	{
+		unsigned long long v = set[i];
+		if ( v == key )
+		{
+			set[i] = D_PAIR_REMOVED;
+			return;
+		}
+		if ( v == D_PAIR_EMPTY ) return;
+		i = ( i + 1u ) & mask;
+	}
+}
+
 /* ======================= broadphase pair query ======================= */
 struct d_markMovedArgs
 {
@@ -532,6 +606,8 @@ struct d_findPairsArgs
 	b2gStepCounters* counters;
 	int* packed;  /* every move's pairs, one contiguous run per move */
 	int* offsets; /* where each move's run starts (in pairs) */
+	const unsigned long long* pairSet; /* pairs that have a contact already: dropped */
+	int pairSetCap;
 };
 
 static __device__ void b_findPairs( const d_findPairsArgs& fa, int block, int grid )
@@ -608,6 +684,7 @@ static __device__ void b_findPairs( const d_findPairsArgs& fa, int block, int gr
 				int shapeId = e.y;
 				int a = proxyKey < queryKey ? shapeId : queryShape;
 				int b = proxyKey < queryKey ? queryShape : shapeId;
+				if ( d_pairSetContains( fa.pairSet, fa.pairSetCap, d_pairKey( a, b ) ) ) continue;
 				if ( count < capPerMove )
 				{
 					pairs[2 * ( (size_t)i * capPerMove + count )] = a;
@@ -647,11 +724,31 @@ static __device__ void b_findPairs( const d_findPairsArgs& fa, int block, int gr
 }
 
 /* ======================= contacts ======================= */
+struct d_pairSetArgs
+{
+	const b2gContact* contacts;
+	int n;
+	unsigned long long* set;
+	int cap;
+};
+
+/* the keys of every live slot, into an emptied set */
+static __device__ void b_pairSetRebuild( const d_pairSetArgs& a, int block, int grid )
+{
+	int i = block * blockDim.x + threadIdx.x;
+	if ( i >= a.n ) return;
+	const b2gContact* c = a.contacts + i;
+	if ( ( c->simFlags & B2G_S_LIVE ) == 0 ) return;
+	d_pairSetInsert( a.set, a.cap, d_pairKey( c->shapeIdA, c->shapeIdB ) );
+}
+
 struct d_contactListArgs
 {
 	b2gContact* contacts;
 	const void* list; /* b2gContactInit (init) or contact ids (kill) */
 	int n;
+	unsigned long long* pairSet;
+	int pairSetCap;
 };
 
 static __device__ void b_initContacts( const d_contactListArgs& a, int block, int grid )
@@ -670,13 +767,16 @@ static __device__ void b_initContacts( const d_contactListArgs& a, int block, in
 	c.friction = in.friction;
 	c.restitution = in.restitution;
 	contacts[in.contactId] = c;
+	d_pairSetInsert( a.pairSet, a.pairSetCap, d_pairKey( in.shapeIdA, in.shapeIdB ) );
 }
 
 static __device__ void b_killContacts( const d_contactListArgs& a, int block, int grid )
 {
 	int i = block * blockDim.x + threadIdx.x;
 	if ( i >= a.n ) return;
-	a.contacts[( (const int*)a.list )[i]].simFlags = 0;
+	b2gContact* c = a.contacts + ( (const int*)a.list )[i];
+	if ( c->simFlags & B2G_S_LIVE ) d_pairSetRemove( a.pairSet, a.pairSetCap, d_pairKey( c->shapeIdA, c->shapeIdB ) );
+	c->simFlags = 0;
 }
 
 /* ======================= islands and sleeping ======================= */
@@ -1090,7 +1190,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 					  dw->params,	  dw->center0,	 dw->enlargedBody, dw->shapes,		dw->aabb,		  dw->fat,
 					  dw->shapeEnlarged, dw->contacts, dw->colorIds,	dw->lanes,		dw->joints,		  dw->tree[0],
 					  dw->tree[1],	  dw->tree[2], dw->treeRaw[0], dw->treeRaw[1], dw->treeRaw[2],	 dw->moved[0],	  dw->moved[1],		dw->moved[2],	  
-					  dw->moveStage, dw->pairPacked, dw->pairBuf,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
+					  dw->moveStage, dw->pairPacked, dw->pairBuf, dw->pairSet,	  dw->pairCounts,	dw->changes,	  dw->enlargedRecs,
 					  dw->enlargedBoxes, dw->counters, dw->persistentScratch, dw->partnerOffsets, dw->partnerList,
 					  dw->sleepTime, dw->islandLocal, dw->islandInfo, dw->islandBits, dw->sensorIds, dw->sensorPairs,
 					  dw->sensorCount, dw->bulletSims, dw->bulletRecs, dw->bulletBoxes, dw->bulletCount, dw->sensorHits };
@@ -1371,8 +1471,51 @@ extern "C" int b2gDev_SetBodyForce( b2gDeviceWorld* dw, int awakeIndex, float fx
 	return (int)cudaGetLastError();
 }
 
+/* the pair set sized for every contact slot in use (4x, so that it stays at most half full
+   for a quarter of its capacity in further insertions) and filled from the live slots */
+static int pairSetRebuild( b2gDeviceWorld* dw, long long pending )
+{
+	long long slots = dw->contactSlots;
+	long long want = 4 * ( slots + pending );
+	int cap = dw->pairSetCap > 0 ? dw->pairSetCap : 4096;
+	while ( cap < want ) cap *= 2;
+	if ( cap != dw->pairSetCap || dw->pairSet == NULL )
+	{
+		int c = 0;
+		unsigned long long* fresh = NULL;
+		CK2( grow( dw, (void**)&fresh, &c, cap, sizeof( unsigned long long ) ) );
+		if ( dw->pairSet != NULL )
+		{
+			if ( dw->defer ) dw->retired.push_back( dw->pairSet );
+			else CK( cudaFree( dw->pairSet ) );
+		}
+		dw->pairSet = fresh;
+		dw->pairSetCap = cap;
+	}
+	CK2( dev_memset( dw, dw->pairSet, 0xff, (size_t)cap * sizeof( unsigned long long ) ) );
+	int n = dw->contactSlots < dw->contactCap ? dw->contactSlots : dw->contactCap;
+	if ( n > 0 )
+	{
+		d_pairSetArgs a = { dw->contacts, n, dw->pairSet, cap };
+		CK2( ( dev_launch<d_pairSetArgs, b_pairSetRebuild>( dw, DK_PAIR_SET, blocks( n ), a ) ) );
+	}
+	dw->pairSetUsed = slots;
+	dw->pairSetStale = 0;
+	return 0;
+}
+
+/* room for `pending` more keys (a rebuild when the set would pass half full) */
+static int pairSetReserve( b2gDeviceWorld* dw, long long pending )
+{
+	if ( dw->pairSetCap == 0 || dw->pairSetStale || 2 * ( dw->pairSetUsed + pending ) > dw->pairSetCap )
+		CK2( pairSetRebuild( dw, pending ) );
+	dw->pairSetUsed += pending;
+	return 0;
+}
+
 extern "C" int b2gDev_ReserveContacts( b2gDeviceWorld* dw, int capacity )
 {
+	if ( capacity > dw->contactSlots ) dw->contactSlots = capacity;
 	CK2( grow( dw, (void**)&dw->contacts, &dw->contactCap, capacity > 0 ? capacity : 1, sizeof( b2gContact ) ) );
 	int c = dw->changeCap;
 	CK2( grow( dw, (void**)&dw->changes, &c, 2 * ( capacity > 0 ? capacity : 1 ), sizeof( int ) ) );
@@ -1398,6 +1541,13 @@ extern "C" int b2gDev_UploadContacts( b2gDeviceWorld* dw, const b2gContact* in, 
 {
 	CK2( b2gDev_ReserveContacts( dw, count ) );
 	dw->prefetchValid = 0;
+	/* the slots past the snapshot's held another world state's contacts: cleared, and the
+	   pair set is rebuilt from the uploaded slots before its next use */
+	dw->pairSetStale = 1;
+	dw->contactSlots = count > 0 ? count : 0;
+	if ( dw->contactCap > count && dw->contacts != NULL )
+		CK( cudaMemsetAsync( dw->contacts + ( count > 0 ? count : 0 ), 0,
+							 (size_t)( dw->contactCap - ( count > 0 ? count : 0 ) ) * sizeof( b2gContact ), dw->stream ) );
 	if ( count <= 0 ) return 0;
 	dw->h2dBytes += (long long)count * (long long)sizeof( b2gContact );
 	CK( cudaMemcpyAsync( dw->contacts, in, (size_t)count * sizeof( b2gContact ), cudaMemcpyHostToDevice, dw->stream ) );
@@ -1497,8 +1647,9 @@ extern "C" int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* in
 {
 	if ( count == 0 ) return 0;
 	void* d = NULL;
+	CK2( pairSetReserve( dw, count ) );
 	CK2( uploadStaged( dw, inits, (size_t)count * sizeof( b2gContactInit ), &d ) );
-	d_contactListArgs a = { dw->contacts, d, count };
+	d_contactListArgs a = { dw->contacts, d, count, dw->pairSet, dw->pairSetCap };
 	return dev_launch<d_contactListArgs, b_initContacts>( dw, DK_INIT_CONTACTS, blocks( count ), a );
 }
 
@@ -1507,7 +1658,7 @@ extern "C" int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* ids, int coun
 	if ( count == 0 ) return 0;
 	void* d = NULL;
 	CK2( uploadStaged( dw, ids, (size_t)count * sizeof( int ), &d ) );
-	d_contactListArgs a = { dw->contacts, d, count };
+	d_contactListArgs a = { dw->contacts, d, count, dw->pairSet, dw->pairSetCap };
 	return dev_launch<d_contactListArgs, b_killContacts>( dw, DK_KILL_CONTACTS, blocks( count ), a );
 }
 
@@ -2079,6 +2230,7 @@ extern "C" void b2gDev_HostFree( void* p )
    next wait: counters, per-move counts and offsets, and the first `window` packed pairs */
 static int findPairsIssue( b2gDeviceWorld* dw, int n, bool countersReset )
 {
+	if ( dw->pairSetStale ) CK2( pairSetRebuild( dw, 0 ) );
 	CK2( joinEnlarge( dw ) );
 	CK2( grow( dw, (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
 	CK2( grow( dw, (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
@@ -2107,6 +2259,10 @@ static int findPairsIssue( b2gDeviceWorld* dw, int n, bool countersReset )
 	fa.counters = dw->counters;
 	fa.packed = dw->pairPacked;
 	fa.offsets = offsets;
+	/* B2G_PAIR_SET=0: every pair back to the host, which drops the existing ones itself */
+	static const int s_pairSetOn = getenv( "B2G_PAIR_SET" ) == NULL || atoi( getenv( "B2G_PAIR_SET" ) ) != 0;
+	fa.pairSet = dw->pairSet;
+	fa.pairSetCap = s_pairSetOn ? dw->pairSetCap : 0;
 	CK2( ( dev_launch<d_findPairsArgs, b_findPairs>( dw, DK_FIND_PAIRS, blocks( n ), fa ) ) );
 	CK2( dev_d2h( dw, dw->hCounters, dw->counters, sizeof( b2gStepCounters ) ) );
 	/* per-move counts and offsets are one array: one copy */
@@ -3389,6 +3545,7 @@ extern "C" int b2gDev_BatchFlush( b2gDevBatch* b, b2gDeviceWorld* const* worlds,
 		}
 		CK2( ( d_launchBatched<d_markMovedArgs, b_markMoved, 1>( b, L, DK_MARK_MOVED ) ) );
 		CK2( ( d_launchBatched<d_findPairsArgs, b_findPairs, 1>( b, L, DK_FIND_PAIRS ) ) );
+		CK2( ( d_launchBatched<d_pairSetArgs, b_pairSetRebuild, 1>( b, L, DK_PAIR_SET ) ) );
 		CK2( ( d_launchBatched<d_convertTreeArgs, b_convertTree, 1>( b, L, DK_CONVERT_TREE ) ) );
 		CK2( ( d_launchBatched<d_contactListArgs, b_initContacts, 1>( b, L, DK_INIT_CONTACTS ) ) );
 		CK2( ( d_launchBatched<d_contactListArgs, b_killContacts, 1>( b, L, DK_KILL_CONTACTS ) ) );

@@ -291,6 +291,8 @@ typedef struct h_pairSet
 } h_pairSet;
 void h_pairSetAdd( h_pairSet* s, uint64_t key );
 int h_pairSetContains( const h_pairSet* s, uint64_t key );
+/* start loading the slot a lookup of `key` probes first (a hint; no effect on results) */
+void h_pairSetPrefetch( const h_pairSet* s, uint64_t key );
 void h_pairSetRemove( h_pairSet* s, uint64_t key );
 void h_pairSetFree( h_pairSet* s );
 #define H_SHAPE_PAIR_KEY( K1, K2 ) ( ( K1 ) < ( K2 ) ? (uint64_t)( K1 ) << 32 | (uint64_t)( K2 ) : (uint64_t)( K2 ) << 32 | (uint64_t)( K1 ) )

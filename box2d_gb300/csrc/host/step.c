@@ -190,10 +190,15 @@ static int h_shouldShapesCollide( b2Filter a, b2Filter b )
    self and moved-pair dedupe; the host applies the remaining filters and creates contacts
    newest-first per move, as the reference's prepended pair lists do. */
 /* issue the pair query of the moved proxies; returns whether one was issued */
+static void h_flushContacts( h_world* w );
+
 static int h_pairsIssue( h_world* w )
 {
 	int moveCount = w->moveArray.count;
 	if ( moveCount == 0 ) return 0;
+	/* the device drops pairs whose contact exists: contacts destroyed since the last step
+	   (shape filters, destroyed joints) must leave its pair set before the query */
+	h_flushContacts( w );
 	uint64_t lap = b2GetTicks();
 	for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
 	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
@@ -231,6 +236,9 @@ static void h_pairsFinish( h_world* w )
 	int rc = b2gDev_FindPairsCollect( w->dev, &pairs, &counts, &total );
 	if ( rc != 0 ) h_fail( w, "pair query", rc );
 	h_lap( w, H_PHASE_PAIR_QUERY, &lap );
+	/* most pairs exist already: their set lookups miss the cache one after another unless
+	   the probed slots are requested first, all of them, so that the misses overlap */
+	for ( int p = 0; p < total; ++p ) h_pairSetPrefetch( &w->pairSet, H_SHAPE_PAIR_KEY( pairs[2 * p], pairs[2 * p + 1] ) );
 	int offset = 0;
 	for ( int i = 0; i < moveCount; ++i )
 	{

@@ -77,6 +77,13 @@ int h_pairSetContains( const h_pairSet* s, uint64_t key )
 	return 0;
 }
 
+void h_pairSetPrefetch( const h_pairSet* s, uint64_t key )
+{
+	if ( s->capacity == 0 ) return;
+	uint64_t mask = (uint64_t)s->capacity - 1;
+	__builtin_prefetch( s->keys + ( h_hashKey( key ) & mask ), 0, 3 );
+}
+
 void h_pairSetRemove( h_pairSet* s, uint64_t key )
 {
 	if ( s->capacity == 0 ) return;
