@@ -561,6 +561,8 @@ struct d_markMovedArgs
 	   query's dependent node reads do not each wait on DRAM */
 	const b2gTreeNode* trees[3];
 	int treeNodes[3];
+	const unsigned long long* pairSet; /* the set the query probes, prefetched as well */
+	int pairSetCap;
 };
 
 static __device__ void b_markMoved( const d_markMovedArgs& a, int block, int grid )
@@ -576,6 +578,11 @@ static __device__ void b_markMoved( const d_markMovedArgs& a, int block, int gri
 	{
 		const char* base = (const char*)a.trees[t];
 		const int lines = ( a.treeNodes[t] * (int)sizeof( b2gTreeNode ) + 127 ) / 128;
+		for ( int l = i; l < lines; l += threads ) asm volatile( "prefetch.global.L2 [%0];" ::"l"( base + 128 * (size_t)l ) );
+	}
+	{
+		const char* base = (const char*)a.pairSet;
+		const int lines = (int)( ( (long long)a.pairSetCap * 8 + 127 ) / 128 );
 		for ( int l = i; l < lines; l += threads ) asm volatile( "prefetch.global.L2 [%0];" ::"l"( base + 128 * (size_t)l ) );
 	}
 	if ( i >= a.n ) return;
@@ -2230,7 +2237,6 @@ extern "C" void b2gDev_HostFree( void* p )
    next wait: counters, per-move counts and offsets, and the first `window` packed pairs */
 static int findPairsIssue( b2gDeviceWorld* dw, int n, bool countersReset )
 {
-	if ( dw->pairSetStale ) CK2( pairSetRebuild( dw, 0 ) );
 	CK2( joinEnlarge( dw ) );
 	CK2( grow( dw, (void**)&dw->pairBuf, &dw->pairBufCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
 	CK2( grow( dw, (void**)&dw->pairPacked, &dw->pairPackedCap, 2 * n * dw->pairPerMove, sizeof( int ) ) );
@@ -2275,6 +2281,8 @@ static int findPairsIssue( b2gDeviceWorld* dw, int n, bool countersReset )
 extern "C" int b2gDev_FindPairsIssue( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int n )
 {
 	dev_event( dw, dw->ev[0] );
+	/* the pair set is current before the query and its prefetch use it */
+	if ( dw->pairSetStale ) CK2( pairSetRebuild( dw, 0 ) );
 	/* one staged copy of the moved proxies */
 	int stageBytes = n * 24;
 	CK2( growHost( &dw->hMoveStage, &dw->hMoveStageCap, stageBytes, 1 ) );
@@ -2300,6 +2308,8 @@ extern "C" int b2gDev_FindPairsIssue( b2gDeviceWorld* dw, const int* keys, const
 		ma.trees[t] = dw->tree[t];
 		ma.treeNodes[t] = dw->tree[t] != NULL && dw->treeRoot[t] >= 0 ? dw->treeNodes[t] : 0;
 	}
+	ma.pairSet = dw->pairSet;
+	ma.pairSetCap = dw->pairSet != NULL ? dw->pairSetCap : 0;
 	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
 	return findPairsIssue( dw, n, true );
 }
@@ -2332,7 +2342,7 @@ extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int*
 	dw->defer = deferred;
 	/* clear the moved flags (recorded with the next batch when batching) */
 	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 0,
-						   nullptr, { nullptr, nullptr, nullptr }, { 0, 0, 0 } };
+						   nullptr, { nullptr, nullptr, nullptr }, { 0, 0, 0 }, nullptr, 0 };
 	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
 	/* next step's window follows this step's count, both ways */
 	dw->pairWindow = 2 * total > 64 ? 2 * total : 64;
