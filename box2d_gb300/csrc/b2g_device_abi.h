@@ -317,6 +317,9 @@ int b2gDev_InitContacts( b2gDeviceWorld* dw, const b2gContactInit* inits, int co
 int b2gDev_KillContacts( b2gDeviceWorld* dw, const int* contactIds, int count );
 int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* colorContactIds, const int* colorContactOffsets,
 						 int totalContacts );
+/* the same from the colors' own id lists (listCount lists, counts[i] ids each) */
+int b2gDev_UploadColorLists( b2gDeviceWorld* dw, const int* const* lists, const int* counts, int listCount, const int* offsets,
+							 int total );
 /* contact slots [0, count) to the host (slots the device never held read as zeros), and
    back (a world snapshot's restore) */
 int b2gDev_DownloadContacts( b2gDeviceWorld* dw, b2gContact* out, int count );

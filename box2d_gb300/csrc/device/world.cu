@@ -1810,6 +1810,39 @@ extern "C" int b2gDev_UploadColors( b2gDeviceWorld* dw, const int* ids, const in
 	return 0;
 }
 
+/* the same from the colors' own lists: gathered straight into the upload arena */
+extern "C" int b2gDev_UploadColorLists( b2gDeviceWorld* dw, const int* const* lists, const int* counts, int listCount,
+										const int* offsets, int total )
+{
+	dw->topologyDirty = 1;
+	dw->topologyEpoch += 1;
+	CK2( grow( dw, (void**)&dw->colorIds, &dw->colorIdsCap, total > 0 ? total : 1, sizeof( int ) ) );
+	memcpy( dw->colorOffsets, offsets, sizeof( dw->colorOffsets ) );
+	if ( total <= 0 ) return 0;
+	size_t bytes = (size_t)total * sizeof( int );
+	int* dst = NULL;
+	size_t off = 0;
+	if ( dw->defer )
+	{
+		dst = (int*)malloc( bytes ); /* a recorded upload copies its source at once */
+		if ( dst == NULL ) return (int)cudaErrorMemoryAllocation;
+	}
+	else
+	{
+		CK2( arenaAlloc( dw, bytes, &off ) );
+		dst = (int*)( (char*)dw->upHost + off );
+	}
+	int at = 0;
+	for ( int i = 0; i < listCount; ++i )
+	{
+		if ( counts[i] > 0 ) memcpy( dst + at, lists[i], (size_t)counts[i] * sizeof( int ) );
+		at += counts[i];
+	}
+	int rc = dev_h2d( dw, dw->colorIds, dst, bytes );
+	if ( dw->defer ) free( dst );
+	return rc;
+}
+
 extern "C" void b2gDev_ContactView( b2gDeviceWorld* dw, const b2gContact** contacts, const int** colorIds, int* colorOffsets,
 									void** stream, int* device )
 {

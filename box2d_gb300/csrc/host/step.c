@@ -292,11 +292,14 @@ static void h_uploadColors( h_world* w )
 		total += w->colors[i].contactIds.count;
 	}
 	offsets[B2_GRAPH_COLOR_COUNT] = total;
-	int* ids = malloc( (size_t)( total > 0 ? total : 1 ) * sizeof( int ) );
+	const int* lists[B2_GRAPH_COLOR_COUNT];
+	int counts[B2_GRAPH_COLOR_COUNT];
 	for ( int i = 0; i < B2_GRAPH_COLOR_COUNT; ++i )
-		memcpy( ids + offsets[i], w->colors[i].contactIds.data, (size_t)w->colors[i].contactIds.count * sizeof( int ) );
-	int rc = b2gDev_UploadColors( w->dev, ids, offsets, total );
-	free( ids );
+	{
+		lists[i] = w->colors[i].contactIds.data;
+		counts[i] = w->colors[i].contactIds.count;
+	}
+	int rc = b2gDev_UploadColorLists( w->dev, lists, counts, B2_GRAPH_COLOR_COUNT, offsets, total );
 	if ( rc != 0 ) h_fail( w, "color upload", rc );
 	w->colorsDirty = 0;
 }
@@ -376,8 +379,24 @@ static int h_cmpInt( const void* a, const void* b )
 static void h_contactStatePass( h_world* w, const int* changes, int count )
 {
 	int endEventArrayIndex = w->endEventArrayIndex;
+	/* the changed contacts are scattered over the contact array: their records are
+	   requested first, and each iteration requests the shapes and bodies of a later one, so
+	   that the cache misses overlap instead of following one another */
+	for ( int i = 0; i < count; ++i ) __builtin_prefetch( w->contacts.data + changes[2 * i], 1, 3 );
+	const int ahead = 8;
 	for ( int i = 0; i < count; ++i )
 	{
+		if ( i + ahead < count )
+		{
+			const h_contact* next = w->contacts.data + changes[2 * ( i + ahead )];
+			if ( next->shapeIdA >= 0 && next->shapeIdB >= 0 && next->edges[0].bodyId >= 0 && next->edges[1].bodyId >= 0 )
+			{
+				__builtin_prefetch( w->shapes.data + next->shapeIdA, 0, 3 );
+				__builtin_prefetch( w->shapes.data + next->shapeIdB, 0, 3 );
+				__builtin_prefetch( w->bodies.data + next->edges[0].bodyId, 1, 3 );
+				__builtin_prefetch( w->bodies.data + next->edges[1].bodyId, 1, 3 );
+			}
+		}
 		int contactId = changes[2 * i];
 		uint32_t simFlags = (uint32_t)changes[2 * i + 1];
 		h_contact* contact = w->contacts.data + contactId;
