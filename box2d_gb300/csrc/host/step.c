@@ -206,6 +206,19 @@ static int h_pairsIssue( h_world* w )
 	int* shapeIds = malloc( (size_t)moveCount * sizeof( int ) );
 	for ( int i = 0; i < moveCount; ++i )
 	{
+		/* the moved proxies' nodes and shapes are scattered: a later move's node and a
+		   nearer move's shape are requested ahead */
+		if ( i + 16 < moveCount )
+		{
+			int k16 = w->moveArray.data[i + 16];
+			__builtin_prefetch( w->trees[H_PROXY_TYPE( k16 )].nodes + H_PROXY_ID( k16 ), 0, 3 );
+		}
+		if ( i + 8 < moveCount )
+		{
+			int k8 = w->moveArray.data[i + 8];
+			int s8 = (int)w->trees[H_PROXY_TYPE( k8 )].nodes[H_PROXY_ID( k8 )].userData;
+			__builtin_prefetch( &w->shapes.data[s8].fatAABB, 0, 3 );
+		}
 		/* a leaf's box is its shape's fat box; the shape's copy is read because the worker
 		   may still be enlarging the host tree after the last step */
 		int key = w->moveArray.data[i];
@@ -499,6 +512,8 @@ static int h_enlargeOnDevice( h_world* w, const int* recs, const float* boxes, i
 	}
 	for ( int i = 0; i < count; ++i )
 	{
+		/* the records' shapes are scattered: request a later record's shape ahead */
+		if ( i + 8 < count ) __builtin_prefetch( &w->shapes.data[recs[4 * ( i + 8 ) + 1]].fatAABB, 1, 3 );
 		int shapeId = recs[4 * i + 1];
 		int enlarged = recs[4 * i + 2];
 		int fastBullet = recs[4 * i + 3];
