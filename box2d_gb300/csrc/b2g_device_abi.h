@@ -284,6 +284,10 @@ int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* 
    the pointers refer to page-locked staging valid until the next call */
 /* send the host-mirrored body state down behind the step's work, without waiting */
 int b2gDev_PrefetchState( b2gDeviceWorld* dw, int bodyCount, int awakeCount );
+/* whether the prefetched state is still the device's; put back after device work that
+   changes no body state */
+int b2gDev_PrefetchIsValid( b2gDeviceWorld* dw );
+void b2gDev_PrefetchKeep( b2gDeviceWorld* dw, int valid );
 int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awakeCount, const float** xf, const float** center,
 						  const uint32_t** flags, const float** stateV, const float** sleepTime );
 
@@ -415,6 +419,8 @@ int b2gDev_Solve( b2gDeviceWorld* dw, const b2gStepParams* params, const int* ac
    collect the results after the world's wait (b2gDev_Synchronize) or a batch flush */
 int b2gDev_FindPairsIssue( b2gDeviceWorld* dw, const int* keys, const float* boxes, const int* shapes, int count );
 int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int** outCounts, int* outTotal );
+/* drop the issued query (its results are not collected; its moved flags are cleared) */
+int b2gDev_FindPairsDiscard( b2gDeviceWorld* dw );
 int b2gDev_CollideIssue( b2gDeviceWorld* dw, const b2gStepParams* params, int contactIdCapacity );
 int b2gDev_CollideCollect( b2gDeviceWorld* dw, const int** outChanges, int* outChangeCount, int* outRecycled );
 int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* params, const int* activeColors, int activeColorCount,

@@ -283,6 +283,7 @@ struct b2gDeviceWorld
 	   last prefetch, and no device work was issued or recorded since */
 	int prefetchValid, prefetchBodies, prefetchAwake;
 	int prefetchWait; /* the prefetch copies were issued on the world's stream (not delivered by a flush) */
+	cudaEvent_t prefetchEvent; /* after the prefetch copies: work queued behind them is not waited for */
 	float* hSleepTime;
 	int hSleepTimeCap;
 };
@@ -1191,6 +1192,7 @@ extern "C" void b2gDev_Destroy( b2gDeviceWorld* dw )
 	if ( dw == NULL ) return;
 	cudaStreamSynchronize( dw->stream );
 	cudaEventDestroy( dw->syncEvent );
+	if ( dw->prefetchEvent ) cudaEventDestroy( dw->prefetchEvent );
 	void* dptrs[] = { dw->xf,		  dw->center,	 dw->localCenter, dw->invMass,		dw->invI,		  dw->minExtent,
 					  dw->maxExtent,  dw->sleepThreshold, dw->safetyFactor, dw->awakeIndex, dw->bodyType,	dw->bodyFlags,
 					  dw->shapeStart, dw->shapeCount, dw->shapeList, dw->awakeBodyId,	dw->stateV,		  dw->stateD,
@@ -1369,7 +1371,11 @@ extern "C" int b2gDev_DownloadState( b2gDeviceWorld* dw, int bodyCount, int awak
 		/* the step already sent the state down: wait for it (a batched step's flush has
 		   delivered it already) */
 		dw->prefetchValid = 0;
-		if ( dw->prefetchWait ) CK2( drain( dw ) );
+		if ( dw->prefetchWait )
+		{
+			if ( dw->prefetchEvent != NULL && dw->blockingSync == 0 ) CK( cudaEventSynchronize( dw->prefetchEvent ) );
+			else CK2( drain( dw ) );
+		}
 		*xf = (const float*)dw->hXf;
 		*center = (const float*)dw->hCenter;
 		*flags = dw->hFlags;
@@ -1429,10 +1435,20 @@ extern "C" int b2gDev_PrefetchState( b2gDeviceWorld* dw, int bodyCount, int awak
 	}
 	dw->prefetchValid = 1;
 	dw->prefetchWait = dw->defer == NULL;
+	if ( dw->defer == NULL )
+	{
+		if ( dw->prefetchEvent == NULL ) CK( cudaEventCreateWithFlags( &dw->prefetchEvent, cudaEventDisableTiming ) );
+		CK( cudaEventRecord( dw->prefetchEvent, dw->stream ) );
+	}
 	dw->prefetchBodies = bodyCount;
 	dw->prefetchAwake = awakeCount;
 	return 0;
 }
+
+/* device work that changes no body state (the pair query) may follow the prefetch without
+   making it stale: the caller reads the flag before and puts it back after */
+extern "C" int b2gDev_PrefetchIsValid( b2gDeviceWorld* dw ) { return dw->prefetchValid; }
+extern "C" void b2gDev_PrefetchKeep( b2gDeviceWorld* dw, int valid ) { dw->prefetchValid = valid; }
 
 extern "C" int b2gDev_DownloadBodies( b2gDeviceWorld* dw, int bodyCount, float* xf, float* center, uint32_t* flags )
 {
@@ -2393,6 +2409,20 @@ extern "C" int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int*
 	*outPairs = dw->hPairs;
 	*outCounts = dw->hPairCounts;
 	*outTotal = total;
+	return 0;
+}
+
+/* drop an issued query whose results will not be used: its moved flags are cleared (the
+   next query sets its own) */
+extern "C" int b2gDev_FindPairsDiscard( b2gDeviceWorld* dw )
+{
+	int n = dw->pendingMoves;
+	dw->pendingMoves = 0;
+	dw->pairsTimingPending = 0;
+	if ( n <= 0 ) return 0;
+	d_markMovedArgs ma = { dw->moved[b2_dynamicBody], dw->moved[b2_kinematicBody], dw->moved[b2_staticBody], dw->moveKeys, n, 0,
+						   nullptr, { nullptr, nullptr, nullptr }, { 0, 0, 0 }, nullptr, 0 };
+	CK2( ( dev_launch<d_markMovedArgs, b_markMoved>( dw, DK_MARK_MOVED, blocks( n ), ma ) ) );
 	return 0;
 }
 

@@ -248,6 +248,17 @@ typedef struct h_world
 	float stepTimeStep;
 	uint64_t stepTicks, stepT0;
 	int stepPairsIssued, stepSolveIssued, stepSolveLate;
+	/* the moved proxies' boxes and shapes sent with a pair query (reused buffers) */
+	float* moveBoxes;
+	int* moveShapes;
+	int moveBufCap;
+	/* the next step's pair query, issued at a step's end behind the state download; the next
+	   step uses its results when nothing the query reads changed in between (the move keys
+	   and boxes, the trees, the contacts), else drops it */
+	int specIssued, specCount, specCap, specStale;
+	int* specKeys;
+	float* specBoxes;
+	int specTreeVersion[3];
 	void* rebuildWorker; /* host thread for the tree rebuild (step.c) */
 } h_world;
 
@@ -317,6 +328,8 @@ void h_syncShapeBoxes( h_world* w );
 /* frees every array of the world's simulation state; the device world, the rebuild worker
    and the tape stay (world.c) */
 void h_freeWorldArrays( h_world* w );
+/* drop the pair query issued at the last step's end, if any */
+void h_dropSpeculativePairs( h_world* w );
 /* the host thread pool (batch.c): fn(ctx, i) for i in [0, count) on up to `threads` threads,
    the caller among them; returns 0 without running anything when the pool is taken (by
    another thread, or by the caller itself inside a pool task): the caller then runs the

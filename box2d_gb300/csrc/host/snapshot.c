@@ -255,6 +255,13 @@ static void h_snapClearPointers( h_world* t )
 		memset( &t->movedProxies[i], 0, sizeof( t->movedProxies[i] ) );
 	}
 	memset( &t->moveArray, 0, sizeof( t->moveArray ) );
+	t->moveBoxes = NULL;
+	t->moveShapes = NULL;
+	t->moveBufCap = 0;
+	t->specKeys = NULL;
+	t->specBoxes = NULL;
+	t->specCap = 0;
+	t->specIssued = 0;
 	t->pairSet.keys = NULL;
 	memset( &t->chains, 0, sizeof( t->chains ) );
 	memset( &t->sensors, 0, sizeof( t->sensors ) );
@@ -488,8 +495,10 @@ bool b2World_Restore( b2WorldId worldId, const uint8_t* image, int size )
 		return false;
 	}
 
-	/* the world keeps its slot, generation, device world, rebuild worker and tape */
+	/* the world keeps its slot, generation, device world, rebuild worker and tape; a pair
+	   query issued for the next step is dropped */
 	h_joinRebuild( w );
+	h_dropSpeculativePairs( w );
 	h_freeWorldArrays( w );
 	h_world live = *w;
 	*w = *t;

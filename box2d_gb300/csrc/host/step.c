@@ -192,18 +192,22 @@ static int h_shouldShapesCollide( b2Filter a, b2Filter b )
 /* issue the pair query of the moved proxies; returns whether one was issued */
 static void h_flushContacts( h_world* w );
 
-static int h_pairsIssue( h_world* w )
+/* the moved proxies' fat boxes and shapes, in move order, into the world's buffers */
+static void h_moveBoxes( h_world* w )
 {
 	int moveCount = w->moveArray.count;
-	if ( moveCount == 0 ) return 0;
-	/* the device drops pairs whose contact exists: contacts destroyed since the last step
-	   (shape filters, destroyed joints) must leave its pair set before the query */
-	h_flushContacts( w );
-	uint64_t lap = b2GetTicks();
-	for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
-	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
-	float* boxes = malloc( (size_t)moveCount * 4 * sizeof( float ) );
-	int* shapeIds = malloc( (size_t)moveCount * sizeof( int ) );
+	if ( moveCount > w->moveBufCap )
+	{
+		int cap = w->moveBufCap > 0 ? w->moveBufCap : 256;
+		while ( cap < moveCount ) cap *= 2;
+		free( w->moveBoxes );
+		free( w->moveShapes );
+		w->moveBoxes = malloc( (size_t)cap * 4 * sizeof( float ) );
+		w->moveShapes = malloc( (size_t)cap * sizeof( int ) );
+		w->moveBufCap = cap;
+	}
+	float* boxes = w->moveBoxes;
+	int* shapeIds = w->moveShapes;
 	for ( int i = 0; i < moveCount; ++i )
 	{
 		/* the moved proxies' nodes and shapes are scattered: a later move's node and a
@@ -231,11 +235,91 @@ static int h_pairsIssue( h_world* w )
 		boxes[4 * i + 3] = fat.upperBound.y;
 		shapeIds[i] = shapeId;
 	}
-	int rc = b2gDev_FindPairsIssue( w->dev, w->moveArray.data, boxes, shapeIds, moveCount );
-	free( boxes );
-	free( shapeIds );
+}
+
+void h_dropSpeculativePairs( h_world* w )
+{
+	if ( w->specIssued == 0 ) return;
+	w->specIssued = 0;
+	int rc = b2gDev_FindPairsDiscard( w->dev );
+	if ( rc != 0 ) h_fail( w, "pair query", rc );
+}
+
+/* the query issued at the last step's end answers this step's when it read what this one
+   would: the same move keys, the same boxes (the shapes' fat boxes now), the same tree
+   versions, no contact created or destroyed since, and no world change that re-sends the
+   device state */
+static int h_speculationHolds( h_world* w )
+{
+	int n = w->moveArray.count;
+	if ( w->specStale || n != w->specCount || w->pendingKills.count != 0 || w->pendingInits.count != 0 ) return 0;
+	for ( int t = 0; t < 3; ++t )
+		if ( w->trees[t].version != w->specTreeVersion[t] ) return 0;
+	if ( memcmp( w->moveArray.data, w->specKeys, (size_t)n * sizeof( int ) ) != 0 ) return 0;
+	h_moveBoxes( w );
+	return memcmp( w->moveBoxes, w->specBoxes, (size_t)n * 4 * sizeof( float ) ) == 0;
+}
+
+static int h_pairsIssue( h_world* w )
+{
+	int moveCount = w->moveArray.count;
+	if ( w->specIssued )
+	{
+		if ( moveCount > 0 && b2gDev_IsRecording( w->dev ) == 0 && h_speculationHolds( w ) )
+		{
+			w->specIssued = 0;
+			return 1;
+		}
+		h_dropSpeculativePairs( w );
+	}
+	if ( moveCount == 0 ) return 0;
+	/* the device drops pairs whose contact exists: contacts destroyed since the last step
+	   (shape filters, destroyed joints) must leave its pair set before the query */
+	h_flushContacts( w );
+	uint64_t lap = b2GetTicks();
+	for ( int t = 0; t < 3; ++t ) h_uploadTree( w, t );
+	h_lap( w, H_PHASE_TREE_UPLOAD, &lap );
+	h_moveBoxes( w );
+	int rc = b2gDev_FindPairsIssue( w->dev, w->moveArray.data, w->moveBoxes, w->moveShapes, moveCount );
 	if ( rc != 0 ) h_fail( w, "pair query", rc );
 	return 1;
+}
+
+/* Issue the next step's pair query at this step's end, behind the state download: it runs
+   while the host finishes the step and the caller works between steps, and the next step
+   waits for its results instead of issuing it (B2G_SPECULATE=0: never). */
+static void h_pairsSpeculate( h_world* w )
+{
+	static int s_on = -1;
+	if ( s_on < 0 )
+	{
+		const char* e = getenv( "B2G_SPECULATE" );
+		s_on = e == NULL || atoi( e ) != 0;
+	}
+	if ( s_on == 0 || w->moveArray.count == 0 || b2gDev_IsRecording( w->dev ) || w->devReady == 0 ) return;
+	/* the query, its contact flush and tree uploads change no body state: the state
+	   download issued before it stays the step's */
+	int prefetched = b2gDev_PrefetchIsValid( w->dev );
+	int issued = h_pairsIssue( w );
+	b2gDev_PrefetchKeep( w->dev, prefetched );
+	if ( issued == 0 ) return;
+	int n = w->moveArray.count;
+	if ( n > w->specCap )
+	{
+		int cap = w->specCap > 0 ? w->specCap : 256;
+		while ( cap < n ) cap *= 2;
+		free( w->specKeys );
+		free( w->specBoxes );
+		w->specKeys = malloc( (size_t)cap * sizeof( int ) );
+		w->specBoxes = malloc( (size_t)cap * 4 * sizeof( float ) );
+		w->specCap = cap;
+	}
+	memcpy( w->specKeys, w->moveArray.data, (size_t)n * sizeof( int ) );
+	memcpy( w->specBoxes, w->moveBoxes, (size_t)n * 4 * sizeof( float ) );
+	for ( int t = 0; t < 3; ++t ) w->specTreeVersion[t] = w->trees[t].version;
+	w->specCount = n;
+	w->specStale = 0;
+	w->specIssued = 1;
 }
 
 /* after the wait: filter the pairs and create contacts newest-first per move */
@@ -649,6 +733,9 @@ int h_stepBegin( h_world* w, float timeStep, int subStepCount )
 	w->stepTicks = b2GetTicks();
 	w->stepTimeStep = timeStep;
 
+	/* a world change since the last step re-sends the device state: a query issued at the
+	   last step's end does not hold */
+	if ( w->devReady == 0 ) w->specStale = 1;
 	h_ensureDevice( w );
 	/* contacts whose solver set the API changed since the last step */
 	w->wokeInStep = 0;
@@ -839,6 +926,7 @@ void h_stepFinish( h_world* w )
 		int rc = b2gDev_PrefetchState( w->dev, w->bodies.count, w->awakeBodyIds.count );
 		if ( rc != 0 ) h_fail( w, "state prefetch", rc );
 	}
+	if ( w->stepSolveIssued ) h_pairsSpeculate( w );
 	w->profile.step = h_ms( w->stepTicks );
 	w->endEventArrayIndex = 1 - w->endEventArrayIndex;
 	w->endEvents[w->endEventArrayIndex].count = 0;

@@ -234,6 +234,14 @@ b2WorldId b2CreateWorld( const b2WorldDef* def )
    world, the rebuild worker and the tape stay */
 void h_freeWorldArrays( h_world* w )
 {
+	free( w->moveBoxes );
+	free( w->moveShapes );
+	free( w->specKeys );
+	free( w->specBoxes );
+	w->moveBoxes = w->specBoxes = NULL;
+	w->moveShapes = w->specKeys = NULL;
+	w->moveBufCap = w->specCap = 0;
+	w->specIssued = 0;
 	for ( int i = 0; i < 3; ++i )
 	{
 		h_treeDestroy( w->trees + i );
