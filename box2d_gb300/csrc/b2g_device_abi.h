@@ -423,6 +423,9 @@ int b2gDev_FindPairsCollect( b2gDeviceWorld* dw, int** outPairs, int** outCounts
 int b2gDev_FindPairsDiscard( b2gDeviceWorld* dw );
 int b2gDev_CollideIssue( b2gDeviceWorld* dw, const b2gStepParams* params, int contactIdCapacity );
 int b2gDev_CollideCollect( b2gDeviceWorld* dw, const int** outChanges, int* outChangeCount, int* outRecycled );
+/* start the solve's component analysis from the touching contacts the narrowphase left,
+   beside the host's contact-state pass (large worlds solved by components) */
+int b2gDev_ComponentsEarly( b2gDeviceWorld* dw, int awakeCount );
 int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* params, const int* activeColors, int activeColorCount,
 					   int awakeCount );
 int b2gDev_SolveCollect( b2gDeviceWorld* dw, const int** outEnlarged, int* outEnlargedCount, const float** outFatBoxes,

@@ -119,6 +119,20 @@ __global__ void k_compUnion( d_solveArgs a, const int* awakeIndex, int* parent, 
 	if ( ia >= 0 && ib >= 0 ) d_unite( parent, ia, ib );
 }
 
+/* unions of the live, awake contacts the narrowphase left touching (their awake indices
+   are the narrowphase's, current for every contact it processed) */
+__global__ void k_compUnionTouching( const b2gContact* contacts, int capacity, int* parent, int n )
+{
+	int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if ( i >= capacity ) return;
+	const b2gContact* c = contacts + i;
+	uint32_t f = c->simFlags;
+	if ( ( f & B2G_S_LIVE ) == 0 || ( f & B2G_S_TOUCHING ) == 0 || ( f & B2G_S_ASLEEP ) != 0 ) return;
+	int ia = c->bodySimIndexA, ib = c->bodySimIndexB;
+	if ( ia < 0 || ib < 0 || ia >= n || ib >= n ) return;
+	d_unite( parent, ia, ib );
+}
+
 /* the forest over the joints, every body pointing at its root (no union runs meanwhile, so
    each root is final), kept for later analyses */
 __global__ void k_compFlatten( int* parent, int* forest, int n )
@@ -618,6 +632,53 @@ static d_compArgs compArgs( b2gCompBuffers* b, const int* jointOffsets, const in
 	return c;
 }
 
+extern "C" int b2gDev_CompUnionEarly( b2gCompBuffers* b, const b2gContact* contacts, int capacity, const b2gJoint* joints,
+									  const int* awakeIndex, int n, int jointTotal, long long jointEpoch, cudaStream_t stream,
+									  long long* launches )
+{
+	b->earlyValid = 0;
+	if ( n <= 0 || jointEpoch < 0 ) return 0;
+	int rc = b2gDev_CompReserve( b, n, 1, jointTotal );
+	if ( rc ) return rc;
+	bool keptForest = jointTotal > 0 && b->jointForest != NULL && b->jointForestEpoch == jointEpoch && b->jointForestN == n &&
+					  b->jointForestJoints == jointTotal;
+	if ( keptForest == false && jointTotal > 0 )
+	{
+		if ( n > b->jointForestCap || b->jointForest == NULL )
+		{
+			int rc2 = growPair( &b->jointForest, NULL, &b->jointForestCap, n, 1 );
+			if ( rc2 ) return rc2;
+		}
+		d_solveArgs ja;
+		memset( &ja, 0, sizeof( ja ) );
+		ja.joints = (b2gJoint*)joints;
+		k_compInit<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
+		k_compUnion<<<compBlocks( jointTotal ), B2G_COMP_THREADS, 0, stream>>>( ja, awakeIndex, b->parent, 0, 0, jointTotal );
+		k_compFlatten<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->jointForest, n );
+		*launches += 3;
+		b->jointForestEpoch = jointEpoch;
+		b->jointForestN = n;
+		b->jointForestJoints = jointTotal;
+		keptForest = true;
+	}
+	if ( keptForest ) k_compInitFrom<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->jointForest, b->compData, n );
+	else k_compInit<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
+	*launches += 1;
+	if ( capacity > 0 )
+	{
+		k_compUnionTouching<<<compBlocks( capacity ), B2G_COMP_THREADS, 0, stream>>>( contacts, capacity, b->parent, n );
+		*launches += 1;
+	}
+	k_compRoots<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
+	*launches += 1;
+	CKC( cudaGetLastError() );
+	b->earlyValid = 1;
+	b->earlyN = n;
+	b->earlyJoints = jointTotal;
+	b->earlyEpoch = jointEpoch;
+	return 0;
+}
+
 extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const int* awakeIndex,
 								   int total, int jointTotal, int forceBig, long long jointEpoch, cudaStream_t stream,
 								   long long* launches )
@@ -641,12 +702,15 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 	CKC( cudaMemsetAsync( b->binRange + 3 * b->binCap, 0, (size_t)3 * b->binCap * sizeof( int ), stream ) );
 	CKC( cudaMemsetAsync( b->summary, 0, sizeof( b2gCompSummary ), stream ) );
 	int cons = total + jointTotal;
+	const bool early = b->earlyValid && jointEpoch >= 0 && b->earlyEpoch == jointEpoch && b->earlyN == n &&
+					   b->earlyJoints == jointTotal;
+	b->earlyValid = 0;
 	/* Roots are the smallest index of each component whatever the order of the unions, so
 	   the joints' unions can be done once and kept: later analyses start from that forest
 	   and add the contacts. Joints change rarely; contacts begin and end every step. */
 	bool keptForest = jointTotal > 0 && jointEpoch >= 0 && b->jointForest != NULL && b->jointForestEpoch == jointEpoch &&
 					  b->jointForestN == n && b->jointForestJoints == jointTotal;
-	if ( keptForest == false && jointTotal > 0 && jointEpoch >= 0 )
+	if ( early == false && keptForest == false && jointTotal > 0 && jointEpoch >= 0 )
 	{
 		if ( n > b->jointForestCap || b->jointForest == NULL )
 		{
@@ -662,7 +726,11 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 		b->jointForestJoints = jointTotal;
 		keptForest = true;
 	}
-	if ( keptForest )
+	if ( early )
+	{
+		/* the roots and body counts are the early pass's */
+	}
+	else if ( keptForest )
 	{
 		k_compInitFrom<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->jointForest, b->compData, n );
 		*launches += 1;
@@ -682,8 +750,11 @@ extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, cons
 			*launches += 1;
 		}
 	}
-	k_compRoots<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
-	*launches += 1;
+	if ( early == false )
+	{
+		k_compRoots<<<compBlocks( n ), B2G_COMP_THREADS, 0, stream>>>( b->parent, b->compData, n );
+		*launches += 1;
+	}
 	if ( cons > 0 )
 	{
 		k_compCountCons<<<compBlocks( cons ), B2G_COMP_THREADS, 0, stream>>>( *a, awakeIndex, b->compData, total, cons );

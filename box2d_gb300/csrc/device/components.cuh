@@ -79,6 +79,10 @@ struct b2gCompBuffers
 	int* jointForest;
 	int jointForestCap, jointForestN, jointForestJoints;
 	long long jointForestEpoch;
+	/* roots computed right after the narrowphase from the contacts it left touching, for
+	   the next analysis when the awake set and the joints are still those (earlyEpoch) */
+	int earlyValid, earlyN, earlyJoints;
+	long long earlyEpoch;
 };
 
 extern "C" int b2gDev_CompReserve( b2gCompBuffers* b, int awake, int slots, int joints );
@@ -92,6 +96,15 @@ extern "C" void b2gDev_CompFree( b2gCompBuffers* b );
 extern "C" int b2gDev_CompAnalyze( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets, const int* awakeIndex,
 								   int total, int jointTotal, int forceBig, long long jointEpoch, cudaStream_t stream,
 								   long long* launches );
+
+/* the union-find and roots of the next analysis, issued straight after the narrowphase:
+   the unions of every live, awake contact the narrowphase left touching (a superset of the
+   colored contacts the solver will see, unless the contact-state pass wakes bodies, which
+   changes jointEpoch) over the kept joint forest; the analysis then starts from these
+   roots when n, jointTotal and jointEpoch match */
+extern "C" int b2gDev_CompUnionEarly( b2gCompBuffers* b, const b2gContact* contacts, int capacity, const b2gJoint* joints,
+									  const int* awakeIndex, int n, int jointTotal, long long jointEpoch, cudaStream_t stream,
+									  long long* launches );
 
 /* solve every bin (small components) */
 extern "C" int b2gDev_CompSolveBins( b2gCompBuffers* b, const d_solveArgs* a, const int* jointOffsets,

@@ -2444,6 +2444,8 @@ static int cmpChange( const void* a, const void* b )
    first `window` state changes arrive with the world's next wait */
 extern "C" int b2gDev_CollideIssue( b2gDeviceWorld* dw, const b2gStepParams* p, int contactIdCapacity )
 {
+	/* roots from an earlier step's early pass never serve this step's analysis */
+	dw->comp.earlyValid = 0;
 	dev_event( dw, dw->ev[2] );
 	CK2( dev_memset( dw, dw->counters, 0, sizeof( b2gStepCounters ) ) );
 	if ( contactIdCapacity > 0 )
@@ -2683,6 +2685,25 @@ static int sideReady( b2gDeviceWorld* dw )
 	dw->hClusterStarted = hFlag;
 	dw->dClusterStarted = dFlag;
 	return 0;
+}
+
+/* The component analysis's union-find, issued right after the narrowphase's results came
+   back so that it runs while the host does the contact-state pass and its uploads; the
+   solve's analysis starts from its roots unless the awake set or the joints changed in
+   between (the state pass woke bodies). Large worlds solved by components only. */
+extern "C" int b2gDev_ComponentsEarly( b2gDeviceWorld* dw, int awakeCount )
+{
+	/* B2G_EARLY_UNION=0: the analysis runs whole at the solve */
+	static const int s_on = getenv( "B2G_EARLY_UNION" ) == NULL || atoi( getenv( "B2G_EARLY_UNION" ) ) != 0;
+	if ( s_on == 0 || dw->solverMode != B2G_SOLVER_COMPONENTS || dw->defer != NULL || dw->compSkip > 0 || awakeCount < 2048 ||
+		 awakeCount >= ( 1 << B2G_CURSOR_BODY_BITS ) )
+		return 0;
+	/* the pass rewrites the analysis buffers: the last analysis is not reused */
+	dw->compValid = 0;
+	int jointTotal = dw->jointOffsets[B2_GRAPH_COLOR_COUNT];
+	int capacity = dw->contactSlots < dw->contactCap ? dw->contactSlots : dw->contactCap;
+	return b2gDev_CompUnionEarly( &dw->comp, dw->contacts, capacity, dw->joints, dw->awakeIndex, awakeCount, jointTotal,
+								  dw->jointEpoch, dw->stream, &dw->launches );
 }
 
 extern "C" int b2gDev_SolveIssue( b2gDeviceWorld* dw, const b2gStepParams* p, const int* activeColors, int activeColorCount,

@@ -805,6 +805,13 @@ int h_stepCollide( h_world* w, int oneBlockOnly )
 	int changeCount = 0, recycled = 0;
 	int rc = b2gDev_CollideCollect( w->dev, &changes, &changeCount, &recycled );
 	if ( rc != 0 ) h_fail( w, "narrowphase", rc );
+	/* contacts began or ended touching: the solve's component analysis starts on the device
+	   now, beside the state pass */
+	if ( changeCount > 0 && w->stepTimeStep > 0.0f && b2gDev_IsRecording( w->dev ) == 0 )
+	{
+		rc = b2gDev_ComponentsEarly( w->dev, w->awakeBodyIds.count );
+		if ( rc != 0 ) h_fail( w, "component analysis", rc );
+	}
 	h_lap( w, H_PHASE_COLLIDE, &lap );
 	w->recycledContactCount = recycled;
 	h_contactStatePass( w, changes, changeCount );
