@@ -65,7 +65,7 @@ WORKLOADS = {
 # DRAM bytes (read + write) per step of the solver-stage kernels (component analysis, bins,
 # cluster assignment, cluster solve) in the timed window, from one ncu capture of each
 # workload's timed steps (profiles/solver_traffic_timed_steps.md: command and per-kernel split)
-SOLVER_TRAFFIC = {"many_pyramids": 43.21e6, "large_pyramid": 3.48e6, "joint_grid": 18.33e6}
+SOLVER_TRAFFIC = {"many_pyramids": 43.45e6, "large_pyramid": 3.48e6, "joint_grid": 18.56e6}
 
 
 def peaks() -> dict:
