@@ -189,7 +189,6 @@ static int h_shouldShapesCollide( b2Filter a, b2Filter b )
    reference's query order (kinematic, static, dynamic trees; DFS child2 first) after the
    self and moved-pair dedupe; the host applies the remaining filters and creates contacts
    newest-first per move, as the reference's prepended pair lists do. */
-/* issue the pair query of the moved proxies; returns whether one was issued */
 static void h_flushContacts( h_world* w );
 
 /* the moved proxies' fat boxes and shapes, in move order, into the world's buffers */
@@ -260,6 +259,8 @@ static int h_speculationHolds( h_world* w )
 	return memcmp( w->moveBoxes, w->specBoxes, (size_t)n * 4 * sizeof( float ) ) == 0;
 }
 
+/* issue the pair query of the moved proxies (or keep the one issued at the last step's
+   end); returns whether one is pending */
 static int h_pairsIssue( h_world* w )
 {
 	int moveCount = w->moveArray.count;
