@@ -187,8 +187,9 @@ static int h_shouldShapesCollide( b2Filter a, b2Filter b )
 
 /* broad_phase.c:412-529. The device returns, per move, every overlapping proxy in the
    reference's query order (kinematic, static, dynamic trees; DFS child2 first) after the
-   self and moved-pair dedupe; the host applies the remaining filters and creates contacts
-   newest-first per move, as the reference's prepended pair lists do. */
+   self and moved-pair dedupe, less the pairs that have a contact already; the host applies
+   the remaining filters and creates contacts newest-first per move, as the reference's
+   prepended pair lists do. */
 static void h_flushContacts( h_world* w );
 
 /* the moved proxies' fat boxes and shapes, in move order, into the world's buffers */
