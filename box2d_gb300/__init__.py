@@ -43,6 +43,7 @@ BODY_ACTIONS = {"force": 0, "force_center": 1, "torque": 2, "impulse": 3, "impul
 NO_CONTINUOUS = 1
 NO_WARM_STARTING = 2
 NO_RECYCLING = 4
+ROLLING_RESISTANCE = 8  # ramp world: rounded boxes with rolling resistance
 
 
 class WorldId(ctypes.Structure):

@@ -44,6 +44,7 @@ struct d_laneAdj
 	float base1, base2, nm1, nm2, tm1, tm2, rv1, rv2;
 	float n1, n2, t1, t2;
 	float friction;
+	float roll; /* rolling impulse */
 };
 
 /* adjoint handed from step n to step n - 1 for one contact id: manifold geometry (normal,
@@ -55,6 +56,7 @@ struct d_carry
 	float base[2];
 	float ni[2], ti[2];
 	float qA[2], qB[2];
+	float roll; /* the manifold's rolling impulse */
 };
 
 static __device__ __forceinline__ d_laneImp d_getImp( const b2gContactLane* c )
@@ -155,6 +157,8 @@ static __device__ void d_adjWarmStart( const b2gContactLane* c, const d_laneImp&
 	/* tangent = (n.y, -n.x) */
 	g->ny += gtx;
 	g->nx -= gty;
+	/* wA -= iA roll, wB += iB roll (contact_solver.c:1863-1864) */
+	g->roll += -c->invIA * gA->w + c->invIB * gB->w;
 }
 
 /* accumulators of one lane point's geometric adjoints */
@@ -344,7 +348,7 @@ struct d_bodyAdj
 
 /* d_solveLane reversed (contact_solver.c:1873-2116): A0/B0 and imp are the body states and
    impulses the lane saw; the forward is recomputed with the forward's own point functions
-   to recover the state between points. Rolling resistance is not differentiated. */
+   to recover the state between points. */
 static __device__ void d_adjSolveLane( const b2gContactLane* c, const d_laneImp& imp, const d_body& A0, const d_body& B0,
 									   const b2gStepParams& P, bool useBias, d_bodyAdj* gA, d_bodyAdj* gB, d_laneAdj* g )
 {
@@ -376,14 +380,51 @@ static __device__ void d_adjSolveLane( const b2gContactLane* c, const d_laneImp&
 	float gdpx = 0.0f, gdpy = 0.0f;
 	if ( useBias == false )
 	{
-		d_body A3 = A2, B3 = B2;
+		/* rolling resistance (contact_solver.c:2021-2031) between the normal points and the
+		   friction: symClamp(lambda + rollingMass (wA - wB), rollingResistance total) */
+		d_body AR = A2, BR = B2;
+		const bool rolling = ( c->groupFlags & 1 ) != 0;
+		float rx = 0.0f, rmax = 0.0f, rinner = 0.0f;
+		if ( rolling )
+		{
+			float deltaLambda = c->rollingMass * ( A2.w - B2.w );
+			rx = imp.roll + deltaLambda;
+			rmax = c->rollingResistance * total;
+			rinner = w_min( rx, rmax );
+			float newRoll = w_symClamp( rx, rmax );
+			deltaLambda = newRoll - imp.roll;
+			AR.w = A2.w - c->invIA * deltaLambda;
+			BR.w = B2.w + c->invIB * deltaLambda;
+		}
+		d_body A3 = AR, B3 = BR;
 		float t1 = imp.t1;
 		d_frictionPoint( c, &A3, &B3, c->anchorA1, c->anchorB1, c->tangentMass1, l1, &t1 );
-		/* friction point 2 saw (A3, B3), point 1 saw (A2, B2) */
+		/* friction point 2 saw (A3, B3), point 1 saw (AR, BR) */
 		d_adjFrictionPoint( c, A3, B3, c->anchorA2, c->anchorB2, c->tangentMass2, l2, imp.t2, &gA->v, &gB->v, &g->t2, &g->n2, &g2,
 							&g->nx, &g->ny, &g->tm2, &g->friction );
-		d_adjFrictionPoint( c, A2, B2, c->anchorA1, c->anchorB1, c->tangentMass1, l1, imp.t1, &gA->v, &gB->v, &g->t1, &g->n1, &g1,
+		d_adjFrictionPoint( c, AR, BR, c->anchorA1, c->anchorB1, c->tangentMass1, l1, imp.t1, &gA->v, &gB->v, &g->t1, &g->n1, &g1,
 							&g->nx, &g->ny, &g->tm1, &g->friction );
+		if ( rolling )
+		{
+			/* the branch the forward took: the bound -max, the bound max, or the sum */
+			float gDelta = -c->invIA * gA->v.w + c->invIB * gB->v.w;
+			float gNew = g->roll + gDelta;
+			float gLambda = -gDelta;
+			float gMax = 0.0f;
+			if ( -rmax > rinner ) gMax = -gNew;
+			else if ( rinner == rmax && !( rx < rmax ) ) gMax = gNew;
+			else
+			{
+				gLambda += gNew;
+				gA->v.w += c->rollingMass * gNew;
+				gB->v.w -= c->rollingMass * gNew;
+			}
+			g->roll = gLambda;
+			/* total = the two points' new normal impulses */
+			float gTotal = c->rollingResistance * gMax;
+			g->n1 += gTotal;
+			g->n2 += gTotal;
+		}
 	}
 	d_adjNormalPoint( c, A1, B1, dpx, dpy, c->anchorA2, c->anchorB2, c->baseSeparation2, c->normalMass2, imp.n2, biasRate, massScale,
 					  impulseScale, inv_h, contactSpeed, &gA->v, &gB->v, &g->n2, &g2, &g->nx, &g->ny, &g->base2, &g->nm2, &gdpx, &gdpy,
@@ -899,12 +940,16 @@ static __device__ void d_adjPrepareCollide( const d_tapeView& V, const d_tapeVie
 		out.qA[1] = cin.qA[1] + gcA[1];
 		out.qB[0] = cin.qB[0] + gcB[0];
 		out.qB[1] = cin.qB[1] + gcB[1];
+		/* a kept manifold keeps its rolling impulse */
+		out.roll = warmScale * g.roll;
 		s.carryNext[k] = out;
 		return;
 	}
-	/* computed this step (contact.c:519-698): the manifold is a function of both poses */
+	/* computed this step (contact.c:519-698): the manifold is a function of both poses, and
+	   takes the old manifold's rolling impulse when it has points (contact.c:609-612) */
 	if ( pc > 0 )
 	{
+		out.roll = warmScale * g.roll;
 		if ( shapeA->type != b2_polygonShape || shapeB->type != b2_polygonShape )
 		{
 			d_fail( s.status, B2_DIFF_UNSUPPORTED, step, 3, slot );
@@ -1107,7 +1152,6 @@ __global__ void __launch_bounds__( B2G_ADJ_THREADS ) k_adjointStep( const d_adjW
 	{
 		d_prepareContactLane( a, i, overflowBegin, s.lanes + i );
 		if ( s.lanes[i].groupFlags & 2 ) s_restitution = 1;
-		if ( s.lanes[i].groupFlags & 1 ) s_bad = B2_DIFF_UNSUPPORTED;
 	}
 	__syncthreads();
 	if ( s_bad != 0 )
@@ -1230,6 +1274,7 @@ __global__ void __launch_bounds__( B2G_ADJ_THREADS ) k_adjointStep( const d_adjW
 		s.gL[i].n2 = cin.ni[1];
 		s.gL[i].t1 = cin.ti[0];
 		s.gL[i].t2 = cin.ti[1];
+		s.gL[i].roll = cin.roll;
 	}
 	__syncthreads();
 

@@ -414,6 +414,13 @@ static void b2sRampWorld( b2sScene* s, int columns, int rows, b2sRng* rng )
 			b2ShapeDef sd = b2DefaultShapeDef();
 			sd.material.friction = b2sRandomFloatRange( rng, 0.3f, 0.8f );
 			b2Polygon box = b2MakeBox( h, h );
+			if ( s->flags & 8 )
+			{
+				/* rounded boxes with rolling resistance (contact.c:553-560 gives their contacts
+				   max(rolling resistance) times the larger radius) */
+				box = b2MakeRoundedBox( h - 0.05f, h - 0.05f, 0.05f );
+				sd.material.rollingResistance = 0.3f;
+			}
 			b2CreatePolygonShape( body, &sd, &box );
 		}
 	}

@@ -459,6 +459,8 @@ struct t_lane
 	V1 anchorA[2], anchorB[2];
 	T1 normalMass[2], tangentMass[2], baseSeparation[2], normalImpulse[2], tangentImpulse[2], totalNormalImpulse[2];
 	T1 relativeVelocity[2];
+	T1 rollingImpulse;
+	float rollingMass, rollingResistance;
 	int groupFlags;
 	int pointCount;
 };
@@ -469,6 +471,7 @@ struct t_manifold
 	V1 normal;
 	V1 anchorA[2], anchorB[2];
 	T1 baseSeparation[2], separation[2], normalImpulse[2], tangentImpulse[2];
+	T1 rollingImpulse;
 	R1 cachedA, cachedB;
 	uint16_t id[2];
 	int pointCount;
@@ -517,10 +520,13 @@ static void t_warmStart( t_lane& c, t_body* A, t_body* B )
 		B->vy = B->vy + c.invMassB * Py;
 		c.totalNormalImpulse[p] = c.totalNormalImpulse[p] + c.normalImpulse[p];
 	}
+	/* contact_solver.c:1863-1864 */
+	A->w = A->w - c.invIA * c.rollingImpulse;
+	B->w = B->w + c.invIB * c.rollingImpulse;
 }
 
 static void t_normalPoint( t_lane& c, int p, t_body* A, t_body* B, T1 dpx, T1 dpy, float biasRate, float massScale, float impulseScale,
-						   float inv_h, float contactSpeed )
+						   float inv_h, float contactSpeed, T1* total )
 {
 	V1 rA = c.anchorA[p], rB = c.anchorB[p];
 	T1 rsAx = A->dqc * rA.x - A->dqs * rA.y;
@@ -544,6 +550,7 @@ static void t_normalPoint( t_lane& c, int p, t_body* A, t_body* B, T1 dpx, T1 dp
 	T1 impulse = newImpulse - c.normalImpulse[p];
 	c.normalImpulse[p] = newImpulse;
 	c.totalNormalImpulse[p] = c.totalNormalImpulse[p] + impulse;
+	*total = *total + newImpulse;
 	t_apply( c, A, B, rA, rB, impulse * c.normal.x, impulse * c.normal.y );
 }
 
@@ -581,10 +588,23 @@ static void t_solve( t_lane& c, t_body* A, t_body* B, float inv_h, float contact
 		impulseScale = 0.0f;
 	}
 	T1 dpx = B->dpx - A->dpx, dpy = B->dpy - A->dpy;
-	t_normalPoint( c, 0, A, B, dpx, dpy, biasRate, massScale, impulseScale, inv_h, contactSpeedNeg );
-	t_normalPoint( c, 1, A, B, dpx, dpy, biasRate, massScale, impulseScale, inv_h, contactSpeedNeg );
+	T1 total = t_c( 0.0f );
+	t_normalPoint( c, 0, A, B, dpx, dpy, biasRate, massScale, impulseScale, inv_h, contactSpeedNeg, &total );
+	t_normalPoint( c, 1, A, B, dpx, dpy, biasRate, massScale, impulseScale, inv_h, contactSpeedNeg, &total );
 	if ( useBias == false )
 	{
+		/* rolling resistance (contact_solver.c:2021-2031) */
+		if ( c.groupFlags & 1 )
+		{
+			T1 deltaLambda = c.rollingMass * ( A->w - B->w );
+			T1 lambda = c.rollingImpulse;
+			T1 maxLambda = c.rollingResistance * total;
+			T1 nb = -maxLambda;
+			c.rollingImpulse = t_max( nb, t_min( lambda + deltaLambda, maxLambda ) );
+			deltaLambda = c.rollingImpulse - lambda;
+			A->w = A->w - c.invIA * deltaLambda;
+			B->w = B->w + c.invIB * deltaLambda;
+		}
 		t_frictionPoint( c, 0, A, B );
 		t_frictionPoint( c, 1, A, B );
 	}
@@ -700,6 +720,13 @@ static t_lane t_prepare( const b2gStepParams& P, const b2gContact* cs, const t_m
 	c.invMassB = mB;
 	c.invIA = iA;
 	c.invIB = iB;
+	{
+		/* contact_solver.c:1675-1678, :1708-1709 */
+		float k = iA + iB;
+		c.rollingMass = k > 0.0f ? 1.0f / k : 0.0f;
+		c.rollingResistance = cs->rollingResistance;
+		c.rollingImpulse = warmStartScale * m.rollingImpulse;
+	}
 	float biasRate = P.contactBiasRate, massScale = P.contactMassScale, impulseScale = P.contactImpulseScale;
 	if ( indexA == -1 || indexB == -1 )
 	{
@@ -926,7 +953,10 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 				}
 				m.cachedA = pose[bA].q;
 				m.cachedB = pose[bB].q;
+				/* the old manifold's rolling impulse (contact.c:609-612) */
+				m.rollingImpulse = old.valid ? old.rollingImpulse : t_c( 0.0f );
 			}
+			if ( t_same( m.rollingImpulse.v, rm.rollingImpulse ) == false ) return -2;
 			/* friction = sqrt(fA fB) (b2MixFriction) */
 			T1 fA = t_v( shapeA->friction, dirFriction[cs->shapeIdA] ), fB = t_v( shapeB->friction, dirFriction[cs->shapeIdB] );
 			T1 friction = t_sqrt( fA * fB );
@@ -934,7 +964,6 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 			man[s] = m;
 			lanes[s] = t_prepare( P, cs, m, friction, v0 );
 			lanes[s].groupFlags = t_groupFlags( h, contacts, s );
-			if ( lanes[s].groupFlags & 1 ) return -1;
 		}
 		/* ---- substeps (solver.c:1010-1198), colors in order ---- */
 		std::vector<t_body> sb( v0 );
@@ -1000,6 +1029,7 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 				m.normalImpulse[p] = lanes[s].normalImpulse[p];
 				m.tangentImpulse[p] = lanes[s].tangentImpulse[p];
 			}
+			m.rollingImpulse = lanes[s].rollingImpulse;
 			next[ids[s]] = m;
 		}
 		carry.swap( next );

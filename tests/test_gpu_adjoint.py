@@ -10,7 +10,8 @@ shape frictions is checked against
     enough for differences to resolve the derivative, <= 1e-3.
 
 The tangent-linear checker is independent of the product: its dual numbers and its
-polygon contact Jacobian are its own, restated from the reference.
+polygon contact Jacobian are its own, restated from the reference. Rounded boxes with
+rolling resistance check the rolling impulse's derivative the same way.
 """
 from __future__ import annotations
 
@@ -99,6 +100,26 @@ def test_adjoint_matches_tangent_linear(gpu_lib, tangent, steps):
     seeds = [901, 902, 903]
     batch, targets = _make(gpu_lib, seeds)
     rng = np.random.default_rng(steps)
+    with batch:
+        v0, f0 = batch.velocities(), batch.friction()
+        _run(batch, v0, f0, steps)
+        _, gc = _loss_and_grad_centers(batch, targets)
+        gv, _, gf = batch.backward(gc)
+        for trial in range(3):
+            du, df = _direction(batch, v0, f0, rng)
+            for w in range(len(seeds)):
+                adjoint = float((gv[w].astype(np.float64) * du[w]).sum() + (gf[w].astype(np.float64) * df[w]).sum())
+                tl = _tangent_derivative(tangent, batch, w, du, df, gc)
+                assert abs(adjoint - tl) <= 1e-3 * max(abs(tl), 1e-6), (steps, w, trial, adjoint, tl)
+
+
+@pytest.mark.parametrize("steps", [1, 10, 60])
+def test_adjoint_with_rolling_resistance_matches_tangent_linear(gpu_lib, tangent, steps):
+    """Rounded boxes with rolling resistance (contact_solver.c:2021-2031): the rolling
+    impulse's clamp, its warm start and its carry between steps are differentiated."""
+    seeds = [905, 906]
+    batch, targets = _make(gpu_lib, seeds, flags=B.ROLLING_RESISTANCE)
+    rng = np.random.default_rng(100 + steps)
     with batch:
         v0, f0 = batch.velocities(), batch.friction()
         _run(batch, v0, f0, steps)
