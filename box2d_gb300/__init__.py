@@ -44,6 +44,7 @@ NO_CONTINUOUS = 1
 NO_WARM_STARTING = 2
 NO_RECYCLING = 4
 ROLLING_RESISTANCE = 8  # ramp world: rounded boxes with rolling resistance
+BALLS = 16  # ramp world: every other body a ball
 
 
 class WorldId(ctypes.Structure):

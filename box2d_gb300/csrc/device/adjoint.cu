@@ -950,14 +950,20 @@ static __device__ void d_adjPrepareCollide( const d_tapeView& V, const d_tapeVie
 	if ( pc > 0 )
 	{
 		out.roll = warmScale * g.roll;
-		if ( shapeA->type != b2_polygonShape || shapeB->type != b2_polygonShape )
+		/* polygons and circles; a mixed pair has the polygon as shape A (contact.c's
+		   registered manifold functions) */
+		const int kindA = shapeA->type == b2_polygonShape ? 1 : ( shapeA->type == b2_circleShape ? 0 : -1 );
+		const int kindB = shapeB->type == b2_polygonShape ? 1 : ( shapeB->type == b2_circleShape ? 0 : -1 );
+		if ( kindA < 0 || kindB < 0 || ( kindA == 0 && kindB == 1 ) )
 		{
 			d_fail( s.status, B2_DIFF_UNSUPPORTED, step, 3, slot );
 			return;
 		}
 		b2dPoly<d_dual8> polyA, polyB;
-		d_dualPoly( shapeA, &polyA );
-		d_dualPoly( shapeB, &polyB );
+		if ( kindA == 1 ) d_dualPoly( shapeA, &polyA );
+		if ( kindB == 1 ) d_dualPoly( shapeB, &polyB );
+		const b2dVec2<d_dual8> centerA = b2dV( d_dual8::make( shapeA->v[0].x ), d_dual8::make( shapeA->v[0].y ) );
+		const b2dVec2<d_dual8> centerB = b2dV( d_dual8::make( shapeB->v[0].x ), d_dual8::make( shapeB->v[0].y ) );
 		b2dXf<d_dual8> xfA, xfB;
 		xfA.p = b2dV( d_seed( TA.xf.p.x, 0 ), d_seed( TA.xf.p.y, 1 ) );
 		xfA.q.c = d_seed( TA.xf.q.c, 2 );
@@ -965,8 +971,13 @@ static __device__ void d_adjPrepareCollide( const d_tapeView& V, const d_tapeVie
 		xfB.p = b2dV( d_seed( TB.xf.p.x, 4 ), d_seed( TB.xf.p.y, 5 ) );
 		xfB.q.c = d_seed( TB.xf.q.c, 6 );
 		xfB.q.s = d_seed( TB.xf.q.s, 7 );
-		b2dContactGeometry<d_dual8> cg = b2dContactManifold( &polyA, &polyB, xfA, xfB, TA.localCenter.x, TA.localCenter.y,
-															 TB.localCenter.x, TB.localCenter.y );
+		b2dContactGeometry<d_dual8> cg =
+			kindA == 1 && kindB == 1
+				? b2dContactManifold( &polyA, &polyB, xfA, xfB, TA.localCenter.x, TA.localCenter.y, TB.localCenter.x, TB.localCenter.y )
+			: kindA == 1 ? b2dContactPolygonCircle( &polyA, centerB, shapeB->radius, xfA, xfB, TA.localCenter.x, TA.localCenter.y,
+													  TB.localCenter.x, TB.localCenter.y )
+						 : b2dContactCircles( centerA, shapeA->radius, centerB, shapeB->radius, xfA, xfB, TA.localCenter.x,
+											  TA.localCenter.y, TB.localCenter.x, TB.localCenter.y );
 		/* the recomputed manifold must be the recorded one */
 		bool same = cg.count == pc && cg.normal.x.v == n.x && cg.normal.y.v == n.y;
 		for ( int p = 0; p < pc && same; ++p )

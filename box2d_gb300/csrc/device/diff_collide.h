@@ -1,6 +1,7 @@
 /*
  * Polygon-polygon manifold (manifold.c:511-1028 b2ClipPolygons / b2FindMaxSeparation /
- * b2CollidePolygons, distance.c:33-106 b2SegmentDistance) over a dual scalar, for the
+ * b2CollidePolygons, distance.c:33-106 b2SegmentDistance), and the circle-circle and
+ * polygon-circle manifolds (manifold.c:36-66, :127-230), over a dual scalar, for the
  * Jacobian of a contact's manifold with respect to the two body poses. The operation order
  * is the forward narrowphase's, so the primal reproduces its float result and the same
  * reference edge, incident edge, flip and clip branches are taken; the tangents are the
@@ -381,6 +382,116 @@ template <class S> B2D_HD b2dManifold<S> b2dCollidePolygons( const b2dPoly<S>* p
 	return m;
 }
 
+template <class S> B2D_HD b2dVec2<S> b2dMulSubF( b2dVec2<S> a, float s, b2dVec2<S> b )
+{
+	return b2dV( a.x - s * b.x, a.y - s * b.y );
+}
+
+/* math_functions.h b2Normalize and b2GetLengthAndNormalize */
+template <class S> B2D_HD b2dVec2<S> b2dNormalize( b2dVec2<S> a )
+{
+	S lengthSquared = a.x * a.x + a.y * a.y;
+	if ( lengthSquared.v > 1000.0f * FLT_MIN )
+	{
+		S s = 1.0f / b2dSqrt( lengthSquared );
+		return b2dV( s * a.x, s * a.y );
+	}
+	return b2dV( S::make( 0.0f ), S::make( 0.0f ) );
+}
+
+template <class S> B2D_HD b2dVec2<S> b2dGetLengthAndNormalize( S* length, b2dVec2<S> a )
+{
+	S lengthSquared = a.x * a.x + a.y * a.y;
+	if ( lengthSquared.v > 1000.0f * FLT_MIN )
+	{
+		*length = b2dSqrt( lengthSquared );
+		S s = 1.0f / *length;
+		return b2dV( s * a.x, s * a.y );
+	}
+	*length = S::make( 0.0f );
+	return b2dV( S::make( 0.0f ), S::make( 0.0f ) );
+}
+
+/* manifold.c:36-66 b2CollideCircles: circle A in its own frame, B placed by xf */
+template <class S>
+B2D_HD b2dManifold<S> b2dCollideCircles( b2dVec2<S> centerA, float radiusA, b2dVec2<S> centerB, float radiusB, b2dXf<S> xf )
+{
+	b2dManifold<S> m;
+	m.count = 0;
+	m.normal = b2dV( S::make( 0.0f ), S::make( 0.0f ) );
+	b2dVec2<S> pointA = centerA;
+	b2dVec2<S> pointB = b2dTransformPoint( xf, centerB );
+	S distance;
+	b2dVec2<S> normal = b2dGetLengthAndNormalize( &distance, b2dSub( pointB, pointA ) );
+	S separation = distance - radiusA - radiusB;
+	if ( separation.v > B2D_SPECULATIVE_DISTANCE ) return m;
+	b2dVec2<S> cA = b2dMulAddF( pointA, radiusA, normal );
+	b2dVec2<S> cB = b2dMulAddF( pointB, -radiusB, normal );
+	m.normal = normal;
+	m.points[0].point = b2dLerpF( cA, cB, 0.5f );
+	m.points[0].separation = separation;
+	m.points[0].id = 0;
+	m.count = 1;
+	return m;
+}
+
+/* manifold.c:127-230 b2CollidePolygonAndCircle: polygon A in its own frame, circle B placed
+   by xf */
+template <class S>
+B2D_HD b2dManifold<S> b2dCollidePolygonAndCircle( const b2dPoly<S>* polygonA, b2dVec2<S> centerB, float radiusB, b2dXf<S> xf )
+{
+	b2dManifold<S> m;
+	m.count = 0;
+	m.normal = b2dV( S::make( 0.0f ), S::make( 0.0f ) );
+	const float speculativeDistance = B2D_SPECULATIVE_DISTANCE;
+	b2dVec2<S> center = b2dTransformPoint( xf, centerB );
+	float radiusA = polygonA->radius;
+	float radius = radiusA + radiusB;
+	int normalIndex = 0;
+	S separation = S::make( -FLT_MAX );
+	for ( int i = 0; i < polygonA->count; ++i )
+	{
+		S s = b2dDot( polygonA->n[i], b2dSub( center, polygonA->v[i] ) );
+		if ( s.v > separation.v )
+		{
+			separation = s;
+			normalIndex = i;
+		}
+	}
+	if ( separation.v > radius + speculativeDistance ) return m;
+	int vertIndex1 = normalIndex;
+	int vertIndex2 = vertIndex1 + 1 < polygonA->count ? vertIndex1 + 1 : 0;
+	b2dVec2<S> v1 = polygonA->v[vertIndex1];
+	b2dVec2<S> v2 = polygonA->v[vertIndex2];
+	S u1 = b2dDot( b2dSub( center, v1 ), b2dSub( v2, v1 ) );
+	S u2 = b2dDot( b2dSub( center, v2 ), b2dSub( v1, v2 ) );
+	if ( ( u1.v < 0.0f && separation.v > FLT_EPSILON ) || ( u2.v < 0.0f && separation.v > FLT_EPSILON ) )
+	{
+		/* the circle center is closest to a vertex and safely outside the polygon */
+		b2dVec2<S> v = u1.v < 0.0f ? v1 : v2;
+		b2dVec2<S> normal = b2dNormalize( b2dSub( center, v ) );
+		S sep = b2dDot( b2dSub( center, v ), normal );
+		if ( sep.v > radius + speculativeDistance ) return m;
+		b2dVec2<S> cA = b2dMulAddF( v, radiusA, normal );
+		b2dVec2<S> cB = b2dMulSubF( center, radiusB, normal );
+		m.normal = normal;
+		m.points[0].point = b2dLerpF( cA, cB, 0.5f );
+		m.points[0].separation = b2dDot( b2dSub( cB, cA ), normal );
+		m.points[0].id = 0;
+		m.count = 1;
+		return m;
+	}
+	b2dVec2<S> normal = polygonA->n[normalIndex];
+	m.normal = normal;
+	b2dVec2<S> cA = b2dMulAdd( center, radiusA - b2dDot( b2dSub( center, v1 ), normal ), normal );
+	b2dVec2<S> cB = b2dMulSubF( center, radiusB, normal );
+	m.points[0].point = b2dLerpF( cA, cB, 0.5f );
+	m.points[0].separation = separation - radius;
+	m.points[0].id = 0;
+	m.count = 1;
+	return m;
+}
+
 /* a polygon shape's local geometry as dual constants */
 template <class S>
 B2D_HD void b2dMakePoly( b2dPoly<S>* p, const float* verts, const float* normals, int count, float radius )
@@ -405,12 +516,41 @@ template <class S> struct b2dContactGeometry
 	int count;
 };
 
+/* the world geometry of a manifold computed in frame A */
+template <class S>
+B2D_HD b2dContactGeometry<S> b2dContactFromLocal( const b2dManifold<S>& local, b2dXf<S> xfA, b2dXf<S> xfB, float lcAx, float lcAy,
+												   float lcBx, float lcBy );
+
 template <class S>
 B2D_HD b2dContactGeometry<S> b2dContactManifold( const b2dPoly<S>* polyA, const b2dPoly<S>* polyB, b2dXf<S> xfA, b2dXf<S> xfB,
 												  float lcAx, float lcAy, float lcBx, float lcBy )
 {
 	b2dXf<S> rel = b2dInvMulTransforms( xfA, xfB );
-	b2dManifold<S> local = b2dCollidePolygons( polyA, polyB, rel );
+	return b2dContactFromLocal( b2dCollidePolygons( polyA, polyB, rel ), xfA, xfB, lcAx, lcAy, lcBx, lcBy );
+}
+
+/* a polygon (A) and a circle (B, center in its body frame) */
+template <class S>
+B2D_HD b2dContactGeometry<S> b2dContactPolygonCircle( const b2dPoly<S>* polyA, b2dVec2<S> centerB, float radiusB, b2dXf<S> xfA,
+													   b2dXf<S> xfB, float lcAx, float lcAy, float lcBx, float lcBy )
+{
+	b2dXf<S> rel = b2dInvMulTransforms( xfA, xfB );
+	return b2dContactFromLocal( b2dCollidePolygonAndCircle( polyA, centerB, radiusB, rel ), xfA, xfB, lcAx, lcAy, lcBx, lcBy );
+}
+
+/* two circles */
+template <class S>
+B2D_HD b2dContactGeometry<S> b2dContactCircles( b2dVec2<S> centerA, float radiusA, b2dVec2<S> centerB, float radiusB, b2dXf<S> xfA,
+												 b2dXf<S> xfB, float lcAx, float lcAy, float lcBx, float lcBy )
+{
+	b2dXf<S> rel = b2dInvMulTransforms( xfA, xfB );
+	return b2dContactFromLocal( b2dCollideCircles( centerA, radiusA, centerB, radiusB, rel ), xfA, xfB, lcAx, lcAy, lcBx, lcBy );
+}
+
+template <class S>
+B2D_HD b2dContactGeometry<S> b2dContactFromLocal( const b2dManifold<S>& local, b2dXf<S> xfA, b2dXf<S> xfB, float lcAx, float lcAy,
+												   float lcBx, float lcBy )
+{
 	b2dContactGeometry<S> g;
 	g.count = local.count;
 	g.normal = b2dRotate( xfA.q, local.normal );

@@ -421,7 +421,16 @@ static void b2sRampWorld( b2sScene* s, int columns, int rows, b2sRng* rng )
 				box = b2MakeRoundedBox( h - 0.05f, h - 0.05f, 0.05f );
 				sd.material.rollingResistance = 0.3f;
 			}
-			b2CreatePolygonShape( body, &sd, &box );
+			if ( ( s->flags & 16 ) && ( c + r ) % 2 == 1 )
+			{
+				/* every other body a ball: polygon-circle and circle-circle contacts */
+				b2Circle ball = { { 0.0f, 0.0f }, h };
+				b2CreateCircleShape( body, &sd, &ball );
+			}
+			else
+			{
+				b2CreatePolygonShape( body, &sd, &box );
+			}
 		}
 	}
 	s->targetX = b2sRandomFloatRange( rng, -10.0f, 10.0f );

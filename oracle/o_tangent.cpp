@@ -411,15 +411,127 @@ static t_polygon t_polygonOf( const b2gShape* s )
 	return p;
 }
 
+/* math_functions.h b2Normalize / b2GetLengthAndNormalize */
+static V1 t_normalize( V1 a )
+{
+	T1 lengthSquared = a.x * a.x + a.y * a.y;
+	if ( lengthSquared.v > 1000.0f * FLT_MIN )
+	{
+		T1 s = 1.0f / t_sqrt( lengthSquared );
+		return t_v2( s * a.x, s * a.y );
+	}
+	return t_v2( t_c( 0.0f ), t_c( 0.0f ) );
+}
+
+static V1 t_lengthAndNormalize( T1* length, V1 a )
+{
+	T1 lengthSquared = a.x * a.x + a.y * a.y;
+	if ( lengthSquared.v > 1000.0f * FLT_MIN )
+	{
+		*length = t_sqrt( lengthSquared );
+		T1 s = 1.0f / *length;
+		return t_v2( s * a.x, s * a.y );
+	}
+	*length = t_c( 0.0f );
+	return t_v2( t_c( 0.0f ), t_c( 0.0f ) );
+}
+
+static t_local t_emptyLocal( void )
+{
+	t_local m;
+	memset( &m, 0, sizeof( m ) );
+	return m;
+}
+
+/* manifold.c:36-66 */
+static t_local t_collideCircles( V1 centerA, float radiusA, V1 centerB, float radiusB, const t_xf& xf )
+{
+	t_local m = t_emptyLocal();
+	V1 pointA = centerA;
+	V1 pointB = t_transformPoint( xf, centerB );
+	T1 distance;
+	V1 normal = t_lengthAndNormalize( &distance, t_sub( pointB, pointA ) );
+	T1 separation = distance - radiusA - radiusB;
+	if ( separation.v > T_SPECULATIVE_DISTANCE ) return m;
+	V1 cA = t_v2( pointA.x + radiusA * normal.x, pointA.y + radiusA * normal.y );
+	V1 cB = t_v2( pointB.x + ( -radiusB ) * normal.x, pointB.y + ( -radiusB ) * normal.y );
+	m.normal = normal;
+	m.point[0] = t_lerp( cA, cB, 0.5f );
+	m.separation[0] = separation;
+	m.id[0] = 0;
+	m.count = 1;
+	return m;
+}
+
+/* manifold.c:127-230 */
+static t_local t_collidePolygonAndCircle( const t_polygon& poly, V1 centerB, float radiusB, const t_xf& xf )
+{
+	t_local m = t_emptyLocal();
+	V1 center = t_transformPoint( xf, centerB );
+	float radiusA = poly.radius;
+	float radius = radiusA + radiusB;
+	int normalIndex = 0;
+	T1 separation = t_c( -FLT_MAX );
+	for ( int i = 0; i < poly.count; ++i )
+	{
+		T1 s = t_dot( poly.n[i], t_sub( center, poly.v[i] ) );
+		if ( s.v > separation.v )
+		{
+			separation = s;
+			normalIndex = i;
+		}
+	}
+	if ( separation.v > radius + T_SPECULATIVE_DISTANCE ) return m;
+	int i1 = normalIndex, i2 = i1 + 1 < poly.count ? i1 + 1 : 0;
+	V1 v1 = poly.v[i1], v2 = poly.v[i2];
+	T1 u1 = t_dot( t_sub( center, v1 ), t_sub( v2, v1 ) );
+	T1 u2 = t_dot( t_sub( center, v2 ), t_sub( v1, v2 ) );
+	for ( int k = 0; k < 2; ++k )
+	{
+		/* the circle center closest to vertex 1, then vertex 2, and safely outside */
+		T1 u = k == 0 ? u1 : u2;
+		if ( !( u.v < 0.0f && separation.v > FLT_EPSILON ) ) continue;
+		V1 v = k == 0 ? v1 : v2;
+		V1 normal = t_normalize( t_sub( center, v ) );
+		T1 sep = t_dot( t_sub( center, v ), normal );
+		if ( sep.v > radius + T_SPECULATIVE_DISTANCE ) return m;
+		V1 cA = t_v2( v.x + radiusA * normal.x, v.y + radiusA * normal.y );
+		V1 cB = t_v2( center.x - radiusB * normal.x, center.y - radiusB * normal.y );
+		m.normal = normal;
+		m.point[0] = t_lerp( cA, cB, 0.5f );
+		m.separation[0] = t_dot( t_sub( cB, cA ), normal );
+		m.id[0] = 0;
+		m.count = 1;
+		return m;
+	}
+	V1 normal = poly.n[normalIndex];
+	m.normal = normal;
+	T1 depth = radiusA - t_dot( t_sub( center, v1 ), normal );
+	V1 cA = t_v2( center.x + depth * normal.x, center.y + depth * normal.y );
+	V1 cB = t_v2( center.x - radiusB * normal.x, center.y - radiusB * normal.y );
+	m.point[0] = t_lerp( cA, cB, 0.5f );
+	m.separation[0] = separation - radius;
+	m.id[0] = 0;
+	m.count = 1;
+	return m;
+}
+
 /* contact.c:519-545 and :619-623: the manifold in frame A, then world anchors, then
-   anchors relative to the centers of mass (physics_world.c:568-569) */
+   anchors relative to the centers of mass (physics_world.c:568-569); polygons and circles,
+   a mixed pair with the polygon as shape A */
 static t_geometry t_polygonContact( const b2gShape* shapeA, const b2gShape* shapeB, const t_xf& xfA, const t_xf& xfB, b2Vec2 lcA,
 								   b2Vec2 lcB )
 {
 	t_xf rel;
 	rel.q = t_invMulRot( xfA.q, xfB.q );
 	rel.p = t_invRotate( xfA.q, t_v2( xfB.p.x - xfA.p.x, xfB.p.y - xfA.p.y ) );
-	t_local local = t_collidePolygons( t_polygonOf( shapeA ), t_polygonOf( shapeB ), rel );
+	t_local local;
+	if ( shapeA->type == b2_polygonShape && shapeB->type == b2_polygonShape )
+		local = t_collidePolygons( t_polygonOf( shapeA ), t_polygonOf( shapeB ), rel );
+	else if ( shapeA->type == b2_polygonShape )
+		local = t_collidePolygonAndCircle( t_polygonOf( shapeA ), t_vec( shapeB->v[0] ), shapeB->radius, rel );
+	else
+		local = t_collideCircles( t_vec( shapeA->v[0] ), shapeA->radius, t_vec( shapeB->v[0] ), shapeB->radius, rel );
 	t_geometry g;
 	memset( &g, 0, sizeof( g ) );
 	g.count = local.count;
@@ -915,7 +1027,9 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 			}
 			else if ( rm.pointCount > 0 )
 			{
-				if ( shapeA->type != b2_polygonShape || shapeB->type != b2_polygonShape ) return -1;
+				bool polyA = shapeA->type == b2_polygonShape, polyB = shapeB->type == b2_polygonShape;
+				bool circleA = shapeA->type == b2_circleShape, circleB = shapeB->type == b2_circleShape;
+				if ( !( ( polyA && ( polyB || circleB ) ) || ( circleA && circleB ) ) ) return -1;
 				t_xf xfA = t_transform( pose[bA], bodies[bA].localCenter, bodies[bA].xf );
 				t_xf xfB = t_transform( pose[bB], bodies[bB].localCenter, bodies[bB].xf );
 				t_geometry g = t_polygonContact( shapeA, shapeB, xfA, xfB, bodies[bA].localCenter, bodies[bB].localCenter );

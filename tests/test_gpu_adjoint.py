@@ -133,6 +133,28 @@ def test_adjoint_with_rolling_resistance_matches_tangent_linear(gpu_lib, tangent
                 assert abs(adjoint - tl) <= 1e-3 * max(abs(tl), 1e-6), (steps, w, trial, adjoint, tl)
 
 
+@pytest.mark.parametrize("flags", [B.BALLS, B.BALLS | B.ROLLING_RESISTANCE])
+@pytest.mark.parametrize("steps", [1, 10, 60])
+def test_adjoint_with_balls_matches_tangent_linear(gpu_lib, tangent, steps, flags):
+    """Boxes and balls on the ramp: polygon-circle (manifold.c:127-230) and circle-circle
+    (manifold.c:36-66) manifolds are differentiated, with rolling resistance on the balls
+    and rounded boxes in the second case."""
+    seeds = [907, 908]
+    batch, targets = _make(gpu_lib, seeds, flags=flags)
+    rng = np.random.default_rng(200 + steps + flags)
+    with batch:
+        v0, f0 = batch.velocities(), batch.friction()
+        _run(batch, v0, f0, steps)
+        _, gc = _loss_and_grad_centers(batch, targets)
+        gv, _, gf = batch.backward(gc)
+        for trial in range(3):
+            du, df = _direction(batch, v0, f0, rng)
+            for w in range(len(seeds)):
+                adjoint = float((gv[w].astype(np.float64) * du[w]).sum() + (gf[w].astype(np.float64) * df[w]).sum())
+                tl = _tangent_derivative(tangent, batch, w, du, df, gc)
+                assert abs(adjoint - tl) <= 1e-3 * max(abs(tl), 1e-6), (steps, flags, w, trial, adjoint, tl)
+
+
 @pytest.mark.parametrize("flags", [0, B.NO_RECYCLING, B.NO_WARM_STARTING])
 def test_adjoint_matches_tangent_linear_without_recycling_or_warm_start(gpu_lib, tangent, flags):
     batch, targets = _make(gpu_lib, [444], flags=flags)
