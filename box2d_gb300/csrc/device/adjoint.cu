@@ -1165,11 +1165,6 @@ __global__ void __launch_bounds__( B2G_ADJ_THREADS ) k_adjointStep( const d_adjW
 		if ( s.lanes[i].groupFlags & 2 ) s_restitution = 1;
 	}
 	__syncthreads();
-	if ( s_bad != 0 )
-	{
-		if ( tid == 0 ) d_fail( s.status, s_bad, step, 5, 0 );
-		return;
-	}
 
 	/* ---- forward replay with a checkpoint per substep ---- */
 	for ( int sub = 0; sub < S; ++sub )

@@ -10,12 +10,12 @@
  * swept in reverse; each substep is recomputed from a per-substep checkpoint to get the
  * inputs of every constraint solve, so memory stays bounded by one substep per world.
  *
- * Differentiated: contacts between polygons (boxes and convex polygons, including the
- * manifold's dependence on both poses and contact recycling), restitution, speed
- * clamping, gravity and damping. Not differentiated (b2Diff_Backward returns
- * B2_DIFF_UNSUPPORTED for a tape that contains them): joints, rolling resistance, shapes
- * other than polygons, constraints in the overflow color, and islands that fall asleep or
- * wake while recording.
+ * Differentiated: contacts between polygons (boxes and convex polygons, rounded or not),
+ * between a polygon and a circle and between circles (the manifold's dependence on both
+ * poses, and contact recycling), restitution, rolling resistance, speed clamping, gravity
+ * and damping. Not differentiated (b2Diff_Backward returns B2_DIFF_UNSUPPORTED for a tape
+ * that contains them): joints, capsules, segments and chains, constraints in the overflow
+ * color, and islands that fall asleep or wake while recording.
  */
 #ifndef BOX2D_GB300_DIFF_H
 #define BOX2D_GB300_DIFF_H
@@ -65,9 +65,8 @@ B2G_API int b2Diff_Backward( b2DiffTape* tape, const float* adjCenter, const flo
 B2G_API void b2Diff_Sizes( const b2DiffTape* tape, int* bodyCounts, int* shapeCounts );
 
 /* Where the last b2Diff_Backward failed: code, world, step, check (1 narrowphase replay,
-   2 step replay, 3 unsupported shape, 4 unsupported step, 5 rolling resistance, 6 an
-   island slept or woke while recording) and the contact slot or body id. All zero after a
-   success. */
+   2 step replay, 3 unsupported shape, 4 unsupported step, 6 an island slept or woke
+   while recording) and the contact slot or body id. All zero after a success. */
 B2G_API void b2Diff_LastFailure( const b2DiffTape* tape, int* out );
 
 /* Device time of the last b2Diff_Backward (ms) and the kernels it launched. */
