@@ -12,7 +12,8 @@
  *      integrate velocities backwards, colors in reverse order (contact_solver.c:1811-2228,
  *      solver.c:66-162);
  *   4. runs the adjoint of prepare (contact_solver.c:1573-1809) and of the narrowphase
- *      (contact.c:519-698 through a dual-number evaluation of b2CollidePolygons; for a
+ *      (contact.c:519-698 through a dual-number evaluation of b2CollidePolygons,
+ *      b2CollidePolygonAndCircle or b2CollideCircles; for a
  *      recycled manifold, the separation update of physics_world.c:508-560), and hands the
  *      manifold and warm-start adjoints of each contact to step n - 1 by contact id.
  * Branches (clamps, speculative or soft contact, friction cone, speed caps, clip and edge
