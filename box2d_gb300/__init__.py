@@ -45,6 +45,8 @@ NO_WARM_STARTING = 2
 NO_RECYCLING = 4
 ROLLING_RESISTANCE = 8  # ramp world: rounded boxes with rolling resistance
 BALLS = 16  # ramp world: every other body a ball
+CAPSULES = 32  # ramp world: two capsules at the ends of the bottom row
+SEGMENT_RAMP = 64  # ramp world: the ramp's top face is a segment shape
 
 
 class WorldId(ctypes.Structure):

@@ -731,6 +731,21 @@ static __device__ void d_dualPoly( const b2gShape* s, b2dPoly<d_dual8>* p )
 	}
 }
 
+/* a capsule (or a segment, radius 0) as the two-vertex polygon the narrowphase collides
+   it as (manifold.c:16-34 b2MakeCapsule, the same float operations) */
+static __device__ void d_dualCapsule( b2Vec2 p1, b2Vec2 p2, float radius, b2dPoly<d_dual8>* p )
+{
+	b2Vec2 axis = d_normalize( d_sub( p2, p1 ) );
+	b2Vec2 normal = d_rightPerp( axis );
+	b2Vec2 neg = d_neg( normal );
+	p->count = 2;
+	p->radius = radius;
+	p->v[0] = b2dV( d_dual8::make( p1.x ), d_dual8::make( p1.y ) );
+	p->v[1] = b2dV( d_dual8::make( p2.x ), d_dual8::make( p2.y ) );
+	p->n[0] = b2dV( d_dual8::make( normal.x ), d_dual8::make( normal.y ) );
+	p->n[1] = b2dV( d_dual8::make( neg.x ), d_dual8::make( neg.y ) );
+}
+
 static __device__ __forceinline__ d_dual8 d_seed( float v, int k )
 {
 	d_dual8 r = d_dual8::make( v );
@@ -951,18 +966,30 @@ static __device__ void d_adjPrepareCollide( const d_tapeView& V, const d_tapeVie
 	if ( pc > 0 )
 	{
 		out.roll = warmScale * g.roll;
-		/* polygons and circles; a mixed pair has the polygon as shape A (contact.c's
-		   registered manifold functions) */
-		const int kindA = shapeA->type == b2_polygonShape ? 1 : ( shapeA->type == b2_circleShape ? 0 : -1 );
-		const int kindB = shapeB->type == b2_polygonShape ? 1 : ( shapeB->type == b2_circleShape ? 0 : -1 );
+		/* the pairs contact.c registers with polygon manifolds (polygon-polygon,
+		   polygon-capsule, segment-polygon: a capsule or segment as a two-vertex polygon),
+		   polygon-circle and circle-circle; shape A is the registered first type */
+		const int tA = shapeA->type, tB = shapeB->type;
+		const bool polyPair = ( tA == b2_polygonShape && ( tB == b2_polygonShape || tB == b2_capsuleShape ) ) ||
+							  ( tA == b2_segmentShape && tB == b2_polygonShape );
+		const int kindA = polyPair ? 1 : ( tA == b2_polygonShape ? 1 : ( tA == b2_circleShape ? 0 : -1 ) );
+		const int kindB = polyPair ? 1 : ( tB == b2_circleShape ? 0 : -1 );
 		if ( kindA < 0 || kindB < 0 || ( kindA == 0 && kindB == 1 ) )
 		{
 			d_fail( s.status, B2_DIFF_UNSUPPORTED, step, 3, slot );
 			return;
 		}
 		b2dPoly<d_dual8> polyA, polyB;
-		if ( kindA == 1 ) d_dualPoly( shapeA, &polyA );
-		if ( kindB == 1 ) d_dualPoly( shapeB, &polyB );
+		if ( kindA == 1 )
+		{
+			if ( tA == b2_segmentShape ) d_dualCapsule( shapeA->v[0], shapeA->v[1], 0.0f, &polyA );
+			else d_dualPoly( shapeA, &polyA );
+		}
+		if ( kindB == 1 )
+		{
+			if ( tB == b2_capsuleShape ) d_dualCapsule( shapeB->v[0], shapeB->v[1], shapeB->radius, &polyB );
+			else d_dualPoly( shapeB, &polyB );
+		}
 		const b2dVec2<d_dual8> centerA = b2dV( d_dual8::make( shapeA->v[0].x ), d_dual8::make( shapeA->v[0].y ) );
 		const b2dVec2<d_dual8> centerB = b2dV( d_dual8::make( shapeB->v[0].x ), d_dual8::make( shapeB->v[0].y ) );
 		b2dXf<d_dual8> xfA, xfB;

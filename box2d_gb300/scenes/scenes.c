@@ -391,7 +391,16 @@ static void b2sRampWorld( b2sScene* s, int columns, int rows, b2sRng* rng )
 	b2sAddBody( s, ground, 0 );
 	b2ShapeDef gd = b2DefaultShapeDef();
 	b2Polygon ramp = b2MakeBox( 30.0f, 0.5f );
-	b2CreatePolygonShape( ground, &gd, &ramp );
+	if ( s->flags & 64 )
+	{
+		/* the ramp's top face as a segment: segment-polygon contacts */
+		b2Segment top = { { -30.0f, 0.5f }, { 30.0f, 0.5f } };
+		b2CreateSegmentShape( ground, &gd, &top );
+	}
+	else
+	{
+		b2CreatePolygonShape( ground, &gd, &ramp );
+	}
 	b2Rot q = b2MakeRot( -angle );
 	float h = 0.25f;
 	for ( int c = 0; c < columns; ++c )
@@ -426,6 +435,13 @@ static void b2sRampWorld( b2sScene* s, int columns, int rows, b2sRng* rng )
 				/* every other body a ball: polygon-circle and circle-circle contacts */
 				b2Circle ball = { { 0.0f, 0.0f }, h };
 				b2CreateCircleShape( body, &sd, &ball );
+			}
+			else if ( ( s->flags & 32 ) && ( c == 1 || c == columns - 2 ) && r == 0 )
+			{
+				/* two capsules at the far ends of the bottom row among the boxes:
+				   polygon-capsule contacts */
+				b2Capsule capsule = { { -0.5f * h, 0.0f }, { 0.5f * h, 0.0f }, 0.5f * h };
+				b2CreateCapsuleShape( body, &sd, &capsule );
 			}
 			else
 			{

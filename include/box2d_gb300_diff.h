@@ -11,11 +11,12 @@
  * inputs of every constraint solve, so memory stays bounded by one substep per world.
  *
  * Differentiated: contacts between polygons (boxes and convex polygons, rounded or not),
- * between a polygon and a circle and between circles (the manifold's dependence on both
- * poses, and contact recycling), restitution, rolling resistance, speed clamping, gravity
- * and damping. Not differentiated (b2Diff_Backward returns B2_DIFF_UNSUPPORTED for a tape
- * that contains them): joints, capsules, segments and chains, constraints in the overflow
- * color, and islands that fall asleep or wake while recording.
+ * polygon-capsule, segment-polygon, polygon-circle and circle-circle contacts (the
+ * manifold's dependence on both poses, and contact recycling), restitution, rolling
+ * resistance, speed clamping, gravity and damping. Not differentiated (b2Diff_Backward
+ * returns B2_DIFF_UNSUPPORTED for a tape that contains them): joints, capsule-capsule,
+ * capsule-circle, segment-circle and segment-capsule contacts, chains, constraints in the
+ * overflow color, and islands that fall asleep or wake while recording.
  */
 #ifndef BOX2D_GB300_DIFF_H
 #define BOX2D_GB300_DIFF_H

@@ -411,6 +411,32 @@ static t_polygon t_polygonOf( const b2gShape* s )
 	return p;
 }
 
+/* manifold.c:16-34 b2MakeCapsule: a capsule (or a segment, radius 0) as a two-vertex
+   polygon; shape-local constants, in float */
+static t_polygon t_capsulePolygon( b2Vec2 p1, b2Vec2 p2, float radius )
+{
+	t_polygon p;
+	memset( &p, 0, sizeof( p ) );
+	float dx = p2.x - p1.x, dy = p2.y - p1.y;
+	float lengthSquared = dx * dx + dy * dy;
+	float ax = 0.0f, ay = 0.0f;
+	if ( lengthSquared > 1000.0f * FLT_MIN )
+	{
+		float s = 1.0f / sqrtf( lengthSquared );
+		ax = s * dx;
+		ay = s * dy;
+	}
+	/* right perpendicular of the axis, then its negation */
+	b2Vec2 n0 = { ay, -ax }, n1 = { -ay, ax };
+	p.count = 2;
+	p.radius = radius;
+	p.v[0] = t_vec( p1 );
+	p.v[1] = t_vec( p2 );
+	p.n[0] = t_vec( n0 );
+	p.n[1] = t_vec( n1 );
+	return p;
+}
+
 /* math_functions.h b2Normalize / b2GetLengthAndNormalize */
 static V1 t_normalize( V1 a )
 {
@@ -528,6 +554,10 @@ static t_geometry t_polygonContact( const b2gShape* shapeA, const b2gShape* shap
 	t_local local;
 	if ( shapeA->type == b2_polygonShape && shapeB->type == b2_polygonShape )
 		local = t_collidePolygons( t_polygonOf( shapeA ), t_polygonOf( shapeB ), rel );
+	else if ( shapeA->type == b2_polygonShape && shapeB->type == b2_capsuleShape )
+		local = t_collidePolygons( t_polygonOf( shapeA ), t_capsulePolygon( shapeB->v[0], shapeB->v[1], shapeB->radius ), rel );
+	else if ( shapeA->type == b2_segmentShape )
+		local = t_collidePolygons( t_capsulePolygon( shapeA->v[0], shapeA->v[1], 0.0f ), t_polygonOf( shapeB ), rel );
 	else if ( shapeA->type == b2_polygonShape )
 		local = t_collidePolygonAndCircle( t_polygonOf( shapeA ), t_vec( shapeB->v[0] ), shapeB->radius, rel );
 	else
@@ -1029,7 +1059,8 @@ extern "C" __attribute__( ( visibility( "default" ) ) ) int b2t_tangent( const v
 			{
 				bool polyA = shapeA->type == b2_polygonShape, polyB = shapeB->type == b2_polygonShape;
 				bool circleA = shapeA->type == b2_circleShape, circleB = shapeB->type == b2_circleShape;
-				if ( !( ( polyA && ( polyB || circleB ) ) || ( circleA && circleB ) ) ) return -1;
+				bool capsuleB = shapeB->type == b2_capsuleShape, segmentA = shapeA->type == b2_segmentShape;
+				if ( !( ( polyA && ( polyB || circleB || capsuleB ) ) || ( segmentA && polyB ) || ( circleA && circleB ) ) ) return -1;
 				t_xf xfA = t_transform( pose[bA], bodies[bA].localCenter, bodies[bA].xf );
 				t_xf xfB = t_transform( pose[bB], bodies[bB].localCenter, bodies[bB].xf );
 				t_geometry g = t_polygonContact( shapeA, shapeB, xfA, xfB, bodies[bA].localCenter, bodies[bB].localCenter );

@@ -133,12 +133,13 @@ def test_adjoint_with_rolling_resistance_matches_tangent_linear(gpu_lib, tangent
                 assert abs(adjoint - tl) <= 1e-3 * max(abs(tl), 1e-6), (steps, w, trial, adjoint, tl)
 
 
-@pytest.mark.parametrize("flags", [B.BALLS, B.BALLS | B.ROLLING_RESISTANCE])
+@pytest.mark.parametrize("flags", [B.BALLS, B.BALLS | B.ROLLING_RESISTANCE, B.CAPSULES, B.SEGMENT_RAMP])
 @pytest.mark.parametrize("steps", [1, 10, 60])
 def test_adjoint_with_balls_matches_tangent_linear(gpu_lib, tangent, steps, flags):
-    """Boxes and balls on the ramp: polygon-circle (manifold.c:127-230) and circle-circle
-    (manifold.c:36-66) manifolds are differentiated, with rolling resistance on the balls
-    and rounded boxes in the second case."""
+    """Boxes with balls on the ramp: polygon-circle (manifold.c:127-230) and circle-circle
+    (manifold.c:36-66) manifolds, with rolling resistance on the balls and rounded boxes
+    in the second case; boxes with capsules (polygon-capsule, manifold.c:504-508), and boxes
+    on a segment ramp (segment-polygon, manifold.c:1036-1040)."""
     seeds = [907, 908]
     batch, targets = _make(gpu_lib, seeds, flags=flags)
     rng = np.random.default_rng(200 + steps + flags)
